@@ -1,0 +1,162 @@
+/*
+ * nmag_gpu.h -- C-ABI of libnmaggpu.so: a GB300 (sm_103a) implementation of
+ * nsim's LLG right-hand side and its time integration.
+ *
+ * The reference exposes this path to Python through the embedded "ocaml"
+ * module (src/nsimexec.ml:4467-4674).  Each entry point below names the
+ * reference call it replaces.  Conventions: every function returns an int
+ * status (0 = ok, < 0 = invalid argument, > 0 = numerical failure such as a
+ * solver iteration cap or non-finite values); nothing aborts or traps.  The
+ * handle owns all device memory; the caller owns host arrays, which are
+ * copied in and out.  Handles are not thread-safe; use one per thread.
+ *
+ * Units: simulation units throughout (m = 1e-9, s = 1e-12, A = 1e-3,
+ * kg = 1e-27; interface/nmag/main.py:188-196).  Vector fields are node-major,
+ * component-minor (dof = 3*node + c), which is the reference's DOF order for
+ * one material covering the mesh (src/fem.ml:2592-2720).
+ */
+#ifndef NMAG_GPU_H
+#define NMAG_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NMG_VERSION 10000
+
+typedef struct nmg_handle nmg_handle;
+
+/* Material constants in simulation units, as the reference's local equations
+ * and operator strings see them (interface/nmag/main.py:347-465,
+ * interface/nmag/nmag_lam.py:417-460). */
+typedef struct nmg_material {
+  double Ms;            /* su_Ms                                                  */
+  double exch_coeff;    /* su_exch_prefactor = 2A/(mu0 Ms)                        */
+  double C1, C2, C3;    /* LLG coefficients: C1 m x H + C2 m x (m x H) + C3 (1-m.m) m */
+  double K1;            /* uniaxial anisotropy constant (su); 0 = none            */
+  double axis[3];       /* unit easy axis                                         */
+  double anis_coeff;    /* 2 K1 / (mu0 Ms)                                        */
+  double E_coeff_half;  /* -0.5 Ms mu0 (exchange and demag energy densities)      */
+  double E_coeff_ext;   /* -1.0 Ms mu0 (Zeeman energy density)                    */
+} nmg_material;
+
+/* Solver and precision options (nmag.Simulation(...) kwargs, main.py:829-845,
+ * and the ksp_tolerances of nmag_lam.py:614-634). */
+typedef struct nmg_options {
+  int do_demag;                          /* 0: skip FEM/BEM demag                      */
+  double nbc_rtol, nbc_atol; int nbc_maxits;   /* Neumann Poisson solve              */
+  double dbc_rtol, dbc_atol; int dbc_maxits;   /* Dirichlet Poisson solve            */
+  int bem_precision;                     /* 0: FP64 matrix; 1: FP32 matrix, FP64 sums  */
+  int cg_precision;                      /* 0: FP64 CG; reserved                       */
+  int reserved[6];
+} nmg_options;
+
+/* Integrator statistics (CVODE counters; nsim.ml:354-387 timings). */
+typedef struct nmg_ts_stats {
+  int64_t nst, nfe, nni, nli, ncfn, netf, npe, nps, njv, nje;
+  double hcur, tcur;
+  int32_t qcur, last_cg_iters_nbc, last_cg_iters_dbc, pad;
+  double time_rhs_ms, time_jv_ms, time_psolve_ms;
+} nmg_ts_stats;
+
+/* Library version; replaces nothing (ocaml.version). */
+int nmg_version(void);
+
+/* Message of the last failing call on this handle (or the last create error
+ * when h == NULL). */
+const char *nmg_last_error(const nmg_handle *h);
+
+/* Build the mesh topology, the P1 CSR operators, the box volumes, the surface
+ * triangles, solid angles and the dense Lindholm BEM on the device.
+ * Replaces ocaml.raw_make_lam -> Nsim.make_linalg_machine (nsimexec.ml:3605,
+ * nsim.ml:2828-3150): operator vivification (fem.ml:4890-5366) and the BEM
+ * fill (bem3d.ml:938-1047, bem3d_stubs.c:413-610). */
+int nmg_create(const double *coords, int n_nodes, const int32_t *tets, int n_tets,
+               const nmg_material *mat, const nmg_options *opt, nmg_handle **out);
+
+/* Release every device resource of the handle. */
+int nmg_destroy(nmg_handle *h);
+
+/* Sizes: info[0..5] = N, T, nnz (scalar P1 pattern), Nb, number of surface
+ * triangles, number of outer faces. */
+int nmg_mesh_info(const nmg_handle *h, int64_t info[6]);
+
+/* Copy the scalar P1 CSR and its value arrays (K, G_x|G_y|G_z, D_x|D_y|D_z,
+ * box volumes) to the host.  Any pointer may be NULL. */
+int nmg_get_csr(const nmg_handle *h, int32_t *row_ptr, int32_t *col_idx, double *K, double *G3,
+                double *D3, double *vol);
+
+/* Reference-shaped CSR of one of the six operators of nmag_lam.py:569-606:
+ * which = 0 op_H_exch (3N x 3N), 1 op_div_m (N x 3N), 2 op_neg_laplace_phi
+ * (N x N), 3 op_grad_phi (3N x N), 4 op_laplace_DBC (N x N), 5 op_load_DBC
+ * (N x Nb); entries scaled by coeff.  Built on the device from the scalar
+ * pattern.  Call with NULL arrays to query rows/cols/nnz first. */
+int nmg_export_operator(const nmg_handle *h, int which, double coeff, int *rows, int *cols, int *nnz,
+                        int32_t *row_ptr, int32_t *col_idx, double *vals);
+
+/* Boundary data: node of each boundary short index (Nb), surface triangles
+ * (3 per triangle, short indices), outward unit normals (3 per triangle),
+ * interior solid angles (Nb).  Any pointer may be NULL. */
+int nmg_get_boundary(const nmg_handle *h, int32_t *node_of_b, int32_t *tri, double *tri_normal,
+                     double *solid_angle);
+
+/* Dense BEM matrix, row-major Nb x Nb (row = observer). */
+int nmg_get_bem(const nmg_handle *h, double *out);
+
+/* Magnetisation (3N); replaces ocaml.lam_set_field/lam_get_field on v_m
+ * (nsimexec.ml:4286).  set_m copies as given (normalise on the host, as
+ * Fields.set_subfield does with auto_normalise, main.py:635-705). */
+int nmg_set_m(nmg_handle *h, const double *m);
+int nmg_get_m(const nmg_handle *h, double *m);
+
+/* Applied field H_ext (3N, su); v_H_ext of nmag_lam.py:358. */
+int nmg_set_h_ext(nmg_handle *h, const double *h_ext);
+
+/* Replace the material constants (e.g. the damping between a relax stage
+ * and the dynamics); invalidates the integrator like the reference's
+ * reinitialise. */
+int nmg_set_material(nmg_handle *h, const nmg_material *mat);
+
+/* Evaluate the RHS at the current m (program update_dmdt, nmag_lam.py:784-
+ * 795) and copy fields out: fields = [H_exch | H_demag | H_anis | H_total |
+ * dmdt] (5 x 3N), scalars = [phi | rho] (2 x N).  Either may be NULL. */
+int nmg_eval_fields(nmg_handle *h, double *fields, double *scalars);
+
+/* Energy densities [E_exch | E_demag | E_ext | E_anis | E_total] (5 x N) at
+ * the current m (program update_E, nmag_lam.py:454-460,659-662). */
+int nmg_energy_density(nmg_handle *h, double *E5);
+
+/* Volume averages of m (3) and total energies (5) = sum_i E_i V_i
+ * (main.py:2313-2480, fem.ml:3246-3283). */
+int nmg_averages(nmg_handle *h, double avg_m[3], double energies[5]);
+
+/* Timestepper (re)initialisation at t0 from the current m; replaces
+ * ocaml.lam_ts_init -> timestepper_set_initial_from_phys (nsim.ml:2485-2535). */
+int nmg_ts_init(nmg_handle *h, double t0, double rtol, double atol, int max_order, int krylov_max);
+
+/* Advance to t_final (CV_NORMAL_TSTOP when exact_tstop, else CV_NORMAL with
+ * interpolated output), or stop after max_steps steps when max_steps >= 0
+ * (CV_ONE_STEP_TSTOP loop).  m is updated to the returned time.  Replaces
+ * ocaml.lam_ts_advance -> timestepper_advance -> My_CVode_Advance_Time
+ * (nsimexec.ml:4130, nsim.ml:3641, sundials_sp_stubs.c:1239-1310). */
+int nmg_ts_advance(nmg_handle *h, double t_final, int exact_tstop, int64_t max_steps, double *t_reached,
+                   nmg_ts_stats *stats);
+
+/* max_i |m_i - m_prev_i| over nodes (Euclidean norm of the 3-vector); the
+ * reference's mwe_norm_dist_fun (nsimexec.ml:2332-2368, fem.ml:4717-4793). */
+int nmg_max_dm(nmg_handle *h, const double *m_prev, double *out);
+
+/* Device-pointer entry points (pointers are CUDA device addresses, e.g. from
+ * torch tensors): one RHS evaluation dmdt = f(m) on the handle's stream and
+ * one fixed-step RK4 trajectory.  No host copies.  */
+int nmg_rhs_device(nmg_handle *h, const double *d_m, double *d_dmdt);
+int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps);
+
+/* Wall-clock split of the last nmg_ts_advance / RHS work, in ms (CUDA events). */
+int nmg_get_timings(const nmg_handle *h, double out[8]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

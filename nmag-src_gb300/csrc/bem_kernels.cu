@@ -1,0 +1,168 @@
+// bem_kernels.cu -- dense Lindholm double-layer BEM on the device.
+//
+// Replaces the reference's BEM fill: nas_partially_fill_bem_matrix_row_constrained
+// (src/bem3d.ml:938-1047) driving caml_bem3d_raw_lindholm_block_pbc
+// (src/bem3d_stubs.c:413-610) for every (surface triangle, observer row), then
+// adding Omega_i/(4 pi) - 1 on the diagonal (bem3d.ml:1040-1043).
+//
+// Layout: the matrix is stored column-major, bem[c*nb + k] = B[k][c] (k =
+// observer row, c = boundary column).  One thread owns one observer row and
+// walks the triangles in the reference's order, so every entry is accumulated
+// in exactly the reference's order with no atomics, and a warp's 32 rows are
+// adjacent in memory (coalesced read-modify-write).  Compiled with
+// --fmad=false to follow the written operation order.
+#include "nmg_internal.h"
+
+namespace nmg {
+namespace {
+
+constexpr double kPi = 3.141592653589793;
+
+// Per-triangle constants of the Lindholm formula (bem3d_stubs.c:466-525).
+__global__ void k_tri_setup(int ntri, const int32_t *__restrict__ tri, const double *__restrict__ tri_normal,
+                            const int32_t *__restrict__ node_of_b, const double *__restrict__ X,
+                            TriGeo *__restrict__ geo) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntri) return;
+  TriGeo g;
+  double s[3][3], xi[3][3];
+  g.ok = 0;
+  g.maxgeo = 0.0;
+  for (int k = 0; k < 3; ++k)
+    for (int d = 0; d < 3; ++d) {
+      g.p[k][d] = X[3 * (size_t)node_of_b[tri[3 * (size_t)t + k]] + d];
+      double ax = fabs(g.p[k][d]);
+      if (ax > g.maxgeo) g.maxgeo = ax;
+    }
+  for (int d = 0; d < 3; ++d) {
+    s[0][d] = g.p[2][d] - g.p[1][d]; s[1][d] = g.p[0][d] - g.p[2][d]; s[2][d] = g.p[1][d] - g.p[0][d];
+  }
+  bool ok = true;
+  for (int k = 0; k < 3; ++k) {
+    g.s_l[k] = sqrt(s[k][0] * s[k][0] + s[k][1] * s[k][1] + s[k][2] * s[k][2]);
+    if (g.s_l[k] == 0.0) { ok = false; g.s_l[k] = 1.0; }
+    double inv = 1.0 / g.s_l[k];
+    for (int d = 0; d < 3; ++d) xi[k][d] = s[k][d] * inv;
+  }
+  double z[3];
+  z[0] = s[1][1] * s[2][2] - s[1][2] * s[2][1];
+  z[1] = s[1][2] * s[2][0] - s[1][0] * s[2][2];
+  z[2] = s[1][0] * s[2][1] - s[1][1] * s[2][0];
+  double len = sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+  if (len == 0.0) { ok = false; len = 1.0; }
+  double area = 0.5 * len, inv = 1.0 / len;
+  for (int d = 0; d < 3; ++d) g.zeta_v[d] = z[d] * inv;
+  g.gam01 = xi[0][0] * xi[1][0] + xi[0][1] * xi[1][1] + xi[0][2] * xi[1][2];
+  g.gam12 = xi[1][0] * xi[2][0] + xi[1][1] * xi[2][1] + xi[1][2] * xi[2][2];
+  g.gam20 = xi[2][0] * xi[0][0] + xi[2][1] * xi[0][1] + xi[2][2] * xi[0][2];
+  for (int k = 0; k < 3; ++k) {
+    const double *zv = g.zeta_v;
+    g.eta[k][0] = zv[1] * xi[k][2] - zv[2] * xi[k][1];
+    g.eta[k][1] = zv[2] * xi[k][0] - zv[0] * xi[k][2];
+    g.eta[k][2] = zv[0] * xi[k][1] - zv[1] * xi[k][0];
+  }
+  double f = 1.0 * (1.0 / (8.0 * kPi * area));
+  const double *n = tri_normal + 3 * (size_t)t;
+  if (g.zeta_v[0] * n[0] + g.zeta_v[1] * n[1] + g.zeta_v[2] * n[2] < 0.0) f = -f;
+  g.factor = f;
+  g.ok = ok ? 1 : 0;
+  geo[t] = g;
+}
+
+// Running maximum of |observer coordinate| in row order: the reference's
+// geo_eps = 1e-13 * max over the triangle and the observers visited so far
+// within one block call (bem3d_stubs.c:531-533).
+__global__ void k_observer_prefix_max(int nb, const int32_t *__restrict__ node_of_b, const double *__restrict__ X,
+                                      double *__restrict__ out) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double run = 0.0;
+  for (int k = 0; k < nb; ++k) {
+    const double *o = X + 3 * (size_t)node_of_b[k];
+    for (int d = 0; d < 3; ++d) { double a = fabs(o[d]); if (a > run) run = a; }
+    out[k] = run;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_bem_fill(int nb, int ntri, const TriGeo *__restrict__ geo,
+                                                  const int32_t *__restrict__ tri,
+                                                  const int32_t *__restrict__ node_of_b,
+                                                  const double *__restrict__ X, const double *__restrict__ obs_max,
+                                                  const double *__restrict__ solid_angle, double *__restrict__ bem) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nb) return;
+  const double ox = X[3 * (size_t)node_of_b[k]], oy = X[3 * (size_t)node_of_b[k] + 1],
+               oz = X[3 * (size_t)node_of_b[k] + 2];
+  const double omax = obs_max[k];
+  for (int t = 0; t < ntri; ++t) {
+    const TriGeo &g = geo[t];
+    if (!g.ok) continue;
+    double r[3][3], rl[3];
+    for (int v = 0; v < 3; ++v) {
+      r[v][0] = g.p[v][0] - ox; r[v][1] = g.p[v][1] - oy; r[v][2] = g.p[v][2] - oz;
+      rl[v] = sqrt(r[v][0] * r[v][0] + r[v][1] * r[v][1] + r[v][2] * r[v][2]);
+    }
+    if (rl[0] <= 0.0 || rl[1] <= 0.0 || rl[2] <= 0.0) continue;
+    double vlog0 = log((rl[1] + rl[2] + g.s_l[0]) / (rl[1] + rl[2] - g.s_l[0]));
+    double vlog1 = log((rl[2] + rl[0] + g.s_l[1]) / (rl[2] + rl[0] - g.s_l[1]));
+    double vlog2 = log((rl[0] + rl[1] + g.s_l[2]) / (rl[0] + rl[1] - g.s_l[2]));
+    double sp01 = r[0][0] * r[1][0] + r[0][1] * r[1][1] + r[0][2] * r[1][2];
+    double sp12 = r[1][0] * r[2][0] + r[1][1] * r[2][1] + r[1][2] * r[2][2];
+    double sp20 = r[2][0] * r[0][0] + r[2][1] * r[0][1] + r[2][2] * r[0][2];
+    double num = rl[0] * rl[1] * rl[2] + rl[0] * sp12 + rl[1] * sp20 + rl[2] * sp01;
+    double den = sqrt(2.0 * (rl[1] * rl[2] + sp12) * (rl[2] * rl[0] + sp20) * (rl[0] * rl[1] + sp01));
+    if (den == 0.0) continue;
+    double angle = num / den;
+    angle = angle < -1.0 ? -1.0 : (angle > 1.0 ? 1.0 : angle);
+    angle = 2.0 * acos(angle);
+    double zeta = g.zeta_v[0] * r[0][0] + g.zeta_v[1] * r[0][1] + g.zeta_v[2] * r[0][2];
+    if (zeta < 0.0) angle = -angle;
+    double f = g.factor;
+    double geo_eps = (g.maxgeo > omax ? g.maxgeo : omax) * 1e-13;
+    if (fabs(zeta) < geo_eps) f = 0.0;
+    double gl0 = 1.0 * vlog0 + g.gam01 * vlog1 + g.gam20 * vlog2;
+    double gl1 = g.gam01 * vlog0 + 1.0 * vlog1 + g.gam12 * vlog2;
+    double gl2 = g.gam20 * vlog0 + g.gam12 * vlog1 + 1.0 * vlog2;
+    double e0 = g.eta[0][0] * r[1][0] + g.eta[0][1] * r[1][1] + g.eta[0][2] * r[1][2];
+    double e1 = g.eta[1][0] * r[2][0] + g.eta[1][1] * r[2][1] + g.eta[1][2] * r[2][2];
+    double e2 = g.eta[2][0] * r[0][0] + g.eta[2][1] * r[0][1] + g.eta[2][2] * r[0][2];
+    double lh0 = f * g.s_l[0] * (angle * e0 - zeta * gl0);
+    double lh1 = f * g.s_l[1] * (angle * e1 - zeta * gl1);
+    double lh2 = f * g.s_l[2] * (angle * e2 - zeta * gl2);
+    const int32_t *tv = tri + 3 * (size_t)t;
+    bem[(size_t)tv[0] * nb + k] += lh0;
+    bem[(size_t)tv[1] * nb + k] += lh1;
+    bem[(size_t)tv[2] * nb + k] += lh2;
+  }
+  bem[(size_t)k * nb + k] += solid_angle[k] / (4.0 * kPi) - 1.0;
+}
+
+__global__ void k_to_f32(size_t n, const double *__restrict__ a, float *__restrict__ b) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) b[i] = (float)a[i];
+}
+
+}  // namespace
+
+int fill_bem(nmg_handle *h, std::string &err) {
+  Mesh &M = h->mesh;
+  cudaStream_t s = h->stream;
+  if (M.nb == 0) return 0;
+  NMG_CUDA_TRY(M.trigeo.alloc(M.ntri), "alloc trigeo");
+  NMG_CUDA_TRY(M.obs_max.alloc(M.nb), "alloc obs_max");
+  NMG_CUDA_TRY(M.bem.alloc((size_t)M.nb * M.nb), "alloc BEM (nb^2 doubles)");
+  NMG_CUDA_TRY(cudaMemsetAsync(M.bem.p, 0, sizeof(double) * (size_t)M.nb * M.nb, s), "zero BEM");
+  k_tri_setup<<<(M.ntri + 127) / 128, 128, 0, s>>>(M.ntri, M.tri, M.tri_normal, M.node_of_b, M.coords, M.trigeo);
+  k_observer_prefix_max<<<1, 32, 0, s>>>(M.nb, M.node_of_b, M.coords, M.obs_max);
+  k_bem_fill<<<(M.nb + 127) / 128, 128, 0, s>>>(M.nb, M.ntri, M.trigeo, M.tri, M.node_of_b, M.coords, M.obs_max,
+                                                 M.solid_angle, M.bem);
+  NMG_CUDA_TRY(cudaGetLastError(), "bem fill launch");
+  if (h->opt.bem_precision == 1) {
+    NMG_CUDA_TRY(M.bem32.alloc((size_t)M.nb * M.nb), "alloc FP32 BEM");
+    k_to_f32<<<h->sm_count * 8, 256, 0, s>>>((size_t)M.nb * M.nb, M.bem, M.bem32);
+  }
+  NMG_CUDA_TRY(cudaStreamSynchronize(s), "bem fill");
+  return 0;
+}
+
+}  // namespace nmg

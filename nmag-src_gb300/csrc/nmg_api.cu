@@ -1,0 +1,279 @@
+// nmg_api.cu -- the extern "C" boundary of libnmaggpu.so (declared in
+// include/nmag_gpu.h).  Argument checking, handle lifetime, host<->device
+// copies and error reporting; the numerical work is in the *_kernels.cu files.
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "nmg_internal.h"
+
+namespace {
+thread_local std::string g_create_error;
+
+int fail(nmg_handle *h, int code, const std::string &msg) {
+  if (h) h->last_error = msg;
+  else g_create_error = msg;
+  return code;
+}
+
+bool finite_material(const nmg_material *m) {
+  const double v[] = {m->Ms, m->exch_coeff, m->C1, m->C2, m->C3, m->K1, m->axis[0], m->axis[1], m->axis[2],
+                      m->anis_coeff, m->E_coeff_half, m->E_coeff_ext};
+  for (double x : v)
+    if (!(x == x) || x > 1e300 || x < -1e300) return false;
+  return true;
+}
+}  // namespace
+
+extern "C" {
+
+int nmg_version(void) { return NMG_VERSION; }
+
+const char *nmg_last_error(const nmg_handle *h) { return h ? h->last_error.c_str() : g_create_error.c_str(); }
+
+int nmg_create(const double *coords, int n_nodes, const int32_t *tets, int n_tets, const nmg_material *mat,
+               const nmg_options *opt, nmg_handle **out) {
+  if (!out) return fail(nullptr, -1, "nmg_create: out is NULL");
+  *out = nullptr;
+  if (!coords || !tets || !mat) return fail(nullptr, -1, "nmg_create: NULL input array");
+  if (n_nodes < 4 || n_tets < 1) return fail(nullptr, -2, "nmg_create: need at least 4 nodes and 1 tetrahedron");
+  for (long long k = 0; k < 4LL * n_tets; ++k)
+    if (tets[k] < 0 || tets[k] >= n_nodes) return fail(nullptr, -3, "nmg_create: tetrahedron refers to a missing node");
+  for (long long k = 0; k < 3LL * n_nodes; ++k)
+    if (!(coords[k] == coords[k])) return fail(nullptr, -4, "nmg_create: non-finite coordinate");
+  if (!finite_material(mat)) return fail(nullptr, -5, "nmg_create: non-finite material constant");
+  if (mat->Ms == 0.0) return fail(nullptr, -5, "nmg_create: Ms must be non-zero");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(nullptr, 101, "nmg_create: no CUDA device");
+  nmg_handle *h = new nmg_handle();
+  h->mat = *mat;
+  if (opt) h->opt = *opt;
+  else {
+    h->opt.do_demag = 1;
+    h->opt.nbc_rtol = h->opt.dbc_rtol = 1e-5;
+    h->opt.nbc_atol = h->opt.dbc_atol = 1e-50;
+    h->opt.nbc_maxits = h->opt.dbc_maxits = 10000;
+  }
+  cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return fail(nullptr, 101, "nmg_create: stream creation failed");
+  }
+  h->mesh.N = n_nodes;
+  h->mesh.T = n_tets;
+  std::string err;
+  if (h->ws.err.alloc(1) != cudaSuccess) err = "alloc";
+  else cudaMemsetAsync(h->ws.err.p, 0, sizeof(int), h->stream);
+  int rc = err.empty() ? nmg::build_mesh(h, coords, tets, err) : 100;
+  if (!rc) rc = nmg::init_workspace(h, err);
+  if (!rc && h->opt.do_demag) rc = nmg::fill_bem(h, err);
+  if (rc) {
+    g_create_error = "nmg_create: " + err;
+    nmg_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return 0;
+}
+
+int nmg_destroy(nmg_handle *h) {
+  if (!h) return -1;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  nmg::ts_destroy(h->ts);
+  h->ts = nullptr;
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;  // member destructors release the device buffers
+  return 0;
+}
+
+int nmg_mesh_info(const nmg_handle *h, int64_t info[6]) {
+  if (!h || !info) return -1;
+  info[0] = h->mesh.N; info[1] = h->mesh.T; info[2] = h->mesh.nnz;
+  info[3] = h->mesh.nb; info[4] = h->mesh.ntri; info[5] = h->mesh.nouter;
+  return 0;
+}
+
+static int d2h(const nmg_handle *h, void *dst, const void *src, size_t bytes) {
+  if (!dst || !bytes) return 0;
+  if (cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) return 100;
+  return cudaStreamSynchronize(h->stream) == cudaSuccess ? 0 : 100;
+}
+
+int nmg_get_csr(const nmg_handle *h, int32_t *row_ptr, int32_t *col_idx, double *K, double *G3, double *D3,
+                double *vol) {
+  if (!h) return -1;
+  const nmg::Mesh &M = h->mesh;
+  int rc = d2h(h, row_ptr, M.row_ptr.p, sizeof(int32_t) * (M.N + 1));
+  rc |= d2h(h, col_idx, M.col_idx.p, sizeof(int32_t) * M.nnz);
+  rc |= d2h(h, K, M.K.p, sizeof(double) * M.nnz);
+  rc |= d2h(h, G3, M.G.p, sizeof(double) * 3 * (size_t)M.nnz);
+  rc |= d2h(h, D3, M.D.p, sizeof(double) * 3 * (size_t)M.nnz);
+  rc |= d2h(h, vol, M.vol.p, sizeof(double) * M.N);
+  return rc;
+}
+
+int nmg_export_operator(const nmg_handle *h, int which, double coeff, int *rows, int *cols, int *nnz,
+                        int32_t *row_ptr, int32_t *col_idx, double *vals) {
+  if (!h || !rows || !cols || !nnz) return -1;
+  if (which < 0 || which > 5) return -2;
+  return nmg::export_operator(h, which, coeff, rows, cols, nnz, row_ptr, col_idx, vals);
+}
+
+int nmg_get_boundary(const nmg_handle *h, int32_t *node_of_b, int32_t *tri, double *tri_normal, double *solid_angle) {
+  if (!h) return -1;
+  const nmg::Mesh &M = h->mesh;
+  int rc = d2h(h, node_of_b, M.node_of_b.p, sizeof(int32_t) * M.nb);
+  rc |= d2h(h, tri, M.tri.p, sizeof(int32_t) * 3 * (size_t)M.ntri);
+  rc |= d2h(h, tri_normal, M.tri_normal.p, sizeof(double) * 3 * (size_t)M.ntri);
+  rc |= d2h(h, solid_angle, M.solid_angle.p, sizeof(double) * M.nb);
+  return rc;
+}
+
+int nmg_get_bem(const nmg_handle *h, double *out) {
+  if (!h || !out) return -1;
+  const nmg::Mesh &M = h->mesh;
+  if (!M.bem.p) return fail(const_cast<nmg_handle *>(h), 2, "no BEM matrix (demag disabled)");
+  // stored column-major; transpose on the host into row-major
+  const size_t nb = M.nb;
+  double *tmp = nullptr;
+  if (cudaMallocHost(&tmp, sizeof(double) * nb * nb) != cudaSuccess) return 100;
+  int rc = d2h(h, tmp, M.bem.p, sizeof(double) * nb * nb);
+  for (size_t c = 0; c < nb && !rc; ++c)
+    for (size_t k = 0; k < nb; ++k) out[k * nb + c] = tmp[c * nb + k];
+  cudaFreeHost(tmp);
+  return rc;
+}
+
+int nmg_set_m(nmg_handle *h, const double *m) {
+  if (!h || !m) return -1;
+  for (long long k = 0; k < 3LL * h->mesh.N; ++k)
+    if (!(m[k] == m[k])) return fail(h, -4, "nmg_set_m: non-finite magnetisation");
+  if (cudaMemcpyAsync(h->ws.m.p, m, sizeof(double) * 3 * h->mesh.N, cudaMemcpyHostToDevice, h->stream))
+    return fail(h, 100, "nmg_set_m: copy failed");
+  h->ts_ready = 0;
+  return cudaStreamSynchronize(h->stream) == cudaSuccess ? 0 : fail(h, 100, "nmg_set_m: sync failed");
+}
+
+int nmg_get_m(const nmg_handle *h, double *m) {
+  if (!h || !m) return -1;
+  return d2h(h, m, h->ws.m.p, sizeof(double) * 3 * h->mesh.N);
+}
+
+int nmg_set_h_ext(nmg_handle *h, const double *hx) {
+  if (!h || !hx) return -1;
+  for (long long k = 0; k < 3LL * h->mesh.N; ++k)
+    if (!(hx[k] == hx[k])) return fail(h, -4, "nmg_set_h_ext: non-finite field");
+  if (cudaMemcpyAsync(h->ws.h_ext.p, hx, sizeof(double) * 3 * h->mesh.N, cudaMemcpyHostToDevice, h->stream))
+    return fail(h, 100, "nmg_set_h_ext: copy failed");
+  h->ts_ready = 0;
+  return cudaStreamSynchronize(h->stream) == cudaSuccess ? 0 : fail(h, 100, "nmg_set_h_ext: sync failed");
+}
+
+int nmg_set_material(nmg_handle *h, const nmg_material *mat) {
+  if (!h || !mat) return -1;
+  if (!finite_material(mat) || mat->Ms == 0.0) return fail(h, -5, "nmg_set_material: invalid constants");
+  h->mat = *mat;
+  h->ts_ready = 0;
+  return 0;
+}
+
+int nmg_eval_fields(nmg_handle *h, double *fields, double *scalars) {
+  if (!h) return -1;
+  int rc = nmg::rhs_eval(h, h->ws.m, h->ws.dmdt);
+  if (rc) return fail(h, rc, "nmg_eval_fields: launch failed");
+  rc = nmg::check_device_error(h, "nmg_eval_fields");
+  if (rc) return rc;
+  const size_t n3 = 3 * (size_t)h->mesh.N, N = h->mesh.N;
+  if (fields) {
+    const double *src[5] = {h->ws.h_exch, h->ws.h_demag, h->ws.h_anis, h->ws.h_total, h->ws.dmdt};
+    for (int k = 0; k < 5; ++k)
+      if (d2h(h, fields + k * n3, src[k], sizeof(double) * n3)) return fail(h, 100, "copy failed");
+  }
+  if (scalars) {
+    if (d2h(h, scalars, h->ws.phi.p, sizeof(double) * N) || d2h(h, scalars + N, h->ws.rho.p, sizeof(double) * N))
+      return fail(h, 100, "copy failed");
+  }
+  int it[2] = {0, 0};
+  d2h(h, it, h->ws.iters.p, sizeof(it));
+  h->last_iters_nbc = it[0];
+  h->last_iters_dbc = it[1];
+  return 0;
+}
+
+int nmg_energy_density(nmg_handle *h, double *E5) {
+  if (!h || !E5) return -1;
+  if (nmg::energy_density(h, h->ws.m, h->ws.E5)) return fail(h, 100, "energy launch failed");
+  return d2h(h, E5, h->ws.E5.p, sizeof(double) * 5 * h->mesh.N);
+}
+
+int nmg_averages(nmg_handle *h, double avg_m[3], double energies[5]) {
+  if (!h || !avg_m) return -1;
+  return nmg::averages(h, h->ws.m, avg_m, energies);
+}
+
+int nmg_ts_init(nmg_handle *h, double t0, double rtol, double atol, int max_order, int krylov_max) {
+  if (!h) return -1;
+  if (!(rtol > 0.0) || !(atol > 0.0)) return fail(h, -2, "nmg_ts_init: tolerances must be positive");
+  if (max_order < 1 || max_order > 5) return fail(h, -2, "nmg_ts_init: max_order must be 1..5");
+  if (krylov_max < 1) return fail(h, -2, "nmg_ts_init: krylov_max must be >= 1");
+  if (!h->ts || !nmg::ts_matches(h->ts, max_order, krylov_max)) {
+    nmg::ts_destroy(h->ts);
+    h->ts = nmg::ts_create(h, max_order, krylov_max, rtol, atol);
+    if (!h->ts) return fail(h, 100, "nmg_ts_init: out of device memory for the integrator");
+  }
+  nmg::ts_set_tolerances(h->ts, rtol, atol);
+  int rc = nmg::ts_init(h, t0);
+  if (rc) return rc;
+  return 0;
+}
+
+int nmg_ts_advance(nmg_handle *h, double t_final, int exact_tstop, int64_t max_steps, double *t_reached,
+                   nmg_ts_stats *stats) {
+  if (!h || !t_reached) return -1;
+  if (!h->ts || !h->ts_ready) return fail(h, -3, "nmg_ts_advance: timestepper not initialised");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, h->stream);
+  int rc = nmg::ts_advance(h, t_final, exact_tstop, max_steps, t_reached, stats);
+  cudaEventRecord(e1, h->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  h->timings[0] = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) {
+    if (h->last_error.empty()) h->last_error = "nmg_ts_advance failed";
+    h->ts_ready = 0;
+  }
+  return rc;
+}
+
+int nmg_max_dm(nmg_handle *h, const double *m_prev, double *out) {
+  if (!h || !m_prev || !out) return -1;
+  nmg::DevBuf<double> tmp;
+  if (tmp.alloc(3 * (size_t)h->mesh.N)) return 100;
+  cudaMemcpyAsync(tmp.p, m_prev, sizeof(double) * 3 * h->mesh.N, cudaMemcpyHostToDevice, h->stream);
+  return nmg::max_dm(h, h->ws.m, tmp, out);
+}
+
+int nmg_rhs_device(nmg_handle *h, const double *d_m, double *d_dmdt) {
+  if (!h || !d_m || !d_dmdt) return -1;
+  int rc = nmg::rhs_eval(h, d_m, d_dmdt);
+  if (rc) return fail(h, rc, "nmg_rhs_device: launch failed");
+  return nmg::check_device_error(h, "nmg_rhs_device");
+}
+
+int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps) {
+  if (!h || !d_m || nsteps < 0) return -1;
+  return nmg::rk4_device(h, d_m, dt, nsteps);
+}
+
+int nmg_get_timings(const nmg_handle *h, double out[8]) {
+  if (!h || !out) return -1;
+  for (int k = 0; k < 8; ++k) out[k] = h->timings[k];
+  return 0;
+}
+
+}  // extern "C"

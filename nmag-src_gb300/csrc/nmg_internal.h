@@ -1,0 +1,130 @@
+// nmg_internal.h -- internal types of libnmaggpu.so (device buffers, launch
+// helpers and the kernels' host-side launchers).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/nmag_gpu.h"
+
+namespace nmg {
+
+// Error flag bits written by device code (never trap): the host turns them
+// into a status code and a message.
+enum DeviceError : int {
+  ERR_NONE = 0,
+  ERR_DEGREE = 1,       // a node belongs to more tets than the fixed-size row buffer allows
+  ERR_BARRIER = 2,      // a grid barrier gave up waiting (bounded spin)
+  ERR_NONFINITE = 4,    // a solver produced NaN/Inf
+  ERR_CG_MAXITS = 8,    // CG hit its iteration cap
+};
+
+constexpr int kMaxRowLen = 64;     // max distinct neighbours (incl. self) per node
+constexpr int kMaxNodeTets = 128;  // max tets around one node
+
+template <class T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  cudaError_t alloc(size_t count) {
+    release();
+    n = count;
+    if (!count) return cudaSuccess;
+    return cudaMalloc(&p, sizeof(T) * count);
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  ~DevBuf() { release(); }
+  operator T *() const { return p; }
+};
+
+// Triangle geometry for the Lindholm evaluation (bem3d_stubs.c:466-525).
+struct TriGeo {
+  double p[3][3], s_l[3], eta[3][3], zeta_v[3], gam01, gam12, gam20, factor, maxgeo;
+  int ok, pad;
+};
+
+struct Mesh {
+  int N = 0, T = 0, nnz = 0, nb = 0, ntri = 0, nouter = 0;
+  DevBuf<double> coords, dL, adet, K, G, D, vol, tri_normal, solid_angle;
+  DevBuf<int32_t> tets, nt_ptr, nt_idx, nbr, row_ptr, col_idx, diag_pos, b_of_node, node_of_b, tri;
+  DevBuf<double> bem;      // FP64 BEM, column-major (bem[c*nb + k] = B[k][c])
+  DevBuf<float> bem32;     // FP32 copy (precision form)
+  DevBuf<TriGeo> trigeo;
+  DevBuf<double> obs_max;
+};
+
+struct Workspace {
+  DevBuf<double> m, h_ext, h_exch, h_demag, h_anis, h_total, dmdt, rho, phi1, phi2, phi, rhs2;
+  DevBuf<double> b1, b2, bpart, cg_r, cg_z, cg_p, cg_q, dinv_n, dinv_d, red, E5;
+  DevBuf<unsigned> bar;     // grid barrier {count, generation}
+  DevBuf<int> err;          // device error flags
+  DevBuf<int> iters;        // CG iterations written by the persistent kernel
+  int cg_blocks = 0;
+  int gemv_slabs = 1;
+};
+
+struct Integrator;
+
+}  // namespace nmg
+
+struct nmg_handle {
+  nmg::Mesh mesh;
+  nmg::Workspace ws;
+  nmg_material mat{};
+  nmg_options opt{};
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  std::string last_error;
+  nmg::Integrator *ts = nullptr;
+  int ts_ready = 0;             // integrator initialised for the current m / H_ext / material
+  double *h_pinned = nullptr;   // small pinned staging buffer for scalars
+  int last_iters_nbc = 0, last_iters_dbc = 0;
+  int64_t n_rhs = 0;
+  double timings[8] = {0};
+};
+
+namespace nmg {
+// ---- launchers (mesh_kernels.cu) ----
+int build_mesh(nmg_handle *h, const double *coords, const int32_t *tets, std::string &err);
+int export_operator(const nmg_handle *h, int which, double coeff, int *rows, int *cols, int *nnz,
+                    int32_t *rp, int32_t *ci, double *vals);
+// ---- bem_kernels.cu ----
+int fill_bem(nmg_handle *h, std::string &err);
+void bem_gemv(nmg_handle *h, const double *x, double *y);
+// ---- rhs_kernels.cu ----
+int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt);  // full RHS on device vectors
+int energy_density(nmg_handle *h, const double *d_m, double *d_E5);
+int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5]);
+int max_dm(nmg_handle *h, const double *d_m, const double *d_mprev, double *out);
+int init_workspace(nmg_handle *h, std::string &err);
+int check_device_error(nmg_handle *h, const char *where);
+// ---- ts (nmg_ts.cu) ----
+Integrator *ts_create(nmg_handle *h, int qmax, int maxl, double rtol, double atol);
+void ts_destroy(Integrator *t);
+bool ts_matches(const Integrator *t, int qmax, int maxl);
+void ts_set_tolerances(Integrator *t, double rtol, double atol);
+int ts_init(nmg_handle *h, double t0);
+int ts_advance(nmg_handle *h, double tout, int exact_tstop, int64_t max_steps, double *t_reached,
+               nmg_ts_stats *st);
+int rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps);
+// ---- shared device helpers (vec_kernels.cu) ----
+void launch_axpby(cudaStream_t s, int n, double a, const double *x, double b, const double *y, double *z);
+double reduce_dot(nmg_handle *h, int n, const double *x, const double *y);
+}  // namespace nmg
+
+#define NMG_CUDA_TRY(expr, msg)                                                    \
+  do {                                                                             \
+    cudaError_t e__ = (expr);                                                      \
+    if (e__ != cudaSuccess) {                                                      \
+      err = std::string(msg) + ": " + cudaGetErrorString(e__);                     \
+      return 100;                                                                  \
+    }                                                                              \
+  } while (0)

@@ -1,0 +1,605 @@
+// rhs_kernels.cu -- the LLG right-hand side on the device.
+//
+// Replaces the reference's RHS program update_dmdt (interface/nmag/nmag_lam.py
+// :784-795): set_H_demag (:740-760; PETSc MatMult + two KSPSolves + dense BEM
+// MatMult), set_H_exch (:734-739), the site-wise anisotropy, H_total and LLG
+// local equations (:417-430,503,635-650; generated C run by fem_stubs.c:42-144).
+//
+// Kernels:
+//   k_div          rho = -Ms * sum_k D(i,k) . m_k                 (op_div_m + SCALE -1)
+//   k_cg           persistent cooperative Jacobi-PCG, bounded grid barriers
+//   k_gather_b     phi1b = phi1[node_of_b]                          (PULL-FEM)
+//   k_gemv_*       phi2b = BEM phi1b, column-major slabs + ordered slab sum
+//   k_dbc_rhs      rhs = -K_IB phi2b (interior), phi2b (boundary)  (op_load_DBC)
+//   k_heff_llg     H_exch (K SpMV), H_demag (G SpMV on phi1+phi2), H_anis,
+//                  H_total and dm/dt fused in one node kernel (CFBOX = / V_i)
+#include <cooperative_groups.h>
+
+#include "nmg_internal.h"
+
+namespace nmg {
+namespace {
+
+constexpr unsigned long long kBarrierSpinLimit = 1ull << 24;  // ~1-2 s with nanosleep
+constexpr int kCGThreads = 256;
+
+inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of NV values in a fixed order; result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double *smem) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = 0; j < NV; ++j) {
+    double s = warp_sum(v[j]);
+    if (lane == 0) smem[wid * NV + j] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < NV; ++j) {
+      double s = 0.0;
+      for (int w = 0; w < nw; ++w) s += smem[w * NV + j];
+      v[j] = s;
+    }
+  }
+  __syncthreads();
+}
+
+// Bounded grid barrier for a cooperative launch (all blocks co-resident).
+// On timeout it records ERR_BARRIER and every block leaves.
+__device__ __forceinline__ bool grid_sync(unsigned *bar, int *err, unsigned nblocks) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *vgen = bar + 1;
+    unsigned gen = *vgen;
+    __threadfence();
+    unsigned arrived = atomicAdd(bar, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned long long spins = 0;
+      while (*vgen == gen) {
+        if (++spins > kBarrierSpinLimit) { atomicOr(err, ERR_BARRIER); break; }
+        if (*(volatile int *)err & ERR_BARRIER) break;
+        __nanosleep(40);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return !(*(volatile int *)err & ERR_BARRIER);
+}
+
+// Sum red[0..nblocks*NV) column j in block order (identical in every block).
+template <int NV>
+__device__ __forceinline__ void grid_total(const double *red, unsigned nblocks, double (&out)[NV], double *smem) {
+  if (threadIdx.x < 32) {
+    for (int j = 0; j < NV; ++j) {
+      double s = 0.0;
+      for (unsigned b = threadIdx.x; b < nblocks; b += 32) s += ((volatile const double *)red)[b * NV + j];
+      s = warp_sum(s);
+      if (threadIdx.x == 0) smem[j] = s;
+    }
+  }
+  __syncthreads();
+  for (int j = 0; j < NV; ++j) out[j] = smem[j];
+  __syncthreads();
+}
+
+struct CGArgs {
+  int N, mode;  // mode 0: K (Neumann, constant null space projected); 1: K_II (+) I_B
+  const int32_t *row_ptr, *col_idx, *b_of_node;
+  const double *K, *dinv, *b;
+  double *x, *r, *z, *p, *q, *red;
+  unsigned *bar;
+  int *err, *iters;
+  double rtol, atol;
+  int maxits;
+};
+
+__device__ __forceinline__ double row_apply(const CGArgs &a, int i, const double *__restrict__ v) {
+  if (a.mode == 1 && a.b_of_node[i] >= 0) return v[i];
+  double s = 0.0;
+  const int lo = a.row_ptr[i], hi = a.row_ptr[i + 1];
+  for (int k = lo; k < hi; ++k) {
+    int j = a.col_idx[k];
+    if (a.mode == 1 && a.b_of_node[j] >= 0) continue;
+    s += a.K[k] * v[j];
+  }
+  return s;
+}
+
+// Jacobi-preconditioned CG; stops when ||r||_2 <= max(rtol ||b||_2, atol).
+__global__ void __launch_bounds__(kCGThreads) k_cg(CGArgs a) {
+  __shared__ double smem[32 * 4];
+  const unsigned nblocks = gridDim.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  double mean_b = 0.0;
+  if (a.mode == 0) {
+    double v[1] = {0.0};
+    for (int i = tid; i < a.N; i += stride) v[0] += a.b[i];
+    block_sum<1>(v, smem);
+    if (threadIdx.x == 0) a.red[blockIdx.x] = v[0];
+    if (!grid_sync(a.bar, a.err, nblocks)) return;
+    double t[1];
+    grid_total<1>(a.red, nblocks, t, smem);
+    mean_b = t[0] / a.N;
+    if (!grid_sync(a.bar, a.err, nblocks)) return;
+  }
+  {
+    double v[3] = {0.0, 0.0, 0.0};  // rr, rz, bb
+    for (int i = tid; i < a.N; i += stride) {
+      double bi = a.b[i] - mean_b;
+      double ri = bi - row_apply(a, i, a.x);
+      double zi = a.dinv[i] * ri;
+      a.r[i] = ri; a.z[i] = zi; a.p[i] = zi;
+      v[0] += ri * ri; v[1] += ri * zi; v[2] += bi * bi;
+    }
+    block_sum<3>(v, smem);
+    if (threadIdx.x == 0) { a.red[3 * blockIdx.x] = v[0]; a.red[3 * blockIdx.x + 1] = v[1]; a.red[3 * blockIdx.x + 2] = v[2]; }
+  }
+  if (!grid_sync(a.bar, a.err, nblocks)) return;
+  double tot[3];
+  grid_total<3>(a.red, nblocks, tot, smem);
+  const double tol = fmax(a.rtol * sqrt(tot[2]), a.atol);
+  double rr = tot[0], rz = tot[1];
+  int it = 0;
+  bool failed = false;
+  if (!grid_sync(a.bar, a.err, nblocks)) return;
+  while (sqrt(rr) > tol) {
+    if (it >= a.maxits) { failed = true; break; }
+    {  // q = A p, partial p.q
+      double v[1] = {0.0};
+      for (int i = tid; i < a.N; i += stride) {
+        double qi = row_apply(a, i, a.p);
+        a.q[i] = qi;
+        v[0] += a.p[i] * qi;
+      }
+      block_sum<1>(v, smem);
+      if (threadIdx.x == 0) a.red[blockIdx.x] = v[0];
+    }
+    if (!grid_sync(a.bar, a.err, nblocks)) return;
+    double pq[1];
+    grid_total<1>(a.red, nblocks, pq, smem);
+    const double alpha = rz / pq[0];
+    if (!grid_sync(a.bar, a.err, nblocks)) return;
+    {
+      double v[2] = {0.0, 0.0};
+      for (int i = tid; i < a.N; i += stride) {
+        a.x[i] += alpha * a.p[i];
+        double ri = a.r[i] - alpha * a.q[i];
+        double zi = a.dinv[i] * ri;
+        a.r[i] = ri; a.z[i] = zi;
+        v[0] += ri * ri; v[1] += ri * zi;
+      }
+      block_sum<2>(v, smem);
+      if (threadIdx.x == 0) { a.red[2 * blockIdx.x] = v[0]; a.red[2 * blockIdx.x + 1] = v[1]; }
+    }
+    if (!grid_sync(a.bar, a.err, nblocks)) return;
+    double t2[2];
+    grid_total<2>(a.red, nblocks, t2, smem);
+    ++it;
+    rr = t2[0];
+    if (!(rr == rr) || isinf(rr)) { failed = true; break; }
+    const double beta = t2[1] / rz;
+    rz = t2[1];
+    if (sqrt(rr) <= tol) break;
+    for (int i = tid; i < a.N; i += stride) a.p[i] = a.z[i] + beta * a.p[i];
+    if (!grid_sync(a.bar, a.err, nblocks)) return;
+  }
+  if (a.mode == 0) {  // remove the constant component of the solution
+    if (!grid_sync(a.bar, a.err, nblocks)) return;
+    double v[1] = {0.0};
+    for (int i = tid; i < a.N; i += stride) v[0] += a.x[i];
+    block_sum<1>(v, smem);
+    if (threadIdx.x == 0) a.red[blockIdx.x] = v[0];
+    if (!grid_sync(a.bar, a.err, nblocks)) return;
+    double t[1];
+    grid_total<1>(a.red, nblocks, t, smem);
+    const double mx = t[0] / a.N;
+    for (int i = tid; i < a.N; i += stride) a.x[i] -= mx;
+  }
+  if (tid == 0) {
+    a.iters[a.mode] = it;
+    if (failed) atomicOr(a.err, (rr == rr) ? ERR_CG_MAXITS : ERR_NONFINITE);
+  }
+}
+
+__global__ void k_dinv(int N, const int32_t *__restrict__ diag_pos, const double *__restrict__ K,
+                       const int32_t *__restrict__ b_of_node, double *__restrict__ dn, double *__restrict__ dd) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double inv = 1.0 / K[diag_pos[i]];
+  dn[i] = inv;
+  dd[i] = b_of_node[i] >= 0 ? 1.0 : inv;
+}
+
+// rho = -(Ms * sum_k (D_x m_x + D_y m_y + D_z m_z))
+__global__ void k_div(int N, int nnz, double Ms, const int32_t *__restrict__ row_ptr,
+                      const int32_t *__restrict__ col_idx, const double *__restrict__ D,
+                      const double *__restrict__ m, double *__restrict__ rho) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double s = 0.0;
+  for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+    const double *mj = m + 3 * (size_t)col_idx[k];
+    s += (D[k] * mj[0] + D[(size_t)nnz + k] * mj[1]) + D[2 * (size_t)nnz + k] * mj[2];
+  }
+  rho[i] = -(Ms * s);
+}
+
+__global__ void k_gather_b(int nb, const int32_t *__restrict__ node_of_b, const double *__restrict__ phi,
+                           double *__restrict__ out) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nb) out[b] = phi[node_of_b[b]];
+}
+
+// y_part[s][k] = sum_{c in slab s} B[k][c] x[c]  (column-major B, FP64)
+constexpr int kGemvRows = 256;
+__global__ void __launch_bounds__(kGemvRows) k_gemv_f64(int nb, int slab, const double *__restrict__ B,
+                                                          const double *__restrict__ x, double *__restrict__ part) {
+  __shared__ double xs[1024];
+  const int k = blockIdx.x * kGemvRows + threadIdx.x;
+  const int c0 = blockIdx.y * slab, c1 = min(nb, c0 + slab);
+  double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
+  for (int cb = c0; cb < c1; cb += 1024) {
+    const int ce = min(c1, cb + 1024);
+    __syncthreads();
+    for (int c = cb + threadIdx.x; c < ce; c += blockDim.x) xs[c - cb] = x[c];
+    __syncthreads();
+    if (k < nb) {
+      const double *col = B + (size_t)cb * nb + k;
+      int c = cb;
+      for (; c + 3 < ce; c += 4, col += 4 * (size_t)nb) {
+        acc0 = fma(col[0], xs[c - cb], acc0);
+        acc1 = fma(col[nb], xs[c - cb + 1], acc1);
+        acc2 = fma(col[2 * (size_t)nb], xs[c - cb + 2], acc2);
+        acc3 = fma(col[3 * (size_t)nb], xs[c - cb + 3], acc3);
+      }
+      for (; c < ce; ++c, col += nb) acc0 = fma(col[0], xs[c - cb], acc0);
+    }
+  }
+  if (k < nb) part[(size_t)blockIdx.y * nb + k] = (acc0 + acc1) + (acc2 + acc3);
+}
+
+// FP32 matrix, FP32 products summed in 64-term chunks, chunks summed in FP64.
+__global__ void __launch_bounds__(kGemvRows) k_gemv_f32(int nb, int slab, const float *__restrict__ B,
+                                                          const float *__restrict__ x, double *__restrict__ part) {
+  __shared__ float xs[2048];
+  const int k = blockIdx.x * kGemvRows + threadIdx.x;
+  const int c0 = blockIdx.y * slab, c1 = min(nb, c0 + slab);
+  double acc = 0.0;
+  for (int cb = c0; cb < c1; cb += 2048) {
+    const int ce = min(c1, cb + 2048);
+    __syncthreads();
+    for (int c = cb + threadIdx.x; c < ce; c += blockDim.x) xs[c - cb] = x[c];
+    __syncthreads();
+    if (k < nb) {
+      const float *col = B + (size_t)cb * nb + k;
+      int c = cb;
+      while (c < ce) {
+        const int cc = min(ce, c + 64);
+        float a0 = 0.f, a1 = 0.f;
+        for (; c + 1 < cc; c += 2, col += 2 * (size_t)nb) {
+          a0 = fmaf(col[0], xs[c - cb], a0);
+          a1 = fmaf(col[nb], xs[c - cb + 1], a1);
+        }
+        for (; c < cc; ++c, col += nb) a0 = fmaf(col[0], xs[c - cb], a0);
+        acc += (double)a0 + (double)a1;
+      }
+    }
+  }
+  if (k < nb) part[(size_t)blockIdx.y * nb + k] = acc;
+}
+
+__global__ void k_slab_sum(int nb, int nslab, const double *__restrict__ part, double *__restrict__ y) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nb) return;
+  double s = 0.0;
+  for (int j = 0; j < nslab; ++j) s += part[(size_t)j * nb + k];
+  y[k] = s;
+}
+
+__global__ void k_to_f32_vec(int n, const double *__restrict__ a, float *__restrict__ b) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+// Dirichlet right-hand side (op_load_DBC, sign folded): interior rows
+// -sum_{j boundary} K_ij phi2b_j, boundary rows phi2b; boundary values of the
+// warm start are set to phi2b.
+__global__ void k_dbc_rhs(int N, const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col_idx,
+                          const double *__restrict__ K, const int32_t *__restrict__ b_of_node,
+                          const double *__restrict__ phi2b, double *__restrict__ rhs, double *__restrict__ phi2) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  int bi = b_of_node[i];
+  if (bi >= 0) { rhs[i] = phi2b[bi]; phi2[i] = phi2b[bi]; return; }
+  double s = 0.0;
+  for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+    int b = b_of_node[col_idx[k]];
+    if (b >= 0) s += K[k] * phi2b[b];
+  }
+  rhs[i] = -s;
+}
+
+__global__ void k_add(int n, const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ c) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) c[i] = a[i] + b[i];
+}
+
+struct NodeArgs {
+  int N, nnz, do_demag;
+  const int32_t *row_ptr, *col_idx;
+  const double *K, *G, *vol, *m, *phi, *h_ext;
+  double c_exch, C1, C2, C3, K1, anis, ax, ay, az;
+  double *h_exch, *h_demag, *h_anis, *h_total, *dmdt;
+};
+
+// Fused node kernel: the two SpMV epilogues and every site-wise equation.
+__global__ void k_heff_llg(NodeArgs a) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.N) return;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
+  const int lo = a.row_ptr[i], hi = a.row_ptr[i + 1];
+  for (int k = lo; k < hi; ++k) {
+    const int j = a.col_idx[k];
+    const double kv = a.K[k];
+    const double *mj = a.m + 3 * (size_t)j;
+    s0 += kv * mj[0]; s1 += kv * mj[1]; s2 += kv * mj[2];
+    if (a.do_demag) {
+      const double pj = a.phi[j];
+      g0 += a.G[k] * pj; g1 += a.G[(size_t)a.nnz + k] * pj; g2 += a.G[2 * (size_t)a.nnz + k] * pj;
+    }
+  }
+  const double V = a.vol[i];
+  const double hx[3] = {-a.c_exch * s0 / V, -a.c_exch * s1 / V, -a.c_exch * s2 / V};
+  const double hd[3] = {-g0 / V, -g1 / V, -g2 / V};
+  const double *m = a.m + 3 * (size_t)i;
+  double ha[3] = {0.0, 0.0, 0.0};
+  if (a.K1 != 0.0) {
+    double am = (a.ax * m[0] + a.ay * m[1]) + a.az * m[2];
+    ha[0] = a.anis * am * (a.ax - am * m[0]);
+    ha[1] = a.anis * am * (a.ay - am * m[1]);
+    ha[2] = a.anis * am * (a.az - am * m[2]);
+  }
+  const double *he = a.h_ext + 3 * (size_t)i;
+  double H[3];
+  for (int d = 0; d < 3; ++d) H[d] = ((he[d] + hx[d]) + ha[d]) + hd[d];
+  const double mxH[3] = {m[1] * H[2] - m[2] * H[1], m[2] * H[0] - m[0] * H[2], m[0] * H[1] - m[1] * H[0]};
+  const double mxmxH[3] = {m[1] * mxH[2] - m[2] * mxH[1], m[2] * mxH[0] - m[0] * mxH[2],
+                           m[0] * mxH[1] - m[1] * mxH[0]};
+  const double c3 = a.C3 * (1.0 - ((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2]));
+  for (int d = 0; d < 3; ++d) {
+    const size_t o = 3 * (size_t)i + d;
+    a.h_exch[o] = hx[d]; a.h_demag[o] = hd[d]; a.h_anis[o] = ha[d]; a.h_total[o] = H[d];
+    a.dmdt[o] = (a.C1 * mxH[d] + a.C2 * mxmxH[d]) + c3 * m[d];
+  }
+}
+
+// Energy densities (nmag_lam.py:454-460): E_exch, E_demag, E_ext, E_anis, E_total.
+__global__ void k_energy(int N, const double *__restrict__ m, const double *__restrict__ hx,
+                         const double *__restrict__ hd, const double *__restrict__ he, double ch, double ce,
+                         double K1, double ax, double ay, double az, double *__restrict__ E) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double *mi = m + 3 * (size_t)i, *x = hx + 3 * (size_t)i, *d = hd + 3 * (size_t)i, *e = he + 3 * (size_t)i;
+  double ex = ch * ((mi[0] * x[0] + mi[1] * x[1]) + mi[2] * x[2]);
+  double dm = ch * ((mi[0] * d[0] + mi[1] * d[1]) + mi[2] * d[2]);
+  double ez = ce * ((mi[0] * e[0] + mi[1] * e[1]) + mi[2] * e[2]);
+  double an = 0.0;
+  if (K1 != 0.0) { double am = (ax * mi[0] + ay * mi[1]) + az * mi[2]; an = -K1 * am * am; }
+  E[i] = ex; E[N + i] = dm; E[2 * (size_t)N + i] = ez; E[3 * (size_t)N + i] = an;
+  E[4 * (size_t)N + i] = ((dm + ex) + ez) + an;
+}
+
+// Block partial sums of V_i, V_i m_i (3) and V_i E_k,i (5): 9 columns.
+__global__ void k_avg_partials(int N, const double *__restrict__ m, const double *__restrict__ vol,
+                               const double *__restrict__ E, double *__restrict__ part) {
+  __shared__ double smem[32 * 9];
+  double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    double V = vol[i];
+    v[0] += V;
+    for (int d = 0; d < 3; ++d) v[1 + d] += V * m[3 * (size_t)i + d];
+    if (E) for (int k = 0; k < 5; ++k) v[4 + k] += V * E[(size_t)k * N + i];
+  }
+  block_sum<9>(v, smem);
+  if (threadIdx.x == 0) for (int j = 0; j < 9; ++j) part[9 * blockIdx.x + j] = v[j];
+}
+
+__global__ void k_maxdm_partials(int N, const double *__restrict__ a, const double *__restrict__ b,
+                                 double *__restrict__ part) {
+  __shared__ double smem[32];
+  double mx = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    double d0 = a[3 * (size_t)i] - b[3 * (size_t)i], d1 = a[3 * (size_t)i + 1] - b[3 * (size_t)i + 1],
+           d2 = a[3 * (size_t)i + 2] - b[3 * (size_t)i + 2];
+    mx = fmax(mx, sqrt(d0 * d0 + d1 * d1 + d2 * d2));
+  }
+  for (int o = 16; o; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) smem[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, smem[w]);
+    part[blockIdx.x] = r;
+  }
+}
+
+int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, double atol, int maxits) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  CGArgs a;
+  a.N = M.N; a.mode = mode;
+  a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.b_of_node = M.b_of_node; a.K = M.K;
+  a.dinv = mode == 0 ? W.dinv_n.p : W.dinv_d.p;
+  a.b = b; a.x = x; a.r = W.cg_r; a.z = W.cg_z; a.p = W.cg_p; a.q = W.cg_q; a.red = W.red;
+  a.bar = W.bar; a.err = W.err; a.iters = W.iters;
+  a.rtol = rtol; a.atol = atol; a.maxits = maxits;
+  void *args[] = {&a};
+  cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cg, dim3(W.cg_blocks), dim3(kCGThreads), args, 0,
+                                              h->stream);
+  return e == cudaSuccess ? 0 : 100;
+}
+
+}  // namespace
+
+int init_workspace(nmg_handle *h, std::string &err) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  const int N = M.N, nb = M.nb;
+  const size_t n3 = 3 * (size_t)N;
+  for (DevBuf<double> *b : {&W.m, &W.h_ext, &W.h_exch, &W.h_demag, &W.h_anis, &W.h_total, &W.dmdt})
+    NMG_CUDA_TRY(b->alloc(n3), "alloc field");
+  for (DevBuf<double> *b : {&W.rho, &W.phi1, &W.phi2, &W.phi, &W.rhs2, &W.cg_r, &W.cg_z, &W.cg_p, &W.cg_q,
+                            &W.dinv_n, &W.dinv_d})
+    NMG_CUDA_TRY(b->alloc(N), "alloc scalar field");
+  NMG_CUDA_TRY(W.b1.alloc(nb > 0 ? nb : 1), "alloc");
+  NMG_CUDA_TRY(W.b2.alloc(nb > 0 ? nb : 1), "alloc");
+  NMG_CUDA_TRY(W.E5.alloc(5 * (size_t)N), "alloc");
+  cudaMemsetAsync(W.m.p, 0, sizeof(double) * n3, h->stream);
+  cudaMemsetAsync(W.h_ext.p, 0, sizeof(double) * n3, h->stream);
+  cudaMemsetAsync(W.phi1.p, 0, sizeof(double) * N, h->stream);
+  cudaMemsetAsync(W.phi2.p, 0, sizeof(double) * N, h->stream);
+  cudaMemsetAsync(W.phi.p, 0, sizeof(double) * N, h->stream);
+  for (DevBuf<double> *b : {&W.h_exch, &W.h_demag, &W.h_anis, &W.h_total, &W.dmdt})
+    cudaMemsetAsync(b->p, 0, sizeof(double) * n3, h->stream);
+  // CG grid: one row per thread when it fits in one co-resident wave.
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg, kCGThreads, 0);
+  int max_blocks = per_sm * h->sm_count;
+  int want = nblk(N, kCGThreads);
+  W.cg_blocks = want < max_blocks ? want : max_blocks;
+  if (W.cg_blocks < 1) W.cg_blocks = 1;
+  // GEMV slabs: about 4 blocks per SM in total.
+  int row_tiles = nblk(nb, kGemvRows);
+  int slabs = row_tiles > 0 ? (4 * h->sm_count + row_tiles - 1) / row_tiles : 1;
+  if (slabs < 1) slabs = 1;
+  if (slabs > 64) slabs = 64;
+  if (nb > 0 && slabs > nb) slabs = nb;
+  W.gemv_slabs = slabs;
+  NMG_CUDA_TRY(W.bpart.alloc((size_t)slabs * (nb > 0 ? nb : 1) + (size_t)nb), "alloc gemv partials");
+  size_t red_n = 9 * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);
+  NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
+  NMG_CUDA_TRY(W.bar.alloc(2), "alloc barrier");
+  NMG_CUDA_TRY(W.iters.alloc(2), "alloc");
+  cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);
+  cudaMemsetAsync(W.iters.p, 0, sizeof(int) * 2, h->stream);
+  k_dinv<<<nblk(N, 256), 256, 0, h->stream>>>(N, M.diag_pos, M.K, M.b_of_node, W.dinv_n, W.dinv_d);
+  NMG_CUDA_TRY(cudaGetLastError(), "workspace init");
+  NMG_CUDA_TRY(cudaStreamSynchronize(h->stream), "workspace init");
+  return 0;
+}
+
+void bem_gemv(nmg_handle *h, const double *x, double *y) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  const int nb = M.nb, slabs = W.gemv_slabs;
+  const int slab = (nb + slabs - 1) / slabs;
+  dim3 grid(nblk(nb, kGemvRows), slabs);
+  if (h->opt.bem_precision == 1 && M.bem32.p) {
+    float *x32 = reinterpret_cast<float *>(W.bpart.p + (size_t)slabs * nb);
+    k_to_f32_vec<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, x, x32);
+    k_gemv_f32<<<grid, kGemvRows, 0, h->stream>>>(nb, slab, M.bem32, x32, W.bpart);
+  } else {
+    k_gemv_f64<<<grid, kGemvRows, 0, h->stream>>>(nb, slab, M.bem, x, W.bpart);
+  }
+  k_slab_sum<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, slabs, W.bpart, y);
+}
+
+int check_device_error(nmg_handle *h, const char *where) {
+  int derr = 0;
+  cudaError_t e = cudaMemcpyAsync(&derr, h->ws.err.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    h->last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return 100;
+  }
+  if (derr) {
+    cudaMemsetAsync(h->ws.err.p, 0, sizeof(int), h->stream);
+    if (derr & ERR_BARRIER) h->last_error = std::string(where) + ": grid barrier timed out";
+    else if (derr & ERR_NONFINITE) h->last_error = std::string(where) + ": solver produced non-finite values";
+    else if (derr & ERR_CG_MAXITS) h->last_error = std::string(where) + ": CG reached its iteration limit";
+    else h->last_error = std::string(where) + ": device error flag " + std::to_string(derr);
+    return (derr & ERR_BARRIER) ? 7 : ((derr & ERR_NONFINITE) ? 6 : 5);
+  }
+  return 0;
+}
+
+int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  cudaStream_t s = h->stream;
+  const int N = M.N;
+  const nmg_material &mt = h->mat;
+  if (h->opt.do_demag && M.nb > 0) {
+    k_div<<<nblk(N, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, M.D, d_m, W.rho);
+    if (run_cg(h, 0, W.rho, W.phi1, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
+    k_gather_b<<<nblk(M.nb, 256), 256, 0, s>>>(M.nb, M.node_of_b, W.phi1, W.b1);
+    bem_gemv(h, W.b1, W.b2);
+    k_dbc_rhs<<<nblk(N, 256), 256, 0, s>>>(N, M.row_ptr, M.col_idx, M.K, M.b_of_node, W.b2, W.rhs2, W.phi2);
+    if (run_cg(h, 1, W.rhs2, W.phi2, h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)) return 100;
+    k_add<<<nblk(N, 256), 256, 0, s>>>(N, W.phi1, W.phi2, W.phi);
+  }
+  NodeArgs a;
+  a.N = N; a.nnz = M.nnz; a.do_demag = (h->opt.do_demag && M.nb > 0) ? 1 : 0;
+  a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.K = M.K; a.G = M.G; a.vol = M.vol;
+  a.m = d_m; a.phi = W.phi; a.h_ext = W.h_ext;
+  a.c_exch = mt.exch_coeff; a.C1 = mt.C1; a.C2 = mt.C2; a.C3 = mt.C3; a.K1 = mt.K1; a.anis = mt.anis_coeff;
+  a.ax = mt.axis[0]; a.ay = mt.axis[1]; a.az = mt.axis[2];
+  a.h_exch = W.h_exch; a.h_demag = W.h_demag; a.h_anis = W.h_anis; a.h_total = W.h_total;
+  a.dmdt = d_dmdt ? d_dmdt : W.dmdt.p;
+  k_heff_llg<<<nblk(N, 128), 128, 0, s>>>(a);
+  h->n_rhs++;
+  return cudaGetLastError() == cudaSuccess ? 0 : 100;
+}
+
+int energy_density(nmg_handle *h, const double *d_m, double *d_E5) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  const nmg_material &mt = h->mat;
+  k_energy<<<nblk(M.N, 256), 256, 0, h->stream>>>(M.N, d_m, W.h_exch, W.h_demag, W.h_ext, mt.E_coeff_half,
+                                                  mt.E_coeff_ext, mt.K1, mt.axis[0], mt.axis[1], mt.axis[2], d_E5);
+  return cudaGetLastError() == cudaSuccess ? 0 : 100;
+}
+
+int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5]) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  const int nblocks = 64;
+  const double *E = energies ? W.E5.p : nullptr;
+  if (energies && energy_density(h, d_m, W.E5)) return 100;
+  k_avg_partials<<<nblocks, 256, 0, h->stream>>>(M.N, d_m, M.vol, E, W.red);
+  std::vector<double> part(9 * nblocks);
+  if (cudaMemcpyAsync(part.data(), W.red.p, sizeof(double) * 9 * nblocks, cudaMemcpyDeviceToHost, h->stream) ||
+      cudaStreamSynchronize(h->stream))
+    return 100;
+  double tot[9] = {0};
+  for (int b = 0; b < nblocks; ++b)
+    for (int j = 0; j < 9; ++j) tot[j] += part[9 * b + j];
+  for (int d = 0; d < 3; ++d) avg[d] = tot[1 + d] / tot[0];
+  if (energies) for (int k = 0; k < 5; ++k) energies[k] = tot[4 + k];
+  return 0;
+}
+
+int max_dm(nmg_handle *h, const double *d_m, const double *d_mprev, double *out) {
+  const int nblocks = 64;
+  k_maxdm_partials<<<nblocks, 256, 0, h->stream>>>(h->mesh.N, d_m, d_mprev, h->ws.red);
+  double part[nblocks];
+  if (cudaMemcpyAsync(part, h->ws.red.p, sizeof(double) * nblocks, cudaMemcpyDeviceToHost, h->stream) ||
+      cudaStreamSynchronize(h->stream))
+    return 100;
+  double mx = 0.0;
+  for (int b = 0; b < nblocks; ++b) mx = part[b] > mx ? part[b] : mx;
+  *out = mx;
+  return 0;
+}
+
+}  // namespace nmg

@@ -1,0 +1,19 @@
+"""nmag (GB300 build): the LLG right-hand side and time integration of
+nmag/nsim on hand-written sm_103a CUDA kernels, behind nmag's Python API.
+
+    import nmag
+    from nmag import SI
+    mat = nmag.MagMaterial("Py", Ms=SI(0.86e6, "A/m"), exchange_coupling=SI(13e-12, "J/m"), llg_damping=0.5)
+    sim = nmag.Simulation()
+    sim.load_mesh(nmag.mesh.cube_mesh(), [("cube", mat)], unit_length=SI(1e-9, "m"))
+    sim.set_m([1, 1, 1])
+    sim.advance_time(SI(1e-12, "s"))
+"""
+from . import mesh
+from .si import SI, simulation_units
+from .material import MagMaterial, uniaxial_anisotropy
+from .simulation import Simulation, every, at
+from ._lib import NmagGpuError
+
+__all__ = ["SI", "simulation_units", "MagMaterial", "uniaxial_anisotropy", "Simulation", "every", "at", "mesh",
+           "NmagGpuError"]

@@ -1,0 +1,225 @@
+"""ctypes binding of libnmaggpu.so (include/nmag_gpu.h).
+
+The library is the only compute path: if it is missing or cannot be loaded,
+``lib()`` raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _build
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+class Material(C.Structure):
+    _fields_ = [("Ms", C.c_double), ("exch_coeff", C.c_double), ("C1", C.c_double), ("C2", C.c_double),
+                ("C3", C.c_double), ("K1", C.c_double), ("axis", C.c_double * 3), ("anis_coeff", C.c_double),
+                ("E_coeff_half", C.c_double), ("E_coeff_ext", C.c_double)]
+
+
+class Options(C.Structure):
+    _fields_ = [("do_demag", C.c_int), ("nbc_rtol", C.c_double), ("nbc_atol", C.c_double), ("nbc_maxits", C.c_int),
+                ("dbc_rtol", C.c_double), ("dbc_atol", C.c_double), ("dbc_maxits", C.c_int),
+                ("bem_precision", C.c_int), ("cg_precision", C.c_int), ("reserved", C.c_int * 6)]
+
+
+class TsStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("nst", "nfe", "nni", "nli", "ncfn", "netf", "npe", "nps", "njv", "nje")] + \
+               [("hcur", C.c_double), ("tcur", C.c_double), ("qcur", C.c_int32), ("last_cg_iters_nbc", C.c_int32),
+                ("last_cg_iters_dbc", C.c_int32), ("pad", C.c_int32), ("time_rhs_ms", C.c_double),
+                ("time_jv_ms", C.c_double), ("time_psolve_ms", C.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad"}
+
+
+# every symbol declared in include/nmag_gpu.h
+EXPORTS = ["nmg_version", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_mesh_info", "nmg_get_csr",
+           "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
+           "nmg_set_material", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
+           "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings"]
+
+_lib = None
+
+
+class NmagGpuError(RuntimeError):
+    pass
+
+
+def lib_path():
+    return _build.LIB
+
+
+def lib(build_if_missing=True):
+    """Load libnmaggpu.so (building it in-tree with nvcc if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB) or not _build.up_to_date():
+        if not build_if_missing:
+            raise NmagGpuError("libnmaggpu.so is not built (run nmag._build.build())")
+        _build.build()
+    L = C.CDLL(_build.LIB)
+    vp = C.c_void_p
+    L.nmg_version.restype = C.c_int
+    L.nmg_last_error.argtypes = [vp]
+    L.nmg_last_error.restype = C.c_char_p
+    L.nmg_create.argtypes = [_f64p, C.c_int, _i32p, C.c_int, C.POINTER(Material), C.POINTER(Options), C.POINTER(vp)]
+    L.nmg_destroy.argtypes = [vp]
+    L.nmg_mesh_info.argtypes = [vp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]
+    L.nmg_get_csr.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.nmg_export_operator.argtypes = [vp, C.c_int, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int), vp, vp, vp]
+    L.nmg_get_boundary.argtypes = [vp, vp, vp, vp, vp]
+    L.nmg_get_bem.argtypes = [vp, _f64p]
+    L.nmg_set_m.argtypes = [vp, _f64p]
+    L.nmg_get_m.argtypes = [vp, _f64p]
+    L.nmg_set_h_ext.argtypes = [vp, _f64p]
+    L.nmg_set_material.argtypes = [vp, C.POINTER(Material)]
+    L.nmg_eval_fields.argtypes = [vp, vp, vp]
+    L.nmg_energy_density.argtypes = [vp, _f64p]
+    L.nmg_averages.argtypes = [vp, _f64p, vp]
+    L.nmg_ts_init.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]
+    L.nmg_ts_advance.argtypes = [vp, C.c_double, C.c_int, C.c_int64, C.POINTER(C.c_double), C.POINTER(TsStats)]
+    L.nmg_max_dm.argtypes = [vp, _f64p, C.POINTER(C.c_double)]
+    L.nmg_rhs_device.argtypes = [vp, vp, vp]
+    L.nmg_rk4_device.argtypes = [vp, vp, C.c_double, C.c_int]
+    L.nmg_get_timings.argtypes = [vp, _f64p]
+    _lib = L
+    return L
+
+
+def check(rc, handle=None, what="call"):
+    if rc != 0:
+        msg = lib().nmg_last_error(handle)
+        raise NmagGpuError("%s failed (status %d): %s" % (what, rc, msg.decode() if msg else ""))
+
+
+class Engine(object):
+    """Owns one nmg_handle: the device state of one simulation."""
+
+    def __init__(self, points, simplices, material: Material, options: Options):
+        L = lib()
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1)
+        sim = np.ascontiguousarray(simplices, dtype=np.int32).reshape(-1)
+        h = C.c_void_p()
+        rc = L.nmg_create(pts, len(pts) // 3, sim, len(sim) // 4, C.byref(material), C.byref(options), C.byref(h))
+        if rc != 0:
+            raise NmagGpuError("nmg_create failed (status %d): %s" % (rc, L.nmg_last_error(None).decode()))
+        self.h = h
+        info = np.zeros(6, np.int64)
+        L.nmg_mesh_info(h, info)
+        self.N, self.T, self.nnz, self.nb, self.ntri, self.nouter = (int(v) for v in info)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().nmg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- state ----
+    def set_m(self, m):
+        check(lib().nmg_set_m(self.h, np.ascontiguousarray(m, dtype=np.float64).reshape(-1)), self.h, "set_m")
+
+    def get_m(self):
+        out = np.zeros(3 * self.N)
+        check(lib().nmg_get_m(self.h, out), self.h, "get_m")
+        return out.reshape(self.N, 3)
+
+    def set_h_ext(self, h):
+        h = np.broadcast_to(np.asarray(h, dtype=np.float64), (self.N, 3))
+        check(lib().nmg_set_h_ext(self.h, np.ascontiguousarray(h).reshape(-1)), self.h, "set_h_ext")
+
+    def set_material(self, mat: Material):
+        check(lib().nmg_set_material(self.h, C.byref(mat)), self.h, "set_material")
+
+    # ---- evaluation ----
+    def eval_fields(self):
+        f = np.zeros(15 * self.N)
+        s = np.zeros(2 * self.N)
+        check(lib().nmg_eval_fields(self.h, f.ctypes.data, s.ctypes.data), self.h, "eval_fields")
+        f = f.reshape(5, self.N, 3)
+        return {"H_exch": f[0], "H_demag": f[1], "H_anis": f[2], "H_total": f[3], "dmdt": f[4],
+                "phi": s[:self.N], "rho": s[self.N:]}
+
+    def energy_density(self):
+        E = np.zeros(5 * self.N)
+        check(lib().nmg_energy_density(self.h, E), self.h, "energy_density")
+        E = E.reshape(5, self.N)
+        return {"E_exch": E[0], "E_demag": E[1], "E_ext": E[2], "E_anis": E[3], "E_total": E[4]}
+
+    def averages(self, energies=False):
+        a = np.zeros(3)
+        e = np.zeros(5)
+        check(lib().nmg_averages(self.h, a, e.ctypes.data if energies else None), self.h, "averages")
+        return (a, e) if energies else a
+
+    # ---- time integration ----
+    def ts_init(self, t0=0.0, rtol=1e-6, atol=1e-6, max_order=2, krylov_max=300):
+        check(lib().nmg_ts_init(self.h, t0, rtol, atol, max_order, krylov_max), self.h, "ts_init")
+
+    def ts_advance(self, t, exact_tstop=True, max_steps=-1):
+        tr = C.c_double()
+        st = TsStats()
+        check(lib().nmg_ts_advance(self.h, t, int(bool(exact_tstop)), int(max_steps), C.byref(tr), C.byref(st)),
+              self.h, "ts_advance")
+        return tr.value, st.as_dict()
+
+    def max_dm(self, m_prev):
+        out = C.c_double()
+        check(lib().nmg_max_dm(self.h, np.ascontiguousarray(m_prev, dtype=np.float64).reshape(-1), C.byref(out)),
+              self.h, "max_dm")
+        return out.value
+
+    def timings(self):
+        t = np.zeros(8)
+        lib().nmg_get_timings(self.h, t)
+        return t
+
+    # ---- inspection (parity tests) ----
+    def csr(self):
+        N, nnz = self.N, self.nnz
+        rp = np.zeros(N + 1, np.int32); ci = np.zeros(nnz, np.int32); K = np.zeros(nnz)
+        G = np.zeros(3 * nnz); D = np.zeros(3 * nnz); V = np.zeros(N)
+        check(lib().nmg_get_csr(self.h, rp.ctypes.data, ci.ctypes.data, K.ctypes.data, G.ctypes.data, D.ctypes.data,
+                                V.ctypes.data), self.h, "get_csr")
+        return rp, ci, K, G.reshape(3, nnz), D.reshape(3, nnz), V
+
+    def export_operator(self, which, coeff=1.0):
+        L = lib()
+        r, c, n = C.c_int(), C.c_int(), C.c_int()
+        check(L.nmg_export_operator(self.h, which, coeff, C.byref(r), C.byref(c), C.byref(n), None, None, None),
+              self.h, "export_operator")
+        rp = np.zeros(r.value + 1, np.int32); ci = np.zeros(n.value, np.int32); va = np.zeros(n.value)
+        check(L.nmg_export_operator(self.h, which, coeff, C.byref(r), C.byref(c), C.byref(n), rp.ctypes.data,
+                                    ci.ctypes.data, va.ctypes.data), self.h, "export_operator")
+        return rp, ci, va, (r.value, c.value)
+
+    def boundary(self):
+        nob = np.zeros(self.nb, np.int32); tri = np.zeros(3 * self.ntri, np.int32)
+        nrm = np.zeros(3 * self.ntri); sa = np.zeros(self.nb)
+        check(lib().nmg_get_boundary(self.h, nob.ctypes.data, tri.ctypes.data, nrm.ctypes.data, sa.ctypes.data),
+              self.h, "get_boundary")
+        return nob, tri.reshape(-1, 3), nrm.reshape(-1, 3), sa
+
+    def bem(self):
+        out = np.zeros(self.nb * self.nb)
+        check(lib().nmg_get_bem(self.h, out), self.h, "get_bem")
+        return out.reshape(self.nb, self.nb)
+
+    # ---- device pointers (torch tensors) ----
+    def rhs_device(self, d_m, d_dmdt):
+        check(lib().nmg_rhs_device(self.h, C.c_void_p(d_m), C.c_void_p(d_dmdt)), self.h, "rhs_device")
+
+    def rk4_device(self, d_m, dt, nsteps):
+        check(lib().nmg_rk4_device(self.h, C.c_void_p(d_m), dt, nsteps), self.h, "rk4_device")

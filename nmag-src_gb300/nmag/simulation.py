@@ -1,0 +1,419 @@
+"""nmag.Simulation on libnmaggpu: the drop-in for the LLG path of
+interface/nmag/main.py (Simulation, main.py:776-2883), simulation_core.py
+(relax/hysteresis entry points, :276-278), hysteresis.py (:207-557) and
+convergence.py (:54-100).
+
+State lives on the GPU in one ``nmg_handle``; the host keeps the "master
+buffer" copy of m that the reference keeps (main.py:550-705): every
+``advance_time`` copies m back once, exactly like the reference's
+``_to_mbuf_copier("m")`` (main.py:1383), and computes max|dm| from it.
+"""
+from __future__ import annotations
+
+import logging
+import math
+import os
+import time as _time
+
+import numpy as np
+
+from . import mesh as _mesh
+from . import si as _si
+from ._lib import Engine, Material, Options, NmagGpuError
+from .material import MagMaterial
+from .si import SI, simulation_units
+
+log = logging.getLogger("nmag")
+
+_FIELD_SI = {"H": SI(1.0, "A/m"), "E": SI(1.0, "J/m^3"), "phi": SI(1.0, "A"), "rho": SI(1.0, "A/m^2"),
+             "dmdt": SI(1.0, "1/s")}
+
+
+def _su_factor(kind):
+    return 1.0 / simulation_units.of(_FIELD_SI[kind])
+
+
+class Clock(dict):
+    """Simulation clock (interface/nmag/clock.py): ids, steps, stage data."""
+
+    def __init__(self):
+        super().__init__(id=-1, stage=1, step=0, time_su=0.0, stage_step=0, stage_time_su=0.0,
+                         real_time=0.0, stage_end=False, convergence=False, exit_hysteresis=False,
+                         last_step_dt_su=0.0, time_reached_su=0.0)
+
+    def __getattr__(self, k):
+        try:
+            return self[k]
+        except KeyError:
+            raise AttributeError(k)
+
+    def __setattr__(self, k, v):
+        self[k] = v
+
+
+class every(object):
+    """Schedule: every('step', 5), every('time', SI(1e-12, 's')) (nsim/when.py)."""
+
+    def __init__(self, what, value, first=0):
+        self.what, self.value, self.first = what, value, first
+
+    def next_delta(self, clock):
+        if self.what == "step":
+            n = int(self.value)
+            return ("step", n - (clock.stage_step % n) if clock.stage_step % n else n)
+        if self.what == "time":
+            dt = simulation_units.of(self.value, compatible_with=SI("s")) if isinstance(self.value, SI) else float(self.value)
+            k = math.floor(clock.stage_time_su / dt + 1e-9) + 1
+            return ("time", k * dt - clock.stage_time_su)
+        return (None, None)
+
+    def match(self, clock):
+        if self.what == "step":
+            return clock.stage_step % int(self.value) == 0
+        if self.what == "time":
+            dt = simulation_units.of(self.value, compatible_with=SI("s")) if isinstance(self.value, SI) else float(self.value)
+            r = clock.stage_time_su / dt
+            return abs(r - round(r)) < 1e-9
+        return False
+
+
+class at(object):
+    """Schedule at an event: at('stage_end'), at('convergence'), at('step', n)."""
+
+    def __init__(self, what, value=None):
+        self.what, self.value = what, value
+
+    def next_delta(self, clock):
+        return (None, None)
+
+    def match(self, clock):
+        if self.what in ("stage_end", "convergence"):
+            return bool(clock.stage_end)
+        if self.what == "step":
+            return clock.stage_step == self.value
+        return False
+
+
+class Simulation(object):
+    """Micromagnetic simulation (main.py:776-845 constructor arguments)."""
+
+    def __init__(self, name=None, phi_BEM=None, periodic_bc=None, do_demag=True, do_anisotropy_jacobian=False,
+                 temperature=None, thermal_delta_t=None, user_seed_T=0, timestepper_max_order=2,
+                 timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
+                 lam_debugfile=None, quirks="nmag", bem_precision="fp64"):
+        if periodic_bc is not None:
+            raise NotImplementedError("periodic boundary conditions are outside this path")
+        if temperature is not None:
+            raise NotImplementedError("thermal (Heun) integration is disabled in the reference (main.py:797-806)")
+        if do_anisotropy_jacobian:
+            raise NotImplementedError("do_anisotropy_jacobian is not implemented on this path")
+        self.name = name or "nmag"
+        self._do_demag = bool(do_demag)
+        self.max_order = int(timestepper_max_order)
+        self.krylov_max = int(timestepper_krylov_max)
+        self.ksp_tolerances = dict(ksp_tolerances or {})
+        self.quirks = quirks
+        self.bem_precision = bem_precision
+        self.ts_rel_tol = 1e-6
+        self.ts_abs_tol = 1e-6
+        self.stopping_dm_dt = simulation_units.of(_si.degrees_per_ns)   # 1 deg/ns
+        self._default_exact_tstop = True
+        self.max_time_reached = simulation_units.of(SI(1.0, "s"))
+        self.clock = Clock()
+        self.max_dm_dt = None
+        self._countdown_initial = 2
+        self._countdown = 2
+        self.engine = None
+        self.mesh = None
+        self.material = None
+        self._m = None          # host master buffer of m (N,3)
+        self._h_ext = None
+        self._ts_ready = False
+        self._last_nst = 0
+        self.last_stats = {}
+
+    # ---- setup -----------------------------------------------------------
+    def load_mesh(self, filename, region_names_and_mag_mats, unit_length, do_reorder=False, manual_distribution=None):
+        """main.py:1075.  ``filename`` is an nmesh ASCII file or a ``nmag.mesh.Mesh``."""
+        m = _mesh.load(filename)
+        mats = []
+        for entry in region_names_and_mag_mats:
+            region_name, mat = entry
+            mats.extend(mat if isinstance(mat, (list, tuple)) else [mat])
+        if len(mats) != 1:
+            raise NotImplementedError("exactly one magnetic material is supported on this path")
+        if np.any(m.regions <= 0):
+            raise NotImplementedError("vacuum (region 0) simplices are not supported on this path")
+        self.material = mats[0]
+        scale = simulation_units.of(unit_length, compatible_with=SI("m"))
+        self.mesh = _mesh.Mesh(m.points * scale, m.simplices, m.regions)
+        opts = Options()
+        opts.do_demag = int(self._do_demag)
+
+        def tol(key, default):
+            v = self.ksp_tolerances.get(key)
+            return default if v is None else v
+        opts.nbc_rtol, opts.nbc_atol, opts.nbc_maxits = tol("NBC.rtol", 1e-5), tol("NBC.atol", 1e-50), int(tol("NBC.maxits", 10000))
+        opts.dbc_rtol, opts.dbc_atol, opts.dbc_maxits = tol("DBC.rtol", 1e-5), tol("DBC.atol", 1e-50), int(tol("DBC.maxits", 10000))
+        opts.bem_precision = {"fp64": 0, "fp32": 1}[self.bem_precision]
+        self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
+        N = self.engine.N
+        self._m = np.zeros((N, 3))
+        self._h_ext = np.zeros((N, 3))
+        self._ts_ready = False
+        return self.mesh
+
+    def _material_struct(self):
+        c = self.material.coefficients(self.quirks)
+        mt = Material()
+        mt.Ms, mt.exch_coeff, mt.C1, mt.C2, mt.C3 = c["Ms"], c["exch_coeff"], c["C1"], c["C2"], c["C3"]
+        mt.K1 = c["K1"]
+        for d in range(3):
+            mt.axis[d] = c["axis"][d]
+        mt.anis_coeff, mt.E_coeff_half, mt.E_coeff_ext = c["anis_coeff"], c["E_coeff_half"], c["E_coeff_ext"]
+        return mt
+
+    def set_damping(self, llg_damping):
+        """Change the material's damping (e.g. between relax and dynamics)."""
+        self.material.set_damping(llg_damping)
+        self.engine.set_material(self._material_struct())
+        self._ts_ready = False
+
+    def _positions_si(self):
+        return self.mesh.points * simulation_units.conversion_factor_of(SI("m"))
+
+    def _vector_values(self, values):
+        N = self.engine.N
+        if callable(values):
+            pos = self._positions_si()
+            return np.array([values(p) for p in pos], dtype=np.float64).reshape(N, 3)
+        arr = np.asarray(values, dtype=np.float64)
+        if arr.shape == (3,):
+            return np.broadcast_to(arr, (N, 3)).copy()
+        return arr.reshape(N, 3).copy()
+
+    def set_m(self, values, subfieldname=None):
+        """main.py:1787: set m (auto-normalised)."""
+        m = self._vector_values(values)
+        n = np.linalg.norm(m, axis=1)
+        if np.any(n == 0.0):
+            raise ValueError("set_m: zero-length magnetisation vector")
+        m = m / n[:, None]
+        self._m = m
+        self.engine.set_m(m)
+        self._ts_ready = False
+
+    def set_H_ext(self, values, unit=None):
+        """main.py:1726: values times unit (SI, compatible with A/m)."""
+        if unit is None:
+            vals = values
+            if isinstance(values, (list, tuple)) and values and isinstance(values[0], SI):
+                vals = [simulation_units.of(v, compatible_with=SI("A/m")) for v in values]
+                h = self._vector_values(vals)
+            else:
+                h = self._vector_values(vals) / _su_factor("H")
+        else:
+            h = self._vector_values(values) * simulation_units.of(unit, compatible_with=SI("A/m"))
+        self._h_ext = h
+        self.engine.set_h_ext(h)
+        self._ts_ready = False
+
+    def set_params(self, stopping_dm_dt=None, ts_rel_tol=None, ts_abs_tol=None, exact_tstop=None):
+        """main.py:1048-1073."""
+        if stopping_dm_dt is not None:
+            self.stopping_dm_dt = simulation_units.of(stopping_dm_dt, compatible_with=SI("1/s"))
+        if ts_rel_tol is not None:
+            self.ts_rel_tol = float(ts_rel_tol)
+            self._ts_ready = False
+        if ts_abs_tol is not None:
+            self.ts_abs_tol = float(ts_abs_tol)
+            self._ts_ready = False
+        if exact_tstop is not None:
+            self._default_exact_tstop = bool(exact_tstop)
+
+    def reinitialise(self, initial_time=None):
+        """main.py:2707: (re)create the integrator at the current state."""
+        if initial_time is not None:
+            self.clock.stage_time_su = 0.0
+            self.clock.stage_step = 0
+            t0 = 0.0
+        else:
+            t0 = self.clock.stage_time_su
+        self.engine.ts_init(t0, self.ts_rel_tol, self.ts_abs_tol, self.max_order, self.krylov_max)
+        self._ts_t0 = t0
+        self._last_nst = 0
+        self._ts_ready = True
+
+    # ---- dynamics ----------------------------------------------------------
+    def advance_time(self, target_time, max_it=-1, exact_tstop=None):
+        """main.py:1325-1460: integrate to target_time (SI), or max_it steps."""
+        if max_it is None or max_it < 0:
+            max_it = -1
+        if exact_tstop is None:
+            exact_tstop = self._default_exact_tstop
+        target_su = simulation_units.of(target_time, compatible_with=SI("s")) if isinstance(target_time, SI) else float(target_time)
+        if not self._ts_ready:
+            self.reinitialise()
+        if target_su == 0:
+            return target_time
+        prev_m = self._m
+        t_stage, stats = self.engine.ts_advance(target_su, exact_tstop, max_it)
+        self._m = self.engine.get_m()
+        delta_steps = stats["nst"] - self._last_nst
+        self._last_nst = stats["nst"]
+        delta_t = t_stage - self.clock.stage_time_su
+        self.clock.stage_time_su = t_stage
+        self.clock.time_su += delta_t
+        self.clock.time_reached_su = self.clock.time_su
+        self.clock.step += max(delta_steps, 0)
+        self.clock.stage_step += max(delta_steps, 0)
+        self.clock.last_step_dt_su = stats["hcur"]
+        self.last_stats = stats
+        if prev_m is not None and delta_t > 0.0:
+            dm = np.sqrt(((self._m - prev_m) ** 2).sum(axis=1)).max()
+            self.max_dm_dt = dm / delta_t
+        return SI(t_stage * simulation_units.conversion_factor_of(SI("s")), "s")
+
+    def is_converged(self):
+        """convergence.py:54-100: max dm/dt below stopping_dm_dt twice in a row."""
+        if self.max_dm_dt is None:
+            return False
+        if self.max_dm_dt < self.stopping_dm_dt:
+            self._countdown -= 1
+            if self._countdown < 1:
+                self._countdown = self._countdown_initial
+                return True
+            return False
+        self._countdown = self._countdown_initial
+        return False
+
+    def hysteresis(self, H_ext_list, save=None, do=None, convergence_check=every("step", 5)):
+        """hysteresis.py:244-557: for each field, relax until converged."""
+        save = list(save or [])
+        do = list(do or [])
+        for stage_idx, H in enumerate(H_ext_list):
+            self.clock.stage = stage_idx + 1
+            self.clock.stage_end = False
+            if H is not None:
+                if isinstance(H, (list, tuple)) and len(H) == 3 and all(isinstance(v, SI) for v in H):
+                    self.set_H_ext(H)
+                elif isinstance(H, tuple) and len(H) == 2 and isinstance(H[1], SI):
+                    self.set_H_ext(H[0], H[1])
+                else:
+                    self.set_H_ext(H)
+            self.max_dm_dt = None
+            self._countdown = self._countdown_initial
+            self._last_nst = 0
+            self.reinitialise(initial_time=0)
+            while True:
+                self.clock.stage_end = self.is_converged()
+                for what, when in save + do:
+                    if when.match(self.clock):
+                        self._do_action(what)
+                if self.clock.exit_hysteresis:
+                    return
+                if self.clock.stage_end:
+                    break
+                kind, delta = convergence_check.next_delta(self.clock)
+                if kind == "step":
+                    target, max_it = self.max_time_reached, int(delta)
+                elif kind == "time":
+                    target, max_it = self.clock.stage_time_su + delta, -1
+                else:
+                    target, max_it = self.max_time_reached, -1
+                t = self.advance_time(target, max_it=max_it)
+                if simulation_units.of(t, compatible_with=SI("s")) > 0.99 * self.max_time_reached:
+                    raise RuntimeError("Simulation time reached %s: are you starting from a zero torque "
+                                       "configuration?" % self.max_time_reached)
+
+    def relax(self, save=None, do=None, convergence_check=every("step", 5)):
+        """hysteresis.py:207-242: hysteresis([None])."""
+        return self.hysteresis([None], save=save, do=do, convergence_check=convergence_check)
+
+    def _do_action(self, what):
+        if callable(what):
+            what(self)
+        elif what == "averages":
+            self.save_data()
+        elif what == "fields":
+            self.save_data(fields="all")
+        elif what == "restart":
+            self.save_restart_file()
+        elif what == "exit":
+            self.clock.exit_hysteresis = True
+
+    # ---- read-out ------------------------------------------------------------
+    def get_subfield(self, subfieldname, units=None):
+        """Field values per node in SI (m is dimensionless)."""
+        name = subfieldname.split("_")[0] if subfieldname.startswith("m_") else subfieldname
+        if subfieldname == "m" or subfieldname.startswith("m_"):
+            return self._m.copy()
+        if subfieldname.startswith("H_ext"):
+            return self._h_ext * _su_factor("H")
+        f = self.engine.eval_fields()
+        for key in ("H_exch", "H_demag", "H_anis", "H_total"):
+            if subfieldname.startswith(key):
+                return f[key] * _su_factor("H")
+        if subfieldname.startswith("dmdt"):
+            return f["dmdt"] * _su_factor("dmdt")
+        if subfieldname == "phi":
+            return f["phi"] * _su_factor("phi")
+        if subfieldname == "rho":
+            return f["rho"] * _su_factor("rho")
+        if subfieldname.startswith("E_"):
+            E = self.engine.energy_density()
+            for key in E:
+                if subfieldname.startswith(key):
+                    return E[key] * _su_factor("E")
+        raise KeyError("unknown subfield %r" % subfieldname)
+
+    def get_subfield_average_siv(self, field, subfield=None):
+        name = field if subfield is None else field
+        if name == "m" or name.startswith("m_"):
+            return list(self.engine.averages())
+        vals = self.get_subfield(name)
+        V = self._volumes()
+        if vals.ndim == 2:
+            return list((vals * V[:, None]).sum(0) / V.sum())
+        return float((vals * V).sum() / V.sum())
+
+    def get_subfield_average(self, field, subfield=None):
+        return self.get_subfield_average_siv(field, subfield)
+
+    def _volumes(self):
+        if not hasattr(self, "_vol_cache"):
+            self._vol_cache = self.engine.csr()[5]
+        return self._vol_cache
+
+    def energies(self):
+        """Total energies (J) [E_exch, E_demag, E_ext, E_anis, E_total] at the current m."""
+        self.engine.eval_fields()
+        _, e = self.engine.averages(energies=True)
+        return e * _su_factor("E") * (simulation_units.conversion_factor_of(SI("m")) ** 3)
+
+    def save_data(self, fields=None, avoid_same_step=False):
+        """Append averages to <name>_dat.ndt (main.py:2481-2636 column subset)."""
+        fn = "%s_dat.ndt" % self.name
+        avg = self.engine.averages()
+        new = not os.path.exists(fn)
+        with open(fn, "a") as f:
+            if new:
+                f.write("#%9s %12s %16s %16s %16s %16s\n" % ("step", "stage", "time", "m_Py_0", "m_Py_1", "m_Py_2"))
+            f.write(" %9d %12d %16.9e %16.9e %16.9e %16.9e\n" % (
+                self.clock.step, self.clock.stage, self.clock.time_su * 1e-12, avg[0], avg[1], avg[2]))
+        if fields == "all":
+            np.savez("%s_fields_%06d.npz" % (self.name, self.clock.step), m=self._m)
+
+    def save_restart_file(self, filename=None):
+        """main.py:2764-2857: m and the clock, written via a temp file + rename."""
+        fn = filename or "%s_restart.npz" % self.name
+        tmp = fn + ".tmp.npz"
+        np.savez(tmp, m=self._m, clock=np.array([repr(dict(self.clock))]))
+        os.replace(tmp, fn)
+
+    def load_restart_file(self, filename=None):
+        fn = filename or "%s_restart.npz" % self.name
+        d = np.load(fn, allow_pickle=False)
+        self.set_m(d["m"])
+        import ast
+        self.clock.update(ast.literal_eval(str(d["clock"][0])))

@@ -1,0 +1,131 @@
+/*
+ * nmag_oracle.h -- CPU restatement of nmag/nsim's LLG right-hand side and its
+ * time integration, used ONLY as test infrastructure: the checker for the CUDA
+ * library's parity tests and the timed CPU baseline of bench.py.  Nothing in
+ * the product links, imports or calls this code.
+ *
+ * Parity status: the reference (OCaml + Python 2 + PETSc 2.3.3 + SUNDIALS
+ * CVODE 2.3.0) cannot be built or run here, and the reference tree holds no
+ * golden vectors for this path, so parity is UNPINNED against reference
+ * outputs.  The restatement is pinned instead against known-answer
+ * invariants (uniform-m exchange field, cube demag factor 1/3, BEM row sums,
+ * single-spin LLG solution, SI<->su conversions).
+ *
+ * Every routine cites the reference file:line it restates (paths relative to
+ * the nmag-src project root).
+ */
+#ifndef NMAG_ORACLE_H
+#define NMAG_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct om_mesh {
+  int n_nodes, n_tets;
+  double *coords;        /* 3N, copied */
+  int32_t *tets;         /* 4T, copied */
+  /* node -> tet adjacency, tets ascending (fem.ml:2523-2577 keeps simplices of a site ascending) */
+  int32_t *nt_ptr, *nt_idx;
+  /* per-tet geometry: barycentric gradients dL[t][a][d] and |det| of the point matrix */
+  double *dL, *adet;
+  /* face neighbours: nbr[4t+f] is the tet across the face opposite local vertex f, -1 = outer face */
+  int32_t *nbr;
+  /* scalar P1 CSR pattern (N + 2*edges entries), columns ascending */
+  int nnz;
+  int32_t *row_ptr, *col_idx;
+  double *K;             /* int grad phi_i . grad phi_j                   */
+  double *G[3];          /* int phi_i d_d phi_j                           */
+  double *D[3];          /* G_d minus the outer-surface term (div of m)   */
+  double *vol;           /* box volumes V_i = int phi_i                   */
+  /* boundary ("phi[outer]") short vector, ascending node order */
+  int nb;
+  int32_t *b_of_node, *node_of_b;
+  /* surface triangles in the order the reference's fill loop visits them */
+  int ntri;
+  int32_t *tri;          /* 3*ntri short indices */
+  double *tri_normal;    /* 3*ntri outward unit normals */
+  double *solid_angle;   /* nb interior solid angles */
+  double *bem;           /* nb*nb row-major, filled by om_fill_bem */
+} om_mesh;
+
+/* Build topology, CSR pattern, P1 values, boundary data (no BEM fill). 0 = ok. */
+int om_build(om_mesh *M, int n_nodes, const double *coords, int n_tets, const int32_t *tets);
+/* Lindholm BEM fill (bem3d.ml:938-1047 + bem3d_stubs.c:413-610). */
+int om_fill_bem(om_mesh *M, int nthreads);
+void om_free(om_mesh *M);
+
+/* Reference-shaped CSR export of the six operators (nmag_lam.py:569-606).
+ * which: 0 op_H_exch (3N x 3N), 1 op_div_m (N x 3N), 2 op_neg_laplace_phi (N x N),
+ *        3 op_grad_phi (3N x N), 4 op_laplace_DBC (N x N), 5 op_load_DBC (N x Nb).
+ * Call with NULL arrays to get sizes (rows, nnz); then with arrays. */
+int om_export_operator(const om_mesh *M, int which, double coeff, int *rows, int *cols, int *nnz,
+                       int32_t *row_ptr, int32_t *col_idx, double *vals);
+
+/* Material in simulation units (main.py:347-465). */
+typedef struct om_material {
+  double Ms, exch_coeff;            /* su_Ms, su_exch_prefactor (2A/(mu0 Ms)) */
+  double C1, C2, C3;                /* LLG coefficients as the local equation sees them */
+  double K1, axis[3], anis_coeff;   /* uniaxial anisotropy; anis_coeff = 2 K1/(mu0 Ms) */
+  double E_coeff_half, E_coeff_ext; /* -0.5 Ms mu0 and -1.0 Ms mu0 (energy densities) */
+} om_material;
+
+/* Solver tolerances for the two Poisson solves (nmag_lam.py:614-634). */
+typedef struct om_solver {
+  double rtol, atol; int maxits;
+} om_solver;
+
+typedef struct om_state {
+  const om_mesh *M;
+  om_material mat;
+  om_solver nbc, dbc;
+  int do_demag;
+  double *phi1, *phi2;   /* warm-start state of the two solves, N each */
+  double *h_ext;         /* 3N */
+  /* scratch / outputs of the last evaluation */
+  double *h_exch, *h_demag, *h_anis, *h_total, *rho, *phi, *dmdt;
+  double *tmp_b1, *tmp_b2;
+  int last_iters_nbc, last_iters_dbc;
+  long long n_rhs;
+  int nthreads;
+} om_state;
+
+int om_state_init(om_state *S, const om_mesh *M, const om_material *mat, const om_solver *nbc,
+                  const om_solver *dbc, int do_demag, int nthreads);
+void om_state_free(om_state *S);
+/* Full RHS: H_exch, H_demag (FEM/BEM), H_anis, H_total, dm/dt (nmag_lam.py:734-832). */
+int om_rhs(om_state *S, const double *m, double *dmdt_out);
+/* Energy densities E_exch, E_demag, E_ext, E_anis, E_total (5 x N) from the last fields. */
+int om_energy_density(const om_state *S, const double *m, double *E5);
+/* Matrix-free Jacobian-vector product with frozen (mJ, HJ) (nsim.ml:967-1050, 2315-2417). */
+void om_jv(const om_state *S, const double *mJ, const double *HJ, const double *v, double *out);
+
+/* CVODE-style BDF (orders 1..qmax), Newton + left-preconditioned GMRES. */
+typedef struct om_ts_stats {
+  long long nst, nfe, nni, nli, ncfn, netf, npe, nps, njv, nje;
+  double hcur, tcur; int qcur;
+} om_ts_stats;
+
+typedef struct om_bdf om_bdf;
+om_bdf *om_bdf_create(om_state *S, int qmax, int maxl, double rtol, double atol,
+                      double pc_rtol, double pc_atol);
+void om_bdf_free(om_bdf *B);
+int om_bdf_init(om_bdf *B, double t0, const double *m0);
+/* Advance to tout (CV_NORMAL, interpolated output) or stop exactly at tout (tstop). */
+int om_bdf_advance(om_bdf *B, double tout, int exact_tstop, long long max_steps, double *t_reached,
+                   double *m_out);
+void om_bdf_stats(const om_bdf *B, om_ts_stats *st);
+
+/* Fixed-step RK4 (differentiation form forward). */
+int om_rk4(om_state *S, double *m, double dt, int nsteps);
+
+/* Shape-quality helpers used by tests. */
+double om_triangle_space_angle(const double *obs, const double *p0, const double *p1, const double *p2);
+void om_lindholm_single(const double *p0, const double *p1, const double *p2, const double *normal,
+                        const double *obs, double *lh);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

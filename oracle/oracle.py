@@ -1,0 +1,287 @@
+"""ctypes wrapper of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg as the checker.  The product never imports it.
+
+The oracle restates nsim's LLG right-hand side and CVODE-style integrator on
+the CPU (see nmag_oracle.h for the reference citations).  Parity with the
+reference's own outputs is unpinned (the reference cannot run here and ships
+no golden vectors); known-answer tests pin the restatement instead.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+class OmMesh(C.Structure):
+    _fields_ = [("n_nodes", C.c_int), ("n_tets", C.c_int),
+                ("coords", C.POINTER(C.c_double)), ("tets", C.POINTER(C.c_int32)),
+                ("nt_ptr", C.POINTER(C.c_int32)), ("nt_idx", C.POINTER(C.c_int32)),
+                ("dL", C.POINTER(C.c_double)), ("adet", C.POINTER(C.c_double)),
+                ("nbr", C.POINTER(C.c_int32)),
+                ("nnz", C.c_int), ("row_ptr", C.POINTER(C.c_int32)), ("col_idx", C.POINTER(C.c_int32)),
+                ("K", C.POINTER(C.c_double)), ("G", C.POINTER(C.c_double) * 3), ("D", C.POINTER(C.c_double) * 3),
+                ("vol", C.POINTER(C.c_double)),
+                ("nb", C.c_int), ("b_of_node", C.POINTER(C.c_int32)), ("node_of_b", C.POINTER(C.c_int32)),
+                ("ntri", C.c_int), ("tri", C.POINTER(C.c_int32)), ("tri_normal", C.POINTER(C.c_double)),
+                ("solid_angle", C.POINTER(C.c_double)), ("bem", C.POINTER(C.c_double))]
+
+
+class OmMaterial(C.Structure):
+    _fields_ = [("Ms", C.c_double), ("exch_coeff", C.c_double), ("C1", C.c_double), ("C2", C.c_double),
+                ("C3", C.c_double), ("K1", C.c_double), ("axis", C.c_double * 3), ("anis_coeff", C.c_double),
+                ("E_coeff_half", C.c_double), ("E_coeff_ext", C.c_double)]
+
+
+class OmSolver(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("maxits", C.c_int)]
+
+
+class OmState(C.Structure):
+    _fields_ = [("M", C.POINTER(OmMesh)), ("mat", OmMaterial), ("nbc", OmSolver), ("dbc", OmSolver),
+                ("do_demag", C.c_int),
+                ("phi1", C.POINTER(C.c_double)), ("phi2", C.POINTER(C.c_double)), ("h_ext", C.POINTER(C.c_double)),
+                ("h_exch", C.POINTER(C.c_double)), ("h_demag", C.POINTER(C.c_double)),
+                ("h_anis", C.POINTER(C.c_double)), ("h_total", C.POINTER(C.c_double)),
+                ("rho", C.POINTER(C.c_double)), ("phi", C.POINTER(C.c_double)), ("dmdt", C.POINTER(C.c_double)),
+                ("tmp_b1", C.POINTER(C.c_double)), ("tmp_b2", C.POINTER(C.c_double)),
+                ("last_iters_nbc", C.c_int), ("last_iters_dbc", C.c_int), ("n_rhs", C.c_longlong),
+                ("nthreads", C.c_int)]
+
+
+class OmStats(C.Structure):
+    _fields_ = [(n, C.c_longlong) for n in ("nst", "nfe", "nni", "nli", "ncfn", "netf", "npe", "nps", "njv", "nje")] + \
+               [("hcur", C.c_double), ("tcur", C.c_double), ("qcur", C.c_int)]
+
+
+_lib = None
+
+
+def build(force=False):
+    """Compile the oracle with its Makefile (gcc, OpenMP)."""
+    if force or not os.path.exists(LIB) or any(
+            os.path.getmtime(os.path.join(HERE, f)) > os.path.getmtime(LIB)
+            for f in ("nmag_oracle.c", "nmag_bdf.c", "nmag_oracle.h")):
+        subprocess.check_call(["make", "-s", "-C", HERE])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        L.om_build.argtypes = [C.POINTER(OmMesh), C.c_int, _f64p, C.c_int, _i32p]
+        L.om_fill_bem.argtypes = [C.POINTER(OmMesh), C.c_int]
+        L.om_free.argtypes = [C.POINTER(OmMesh)]
+        L.om_export_operator.argtypes = [C.POINTER(OmMesh), C.c_int, C.c_double, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_void_p,
+                                         C.c_void_p]
+        L.om_state_init.argtypes = [C.POINTER(OmState), C.POINTER(OmMesh), C.POINTER(OmMaterial),
+                                    C.POINTER(OmSolver), C.POINTER(OmSolver), C.c_int, C.c_int]
+        L.om_state_free.argtypes = [C.POINTER(OmState)]
+        L.om_rhs.argtypes = [C.POINTER(OmState), _f64p, C.c_void_p]
+        L.om_energy_density.argtypes = [C.POINTER(OmState), _f64p, _f64p]
+        L.om_jv.argtypes = [C.POINTER(OmState), _f64p, _f64p, _f64p, _f64p]
+        L.om_bdf_create.argtypes = [C.POINTER(OmState), C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                    C.c_double]
+        L.om_bdf_create.restype = C.c_void_p
+        L.om_bdf_free.argtypes = [C.c_void_p]
+        L.om_bdf_init.argtypes = [C.c_void_p, C.c_double, _f64p]
+        L.om_bdf_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_longlong, C.POINTER(C.c_double), _f64p]
+        L.om_bdf_stats.argtypes = [C.c_void_p, C.POINTER(OmStats)]
+        L.om_rk4.argtypes = [C.POINTER(OmState), _f64p, C.c_double, C.c_int]
+        L.om_triangle_space_angle.argtypes = [_f64p, _f64p, _f64p, _f64p]
+        L.om_triangle_space_angle.restype = C.c_double
+        L.om_lindholm_single.argtypes = [_f64p, _f64p, _f64p, _f64p, _f64p, _f64p]
+        _lib = L
+    return _lib
+
+
+def lindholm_single(p0, p1, p2, normal, obs):
+    """Double-layer weights of one triangle for one observer."""
+    f = lambda v: np.ascontiguousarray(v, dtype=np.float64)
+    lh = np.zeros(3)
+    lib().om_lindholm_single(f(p0), f(p1), f(p2), f(normal), f(obs), lh)
+    return lh
+
+
+def solid_angle(obs, p0, p1, p2):
+    f = lambda v: np.ascontiguousarray(v, dtype=np.float64)
+    return lib().om_triangle_space_angle(f(obs), f(p0), f(p1), f(p2))
+
+
+def _arr(ptr, n, dtype):
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+
+class OracleMesh(object):
+    """Topology, CSR and BEM of a tetrahedral mesh, computed by the oracle."""
+
+    def __init__(self, points, simplices, fill_bem=True, nthreads=0):
+        L = lib()
+        self._m = OmMesh()
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1)
+        sim = np.ascontiguousarray(simplices, dtype=np.int32).reshape(-1)
+        st = L.om_build(C.byref(self._m), len(pts) // 3, pts, len(sim) // 4, sim)
+        if st != 0:
+            raise ValueError("oracle mesh build failed (%d)" % st)
+        if fill_bem:
+            L.om_fill_bem(C.byref(self._m), nthreads)
+        m = self._m
+        N, T, nnz, nb = m.n_nodes, m.n_tets, m.nnz, m.nb
+        self.n_nodes, self.n_tets, self.nnz, self.nb, self.ntri = N, T, nnz, nb, m.ntri
+        self.row_ptr = _arr(m.row_ptr, N + 1, np.int32)
+        self.col_idx = _arr(m.col_idx, nnz, np.int32)
+        self.K = _arr(m.K, nnz, np.float64)
+        self.G = np.stack([_arr(m.G[d], nnz, np.float64) for d in range(3)])
+        self.D = np.stack([_arr(m.D[d], nnz, np.float64) for d in range(3)])
+        self.vol = _arr(m.vol, N, np.float64)
+        self.b_of_node = _arr(m.b_of_node, N, np.int32)
+        self.node_of_b = _arr(m.node_of_b, nb, np.int32)
+        self.tri = _arr(m.tri, 3 * m.ntri, np.int32).reshape(-1, 3)
+        self.tri_normal = _arr(m.tri_normal, 3 * m.ntri, np.float64).reshape(-1, 3)
+        self.solid_angle = _arr(m.solid_angle, nb, np.float64)
+        self.nbr = _arr(m.nbr, 4 * T, np.int32).reshape(-1, 4)
+        self.dL = _arr(m.dL, 12 * T, np.float64).reshape(-1, 4, 3)
+        self.adet = _arr(m.adet, T, np.float64)
+        self._filled = fill_bem
+
+    @property
+    def bem(self):
+        """The dense BEM (row-major nb x nb), copied out on first access."""
+        if not self._filled:
+            return None
+        if not hasattr(self, "_bem"):
+            self._bem = _arr(self._m.bem, self.nb * self.nb, np.float64).reshape(self.nb, self.nb)
+        return self._bem
+
+    def export_operator(self, which, coeff=1.0):
+        L = lib()
+        r, c, n = C.c_int(), C.c_int(), C.c_int()
+        L.om_export_operator(C.byref(self._m), which, coeff, C.byref(r), C.byref(c), C.byref(n), None, None, None)
+        rp = np.zeros(r.value + 1, np.int32)
+        ci = np.zeros(n.value, np.int32)
+        va = np.zeros(n.value, np.float64)
+        L.om_export_operator(C.byref(self._m), which, coeff, C.byref(r), C.byref(c), C.byref(n),
+                             rp.ctypes.data, ci.ctypes.data, va.ctypes.data)
+        return rp, ci, va, (r.value, c.value)
+
+    def __del__(self):
+        try:
+            lib().om_free(C.byref(self._m))
+        except Exception:
+            pass
+
+
+class OracleSim(object):
+    """RHS + BDF integration on the oracle for one material."""
+
+    def __init__(self, omesh, coeffs, do_demag=True, nbc=(1e-5, 1e-50, 10000), dbc=(1e-5, 1e-50, 10000),
+                 nthreads=0):
+        L = lib()
+        self.omesh = omesh
+        mat = OmMaterial()
+        mat.Ms = coeffs["Ms"]; mat.exch_coeff = coeffs["exch_coeff"]
+        mat.C1 = coeffs["C1"]; mat.C2 = coeffs["C2"]; mat.C3 = coeffs["C3"]
+        mat.K1 = coeffs.get("K1", 0.0)
+        ax = coeffs.get("axis", (0.0, 0.0, 1.0))
+        for d in range(3):
+            mat.axis[d] = ax[d]
+        mat.anis_coeff = coeffs.get("anis_coeff", 0.0)
+        mat.E_coeff_half = coeffs.get("E_coeff_half", 0.0)
+        mat.E_coeff_ext = coeffs.get("E_coeff_ext", 0.0)
+        self._s = OmState()
+        n1 = OmSolver(nbc[0], nbc[1], int(nbc[2]))
+        n2 = OmSolver(dbc[0], dbc[1], int(dbc[2]))
+        L.om_state_init(C.byref(self._s), C.byref(omesh._m), C.byref(mat), C.byref(n1), C.byref(n2),
+                        int(bool(do_demag)), nthreads)
+        self.N = omesh.n_nodes
+        self._bdf = None
+
+    def set_h_ext(self, h):
+        h = np.broadcast_to(np.asarray(h, dtype=np.float64), (self.N, 3)).reshape(-1)
+        np.ctypeslib.as_array(self._s.h_ext, shape=(3 * self.N,))[:] = h
+
+    def rhs(self, m):
+        m = np.ascontiguousarray(m, dtype=np.float64).reshape(-1)
+        out = np.zeros(3 * self.N)
+        st = lib().om_rhs(C.byref(self._s), m, out.ctypes.data)
+        if st:
+            raise RuntimeError("oracle rhs failed: %d" % st)
+        return out
+
+    def field(self, name):
+        n = self.N
+        ptr = getattr(self._s, {"H_exch": "h_exch", "H_demag": "h_demag", "H_anis": "h_anis",
+                                "H_total": "h_total", "H_ext": "h_ext", "dmdt": "dmdt"}[name])
+        return np.ctypeslib.as_array(ptr, shape=(3 * n,)).copy().reshape(n, 3)
+
+    def scalar_field(self, name):
+        ptr = getattr(self._s, {"phi": "phi", "rho": "rho", "phi1": "phi1", "phi2": "phi2"}[name])
+        return np.ctypeslib.as_array(ptr, shape=(self.N,)).copy()
+
+    @property
+    def iters(self):
+        return self._s.last_iters_nbc, self._s.last_iters_dbc
+
+    def energy_density(self, m):
+        m = np.ascontiguousarray(m, dtype=np.float64).reshape(-1)
+        E = np.zeros(5 * self.N)
+        lib().om_energy_density(C.byref(self._s), m, E)
+        return E.reshape(5, self.N)
+
+    def jv(self, mJ, HJ, v):
+        out = np.zeros(3 * self.N)
+        lib().om_jv(C.byref(self._s), np.ascontiguousarray(mJ, dtype=np.float64).reshape(-1),
+                    np.ascontiguousarray(HJ, dtype=np.float64).reshape(-1),
+                    np.ascontiguousarray(v, dtype=np.float64).reshape(-1), out)
+        return out
+
+    def ts_init(self, m0, t0=0.0, rtol=1e-6, atol=1e-6, max_order=2, krylov_max=300, pc_rtol=1e-2, pc_atol=1e-7):
+        L = lib()
+        if self._bdf:
+            L.om_bdf_free(self._bdf)
+        self._bdf = L.om_bdf_create(C.byref(self._s), max_order, krylov_max, rtol, atol, pc_rtol, pc_atol)
+        st = L.om_bdf_init(self._bdf, t0, np.ascontiguousarray(m0, dtype=np.float64).reshape(-1))
+        if st:
+            raise RuntimeError("oracle ts init failed: %d" % st)
+
+    def ts_advance(self, t, exact_tstop=True, max_steps=-1):
+        out = np.zeros(3 * self.N)
+        tr = C.c_double()
+        st = lib().om_bdf_advance(self._bdf, t, int(bool(exact_tstop)), max_steps, C.byref(tr), out)
+        if st:
+            raise RuntimeError("oracle ts advance failed: %d" % st)
+        return tr.value, out.reshape(self.N, 3)
+
+    def ts_stats(self):
+        s = OmStats()
+        lib().om_bdf_stats(self._bdf, C.byref(s))
+        return {n: getattr(s, n) for n, _ in OmStats._fields_}
+
+    def rk4(self, m, dt, nsteps):
+        m = np.ascontiguousarray(m, dtype=np.float64).reshape(-1).copy()
+        st = lib().om_rk4(C.byref(self._s), m, dt, nsteps)
+        if st:
+            raise RuntimeError("oracle rk4 failed")
+        return m.reshape(self.N, 3)
+
+    def __del__(self):
+        try:
+            if self._bdf:
+                lib().om_bdf_free(self._bdf)
+            lib().om_state_free(C.byref(self._s))
+        except Exception:
+            pass

@@ -1,0 +1,104 @@
+"""Host-side tests (CPU): units, materials, meshes, the C-ABI library's
+exports, and the product's independence from the oracle."""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+import nmag
+from nmag import SI, mesh
+from nmag import _build, _lib
+from conftest import ROOT, permalloy
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "kat.json")))
+
+
+def test_si_parsing_and_units():
+    assert SI(1.0, "m/A s").dims == {"m": 1, "A": -1, "s": -1}
+    assert SI(1.0, "J/m^3").dims == {"kg": 1, "m": -1, "s": -2}
+    assert SI(2.0, "s^(-1)").dims == {"s": -1}
+    su = nmag.simulation_units
+    assert su.of(SI(8.6e5, "A/m")) == pytest.approx(0.86, rel=1e-15)
+    assert su.of(SI(1e-12, "s")) == pytest.approx(1.0, rel=1e-15)
+    assert su.of(SI(1e-9, "m")) == pytest.approx(1.0, rel=1e-15)
+    assert su.of(nmag.si.mu0) == pytest.approx(GOLD["permalloy_alpha05"]["su_mu0"], rel=1e-15)
+    with pytest.raises(ValueError):
+        su.of(SI(1.0, "A/m"), compatible_with=SI("m"))
+
+
+def test_material_coefficients_and_quirks():
+    for key, alpha in (("permalloy_alpha05", 0.5), ("permalloy_alpha002", 0.02)):
+        g = GOLD[key]
+        c = permalloy(alpha).coefficients(None)
+        assert c["C1"] == pytest.approx(g["C1"], rel=1e-14)
+        assert c["C2"] == pytest.approx(g["C2"], rel=1e-14)
+        q = permalloy(alpha).coefficients("nmag")
+        # %g keeps 6 significant digits
+        assert float("%g" % g["C1"]) == q["C1"]
+        assert abs(q["C1"] / g["C1"] - 1) < 5e-6
+    m = nmag.MagMaterial("x", do_precession=False)
+    assert m.coefficients()["C1"] == 0.0
+    with pytest.raises(NotImplementedError):
+        nmag.MagMaterial("stt", llg_polarisation=0.5)
+
+
+@pytest.mark.parametrize("n", [4, 8])
+def test_box_mesh_counts(n):
+    m = mesh.box_mesh(n, n, n, 2.0)
+    g = GOLD["particles"][str(n)]
+    assert m.n_nodes == g["nodes"] and m.n_tets == g["tets"]
+    # every tet positively oriented volume h^3/6
+    p = m.points[m.simplices]
+    det = np.einsum("ij,ij->i", p[:, 1] - p[:, 0], np.cross(p[:, 2] - p[:, 0], p[:, 3] - p[:, 0]))
+    assert np.allclose(np.abs(det), 8.0)
+
+
+def test_nmesh_ascii_round_trip(tmp_path, small_box):
+    fn = str(tmp_path / "box.nmesh")
+    mesh.save_ascii(small_box, fn)
+    back = mesh.load_ascii(fn)
+    assert np.array_equal(back.simplices, small_box.simplices)
+    assert np.array_equal(back.regions, small_box.regions)
+    assert np.array_equal(back.points, small_box.points)
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "nmag_gpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(nmg_\w+)\s*\(", txt, re.M)))
+
+
+def test_exports_list_matches_header():
+    assert sorted(_lib.EXPORTS) == header_symbols()
+
+
+def test_library_builds_and_exports_every_symbol():
+    path = _build.build()
+    import ctypes
+    L = ctypes.CDLL(path)
+    for name in header_symbols():
+        assert hasattr(L, name), name
+    assert L.nmg_version() == 10000
+
+
+def test_create_rejects_bad_input_without_gpu():
+    # argument checks run before any CUDA call
+    L = _lib.lib()
+    import ctypes as C
+    mt = _lib.Material()
+    h = C.c_void_p()
+    pts = np.zeros(12)
+    bad = np.array([0, 1, 2, 7], dtype=np.int32)
+    rc = L.nmg_create(pts, 4, bad, 1, C.byref(mt), None, C.byref(h))
+    assert rc == -3
+    assert b"missing node" in L.nmg_last_error(None)
+
+
+def test_product_does_not_import_oracle():
+    pkg = os.path.join(ROOT, "nmag-src_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".h")):
+                txt = open(os.path.join(dirpath, f)).read()
+                assert "import oracle" not in txt and "liboracle" not in txt, f
