@@ -220,6 +220,7 @@ __global__ void k_values(int N, int nnz, const int32_t *__restrict__ tets, const
     double kc = ad / 6.0, gc = ad / 24.0;
     for (int b = 0; b < 4; ++b) {
       int pos = row_find(col_idx, lo, hi, v[b]);
+      if (pos >= hi || col_idx[pos] != v[b]) continue;  // only after a reported degree overflow
       K[pos] += kc * ((g[3 * a] * g[3 * b] + g[3 * a + 1] * g[3 * b + 1]) + g[3 * a + 2] * g[3 * b + 2]);
       for (int d = 0; d < 3; ++d) G[(size_t)d * nnz + pos] += gc * g[3 * b + d];
     }
@@ -239,6 +240,7 @@ __global__ void k_values(int N, int nnz, const int32_t *__restrict__ tets, const
       for (int b = 0; b < 4; ++b) {
         if (b == f) continue;
         int pos = row_find(col_idx, lo, hi, v[b]);
+        if (pos >= hi || col_idx[pos] != v[b]) continue;
         for (int d = 0; d < 3; ++d) D[(size_t)d * nnz + pos] += (a == b) ? (sf[d] + sf[d]) : sf[d];
       }
     }

@@ -444,6 +444,7 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   a.bar = W.bar; a.err = W.err; a.iters = W.iters;
   a.rtol = rtol; a.atol = atol; a.maxits = maxits;
   void *args[] = {&a};
+  cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);  // fresh barrier state per solve
   cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cg, dim3(W.cg_blocks), dim3(kCGThreads), args, 0,
                                               h->stream);
   return e == cudaSuccess ? 0 : 100;
