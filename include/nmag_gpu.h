@@ -156,6 +156,18 @@ int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps);
 /* Wall-clock split of the last nmg_ts_advance / RHS work, in ms (CUDA events). */
 int nmg_get_timings(const nmg_handle *h, double out[8]);
 
+/* Measurement hooks (no counterpart in the reference; they replace the
+ * TSTART/TSTOP timers of nsim.ml:3414-3455).  While profiling is enabled,
+ * CUDA events bracket every launch of the hot kernels on the handle's stream:
+ * kernel 0 = BEM matrix-vector product, 1 = Neumann CG, 2 = Dirichlet CG,
+ * 3 = fused H_eff + LLG node kernel, 4 = Jacobian-vector + preconditioner.
+ * nmg_profile(h, 1) clears and starts, nmg_profile(h, 0) stops;
+ * nmg_profile_read returns launches and summed device milliseconds.
+ * nmg_launch_count returns the number of kernels this handle has launched. */
+int nmg_profile(nmg_handle *h, int enable);
+int nmg_profile_read(nmg_handle *h, int kernel, int64_t *launches, double *total_ms);
+int64_t nmg_launch_count(const nmg_handle *h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -276,4 +276,52 @@ int nmg_get_timings(const nmg_handle *h, double out[8]) {
   return 0;
 }
 
+int nmg_profile(nmg_handle *h, int enable) {
+  if (!h) return -1;
+  if (enable) {
+    cudaStreamSynchronize(h->stream);
+    h->prof.reset();
+  }
+  h->prof.enabled = enable != 0;
+  return 0;
+}
+
+int nmg_profile_read(nmg_handle *h, int kernel, int64_t *launches, double *total_ms) {
+  if (!h || !launches || !total_ms || kernel < 0 || kernel >= nmg::Profiler::kKernels) return -1;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return 100;
+  int64_t n = 0;
+  double ms = 0.0;
+  for (int k = 0; k < h->prof.used; ++k) {
+    if (h->prof.kernel_of[k] != kernel) continue;
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, h->prof.pool[2 * k], h->prof.pool[2 * k + 1]) == cudaSuccess) {
+      ms += t;
+      ++n;
+    }
+  }
+  *launches = n;
+  *total_ms = ms;
+  return 0;
+}
+
+int64_t nmg_launch_count(const nmg_handle *h) { return h ? h->launches : -1; }
+
 }  // extern "C"
+
+namespace nmg {
+void Profiler::begin(cudaStream_t s, int kernel, int *slot) {
+  *slot = -1;
+  if (used >= kMaxPairs) return;
+  if (pool.empty()) {
+    pool.resize(2 * kMaxPairs);
+    for (auto &e : pool) cudaEventCreate(&e);
+  }
+  kernel_of[used] = kernel;
+  cudaEventRecord(pool[2 * used], s);
+  *slot = used++;
+}
+void Profiler::end(cudaStream_t s, int slot) { cudaEventRecord(pool[2 * slot + 1], s); }
+Profiler::~Profiler() {
+  for (auto &e : pool) cudaEventDestroy(e);
+}
+}  // namespace nmg

@@ -73,6 +73,20 @@ struct Workspace {
 
 struct Integrator;
 
+// CUDA-event brackets around hot-kernel launches (resolved after the run).
+struct Profiler {
+  static constexpr int kKernels = 5;
+  static constexpr int kMaxPairs = 8192;
+  bool enabled = false;
+  std::vector<cudaEvent_t> pool;   // 2 * kMaxPairs events, created lazily
+  int used = 0;
+  int kernel_of[kMaxPairs];
+  void begin(cudaStream_t s, int kernel, int *slot);
+  void end(cudaStream_t s, int slot);
+  void reset() { used = 0; }
+  ~Profiler();
+};
+
 }  // namespace nmg
 
 struct nmg_handle {
@@ -88,8 +102,17 @@ struct nmg_handle {
   double *h_pinned = nullptr;   // small pinned staging buffer for scalars
   int last_iters_nbc = 0, last_iters_dbc = 0;
   int64_t n_rhs = 0;
+  int64_t launches = 0;         // kernels launched by this handle
   double timings[8] = {0};
+  nmg::Profiler prof;
 };
+
+// Bracket one hot-kernel launch with profiler events (no-op when disabled).
+#define NMG_PROF_BEGIN(h, kernel) \
+  int prof_slot__ = -1;           \
+  if ((h)->prof.enabled) (h)->prof.begin((h)->stream, kernel, &prof_slot__)
+#define NMG_PROF_END(h) \
+  if (prof_slot__ >= 0) (h)->prof.end((h)->stream, prof_slot__)
 
 namespace nmg {
 // ---- launchers (mesh_kernels.cu) ----

@@ -311,7 +311,7 @@ struct Integrator {
   ZnPtrs znp() const { ZnPtrs z; for (int j = 0; j < QMAXB + 2; ++j) z.z[j] = zn[j]; return z; }
 
   double wrms(const double *x, const double *w) {
-    k_red<<<kRedBlocks, 256, 0, s()>>>(n, 0, x, w, part);
+    k_red<<<kRedBlocks, 256, 0, s()>>>(n, 0, x, w, part); ++hd->launches;
     cudaMemcpyAsync(hpin, part.p, sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, s());
     if (cudaStreamSynchronize(s()) != cudaSuccess) { status = 100; return 0.0; }
     double acc = 0.0;
@@ -319,7 +319,7 @@ struct Integrator {
     return std::sqrt(acc / n);
   }
   double maxval(const double *x) {
-    k_red<<<kRedBlocks, 256, 0, s()>>>(n, 2, x, x, part);
+    k_red<<<kRedBlocks, 256, 0, s()>>>(n, 2, x, x, part); ++hd->launches;
     cudaMemcpyAsync(hpin, part.p, sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, s());
     if (cudaStreamSynchronize(s()) != cudaSuccess) { status = 100; return 0.0; }
     double mx = 0.0;
@@ -327,7 +327,7 @@ struct Integrator {
     return mx;
   }
   void lin(double a, const double *x, double b, const double *yv, double *z) {
-    k_lin<<<nblk(n, 256), 256, 0, s()>>>(n, a, x, b, yv, z);
+    k_lin<<<nblk(n, 256), 256, 0, s()>>>(n, a, x, b, yv, z); ++hd->launches;
   }
   int rhs(const double *yv, double *f) {
     nfe++;
@@ -335,7 +335,7 @@ struct Integrator {
     if (r) status = r;
     return r;
   }
-  void set_ewt(const double *yv) { k_ewt<<<nblk(n, 256), 256, 0, s()>>>(n, rtol, atol, yv, ewt); }
+  void set_ewt(const double *yv) { k_ewt<<<nblk(n, 256), 256, 0, s()>>>(n, rtol, atol, yv, ewt); ++hd->launches; }
 };
 
 namespace {
@@ -345,7 +345,7 @@ double initial_h(Integrator &I, double tout) {
   double tdist = std::fabs(tout - I.tn);
   double tround = UROUND * std::fmax(std::fabs(I.tn), std::fabs(tout));
   double hlb = 100.0 * tround;
-  k_hub<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.zn[0], I.zn[1], I.ewt, I.tempv);
+  k_hub<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.zn[0], I.zn[1], I.ewt, I.tempv); ++I.hd->launches;
   double hub_inv = I.maxval(I.tempv);
   double hub = 0.1 * tdist;
   if (hub * hub_inv > 1.0) hub = 1.0 / hub_inv;
@@ -401,15 +401,15 @@ void orthogonalise(Integrator &I, int nv, double *w) {
       int cnt = nv - k0 < 32 ? nv - k0 : 32;
       VecPtrs vp;
       for (int k = 0; k < cnt; ++k) vp.v[k] = I.V[k0 + k];
-      k_mdot<<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part);
-      k_mdot_final<<<1, 32, 0, I.s()>>>(kRedBlocks, cnt, I.part, I.hdev.p + k0);
+      k_mdot<<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part); ++I.hd->launches;
+      k_mdot_final<<<1, 32, 0, I.s()>>>(kRedBlocks, cnt, I.part, I.hdev.p + k0); ++I.hd->launches;
     }
     for (int k0 = 0; k0 < nv; k0 += 32) {
       int cnt = nv - k0 < 32 ? nv - k0 : 32;
       VecPtrs vp;
       for (int k = 0; k < cnt; ++k) vp.v[k] = I.V[k0 + k];
-      k_orth<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, cnt, vp, I.hdev.p + k0, w);
-      k_hacc<<<1, 32, 0, I.s()>>>(cnt, I.hdev.p + k0, I.hcol.p + k0, pass == 0);
+      k_orth<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, cnt, vp, I.hdev.p + k0, w); ++I.hd->launches;
+      k_hacc<<<1, 32, 0, I.s()>>>(cnt, I.hdev.p + k0, I.hcol.p + k0, pass == 0); ++I.hd->launches;
     }
   }
 }
@@ -423,11 +423,11 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
   auto HM = [&](int i, int j) -> double & { return I.Hm[(size_t)i * maxl + j]; };
   *nli_out = 0;
   k_psolve<<<nblk(M.N, 128), 128, 0, I.s()>>>(M.N, M.diag_pos, M.K, M.vol, I.mJ, I.HJ, mt.exch_coeff, mt.C1,
-                                              mt.C2, I.gammap, b, I.ewt, I.V[0]);
+                                              mt.C2, I.gammap, b, I.ewt, I.V[0]); ++I.hd->launches;
   I.nps++;
   double rho = 0.0;  // ||V0||_2 (unweighted)
   {
-    k_red<<<kRedBlocks, 256, 0, I.s()>>>(n, 1, I.V[0], I.V[0], I.part);
+    k_red<<<kRedBlocks, 256, 0, I.s()>>>(n, 1, I.V[0], I.V[0], I.part); ++I.hd->launches;
     cudaMemcpyAsync(I.hpin, I.part.p, sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, I.s());
     if (cudaStreamSynchronize(I.s()) != cudaSuccess) return -1;
     double acc = 0.0;
@@ -437,17 +437,21 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
   cudaMemsetAsync(x, 0, sizeof(double) * n, I.s());
   if (rho <= delta) return 0;
   I.beta0 = rho;
-  k_scale<<<nblk(n, 256), 256, 0, I.s()>>>(n, 1.0 / rho, I.V[0]);
+  k_scale<<<nblk(n, 256), 256, 0, I.s()>>>(n, 1.0 / rho, I.V[0]); ++I.hd->launches;
   std::fill(I.yg.begin(), I.yg.end(), 0.0);
   I.yg[0] = rho;
   int converged = 0, kdim = 0;
   for (int l = 0; l < maxl; ++l) {
-    k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewt, I.tvec);
+    k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewt, I.tvec); ++I.hd->launches;
     JvArgs a = jv_args(I, I.tvec, I.V[l + 1], 1);
-    k_jv_psolve<<<nblk(M.N, 128), 128, 0, I.s()>>>(a);
+    {
+      NMG_PROF_BEGIN(I.hd, 4);
+      k_jv_psolve<<<nblk(M.N, 128), 128, 0, I.s()>>>(a); ++I.hd->launches;
+      NMG_PROF_END(I.hd);
+    }
     I.njv++; I.nps++;
     orthogonalise(I, l + 1, I.V[l + 1]);
-    k_red<<<kRedBlocks, 256, 0, I.s()>>>(n, 1, I.V[l + 1], I.V[l + 1], I.part);
+    k_red<<<kRedBlocks, 256, 0, I.s()>>>(n, 1, I.V[l + 1], I.V[l + 1], I.part); ++I.hd->launches;
     cudaMemcpyAsync(I.hpin, I.hcol.p, sizeof(double) * (l + 1), cudaMemcpyDeviceToHost, I.s());
     double *hp2 = I.hpin + maxl + 1;
     cudaMemcpyAsync(hp2, I.part.p, sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, I.s());
@@ -476,7 +480,7 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
     kdim = l + 1;
     if (rho <= delta) { converged = 1; break; }
     if (hn == 0.0) break;
-    k_scale<<<nblk(n, 256), 256, 0, I.s()>>>(n, 1.0 / hn, I.V[l + 1]);
+    k_scale<<<nblk(n, 256), 256, 0, I.s()>>>(n, 1.0 / hn, I.V[l + 1]); ++I.hd->launches;
   }
   *nli_out = kdim;
   for (int k = kdim - 1; k >= 0; --k) {
@@ -490,24 +494,24 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
     for (int k = 0; k < cnt; ++k) vp.v[k] = I.V[k0 + k];
     for (int k = 0; k < cnt; ++k) I.hpin[k] = -I.yg[k0 + k];
     cudaMemcpyAsync(I.hdev.p, I.hpin, sizeof(double) * cnt, cudaMemcpyHostToDevice, I.s());
-    k_orth<<<nblk(n, 256), 256, 0, I.s()>>>(n, cnt, vp, I.hdev, x);  // x -= (-y) V
+    k_orth<<<nblk(n, 256), 256, 0, I.s()>>>(n, cnt, vp, I.hdev, x);  // x -= (-y) V ++I.hd->launches;
     cudaStreamSynchronize(I.s());
   }
-  k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, x, I.ewt, x);
+  k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, x, I.ewt, x); ++I.hd->launches;
   if (converged) return 0;
   return (rho < I.beta0) ? 2 : 1;
 }
 
 void predict(Integrator &I) {
   I.tn += I.h;
-  k_predict<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), 1);
+  k_predict<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), 1); ++I.hd->launches;
 }
 void restore(Integrator &I, double saved_t) {
   I.tn = saved_t;
-  k_predict<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), -1);
+  k_predict<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), -1); ++I.hd->launches;
 }
 void rescale(Integrator &I) {
-  k_rescale<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), I.eta);
+  k_rescale<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), I.eta); ++I.hd->launches;
   I.h = I.hscale * I.eta;
   I.hprime = I.h;
   I.hscale = I.h;
@@ -588,7 +592,7 @@ int nls(Integrator &I, int nflag_first) {
     double delp = 0.0, del;
     for (;;) {
       I.nni++;
-      k_newton_res<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.gamma, I.ftemp, I.rl1, I.zn[1], I.acor, I.tempv);
+      k_newton_res<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.gamma, I.ftemp, I.rl1, I.zn[1], I.acor, I.tempv); ++I.hd->launches;
       double deltar = SPILS_DELT * I.tq[4];
       double bnorm = I.wrms(I.tempv, I.ewt);
       if (I.status) return -4;
@@ -608,7 +612,7 @@ int nls(Integrator &I, int nflag_first) {
         break;
       }
       del = I.wrms(I.tempv, I.ewt);
-      k_newton_upd<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.tempv, I.acor, I.zn[0], I.y);
+      k_newton_upd<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.tempv, I.acor, I.zn[0], I.y); ++I.hd->launches;
       if (m > 0) { double r = del / delp; I.crate = CRDOWN * I.crate > r ? CRDOWN * I.crate : r; }
       double dcon = del * (I.crate < 1.0 ? I.crate : 1.0) / I.tq[4];
       if (dcon <= 1.0) {
@@ -635,7 +639,7 @@ void complete_step(Integrator &I) {
   I.tau[1] = I.h;
   Coef c;
   for (int j = 0; j < QMAXB + 2; ++j) c.c[j] = j <= QMAXB ? I.l[j] : 0.0;
-  k_complete<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), c, I.acor);
+  k_complete<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), c, I.acor); ++I.hd->launches;
   I.qwait--;
   if (I.qwait == 1 && I.q != I.qmax) {
     cudaMemcpyAsync(I.zn[I.qmax], I.acor.p, sizeof(double) * I.n, cudaMemcpyDeviceToDevice, I.s());
@@ -779,7 +783,7 @@ int step(Integrator &I) {
 
 void interpolate(Integrator &I, double t, double *out) {
   double sv = (t - I.tn) / I.h;
-  k_interp<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), sv, out);
+  k_interp<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), sv, out); ++I.hd->launches;
 }
 
 }  // namespace
@@ -846,7 +850,7 @@ int ts_advance(nmg_handle *h, double tout, int exact_tstop, int64_t max_steps, d
     if (I.status) return I.status;
     if (exact_tstop && (I.tn + h0 - tout) * h0 > 0.0) h0 = (tout - I.tn) * (1.0 - 4.0 * UROUND);
     I.h = h0; I.hprime = h0; I.hscale = h0; I.qprime = I.q;
-    k_scale<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, h0, I.zn[1]);
+    k_scale<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, h0, I.zn[1]); ++I.hd->launches;
   }
   int64_t taken = 0;
   double troundoff = 100.0 * UROUND * (std::fabs(I.tn) + std::fabs(I.h));
@@ -893,17 +897,17 @@ int rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps) {
   cudaStream_t s = h->stream;
   for (int st = 0; st < nsteps; ++st) {
     if (rhs_eval(h, d_m, k1)) return 100;
-    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, d_m, 0.5 * dt, k1, y);
+    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, d_m, 0.5 * dt, k1, y); ++h->launches;
     if (rhs_eval(h, y, k2)) return 100;
-    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, d_m, 0.5 * dt, k2, y);
+    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, d_m, 0.5 * dt, k2, y); ++h->launches;
     if (rhs_eval(h, y, k3)) return 100;
-    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, d_m, dt, k3, y);
+    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, d_m, dt, k3, y); ++h->launches;
     if (rhs_eval(h, y, k4)) return 100;
     // m += dt/6 (k1 + 2 k2 + 2 k3 + k4)
-    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, k1, 2.0, k2, y);
-    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, y, 2.0, k3, y);
-    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, y, 1.0, k4, y);
-    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, d_m, dt / 6.0, y, d_m);
+    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, k1, 2.0, k2, y); ++h->launches;
+    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, y, 2.0, k3, y); ++h->launches;
+    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, y, 1.0, k4, y); ++h->launches;
+    k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, d_m, dt / 6.0, y, d_m); ++h->launches;
   }
   return check_device_error(h, "rk4");
 }

@@ -445,8 +445,11 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   a.rtol = rtol; a.atol = atol; a.maxits = maxits;
   void *args[] = {&a};
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);  // fresh barrier state per solve
+  NMG_PROF_BEGIN(h, 1 + mode);
   cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cg, dim3(W.cg_blocks), dim3(kCGThreads), args, 0,
                                               h->stream);
+  NMG_PROF_END(h);
+  ++h->launches;
   return e == cudaSuccess ? 0 : 100;
 }
 
@@ -493,7 +496,7 @@ int init_workspace(nmg_handle *h, std::string &err) {
   NMG_CUDA_TRY(W.iters.alloc(2), "alloc");
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);
   cudaMemsetAsync(W.iters.p, 0, sizeof(int) * 2, h->stream);
-  k_dinv<<<nblk(N, 256), 256, 0, h->stream>>>(N, M.diag_pos, M.K, M.b_of_node, W.dinv_n, W.dinv_d);
+  k_dinv<<<nblk(N, 256), 256, 0, h->stream>>>(N, M.diag_pos, M.K, M.b_of_node, W.dinv_n, W.dinv_d); ++h->launches;
   NMG_CUDA_TRY(cudaGetLastError(), "workspace init");
   NMG_CUDA_TRY(cudaStreamSynchronize(h->stream), "workspace init");
   return 0;
@@ -507,12 +510,16 @@ void bem_gemv(nmg_handle *h, const double *x, double *y) {
   dim3 grid(nblk(nb, kGemvRows), slabs);
   if (h->opt.bem_precision == 1 && M.bem32.p) {
     float *x32 = reinterpret_cast<float *>(W.bpart.p + (size_t)slabs * nb);
-    k_to_f32_vec<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, x, x32);
-    k_gemv_f32<<<grid, kGemvRows, 0, h->stream>>>(nb, slab, M.bem32, x32, W.bpart);
+    k_to_f32_vec<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, x, x32); ++h->launches;
+    NMG_PROF_BEGIN(h, 0);
+    k_gemv_f32<<<grid, kGemvRows, 0, h->stream>>>(nb, slab, M.bem32, x32, W.bpart); ++h->launches;
+    NMG_PROF_END(h);
   } else {
-    k_gemv_f64<<<grid, kGemvRows, 0, h->stream>>>(nb, slab, M.bem, x, W.bpart);
+    NMG_PROF_BEGIN(h, 0);
+    k_gemv_f64<<<grid, kGemvRows, 0, h->stream>>>(nb, slab, M.bem, x, W.bpart); ++h->launches;
+    NMG_PROF_END(h);
   }
-  k_slab_sum<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, slabs, W.bpart, y);
+  k_slab_sum<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, slabs, W.bpart, y); ++h->launches;
 }
 
 int check_device_error(nmg_handle *h, const char *where) {
@@ -541,13 +548,13 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
   const int N = M.N;
   const nmg_material &mt = h->mat;
   if (h->opt.do_demag && M.nb > 0) {
-    k_div<<<nblk(N, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, M.D, d_m, W.rho);
+    k_div<<<nblk(N, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, M.D, d_m, W.rho); ++h->launches;
     if (run_cg(h, 0, W.rho, W.phi1, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
-    k_gather_b<<<nblk(M.nb, 256), 256, 0, s>>>(M.nb, M.node_of_b, W.phi1, W.b1);
+    k_gather_b<<<nblk(M.nb, 256), 256, 0, s>>>(M.nb, M.node_of_b, W.phi1, W.b1); ++h->launches;
     bem_gemv(h, W.b1, W.b2);
-    k_dbc_rhs<<<nblk(N, 256), 256, 0, s>>>(N, M.row_ptr, M.col_idx, M.K, M.b_of_node, W.b2, W.rhs2, W.phi2);
+    k_dbc_rhs<<<nblk(N, 256), 256, 0, s>>>(N, M.row_ptr, M.col_idx, M.K, M.b_of_node, W.b2, W.rhs2, W.phi2); ++h->launches;
     if (run_cg(h, 1, W.rhs2, W.phi2, h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)) return 100;
-    k_add<<<nblk(N, 256), 256, 0, s>>>(N, W.phi1, W.phi2, W.phi);
+    k_add<<<nblk(N, 256), 256, 0, s>>>(N, W.phi1, W.phi2, W.phi); ++h->launches;
   }
   NodeArgs a;
   a.N = N; a.nnz = M.nnz; a.do_demag = (h->opt.do_demag && M.nb > 0) ? 1 : 0;
@@ -557,7 +564,11 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
   a.ax = mt.axis[0]; a.ay = mt.axis[1]; a.az = mt.axis[2];
   a.h_exch = W.h_exch; a.h_demag = W.h_demag; a.h_anis = W.h_anis; a.h_total = W.h_total;
   a.dmdt = d_dmdt ? d_dmdt : W.dmdt.p;
-  k_heff_llg<<<nblk(N, 128), 128, 0, s>>>(a);
+  {
+    NMG_PROF_BEGIN(h, 3);
+    k_heff_llg<<<nblk(N, 128), 128, 0, s>>>(a); ++h->launches;
+    NMG_PROF_END(h);
+  }
   h->n_rhs++;
   return cudaGetLastError() == cudaSuccess ? 0 : 100;
 }
@@ -567,7 +578,7 @@ int energy_density(nmg_handle *h, const double *d_m, double *d_E5) {
   Workspace &W = h->ws;
   const nmg_material &mt = h->mat;
   k_energy<<<nblk(M.N, 256), 256, 0, h->stream>>>(M.N, d_m, W.h_exch, W.h_demag, W.h_ext, mt.E_coeff_half,
-                                                  mt.E_coeff_ext, mt.K1, mt.axis[0], mt.axis[1], mt.axis[2], d_E5);
+                                                  mt.E_coeff_ext, mt.K1, mt.axis[0], mt.axis[1], mt.axis[2], d_E5); ++h->launches;
   return cudaGetLastError() == cudaSuccess ? 0 : 100;
 }
 
@@ -577,7 +588,7 @@ int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5]
   const int nblocks = 64;
   const double *E = energies ? W.E5.p : nullptr;
   if (energies && energy_density(h, d_m, W.E5)) return 100;
-  k_avg_partials<<<nblocks, 256, 0, h->stream>>>(M.N, d_m, M.vol, E, W.red);
+  k_avg_partials<<<nblocks, 256, 0, h->stream>>>(M.N, d_m, M.vol, E, W.red); ++h->launches;
   std::vector<double> part(9 * nblocks);
   if (cudaMemcpyAsync(part.data(), W.red.p, sizeof(double) * 9 * nblocks, cudaMemcpyDeviceToHost, h->stream) ||
       cudaStreamSynchronize(h->stream))
@@ -592,7 +603,7 @@ int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5]
 
 int max_dm(nmg_handle *h, const double *d_m, const double *d_mprev, double *out) {
   const int nblocks = 64;
-  k_maxdm_partials<<<nblocks, 256, 0, h->stream>>>(h->mesh.N, d_m, d_mprev, h->ws.red);
+  k_maxdm_partials<<<nblocks, 256, 0, h->stream>>>(h->mesh.N, d_m, d_mprev, h->ws.red); ++h->launches;
   double part[nblocks];
   if (cudaMemcpyAsync(part, h->ws.red.p, sizeof(double) * nblocks, cudaMemcpyDeviceToHost, h->stream) ||
       cudaStreamSynchronize(h->stream))

@@ -42,7 +42,10 @@ class TsStats(C.Structure):
 EXPORTS = ["nmg_version", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_mesh_info", "nmg_get_csr",
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
            "nmg_set_material", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
-           "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings"]
+           "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
+           "nmg_profile_read", "nmg_launch_count"]
+
+PROFILED_KERNELS = ["bem_gemv", "cg_neumann", "cg_dirichlet", "heff_llg", "jv_psolve"]
 
 _lib = None
 
@@ -90,6 +93,10 @@ def lib(build_if_missing=True):
     L.nmg_rhs_device.argtypes = [vp, vp, vp]
     L.nmg_rk4_device.argtypes = [vp, vp, C.c_double, C.c_int]
     L.nmg_get_timings.argtypes = [vp, _f64p]
+    L.nmg_profile.argtypes = [vp, C.c_int]
+    L.nmg_profile_read.argtypes = [vp, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+    L.nmg_launch_count.argtypes = [vp]
+    L.nmg_launch_count.restype = C.c_int64
     _lib = L
     return L
 
@@ -185,6 +192,21 @@ class Engine(object):
         t = np.zeros(8)
         lib().nmg_get_timings(self.h, t)
         return t
+
+    def profile(self, enable):
+        check(lib().nmg_profile(self.h, int(bool(enable))), self.h, "profile")
+
+    def profile_read(self):
+        """{kernel: (launches, total device ms)} since the last profile(True)."""
+        out = {}
+        for k, name in enumerate(PROFILED_KERNELS):
+            n, ms = C.c_int64(), C.c_double()
+            check(lib().nmg_profile_read(self.h, k, C.byref(n), C.byref(ms)), self.h, "profile_read")
+            out[name] = (n.value, ms.value)
+        return out
+
+    def launch_count(self):
+        return int(lib().nmg_launch_count(self.h))
 
     # ---- inspection (parity tests) ----
     def csr(self):
