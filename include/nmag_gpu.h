@@ -167,6 +167,9 @@ int nmg_get_timings(const nmg_handle *h, double out[8]);
 int nmg_profile(nmg_handle *h, int enable);
 int nmg_profile_read(nmg_handle *h, int kernel, int64_t *launches, double *total_ms);
 int64_t nmg_launch_count(const nmg_handle *h);
+/* Total CG iterations since nmg_create: [Neumann, Dirichlet] (the reference
+ * reports KSP iteration counts through PETSc logging, nsim.ml:2462-2478). */
+int nmg_cg_iterations(const nmg_handle *h, int64_t total[2]);
 
 #ifdef __cplusplus
 }

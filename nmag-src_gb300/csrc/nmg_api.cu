@@ -306,6 +306,15 @@ int nmg_profile_read(nmg_handle *h, int kernel, int64_t *launches, double *total
 
 int64_t nmg_launch_count(const nmg_handle *h) { return h ? h->launches : -1; }
 
+int nmg_cg_iterations(const nmg_handle *h, int64_t total[2]) {
+  if (!h || !total) return -1;
+  int it[4] = {0, 0, 0, 0};
+  if (d2h(h, it, h->ws.iters.p, sizeof(it))) return 100;
+  total[0] = it[2];
+  total[1] = it[3];
+  return 0;
+}
+
 }  // extern "C"
 
 namespace nmg {

@@ -207,6 +207,7 @@ __global__ void __launch_bounds__(kCGThreads) k_cg(CGArgs a) {
   }
   if (tid == 0) {
     a.iters[a.mode] = it;
+    a.iters[2 + a.mode] += it;   // cumulative per solve kind
     if (failed) atomicOr(a.err, (rr == rr) ? ERR_CG_MAXITS : ERR_NONFINITE);
   }
 }
@@ -493,9 +494,9 @@ int init_workspace(nmg_handle *h, std::string &err) {
   size_t red_n = 9 * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);
   NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
   NMG_CUDA_TRY(W.bar.alloc(2), "alloc barrier");
-  NMG_CUDA_TRY(W.iters.alloc(2), "alloc");
+  NMG_CUDA_TRY(W.iters.alloc(4), "alloc");
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);
-  cudaMemsetAsync(W.iters.p, 0, sizeof(int) * 2, h->stream);
+  cudaMemsetAsync(W.iters.p, 0, sizeof(int) * 4, h->stream);
   k_dinv<<<nblk(N, 256), 256, 0, h->stream>>>(N, M.diag_pos, M.K, M.b_of_node, W.dinv_n, W.dinv_d); ++h->launches;
   NMG_CUDA_TRY(cudaGetLastError(), "workspace init");
   NMG_CUDA_TRY(cudaStreamSynchronize(h->stream), "workspace init");
