@@ -63,8 +63,8 @@ struct Mesh {
 
 struct Workspace {
   DevBuf<double> m, h_ext, h_exch, h_demag, h_anis, h_total, dmdt, rho, phi1, phi2, phi, rhs2;
-  DevBuf<double> b1, b2, bpart, cg_r, cg_z, cg_p, cg_q, dinv_n, dinv_d, red, E5;
-  DevBuf<unsigned> bar;     // grid barrier {count, generation}
+  DevBuf<double> b1, b2, bpart, cg_r, cg_z, cg_p, cg_q, cg_w, cg_tot, dinv_n, dinv_d, red, E5;
+  DevBuf<unsigned> bar;     // grid barrier words: per-block arrival epochs + release epoch
   DevBuf<int> err;          // device error flags
   DevBuf<int> iters;        // CG iterations written by the persistent kernel
   int cg_blocks = 0;

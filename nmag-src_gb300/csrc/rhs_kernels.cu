@@ -101,6 +101,9 @@ struct CGArgs {
   int *err, *iters;
   double rtol, atol;
   int maxits;
+  double *w;          // A u (single-reduction CG)
+  unsigned *flags;    // per-block arrival epochs (reduce-barrier)
+  double *tot;        // reduced totals, double-buffered by epoch parity
 };
 
 __device__ __forceinline__ double row_apply(const CGArgs &a, int i, const double *__restrict__ v) {
@@ -209,6 +212,149 @@ __global__ void __launch_bounds__(kCGThreads) k_cg(CGArgs a) {
     a.iters[a.mode] = it;
     a.iters[2 + a.mode] += it;   // cumulative per solve kind
     if (failed) atomicOr(a.err, (rr == rr) ? ERR_CG_MAXITS : ERR_NONFINITE);
+  }
+}
+
+// ---- single-reduction CG with a flag-based reduce-barrier ----
+//
+// Every block publishes its partial sums and then its arrival epoch in its own
+// flag word; block 0 waits for all flags (one poller thread per block),
+// reduces the partials in block order (deterministic) and publishes the
+// totals plus a release epoch; every block waits for the release.  No atomics
+// on a shared counter, and the reduction travels with the barrier.  All waits
+// are bounded: on timeout the kernel records ERR_BARRIER and every block exits.
+constexpr int kCG2MaxRed = 4;
+
+template <int NV>
+__device__ __forceinline__ bool reduce_barrier(const CGArgs &a, unsigned epoch, double (&v)[NV], double *smem,
+                                               double (&out)[NV]) {
+  block_sum<NV>(v, smem);
+  const unsigned nblocks = gridDim.x;
+  volatile unsigned *vflags = a.flags;
+  volatile unsigned *vrelease = a.flags + nblocks;
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < NV; ++j) a.red[blockIdx.x * kCG2MaxRed + j] = v[j];
+    __threadfence();
+    vflags[blockIdx.x] = epoch;
+  }
+  if (blockIdx.x == 0) {
+    double acc[NV];
+    for (int j = 0; j < NV; ++j) acc[j] = 0.0;
+    for (unsigned b = threadIdx.x; b < nblocks; b += blockDim.x) {
+      unsigned long long spins = 0;
+      while (vflags[b] != epoch) {
+        if (++spins > kBarrierSpinLimit || (*(volatile int *)a.err & ERR_BARRIER)) { atomicOr(a.err, ERR_BARRIER); break; }
+      }
+      __threadfence();
+      for (int j = 0; j < NV; ++j) acc[j] += ((volatile double *)a.red)[b * kCG2MaxRed + j];
+    }
+    block_sum<NV>(acc, smem);
+    if (threadIdx.x == 0) {
+      for (int j = 0; j < NV; ++j) a.tot[(epoch & 1) * kCG2MaxRed + j] = acc[j];
+      __threadfence();
+      *vrelease = epoch;
+    }
+  }
+  if (threadIdx.x == 0) {
+    unsigned long long spins = 0;
+    while (*vrelease != epoch) {
+      if (++spins > kBarrierSpinLimit || (*(volatile int *)a.err & ERR_BARRIER)) { atomicOr(a.err, ERR_BARRIER); break; }
+      __nanosleep(20);
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  for (int j = 0; j < NV; ++j) out[j] = ((volatile double *)a.tot)[(epoch & 1) * kCG2MaxRed + j];
+  const bool ok = !(*(volatile int *)a.err & ERR_BARRIER);
+  __syncthreads();
+  return ok;
+}
+
+// Row of A applied to v, reading v through L2 only (v is rewritten by other
+// blocks between barriers; L1 is not coherent across SMs).
+__device__ __forceinline__ double row_apply_cg(const CGArgs &a, int i, const double *v) {
+  if (a.mode == 1 && a.b_of_node[i] >= 0) return __ldcg(v + i);
+  double s = 0.0;
+  const int lo = a.row_ptr[i], hi = a.row_ptr[i + 1];
+  for (int k = lo; k < hi; ++k) {
+    int j = a.col_idx[k];
+    if (a.mode == 1 && a.b_of_node[j] >= 0) continue;
+    s += a.K[k] * __ldcg(v + j);
+  }
+  return s;
+}
+
+// Jacobi-preconditioned CG in the single-reduction (Chronopoulos-Gear) form:
+// one reduction of (r,u), (w,u), (r,r) and two barriers per iteration.  Same
+// stopping rule as k_cg: ||r||_2 <= max(rtol ||b - mean||_2, atol).
+__global__ void __launch_bounds__(kCGThreads) k_cg2(CGArgs a) {
+  __shared__ double smem[32 * kCG2MaxRed];
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  unsigned epoch = 0;
+  double mean_b = 0.0;
+  if (a.mode == 0) {
+    double v[1] = {0.0}, t[1];
+    for (int i = tid; i < a.N; i += stride) v[0] += a.b[i];
+    if (!reduce_barrier<1>(a, ++epoch, v, smem, t)) return;
+    mean_b = t[0] / a.N;
+  }
+  double bb_loc = 0.0;
+  for (int i = tid; i < a.N; i += stride) {
+    const double bi = a.b[i] - mean_b;
+    const double ri = bi - row_apply(a, i, a.x);
+    a.r[i] = ri;
+    a.z[i] = a.dinv[i] * ri;   // u
+    bb_loc += bi * bi;
+  }
+  double tol = 0.0, gamma = 0.0, alpha = 0.0, beta = 0.0;
+  int it = 0;
+  bool failed = false;
+  {
+    double v[1] = {bb_loc}, t[1];
+    if (!reduce_barrier<1>(a, ++epoch, v, smem, t)) return;   // also publishes u
+    tol = fmax(a.rtol * sqrt(t[0]), a.atol);
+  }
+  for (;;) {
+    // w = A u ; (r,u), (w,u), (r,r)
+    double v[3] = {0.0, 0.0, 0.0}, t[3];
+    for (int i = tid; i < a.N; i += stride) {
+      const double wi = row_apply_cg(a, i, a.z);
+      const double ui = a.z[i], ri = a.r[i];
+      a.w[i] = wi;
+      v[0] += ri * ui; v[1] += wi * ui; v[2] += ri * ri;
+    }
+    if (!reduce_barrier<3>(a, ++epoch, v, smem, t)) return;
+    if (!(t[2] == t[2]) || isinf(t[2])) { failed = true; break; }
+    if (sqrt(t[2]) <= tol) break;
+    if (it >= a.maxits) { failed = true; break; }
+    const double gamma_new = t[0], delta = t[1];
+    if (it == 0) { beta = 0.0; alpha = gamma_new / delta; }
+    else { beta = gamma_new / gamma; alpha = gamma_new / (delta - beta * gamma_new / alpha); }
+    gamma = gamma_new;
+    for (int i = tid; i < a.N; i += stride) {
+      const double pi = a.z[i] + beta * (it ? a.p[i] : 0.0);
+      const double si = a.w[i] + beta * (it ? a.q[i] : 0.0);
+      a.p[i] = pi; a.q[i] = si;
+      a.x[i] += alpha * pi;
+      const double ri = a.r[i] - alpha * si;
+      a.r[i] = ri;
+      a.z[i] = a.dinv[i] * ri;
+    }
+    ++it;
+    double d[1] = {0.0}, dd[1];
+    if (!reduce_barrier<1>(a, ++epoch, d, smem, dd)) return;   // publishes the new u
+  }
+  if (a.mode == 0) {  // remove the constant component of the solution
+    double v[1] = {0.0}, t[1];
+    for (int i = tid; i < a.N; i += stride) v[0] += a.x[i];
+    if (!reduce_barrier<1>(a, ++epoch, v, smem, t)) return;
+    const double mx = t[0] / a.N;
+    for (int i = tid; i < a.N; i += stride) a.x[i] -= mx;
+  }
+  if (tid == 0) {
+    a.iters[a.mode] = it;
+    a.iters[2 + a.mode] += it;
+    if (failed) atomicOr(a.err, ERR_CG_MAXITS);
   }
 }
 
@@ -442,12 +588,14 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.b_of_node = M.b_of_node; a.K = M.K;
   a.dinv = mode == 0 ? W.dinv_n.p : W.dinv_d.p;
   a.b = b; a.x = x; a.r = W.cg_r; a.z = W.cg_z; a.p = W.cg_p; a.q = W.cg_q; a.red = W.red;
+  a.w = W.cg_w; a.flags = W.bar; a.tot = W.cg_tot;
   a.bar = W.bar; a.err = W.err; a.iters = W.iters;
   a.rtol = rtol; a.atol = atol; a.maxits = maxits;
   void *args[] = {&a};
-  cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);  // fresh barrier state per solve
+  // fresh barrier words per solve: epochs restart at 1 inside the kernel
+  cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
   NMG_PROF_BEGIN(h, 1 + mode);
-  cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cg, dim3(W.cg_blocks), dim3(kCGThreads), args, 0,
+  cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cg2, dim3(W.cg_blocks), dim3(kCGThreads), args, 0,
                                               h->stream);
   NMG_PROF_END(h);
   ++h->launches;
@@ -478,7 +626,7 @@ int init_workspace(nmg_handle *h, std::string &err) {
     cudaMemsetAsync(b->p, 0, sizeof(double) * n3, h->stream);
   // CG grid: one row per thread when it fits in one co-resident wave.
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg, kCGThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg2, kCGThreads, 0);
   int max_blocks = per_sm * h->sm_count;
   int want = nblk(N, kCGThreads);
   W.cg_blocks = want < max_blocks ? want : max_blocks;
@@ -493,7 +641,9 @@ int init_workspace(nmg_handle *h, std::string &err) {
   NMG_CUDA_TRY(W.bpart.alloc((size_t)slabs * (nb > 0 ? nb : 1) + (size_t)nb), "alloc gemv partials");
   size_t red_n = 9 * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);
   NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
-  NMG_CUDA_TRY(W.bar.alloc(2), "alloc barrier");
+  NMG_CUDA_TRY(W.bar.alloc(W.cg_blocks + 2), "alloc barrier");
+  NMG_CUDA_TRY(W.cg_w.alloc(N), "alloc");
+  NMG_CUDA_TRY(W.cg_tot.alloc(2 * 4), "alloc");
   NMG_CUDA_TRY(W.iters.alloc(4), "alloc");
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);
   cudaMemsetAsync(W.iters.p, 0, sizeof(int) * 4, h->stream);
