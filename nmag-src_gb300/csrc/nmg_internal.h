@@ -68,6 +68,8 @@ struct Workspace {
   DevBuf<int> err;          // device error flags
   DevBuf<int> iters;        // CG iterations written by the persistent kernel
   int cg_blocks = 0;
+  int cg_smem_bytes = 0;     // >0: shared-memory CG (one row per thread)
+  int cg_nnz_cap = 0;
   int gemv_slabs = 1;
 };
 

@@ -358,6 +358,115 @@ __global__ void __launch_bounds__(kCGThreads) k_cg2(CGArgs a) {
   }
 }
 
+// The same single-reduction CG with one row per thread and the block's CSR
+// rows (values with Dirichlet-masked columns zeroed, column indices) staged in
+// shared memory once per solve; each iteration then only gathers the
+// neighbours' u from L2, all loads of a row issued together.
+struct CGSmemLayout {
+  int nnz_cap;  // entries per block
+};
+
+__global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap) {
+  extern __shared__ double dyn[];
+  __shared__ double smem[32 * kCG2MaxRed];
+  double *sK = dyn;
+  int *sC = reinterpret_cast<int *>(sK + nnz_cap);
+  const int row0 = blockIdx.x * blockDim.x;
+  const int i = row0 + threadIdx.x;
+  const bool active = i < a.N;
+  const int base = a.row_ptr[row0];
+  const int rend = a.row_ptr[min(row0 + (int)blockDim.x, a.N)];
+  for (int k = base + threadIdx.x; k < rend; k += blockDim.x) {
+    const int j = a.col_idx[k];
+    sC[k - base] = j;
+    sK[k - base] = (a.mode == 1 && a.b_of_node[j] >= 0) ? 0.0 : a.K[k];
+  }
+  int lo = 0, hi = 0;
+  bool ident = false;
+  double dinv = 1.0, xi = 0.0;
+  if (active) {
+    lo = a.row_ptr[i] - base;
+    hi = a.row_ptr[i + 1] - base;
+    ident = a.mode == 1 && a.b_of_node[i] >= 0;
+    dinv = a.dinv[i];
+    xi = a.x[i];
+  }
+  __syncthreads();
+  auto apply = [&](const double *v) -> double {
+    if (ident) return __ldcg(v + i);
+    double s = 0.0;
+    int k = lo;
+    for (; k + 4 <= hi; k += 4) {
+      const double v0 = __ldcg(v + sC[k]), v1 = __ldcg(v + sC[k + 1]), v2 = __ldcg(v + sC[k + 2]),
+                   v3 = __ldcg(v + sC[k + 3]);
+      s += sK[k] * v0; s += sK[k + 1] * v1; s += sK[k + 2] * v2; s += sK[k + 3] * v3;
+    }
+    for (; k < hi; ++k) s += sK[k] * __ldcg(v + sC[k]);
+    return s;
+  };
+  unsigned epoch = 0;
+  double mean_b = 0.0;
+  const double bi0 = active ? a.b[i] : 0.0;
+  if (a.mode == 0) {
+    double v[1] = {bi0}, t[1];
+    if (!reduce_barrier<1>(a, ++epoch, v, smem, t)) return;
+    mean_b = t[0] / a.N;
+  }
+  double ri = 0.0, ui = 0.0, pi = 0.0, si = 0.0, wi = 0.0, bb_loc = 0.0;
+  if (active) {
+    const double bi = bi0 - mean_b;
+    ri = bi - apply(a.x);
+    ui = dinv * ri;
+    a.z[i] = ui;
+    bb_loc = bi * bi;
+  }
+  double tol, gamma = 0.0, alpha = 0.0, beta = 0.0;
+  int it = 0;
+  bool failed = false;
+  {
+    double v[1] = {bb_loc}, t[1];
+    if (!reduce_barrier<1>(a, ++epoch, v, smem, t)) return;
+    tol = fmax(a.rtol * sqrt(t[0]), a.atol);
+  }
+  for (;;) {
+    double v[3] = {0.0, 0.0, 0.0}, t[3];
+    if (active) {
+      wi = apply(a.z);
+      v[0] = ri * ui; v[1] = wi * ui; v[2] = ri * ri;
+    }
+    if (!reduce_barrier<3>(a, ++epoch, v, smem, t)) return;
+    if (!(t[2] == t[2]) || isinf(t[2])) { failed = true; break; }
+    if (sqrt(t[2]) <= tol) break;
+    if (it >= a.maxits) { failed = true; break; }
+    const double gamma_new = t[0], delta = t[1];
+    if (it == 0) { beta = 0.0; alpha = gamma_new / delta; }
+    else { beta = gamma_new / gamma; alpha = gamma_new / (delta - beta * gamma_new / alpha); }
+    gamma = gamma_new;
+    if (active) {
+      pi = ui + beta * pi;
+      si = wi + beta * si;
+      xi += alpha * pi;
+      ri -= alpha * si;
+      ui = dinv * ri;
+      a.z[i] = ui;
+    }
+    ++it;
+    double d[1] = {0.0}, dd[1];
+    if (!reduce_barrier<1>(a, ++epoch, d, smem, dd)) return;
+  }
+  if (a.mode == 0) {
+    double v[1] = {active ? xi : 0.0}, t[1];
+    if (!reduce_barrier<1>(a, ++epoch, v, smem, t)) return;
+    xi -= t[0] / a.N;
+  }
+  if (active) a.x[i] = xi;
+  if (i == 0) {
+    a.iters[a.mode] = it;
+    a.iters[2 + a.mode] += it;
+    if (failed) atomicOr(a.err, ERR_CG_MAXITS);
+  }
+}
+
 __global__ void k_dinv(int N, const int32_t *__restrict__ diag_pos, const double *__restrict__ K,
                        const int32_t *__restrict__ b_of_node, double *__restrict__ dn, double *__restrict__ dd) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -595,8 +704,15 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   // fresh barrier words per solve: epochs restart at 1 inside the kernel
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
   NMG_PROF_BEGIN(h, 1 + mode);
-  cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cg2, dim3(W.cg_blocks), dim3(kCGThreads), args, 0,
-                                              h->stream);
+  cudaError_t e;
+  if (W.cg_smem_bytes > 0) {
+    int cap = W.cg_nnz_cap;
+    void *args3[] = {&a, &cap};
+    e = cudaLaunchCooperativeKernel((const void *)k_cg3, dim3(W.cg_blocks), dim3(kCGThreads), args3,
+                                    (size_t)W.cg_smem_bytes, h->stream);
+  } else {
+    e = cudaLaunchCooperativeKernel((const void *)k_cg2, dim3(W.cg_blocks), dim3(kCGThreads), args, 0, h->stream);
+  }
   NMG_PROF_END(h);
   ++h->launches;
   return e == cudaSuccess ? 0 : 100;
@@ -631,6 +747,30 @@ int init_workspace(nmg_handle *h, std::string &err) {
   int want = nblk(N, kCGThreads);
   W.cg_blocks = want < max_blocks ? want : max_blocks;
   if (W.cg_blocks < 1) W.cg_blocks = 1;
+  // Shared-memory CG: one row per thread, each block's CSR rows resident.
+  {
+    std::vector<int32_t> rp(N + 1);
+    NMG_CUDA_TRY(cudaMemcpy(rp.data(), M.row_ptr.p, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost), "d2h");
+    int cap = 0;
+    for (int r0 = 0; r0 < N; r0 += kCGThreads) {
+      int r1 = r0 + kCGThreads < N ? r0 + kCGThreads : N;
+      cap = rp[r1] - rp[r0] > cap ? rp[r1] - rp[r0] : cap;
+    }
+    cap = (cap + 1) & ~1;
+    const int bytes = cap * (int)(sizeof(double) + sizeof(int));
+    W.cg_smem_bytes = 0;
+    W.cg_nnz_cap = cap;
+    if (bytes <= 160 * 1024 &&
+        cudaFuncSetAttribute(k_cg3, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess) {
+      int per3 = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per3, k_cg3, kCGThreads, bytes);
+      if (per3 > 0 && want <= per3 * h->sm_count) {
+        W.cg_smem_bytes = bytes;
+        W.cg_blocks = want;
+      }
+    }
+    cudaGetLastError();
+  }
   // GEMV slabs: about 4 blocks per SM in total.
   int row_tiles = nblk(nb, kGemvRows);
   int slabs = row_tiles > 0 ? (4 * h->sm_count + row_tiles - 1) / row_tiles : 1;
