@@ -715,7 +715,11 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   }
   NMG_PROF_END(h);
   ++h->launches;
-  return e == cudaSuccess ? 0 : 100;
+  if (e != cudaSuccess) {
+    h->last_error = std::string("CG launch failed: ") + cudaGetErrorString(e);
+    return 100;
+  }
+  return 0;
 }
 
 }  // namespace
@@ -760,8 +764,10 @@ int init_workspace(nmg_handle *h, std::string &err) {
     const int bytes = cap * (int)(sizeof(double) + sizeof(int));
     W.cg_smem_bytes = 0;
     W.cg_nnz_cap = cap;
+    // The attribute is per function (shared by every handle): always raise it
+    // to the cap so that handles with different meshes do not undercut it.
     if (bytes <= 160 * 1024 &&
-        cudaFuncSetAttribute(k_cg3, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) == cudaSuccess) {
+        cudaFuncSetAttribute(k_cg3, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) == cudaSuccess) {
       int per3 = 0;
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per3, k_cg3, kCGThreads, bytes);
       if (per3 > 0 && want <= per3 * h->sm_count) {
