@@ -225,43 +225,49 @@ __global__ void __launch_bounds__(kCGThreads) k_cg(CGArgs a) {
 // are bounded: on timeout the kernel records ERR_BARRIER and every block exits.
 constexpr int kCG2MaxRed = 4;
 
+// gpu-scope release store / acquire load (the block's other threads are
+// ordered before the release through the preceding __syncthreads).
+__device__ __forceinline__ void st_release_gpu(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 template <int NV>
 __device__ __forceinline__ bool reduce_barrier(const CGArgs &a, unsigned epoch, double (&v)[NV], double *smem,
                                                double (&out)[NV]) {
-  block_sum<NV>(v, smem);
+  block_sum<NV>(v, smem);  // ends with __syncthreads: the block's writes precede thread 0's release
   const unsigned nblocks = gridDim.x;
-  volatile unsigned *vflags = a.flags;
-  volatile unsigned *vrelease = a.flags + nblocks;
+  unsigned *flags = a.flags;
+  unsigned *release = a.flags + nblocks;
   if (threadIdx.x == 0) {
     for (int j = 0; j < NV; ++j) a.red[blockIdx.x * kCG2MaxRed + j] = v[j];
-    __threadfence();
-    vflags[blockIdx.x] = epoch;
+    st_release_gpu(flags + blockIdx.x, epoch);
   }
   if (blockIdx.x == 0) {
     double acc[NV];
     for (int j = 0; j < NV; ++j) acc[j] = 0.0;
     for (unsigned b = threadIdx.x; b < nblocks; b += blockDim.x) {
       unsigned long long spins = 0;
-      while (vflags[b] != epoch) {
+      while (ld_acquire_gpu(flags + b) != epoch) {
         if (++spins > kBarrierSpinLimit || (*(volatile int *)a.err & ERR_BARRIER)) { atomicOr(a.err, ERR_BARRIER); break; }
       }
-      __threadfence();
-      for (int j = 0; j < NV; ++j) acc[j] += ((volatile double *)a.red)[b * kCG2MaxRed + j];
+      for (int j = 0; j < NV; ++j) acc[j] += __ldcg(a.red + b * kCG2MaxRed + j);
     }
     block_sum<NV>(acc, smem);
     if (threadIdx.x == 0) {
       for (int j = 0; j < NV; ++j) a.tot[(epoch & 1) * kCG2MaxRed + j] = acc[j];
-      __threadfence();
-      *vrelease = epoch;
+      st_release_gpu(release, epoch);
     }
   }
   if (threadIdx.x == 0) {
     unsigned long long spins = 0;
-    while (*vrelease != epoch) {
+    while (ld_acquire_gpu(release) != epoch) {
       if (++spins > kBarrierSpinLimit || (*(volatile int *)a.err & ERR_BARRIER)) { atomicOr(a.err, ERR_BARRIER); break; }
-      __nanosleep(20);
     }
-    __threadfence();
   }
   __syncthreads();
   for (int j = 0; j < NV; ++j) out[j] = ((volatile double *)a.tot)[(epoch & 1) * kCG2MaxRed + j];
