@@ -45,6 +45,8 @@ def workload(name):
         return mesh.film_mesh(), (1.0, 0.25, 0.1), 1
     if name == "cube":
         return mesh.cube_mesh(), (1.0, 1.0, 1.0), 0
+    if name == "film_small":
+        return mesh.box_mesh(100, 40, 2, 2.5, 2.5, 1.5), (1.0, 0.25, 0.1), 1
     raise ValueError(name)
 
 
@@ -146,14 +148,21 @@ def barrier(world):
 
 
 def cpu_reference_run(args, msh, base, seed, steps, warmup, max_wall=25.0, sample_ps=None):
-    """Time the oracle (CPU restatement, all host threads) on the workload."""
+    """Time the oracle (CPU restatement, all host threads) on the workload:
+    the same relax stage (alpha = 1, no field, RELAX_PS), then the timed
+    alpha = 0.02 dynamics under H_ext."""
     import oracle
     t0 = time.perf_counter()
     om = oracle.OracleMesh(msh.points, msh.simplices, nthreads=0)
-    mat = material(0.02)
-    s = oracle.OracleSim(om, mat.coefficients("nmag"))
+    m = initial_m(msh.n_nodes, base, seed)
+    if args.relax_ps > 0:
+        r = oracle.OracleSim(om, material(1.0).coefficients("nmag"))
+        r.ts_init(m, rtol=1e-6, atol=1e-6)
+        _, m = r.ts_advance(args.relax_ps)
+        del r
+    s = oracle.OracleSim(om, material(0.02).coefficients("nmag"))
     s.set_h_ext(h_ext_su())
-    s.ts_init(initial_m(msh.n_nodes, base, seed), rtol=1e-6, atol=1e-6)
+    s.ts_init(m, rtol=1e-6, atol=1e-6)
     setup = time.perf_counter() - t0
     t = 0.0
     dt = sample_ps or args.step_ps
@@ -201,9 +210,16 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+WORKLOAD_NAMES = {
+    "film": "film 500x125x3 nm, 30753 nodes, 21002 boundary nodes, alpha 0.02, H_ext (-24.6,4.3,0) mT",
+    "cube": "cube 30 nm, 1331 nodes, 602 boundary nodes",
+    "film_small": "film 250x100x3 nm (profiling size), 12423 nodes, 8562 boundary nodes, alpha 0.02",
+}
+
+
 def config_dict(args, msh):
-    return {"workload": "film 500x125x3 nm, 30753 nodes, 21002 boundary nodes, alpha 0.02, H_ext (-24.6,4.3,0) mT"
-            if args.workload == "film" else "cube 30 nm, 1331 nodes, 602 boundary nodes",
+    return {"workload": WORKLOAD_NAMES[args.workload],
+            "relax": "alpha=1, H_ext=0 for %.3g ps before the timed dynamics (untimed)" % args.relax_ps,
             "nodes": int(msh.n_nodes), "tets": int(msh.n_tets), "step": "%.3g ps advance + <m> read" % args.step_ps,
             "form": args.form, "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
             "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % (8 if args.form == "fp64" else 4)}
@@ -223,6 +239,14 @@ def run_ours(args):
     eng = sim.engine
     m0 = initial_m(msh.n_nodes, base, seed)
     sim.set_m(m0)
+    relax_wall = 0.0
+    if args.relax_ps > 0:   # relax stage: alpha = 1, no applied field
+        w = time.perf_counter()
+        sim.set_damping(1.0)
+        sim.reinitialise(initial_time=0)
+        sim.advance_time(SI(args.relax_ps * 1e-12, "s"))
+        sim.set_damping(0.02)
+        relax_wall = time.perf_counter() - w
     sim.set_H_ext(h_ext_su() * 1e6, SI(1.0, "A/m"))
     sim.reinitialise(initial_time=0)
     ps = args.step_ps
@@ -235,6 +259,7 @@ def run_ours(args):
     sampler.start()
     eng.profile(True)
     launches0 = eng.launch_count()
+    cg0 = eng.cg_iterations()
     _, st0 = eng.ts_advance(t)   # no-op advance to read the counters
     torch.cuda.synchronize()
     barrier(world)
@@ -251,6 +276,7 @@ def run_ours(args):
     wall_value = time.perf_counter() - w0
     barrier(world)
     launches = eng.launch_count() - launches0
+    cg1 = eng.cg_iterations()
     eng.profile(False)
     prof = eng.profile_read()
     clocks = sampler.stop()
@@ -298,6 +324,8 @@ def run_ours(args):
         "wall_value_s": wall_value,
         "roofline": roof,
         "kernels_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
+        "cg_iterations": {"neumann": cg1[0] - cg0[0], "dirichlet": cg1[1] - cg0[1]},
+        "relax_wall_s": relax_wall,
         "e2e": {"value": e2e_value, "unit": "ns/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": msh.n_nodes * 3 * 8 + 24,
                 "call": "nmag.Simulation.advance_time + get_subfield_average_siv('m')"},
@@ -322,8 +350,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--workload", default="film", choices=["film", "cube"])
+    ap.add_argument("--workload", default="film", choices=["film", "cube", "film_small"])
     ap.add_argument("--step-ps", type=float, default=1.0)
+    ap.add_argument("--relax-ps", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
