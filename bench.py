@@ -38,6 +38,12 @@ for _p in (os.path.join(ROOT, "nmag-src_gb300"), os.path.join(ROOT, "oracle")):
 MU0 = 4e-7 * np.pi
 H_EXT_MT = (-24.6, 4.3, 0.0)
 
+# DRAM bytes per launch of the BEM product divided by its algorithmic bytes,
+# from one ncu capture on the 8,562-boundary-node profiling film (matrix
+# 586.6 MB > L2; profiles/k_gemv_f64_film_small.txt: 590.04 MB read+written).
+# The traffic grows with the matrix entries, so it scales to the full film.
+NCU_TRAFFIC_RATIO = {"fp64": (586.81 + 3.23) / 586.60}
+
 
 def workload(name):
     from nmag import mesh
@@ -312,7 +318,11 @@ def run_ours(args):
         achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
         roof = {"bound": "hbm", "kernel": "k_gemv_f64" if args.form == "fp64" else "k_gemv_f32",
                 "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "peak_kind": peak_kind, "traffic": None, "launches": gl, "avg_launch_ms": avg_ms,
+                "peak_kind": peak_kind,
+                "traffic": (NCU_TRAFFIC_RATIO[args.form] * bytes_per_launch / 1e9
+                            if args.form in NCU_TRAFFIC_RATIO else None),
+                "traffic_unit": "GB per launch (ncu dram__bytes_read+write, scaled from the profiling film)",
+                "launches": gl, "avg_launch_ms": avg_ms,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "share_of_step": gms / max(dev_ms, 1e-9)}
     line = {
