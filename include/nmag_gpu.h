@@ -63,8 +63,8 @@ typedef struct nmg_ts_stats {
 /* Library version; replaces nothing (ocaml.version). */
 int nmg_version(void);
 
-/* Message of the last failing call on this handle (or the last create error
- * when h == NULL). */
+/* Message of the last failing call on this handle (or, when h == NULL, of the
+ * last failing nmg_create or handle-less call on this thread). */
 const char *nmg_last_error(const nmg_handle *h);
 
 /* Build the mesh topology, the P1 CSR operators, the box volumes, the surface
@@ -170,6 +170,19 @@ int64_t nmg_launch_count(const nmg_handle *h);
 /* Total CG iterations since nmg_create: [Neumann, Dirichlet] (the reference
  * reports KSP iteration counts through PETSc logging, nsim.ml:2462-2478). */
 int nmg_cg_iterations(const nmg_handle *h, int64_t total[2]);
+
+/* max over nodes of |m_i - m_prev_i| for device arrays d_m, d_m_prev (3 x
+ * n_nodes doubles each), written to the host double *out -- the reduction of
+ * nmg_max_dm without any device allocation.  No counterpart in the reference.
+ * For callers that may not allocate GPU memory: programs whose device memory
+ * belongs to their own pool, or control loops that cannot pay for the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  Its scratch is a fixed
+ * 8 KB static device array (kept by every GPU that loads the library), which
+ * limits n_nodes to 2,097,152; larger sizes return -2.  The first call on a
+ * device sets that device up (make it before any stream capture); calls that
+ * overlap on the GPU share the scratch and race.  Runs on the default stream
+ * and returns after the result is on the host; errors via nmg_last_error(NULL). */
+int nmg_max_dm_static(const double *d_m, const double *d_m_prev, int n_nodes, double *out);
 
 #ifdef __cplusplus
 }

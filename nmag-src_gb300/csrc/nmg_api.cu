@@ -25,6 +25,10 @@ bool finite_material(const nmg_material *m) {
 }
 }  // namespace
 
+namespace nmg {
+void set_handleless_error(const std::string &msg) { g_create_error = msg; }
+}  // namespace nmg
+
 extern "C" {
 
 int nmg_version(void) { return NMG_VERSION; }

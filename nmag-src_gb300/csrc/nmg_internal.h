@@ -140,9 +140,8 @@ int ts_init(nmg_handle *h, double t0);
 int ts_advance(nmg_handle *h, double tout, int exact_tstop, int64_t max_steps, double *t_reached,
                nmg_ts_stats *st);
 int rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps);
-// ---- shared device helpers (vec_kernels.cu) ----
-void launch_axpby(cudaStream_t s, int n, double a, const double *x, double b, const double *y, double *z);
-double reduce_dot(nmg_handle *h, int n, const double *x, const double *y);
+// ---- nmg_api.cu ----
+void set_handleless_error(const std::string &msg);  // what nmg_last_error(NULL) reports
 }  // namespace nmg
 
 #define NMG_CUDA_TRY(expr, msg)                                                    \

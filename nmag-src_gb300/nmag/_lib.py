@@ -43,7 +43,7 @@ EXPORTS = ["nmg_version", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_me
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
            "nmg_set_material", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
            "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
-           "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations"]
+           "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_max_dm_static"]
 
 PROFILED_KERNELS = ["bem_gemv", "cg_neumann", "cg_dirichlet", "heff_llg", "jv_psolve"]
 
@@ -98,6 +98,7 @@ def lib(build_if_missing=True):
     L.nmg_launch_count.argtypes = [vp]
     L.nmg_launch_count.restype = C.c_int64
     L.nmg_cg_iterations.argtypes = [vp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]
+    L.nmg_max_dm_static.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_double)]
     _lib = L
     return L
 
