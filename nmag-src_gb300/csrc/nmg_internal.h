@@ -67,6 +67,8 @@ struct Workspace {
   DevBuf<unsigned> bar;     // grid barrier words: per-block arrival epochs + release epoch
   DevBuf<int> err;          // device error flags
   DevBuf<int> iters;        // CG iterations written by the persistent kernel
+  DevBuf<double> basis_b, basis_x, basis_gram;  // CG initial-guess basis per solve kind
+  DevBuf<int> basis_ring;
   int cg_blocks = 0;
   int cg_smem_bytes = 0;     // >0: shared-memory CG (one row per thread)
   int cg_nnz_cap = 0;

@@ -64,13 +64,9 @@ struct CGArgs {
 };
 
 // ---- single-reduction CG on a counter barrier ----
-constexpr int kCG2MaxRed = 4;
+constexpr int kCG2MaxRed = 8;   // widest fused reduction (projection dots + b.b)
 
-// gpu-scope release store / acquire load (the block's other threads are
-// ordered before the release through the preceding __syncthreads).
-__device__ __forceinline__ void st_release_gpu(unsigned *p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
+// gpu-scope acquire load
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -120,17 +116,61 @@ __device__ __forceinline__ bool reduce_all(const CGArgs &a, unsigned epoch, doub
   return true;
 }
 
-// The same single-reduction CG with one row per thread and the block's CSR
-// rows (values with Dirichlet-masked columns zeroed, column indices) staged in
-// shared memory once per solve; each iteration then only gathers the
-// neighbours' u from L2, all loads of a row issued together.
-struct CGSmemLayout {
-  int nnz_cap;  // entries per block
+// Jacobi-preconditioned CG in the single-reduction (Chronopoulos-Gear) form,
+// one row per thread, the block's CSR rows (Dirichlet-masked columns zeroed)
+// resident in shared memory; each iteration gathers only the neighbours' u
+// from L2.  Stopping rule ||r||_2 <= max(rtol ||b - mean||_2, atol).
+//
+// Initial guess: the solution is linear in b, so b is projected (least
+// squares) onto the span of the last kBasis right-hand sides of this solve
+// kind, and x starts from the same combination of their solutions.  The dots
+// b.b_j come with the first reduction and also update the Gram matrix; every
+// block solves the small system identically.  With an empty basis the
+// previous solution is the start, like the reference's initial_guess_nonzero.
+constexpr int kBasis = 6;
+
+struct CGBasis {
+  double *b, *x;   // kBasis x N right-hand sides and solutions
+  double *gram;    // kBasis x kBasis
+  int *ring;       // {count, head}
 };
 
-__global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap) {
+// Least squares for c: (G + eps diag G) c = v via Cholesky; directions whose
+// pivot collapses (nearly dependent right-hand sides) get c = 0.
+__device__ void small_solve(int n, const double *G, const double *v, double *c) {
+  double L[kBasis][kBasis], y[kBasis];
+  bool on[kBasis];
+  for (int i = 0; i < n; ++i) {
+    on[i] = true;
+    for (int j = 0; j <= i; ++j) {
+      double s = G[i * kBasis + j];
+      if (i == j) s *= 1.0 + 1e-12;
+      for (int k = 0; k < j; ++k) if (on[k]) s -= L[i][k] * L[j][k];
+      if (i == j) {
+        if (!(s > 1e-14 * G[i * kBasis + i]) || !on[i]) { on[i] = false; L[i][i] = 1.0; }
+        else L[i][i] = sqrt(s);
+      } else {
+        L[i][j] = on[j] ? s / L[j][j] : 0.0;
+      }
+    }
+    if (!on[i]) for (int j = 0; j < i; ++j) L[i][j] = 0.0;
+  }
+  for (int i = 0; i < n; ++i) {
+    double s = v[i];
+    for (int k = 0; k < i; ++k) s -= L[i][k] * y[k];
+    y[i] = on[i] ? s / L[i][i] : 0.0;
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = y[i];
+    for (int k = i + 1; k < n; ++k) s -= L[k][i] * c[k];
+    c[i] = on[i] ? s / L[i][i] : 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBasis B) {
   extern __shared__ double dyn[];
-  __shared__ double smem[32 * kCG2MaxRed];
+  __shared__ double smem[32 * (kBasis + 1)];
+  __shared__ double sc[kBasis + 4];
   double *sK = dyn;
   int *sC = reinterpret_cast<int *>(sK + nnz_cap);
   const int row0 = blockIdx.x * blockDim.x;
@@ -174,22 +214,42 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap) {
     if (!reduce_all<1>(a, ++epoch, v, smem, t)) return;
     mean_b = t[0] / a.N;
   }
-  double ri = 0.0, ui = 0.0, pi = 0.0, si = 0.0, wi = 0.0, bb_loc = 0.0;
+  const double bi = active ? bi0 - mean_b : 0.0;
+  // ---- projection of b onto the stored right-hand sides ----
+  const int count = B.ring[0], head = B.ring[1];
+  double proj[kBasis + 1], bdot[kBasis + 1];
+  for (int j = 0; j <= kBasis; ++j) proj[j] = 0.0;
   if (active) {
-    const double bi = bi0 - mean_b;
+    for (int j = 0; j < count; ++j) proj[j] = bi * B.b[(size_t)j * a.N + i];
+    proj[kBasis] = bi * bi;
+  }
+  if (!reduce_all<kBasis + 1>(a, ++epoch, proj, smem, bdot)) return;
+  const double tol = fmax(a.rtol * sqrt(bdot[kBasis]), a.atol);
+  if (count > 0) {
+    if (threadIdx.x == 0) {
+      double c[kBasis];
+      small_solve(count, B.gram, bdot, c);
+      for (int j = 0; j < count; ++j) sc[j] = c[j];
+    }
+    __syncthreads();
+    if (active) {
+      double g = 0.0;
+      for (int j = 0; j < count; ++j) g += sc[j] * B.x[(size_t)j * a.N + i];
+      xi = ident ? bi : g;   // identity (Dirichlet boundary) rows are exact
+      a.x[i] = xi;
+    }
+    if (!arrive_wait(a, ++epoch)) return;   // publish the initial guess
+  }
+  double ri = 0.0, ui = 0.0, pi = 0.0, si = 0.0, wi = 0.0;
+  if (active) {
     ri = bi - apply(a.x);
     ui = dinv * ri;
     a.z[i] = ui;
-    bb_loc = bi * bi;
   }
-  double tol, gamma = 0.0, alpha = 0.0, beta = 0.0;
+  if (!arrive_wait(a, ++epoch)) return;   // publish u
+  double gamma = 0.0, alpha = 0.0;
   int it = 0;
   bool failed = false;
-  {
-    double v[1] = {bb_loc}, t[1];
-    if (!reduce_all<1>(a, ++epoch, v, smem, t)) return;
-    tol = fmax(a.rtol * sqrt(t[0]), a.atol);
-  }
   for (;;) {
     double v[3] = {0.0, 0.0, 0.0}, t[3];
     if (active) {
@@ -197,13 +257,26 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap) {
       v[0] = ri * ui; v[1] = wi * ui; v[2] = ri * ri;
     }
     if (!reduce_all<3>(a, ++epoch, v, smem, t)) return;
-    if (!(t[2] == t[2]) || isinf(t[2])) { failed = true; break; }
-    if (sqrt(t[2]) <= tol) break;
-    if (it >= a.maxits) { failed = true; break; }
-    const double gamma_new = t[0], delta = t[1];
-    if (it == 0) { beta = 0.0; alpha = gamma_new / delta; }
-    else { beta = gamma_new / gamma; alpha = gamma_new / (delta - beta * gamma_new / alpha); }
-    gamma = gamma_new;
+    // scalar recurrences once per block (FP64 is scarce), broadcast in smem
+    if (threadIdx.x == 0) {
+      int state = 0;  // 0 continue, 1 converged, 2 failed
+      if (!(t[2] == t[2]) || isinf(t[2])) state = 2;
+      else if (sqrt(t[2]) <= tol) state = 1;
+      else if (it >= a.maxits) state = 2;
+      double beta = 0.0, al = alpha;
+      if (state == 0) {
+        if (it == 0) al = t[0] / t[1];
+        else { beta = t[0] / gamma; al = t[0] / (t[1] - beta * t[0] / alpha); }
+      }
+      sc[0] = al; sc[1] = beta; sc[2] = t[0]; sc[3] = (double)state;
+    }
+    __syncthreads();
+    const int state = (int)sc[3];
+    const double beta = sc[1];
+    alpha = sc[0];
+    gamma = sc[2];
+    __syncthreads();
+    if (state != 0) { failed = state == 2; break; }
     if (active) {
       pi = ui + beta * pi;
       si = wi + beta * si;
@@ -213,18 +286,31 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap) {
       a.z[i] = ui;
     }
     ++it;
-    if (!arrive_wait(a, ++epoch)) return;
+    if (!arrive_wait(a, ++epoch)) return;   // publish the new u
   }
   if (a.mode == 0) {
     double v[1] = {active ? xi : 0.0}, t[1];
     if (!reduce_all<1>(a, ++epoch, v, smem, t)) return;
     xi -= t[0] / a.N;
   }
-  if (active) a.x[i] = xi;
+  if (active) {
+    a.x[i] = xi;
+    B.b[(size_t)head * a.N + i] = bi;   // remember this solve for the next guess
+    B.x[(size_t)head * a.N + i] = xi;
+  }
   if (i == 0) {
     a.iters[a.mode] = it;
     a.iters[2 + a.mode] += it;
     if (failed) atomicOr(a.err, ERR_CG_MAXITS);
+    // Gram matrix row/column of the slot being replaced: its new vector is b
+    const int ncount = count < kBasis ? count + 1 : kBasis;
+    for (int j = 0; j < ncount; ++j) {
+      const double g = (j == head) ? bdot[kBasis] : bdot[j];
+      B.gram[head * kBasis + j] = g;
+      B.gram[j * kBasis + head] = g;
+    }
+    B.ring[0] = ncount;
+    B.ring[1] = (head + 1) % kBasis;
   }
 }
 
@@ -467,7 +553,12 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   cudaError_t e;
   {
     int cap = W.cg_nnz_cap;
-    void *args3[] = {&a, &cap};
+    CGBasis basis;
+    basis.b = W.basis_b.p + (size_t)mode * kBasis * M.N;
+    basis.x = W.basis_x.p + (size_t)mode * kBasis * M.N;
+    basis.gram = W.basis_gram.p + mode * kBasis * kBasis;
+    basis.ring = W.basis_ring.p + 2 * mode;
+    void *args3[] = {&a, &cap, &basis};
     e = cudaLaunchCooperativeKernel((const void *)k_cg3, dim3(W.cg_blocks), dim3(kCGThreads), args3,
                                     (size_t)W.cg_smem_bytes, h->stream);
   }
@@ -548,10 +639,15 @@ int init_workspace(nmg_handle *h, std::string &err) {
   if (nb > 0 && slabs > nb) slabs = nb;
   W.gemv_slabs = slabs;
   NMG_CUDA_TRY(W.bpart.alloc((size_t)slabs * (nb > 0 ? nb : 1) + (size_t)nb), "alloc gemv partials");
-  size_t red_n = 9 * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);
+  size_t red_n = 2 * 8 * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);  // 2 parities x 8 values
   NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
   NMG_CUDA_TRY(W.bar.alloc(W.cg_blocks + 2), "alloc barrier");
   NMG_CUDA_TRY(W.cg_w.alloc(N), "alloc");
+  NMG_CUDA_TRY(W.basis_b.alloc(2 * (size_t)kBasis * N), "alloc CG basis");
+  NMG_CUDA_TRY(W.basis_x.alloc(2 * (size_t)kBasis * N), "alloc CG basis");
+  NMG_CUDA_TRY(W.basis_gram.alloc(2 * kBasis * kBasis), "alloc");
+  NMG_CUDA_TRY(W.basis_ring.alloc(4), "alloc");
+  cudaMemsetAsync(W.basis_ring.p, 0, sizeof(int) * 4, h->stream);
   NMG_CUDA_TRY(W.cg_tot.alloc(2 * 4), "alloc");
   NMG_CUDA_TRY(W.iters.alloc(4), "alloc");
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);

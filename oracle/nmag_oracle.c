@@ -479,6 +479,7 @@ int om_state_init(om_state *S, const om_mesh *M, const om_material *mat, const o
 void om_state_free(om_state *S) {
   free(S->phi1); free(S->phi2); free(S->phi); free(S->rho); free(S->h_ext); free(S->h_exch); free(S->h_demag);
   free(S->h_anis); free(S->h_total); free(S->dmdt); free(S->tmp_b1); free(S->tmp_b2);
+  for (int k = 0; k < 2; ++k) { free(S->basis_b[k]); free(S->basis_x[k]); }
   memset(S, 0, sizeof(*S));
 }
 
@@ -510,11 +511,49 @@ static double dot(int n, const double *a, const double *b) {
   return s;
 }
 
-/* Jacobi-preconditioned CG, warm start in x, stop when ||r||_2 <= max(rtol ||b||_2, atol)
- * (PETSc's default test measured on ||b||).  mode 0 projects out the constant
- * null space of the Neumann operator (nullspace_subfields=["phi"],
- * nmag_lam.py:623-624).  Returns iterations, or -1 on non-convergence. */
-static int pcg(const om_mesh *M, int mode, const double *b_in, double *x, double rtol, double atol, int maxits) {
+/* Least squares (G + 1e-12 diag G) c = v by Cholesky; nearly dependent
+ * directions (collapsed pivots) get c = 0.  Same algorithm as the device. */
+static void small_solve(int n, const double *G, const double *v, double *c) {
+  double L[OM_BASIS][OM_BASIS], y[OM_BASIS];
+  int on[OM_BASIS];
+  for (int i = 0; i < n; ++i) {
+    on[i] = 1;
+    for (int j = 0; j <= i; ++j) {
+      double s = G[i * OM_BASIS + j];
+      if (i == j) s *= 1.0 + 1e-12;
+      for (int k = 0; k < j; ++k) if (on[k]) s -= L[i][k] * L[j][k];
+      if (i == j) {
+        if (!(s > 1e-14 * G[i * OM_BASIS + i]) || !on[i]) { on[i] = 0; L[i][i] = 1.0; }
+        else L[i][i] = sqrt(s);
+      } else {
+        L[i][j] = on[j] ? s / L[j][j] : 0.0;
+      }
+    }
+    if (!on[i]) for (int j = 0; j < i; ++j) L[i][j] = 0.0;
+  }
+  for (int i = 0; i < n; ++i) {
+    double s = v[i];
+    for (int k = 0; k < i; ++k) s -= L[i][k] * y[k];
+    y[i] = on[i] ? s / L[i][i] : 0.0;
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = y[i];
+    for (int k = i + 1; k < n; ++k) s -= L[k][i] * c[k];
+    c[i] = on[i] ? s / L[i][i] : 0.0;
+  }
+}
+
+/* Jacobi-preconditioned CG, stop when ||r||_2 <= max(rtol ||b||_2, atol)
+ * (PETSc's default test measured on ||b||).  mode 0 projects the constant
+ * null space of the Neumann operator out of b and of the solution
+ * (nullspace_subfields=["phi"], nmag_lam.py:623-624).
+ * Initial guess: the reference warm-starts from the previous solution
+ * (initial_guess_nonzero, nmag_lam.py:617,628); here b is first projected
+ * onto the span of the last OM_BASIS right-hand sides of this solve kind and
+ * x starts from the same combination of their solutions (the previous
+ * solution when the basis is empty).  Returns iterations, or -1. */
+static int pcg(om_state *S, int mode, const double *b_in, double *x, double rtol, double atol, int maxits) {
+  const om_mesh *M = S->M;
   int N = M->n_nodes;
   double *r = malloc(sizeof(double) * N), *z = malloc(sizeof(double) * N), *p = malloc(sizeof(double) * N),
          *q = malloc(sizeof(double) * N), *dinv = malloc(sizeof(double) * N), *b = malloc(sizeof(double) * N);
@@ -531,7 +570,24 @@ static int pcg(const om_mesh *M, int mode, const double *b_in, double *x, double
     double mb = 0.0; for (int i = 0; i < N; ++i) mb += b[i]; mb /= N;
     for (int i = 0; i < N; ++i) b[i] -= mb;
   }
-  double bnorm = sqrt(dot(N, b, b));
+  if (!S->basis_b[mode]) {
+    S->basis_b[mode] = xcalloc((size_t)OM_BASIS * N, sizeof(double));
+    S->basis_x[mode] = xcalloc((size_t)OM_BASIS * N, sizeof(double));
+  }
+  const int count = S->bcount[mode], head = S->bhead[mode];
+  double bdot[OM_BASIS];
+  for (int j = 0; j < count; ++j) bdot[j] = dot(N, b, S->basis_b[mode] + (size_t)j * N);
+  double bb = dot(N, b, b);
+  if (count > 0) {
+    double c[OM_BASIS];
+    small_solve(count, S->gram[mode], bdot, c);
+    for (int i = 0; i < N; ++i) {
+      double g = 0.0;
+      for (int j = 0; j < count; ++j) g += c[j] * S->basis_x[mode][(size_t)j * N + i];
+      x[i] = (mode == 1 && M->b_of_node[i] >= 0) ? b[i] : g;
+    }
+  }
+  double bnorm = sqrt(bb);
   double tol = rtol * bnorm; if (atol > tol) tol = atol;
   spmv_K(M, mode, x, q);
   for (int i = 0; i < N; ++i) r[i] = b[i] - q[i];
@@ -541,7 +597,6 @@ static int pcg(const om_mesh *M, int mode, const double *b_in, double *x, double
   while (rnorm > tol) {
     if (it >= maxits) { status = -1; break; }
     for (int i = 0; i < N; ++i) z[i] = dinv[i] * r[i];
-    if (mode == 0) { double mz = 0.0; for (int i = 0; i < N; ++i) mz += z[i]; mz /= N; for (int i = 0; i < N; ++i) z[i] -= mz; }
     double rz_new = dot(N, r, z);
     if (it == 0) { memcpy(p, z, sizeof(double) * N); }
     else { double beta = rz_new / rz; for (int i = 0; i < N; ++i) p[i] = z[i] + beta * p[i]; }
@@ -553,6 +608,17 @@ static int pcg(const om_mesh *M, int mode, const double *b_in, double *x, double
     ++it;
   }
   if (mode == 0) { double mx = 0.0; for (int i = 0; i < N; ++i) mx += x[i]; mx /= N; for (int i = 0; i < N; ++i) x[i] -= mx; }
+  /* remember (b, x) in the ring and update the Gram matrix */
+  memcpy(S->basis_b[mode] + (size_t)head * N, b, sizeof(double) * N);
+  memcpy(S->basis_x[mode] + (size_t)head * N, x, sizeof(double) * N);
+  int ncount = count < OM_BASIS ? count + 1 : OM_BASIS;
+  for (int j = 0; j < ncount; ++j) {
+    double g = (j == head) ? bb : bdot[j];
+    S->gram[mode][head * OM_BASIS + j] = g;
+    S->gram[mode][j * OM_BASIS + head] = g;
+  }
+  S->bcount[mode] = ncount;
+  S->bhead[mode] = (head + 1) % OM_BASIS;
   free(r); free(z); free(p); free(q); free(dinv); free(b);
   return status < 0 ? -1 : it;
 }
@@ -574,7 +640,7 @@ static int demag(om_state *S, const double *m) {
     }
     S->rho[i] = -(Ms * s);
   }
-  int it1 = pcg(M, 0, S->rho, S->phi1, S->nbc.rtol, S->nbc.atol, S->nbc.maxits);
+  int it1 = pcg(S, 0, S->rho, S->phi1, S->nbc.rtol, S->nbc.atol, S->nbc.maxits);
   S->last_iters_nbc = it1;
   if (it1 < 0) return 1;
   /* phi2b = BEM phi1b */
@@ -600,7 +666,7 @@ static int demag(om_state *S, const double *m) {
     }
     rhs[i] = -s;
   }
-  int it2 = pcg(M, 1, rhs, S->phi2, S->dbc.rtol, S->dbc.atol, S->dbc.maxits);
+  int it2 = pcg(S, 1, rhs, S->phi2, S->dbc.rtol, S->dbc.atol, S->dbc.maxits);
   free(rhs);
   S->last_iters_dbc = it2;
   if (it2 < 0) return 2;

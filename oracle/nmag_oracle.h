@@ -89,7 +89,14 @@ typedef struct om_state {
   int last_iters_nbc, last_iters_dbc;
   long long n_rhs;
   int nthreads;
+  /* initial-guess basis of each solve kind: last OM_BASIS right-hand sides
+     and solutions, their Gram matrix, {count, head} */
+  double *basis_b[2], *basis_x[2];
+  double gram[2][36];
+  int bcount[2], bhead[2];
 } om_state;
+
+#define OM_BASIS 6
 
 int om_state_init(om_state *S, const om_mesh *M, const om_material *mat, const om_solver *nbc,
                   const om_solver *dbc, int do_demag, int nthreads);

@@ -56,7 +56,9 @@ class OmState(C.Structure):
                 ("rho", C.POINTER(C.c_double)), ("phi", C.POINTER(C.c_double)), ("dmdt", C.POINTER(C.c_double)),
                 ("tmp_b1", C.POINTER(C.c_double)), ("tmp_b2", C.POINTER(C.c_double)),
                 ("last_iters_nbc", C.c_int), ("last_iters_dbc", C.c_int), ("n_rhs", C.c_longlong),
-                ("nthreads", C.c_int)]
+                ("nthreads", C.c_int),
+                ("basis_b", C.POINTER(C.c_double) * 2), ("basis_x", C.POINTER(C.c_double) * 2),
+                ("gram", (C.c_double * 36) * 2), ("bcount", C.c_int * 2), ("bhead", C.c_int * 2)]
 
 
 class OmStats(C.Structure):
