@@ -49,7 +49,8 @@ typedef struct nmg_options {
   double dbc_rtol, dbc_atol; int dbc_maxits;   /* Dirichlet Poisson solve            */
   int bem_precision;                     /* 0: FP64 matrix; 1: FP32 matrix, FP64 sums  */
   int cg_precision;                      /* 0: FP64 CG; reserved                       */
-  int reserved[6];
+  int cg_no_coarse;                      /* 1: Jacobi only (no two-level Neumann CG)   */
+  int reserved[5];
 } nmg_options;
 
 /* Integrator statistics (CVODE counters; nsim.ml:354-387 timings). */

@@ -69,6 +69,9 @@ struct Workspace {
   DevBuf<int> iters;        // CG iterations written by the persistent kernel
   DevBuf<double> basis_b, basis_x, basis_gram;  // CG initial-guess basis per solve kind
   DevBuf<int> basis_ring;
+  DevBuf<int32_t> perm, prow, pcol, pbnd;     // CG solver ordering (spatially binned nodes)
+  DevBuf<double> pK, xperm, ainv, rc;         // K in that order, iterate, coarse inverse, coarse residual
+  int nc = 0;                                 // aggregates of the two-level Neumann CG (0: none)
   int cg_blocks = 0;
   int cg_smem_bytes = 0;     // >0: shared-memory CG (one row per thread)
   int cg_nnz_cap = 0;

@@ -13,6 +13,9 @@
 //   k_dbc_rhs      rhs = -K_IB phi2b (interior), phi2b (boundary)  (op_load_DBC)
 //   k_heff_llg     H_exch (K SpMV), H_demag (G SpMV on phi1+phi2), H_anis,
 //                  H_total and dm/dt fused in one node kernel (CFBOX = / V_i)
+#include <algorithm>
+#include <cmath>
+
 #include <cooperative_groups.h>
 
 #include "nmg_internal.h"
@@ -59,9 +62,18 @@ struct CGArgs {
   double rtol, atol;
   int maxits;
   double *w;          // A u (single-reduction CG)
-  unsigned *flags;    // per-block arrival epochs (reduce-barrier)
-  double *tot;        // reduced totals, double-buffered by epoch parity
+  unsigned *flags;    // barrier counter (word 0)
+  double *tot;        // unused
+  // solver ordering: row r of the solve is node perm[r]; CSR in that order
+  const int32_t *perm, *prow, *pcol, *pbnd;   // pbnd[r]: node perm[r] is a boundary node
+  const double *pK;
+  double *xperm;      // current iterate in solver order (published for the SpMV)
+  // two-level preconditioner (mode 0): aggregates of kAgg consecutive rows
+  int coarse, nc;
+  const double *ainv; // nc x nc inverse of the (regularised) aggregated operator
+  double *rc;         // restricted residual, nc
 };
+constexpr int kAgg = 64;   // rows per aggregate (4 aggregates per 256-row block)
 
 // ---- single-reduction CG on a counter barrier ----
 constexpr int kCG2MaxRed = 8;   // widest fused reduction (projection dots + b.b)
@@ -171,31 +183,33 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBas
   extern __shared__ double dyn[];
   __shared__ double smem[32 * (kBasis + 1)];
   __shared__ double sc[kBasis + 4];
+  __shared__ double sagg[2 * (kCGThreads / kAgg)], sec[kCGThreads / kAgg];
   double *sK = dyn;
   int *sC = reinterpret_cast<int *>(sK + nnz_cap);
   const int row0 = blockIdx.x * blockDim.x;
-  const int i = row0 + threadIdx.x;
-  const bool active = i < a.N;
-  const int base = a.row_ptr[row0];
-  const int rend = a.row_ptr[min(row0 + (int)blockDim.x, a.N)];
+  const int r = row0 + threadIdx.x;           // solver row
+  const bool active = r < a.N;
+  const int node = active ? a.perm[r] : 0;
+  const int base = a.prow[row0];
+  const int rend = a.prow[min(row0 + (int)blockDim.x, a.N)];
   for (int k = base + threadIdx.x; k < rend; k += blockDim.x) {
-    const int j = a.col_idx[k];
+    const int j = a.pcol[k];
     sC[k - base] = j;
-    sK[k - base] = (a.mode == 1 && a.b_of_node[j] >= 0) ? 0.0 : a.K[k];
+    sK[k - base] = (a.mode == 1 && a.pbnd[j]) ? 0.0 : a.pK[k];
   }
   int lo = 0, hi = 0;
   bool ident = false;
   double dinv = 1.0, xi = 0.0;
   if (active) {
-    lo = a.row_ptr[i] - base;
-    hi = a.row_ptr[i + 1] - base;
-    ident = a.mode == 1 && a.b_of_node[i] >= 0;
-    dinv = a.dinv[i];
-    xi = a.x[i];
+    lo = a.prow[r] - base;
+    hi = a.prow[r + 1] - base;
+    ident = a.mode == 1 && a.pbnd[r];
+    dinv = a.dinv[node];
+    xi = a.x[node];
   }
   __syncthreads();
   auto apply = [&](const double *v) -> double {
-    if (ident) return __ldcg(v + i);
+    if (ident) return __ldcg(v + r);
     double s = 0.0;
     int k = lo;
     for (; k + 4 <= hi; k += 4) {
@@ -207,8 +221,40 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBas
     return s;
   };
   unsigned epoch = 0;
+  // u = M^-1 r: Jacobi, plus (mode 0) the aggregate correction P Ainv P^T r.
+  // Every block restricts its own kCGThreads/kAgg aggregates, and after one
+  // barrier computes the coarse correction of exactly those aggregates.
+  auto precond = [&](double rr, double &uu) -> bool {
+    uu = dinv * rr;
+    if (!a.coarse) return true;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double s = warp_sum(active ? rr : 0.0);
+    if (lane == 0) sagg[wid] = s;
+    __syncthreads();
+    if (threadIdx.x < kCGThreads / kAgg) {
+      const int I = blockIdx.x * (kCGThreads / kAgg) + threadIdx.x;
+      if (I < a.nc) a.rc[I] = sagg[2 * threadIdx.x] + sagg[2 * threadIdx.x + 1];
+    }
+    if (!arrive_wait(a, ++epoch)) return false;
+    {
+      const int g = threadIdx.x / kAgg, t = threadIdx.x % kAgg;
+      const int I = blockIdx.x * (kCGThreads / kAgg) + g;
+      double acc = 0.0;
+      if (I < a.nc) {
+        const double *row = a.ainv + (size_t)I * a.nc;
+        for (int J = t; J < a.nc; J += kAgg) acc += row[J] * __ldcg(a.rc + J);
+      }
+      acc = warp_sum(acc);
+      if (lane == 0) sagg[wid] = acc;
+      __syncthreads();
+      if (threadIdx.x < kCGThreads / kAgg) sec[threadIdx.x] = sagg[2 * threadIdx.x] + sagg[2 * threadIdx.x + 1];
+      __syncthreads();
+      uu += sec[g];
+    }
+    return true;
+  };
   double mean_b = 0.0;
-  const double bi0 = active ? a.b[i] : 0.0;
+  const double bi0 = active ? a.b[node] : 0.0;
   if (a.mode == 0) {
     double v[1] = {bi0}, t[1];
     if (!reduce_all<1>(a, ++epoch, v, smem, t)) return;
@@ -220,7 +266,7 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBas
   double proj[kBasis + 1], bdot[kBasis + 1];
   for (int j = 0; j <= kBasis; ++j) proj[j] = 0.0;
   if (active) {
-    for (int j = 0; j < count; ++j) proj[j] = bi * B.b[(size_t)j * a.N + i];
+    for (int j = 0; j < count; ++j) proj[j] = bi * B.b[(size_t)j * a.N + r];
     proj[kBasis] = bi * bi;
   }
   if (!reduce_all<kBasis + 1>(a, ++epoch, proj, smem, bdot)) return;
@@ -234,18 +280,16 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBas
     __syncthreads();
     if (active) {
       double g = 0.0;
-      for (int j = 0; j < count; ++j) g += sc[j] * B.x[(size_t)j * a.N + i];
+      for (int j = 0; j < count; ++j) g += sc[j] * B.x[(size_t)j * a.N + r];
       xi = ident ? bi : g;   // identity (Dirichlet boundary) rows are exact
-      a.x[i] = xi;
     }
-    if (!arrive_wait(a, ++epoch)) return;   // publish the initial guess
   }
+  if (active) a.xperm[r] = xi;
+  if (!arrive_wait(a, ++epoch)) return;   // publish the initial iterate
   double ri = 0.0, ui = 0.0, pi = 0.0, si = 0.0, wi = 0.0;
-  if (active) {
-    ri = bi - apply(a.x);
-    ui = dinv * ri;
-    a.z[i] = ui;
-  }
+  if (active) ri = bi - apply(a.xperm);
+  if (!precond(ri, ui)) return;
+  if (active) a.z[r] = ui;
   if (!arrive_wait(a, ++epoch)) return;   // publish u
   double gamma = 0.0, alpha = 0.0;
   int it = 0;
@@ -282,9 +326,9 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBas
       si = wi + beta * si;
       xi += alpha * pi;
       ri -= alpha * si;
-      ui = dinv * ri;
-      a.z[i] = ui;
     }
+    if (!precond(ri, ui)) return;
+    if (active) a.z[r] = ui;
     ++it;
     if (!arrive_wait(a, ++epoch)) return;   // publish the new u
   }
@@ -294,11 +338,11 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBas
     xi -= t[0] / a.N;
   }
   if (active) {
-    a.x[i] = xi;
-    B.b[(size_t)head * a.N + i] = bi;   // remember this solve for the next guess
-    B.x[(size_t)head * a.N + i] = xi;
+    a.x[node] = xi;
+    B.b[(size_t)head * a.N + r] = bi;   // remember this solve for the next guess
+    B.x[(size_t)head * a.N + r] = xi;
   }
-  if (i == 0) {
+  if (r == 0) {
     a.iters[a.mode] = it;
     a.iters[2 + a.mode] += it;
     if (failed) atomicOr(a.err, ERR_CG_MAXITS);
@@ -536,6 +580,128 @@ __global__ void k_maxdm_partials(int N, const double *__restrict__ a, const doub
   }
 }
 
+// Solver ordering and two-level data, built once on the host:
+//  * nodes sorted by spatial bin (Morton order of bins sized for ~kAgg nodes),
+//    so that kAgg consecutive solver rows form a compact aggregate and each
+//    256-row CG block holds 4 whole aggregates;
+//  * the CSR of K in that order (columns sorted);
+//  * the aggregated operator A_c = P^T K P (P: piecewise-constant
+//    prolongation), regularised by (mean diagonal / nc) 1 1^T for the
+//    constant null space, inverted densely (Cholesky).  Skipped for more
+//    than kMaxCoarse aggregates or when the options disable it.
+constexpr int kMaxCoarse = 2048;
+
+uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+  auto spread = [](uint64_t v) {
+    v &= 0x1fffff;
+    v = (v | v << 32) & 0x1f00000000ffffull;
+    v = (v | v << 16) & 0x1f0000ff0000ffull;
+    v = (v | v << 8) & 0x100f00f00f00f00full;
+    v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+    v = (v | v << 2) & 0x1249249249249249ull;
+    return v;
+  };
+  return spread(x) | spread(y) << 1 | spread(z) << 2;
+}
+
+int build_cg_ordering(nmg_handle *h, std::string &err) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  const int N = M.N, nnz = M.nnz;
+  std::vector<int32_t> rp(N + 1), ci(nnz), bon(N);
+  std::vector<double> K(nnz), X(3 * (size_t)N);
+  NMG_CUDA_TRY(cudaMemcpy(rp.data(), M.row_ptr.p, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost), "d2h");
+  NMG_CUDA_TRY(cudaMemcpy(ci.data(), M.col_idx.p, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost), "d2h");
+  NMG_CUDA_TRY(cudaMemcpy(K.data(), M.K.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost), "d2h");
+  NMG_CUDA_TRY(cudaMemcpy(X.data(), M.coords.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost), "d2h");
+  NMG_CUDA_TRY(cudaMemcpy(bon.data(), M.b_of_node.p, sizeof(int32_t) * N, cudaMemcpyDeviceToHost), "d2h");
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) { lo[d] = X[d]; hi[d] = X[d]; }
+  for (int i = 0; i < N; ++i)
+    for (int d = 0; d < 3; ++d) { lo[d] = std::min(lo[d], X[3 * i + d]); hi[d] = std::max(hi[d], X[3 * i + d]); }
+  double vol = 1.0;
+  for (int d = 0; d < 3; ++d) vol *= std::max(hi[d] - lo[d], 1e-30);
+  const double H = std::cbrt(vol * kAgg / N);
+  std::vector<std::pair<uint64_t, int>> key(N);
+  for (int i = 0; i < N; ++i) {
+    uint32_t b[3];
+    for (int d = 0; d < 3; ++d) b[d] = (uint32_t)std::min(2097151.0, std::floor((X[3 * i + d] - lo[d]) / H));
+    key[i] = {morton3(b[0], b[1], b[2]), i};
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<int32_t> perm(N), inv(N), prow(N + 1), pcol(nnz), pbnd(N);
+  std::vector<double> pK(nnz);
+  for (int r = 0; r < N; ++r) { perm[r] = key[r].second; inv[key[r].second] = r; }
+  prow[0] = 0;
+  std::vector<std::pair<int32_t, double>> row;
+  for (int r = 0; r < N; ++r) {
+    const int node = perm[r];
+    row.clear();
+    for (int k = rp[node]; k < rp[node + 1]; ++k) row.push_back({inv[ci[k]], K[k]});
+    std::sort(row.begin(), row.end(), [](const std::pair<int32_t, double> &x, const std::pair<int32_t, double> &y) {
+      return x.first < y.first;
+    });
+    int o = prow[r];
+    for (auto &e : row) { pcol[o] = e.first; pK[o] = e.second; ++o; }
+    prow[r + 1] = o;
+    pbnd[r] = bon[node] >= 0 ? 1 : 0;
+  }
+  NMG_CUDA_TRY(W.perm.alloc(N), "alloc");
+  NMG_CUDA_TRY(W.prow.alloc(N + 1), "alloc");
+  NMG_CUDA_TRY(W.pcol.alloc(nnz), "alloc");
+  NMG_CUDA_TRY(W.pbnd.alloc(N), "alloc");
+  NMG_CUDA_TRY(W.pK.alloc(nnz), "alloc");
+  NMG_CUDA_TRY(W.xperm.alloc(N), "alloc");
+  NMG_CUDA_TRY(cudaMemcpy(W.perm.p, perm.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "h2d");
+  NMG_CUDA_TRY(cudaMemcpy(W.prow.p, prow.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice), "h2d");
+  NMG_CUDA_TRY(cudaMemcpy(W.pcol.p, pcol.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice), "h2d");
+  NMG_CUDA_TRY(cudaMemcpy(W.pbnd.p, pbnd.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "h2d");
+  NMG_CUDA_TRY(cudaMemcpy(W.pK.p, pK.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice), "h2d");
+  W.nc = 0;
+  const int nc = (N + kAgg - 1) / kAgg;
+  if (h->opt.cg_no_coarse || nc > kMaxCoarse || nc < 2) return 0;
+  std::vector<double> A((size_t)nc * nc, 0.0);
+  for (int r = 0; r < N; ++r)
+    for (int k = prow[r]; k < prow[r + 1]; ++k) A[(size_t)(r / kAgg) * nc + pcol[k] / kAgg] += pK[k];
+  double md = 0.0;
+  for (int I = 0; I < nc; ++I) md += A[(size_t)I * nc + I];
+  md /= nc;
+  for (auto &v : A) v += md / nc;
+  // Cholesky A = L L^T (lower, in place), then A^-1 = L^-T L^-1
+  for (int j = 0; j < nc; ++j) {
+    double d = A[(size_t)j * nc + j];
+    for (int k = 0; k < j; ++k) d -= A[(size_t)j * nc + k] * A[(size_t)j * nc + k];
+    if (!(d > 0.0)) return 0;   // not positive definite: run without the coarse level
+    d = std::sqrt(d);
+    A[(size_t)j * nc + j] = d;
+    for (int i = j + 1; i < nc; ++i) {
+      double s = A[(size_t)i * nc + j];
+      for (int k = 0; k < j; ++k) s -= A[(size_t)i * nc + k] * A[(size_t)j * nc + k];
+      A[(size_t)i * nc + j] = s / d;
+    }
+  }
+  std::vector<double> Linv((size_t)nc * nc, 0.0), Ainv((size_t)nc * nc, 0.0);
+  for (int j = 0; j < nc; ++j) {   // column j of L^-1 by forward substitution
+    for (int i = j; i < nc; ++i) {
+      double s = (i == j) ? 1.0 : 0.0;
+      for (int k = j; k < i; ++k) s -= A[(size_t)i * nc + k] * Linv[(size_t)k * nc + j];
+      Linv[(size_t)i * nc + j] = s / A[(size_t)i * nc + i];
+    }
+  }
+  for (int i = 0; i < nc; ++i)
+    for (int j = 0; j <= i; ++j) {
+      double s = 0.0;
+      for (int k = i; k < nc; ++k) s += Linv[(size_t)k * nc + i] * Linv[(size_t)k * nc + j];
+      Ainv[(size_t)i * nc + j] = s;
+      Ainv[(size_t)j * nc + i] = s;
+    }
+  NMG_CUDA_TRY(W.ainv.alloc((size_t)nc * nc), "alloc coarse inverse");
+  NMG_CUDA_TRY(W.rc.alloc(nc), "alloc");
+  NMG_CUDA_TRY(cudaMemcpy(W.ainv.p, Ainv.data(), sizeof(double) * nc * nc, cudaMemcpyHostToDevice), "h2d");
+  W.nc = nc;
+  return 0;
+}
+
 int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, double atol, int maxits) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
@@ -547,6 +713,9 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   a.w = W.cg_w; a.flags = W.bar; a.tot = W.cg_tot;
   a.bar = W.bar; a.err = W.err; a.iters = W.iters;
   a.rtol = rtol; a.atol = atol; a.maxits = maxits;
+  a.perm = W.perm; a.prow = W.prow; a.pcol = W.pcol; a.pbnd = W.pbnd; a.pK = W.pK; a.xperm = W.xperm;
+  a.coarse = (mode == 0 && W.nc > 0) ? 1 : 0;
+  a.nc = W.nc; a.ainv = W.ainv; a.rc = W.rc;
   // fresh barrier words per solve: epochs restart at 1 inside the kernel
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
   NMG_PROF_BEGIN(h, 1 + mode);
@@ -602,8 +771,10 @@ int init_workspace(nmg_handle *h, std::string &err) {
   if (W.cg_blocks < 1) W.cg_blocks = 1;
   // Shared-memory CG: one row per thread, each block's CSR rows resident.
   {
+    int rc_order = build_cg_ordering(h, err);
+    if (rc_order) return rc_order;
     std::vector<int32_t> rp(N + 1);
-    NMG_CUDA_TRY(cudaMemcpy(rp.data(), M.row_ptr.p, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost), "d2h");
+    NMG_CUDA_TRY(cudaMemcpy(rp.data(), W.prow.p, sizeof(int32_t) * (N + 1), cudaMemcpyDeviceToHost), "d2h");
     int cap = 0;
     for (int r0 = 0; r0 < N; r0 += kCGThreads) {
       int r1 = r0 + kCGThreads < N ? r0 + kCGThreads : N;

@@ -25,7 +25,8 @@ class Material(C.Structure):
 class Options(C.Structure):
     _fields_ = [("do_demag", C.c_int), ("nbc_rtol", C.c_double), ("nbc_atol", C.c_double), ("nbc_maxits", C.c_int),
                 ("dbc_rtol", C.c_double), ("dbc_atol", C.c_double), ("dbc_maxits", C.c_int),
-                ("bem_precision", C.c_int), ("cg_precision", C.c_int), ("reserved", C.c_int * 6)]
+                ("bem_precision", C.c_int), ("cg_precision", C.c_int), ("cg_no_coarse", C.c_int),
+                ("reserved", C.c_int * 5)]
 
 
 class TsStats(C.Structure):
