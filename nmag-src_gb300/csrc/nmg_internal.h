@@ -76,6 +76,7 @@ struct Workspace {
   int cg_smem_bytes = 0;     // >0: shared-memory CG (one row per thread)
   int cg_nnz_cap = 0;
   int gemv_slabs = 1;
+  int gemv_rpb = 256, gemv_groups = 1, gemv_threads = 256;   // GEMV row groups
 };
 
 struct Integrator;

@@ -387,12 +387,15 @@ __global__ void k_gather_b(int nb, const int32_t *__restrict__ node_of_b, const 
   if (b < nb) out[b] = phi[node_of_b[b]];
 }
 
-// y_part[s][k] = sum_{c in slab s} B[k][c] x[c]  (column-major B, FP64)
-constexpr int kGemvRows = 256;
-__global__ void __launch_bounds__(kGemvRows) k_gemv_f64(int nb, int slab, const double *__restrict__ B,
-                                                          const double *__restrict__ x, double *__restrict__ part) {
+// y_part[s][k] = sum_{c in slab s} B[k][c] x[c]  (column-major B, FP64).
+// Grid: row groups of rpb rows (blockIdx.x) x column slabs (blockIdx.y); the
+// host picks the split so that the grid is exactly 4 blocks per SM with equal
+// work per block (no partial last wave).
+constexpr int kGemvMaxThreads = 512;
+__global__ void __launch_bounds__(kGemvMaxThreads) k_gemv_f64(int nb, int slab, int rpb, const double *__restrict__ B,
+                                                               const double *__restrict__ x, double *__restrict__ part) {
   __shared__ double xs[1024];
-  const int k = blockIdx.x * kGemvRows + threadIdx.x;
+  const int k = (threadIdx.x < rpb) ? blockIdx.x * rpb + threadIdx.x : nb;
   const int c0 = blockIdx.y * slab, c1 = min(nb, c0 + slab);
   double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
   for (int cb = c0; cb < c1; cb += 1024) {
@@ -416,10 +419,10 @@ __global__ void __launch_bounds__(kGemvRows) k_gemv_f64(int nb, int slab, const 
 }
 
 // FP32 matrix, FP32 products summed in 64-term chunks, chunks summed in FP64.
-__global__ void __launch_bounds__(kGemvRows) k_gemv_f32(int nb, int slab, const float *__restrict__ B,
-                                                          const float *__restrict__ x, double *__restrict__ part) {
+__global__ void __launch_bounds__(kGemvMaxThreads) k_gemv_f32(int nb, int slab, int rpb, const float *__restrict__ B,
+                                                               const float *__restrict__ x, double *__restrict__ part) {
   __shared__ float xs[2048];
-  const int k = blockIdx.x * kGemvRows + threadIdx.x;
+  const int k = (threadIdx.x < rpb) ? blockIdx.x * rpb + threadIdx.x : nb;
   const int c0 = blockIdx.y * slab, c1 = min(nb, c0 + slab);
   double acc = 0.0;
   for (int cb = c0; cb < c1; cb += 2048) {
@@ -803,13 +806,27 @@ int init_workspace(nmg_handle *h, std::string &err) {
     }
   }
   // GEMV slabs: about 4 blocks per SM in total.
-  int row_tiles = nblk(nb, kGemvRows);
-  int slabs = row_tiles > 0 ? (4 * h->sm_count + row_tiles - 1) / row_tiles : 1;
-  if (slabs < 1) slabs = 1;
-  if (slabs > 64) slabs = 64;
-  if (nb > 0 && slabs > nb) slabs = nb;
-  W.gemv_slabs = slabs;
-  NMG_CUDA_TRY(W.bpart.alloc((size_t)slabs * (nb > 0 ? nb : 1) + (size_t)nb), "alloc gemv partials");
+  // GEMV grid: (row groups) x (column slabs) = 4 blocks per SM exactly,
+  // slabs a divisor of that count, row groups of at most kGemvMaxThreads rows.
+  {
+    const int target = 4 * h->sm_count;
+    int best_s = 1, best_r = nb > 0 ? nb : 1;
+    double best_cost = 1e300;
+    for (int s_ = 1; s_ <= target; ++s_) {
+      if (target % s_) continue;
+      const int groups = target / s_;
+      const int rpb = nb > 0 ? (nb + groups - 1) / groups : 1;
+      if (rpb > kGemvMaxThreads || (nb > 0 && nb / s_ < 32)) continue;
+      // prefer ~256-row groups (coalesced, enough columns per slab)
+      const double cost = std::fabs(std::log((double)rpb / 256.0));
+      if (cost < best_cost) { best_cost = cost; best_s = s_; best_r = rpb; }
+    }
+    W.gemv_rpb = best_r;
+    W.gemv_groups = nb > 0 ? (nb + best_r - 1) / best_r : 1;
+    W.gemv_threads = ((best_r + 31) / 32) * 32;
+    W.gemv_slabs = best_s;
+  }
+  NMG_CUDA_TRY(W.bpart.alloc((size_t)W.gemv_slabs * (nb > 0 ? nb : 1) + (size_t)nb), "alloc gemv partials");
   size_t red_n = 2 * 8 * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);  // 2 parities x 8 values
   NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
   NMG_CUDA_TRY(W.bar.alloc(W.cg_blocks + 2), "alloc barrier");
@@ -834,16 +851,16 @@ void bem_gemv(nmg_handle *h, const double *x, double *y) {
   Workspace &W = h->ws;
   const int nb = M.nb, slabs = W.gemv_slabs;
   const int slab = (nb + slabs - 1) / slabs;
-  dim3 grid(nblk(nb, kGemvRows), slabs);
+  dim3 grid(W.gemv_groups, slabs);
   if (h->opt.bem_precision == 1 && M.bem32.p) {
     float *x32 = reinterpret_cast<float *>(W.bpart.p + (size_t)slabs * nb);
     k_to_f32_vec<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, x, x32); ++h->launches;
     NMG_PROF_BEGIN(h, 0);
-    k_gemv_f32<<<grid, kGemvRows, 0, h->stream>>>(nb, slab, M.bem32, x32, W.bpart); ++h->launches;
+    k_gemv_f32<<<grid, W.gemv_threads, 0, h->stream>>>(nb, slab, W.gemv_rpb, M.bem32, x32, W.bpart); ++h->launches;
     NMG_PROF_END(h);
   } else {
     NMG_PROF_BEGIN(h, 0);
-    k_gemv_f64<<<grid, kGemvRows, 0, h->stream>>>(nb, slab, M.bem, x, W.bpart); ++h->launches;
+    k_gemv_f64<<<grid, W.gemv_threads, 0, h->stream>>>(nb, slab, W.gemv_rpb, M.bem, x, W.bpart); ++h->launches;
     NMG_PROF_END(h);
   }
   k_slab_sum<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, slabs, W.bpart, y); ++h->launches;
