@@ -136,10 +136,15 @@ __global__ void __launch_bounds__(128) k_bem_fill(int nb, int ntri, const TriGeo
   bem[(size_t)k * nb + k] += solid_angle[k] / (4.0 * kPi) - 1.0;
 }
 
-__global__ void k_to_f32(size_t n, const double *__restrict__ a, float *__restrict__ b) {
+// FP32 copy with the leading dimension padded to ld (pad rows zero).
+__global__ void k_to_f32(int nb, int ld, const double *__restrict__ a, float *__restrict__ b) {
+  const size_t n = (size_t)ld * nb;
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (; i < n; i += stride) b[i] = (float)a[i];
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) {
+    const size_t c = i / ld, k = i % ld;
+    b[i] = k < (size_t)nb ? (float)a[c * nb + k] : 0.0f;
+  }
 }
 
 }  // namespace
@@ -158,8 +163,9 @@ int fill_bem(nmg_handle *h, std::string &err) {
                                                  M.solid_angle, M.bem);
   NMG_CUDA_TRY(cudaGetLastError(), "bem fill launch");
   if (h->opt.bem_precision == 1) {
-    NMG_CUDA_TRY(M.bem32.alloc((size_t)M.nb * M.nb), "alloc FP32 BEM");
-    k_to_f32<<<h->sm_count * 8, 256, 0, s>>>((size_t)M.nb * M.nb, M.bem, M.bem32);
+    M.ld32 = (M.nb + 3) / 4 * 4;
+    NMG_CUDA_TRY(M.bem32.alloc((size_t)M.ld32 * M.nb), "alloc FP32 BEM");
+    k_to_f32<<<h->sm_count * 8, 256, 0, s>>>(M.nb, M.ld32, M.bem, M.bem32);
   }
   NMG_CUDA_TRY(cudaStreamSynchronize(s), "bem fill");
   return 0;

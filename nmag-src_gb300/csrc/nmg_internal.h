@@ -56,7 +56,8 @@ struct Mesh {
   DevBuf<double> coords, dL, adet, K, G, D, vol, tri_normal, solid_angle;
   DevBuf<int32_t> tets, nt_ptr, nt_idx, nbr, row_ptr, col_idx, diag_pos, b_of_node, node_of_b, tri;
   DevBuf<double> bem;      // FP64 BEM, column-major (bem[c*nb + k] = B[k][c])
-  DevBuf<float> bem32;     // FP32 copy (precision form)
+  DevBuf<float> bem32;     // FP32 copy (precision form), leading dimension ld32
+  int ld32 = 0;
   DevBuf<TriGeo> trigeo;
   DevBuf<double> obs_max;
 };
@@ -77,6 +78,7 @@ struct Workspace {
   int cg_nnz_cap = 0;
   int gemv_slabs = 1;
   int gemv_rpb = 256, gemv_groups = 1, gemv_threads = 256;   // GEMV row groups
+  int gemv_rpb4 = 256, gemv_threads32 = 64;                   // FP32 GEMV: 4 rows per thread
 };
 
 struct Integrator;

@@ -418,34 +418,58 @@ __global__ void __launch_bounds__(kGemvMaxThreads) k_gemv_f64(int nb, int slab, 
   if (k < nb) part[(size_t)blockIdx.y * nb + k] = (acc0 + acc1) + (acc2 + acc3);
 }
 
-// FP32 matrix, FP32 products summed in 64-term chunks, chunks summed in FP64.
-__global__ void __launch_bounds__(kGemvMaxThreads) k_gemv_f32(int nb, int slab, int rpb, const float *__restrict__ B,
+// FP32 matrix (column-major, leading dimension ld = nb rounded up to 4, pad
+// rows zero): each thread owns 4 consecutive rows and reads them with one
+// float4 per column, 8 columns in flight; FP32 products are summed in 64-term
+// chunks and the chunks in FP64.
+__global__ void __launch_bounds__(kGemvMaxThreads) k_gemv_f32(int nb, int ld, int slab, int rpb4,
+                                                               const float *__restrict__ B,
                                                                const float *__restrict__ x, double *__restrict__ part) {
   __shared__ float xs[2048];
-  const int k = (threadIdx.x < rpb) ? blockIdx.x * rpb + threadIdx.x : nb;
+  const int r0 = blockIdx.x * rpb4 + 4 * threadIdx.x;   // first of this thread's 4 rows
+  const bool act = 4 * (int)threadIdx.x < rpb4 && r0 < nb;
   const int c0 = blockIdx.y * slab, c1 = min(nb, c0 + slab);
-  double acc = 0.0;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
   for (int cb = c0; cb < c1; cb += 2048) {
     const int ce = min(c1, cb + 2048);
     __syncthreads();
     for (int c = cb + threadIdx.x; c < ce; c += blockDim.x) xs[c - cb] = x[c];
     __syncthreads();
-    if (k < nb) {
-      const float *col = B + (size_t)cb * nb + k;
+    if (act) {
+      const float4 *col = reinterpret_cast<const float4 *>(B + (size_t)cb * ld + r0);
+      const size_t step = (size_t)ld / 4;
       int c = cb;
       while (c < ce) {
         const int cc = min(ce, c + 64);
-        float a0 = 0.f, a1 = 0.f;
-        for (; c + 1 < cc; c += 2, col += 2 * (size_t)nb) {
-          a0 = fmaf(col[0], xs[c - cb], a0);
-          a1 = fmaf(col[nb], xs[c - cb + 1], a1);
+        float a[4] = {0.f, 0.f, 0.f, 0.f}, b_[4] = {0.f, 0.f, 0.f, 0.f};
+        for (; c + 7 < cc; c += 8, col += 8 * step) {
+          float4 v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) v[u] = __ldg(col + u * step);
+#pragma unroll
+          for (int u = 0; u < 8; u += 2) {
+            const float xa = xs[c - cb + u], xb = xs[c - cb + u + 1];
+            a[0] = fmaf(v[u].x, xa, a[0]); a[1] = fmaf(v[u].y, xa, a[1]);
+            a[2] = fmaf(v[u].z, xa, a[2]); a[3] = fmaf(v[u].w, xa, a[3]);
+            b_[0] = fmaf(v[u + 1].x, xb, b_[0]); b_[1] = fmaf(v[u + 1].y, xb, b_[1]);
+            b_[2] = fmaf(v[u + 1].z, xb, b_[2]); b_[3] = fmaf(v[u + 1].w, xb, b_[3]);
+          }
         }
-        for (; c < cc; ++c, col += nb) a0 = fmaf(col[0], xs[c - cb], a0);
-        acc += (double)a0 + (double)a1;
+        for (; c < cc; ++c, col += step) {
+          const float4 v = __ldg(col);
+          const float xa = xs[c - cb];
+          a[0] = fmaf(v.x, xa, a[0]); a[1] = fmaf(v.y, xa, a[1]); a[2] = fmaf(v.z, xa, a[2]); a[3] = fmaf(v.w, xa, a[3]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] += (double)(a[q] + b_[q]);
       }
     }
   }
-  if (k < nb) part[(size_t)blockIdx.y * nb + k] = acc;
+  if (act) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (r0 + q < nb) part[(size_t)blockIdx.y * nb + r0 + q] = acc[q];
+  }
 }
 
 __global__ void k_slab_sum(int nb, int nslab, const double *__restrict__ part, double *__restrict__ y) {
@@ -824,6 +848,8 @@ int init_workspace(nmg_handle *h, std::string &err) {
     W.gemv_rpb = best_r;
     W.gemv_groups = nb > 0 ? (nb + best_r - 1) / best_r : 1;
     W.gemv_threads = ((best_r + 31) / 32) * 32;
+    W.gemv_rpb4 = ((best_r + 3) / 4) * 4;
+    W.gemv_threads32 = ((W.gemv_rpb4 / 4 + 31) / 32) * 32;
     W.gemv_slabs = best_s;
   }
   NMG_CUDA_TRY(W.bpart.alloc((size_t)W.gemv_slabs * (nb > 0 ? nb : 1) + (size_t)nb), "alloc gemv partials");
@@ -856,7 +882,7 @@ void bem_gemv(nmg_handle *h, const double *x, double *y) {
     float *x32 = reinterpret_cast<float *>(W.bpart.p + (size_t)slabs * nb);
     k_to_f32_vec<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, x, x32); ++h->launches;
     NMG_PROF_BEGIN(h, 0);
-    k_gemv_f32<<<grid, W.gemv_threads, 0, h->stream>>>(nb, slab, W.gemv_rpb, M.bem32, x32, W.bpart); ++h->launches;
+    k_gemv_f32<<<grid, W.gemv_threads32, 0, h->stream>>>(nb, M.ld32, slab, W.gemv_rpb4, M.bem32, x32, W.bpart); ++h->launches;
     NMG_PROF_END(h);
   } else {
     NMG_PROF_BEGIN(h, 0);
