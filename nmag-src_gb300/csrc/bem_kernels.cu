@@ -5,12 +5,14 @@
 // (src/bem3d_stubs.c:413-610) for every (surface triangle, observer row), then
 // adding Omega_i/(4 pi) - 1 on the diagonal (bem3d.ml:1040-1043).
 //
-// Layout: the matrix is stored column-major, bem[c*nb + k] = B[k][c] (k =
-// observer row, c = boundary column).  One thread owns one observer row and
-// walks the triangles in the reference's order, so every entry is accumulated
-// in exactly the reference's order with no atomics, and a warp's 32 rows are
-// adjacent in memory (coalesced read-modify-write).  Compiled with
-// --fmad=false to follow the written operation order.
+// Layout: the fill accumulates into a column-major buffer, a[c*nb + k] =
+// B[k][c] (k = observer row, c = boundary column).  One thread owns one
+// observer row and walks the triangles in the reference's order, so every
+// entry is accumulated in exactly the reference's order with no atomics, and a
+// warp's 32 rows are adjacent in memory (coalesced read-modify-write).  A tiled
+// transpose then stores the matrix row-major with the row stride padded to a
+// multiple of 8 (bem[k*ld + c]), the layout the matrix-vector product streams.
+// Compiled with --fmad=false to follow the written operation order.
 #include "nmg_internal.h"
 
 namespace nmg {
@@ -136,15 +138,27 @@ __global__ void __launch_bounds__(128) k_bem_fill(int nb, int ntri, const TriGeo
   bem[(size_t)k * nb + k] += solid_angle[k] / (4.0 * kPi) - 1.0;
 }
 
-// FP32 copy with the leading dimension padded to ld (pad rows zero).
-__global__ void k_to_f32(int nb, int ld, const double *__restrict__ a, float *__restrict__ b) {
-  const size_t n = (size_t)ld * nb;
+// Column-major fill buffer (a[c*nb + k]) -> row-major matrix with padded row
+// stride ld (b[k*ld + c], pad columns zero), 32x32 tiles through shared memory.
+__global__ void k_transpose_pad(int nb, int ld, const double *__restrict__ a, double *__restrict__ b) {
+  __shared__ double tile[32][33];
+  const int c0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int c = c0 + j, k = k0 + threadIdx.x;
+    tile[j][threadIdx.x] = (c < nb && k < nb) ? a[(size_t)c * nb + k] : 0.0;
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int k = k0 + j, c = c0 + threadIdx.x;
+    if (k < nb && c < ld) b[(size_t)k * ld + c] = tile[threadIdx.x][j];
+  }
+}
+
+// FP32 copy of the row-major matrix (same padded stride).
+__global__ void k_to_f32(size_t n, const double *__restrict__ a, float *__restrict__ b) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (; i < n; i += stride) {
-    const size_t c = i / ld, k = i % ld;
-    b[i] = k < (size_t)nb ? (float)a[c * nb + k] : 0.0f;
-  }
+  for (; i < n; i += stride) b[i] = (float)a[i];
 }
 
 }  // namespace
@@ -153,19 +167,33 @@ int fill_bem(nmg_handle *h, std::string &err) {
   Mesh &M = h->mesh;
   cudaStream_t s = h->stream;
   if (M.nb == 0) return 0;
+  const size_t nb = M.nb;
+  if (M.ld != (M.nb + 7) / 8 * 8) {
+    err = "BEM row stride not set up by the workspace";
+    return 3;
+  }
   NMG_CUDA_TRY(M.trigeo.alloc(M.ntri), "alloc trigeo");
   NMG_CUDA_TRY(M.obs_max.alloc(M.nb), "alloc obs_max");
-  NMG_CUDA_TRY(M.bem.alloc((size_t)M.nb * M.nb), "alloc BEM (nb^2 doubles)");
-  NMG_CUDA_TRY(cudaMemsetAsync(M.bem.p, 0, sizeof(double) * (size_t)M.nb * M.nb, s), "zero BEM");
-  k_tri_setup<<<(M.ntri + 127) / 128, 128, 0, s>>>(M.ntri, M.tri, M.tri_normal, M.node_of_b, M.coords, M.trigeo);
-  k_observer_prefix_max<<<1, 32, 0, s>>>(M.nb, M.node_of_b, M.coords, M.obs_max);
-  k_bem_fill<<<(M.nb + 127) / 128, 128, 0, s>>>(M.nb, M.ntri, M.trigeo, M.tri, M.node_of_b, M.coords, M.obs_max,
-                                                 M.solid_angle, M.bem);
-  NMG_CUDA_TRY(cudaGetLastError(), "bem fill launch");
+  {
+    // The fill accumulates column-major (coalesced, reference order) into a
+    // temporary; one tiled transpose then gives the row-major product layout.
+    DevBuf<double> colmajor;
+    NMG_CUDA_TRY(colmajor.alloc(nb * nb), "alloc BEM fill buffer (nb^2 doubles)");
+    NMG_CUDA_TRY(cudaMemsetAsync(colmajor.p, 0, sizeof(double) * nb * nb, s), "zero BEM");
+    k_tri_setup<<<(M.ntri + 127) / 128, 128, 0, s>>>(M.ntri, M.tri, M.tri_normal, M.node_of_b, M.coords, M.trigeo);
+    k_observer_prefix_max<<<1, 32, 0, s>>>(M.nb, M.node_of_b, M.coords, M.obs_max);
+    k_bem_fill<<<(M.nb + 127) / 128, 128, 0, s>>>(M.nb, M.ntri, M.trigeo, M.tri, M.node_of_b, M.coords, M.obs_max,
+                                                   M.solid_angle, colmajor);
+    NMG_CUDA_TRY(cudaGetLastError(), "bem fill launch");
+    NMG_CUDA_TRY(M.bem.alloc(nb * M.ld), "alloc BEM (nb x ld doubles)");
+    dim3 tb(32, 8), tg((M.ld + 31) / 32, (M.nb + 31) / 32);
+    k_transpose_pad<<<tg, tb, 0, s>>>(M.nb, M.ld, colmajor, M.bem);
+    NMG_CUDA_TRY(cudaGetLastError(), "bem transpose launch");
+    NMG_CUDA_TRY(cudaStreamSynchronize(s), "bem fill");
+  }
   if (h->opt.bem_precision == 1) {
-    M.ld32 = (M.nb + 3) / 4 * 4;
-    NMG_CUDA_TRY(M.bem32.alloc((size_t)M.ld32 * M.nb), "alloc FP32 BEM");
-    k_to_f32<<<h->sm_count * 8, 256, 0, s>>>(M.nb, M.ld32, M.bem, M.bem32);
+    NMG_CUDA_TRY(M.bem32.alloc(nb * M.ld), "alloc FP32 BEM");
+    k_to_f32<<<h->sm_count * 8, 256, 0, s>>>(nb * M.ld, M.bem, M.bem32);
   }
   NMG_CUDA_TRY(cudaStreamSynchronize(s), "bem fill");
   return 0;

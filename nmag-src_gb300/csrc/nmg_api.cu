@@ -137,15 +137,13 @@ int nmg_get_bem(const nmg_handle *h, double *out) {
   if (!h || !out) return -1;
   const nmg::Mesh &M = h->mesh;
   if (!M.bem.p) return fail(const_cast<nmg_handle *>(h), 2, "no BEM matrix (demag disabled)");
-  // stored column-major; transpose on the host into row-major
+  // stored row-major with padded row stride ld: one strided 2D copy
   const size_t nb = M.nb;
-  double *tmp = nullptr;
-  if (cudaMallocHost(&tmp, sizeof(double) * nb * nb) != cudaSuccess) return 100;
-  int rc = d2h(h, tmp, M.bem.p, sizeof(double) * nb * nb);
-  for (size_t c = 0; c < nb && !rc; ++c)
-    for (size_t k = 0; k < nb; ++k) out[k * nb + c] = tmp[c * nb + k];
-  cudaFreeHost(tmp);
-  return rc;
+  cudaError_t e = cudaMemcpy2DAsync(out, sizeof(double) * nb, M.bem.p, sizeof(double) * M.ld, sizeof(double) * nb, nb,
+                                    cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return fail(const_cast<nmg_handle *>(h), 100, std::string("BEM copy: ") + cudaGetErrorString(e));
+  return 0;
 }
 
 int nmg_set_m(nmg_handle *h, const double *m) {

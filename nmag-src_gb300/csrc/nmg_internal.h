@@ -55,9 +55,9 @@ struct Mesh {
   int N = 0, T = 0, nnz = 0, nb = 0, ntri = 0, nouter = 0;
   DevBuf<double> coords, dL, adet, K, G, D, vol, tri_normal, solid_angle;
   DevBuf<int32_t> tets, nt_ptr, nt_idx, nbr, row_ptr, col_idx, diag_pos, b_of_node, node_of_b, tri;
-  DevBuf<double> bem;      // FP64 BEM, column-major (bem[c*nb + k] = B[k][c])
-  DevBuf<float> bem32;     // FP32 copy (precision form), leading dimension ld32
-  int ld32 = 0;
+  DevBuf<double> bem;      // FP64 BEM, row-major with padded row stride ld (bem[k*ld + c] = B[k][c])
+  DevBuf<float> bem32;     // FP32 copy (precision form), same layout
+  int ld = 0;              // row stride: nb rounded up to a multiple of 8 (64-byte aligned FP64 rows)
   DevBuf<TriGeo> trigeo;
   DevBuf<double> obs_max;
 };
@@ -76,9 +76,13 @@ struct Workspace {
   int cg_blocks = 0;
   int cg_smem_bytes = 0;     // >0: shared-memory CG (one row per thread)
   int cg_nnz_cap = 0;
-  int gemv_slabs = 1;
-  int gemv_rpb = 256, gemv_groups = 1, gemv_threads = 256;   // GEMV row groups
-  int gemv_rpb4 = 256, gemv_threads32 = 64;                   // FP32 GEMV: 4 rows per thread
+  // BEM product decomposition: gemv_blocks blocks; each warp streams seg
+  // 32-byte units of the flattened row-major matrix and stores at most maxr
+  // row partials (index [0] FP64 matrix, [1] FP32 matrix)
+  int gemv_blocks = 1;
+  long long gemv_seg[2] = {1, 1};
+  int gemv_maxr[2] = {1, 1};
+  size_t gemv_x32_off = 0;   // offset (doubles) of the padded FP32 x inside bpart
 };
 
 struct Integrator;

@@ -387,102 +387,128 @@ __global__ void k_gather_b(int nb, const int32_t *__restrict__ node_of_b, const 
   if (b < nb) out[b] = phi[node_of_b[b]];
 }
 
-// y_part[s][k] = sum_{c in slab s} B[k][c] x[c]  (column-major B, FP64).
-// Grid: row groups of rpb rows (blockIdx.x) x column slabs (blockIdx.y); the
-// host picks the split so that the grid is exactly 4 blocks per SM with equal
-// work per block (no partial last wave).
-constexpr int kGemvMaxThreads = 512;
-__global__ void __launch_bounds__(kGemvMaxThreads) k_gemv_f64(int nb, int slab, int rpb, const double *__restrict__ B,
-                                                               const double *__restrict__ x, double *__restrict__ part) {
-  __shared__ double xs[1024];
-  const int k = (threadIdx.x < rpb) ? blockIdx.x * rpb + threadIdx.x : nb;
-  const int c0 = blockIdx.y * slab, c1 = min(nb, c0 + slab);
-  double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
-  for (int cb = c0; cb < c1; cb += 1024) {
-    const int ce = min(c1, cb + 1024);
-    __syncthreads();
-    for (int c = cb + threadIdx.x; c < ce; c += blockDim.x) xs[c - cb] = x[c];
-    __syncthreads();
-    if (k < nb) {
-      const double *col = B + (size_t)cb * nb + k;
-      int c = cb;
-      for (; c + 3 < ce; c += 4, col += 4 * (size_t)nb) {
-        acc0 = fma(col[0], xs[c - cb], acc0);
-        acc1 = fma(col[nb], xs[c - cb + 1], acc1);
-        acc2 = fma(col[2 * (size_t)nb], xs[c - cb + 2], acc2);
-        acc3 = fma(col[3 * (size_t)nb], xs[c - cb + 3], acc3);
-      }
-      for (; c < ce; ++c, col += nb) acc0 = fma(col[0], xs[c - cb], acc0);
-    }
-  }
-  if (k < nb) part[(size_t)blockIdx.y * nb + k] = (acc0 + acc1) + (acc2 + acc3);
-}
+// BEM product y = B x over the row-major matrix (row stride ld, a multiple of
+// 8; pad columns zero).  The matrix is streamed as one flat sequence of
+// 32-byte units (4 FP64 or 8 FP32 entries); warp w owns the contiguous unit
+// range [w*seg, (w+1)*seg), so every warp streams the same number of bytes
+// whatever nb is, with no partial last wave.  A warp's range crosses at most
+// a few row ends: per row it touches, the lanes' sums are combined by a fixed
+// shuffle tree and lane 0 stores one partial, part[w*maxr + (row - first row
+// of w)].  k_row_sum adds a row's partials in warp order, so the result is
+// deterministic for a given grid.
+constexpr int kGemvThreads = 256;
+constexpr int kGemvUnroll = 4;
 
-// FP32 matrix (column-major, leading dimension ld = nb rounded up to 4, pad
-// rows zero): each thread owns 4 consecutive rows and reads them with one
-// float4 per column, 8 columns in flight; FP32 products are summed in 64-term
-// chunks and the chunks in FP64.
-__global__ void __launch_bounds__(kGemvMaxThreads) k_gemv_f32(int nb, int ld, int slab, int rpb4,
-                                                               const float *__restrict__ B,
-                                                               const float *__restrict__ x, double *__restrict__ part) {
-  __shared__ float xs[2048];
-  const int r0 = blockIdx.x * rpb4 + 4 * threadIdx.x;   // first of this thread's 4 rows
-  const bool act = 4 * (int)threadIdx.x < rpb4 && r0 < nb;
-  const int c0 = blockIdx.y * slab, c1 = min(nb, c0 + slab);
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int cb = c0; cb < c1; cb += 2048) {
-    const int ce = min(c1, cb + 2048);
-    __syncthreads();
-    for (int c = cb + threadIdx.x; c < ce; c += blockDim.x) xs[c - cb] = x[c];
-    __syncthreads();
-    if (act) {
-      const float4 *col = reinterpret_cast<const float4 *>(B + (size_t)cb * ld + r0);
-      const size_t step = (size_t)ld / 4;
-      int c = cb;
-      while (c < ce) {
-        const int cc = min(ce, c + 64);
-        float a[4] = {0.f, 0.f, 0.f, 0.f}, b_[4] = {0.f, 0.f, 0.f, 0.f};
-        for (; c + 7 < cc; c += 8, col += 8 * step) {
-          float4 v[8];
+__global__ void __launch_bounds__(kGemvThreads) k_gemv_f64(int nb, int ld, long long seg, int maxr,
+                                                            const double *__restrict__ B,
+                                                            const double *__restrict__ x, double *__restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long Q = ld / 4, total = (long long)nb * Q;
+  const long long q0 = w * seg, q1 = min(total, q0 + seg);
+  if (q0 >= q1) return;
+  const long long rfirst = q0 / Q;
+  for (long long r = rfirst; r * Q < q1; ++r) {
+    const long long a = max(q0, r * Q), e = min(q1, (r + 1) * Q);
+    const double *row = B + r * (long long)ld;
+    double acc0 = 0.0, acc1 = 0.0;
+    long long q = a + lane;
+    for (; q + 32 * (kGemvUnroll - 1) < e; q += 32 * kGemvUnroll) {
+      double2 v[kGemvUnroll][2];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) v[u] = __ldg(col + u * step);
+      for (int u = 0; u < kGemvUnroll; ++u) {
+        const double2 *p = reinterpret_cast<const double2 *>(row + 4 * (q - r * Q + 32 * u));
+        v[u][0] = __ldcs(p);
+        v[u][1] = __ldcs(p + 1);
+      }
 #pragma unroll
-          for (int u = 0; u < 8; u += 2) {
-            const float xa = xs[c - cb + u], xb = xs[c - cb + u + 1];
-            a[0] = fmaf(v[u].x, xa, a[0]); a[1] = fmaf(v[u].y, xa, a[1]);
-            a[2] = fmaf(v[u].z, xa, a[2]); a[3] = fmaf(v[u].w, xa, a[3]);
-            b_[0] = fmaf(v[u + 1].x, xb, b_[0]); b_[1] = fmaf(v[u + 1].y, xb, b_[1]);
-            b_[2] = fmaf(v[u + 1].z, xb, b_[2]); b_[3] = fmaf(v[u + 1].w, xb, b_[3]);
-          }
-        }
-        for (; c < cc; ++c, col += step) {
-          const float4 v = __ldg(col);
-          const float xa = xs[c - cb];
-          a[0] = fmaf(v.x, xa, a[0]); a[1] = fmaf(v.y, xa, a[1]); a[2] = fmaf(v.z, xa, a[2]); a[3] = fmaf(v.w, xa, a[3]);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) acc[q] += (double)(a[q] + b_[q]);
+      for (int u = 0; u < kGemvUnroll; ++u) {
+        const int c = (int)(4 * (q - r * Q + 32 * u));
+        acc0 = fma(v[u][0].x, __ldg(x + min(c, nb - 1)), acc0);
+        acc1 = fma(v[u][0].y, __ldg(x + min(c + 1, nb - 1)), acc1);
+        acc0 = fma(v[u][1].x, __ldg(x + min(c + 2, nb - 1)), acc0);
+        acc1 = fma(v[u][1].y, __ldg(x + min(c + 3, nb - 1)), acc1);
       }
     }
-  }
-  if (act) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (r0 + q < nb) part[(size_t)blockIdx.y * nb + r0 + q] = acc[q];
+    for (; q < e; q += 32) {
+      const double2 *p = reinterpret_cast<const double2 *>(row + 4 * (q - r * Q));
+      const double2 v0 = __ldcs(p), v1 = __ldcs(p + 1);
+      const int c = (int)(4 * (q - r * Q));
+      acc0 = fma(v0.x, __ldg(x + min(c, nb - 1)), acc0);
+      acc1 = fma(v0.y, __ldg(x + min(c + 1, nb - 1)), acc1);
+      acc0 = fma(v1.x, __ldg(x + min(c + 2, nb - 1)), acc0);
+      acc1 = fma(v1.y, __ldg(x + min(c + 3, nb - 1)), acc1);
+    }
+    const double s = warp_sum(acc0 + acc1);
+    if (lane == 0) part[w * maxr + (r - rfirst)] = s;
   }
 }
 
-__global__ void k_slab_sum(int nb, int nslab, const double *__restrict__ part, double *__restrict__ y) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nb) return;
+// FP32 matrix, x32 zero-padded to ld: products summed in FP32 per 32-entry
+// group of a lane, groups summed in FP64.
+__global__ void __launch_bounds__(kGemvThreads) k_gemv_f32(int nb, int ld, long long seg, int maxr,
+                                                            const float *__restrict__ B,
+                                                            const float *__restrict__ x, double *__restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long Q = ld / 8, total = (long long)nb * Q;
+  const long long q0 = w * seg, q1 = min(total, q0 + seg);
+  if (q0 >= q1) return;
+  const long long rfirst = q0 / Q;
+  for (long long r = rfirst; r * Q < q1; ++r) {
+    const long long a = max(q0, r * Q), e = min(q1, (r + 1) * Q);
+    const float *row = B + r * (long long)ld;
+    double acc = 0.0;
+    long long q = a + lane;
+    for (; q + 32 * (kGemvUnroll - 1) < e; q += 32 * kGemvUnroll) {
+      float4 v[kGemvUnroll][2];
+#pragma unroll
+      for (int u = 0; u < kGemvUnroll; ++u) {
+        const float4 *p = reinterpret_cast<const float4 *>(row + 8 * (q - r * Q + 32 * u));
+        v[u][0] = __ldcs(p);
+        v[u][1] = __ldcs(p + 1);
+      }
+      float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+      for (int u = 0; u < kGemvUnroll; ++u) {
+        const float4 *px = reinterpret_cast<const float4 *>(x + 8 * (q - r * Q + 32 * u));
+        const float4 x0 = __ldg(px), x1 = __ldg(px + 1);
+        s0 = fmaf(v[u][0].x, x0.x, s0); s1 = fmaf(v[u][0].y, x0.y, s1);
+        s0 = fmaf(v[u][0].z, x0.z, s0); s1 = fmaf(v[u][0].w, x0.w, s1);
+        s0 = fmaf(v[u][1].x, x1.x, s0); s1 = fmaf(v[u][1].y, x1.y, s1);
+        s0 = fmaf(v[u][1].z, x1.z, s0); s1 = fmaf(v[u][1].w, x1.w, s1);
+      }
+      acc += (double)(s0 + s1);
+    }
+    for (; q < e; q += 32) {
+      const float4 *p = reinterpret_cast<const float4 *>(row + 8 * (q - r * Q));
+      const float4 *px = reinterpret_cast<const float4 *>(x + 8 * (q - r * Q));
+      const float4 v0 = __ldcs(p), v1 = __ldcs(p + 1), x0 = __ldg(px), x1 = __ldg(px + 1);
+      float s0 = v0.x * x0.x;
+      s0 = fmaf(v0.y, x0.y, s0); s0 = fmaf(v0.z, x0.z, s0); s0 = fmaf(v0.w, x0.w, s0);
+      s0 = fmaf(v1.x, x1.x, s0); s0 = fmaf(v1.y, x1.y, s0); s0 = fmaf(v1.z, x1.z, s0); s0 = fmaf(v1.w, x1.w, s0);
+      acc += (double)s0;
+    }
+    const double s = warp_sum(acc);
+    if (lane == 0) part[w * maxr + (r - rfirst)] = s;
+  }
+}
+
+// y[r] = sum of the partials of the warps whose unit range meets row r, in
+// warp order (Q = units per row).
+__global__ void k_row_sum(int nb, long long Q, long long seg, int maxr, long long nwarps,
+                          const double *__restrict__ part, double *__restrict__ y) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nb) return;
+  const long long w0 = (r * Q) / seg, w1 = min(nwarps - 1, ((r + 1) * Q - 1) / seg);
   double s = 0.0;
-  for (int j = 0; j < nslab; ++j) s += part[(size_t)j * nb + k];
-  y[k] = s;
+  for (long long w = w0; w <= w1; ++w) s += part[w * maxr + (r - (w * seg) / Q)];
+  y[r] = s;
 }
 
-__global__ void k_to_f32_vec(int n, const double *__restrict__ a, float *__restrict__ b) {
+__global__ void k_to_f32_vec(int n, int ld, const double *__restrict__ a, float *__restrict__ b) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) b[i] = (float)a[i];
+  if (i < ld) b[i] = i < n ? (float)a[i] : 0.0f;
 }
 
 // Dirichlet right-hand side (op_load_DBC, sign folded): interior rows
@@ -829,30 +855,29 @@ int init_workspace(nmg_handle *h, std::string &err) {
       return 4;
     }
   }
-  // GEMV slabs: about 4 blocks per SM in total.
-  // GEMV grid: (row groups) x (column slabs) = 4 blocks per SM exactly,
-  // slabs a divisor of that count, row groups of at most kGemvMaxThreads rows.
-  {
-    const int target = 4 * h->sm_count;
-    int best_s = 1, best_r = nb > 0 ? nb : 1;
-    double best_cost = 1e300;
-    for (int s_ = 1; s_ <= target; ++s_) {
-      if (target % s_) continue;
-      const int groups = target / s_;
-      const int rpb = nb > 0 ? (nb + groups - 1) / groups : 1;
-      if (rpb > kGemvMaxThreads || (nb > 0 && nb / s_ < 32)) continue;
-      // prefer ~256-row groups (coalesced, enough columns per slab)
-      const double cost = std::fabs(std::log((double)rpb / 256.0));
-      if (cost < best_cost) { best_cost = cost; best_s = s_; best_r = rpb; }
+  // BEM product grid: every resident warp streams an equal share of the
+  // flattened matrix (units of 32 bytes; rows of ld entries).
+  size_t part_n = 1;
+  M.ld = (nb + 7) / 8 * 8;   // row stride of the BEM matrix (fill_bem stores with it)
+  if (nb > 0) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemv_f64, kGemvThreads, 0);
+    int per_sm32 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm32, k_gemv_f32, kGemvThreads, 0);
+    per_sm = std::max(1, std::min(std::min(per_sm, per_sm32), 8));
+    W.gemv_blocks = per_sm * h->sm_count;
+    const long long warps = (long long)W.gemv_blocks * (kGemvThreads / 32);
+    for (int f = 0; f < 2; ++f) {
+      const long long Q = M.ld / (f == 0 ? 4 : 8), total = (long long)nb * Q;
+      const long long seg = std::max<long long>(1, (total + warps - 1) / warps);
+      W.gemv_seg[f] = seg;
+      W.gemv_maxr[f] = (int)((seg + Q - 1) / Q + 1);
+      part_n = std::max(part_n, (size_t)(warps * W.gemv_maxr[f]));
     }
-    W.gemv_rpb = best_r;
-    W.gemv_groups = nb > 0 ? (nb + best_r - 1) / best_r : 1;
-    W.gemv_threads = ((best_r + 31) / 32) * 32;
-    W.gemv_rpb4 = ((best_r + 3) / 4) * 4;
-    W.gemv_threads32 = ((W.gemv_rpb4 / 4 + 31) / 32) * 32;
-    W.gemv_slabs = best_s;
   }
-  NMG_CUDA_TRY(W.bpart.alloc((size_t)W.gemv_slabs * (nb > 0 ? nb : 1) + (size_t)nb), "alloc gemv partials");
+  // partials, then an FP32 copy of x padded to ld (ld/2 doubles of room)
+  W.gemv_x32_off = (part_n + 7) / 8 * 8;
+  NMG_CUDA_TRY(W.bpart.alloc(W.gemv_x32_off + (size_t)M.ld / 2 + 8), "alloc gemv partials");
   size_t red_n = 2 * 8 * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);  // 2 parities x 8 values
   NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
   NMG_CUDA_TRY(W.bar.alloc(W.cg_blocks + 2), "alloc barrier");
@@ -875,21 +900,24 @@ int init_workspace(nmg_handle *h, std::string &err) {
 void bem_gemv(nmg_handle *h, const double *x, double *y) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
-  const int nb = M.nb, slabs = W.gemv_slabs;
-  const int slab = (nb + slabs - 1) / slabs;
-  dim3 grid(W.gemv_groups, slabs);
-  if (h->opt.bem_precision == 1 && M.bem32.p) {
-    float *x32 = reinterpret_cast<float *>(W.bpart.p + (size_t)slabs * nb);
-    k_to_f32_vec<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, x, x32); ++h->launches;
+  const int nb = M.nb;
+  const int f = (h->opt.bem_precision == 1 && M.bem32.p) ? 1 : 0;
+  const long long seg = W.gemv_seg[f];
+  const int maxr = W.gemv_maxr[f];
+  if (f == 1) {
+    float *x32 = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
+    k_to_f32_vec<<<nblk(M.ld, 256), 256, 0, h->stream>>>(nb, M.ld, x, x32); ++h->launches;
     NMG_PROF_BEGIN(h, 0);
-    k_gemv_f32<<<grid, W.gemv_threads32, 0, h->stream>>>(nb, M.ld32, slab, W.gemv_rpb4, M.bem32, x32, W.bpart); ++h->launches;
+    k_gemv_f32<<<W.gemv_blocks, kGemvThreads, 0, h->stream>>>(nb, M.ld, seg, maxr, M.bem32, x32, W.bpart); ++h->launches;
     NMG_PROF_END(h);
   } else {
     NMG_PROF_BEGIN(h, 0);
-    k_gemv_f64<<<grid, W.gemv_threads, 0, h->stream>>>(nb, slab, W.gemv_rpb, M.bem, x, W.bpart); ++h->launches;
+    k_gemv_f64<<<W.gemv_blocks, kGemvThreads, 0, h->stream>>>(nb, M.ld, seg, maxr, M.bem, x, W.bpart); ++h->launches;
     NMG_PROF_END(h);
   }
-  k_slab_sum<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, slabs, W.bpart, y); ++h->launches;
+  k_row_sum<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, (long long)(M.ld / (f == 0 ? 4 : 8)), seg, maxr,
+                                                  (long long)W.gemv_blocks * (kGemvThreads / 32), W.bpart, y);
+  ++h->launches;
 }
 
 int check_device_error(nmg_handle *h, const char *where) {
