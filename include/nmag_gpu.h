@@ -154,6 +154,40 @@ int nmg_max_dm(nmg_handle *h, const double *m_prev, double *out);
 int nmg_rhs_device(nmg_handle *h, const double *d_m, double *d_dmdt);
 int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps);
 
+/* Differentiation form.  No counterpart in the reference, whose material
+ * constants are one scalar Ms and K1 per material (main.py:347-465); these
+ * entry points extend its RHS (nmag_lam.py:734-832) with per-element weights,
+ * all DEVICE arrays of n_tets doubles (NULL = all ones, or for kappa all
+ * zeros):
+ *   exchange  H_exch_i = -exch_coeff/V_i sum_j (sum_T wK_T K_T)_ij m_j
+ *   charge    rho_i = Ms sum_T wD_T int_T grad phi_i . m
+ *   anisotropy H_anis_i = c_i (a.m)(a - (a.m) m), c_i = sum_T kappa_T |T|/4 / V_i
+ * With wK = Ms/Ms_T, wD = Ms_T/Ms and kappa = 2 K1_T/(mu0 Ms_T) this is a
+ * per-element Ms_T and K1_T (wK = wD = 1 gives the plain model).  The weights
+ * apply to every later RHS evaluation (also nmg_ts_advance) until cleared. */
+int nmg_set_element_params(nmg_handle *h, const double *d_wK, const double *d_wD, const double *d_kappa,
+                           const double axis[3]);
+int nmg_clear_element_params(nmg_handle *h);
+
+/* Fixed-step RK4 trajectory from d_m0 (device, 3N) over nsteps steps of dt,
+ * with a checkpoint of m every ckpt_every steps kept on the device for
+ * nmg_rk4_adjoint.  The applied field of step n is the handle's H_ext plus
+ * the uniform pulse d_pulses[3k..3k+2] (device) with k = n / steps_per_pulse
+ * (no pulse once k >= n_pulses).  Writes m after the last step to d_m_final and,
+ * when d_avg_hist is not NULL, the volume average <m> after every step
+ * (nsteps x 3, device). */
+int nmg_rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ckpt_every, const double *d_pulses,
+                    int n_pulses, int steps_per_pulse, double *d_m_final, double *d_avg_hist);
+
+/* Discrete adjoint of the last nmg_rk4_forward on this handle: given the
+ * cotangents of m_final (3N) and of the <m> history (nsteps x 3; either may
+ * be NULL), writes the gradients with respect to m0 (3N), the element weights
+ * wK, wD, kappa (n_tets each) and the pulses (3 x n_pulses).  Output pointers
+ * may be NULL; all are device arrays.  Element parameters and H_ext must be
+ * those of the forward call. */
+int nmg_rk4_adjoint(nmg_handle *h, const double *d_m_final_bar, const double *d_avg_hist_bar, double *d_m0_bar,
+                    double *d_wK_bar, double *d_wD_bar, double *d_kappa_bar, double *d_pulses_bar);
+
 /* Wall-clock split of the last nmg_ts_advance / RHS work, in ms (CUDA events). */
 int nmg_get_timings(const nmg_handle *h, double out[8]);
 

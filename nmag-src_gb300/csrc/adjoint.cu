@@ -1,0 +1,726 @@
+// adjoint.cu -- differentiation form: per-element material parameters, a
+// fixed-step RK4 trajectory with checkpoints, and its discrete adjoint.
+//
+// The reference has one scalar Ms and K1 per material (interface/nmag/main.py:
+// 347-465, nmag_lam.py:377-470).  This file extends the same right-hand side
+// (nmag_lam.py:734-832) with per-element weights:
+//   H_exch_i = -c_exch / V_i * sum_j Kx_ij m_j,   Kx = sum_T wK_T K_T
+//   rho_i    = Ms * sum_T wD_T (|det_T|/24) dL_a(i) . sum_{b in T} m_b
+//            (= -Ms (Dx m)_i, the weak divergence int M . grad phi_i, whose
+//             rows sum to zero, so the Neumann problem stays consistent)
+//   H_anis_i = c_i (a.m)(a - (a.m) m),  c_i = sum_T (|det_T|/24) kappa_T / V_i
+// With wK = wD = 1 and kappa_T = 2K1/(mu0 Ms) this is the reference's model:
+// Kx equals K bit for bit, and Dx equals the reference's div operator D
+// (= -G^T) up to rounding.  The host maps (Ms_T, K1_T) to the weights
+// (wK = Ms/Ms_T, wD = Ms_T/Ms, kappa = 2 K1_T/(mu0 Ms_T)).
+//
+// Discrete adjoint of  m_{n+1} = m_n + dt/6 (k1 + 2k2 + 2k3 + k4):
+//   kb4 = dt/6 lam,           ub4 = J(u4)^T kb4
+//   kb3 = dt/3 lam + dt ub4,  ub3 = J(u3)^T kb3
+//   kb2 = dt/3 lam + dt/2 ub3, ub2 = J(u2)^T kb2
+//   kb1 = dt/6 lam + dt/2 ub2, ub1 = J(u1)^T kb1
+//   lam_n = lam + ub1 + ub2 + ub3 + ub4
+// J^T is the exact transpose of the discrete RHS: LLG and anisotropy per
+// node, exchange through Kx (symmetric), demag backwards through grad phi
+// (G^T), the Dirichlet solve (K_II symmetric), the BEM (B^T) and the
+// Neumann solve (K symmetric on the mean-zero space; constants drop out
+// because the rows of Dx sum to zero).  The trajectory is kept as a
+// checkpoint every `ckpt` steps; the backward pass recomputes one segment
+// at a time and stores its stage states and fields.  The CG warm starts
+// are reset at every checkpoint, so a recomputed segment reproduces the
+// forward pass bit for bit.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "nmg_internal.h"
+
+namespace nmg {
+
+struct Tape {
+  int nsteps = 0, ckpt = 0, npulses = 0, spp = 0, n3 = 0;
+  double dt = 0.0;
+  DevBuf<double> ckpts;          // (nsteps/ckpt + 1) x 3N
+  DevBuf<double> su, sH;         // ckpt x 4 x 3N stage states and total fields
+  DevBuf<double> k, y, m;        // 4 x 3N stage slopes, stage state, running m
+  DevBuf<double> lam, kb, ub, acc;
+  DevBuf<double> hbase, pulses;  // 3N, 3 x npulses
+  DevBuf<double> Hbar, sanis, hsum, phibar, rhs, z, y2b, y1b, rhobar, tpart, avgpart, vt;
+  int t_groups = 1, t_slabs = 1, t_rows = 1;
+};
+
+namespace {
+
+inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
+constexpr int kT = 256;
+constexpr int kAvgBlocks = 64;
+
+__device__ __forceinline__ int find_col(const int32_t *__restrict__ cols, int lo, int hi, int c) {
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (cols[mid] < c) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ double wsum(double v) {
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Weighted operator values, one row per thread, tets ascending (the order of
+// the plain assembly, so wK = 1 reproduces K exactly).
+__global__ void k_elem_values(int N, int nnz, const int32_t *__restrict__ tets, const int32_t *__restrict__ ptr,
+                              const int32_t *__restrict__ idx, const double *__restrict__ dL,
+                              const double *__restrict__ adet, const double *__restrict__ vol,
+                              const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col_idx,
+                              const double *__restrict__ wK, const double *__restrict__ wD,
+                              const double *__restrict__ kappa, double *__restrict__ Kx, double *__restrict__ Dx,
+                              double *__restrict__ anis) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int lo = row_ptr[i], hi = row_ptr[i + 1];
+  for (int k = lo; k < hi; ++k) {
+    Kx[k] = 0.0;
+    for (int d = 0; d < 3; ++d) Dx[(size_t)d * nnz + k] = 0.0;
+  }
+  double an = 0.0;
+  for (int q = ptr[i]; q < ptr[i + 1]; ++q) {
+    const int t = idx[q];
+    const int32_t *v = tets + 4 * (size_t)t;
+    const double *g = dL + 12 * (size_t)t;
+    const double ad = adet[t];
+    int a = 0;
+    while (a < 3 && v[a] != i) ++a;
+    const double kc = ad / 6.0, gc = ad / 24.0;
+    const double wk = wK ? wK[t] : 1.0, wd = wD ? wD[t] : 1.0;
+    for (int b = 0; b < 4; ++b) {
+      const int pos = find_col(col_idx, lo, hi, v[b]);
+      if (pos >= hi || col_idx[pos] != v[b]) continue;
+      Kx[pos] += wk * (kc * ((g[3 * a] * g[3 * b] + g[3 * a + 1] * g[3 * b + 1]) + g[3 * a + 2] * g[3 * b + 2]));
+      for (int d = 0; d < 3; ++d) Dx[(size_t)d * nnz + pos] -= wd * (gc * g[3 * a + d]);
+    }
+    if (kappa) an += gc * kappa[t];
+  }
+  anis[i] = an / vol[i];
+}
+
+// tpos[k] = position of entry (j, i) for entry k = (i, j) (symmetric pattern).
+__global__ void k_tpos(int N, const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col_idx,
+                       int32_t *__restrict__ tpos) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+    const int j = col_idx[k];
+    const int p = find_col(col_idx, row_ptr[j], row_ptr[j + 1], i);
+    tpos[k] = (p < row_ptr[j + 1] && col_idx[p] == i) ? p : k;   // the pattern is symmetric; never out of range
+  }
+}
+
+__global__ void k_hext(int n3, const double *__restrict__ base, const double *__restrict__ pulse,
+                       double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n3) out[i] = pulse ? base[i] + pulse[i % 3] : base[i];
+}
+
+__global__ void k_stage(int n, const double *__restrict__ m, double c, const double *__restrict__ k,
+                        double *__restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = m[i] + c * k[i];
+}
+
+// m += dt/6 (k1 + 2 k2 + 2 k3 + k4)
+__global__ void k_rk4_update(int n, double dt, const double *__restrict__ k, double *__restrict__ m) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) m[i] += (dt / 6.0) * (((k[i] + 2.0 * k[n + i]) + 2.0 * k[2 * (size_t)n + i]) + k[3 * (size_t)n + i]);
+}
+
+// Volume-weighted sums of m (3) and V per block, then the ordered total.
+__global__ void k_avg_part(int N, const double *__restrict__ m, const double *__restrict__ vol,
+                           double *__restrict__ part) {
+  __shared__ double sm[4][32];
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const double V = vol[i];
+    v[0] += V;
+    for (int d = 0; d < 3; ++d) v[1 + d] += V * m[3 * (size_t)i + d];
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j = 0; j < 4; ++j) {
+    const double s = wsum(v[j]);
+    if (lane == 0) sm[j][w] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += sm[threadIdx.x][q];
+    part[4 * blockIdx.x + threadIdx.x] = s;
+  }
+}
+
+__global__ void k_avg_final(int nparts, const double *__restrict__ part, double *__restrict__ avg3,
+                            double *__restrict__ vt) {
+  if (threadIdx.x != 0) return;
+  double t[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int b = 0; b < nparts; ++b)
+    for (int j = 0; j < 4; ++j) t[j] += part[4 * b + j];
+  for (int d = 0; d < 3; ++d) avg3[d] = t[1 + d] / t[0];
+  if (vt) vt[0] = t[0];
+}
+
+// lam_i += hbar . V_i / sum V   (cotangent of <m> after a step)
+__global__ void k_hist_inject(int N, const double *__restrict__ vol, const double *__restrict__ vt,
+                              const double *__restrict__ hb, double *__restrict__ lam) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double w = vol[i] / vt[0];
+  for (int d = 0; d < 3; ++d) lam[3 * (size_t)i + d] += hb[d] * w;
+}
+
+struct VjpArgs {
+  int N, anis_on;
+  const double *u, *H, *kb, *anis_node;
+  double C1, C2, C3, anis, ax, ay, az;
+  double *ub, *Hb, *sanis, *hsum;
+};
+
+// Per node: ub = (df/du)^T kb with H fixed (+ the anisotropy term),
+// Hb = (df/dH)^T kb, sanis = Hb . h_anis(u) / c, block sums of Hb.
+__global__ void __launch_bounds__(kT) k_llg_vjp(VjpArgs a) {
+  __shared__ double sm[3][kT / 32];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double hb[3] = {0.0, 0.0, 0.0};
+  if (i < a.N) {
+    const double *u = a.u + 3 * (size_t)i, *H = a.H + 3 * (size_t)i, *g = a.kb + 3 * (size_t)i;
+    const double uH = (u[0] * H[0] + u[1] * H[1]) + u[2] * H[2];
+    const double ug = (u[0] * g[0] + u[1] * g[1]) + u[2] * g[2];
+    const double Hg = (H[0] * g[0] + H[1] * g[1]) + H[2] * g[2];
+    const double uu = (u[0] * u[0] + u[1] * u[1]) + u[2] * u[2];
+    const double Hxg[3] = {H[1] * g[2] - H[2] * g[1], H[2] * g[0] - H[0] * g[2], H[0] * g[1] - H[1] * g[0]};
+    double ub[3];
+    for (int d = 0; d < 3; ++d) {
+      ub[d] = a.C1 * Hxg[d] + a.C2 * ((g[d] * uH + H[d] * ug) - 2.0 * u[d] * Hg) +
+              a.C3 * ((1.0 - uu) * g[d] - 2.0 * u[d] * ug);
+    }
+    const double gxu[3] = {g[1] * u[2] - g[2] * u[1], g[2] * u[0] - g[0] * u[2], g[0] * u[1] - g[1] * u[0]};
+    for (int d = 0; d < 3; ++d) hb[d] = a.C1 * gxu[d] + a.C2 * (u[d] * ug - g[d] * uu);
+    double s_an = 0.0;
+    if (a.anis_on) {
+      const double c = a.anis_node ? a.anis_node[i] : a.anis;
+      const double ax[3] = {a.ax, a.ay, a.az};
+      const double am = (ax[0] * u[0] + ax[1] * u[1]) + ax[2] * u[2];
+      double t = 0.0;
+      for (int d = 0; d < 3; ++d) {
+        t += hb[d] * (ax[d] - 2.0 * am * u[d]);
+        s_an += hb[d] * (am * (ax[d] - am * u[d]));
+      }
+      for (int d = 0; d < 3; ++d) ub[d] += c * (t * ax[d] - am * am * hb[d]);
+    }
+    for (int d = 0; d < 3; ++d) {
+      a.ub[3 * (size_t)i + d] = ub[d];
+      a.Hb[3 * (size_t)i + d] = hb[d];
+    }
+    if (a.sanis) a.sanis[i] = s_an;
+  }
+  if (a.hsum) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int d = 0; d < 3; ++d) {
+      const double s = wsum(hb[d]);
+      if (lane == 0) sm[d][w] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      double s = 0.0;
+      for (int q = 0; q < kT / 32; ++q) s += sm[threadIdx.x][q];
+      a.hsum[3 * blockIdx.x + threadIdx.x] = s;
+    }
+  }
+}
+
+__global__ void k_pulse_acc(int nparts, const double *__restrict__ hsum, double *__restrict__ pbar) {
+  if (threadIdx.x >= 3) return;
+  double s = 0.0;
+  for (int b = 0; b < nparts; ++b) s += hsum[3 * b + threadIdx.x];
+  pbar[threadIdx.x] += s;
+}
+
+// ub += -c_exch Kx (Hb / V) (Kx symmetric); phibar = -sum_c G_c^T (Hb_c / V).
+__global__ void k_adj_spmv(int N, int nnz, const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col_idx,
+                           const int32_t *__restrict__ tpos, const double *__restrict__ Kx,
+                           const double *__restrict__ G, const double *__restrict__ vol,
+                           const double *__restrict__ Hb, double c_exch, int do_demag, double *__restrict__ ub,
+                           double *__restrict__ phibar) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, p = 0.0;
+  for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+    const int j = col_idx[k];
+    const double *hj = Hb + 3 * (size_t)j;
+    const double iv = 1.0 / vol[j];
+    const double h0 = hj[0] * iv, h1 = hj[1] * iv, h2 = hj[2] * iv;
+    const double kv = Kx[k];
+    s0 += kv * h0; s1 += kv * h1; s2 += kv * h2;
+    if (do_demag) {
+      const int tk = tpos[k];
+      p += (G[tk] * h0 + G[(size_t)nnz + tk] * h1) + G[2 * (size_t)nnz + tk] * h2;
+    }
+  }
+  ub[3 * (size_t)i] -= c_exch * s0;
+  ub[3 * (size_t)i + 1] -= c_exch * s1;
+  ub[3 * (size_t)i + 2] -= c_exch * s2;
+  if (do_demag) phibar[i] = -p;
+}
+
+// Adjoint Dirichlet system: interior rows phibar, boundary rows 0 (and a
+// zero boundary warm start).
+__global__ void k_adj_dbc(int N, const int32_t *__restrict__ b_of_node, const double *__restrict__ phibar,
+                          double *__restrict__ rhs, double *__restrict__ z) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const bool bnd = b_of_node[i] >= 0;
+  rhs[i] = bnd ? 0.0 : phibar[i];
+  if (bnd) z[i] = 0.0;
+}
+
+// phibar2b_j = phibar_n - (K_BI z_I)_n, n = node_of_b[j]
+__global__ void k_adj_bnd(int nb, const int32_t *__restrict__ node_of_b, const int32_t *__restrict__ b_of_node,
+                          const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col_idx,
+                          const double *__restrict__ K, const double *__restrict__ z,
+                          const double *__restrict__ phibar, double *__restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nb) return;
+  const int n = node_of_b[j];
+  double s = 0.0;
+  for (int k = row_ptr[n]; k < row_ptr[n + 1]; ++k) {
+    const int c = col_idx[k];
+    if (b_of_node[c] < 0) s += K[k] * z[c];
+  }
+  out[j] = phibar[n] - s;
+}
+
+// B^T y over the row-major BEM: warp (group g, slab s) owns 128 columns
+// (one 4-column quad per lane) and the rows of slab s; part[s][c].
+__global__ void __launch_bounds__(kT) k_gemv_t_f64(int nb, int ld, int groups, int slabs, int rows,
+                                                    const double *__restrict__ B, const double *__restrict__ y,
+                                                    double *__restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int g = (int)(w % groups), sl = (int)(w / groups);
+  const int Q = ld / 4, q = g * 32 + lane;
+  if (sl >= slabs || q >= Q) return;
+  const int k0 = sl * rows, k1 = min(nb, k0 + rows);
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int k = k0;
+  for (; k + 3 < k1; k += 4) {
+    double2 v[4][2];
+    double yk[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const double2 *p = reinterpret_cast<const double2 *>(B + (size_t)(k + u) * ld + 4 * (size_t)q);
+      v[u][0] = __ldcs(p);
+      v[u][1] = __ldcs(p + 1);
+      yk[u] = __ldg(y + k + u);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a0 = fma(v[u][0].x, yk[u], a0); a1 = fma(v[u][0].y, yk[u], a1);
+      a2 = fma(v[u][1].x, yk[u], a2); a3 = fma(v[u][1].y, yk[u], a3);
+    }
+  }
+  for (; k < k1; ++k) {
+    const double2 *p = reinterpret_cast<const double2 *>(B + (size_t)k * ld + 4 * (size_t)q);
+    const double2 v0 = __ldcs(p), v1 = __ldcs(p + 1);
+    const double yv = __ldg(y + k);
+    a0 = fma(v0.x, yv, a0); a1 = fma(v0.y, yv, a1); a2 = fma(v1.x, yv, a2); a3 = fma(v1.y, yv, a3);
+  }
+  double *o = part + (size_t)sl * ld + 4 * (size_t)q;
+  o[0] = a0; o[1] = a1; o[2] = a2; o[3] = a3;
+}
+
+__global__ void k_col_sum(int nb, int ld, int slabs, const double *__restrict__ part, double *__restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nb) return;
+  double s = 0.0;
+  for (int sl = 0; sl < slabs; ++sl) s += part[(size_t)sl * ld + c];
+  out[c] = s;
+}
+
+// Neumann adjoint right-hand side: phibar + scatter(B^T phibar2b)
+__global__ void k_adj_scatter(int N, const int32_t *__restrict__ b_of_node, const double *__restrict__ phibar,
+                              const double *__restrict__ y1b, double *__restrict__ rhs) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int b = b_of_node[i];
+  rhs[i] = phibar[i] + (b >= 0 ? y1b[b] : 0.0);
+}
+
+// ub_j += -Ms sum_i Dx_d[i][j] rhobar_i
+__global__ void k_adj_div(int N, int nnz, double Ms, const int32_t *__restrict__ row_ptr,
+                          const int32_t *__restrict__ col_idx, const int32_t *__restrict__ tpos,
+                          const double *__restrict__ Dx, const double *__restrict__ rhobar, double *__restrict__ ub) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+    const int tk = tpos[k];
+    const double r = rhobar[col_idx[k]];
+    s0 += Dx[tk] * r; s1 += Dx[(size_t)nnz + tk] * r; s2 += Dx[2 * (size_t)nnz + tk] * r;
+  }
+  ub[3 * (size_t)i] -= Ms * s0;
+  ub[3 * (size_t)i + 1] -= Ms * s1;
+  ub[3 * (size_t)i + 2] -= Ms * s2;
+}
+
+// Per-element parameter cotangents of one stage (one thread per tet, no atomics).
+__global__ void k_elem_grad(int T, const int32_t *__restrict__ tets, const double *__restrict__ dL,
+                            const double *__restrict__ adet, const double *__restrict__ vol,
+                            const double *__restrict__ u, const double *__restrict__ Hb,
+                            const double *__restrict__ rhobar, const double *__restrict__ sanis, double c_exch,
+                            double Ms, double *__restrict__ gwK, double *__restrict__ gwD,
+                            double *__restrict__ gkap) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int32_t *v = tets + 4 * (size_t)t;
+  const double *g = dL + 12 * (size_t)t;
+  const double ad = adet[t], kc = ad / 6.0, gc = ad / 24.0;
+  if (gwK) {
+    double acc = 0.0;
+    for (int a = 0; a < 4; ++a) {
+      const double *ha = Hb + 3 * (size_t)v[a];
+      const double iva = 1.0 / vol[v[a]];
+      for (int b = 0; b < 4; ++b) {
+        const double *ubv = u + 3 * (size_t)v[b];
+        const double kab = kc * ((g[3 * a] * g[3 * b] + g[3 * a + 1] * g[3 * b + 1]) + g[3 * a + 2] * g[3 * b + 2]);
+        acc += kab * ((ha[0] * ubv[0] + ha[1] * ubv[1]) + ha[2] * ubv[2]) * iva;
+      }
+    }
+    gwK[t] += -c_exch * acc;
+  }
+  if (gwD && rhobar) {
+    double us[3] = {0.0, 0.0, 0.0};
+    for (int b = 0; b < 4; ++b)
+      for (int d = 0; d < 3; ++d) us[d] += u[3 * (size_t)v[b] + d];
+    double acc = 0.0;
+    for (int a = 0; a < 4; ++a)
+      acc += rhobar[v[a]] * ((g[3 * a] * us[0] + g[3 * a + 1] * us[1]) + g[3 * a + 2] * us[2]);
+    gwD[t] += Ms * gc * acc;
+  }
+  if (gkap && sanis) {
+    double acc = 0.0;
+    for (int a = 0; a < 4; ++a) acc += sanis[v[a]] / vol[v[a]];
+    gkap[t] += gc * acc;
+  }
+}
+
+// kb = ca lam + cb ub ; acc += ub
+__global__ void k_adj_combine(int n, const double *__restrict__ lam, const double *__restrict__ ub, double ca,
+                              double cb, double *__restrict__ kb, double *__restrict__ acc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double u = ub ? ub[i] : 0.0;
+  kb[i] = ca * lam[i] + cb * u;
+  if (ub) acc[i] += u;
+}
+
+__global__ void k_add_to(int n, const double *__restrict__ x, double *__restrict__ y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] += x[i];
+}
+
+#define ADJ_TRY(call)                 \
+  do {                                \
+    int rc__ = (call);                \
+    if (rc__) return rc__;            \
+  } while (0)
+
+inline int launched(nmg_handle *h, const char *what) {
+  ++h->launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    h->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return 100;
+  }
+  return 0;
+}
+
+// Reset the forward solves' warm starts (bases and the phi buffers).
+void reset_forward_solves(nmg_handle *h) {
+  cg_reset_basis(h, 0);
+  cg_reset_basis(h, 1);
+  cudaMemsetAsync(h->ws.phi1.p, 0, sizeof(double) * h->mesh.N, h->stream);
+  cudaMemsetAsync(h->ws.phi2.p, 0, sizeof(double) * h->mesh.N, h->stream);
+}
+
+void set_step_field(nmg_handle *h, Tape &T, int n) {
+  const double *pulse = nullptr;
+  if (T.npulses > 0 && T.spp > 0 && n / T.spp < T.npulses) pulse = T.pulses.p + 3 * (size_t)(n / T.spp);
+  k_hext<<<nblk(T.n3, kT), kT, 0, h->stream>>>(T.n3, T.hbase, pulse, h->ws.h_ext);
+  ++h->launches;
+}
+
+// One RK4 step of m (in place); stage states and fields stored when su/sH given.
+int rk4_step(nmg_handle *h, Tape &T, double *m, double *su, double *sH) {
+  const int n = T.n3;
+  cudaStream_t s = h->stream;
+  double *k = T.k.p;
+  const double cs[4] = {0.0, 0.5 * T.dt, 0.5 * T.dt, T.dt};
+  for (int st = 0; st < 4; ++st) {
+    const double *u = m;
+    if (st > 0) {
+      k_stage<<<nblk(n, kT), kT, 0, s>>>(n, m, cs[st], k + (size_t)(st - 1) * n, T.y);
+      ADJ_TRY(launched(h, "rk4 stage"));
+      u = T.y;
+    }
+    if (rhs_eval(h, u, k + (size_t)st * n)) return 100;
+    if (su) {
+      cudaMemcpyAsync(su + (size_t)st * n, u, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(sH + (size_t)st * n, h->ws.h_total.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    }
+  }
+  k_rk4_update<<<nblk(n, kT), kT, 0, s>>>(n, T.dt, k, m);
+  return launched(h, "rk4 update");
+}
+
+struct GradOut {
+  double *gwK, *gwD, *gkap, *gpul;
+};
+
+// ub = J(u)^T kb at a stored stage (u, H); parameter cotangents accumulated.
+int stage_vjp(nmg_handle *h, Tape &T, const double *u, const double *H, const double *kb, double *ub, int step,
+              const GradOut &G) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  const nmg_material &mt = h->mat;
+  cudaStream_t s = h->stream;
+  const int N = M.N;
+  const int demag = (h->opt.do_demag && M.nb > 0) ? 1 : 0;
+  const int nparts = nblk(N, kT);
+  VjpArgs a;
+  a.N = N;
+  a.anis_on = (h->ep.active || mt.K1 != 0.0) ? 1 : 0;
+  a.u = u; a.H = H; a.kb = kb; a.anis_node = h->ep.active ? h->ep.anis.p : nullptr;
+  a.C1 = mt.C1; a.C2 = mt.C2; a.C3 = mt.C3; a.anis = mt.anis_coeff;
+  a.ax = h->ep.active ? h->ep.axis[0] : mt.axis[0];
+  a.ay = h->ep.active ? h->ep.axis[1] : mt.axis[1];
+  a.az = h->ep.active ? h->ep.axis[2] : mt.axis[2];
+  a.ub = ub; a.Hb = T.Hbar; a.sanis = T.sanis; a.hsum = G.gpul ? T.hsum.p : nullptr;
+  k_llg_vjp<<<nparts, kT, 0, s>>>(a);
+  ADJ_TRY(launched(h, "llg vjp"));
+  if (G.gpul && T.npulses > 0 && T.spp > 0 && step / T.spp < T.npulses) {
+    k_pulse_acc<<<1, 32, 0, s>>>(nparts, T.hsum, G.gpul + 3 * (size_t)(step / T.spp));
+    ADJ_TRY(launched(h, "pulse cotangent"));
+  }
+  k_adj_spmv<<<nblk(N, kT), kT, 0, s>>>(N, M.nnz, M.row_ptr, M.col_idx, h->ep.tpos, h->exch_K(), M.G, M.vol, T.Hbar,
+                                        mt.exch_coeff, demag, ub, T.phibar);
+  ADJ_TRY(launched(h, "exchange/grad adjoint"));
+  if (demag) {
+    k_adj_dbc<<<nblk(N, kT), kT, 0, s>>>(N, M.b_of_node, T.phibar, T.rhs, T.z);
+    ADJ_TRY(launched(h, "adjoint dirichlet rhs"));
+    if (cg_solve(h, 3, T.rhs, T.z, h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)) return 100;
+    k_adj_bnd<<<nblk(M.nb, kT), kT, 0, s>>>(M.nb, M.node_of_b, M.b_of_node, M.row_ptr, M.col_idx, M.K, T.z, T.phibar,
+                                           T.y2b);
+    ADJ_TRY(launched(h, "adjoint boundary"));
+    k_gemv_t_f64<<<nblk((long long)T.t_groups * T.t_slabs * 32, kT), kT, 0, s>>>(M.nb, M.ld, T.t_groups, T.t_slabs,
+                                                                                  T.t_rows, M.bem, T.y2b, T.tpart);
+    ADJ_TRY(launched(h, "BEM transpose product"));
+    k_col_sum<<<nblk(M.nb, kT), kT, 0, s>>>(M.nb, M.ld, T.t_slabs, T.tpart, T.y1b);
+    ADJ_TRY(launched(h, "BEM transpose sum"));
+    k_adj_scatter<<<nblk(N, kT), kT, 0, s>>>(N, M.b_of_node, T.phibar, T.y1b, T.rhs);
+    ADJ_TRY(launched(h, "adjoint neumann rhs"));
+    if (cg_solve(h, 2, T.rhs, T.rhobar, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
+    k_adj_div<<<nblk(N, kT), kT, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, h->ep.tpos,
+                                         h->ep.active ? h->ep.Dx.p : M.D.p, T.rhobar, ub);
+    ADJ_TRY(launched(h, "div adjoint"));
+  }
+  if (G.gwK || G.gwD || G.gkap) {
+    k_elem_grad<<<nblk(M.T, kT), kT, 0, s>>>(M.T, M.tets, M.dL, M.adet, M.vol, u, T.Hbar,
+                                             demag ? T.rhobar.p : nullptr, T.sanis, mt.exch_coeff, mt.Ms, G.gwK,
+                                             G.gwD, G.gkap);
+    ADJ_TRY(launched(h, "element cotangents"));
+  }
+  return 0;
+}
+
+}  // namespace
+
+void tape_free(nmg_handle *h) {
+  delete h->tape;
+  h->tape = nullptr;
+}
+
+int ensure_tpos(nmg_handle *h) {
+  Mesh &M = h->mesh;
+  if (h->ep.tpos.p) return 0;
+  if (h->ep.tpos.alloc(M.nnz)) return 100;
+  k_tpos<<<nblk(M.N, kT), kT, 0, h->stream>>>(M.N, M.row_ptr, M.col_idx, h->ep.tpos);
+  return launched(h, "transpose positions");
+}
+
+int set_element_params(nmg_handle *h, const double *wK, const double *wD, const double *kappa, const double axis[3]) {
+  Mesh &M = h->mesh;
+  ElemParams &E = h->ep;
+  if (!E.Kx.p && (E.Kx.alloc(M.nnz) || E.Dx.alloc(3 * (size_t)M.nnz) || E.anis.alloc(M.N))) {
+    h->last_error = "element parameters: device allocation failed";
+    return 100;
+  }
+  double n2 = axis[0] * axis[0] + axis[1] * axis[1] + axis[2] * axis[2];
+  if (!(n2 > 0.0)) {
+    h->last_error = "element parameters: the anisotropy axis is zero";
+    return -2;
+  }
+  ADJ_TRY(ensure_tpos(h));
+  k_elem_values<<<nblk(M.N, 128), 128, 0, h->stream>>>(M.N, M.nnz, M.tets, M.nt_ptr, M.nt_idx, M.dL, M.adet, M.vol,
+                                                       M.row_ptr, M.col_idx, wK, wD, kappa, E.Kx, E.Dx, E.anis);
+  ADJ_TRY(launched(h, "element parameter assembly"));
+  const double inv = 1.0 / std::sqrt(n2);
+  for (int d = 0; d < 3; ++d) E.axis[d] = axis[d] * inv;
+  E.active = 1;
+  h->ts_ready = 0;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    h->last_error = "element parameter assembly failed";
+    return 100;
+  }
+  return 0;
+}
+
+int rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ckpt, const double *d_pulses,
+                int npulses, int spp, double *d_mT, double *d_hist) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  cudaStream_t s = h->stream;
+  const int n3 = 3 * M.N;
+  if (!h->tape) h->tape = new Tape();
+  Tape &T = *h->tape;
+  const bool same = T.n3 == n3 && T.ckpt == ckpt && T.nsteps == nsteps && T.npulses == npulses;
+  T.nsteps = nsteps; T.ckpt = ckpt; T.npulses = npulses; T.spp = spp; T.dt = dt; T.n3 = n3;
+  if (!same) {
+    const int ncp = nsteps / ckpt + 1;
+    T.su.release();   // stage storage is sized by ckpt: the adjoint reallocates it
+    T.sH.release();
+    if (T.ckpts.alloc((size_t)ncp * n3) || T.k.alloc(4 * (size_t)n3) || T.y.alloc(n3) || T.m.alloc(n3) ||
+        T.hbase.alloc(n3) || T.pulses.alloc(3 * (size_t)std::max(npulses, 1)) ||
+        T.avgpart.alloc(4 * kAvgBlocks + 4) || T.vt.alloc(1)) {
+      h->last_error = "rk4 tape: device allocation failed";
+      return 100;
+    }
+    // B^T decomposition: 32 quads per warp x row slabs, about 64 warps per SM
+    if (M.ld > 0) {
+      T.t_groups = (M.ld / 4 + 31) / 32;
+      const int target = 64 * h->sm_count;
+      int slabs = std::max(1, std::min(M.nb, target / std::max(1, T.t_groups)));
+      T.t_rows = (M.nb + slabs - 1) / slabs;
+      T.t_slabs = (M.nb + T.t_rows - 1) / T.t_rows;
+      if (T.tpart.alloc((size_t)T.t_slabs * M.ld)) return 100;
+    }
+  }
+  cudaMemcpyAsync(T.hbase.p, W.h_ext.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);
+  if (npulses > 0) cudaMemcpyAsync(T.pulses.p, d_pulses, sizeof(double) * 3 * npulses, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(T.m.p, d_m0, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);
+  for (int n = 0; n < nsteps; ++n) {
+    if (n % ckpt == 0) {
+      reset_forward_solves(h);
+      cudaMemcpyAsync(T.ckpts.p + (size_t)(n / ckpt) * n3, T.m.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);
+    }
+    set_step_field(h, T, n);
+    ADJ_TRY(rk4_step(h, T, T.m, nullptr, nullptr));
+    if (d_hist) {
+      k_avg_part<<<kAvgBlocks, kT, 0, s>>>(M.N, T.m, M.vol, T.avgpart);
+      ADJ_TRY(launched(h, "average"));
+      k_avg_final<<<1, 32, 0, s>>>(kAvgBlocks, T.avgpart, d_hist + 3 * (size_t)n, T.vt);
+      ADJ_TRY(launched(h, "average"));
+    }
+    if ((n & 63) == 63) {
+      int rc = check_device_error(h, "rk4 forward");
+      if (rc) return rc;
+    }
+  }
+  if (!d_hist) {
+    k_avg_part<<<kAvgBlocks, kT, 0, s>>>(M.N, T.m, M.vol, T.avgpart);
+    ADJ_TRY(launched(h, "average"));
+    k_avg_final<<<1, 32, 0, s>>>(kAvgBlocks, T.avgpart, T.avgpart.p + 4 * kAvgBlocks, T.vt);
+    ADJ_TRY(launched(h, "average"));
+  }
+  cudaMemcpyAsync(d_mT, T.m.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(W.h_ext.p, T.hbase.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);
+  h->ts_ready = 0;
+  return check_device_error(h, "rk4 forward");
+}
+
+int rk4_adjoint(nmg_handle *h, const double *d_mT_bar, const double *d_hist_bar, double *d_m0_bar, double *d_gwK,
+                double *d_gwD, double *d_gkap, double *d_gpul) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  cudaStream_t s = h->stream;
+  if (!h->tape || h->tape->nsteps <= 0) {
+    h->last_error = "rk4 adjoint: no forward trajectory on this handle";
+    return -3;
+  }
+  Tape &T = *h->tape;
+  const int n3 = T.n3, N = M.N;
+  if (!T.su.p) {
+    if (T.su.alloc((size_t)T.ckpt * 4 * n3) || T.sH.alloc((size_t)T.ckpt * 4 * n3) || T.lam.alloc(n3) ||
+        T.kb.alloc(n3) || T.ub.alloc(n3) || T.acc.alloc(n3) || T.Hbar.alloc(n3) || T.sanis.alloc(N) ||
+        T.hsum.alloc(3 * (size_t)nblk(N, kT)) || T.phibar.alloc(N) || T.rhs.alloc(N) || T.z.alloc(N) ||
+        T.rhobar.alloc(N) || T.y2b.alloc(std::max(M.nb, 1)) || T.y1b.alloc(std::max(M.nb, 1))) {
+      h->last_error = "rk4 adjoint: device allocation failed";
+      return 100;
+    }
+  }
+  ADJ_TRY(ensure_tpos(h));
+  if (d_mT_bar) cudaMemcpyAsync(T.lam.p, d_mT_bar, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);
+  else cudaMemsetAsync(T.lam.p, 0, sizeof(double) * n3, s);
+  if (d_gwK) cudaMemsetAsync(d_gwK, 0, sizeof(double) * M.T, s);
+  if (d_gwD) cudaMemsetAsync(d_gwD, 0, sizeof(double) * M.T, s);
+  if (d_gkap) cudaMemsetAsync(d_gkap, 0, sizeof(double) * M.T, s);
+  if (d_gpul && T.npulses > 0) cudaMemsetAsync(d_gpul, 0, sizeof(double) * 3 * T.npulses, s);
+  cg_reset_basis(h, 2);
+  cg_reset_basis(h, 3);
+  cudaMemsetAsync(T.z.p, 0, sizeof(double) * N, s);
+  cudaMemsetAsync(T.rhobar.p, 0, sizeof(double) * N, s);
+  GradOut G{d_gwK, d_gwD, d_gkap, T.npulses > 0 ? d_gpul : nullptr};
+  const double dt = T.dt;
+  const int nseg = (T.nsteps + T.ckpt - 1) / T.ckpt;
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int n0 = seg * T.ckpt, n1 = std::min(T.nsteps, n0 + T.ckpt);
+    // recompute the segment from its checkpoint, storing stage states and fields
+    reset_forward_solves(h);
+    cudaMemcpyAsync(T.m.p, T.ckpts.p + (size_t)seg * n3, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);
+    for (int n = n0; n < n1; ++n) {
+      set_step_field(h, T, n);
+      const size_t o = (size_t)(n - n0) * 4 * n3;
+      ADJ_TRY(rk4_step(h, T, T.m, T.su.p + o, T.sH.p + o));
+    }
+    for (int n = n1 - 1; n >= n0; --n) {
+      if (d_hist_bar) {
+        k_hist_inject<<<nblk(N, kT), kT, 0, s>>>(N, M.vol, T.vt, d_hist_bar + 3 * (size_t)n, T.lam);
+        ADJ_TRY(launched(h, "history cotangent"));
+      }
+      const size_t o = (size_t)(n - n0) * 4 * n3;
+      const double *su = T.su.p + o, *sH = T.sH.p + o;
+      cudaMemsetAsync(T.acc.p, 0, sizeof(double) * n3, s);
+      // stage 4, 3, 2, 1
+      const double ca[4] = {dt / 6.0, dt / 3.0, dt / 3.0, dt / 6.0};
+      const double cb[4] = {0.0, dt, 0.5 * dt, 0.5 * dt};
+      for (int q = 0; q < 4; ++q) {
+        const int st = 3 - q;
+        k_adj_combine<<<nblk(n3, kT), kT, 0, s>>>(n3, T.lam, q == 0 ? nullptr : T.ub.p, ca[q], cb[q], T.kb, T.acc);
+        ADJ_TRY(launched(h, "adjoint combine"));
+        ADJ_TRY(stage_vjp(h, T, su + (size_t)st * n3, sH + (size_t)st * n3, T.kb, T.ub, n, G));
+      }
+      k_add_to<<<nblk(n3, kT), kT, 0, s>>>(n3, T.ub, T.acc);
+      ADJ_TRY(launched(h, "adjoint accumulate"));
+      k_add_to<<<nblk(n3, kT), kT, 0, s>>>(n3, T.acc, T.lam);
+      ADJ_TRY(launched(h, "adjoint accumulate"));
+      if (((n - n0) & 15) == 0) {
+        int rc = check_device_error(h, "rk4 adjoint");
+        if (rc) return rc;
+      }
+    }
+  }
+  if (d_m0_bar) cudaMemcpyAsync(d_m0_bar, T.lam.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);
+  cudaMemcpyAsync(W.h_ext.p, T.hbase.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);
+  h->ts_ready = 0;
+  return check_device_error(h, "rk4 adjoint");
+}
+
+}  // namespace nmg

@@ -85,6 +85,7 @@ int nmg_destroy(nmg_handle *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   nmg::ts_destroy(h->ts);
   h->ts = nullptr;
+  nmg::tape_free(h);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;  // member destructors release the device buffers
   return 0;
@@ -270,6 +271,38 @@ int nmg_rhs_device(nmg_handle *h, const double *d_m, double *d_dmdt) {
 int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps) {
   if (!h || !d_m || nsteps < 0) return -1;
   return nmg::rk4_device(h, d_m, dt, nsteps);
+}
+
+int nmg_set_element_params(nmg_handle *h, const double *d_wK, const double *d_wD, const double *d_kappa,
+                           const double axis[3]) {
+  if (!h || !axis) return -1;
+  int rc = nmg::set_element_params(h, d_wK, d_wD, d_kappa, axis);
+  return rc ? fail(h, rc, "nmg_set_element_params: " + h->last_error) : 0;
+}
+
+int nmg_clear_element_params(nmg_handle *h) {
+  if (!h) return -1;
+  h->ep.active = 0;
+  h->ts_ready = 0;
+  return 0;
+}
+
+int nmg_rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ckpt_every, const double *d_pulses,
+                    int n_pulses, int steps_per_pulse, double *d_m_final, double *d_avg_hist) {
+  if (!h || !d_m0 || !d_m_final) return -1;
+  if (nsteps < 1 || ckpt_every < 1 || !(dt > 0.0)) return fail(h, -2, "nmg_rk4_forward: need nsteps, ckpt_every >= 1, dt > 0");
+  if (n_pulses < 0 || (n_pulses > 0 && (!d_pulses || steps_per_pulse < 1)))
+    return fail(h, -2, "nmg_rk4_forward: pulses need a device array and steps_per_pulse >= 1");
+  int rc = nmg::rk4_forward(h, d_m0, dt, nsteps, ckpt_every, d_pulses, n_pulses, steps_per_pulse, d_m_final, d_avg_hist);
+  return rc ? fail(h, rc, "nmg_rk4_forward: " + h->last_error) : 0;
+}
+
+int nmg_rk4_adjoint(nmg_handle *h, const double *d_m_final_bar, const double *d_avg_hist_bar, double *d_m0_bar,
+                    double *d_wK_bar, double *d_wD_bar, double *d_kappa_bar, double *d_pulses_bar) {
+  if (!h) return -1;
+  int rc = nmg::rk4_adjoint(h, d_m_final_bar, d_avg_hist_bar, d_m0_bar, d_wK_bar, d_wD_bar, d_kappa_bar,
+                            d_pulses_bar);
+  return rc ? fail(h, rc, "nmg_rk4_adjoint: " + h->last_error) : 0;
 }
 
 int nmg_get_timings(const nmg_handle *h, double out[8]) {

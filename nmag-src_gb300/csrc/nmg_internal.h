@@ -103,6 +103,19 @@ struct Profiler {
 
 }  // namespace nmg
 
+namespace nmg {
+// Per-element parameters of the differentiation form: the exchange operator
+// sum_T wK_T K_T, the divergence operator built from per-element weights wD_T,
+// and the per-node anisotropy coefficient from per-element kappa_T.
+struct ElemParams {
+  int active = 0;
+  DevBuf<double> Kx, Dx, anis;   // nnz, 3 x nnz, N
+  DevBuf<int32_t> tpos;          // position of entry (j,i) for entry (i,j) of the scalar pattern
+  double axis[3] = {0, 0, 1};
+};
+struct Tape;                     // RK4 checkpoints of the differentiation form (adjoint.cu)
+}  // namespace nmg
+
 struct nmg_handle {
   nmg::Mesh mesh;
   nmg::Workspace ws;
@@ -119,6 +132,9 @@ struct nmg_handle {
   int64_t launches = 0;         // kernels launched by this handle
   double timings[8] = {0};
   nmg::Profiler prof;
+  nmg::ElemParams ep;
+  nmg::Tape *tape = nullptr;
+  const double *exch_K() const { return ep.active ? ep.Kx.p : mesh.K.p; }
 };
 
 // Bracket one hot-kernel launch with profiler events (no-op when disabled).
@@ -138,6 +154,17 @@ int fill_bem(nmg_handle *h, std::string &err);
 void bem_gemv(nmg_handle *h, const double *x, double *y);
 // ---- rhs_kernels.cu ----
 int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt);  // full RHS on device vectors
+// CG on slot 0/2 (Neumann operator) or 1/3 (Dirichlet operator); slots 2/3
+// keep their own warm-start bases.
+int cg_solve(nmg_handle *h, int slot, const double *b, double *x, double rtol, double atol, int maxits);
+void cg_reset_basis(nmg_handle *h, int slot);
+// ---- adjoint.cu ----
+void tape_free(nmg_handle *h);
+int set_element_params(nmg_handle *h, const double *wK, const double *wD, const double *kappa, const double axis[3]);
+int rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ckpt, const double *d_pulses,
+                int npulses, int spp, double *d_mT, double *d_hist);
+int rk4_adjoint(nmg_handle *h, const double *d_mT_bar, const double *d_hist_bar, double *d_m0_bar, double *d_gwK,
+                double *d_gwD, double *d_gkap, double *d_gpul);
 int energy_density(nmg_handle *h, const double *d_m, double *d_E5);
 int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5]);
 int max_dm(nmg_handle *h, const double *d_m, const double *d_mprev, double *out);

@@ -386,7 +386,7 @@ int psetup(Integrator &I, int jok, const double *ypred) {
 JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
   const Mesh &M = I.hd->mesh;
   JvArgs a;
-  a.N = M.N; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = M.K; a.vol = M.vol;
+  a.N = M.N; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.vol = M.vol;
   a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt;
   a.c_exch = I.hd->mat.exch_coeff; a.C1 = I.hd->mat.C1; a.C2 = I.hd->mat.C2;
   a.gamma = I.gamma; a.gammap = I.gammap; a.psolve = psolve; a.scale_out = 1; a.out = out;
@@ -422,7 +422,7 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
   const nmg_material &mt = I.hd->mat;
   auto HM = [&](int i, int j) -> double & { return I.Hm[(size_t)i * maxl + j]; };
   *nli_out = 0;
-  k_psolve<<<nblk(M.N, 128), 128, 0, I.s()>>>(M.N, M.diag_pos, M.K, M.vol, I.mJ, I.HJ, mt.exch_coeff, mt.C1,
+  k_psolve<<<nblk(M.N, 128), 128, 0, I.s()>>>(M.N, M.diag_pos, I.hd->exch_K(), M.vol, I.mJ, I.HJ, mt.exch_coeff, mt.C1,
                                               mt.C2, I.gammap, b, I.ewt, I.V[0]); ++I.hd->launches;
   I.nps++;
   double rho = 0.0;  // ||V0||_2 (unweighted)

@@ -9,7 +9,7 @@
 //   k_div          rho = -Ms * sum_k D(i,k) . m_k                 (op_div_m + SCALE -1)
 //   k_cg3          persistent cooperative Jacobi-PCG (single-reduction form), bounded barriers
 //   k_gather_b     phi1b = phi1[node_of_b]                          (PULL-FEM)
-//   k_gemv_*       phi2b = BEM phi1b, column-major slabs + ordered slab sum
+//   k_gemv_*       phi2b = BEM phi1b, row-major warp segments + ordered row sum
 //   k_dbc_rhs      rhs = -K_IB phi2b (interior), phi2b (boundary)  (op_load_DBC)
 //   k_heff_llg     H_exch (K SpMV), H_demag (G SpMV on phi1+phi2), H_anis,
 //                  H_total and dm/dt fused in one node kernel (CFBOX = / V_i)
@@ -140,6 +140,7 @@ __device__ __forceinline__ bool reduce_all(const CGArgs &a, unsigned epoch, doub
 // block solves the small system identically.  With an empty basis the
 // previous solution is the start, like the reference's initial_guess_nonzero.
 constexpr int kBasis = 6;
+constexpr int kCGSlots = 4;   // warm-start bases: 0/1 Neumann/Dirichlet, 2/3 the adjoint solves
 
 struct CGBasis {
   double *b, *x;   // kBasis x N right-hand sides and solutions
@@ -538,6 +539,7 @@ struct NodeArgs {
   int N, nnz, do_demag;
   const int32_t *row_ptr, *col_idx;
   const double *K, *G, *vol, *m, *phi, *h_ext;
+  const double *anis_node;   // per-node anisotropy coefficient (element parameters) or null
   double c_exch, C1, C2, C3, K1, anis, ax, ay, az;
   double *h_exch, *h_demag, *h_anis, *h_total, *dmdt;
 };
@@ -563,11 +565,12 @@ __global__ void k_heff_llg(NodeArgs a) {
   const double hd[3] = {-g0 / V, -g1 / V, -g2 / V};
   const double *m = a.m + 3 * (size_t)i;
   double ha[3] = {0.0, 0.0, 0.0};
-  if (a.K1 != 0.0) {
+  if (a.K1 != 0.0 || a.anis_node) {
+    const double c = a.anis_node ? a.anis_node[i] : a.anis;
     double am = (a.ax * m[0] + a.ay * m[1]) + a.az * m[2];
-    ha[0] = a.anis * am * (a.ax - am * m[0]);
-    ha[1] = a.anis * am * (a.ay - am * m[1]);
-    ha[2] = a.anis * am * (a.az - am * m[2]);
+    ha[0] = c * am * (a.ax - am * m[0]);
+    ha[1] = c * am * (a.ay - am * m[1]);
+    ha[2] = c * am * (a.az - am * m[2]);
   }
   const double *he = a.h_ext + 3 * (size_t)i;
   double H[3];
@@ -759,19 +762,19 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   CGArgs a;
-  a.N = M.N; a.mode = mode;
+  a.N = M.N; a.mode = mode & 1;   // slots 2 and 3: the same operators, separate warm-start bases
   a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.b_of_node = M.b_of_node; a.K = M.K;
-  a.dinv = mode == 0 ? W.dinv_n.p : W.dinv_d.p;
+  a.dinv = (mode & 1) == 0 ? W.dinv_n.p : W.dinv_d.p;
   a.b = b; a.x = x; a.r = W.cg_r; a.z = W.cg_z; a.p = W.cg_p; a.q = W.cg_q; a.red = W.red;
   a.w = W.cg_w; a.flags = W.bar; a.tot = W.cg_tot;
   a.bar = W.bar; a.err = W.err; a.iters = W.iters;
   a.rtol = rtol; a.atol = atol; a.maxits = maxits;
   a.perm = W.perm; a.prow = W.prow; a.pcol = W.pcol; a.pbnd = W.pbnd; a.pK = W.pK; a.xperm = W.xperm;
-  a.coarse = (mode == 0 && W.nc > 0) ? 1 : 0;
+  a.coarse = ((mode & 1) == 0 && W.nc > 0) ? 1 : 0;
   a.nc = W.nc; a.ainv = W.ainv; a.rc = W.rc;
   // fresh barrier words per solve: epochs restart at 1 inside the kernel
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
-  NMG_PROF_BEGIN(h, 1 + mode);
+  NMG_PROF_BEGIN(h, 1 + (mode & 1));
   cudaError_t e;
   {
     int cap = W.cg_nnz_cap;
@@ -794,6 +797,14 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
 }
 
 }  // namespace
+
+int cg_solve(nmg_handle *h, int slot, const double *b, double *x, double rtol, double atol, int maxits) {
+  return run_cg(h, slot, b, x, rtol, atol, maxits);
+}
+
+void cg_reset_basis(nmg_handle *h, int slot) {
+  cudaMemsetAsync(h->ws.basis_ring.p + 2 * slot, 0, sizeof(int) * 2, h->stream);
+}
 
 int init_workspace(nmg_handle *h, std::string &err) {
   Mesh &M = h->mesh;
@@ -882,11 +893,11 @@ int init_workspace(nmg_handle *h, std::string &err) {
   NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
   NMG_CUDA_TRY(W.bar.alloc(W.cg_blocks + 2), "alloc barrier");
   NMG_CUDA_TRY(W.cg_w.alloc(N), "alloc");
-  NMG_CUDA_TRY(W.basis_b.alloc(2 * (size_t)kBasis * N), "alloc CG basis");
-  NMG_CUDA_TRY(W.basis_x.alloc(2 * (size_t)kBasis * N), "alloc CG basis");
-  NMG_CUDA_TRY(W.basis_gram.alloc(2 * kBasis * kBasis), "alloc");
-  NMG_CUDA_TRY(W.basis_ring.alloc(4), "alloc");
-  cudaMemsetAsync(W.basis_ring.p, 0, sizeof(int) * 4, h->stream);
+  NMG_CUDA_TRY(W.basis_b.alloc(kCGSlots * (size_t)kBasis * N), "alloc CG basis");
+  NMG_CUDA_TRY(W.basis_x.alloc(kCGSlots * (size_t)kBasis * N), "alloc CG basis");
+  NMG_CUDA_TRY(W.basis_gram.alloc(kCGSlots * kBasis * kBasis), "alloc");
+  NMG_CUDA_TRY(W.basis_ring.alloc(2 * kCGSlots), "alloc");
+  cudaMemsetAsync(W.basis_ring.p, 0, sizeof(int) * 2 * kCGSlots, h->stream);
   NMG_CUDA_TRY(W.cg_tot.alloc(2 * 4), "alloc");
   NMG_CUDA_TRY(W.iters.alloc(4), "alloc");
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);
@@ -946,7 +957,8 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
   const int N = M.N;
   const nmg_material &mt = h->mat;
   if (h->opt.do_demag && M.nb > 0) {
-    k_div<<<nblk(N, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, M.D, d_m, W.rho); ++h->launches;
+    k_div<<<nblk(N, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, h->ep.active ? h->ep.Dx.p : M.D.p, d_m,
+                                       W.rho); ++h->launches;
     if (run_cg(h, 0, W.rho, W.phi1, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
     k_gather_b<<<nblk(M.nb, 256), 256, 0, s>>>(M.nb, M.node_of_b, W.phi1, W.b1); ++h->launches;
     bem_gemv(h, W.b1, W.b2);
@@ -956,10 +968,12 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
   }
   NodeArgs a;
   a.N = N; a.nnz = M.nnz; a.do_demag = (h->opt.do_demag && M.nb > 0) ? 1 : 0;
-  a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.K = M.K; a.G = M.G; a.vol = M.vol;
+  a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.K = h->exch_K(); a.G = M.G; a.vol = M.vol;
   a.m = d_m; a.phi = W.phi; a.h_ext = W.h_ext;
+  a.anis_node = h->ep.active ? h->ep.anis.p : nullptr;
   a.c_exch = mt.exch_coeff; a.C1 = mt.C1; a.C2 = mt.C2; a.C3 = mt.C3; a.K1 = mt.K1; a.anis = mt.anis_coeff;
   a.ax = mt.axis[0]; a.ay = mt.axis[1]; a.az = mt.axis[2];
+  if (h->ep.active) { a.ax = h->ep.axis[0]; a.ay = h->ep.axis[1]; a.az = h->ep.axis[2]; }
   a.h_exch = W.h_exch; a.h_demag = W.h_demag; a.h_anis = W.h_anis; a.h_total = W.h_total;
   a.dmdt = d_dmdt ? d_dmdt : W.dmdt.p;
   {

@@ -20,8 +20,9 @@ LIB = os.path.join(PKG, "libnmaggpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-strict-aliasing",
           "--expt-relaxed-constexpr"]
-NO_FMA = {"mesh_kernels.cu", "bem_kernels.cu"}
-SOURCES = ["mesh_kernels.cu", "bem_kernels.cu", "rhs_kernels.cu", "nmg_ts.cu", "nmg_api.cu", "nmg_static.cu"]
+NO_FMA = {"mesh_kernels.cu", "bem_kernels.cu", "adjoint.cu"}
+SOURCES = ["mesh_kernels.cu", "bem_kernels.cu", "rhs_kernels.cu", "nmg_ts.cu", "nmg_api.cu", "nmg_static.cu",
+           "adjoint.cu"]
 
 
 def nvcc():

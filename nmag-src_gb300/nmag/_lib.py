@@ -44,7 +44,8 @@ EXPORTS = ["nmg_version", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_me
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
            "nmg_set_material", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
            "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
-           "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_max_dm_static"]
+           "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_max_dm_static",
+           "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint"]
 
 PROFILED_KERNELS = ["bem_gemv", "cg_neumann", "cg_dirichlet", "heff_llg", "jv_psolve"]
 
@@ -100,6 +101,10 @@ def lib(build_if_missing=True):
     L.nmg_launch_count.restype = C.c_int64
     L.nmg_cg_iterations.argtypes = [vp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]
     L.nmg_max_dm_static.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_double)]
+    L.nmg_set_element_params.argtypes = [vp, vp, vp, vp, _f64p]
+    L.nmg_clear_element_params.argtypes = [vp]
+    L.nmg_rk4_forward.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, vp]
+    L.nmg_rk4_adjoint.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 
@@ -253,3 +258,22 @@ class Engine(object):
 
     def rk4_device(self, d_m, dt, nsteps):
         check(lib().nmg_rk4_device(self.h, C.c_void_p(d_m), dt, nsteps), self.h, "rk4_device")
+
+    # ---- differentiation form (device pointers; 0 = NULL) ----
+    def set_element_params(self, d_wK, d_wD, d_kappa, axis):
+        ax = np.ascontiguousarray(axis, dtype=np.float64)
+        check(lib().nmg_set_element_params(self.h, C.c_void_p(d_wK or None), C.c_void_p(d_wD or None),
+                                           C.c_void_p(d_kappa or None), ax), self.h, "set_element_params")
+
+    def clear_element_params(self):
+        check(lib().nmg_clear_element_params(self.h), self.h, "clear_element_params")
+
+    def rk4_forward(self, d_m0, dt, nsteps, ckpt_every, d_pulses, n_pulses, steps_per_pulse, d_m_final, d_hist):
+        check(lib().nmg_rk4_forward(self.h, C.c_void_p(d_m0), dt, nsteps, ckpt_every, C.c_void_p(d_pulses or None),
+                                    n_pulses, steps_per_pulse, C.c_void_p(d_m_final), C.c_void_p(d_hist or None)),
+              self.h, "rk4_forward")
+
+    def rk4_adjoint(self, d_mT_bar, d_hist_bar, d_m0_bar, d_wK_bar, d_wD_bar, d_kappa_bar, d_pulses_bar):
+        ptrs = [C.c_void_p(p or None) for p in (d_mT_bar, d_hist_bar, d_m0_bar, d_wK_bar, d_wD_bar, d_kappa_bar,
+                                                  d_pulses_bar)]
+        check(lib().nmg_rk4_adjoint(self.h, *ptrs), self.h, "rk4_adjoint")
