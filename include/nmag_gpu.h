@@ -50,7 +50,8 @@ typedef struct nmg_options {
   int bem_precision;                     /* 0: FP64 matrix; 1: FP32 matrix, FP64 sums  */
   int cg_precision;                      /* 0: FP64 CG; reserved                       */
   int cg_no_coarse;                      /* 1: Jacobi only (no two-level Neumann CG)   */
-  int reserved[5];
+  int n_members;                         /* ensemble size B (0 or 1: one simulation)   */
+  int reserved[4];
 } nmg_options;
 
 /* Integrator statistics (CVODE counters; nsim.ml:354-387 timings). */
@@ -131,6 +132,14 @@ int nmg_energy_density(nmg_handle *h, double *E5);
 /* Volume averages of m (3) and total energies (5) = sum_i E_i V_i
  * (main.py:2313-2480, fem.ml:3246-3283). */
 int nmg_averages(nmg_handle *h, double avg_m[3], double energies[5]);
+
+/* Ensemble (options n_members = B > 1): B independent simulations on the same
+ * mesh and material, integrated as one ODE system.  Every per-node array of
+ * the calls above then holds B member blocks, member b at offset b * 3N (or
+ * b * N for scalars; energy densities [k][member][node]); nmg_averages
+ * reports member 0 and this call any member.  No counterpart in the
+ * reference, which runs one simulation per process. */
+int nmg_member_averages(nmg_handle *h, int member, double avg_m[3], double energies[5]);
 
 /* Timestepper (re)initialisation at t0 from the current m; replaces
  * ocaml.lam_ts_init -> timestepper_set_initial_from_phys (nsim.ml:2485-2535). */

@@ -558,6 +558,10 @@ int ensure_tpos(nmg_handle *h) {
 
 int set_element_params(nmg_handle *h, const double *wK, const double *wD, const double *kappa, const double axis[3]) {
   Mesh &M = h->mesh;
+  if (h->nrep > 1) {
+    h->last_error = "element parameters apply to single simulations (n_members <= 1)";
+    return -2;
+  }
   ElemParams &E = h->ep;
   if (!E.Kx.p && (E.Kx.alloc(M.nnz) || E.Dx.alloc(3 * (size_t)M.nnz) || E.anis.alloc(M.N))) {
     h->last_error = "element parameters: device allocation failed";
@@ -589,6 +593,10 @@ int rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ck
   Workspace &W = h->ws;
   cudaStream_t s = h->stream;
   const int n3 = 3 * M.N;
+  if (h->nrep > 1) {
+    h->last_error = "the RK4 adjoint applies to single simulations (n_members <= 1)";
+    return -2;
+  }
   if (!h->tape) h->tape = new Tape();
   Tape &T = *h->tape;
   const bool same = T.n3 == n3 && T.ckpt == ckpt && T.nsteps == nsteps && T.npulses == npulses;

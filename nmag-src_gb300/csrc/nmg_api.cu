@@ -47,6 +47,8 @@ int nmg_create(const double *coords, int n_nodes, const int32_t *tets, int n_tet
     if (!(coords[k] == coords[k])) return fail(nullptr, -4, "nmg_create: non-finite coordinate");
   if (!finite_material(mat)) return fail(nullptr, -5, "nmg_create: non-finite material constant");
   if (mat->Ms == 0.0) return fail(nullptr, -5, "nmg_create: Ms must be non-zero");
+  if (opt && (opt->n_members < 0 || opt->n_members > nmg::kMaxMembers))
+    return fail(nullptr, -6, "nmg_create: n_members must be in [0, " + std::to_string(nmg::kMaxMembers) + "]");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(nullptr, 101, "nmg_create: no CUDA device");
   nmg_handle *h = new nmg_handle();
@@ -58,6 +60,7 @@ int nmg_create(const double *coords, int n_nodes, const int32_t *tets, int n_tet
     h->opt.nbc_atol = h->opt.dbc_atol = 1e-50;
     h->opt.nbc_maxits = h->opt.dbc_maxits = 10000;
   }
+  h->nrep = h->opt.n_members > 1 ? h->opt.n_members : 1;
   cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete h;
@@ -149,9 +152,9 @@ int nmg_get_bem(const nmg_handle *h, double *out) {
 
 int nmg_set_m(nmg_handle *h, const double *m) {
   if (!h || !m) return -1;
-  for (long long k = 0; k < 3LL * h->mesh.N; ++k)
+  for (long long k = 0; k < 3LL * h->mesh.N * h->nrep; ++k)
     if (!(m[k] == m[k])) return fail(h, -4, "nmg_set_m: non-finite magnetisation");
-  if (cudaMemcpyAsync(h->ws.m.p, m, sizeof(double) * 3 * h->mesh.N, cudaMemcpyHostToDevice, h->stream))
+  if (cudaMemcpyAsync(h->ws.m.p, m, sizeof(double) * 3 * h->mesh.N * h->nrep, cudaMemcpyHostToDevice, h->stream))
     return fail(h, 100, "nmg_set_m: copy failed");
   h->ts_ready = 0;
   return cudaStreamSynchronize(h->stream) == cudaSuccess ? 0 : fail(h, 100, "nmg_set_m: sync failed");
@@ -159,14 +162,15 @@ int nmg_set_m(nmg_handle *h, const double *m) {
 
 int nmg_get_m(const nmg_handle *h, double *m) {
   if (!h || !m) return -1;
-  return d2h(h, m, h->ws.m.p, sizeof(double) * 3 * h->mesh.N);
+  return d2h(h, m, h->ws.m.p, sizeof(double) * 3 * h->mesh.N * h->nrep);
 }
 
 int nmg_set_h_ext(nmg_handle *h, const double *hx) {
   if (!h || !hx) return -1;
-  for (long long k = 0; k < 3LL * h->mesh.N; ++k)
+  for (long long k = 0; k < 3LL * h->mesh.N * h->nrep; ++k)
     if (!(hx[k] == hx[k])) return fail(h, -4, "nmg_set_h_ext: non-finite field");
-  if (cudaMemcpyAsync(h->ws.h_ext.p, hx, sizeof(double) * 3 * h->mesh.N, cudaMemcpyHostToDevice, h->stream))
+  if (cudaMemcpyAsync(h->ws.h_ext.p, hx, sizeof(double) * 3 * h->mesh.N * h->nrep, cudaMemcpyHostToDevice,
+                      h->stream))
     return fail(h, 100, "nmg_set_h_ext: copy failed");
   h->ts_ready = 0;
   return cudaStreamSynchronize(h->stream) == cudaSuccess ? 0 : fail(h, 100, "nmg_set_h_ext: sync failed");
@@ -186,7 +190,7 @@ int nmg_eval_fields(nmg_handle *h, double *fields, double *scalars) {
   if (rc) return fail(h, rc, "nmg_eval_fields: launch failed");
   rc = nmg::check_device_error(h, "nmg_eval_fields");
   if (rc) return rc;
-  const size_t n3 = 3 * (size_t)h->mesh.N, N = h->mesh.N;
+  const size_t N = (size_t)h->mesh.N * h->nrep, n3 = 3 * N;
   if (fields) {
     const double *src[5] = {h->ws.h_exch, h->ws.h_demag, h->ws.h_anis, h->ws.h_total, h->ws.dmdt};
     for (int k = 0; k < 5; ++k)
@@ -206,12 +210,18 @@ int nmg_eval_fields(nmg_handle *h, double *fields, double *scalars) {
 int nmg_energy_density(nmg_handle *h, double *E5) {
   if (!h || !E5) return -1;
   if (nmg::energy_density(h, h->ws.m, h->ws.E5)) return fail(h, 100, "energy launch failed");
-  return d2h(h, E5, h->ws.E5.p, sizeof(double) * 5 * h->mesh.N);
+  return d2h(h, E5, h->ws.E5.p, sizeof(double) * 5 * h->mesh.N * h->nrep);
 }
 
 int nmg_averages(nmg_handle *h, double avg_m[3], double energies[5]) {
   if (!h || !avg_m) return -1;
   return nmg::averages(h, h->ws.m, avg_m, energies);
+}
+
+int nmg_member_averages(nmg_handle *h, int member, double avg_m[3], double energies[5]) {
+  if (!h || !avg_m) return -1;
+  if (member < 0 || member >= h->nrep) return fail(h, -2, "nmg_member_averages: member out of range");
+  return nmg::averages(h, h->ws.m, avg_m, energies, member);
 }
 
 int nmg_ts_init(nmg_handle *h, double t0, double rtol, double atol, int max_order, int krylov_max) {
@@ -256,8 +266,8 @@ int nmg_ts_advance(nmg_handle *h, double t_final, int exact_tstop, int64_t max_s
 int nmg_max_dm(nmg_handle *h, const double *m_prev, double *out) {
   if (!h || !m_prev || !out) return -1;
   nmg::DevBuf<double> tmp;
-  if (tmp.alloc(3 * (size_t)h->mesh.N)) return 100;
-  cudaMemcpyAsync(tmp.p, m_prev, sizeof(double) * 3 * h->mesh.N, cudaMemcpyHostToDevice, h->stream);
+  if (tmp.alloc(3 * (size_t)h->mesh.N * h->nrep)) return 100;
+  cudaMemcpyAsync(tmp.p, m_prev, sizeof(double) * 3 * h->mesh.N * h->nrep, cudaMemcpyHostToDevice, h->stream);
   return nmg::max_dm(h, h->ws.m, tmp, out);
 }
 

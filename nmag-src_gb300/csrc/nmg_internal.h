@@ -21,6 +21,8 @@ enum DeviceError : int {
 };
 
 constexpr int kMaxRowLen = 64;     // max distinct neighbours (incl. self) per node
+constexpr int kMaxMembers = 64;    // ensemble members per handle
+constexpr int kChunk = 8;          // members per CG / BEM launch
 constexpr int kMaxNodeTets = 128;  // max tets around one node
 
 template <class T>
@@ -70,6 +72,9 @@ struct Workspace {
   DevBuf<int> iters;        // CG iterations written by the persistent kernel
   DevBuf<double> basis_b, basis_x, basis_gram;  // CG initial-guess basis per solve kind
   DevBuf<int> basis_ring;
+  // ensemble: a basis per solve kind and member ([kind][member][kBasis][N])
+  DevBuf<double> ens_basis_b, ens_basis_x, ens_basis_gram;
+  DevBuf<int> ens_basis_ring;
   DevBuf<int32_t> perm, prow, pcol, pbnd;     // CG solver ordering (spatially binned nodes)
   DevBuf<double> pK, xperm, ainv, rc;         // K in that order, iterate, coarse inverse, coarse residual
   int nc = 0;                                 // aggregates of the two-level Neumann CG (0: none)
@@ -132,6 +137,7 @@ struct nmg_handle {
   int64_t launches = 0;         // kernels launched by this handle
   double timings[8] = {0};
   nmg::Profiler prof;
+  int nrep = 1;                 // ensemble members B (member-major vectors: member b at b * 3N / b * N)
   nmg::ElemParams ep;
   nmg::Tape *tape = nullptr;
   const double *exch_K() const { return ep.active ? ep.Kx.p : mesh.K.p; }
@@ -166,7 +172,7 @@ int rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ck
 int rk4_adjoint(nmg_handle *h, const double *d_mT_bar, const double *d_hist_bar, double *d_m0_bar, double *d_gwK,
                 double *d_gwD, double *d_gkap, double *d_gpul);
 int energy_density(nmg_handle *h, const double *d_m, double *d_E5);
-int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5]);
+int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5], int member = 0);
 int max_dm(nmg_handle *h, const double *d_m, const double *d_mprev, double *out);
 int init_workspace(nmg_handle *h, std::string &err);
 int check_device_error(nmg_handle *h, const char *where);

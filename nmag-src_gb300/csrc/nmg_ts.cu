@@ -188,7 +188,7 @@ __global__ void k_hacc(int nv, const double *__restrict__ h, double *__restrict_
 // preconditioner and the ewt scaling:  out = ewt * P^{-1} (t - gamma J t),
 // t = v / ewt (materialised by the caller).  If psolve == 0, out = t - gamma J t.
 struct JvArgs {
-  int N;
+  int N, nrep;   // nodes per member, ensemble members (member-major vectors)
   const int32_t *row_ptr, *col_idx, *diag_pos;
   const double *K, *vol, *mJ, *HJ, *t, *ewt;
   double c_exch, C1, C2, gamma, gammap;
@@ -216,17 +216,19 @@ __device__ __forceinline__ void jac_apply(const double *m, const double *H, cons
 }
 
 __global__ void k_jv_psolve(JvArgs a) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.N) return;
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= (long long)a.N * a.nrep) return;
+  const int mbr = (int)(g / a.N), i = (int)(g - (long long)mbr * a.N);
+  const double *tm = a.t + (size_t)mbr * 3 * a.N;
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
   for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; ++k) {
-    const double *tj = a.t + 3 * (size_t)a.col_idx[k];
+    const double *tj = tm + 3 * (size_t)a.col_idx[k];
     double kv = a.K[k];
     s0 += kv * tj[0]; s1 += kv * tj[1]; s2 += kv * tj[2];
   }
   const double V = a.vol[i];
   const double hv[3] = {-a.c_exch * s0 / V, -a.c_exch * s1 / V, -a.c_exch * s2 / V};
-  const double *m = a.mJ + 3 * (size_t)i, *H = a.HJ + 3 * (size_t)i, *w = a.t + 3 * (size_t)i;
+  const double *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g, *w = a.t + 3 * (size_t)g;
   double jw[3];
   jac_apply(m, H, w, hv, a.C1, a.C2, jw);
   double r[3] = {w[0] - a.gamma * jw[0], w[1] - a.gamma * jw[1], w[2] - a.gamma * jw[2]};
@@ -251,7 +253,7 @@ __global__ void k_jv_psolve(JvArgs a) {
     for (int d = 0; d < 3; ++d) z[d] = (Pi[d][0] * r[0] + Pi[d][1] * r[1]) + Pi[d][2] * r[2];
   }
   for (int d = 0; d < 3; ++d) {
-    size_t o = 3 * (size_t)i + d;
+    size_t o = 3 * (size_t)g + d;
     a.out[o] = a.scale_out ? a.ewt[o] * z[d] : z[d];
   }
 }
@@ -260,11 +262,12 @@ __global__ void k_jv_psolve(JvArgs a) {
 __global__ void k_psolve(int N, const int32_t *__restrict__ diag_pos, const double *__restrict__ K,
                          const double *__restrict__ vol, const double *__restrict__ mJ, const double *__restrict__ HJ,
                          double c_exch, double C1, double C2, double gammap, const double *__restrict__ r,
-                         const double *__restrict__ ewt, double *__restrict__ out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+                         const double *__restrict__ ewt, double *__restrict__ out, int nrep) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= (long long)N * nrep) return;
+  const int i = (int)(g % N);
   const double kap = -c_exch * K[diag_pos[i]] / vol[i];
-  const double *m = mJ + 3 * (size_t)i, *H = HJ + 3 * (size_t)i, *ri = r + 3 * (size_t)i;
+  const double *m = mJ + 3 * (size_t)g, *H = HJ + 3 * (size_t)g, *ri = r + 3 * (size_t)g;
   double P[3][3];
   for (int c = 0; c < 3; ++c) {
     double e[3] = {0.0, 0.0, 0.0};
@@ -281,7 +284,7 @@ __global__ void k_psolve(int N, const int32_t *__restrict__ diag_pos, const doub
                      {c01 * inv, (P[0][0] * P[2][2] - P[0][2] * P[2][0]) * inv, (P[0][2] * P[1][0] - P[0][0] * P[1][2]) * inv},
                      {c02 * inv, (P[0][1] * P[2][0] - P[0][0] * P[2][1]) * inv, (P[0][0] * P[1][1] - P[0][1] * P[1][0]) * inv}};
   for (int d = 0; d < 3; ++d) {
-    size_t o = 3 * (size_t)i + d;
+    size_t o = 3 * (size_t)g + d;
     out[o] = ewt[o] * ((Pi[d][0] * ri[0] + Pi[d][1] * ri[1]) + Pi[d][2] * ri[2]);
   }
 }
@@ -386,7 +389,7 @@ int psetup(Integrator &I, int jok, const double *ypred) {
 JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
   const Mesh &M = I.hd->mesh;
   JvArgs a;
-  a.N = M.N; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.vol = M.vol;
+  a.N = M.N; a.nrep = I.hd->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.vol = M.vol;
   a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt;
   a.c_exch = I.hd->mat.exch_coeff; a.C1 = I.hd->mat.C1; a.C2 = I.hd->mat.C2;
   a.gamma = I.gamma; a.gammap = I.gammap; a.psolve = psolve; a.scale_out = 1; a.out = out;
@@ -422,8 +425,9 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
   const nmg_material &mt = I.hd->mat;
   auto HM = [&](int i, int j) -> double & { return I.Hm[(size_t)i * maxl + j]; };
   *nli_out = 0;
-  k_psolve<<<nblk(M.N, 128), 128, 0, I.s()>>>(M.N, M.diag_pos, I.hd->exch_K(), M.vol, I.mJ, I.HJ, mt.exch_coeff, mt.C1,
-                                              mt.C2, I.gammap, b, I.ewt, I.V[0]); ++I.hd->launches;
+  k_psolve<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(M.N, M.diag_pos, I.hd->exch_K(), M.vol, I.mJ,
+                                                                       I.HJ, mt.exch_coeff, mt.C1, mt.C2, I.gammap, b,
+                                                                       I.ewt, I.V[0], I.hd->nrep); ++I.hd->launches;
   I.nps++;
   double rho = 0.0;  // ||V0||_2 (unweighted)
   {
@@ -446,7 +450,7 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
     JvArgs a = jv_args(I, I.tvec, I.V[l + 1], 1);
     {
       NMG_PROF_BEGIN(I.hd, 4);
-      k_jv_psolve<<<nblk(M.N, 128), 128, 0, I.s()>>>(a); ++I.hd->launches;
+      k_jv_psolve<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(a); ++I.hd->launches;
       NMG_PROF_END(I.hd);
     }
     I.njv++; I.nps++;
@@ -791,7 +795,7 @@ void interpolate(Integrator &I, double t, double *out) {
 Integrator *ts_create(nmg_handle *h, int qmax, int maxl, double rtol, double atol) {
   Integrator *I = new Integrator();
   I->hd = h;
-  I->n = 3 * h->mesh.N;
+  I->n = 3 * h->mesh.N * h->nrep;
   I->qmax = qmax < 1 ? 1 : (qmax > QMAXB ? QMAXB : qmax);
   I->maxl = maxl < 1 ? 5 : maxl;
   I->rtol = rtol; I->atol = atol;
@@ -890,7 +894,7 @@ int ts_advance(nmg_handle *h, double tout, int exact_tstop, int64_t max_steps, d
 
 // Classical RK4 with fixed dt on device vectors (differentiation form forward).
 int rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps) {
-  const int n = 3 * h->mesh.N;
+  const int n = 3 * h->mesh.N * h->nrep;
   DevBuf<double> buf;
   if (buf.alloc(5 * (size_t)n)) return 100;
   double *k1 = buf.p, *k2 = k1 + n, *k3 = k2 + n, *k4 = k3 + n, *y = k4 + n;

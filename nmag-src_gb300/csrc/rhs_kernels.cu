@@ -76,7 +76,7 @@ struct CGArgs {
 constexpr int kAgg = 64;   // rows per aggregate (4 aggregates per 256-row block)
 
 // ---- single-reduction CG on a counter barrier ----
-constexpr int kCG2MaxRed = 8;   // widest fused reduction (projection dots + b.b)
+constexpr int kCG2MaxRed = 7 * kChunk;   // widest fused reduction (projection dots + b.b per ensemble member)
 
 // gpu-scope acquire load
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
@@ -114,12 +114,14 @@ __device__ __forceinline__ bool reduce_all(const CGArgs &a, unsigned epoch, doub
   if (threadIdx.x == 0)
     for (int j = 0; j < NV; ++j) slot[blockIdx.x * kCG2MaxRed + j] = v[j];
   if (!arrive_wait(a, epoch)) return false;
-  if (threadIdx.x < 32) {
-    for (int j = 0; j < NV; ++j) {
+  {
+    // value j is summed by warp j % (warps per block): the values proceed in parallel
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int j = wid; j < NV; j += nw) {
       double s = 0.0;
-      for (unsigned b = threadIdx.x; b < gridDim.x; b += 32) s += __ldcg(slot + b * kCG2MaxRed + j);
+      for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(slot + b * kCG2MaxRed + j);
       s = warp_sum(s);
-      if (threadIdx.x == 0) smem[j] = s;
+      if (lane == 0) smem[j] = s;
     }
   }
   __syncthreads();
@@ -359,6 +361,280 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBas
   }
 }
 
+// Ensemble form of k_cg3: the same persistent single-reduction CG for nm <= MB
+// right-hand sides at once (member m's vectors at offset m * N).  A row's
+// operator entries are read once for all members; every member has its own
+// scalars, stopping test and projection basis (member m's at offset
+// m * kBasis * N, gram m * kBasis^2, ring 2m), and is frozen once converged;
+// the loop ends when all members have stopped.  Member m's scalar work runs
+// on lane 0 of warp m, so the members' FP64 divisions proceed in parallel.
+template <int MB>
+__global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int nm, CGBasis B) {
+  static_assert(MB * 32 <= kCGThreads, "one warp per member for the scalar work");
+  constexpr int P = kBasis + 1;
+  extern __shared__ double dyn[];
+  __shared__ double smem[32 * P * MB];
+  __shared__ double sc[4 * MB + 1];
+  __shared__ double scoef[MB * kBasis];
+  __shared__ double sagg[MB][2 * (kCGThreads / kAgg)], sec[MB][kCGThreads / kAgg];
+  double *sK = dyn;
+  int *sC = reinterpret_cast<int *>(sK + nnz_cap);
+  const int N = a.N;
+  const int row0 = blockIdx.x * blockDim.x;
+  const int r = row0 + threadIdx.x;
+  const bool active = r < N;
+  const int node = active ? a.perm[r] : 0;
+  const int base = a.prow[row0];
+  const int rend = a.prow[min(row0 + (int)blockDim.x, N)];
+  for (int k = base + threadIdx.x; k < rend; k += blockDim.x) {
+    const int j = a.pcol[k];
+    sC[k - base] = j;
+    sK[k - base] = (a.mode == 1 && a.pbnd[j]) ? 0.0 : a.pK[k];
+  }
+  int lo = 0, hi = 0;
+  bool ident = false;
+  double dinv = 1.0;
+  double xi[MB], ri[MB], ui[MB], pi[MB], si[MB], wi[MB], bi[MB];
+#pragma unroll
+  for (int m = 0; m < MB; ++m) { xi[m] = ri[m] = ui[m] = pi[m] = si[m] = wi[m] = bi[m] = 0.0; }
+  if (active) {
+    lo = a.prow[r] - base;
+    hi = a.prow[r + 1] - base;
+    ident = a.mode == 1 && a.pbnd[r];
+    dinv = a.dinv[node];
+#pragma unroll
+    for (int m = 0; m < MB; ++m)
+      if (m < nm) { xi[m] = a.x[(size_t)m * N + node]; bi[m] = a.b[(size_t)m * N + node]; }
+  }
+  __syncthreads();
+  // s[m] = (A v_m)_r for every member
+  auto apply = [&](const double *v, double (&s)[MB]) {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) s[m] = 0.0;
+    if (ident) {
+#pragma unroll
+      for (int m = 0; m < MB; ++m) if (m < nm) s[m] = __ldcg(v + (size_t)m * N + r);
+      return;
+    }
+    for (int k = lo; k < hi; ++k) {
+      const double kv = sK[k];
+      const int c = sC[k];
+#pragma unroll
+      for (int m = 0; m < MB; ++m) if (m < nm) s[m] += kv * __ldcg(v + (size_t)m * N + c);
+    }
+  };
+  unsigned epoch = 0;
+  auto precond = [&](const double (&rr)[MB], double (&uu)[MB]) -> bool {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) uu[m] = dinv * rr[m];
+    if (!a.coarse) return true;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      const double s = warp_sum(active ? rr[m] : 0.0);
+      if (lane == 0) sagg[m][wid] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < kCGThreads / kAgg) {
+      const int I = blockIdx.x * (kCGThreads / kAgg) + threadIdx.x;
+      if (I < a.nc)
+        for (int m = 0; m < nm; ++m) a.rc[(size_t)m * a.nc + I] = sagg[m][2 * threadIdx.x] + sagg[m][2 * threadIdx.x + 1];
+    }
+    if (!arrive_wait(a, ++epoch)) return false;
+    const int g = threadIdx.x / kAgg, t = threadIdx.x % kAgg;
+    const int I = blockIdx.x * (kCGThreads / kAgg) + g;
+    double acc[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) acc[m] = 0.0;
+    if (I < a.nc) {
+      const double *row = a.ainv + (size_t)I * a.nc;
+      for (int J = t; J < a.nc; J += kAgg) {
+        const double w = row[J];
+#pragma unroll
+        for (int m = 0; m < MB; ++m) if (m < nm) acc[m] += w * __ldcg(a.rc + (size_t)m * a.nc + J);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      const double s = warp_sum(acc[m]);
+      if (lane == 0) sagg[m][wid] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < kCGThreads / kAgg)
+      for (int m = 0; m < nm; ++m) sec[m][threadIdx.x] = sagg[m][2 * threadIdx.x] + sagg[m][2 * threadIdx.x + 1];
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < MB; ++m) uu[m] += sec[m][g];
+    return true;
+  };
+  // centre b (Neumann)
+  if (a.mode == 0) {
+    double v[MB], t[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) v[m] = active ? bi[m] : 0.0;
+    if (!reduce_all<MB>(a, ++epoch, v, smem, t)) return;
+#pragma unroll
+    for (int m = 0; m < MB; ++m) if (active) bi[m] -= t[m] / N;
+  }
+  // projection of each member's b onto its stored right-hand sides (+ b.b)
+  int count[MB], head[MB];
+#pragma unroll
+  for (int m = 0; m < MB; ++m) {
+    count[m] = m < nm ? B.ring[2 * m] : 0;
+    head[m] = m < nm ? B.ring[2 * m + 1] : 0;
+  }
+  double bdot[P * MB];
+  {
+    double proj[P * MB];
+#pragma unroll
+    for (int q = 0; q < P * MB; ++q) proj[q] = 0.0;
+    if (active) {
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        const double *bb = B.b + (size_t)m * kBasis * N;
+        for (int j = 0; j < count[m]; ++j) proj[P * m + j] = bi[m] * bb[(size_t)j * N + r];
+        proj[P * m + kBasis] = bi[m] * bi[m];
+      }
+    }
+    if (!reduce_all<P * MB>(a, ++epoch, proj, smem, bdot)) return;
+  }
+  double tol[MB];
+#pragma unroll
+  for (int m = 0; m < MB; ++m) tol[m] = fmax(a.rtol * sqrt(bdot[P * m + kBasis]), a.atol);
+#pragma unroll
+  for (int m = 0; m < MB; ++m) {
+    if (threadIdx.x == 32 * m && count[m] > 0) {
+      double c[kBasis];
+      small_solve(count[m], B.gram + m * kBasis * kBasis, bdot + P * m, c);
+      for (int j = 0; j < count[m]; ++j) scoef[m * kBasis + j] = c[j];
+    }
+  }
+  __syncthreads();
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      if (count[m] == 0) continue;
+      const double *bx = B.x + (size_t)m * kBasis * N;
+      double g = 0.0;
+      for (int j = 0; j < count[m]; ++j) g += scoef[m * kBasis + j] * bx[(size_t)j * N + r];
+      xi[m] = ident ? bi[m] : g;
+    }
+#pragma unroll
+    for (int m = 0; m < MB; ++m) if (m < nm) a.xperm[(size_t)m * N + r] = xi[m];
+  }
+  if (!arrive_wait(a, ++epoch)) return;
+  {
+    double ax[MB];
+    apply(a.xperm, ax);
+#pragma unroll
+    for (int m = 0; m < MB; ++m) ri[m] = active ? bi[m] - ax[m] : 0.0;
+  }
+  if (!precond(ri, ui)) return;
+  if (active)
+#pragma unroll
+    for (int m = 0; m < MB; ++m) if (m < nm) a.z[(size_t)m * N + r] = ui[m];
+  if (!arrive_wait(a, ++epoch)) return;
+  double alpha[MB], gamma[MB];
+  int state[MB];   // 0 running, 1 converged, 2 failed
+#pragma unroll
+  for (int m = 0; m < MB; ++m) { alpha[m] = gamma[m] = 0.0; state[m] = m < nm ? 0 : 1; }
+  int it = 0;
+  for (;;) {
+    double v[3 * MB], t[3 * MB];
+    apply(a.z, wi);
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      v[3 * m] = active ? ri[m] * ui[m] : 0.0;
+      v[3 * m + 1] = active ? wi[m] * ui[m] : 0.0;
+      v[3 * m + 2] = active ? ri[m] * ri[m] : 0.0;
+    }
+    if (!reduce_all<3 * MB>(a, ++epoch, v, smem, t)) return;
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      if (threadIdx.x != 32 * m) continue;
+      int st = state[m];
+      double be = 0.0, al = alpha[m];
+      if (st == 0) {
+        if (!(t[3 * m + 2] == t[3 * m + 2]) || isinf(t[3 * m + 2])) st = 2;
+        else if (sqrt(t[3 * m + 2]) <= tol[m]) st = 1;
+        else if (it >= a.maxits) st = 2;
+      }
+      if (st == 0) {
+        if (it == 0) al = t[3 * m] / t[3 * m + 1];
+        else { be = t[3 * m] / gamma[m]; al = t[3 * m] / (t[3 * m + 1] - be * t[3 * m] / alpha[m]); }
+      }
+      sc[4 * m] = al; sc[4 * m + 1] = be; sc[4 * m + 2] = st == 0 ? t[3 * m] : gamma[m]; sc[4 * m + 3] = st;
+    }
+    __syncthreads();
+    int running = 0;
+    double beta[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      alpha[m] = sc[4 * m];
+      beta[m] = sc[4 * m + 1];
+      gamma[m] = sc[4 * m + 2];
+      state[m] = (int)sc[4 * m + 3];
+      running += state[m] == 0;
+    }
+    __syncthreads();
+    if (running == 0) break;
+    if (active) {
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        if (state[m] != 0) continue;
+        pi[m] = ui[m] + beta[m] * pi[m];
+        si[m] = wi[m] + beta[m] * si[m];
+        xi[m] += alpha[m] * pi[m];
+        ri[m] -= alpha[m] * si[m];
+      }
+    }
+    if (!precond(ri, ui)) return;
+    if (active)
+#pragma unroll
+      for (int m = 0; m < MB; ++m) if (m < nm) a.z[(size_t)m * N + r] = ui[m];
+    ++it;
+    if (!arrive_wait(a, ++epoch)) return;
+  }
+  bool failed = false;
+#pragma unroll
+  for (int m = 0; m < MB; ++m) failed = failed || state[m] == 2;
+  if (a.mode == 0) {
+    double v[MB], t[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) v[m] = active ? xi[m] : 0.0;
+    if (!reduce_all<MB>(a, ++epoch, v, smem, t)) return;
+#pragma unroll
+    for (int m = 0; m < MB; ++m) xi[m] -= t[m] / N;
+  }
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      if (m >= nm) break;
+      a.x[(size_t)m * N + node] = xi[m];
+      B.b[(size_t)m * kBasis * N + (size_t)head[m] * N + r] = bi[m];   // this solve joins the basis
+      B.x[(size_t)m * kBasis * N + (size_t)head[m] * N + r] = xi[m];
+    }
+  }
+  if (r == 0) {
+    a.iters[a.mode] = it;
+    a.iters[2 + a.mode] += it;
+    if (failed) atomicOr(a.err, ERR_CG_MAXITS);
+  }
+#pragma unroll
+  for (int m = 0; m < MB; ++m) {
+    if (r != 32 * m || m >= nm) continue;   // block 0, lane 0 of warp m: member m's Gram row/column and ring
+    double *G = B.gram + m * kBasis * kBasis;
+    const int ncount = count[m] < kBasis ? count[m] + 1 : kBasis;
+    for (int j = 0; j < ncount; ++j) {
+      const double gv = (j == head[m]) ? bdot[P * m + kBasis] : bdot[P * m + j];
+      G[head[m] * kBasis + j] = gv;
+      G[j * kBasis + head[m]] = gv;
+    }
+    B.ring[2 * m] = ncount;
+    B.ring[2 * m + 1] = (head[m] + 1) % kBasis;
+  }
+}
+
 __global__ void k_dinv(int N, const int32_t *__restrict__ diag_pos, const double *__restrict__ K,
                        const int32_t *__restrict__ b_of_node, double *__restrict__ dn, double *__restrict__ dd) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -371,21 +647,25 @@ __global__ void k_dinv(int N, const int32_t *__restrict__ diag_pos, const double
 // rho = -(Ms * sum_k (D_x m_x + D_y m_y + D_z m_z))
 __global__ void k_div(int N, int nnz, double Ms, const int32_t *__restrict__ row_ptr,
                       const int32_t *__restrict__ col_idx, const double *__restrict__ D,
-                      const double *__restrict__ m, double *__restrict__ rho) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+                      const double *__restrict__ m, double *__restrict__ rho, int nrep = 1) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= (long long)N * nrep) return;
+  const int b = (int)(g / N), i = (int)(g - (long long)b * N);
+  const double *mb = m + (size_t)b * 3 * N;
   double s = 0.0;
   for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
-    const double *mj = m + 3 * (size_t)col_idx[k];
+    const double *mj = mb + 3 * (size_t)col_idx[k];
     s += (D[k] * mj[0] + D[(size_t)nnz + k] * mj[1]) + D[2 * (size_t)nnz + k] * mj[2];
   }
-  rho[i] = -(Ms * s);
+  rho[g] = -(Ms * s);
 }
 
 __global__ void k_gather_b(int nb, const int32_t *__restrict__ node_of_b, const double *__restrict__ phi,
-                           double *__restrict__ out) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < nb) out[b] = phi[node_of_b[b]];
+                           double *__restrict__ out, int N = 0, int nrep = 1) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nb * nrep) return;
+  const int mbr = g / nb, j = g - mbr * nb;
+  out[g] = phi[(size_t)mbr * N + node_of_b[j]];
 }
 
 // BEM product y = B x over the row-major matrix (row stride ld, a multiple of
@@ -507,9 +787,233 @@ __global__ void k_row_sum(int nb, long long Q, long long seg, int maxr, long lon
   y[r] = s;
 }
 
-__global__ void k_to_f32_vec(int n, int ld, const double *__restrict__ a, float *__restrict__ b) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < ld) b[i] = i < n ? (float)a[i] : 0.0f;
+__global__ void k_to_f32_vec(int n, int ld, const double *__restrict__ a, float *__restrict__ b, int nm = 1) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ld * nm) return;
+  const int m = g / ld, i = g - m * ld;
+  b[g] = i < n ? (float)a[(size_t)m * n + i] : 0.0f;
+}
+
+// Ensemble BEM products Y = B X for nm <= MB members (x member m at m * nb,
+// FP32 copies at m * ld, zero-padded): the warp-segment decomposition of
+// k_gemv_*, every matrix unit multiplied into all members' accumulators, so
+// the matrix is streamed once per nm right-hand sides.  Partials at
+// part[(w * maxr + row slot) * MB + m].
+template <int MB>
+__global__ void __launch_bounds__(kGemvThreads) k_gemm_f64(int nb, int ld, long long seg, int maxr, int nm,
+                                                            const double *__restrict__ B,
+                                                            const double *__restrict__ x, double *__restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long Q = ld / 4, total = (long long)nb * Q;
+  const long long q0 = w * seg, q1 = min(total, q0 + seg);
+  if (q0 >= q1) return;
+  const long long rfirst = q0 / Q;
+  for (long long r = rfirst; r * Q < q1; ++r) {
+    const long long a = max(q0, r * Q), e = min(q1, (r + 1) * Q);
+    const double *row = B + r * (long long)ld;
+    double acc[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) acc[m] = 0.0;
+    for (long long q = a + lane; q < e; q += 32) {
+      const double2 *p = reinterpret_cast<const double2 *>(row + 4 * (q - r * Q));
+      const double2 v0 = __ldcs(p), v1 = __ldcs(p + 1);
+      const int c = (int)(4 * (q - r * Q));
+      const int c0 = min(c, nb - 1), c1 = min(c + 1, nb - 1), c2 = min(c + 2, nb - 1), c3 = min(c + 3, nb - 1);
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        if (m >= nm) break;
+        const double *xm = x + (size_t)m * nb;
+        double t = fma(v0.x, __ldg(xm + c0), acc[m]);
+        t = fma(v0.y, __ldg(xm + c1), t);
+        t = fma(v1.x, __ldg(xm + c2), t);
+        acc[m] = fma(v1.y, __ldg(xm + c3), t);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      if (m >= nm) break;
+      const double s = warp_sum(acc[m]);
+      if (lane == 0) part[(w * maxr + (r - rfirst)) * MB + m] = s;
+    }
+  }
+}
+
+template <int MB>
+__global__ void __launch_bounds__(kGemvThreads) k_gemm_f32(int nb, int ld, long long seg, int maxr, int nm,
+                                                            const float *__restrict__ B,
+                                                            const float *__restrict__ x, double *__restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long Q = ld / 8, total = (long long)nb * Q;
+  const long long q0 = w * seg, q1 = min(total, q0 + seg);
+  if (q0 >= q1) return;
+  const long long rfirst = q0 / Q;
+  for (long long r = rfirst; r * Q < q1; ++r) {
+    const long long a = max(q0, r * Q), e = min(q1, (r + 1) * Q);
+    const float *row = B + r * (long long)ld;
+    double acc[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) acc[m] = 0.0;
+    long long q = a + lane;
+    for (; q + 32 < e; q += 64) {
+      float4 v[2][2];
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const float4 *p = reinterpret_cast<const float4 *>(row + 8 * (q - r * Q + 32 * u));
+        v[u][0] = __ldcs(p);
+        v[u][1] = __ldcs(p + 1);
+      }
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        if (m >= nm) break;
+        float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const float4 *px = reinterpret_cast<const float4 *>(x + (size_t)m * ld + 8 * (q - r * Q + 32 * u));
+          const float4 x0 = __ldg(px), x1 = __ldg(px + 1);
+          s0 = fmaf(v[u][0].x, x0.x, s0); s1 = fmaf(v[u][0].y, x0.y, s1);
+          s0 = fmaf(v[u][0].z, x0.z, s0); s1 = fmaf(v[u][0].w, x0.w, s1);
+          s0 = fmaf(v[u][1].x, x1.x, s0); s1 = fmaf(v[u][1].y, x1.y, s1);
+          s0 = fmaf(v[u][1].z, x1.z, s0); s1 = fmaf(v[u][1].w, x1.w, s1);
+        }
+        acc[m] += (double)(s0 + s1);
+      }
+    }
+    for (; q < e; q += 32) {
+      const float4 *p = reinterpret_cast<const float4 *>(row + 8 * (q - r * Q));
+      const float4 v0 = __ldcs(p), v1 = __ldcs(p + 1);
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        if (m >= nm) break;
+        const float4 *px = reinterpret_cast<const float4 *>(x + (size_t)m * ld + 8 * (q - r * Q));
+        const float4 x0 = __ldg(px), x1 = __ldg(px + 1);
+        float s0 = v0.x * x0.x;
+        s0 = fmaf(v0.y, x0.y, s0); s0 = fmaf(v0.z, x0.z, s0); s0 = fmaf(v0.w, x0.w, s0);
+        s0 = fmaf(v1.x, x1.x, s0); s0 = fmaf(v1.y, x1.y, s0); s0 = fmaf(v1.z, x1.z, s0); s0 = fmaf(v1.w, x1.w, s0);
+        acc[m] += (double)s0;
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      if (m >= nm) break;
+      const double s = warp_sum(acc[m]);
+      if (lane == 0) part[(w * maxr + (r - rfirst)) * MB + m] = s;
+    }
+  }
+}
+
+// FP32 ensemble product on tiles: block (slab, row block) stages the slab's
+// kTileCols entries of x for every member in shared memory, and each warp
+// streams kTileRpw rows at once, so one shared-memory read of x serves
+// kTileRpw rows.  FP32 sums within the slab, one partial per (slab, row,
+// member) in FP64: part[(slab * nb + row) * MB + m].  A lane's 32 products of
+// a (row, member) are summed in FP32, everything after that in FP64.
+constexpr int kTileCols = 1024, kTileRpw = 4, kTileRows = 64;
+
+// Sum each of NV values over the warp with recursive halving (31 shuffles for
+// NV = 32): afterwards lane L holds the total of value L >> (5 - log2 NV).
+template <int NV>
+__device__ __forceinline__ double warp_transpose_sum(double (&v)[NV]) {
+  const int lane = threadIdx.x & 31;
+  int n = NV;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    if (n > 1) {
+      const bool up = (lane & o) != 0;
+#pragma unroll
+      for (int i = 0; i < NV / 2; ++i) {
+        if (i >= n / 2) break;
+        const double send = up ? v[i] : v[i + n / 2];
+        const double keep = up ? v[i + n / 2] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+      n >>= 1;
+    } else {
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+    }
+  }
+  return v[0];
+}
+
+template <int MB>
+__global__ void __launch_bounds__(256) k_gemm_f32t(int nb, int ld, int nm, const float *__restrict__ B,
+                                                   const float *__restrict__ x, double *__restrict__ part) {
+  __shared__ float4 xs[MB][kTileCols / 4];
+  const int slab = blockIdx.x, c0 = slab * kTileCols;
+  const int ncol = min(kTileCols, ld - c0);   // a multiple of 8 (ld and c0 are)
+  for (int i = threadIdx.x; i < MB * (kTileCols / 4); i += blockDim.x) {
+    const int m = i / (kTileCols / 4), q = i - m * (kTileCols / 4);
+    xs[m][q] = (m < nm && 4 * q < ncol) ? __ldg(reinterpret_cast<const float4 *>(x + (size_t)m * ld + c0) + q)
+                                        : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int units = ncol / 8;
+  const int rend = min(nb, (int)(blockIdx.y + 1) * kTileRows);
+  for (int r0 = blockIdx.y * kTileRows + warp * kTileRpw; r0 < rend; r0 += 8 * kTileRpw) {
+    float acc[kTileRpw * MB];
+#pragma unroll
+    for (int q = 0; q < kTileRpw * MB; ++q) acc[q] = 0.f;
+    const float *rows[kTileRpw];
+#pragma unroll
+    for (int rr = 0; rr < kTileRpw; ++rr) rows[rr] = B + (size_t)min(r0 + rr, nb - 1) * ld + c0;
+    for (int u = lane; u < units; u += 32) {
+      float4 a[kTileRpw][2];
+#pragma unroll
+      for (int rr = 0; rr < kTileRpw; ++rr) {
+        const float4 *p = reinterpret_cast<const float4 *>(rows[rr] + 8 * u);
+        a[rr][0] = __ldcs(p);
+        a[rr][1] = __ldcs(p + 1);
+      }
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        const float4 x0 = xs[m][2 * u], x1 = xs[m][2 * u + 1];
+#pragma unroll
+        for (int rr = 0; rr < kTileRpw; ++rr) {
+          float t = acc[rr * MB + m];
+          t = fmaf(a[rr][0].x, x0.x, t); t = fmaf(a[rr][0].y, x0.y, t);
+          t = fmaf(a[rr][0].z, x0.z, t); t = fmaf(a[rr][0].w, x0.w, t);
+          t = fmaf(a[rr][1].x, x1.x, t); t = fmaf(a[rr][1].y, x1.y, t);
+          t = fmaf(a[rr][1].z, x1.z, t); t = fmaf(a[rr][1].w, x1.w, t);
+          acc[rr * MB + m] = t;
+        }
+      }
+    }
+    constexpr int NV = kTileRpw * MB;
+    constexpr int SH = NV >= 32 ? 0 : (NV >= 16 ? 1 : (NV >= 8 ? 2 : (NV >= 4 ? 3 : (NV >= 2 ? 4 : 5))));
+    double accd[NV];   // lane sums (32 products each in FP32) combined in FP64
+#pragma unroll
+    for (int q = 0; q < NV; ++q) accd[q] = (double)acc[q];
+    const double tot = warp_transpose_sum<NV>(accd);
+    const int v = lane >> SH;
+    const int rr = v / MB, m = v - rr * MB;
+    if ((lane & ((1 << SH) - 1)) == 0 && m < nm && r0 + rr < nb)
+      part[((size_t)slab * nb + r0 + rr) * MB + m] = tot;
+  }
+}
+
+// y[m * nb + r] = sum over slabs of member m's tile partials of row r.
+__global__ void k_slab_sum_m(int nb, int nslab, int nm, int MB, const double *__restrict__ part,
+                             double *__restrict__ y) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nb * nm) return;
+  const int m = g / nb, r = g - m * nb;
+  double s = 0.0;
+  for (int sl = 0; sl < nslab; ++sl) s += part[((size_t)sl * nb + r) * MB + m];
+  y[(size_t)m * nb + r] = s;
+}
+
+// y[m * nb + r] = ordered sum of member m's partials of row r.
+__global__ void k_row_sum_m(int nb, long long Q, long long seg, int maxr, long long nwarps, int nm, int MB,
+                            const double *__restrict__ part, double *__restrict__ y) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= nb * nm) return;
+  const int m = g / nb, r = g - m * nb;
+  const long long w0 = ((long long)r * Q) / seg, w1 = min(nwarps - 1, ((long long)(r + 1) * Q - 1) / seg);
+  double s = 0.0;
+  for (long long w = w0; w <= w1; ++w) s += part[(w * maxr + (r - (w * seg) / Q)) * MB + m];
+  y[(size_t)m * nb + r] = s;
 }
 
 // Dirichlet right-hand side (op_load_DBC, sign folded): interior rows
@@ -517,17 +1021,20 @@ __global__ void k_to_f32_vec(int n, int ld, const double *__restrict__ a, float 
 // warm start are set to phi2b.
 __global__ void k_dbc_rhs(int N, const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col_idx,
                           const double *__restrict__ K, const int32_t *__restrict__ b_of_node,
-                          const double *__restrict__ phi2b, double *__restrict__ rhs, double *__restrict__ phi2) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= N) return;
+                          const double *__restrict__ phi2b_all, double *__restrict__ rhs, double *__restrict__ phi2,
+                          int nb = 0, int nrep = 1) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= (long long)N * nrep) return;
+  const int mbr = (int)(g / N), i = (int)(g - (long long)mbr * N);
+  const double *phi2b = phi2b_all + (size_t)mbr * nb;
   int bi = b_of_node[i];
-  if (bi >= 0) { rhs[i] = phi2b[bi]; phi2[i] = phi2b[bi]; return; }
+  if (bi >= 0) { rhs[g] = phi2b[bi]; phi2[g] = phi2b[bi]; return; }
   double s = 0.0;
   for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
     int b = b_of_node[col_idx[k]];
     if (b >= 0) s += K[k] * phi2b[b];
   }
-  rhs[i] = -s;
+  rhs[g] = -s;
 }
 
 __global__ void k_add(int n, const double *__restrict__ a, const double *__restrict__ b, double *__restrict__ c) {
@@ -536,7 +1043,7 @@ __global__ void k_add(int n, const double *__restrict__ a, const double *__restr
 }
 
 struct NodeArgs {
-  int N, nnz, do_demag;
+  int N, nnz, do_demag, nrep;   // nrep members: m, h_ext and outputs member-major (3N each), phi N each
   const int32_t *row_ptr, *col_idx;
   const double *K, *G, *vol, *m, *phi, *h_ext;
   const double *anis_node;   // per-node anisotropy coefficient (element parameters) or null
@@ -546,24 +1053,27 @@ struct NodeArgs {
 
 // Fused node kernel: the two SpMV epilogues and every site-wise equation.
 __global__ void k_heff_llg(NodeArgs a) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.N) return;
+  const long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gi >= (long long)a.N * a.nrep) return;
+  const int mbr = (int)(gi / a.N), i = (int)(gi - (long long)mbr * a.N);
+  const double *mm = a.m + (size_t)mbr * 3 * a.N;
+  const double *ph = a.do_demag ? a.phi + (size_t)mbr * a.N : a.phi;
   double s0 = 0.0, s1 = 0.0, s2 = 0.0, g0 = 0.0, g1 = 0.0, g2 = 0.0;
   const int lo = a.row_ptr[i], hi = a.row_ptr[i + 1];
   for (int k = lo; k < hi; ++k) {
     const int j = a.col_idx[k];
     const double kv = a.K[k];
-    const double *mj = a.m + 3 * (size_t)j;
+    const double *mj = mm + 3 * (size_t)j;
     s0 += kv * mj[0]; s1 += kv * mj[1]; s2 += kv * mj[2];
     if (a.do_demag) {
-      const double pj = a.phi[j];
+      const double pj = ph[j];
       g0 += a.G[k] * pj; g1 += a.G[(size_t)a.nnz + k] * pj; g2 += a.G[2 * (size_t)a.nnz + k] * pj;
     }
   }
   const double V = a.vol[i];
   const double hx[3] = {-a.c_exch * s0 / V, -a.c_exch * s1 / V, -a.c_exch * s2 / V};
   const double hd[3] = {-g0 / V, -g1 / V, -g2 / V};
-  const double *m = a.m + 3 * (size_t)i;
+  const double *m = mm + 3 * (size_t)i;
   double ha[3] = {0.0, 0.0, 0.0};
   if (a.K1 != 0.0 || a.anis_node) {
     const double c = a.anis_node ? a.anis_node[i] : a.anis;
@@ -572,7 +1082,7 @@ __global__ void k_heff_llg(NodeArgs a) {
     ha[1] = c * am * (a.ay - am * m[1]);
     ha[2] = c * am * (a.az - am * m[2]);
   }
-  const double *he = a.h_ext + 3 * (size_t)i;
+  const double *he = a.h_ext + 3 * (size_t)gi;
   double H[3];
   for (int d = 0; d < 3; ++d) H[d] = ((he[d] + hx[d]) + ha[d]) + hd[d];
   const double mxH[3] = {m[1] * H[2] - m[2] * H[1], m[2] * H[0] - m[0] * H[2], m[0] * H[1] - m[1] * H[0]};
@@ -580,7 +1090,7 @@ __global__ void k_heff_llg(NodeArgs a) {
                            m[0] * mxH[1] - m[1] * mxH[0]};
   const double c3 = a.C3 * (1.0 - ((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2]));
   for (int d = 0; d < 3; ++d) {
-    const size_t o = 3 * (size_t)i + d;
+    const size_t o = 3 * (size_t)gi + d;
     a.h_exch[o] = hx[d]; a.h_demag[o] = hd[d]; a.h_anis[o] = ha[d]; a.h_total[o] = H[d];
     a.dmdt[o] = (a.C1 * mxH[d] + a.C2 * mxmxH[d]) + c3 * m[d];
   }
@@ -604,14 +1114,14 @@ __global__ void k_energy(int N, const double *__restrict__ m, const double *__re
 
 // Block partial sums of V_i, V_i m_i (3) and V_i E_k,i (5): 9 columns.
 __global__ void k_avg_partials(int N, const double *__restrict__ m, const double *__restrict__ vol,
-                               const double *__restrict__ E, double *__restrict__ part) {
+                               const double *__restrict__ E, double *__restrict__ part, size_t estride) {
   __shared__ double smem[32 * 9];
   double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
     double V = vol[i];
     v[0] += V;
     for (int d = 0; d < 3; ++d) v[1 + d] += V * m[3 * (size_t)i + d];
-    if (E) for (int k = 0; k < 5; ++k) v[4 + k] += V * E[(size_t)k * N + i];
+    if (E) for (int k = 0; k < 5; ++k) v[4 + k] += V * E[(size_t)k * estride + i];
   }
   block_sum<9>(v, smem);
   if (threadIdx.x == 0) for (int j = 0; j < 9; ++j) part[9 * blockIdx.x + j] = v[j];
@@ -707,7 +1217,7 @@ int build_cg_ordering(nmg_handle *h, std::string &err) {
   NMG_CUDA_TRY(W.pcol.alloc(nnz), "alloc");
   NMG_CUDA_TRY(W.pbnd.alloc(N), "alloc");
   NMG_CUDA_TRY(W.pK.alloc(nnz), "alloc");
-  NMG_CUDA_TRY(W.xperm.alloc(N), "alloc");
+  NMG_CUDA_TRY(W.xperm.alloc((size_t)N * std::min(h->nrep, kChunk)), "alloc");
   NMG_CUDA_TRY(cudaMemcpy(W.perm.p, perm.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "h2d");
   NMG_CUDA_TRY(cudaMemcpy(W.prow.p, prow.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice), "h2d");
   NMG_CUDA_TRY(cudaMemcpy(W.pcol.p, pcol.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice), "h2d");
@@ -752,7 +1262,7 @@ int build_cg_ordering(nmg_handle *h, std::string &err) {
       Ainv[(size_t)j * nc + i] = s;
     }
   NMG_CUDA_TRY(W.ainv.alloc((size_t)nc * nc), "alloc coarse inverse");
-  NMG_CUDA_TRY(W.rc.alloc(nc), "alloc");
+  NMG_CUDA_TRY(W.rc.alloc((size_t)nc * std::min(h->nrep, kChunk)), "alloc");
   NMG_CUDA_TRY(cudaMemcpy(W.ainv.p, Ainv.data(), sizeof(double) * nc * nc, cudaMemcpyHostToDevice), "h2d");
   W.nc = nc;
   return 0;
@@ -796,6 +1306,44 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   return 0;
 }
 
+// Ensemble CG: nm <= kChunk right-hand sides (member m at b + m * N).
+int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm, double rtol, double atol,
+            int maxits) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  CGArgs a;
+  a.N = M.N; a.mode = mode;
+  a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.b_of_node = M.b_of_node; a.K = M.K;
+  a.dinv = mode == 0 ? W.dinv_n.p : W.dinv_d.p;
+  a.b = b; a.x = x; a.r = W.cg_r; a.z = W.cg_z; a.p = W.cg_p; a.q = W.cg_q; a.red = W.red;
+  a.w = W.cg_w; a.flags = W.bar; a.tot = W.cg_tot;
+  a.bar = W.bar; a.err = W.err; a.iters = W.iters;
+  a.rtol = rtol; a.atol = atol; a.maxits = maxits;
+  a.perm = W.perm; a.prow = W.prow; a.pcol = W.pcol; a.pbnd = W.pbnd; a.pK = W.pK; a.xperm = W.xperm;
+  a.coarse = (mode == 0 && W.nc > 0) ? 1 : 0;
+  a.nc = W.nc; a.ainv = W.ainv; a.rc = W.rc;
+  cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
+  int cap = W.cg_nnz_cap;
+  CGBasis basis;
+  const size_t slot = (size_t)mode * h->nrep + c0;   // first member of this chunk
+  basis.b = W.ens_basis_b.p + slot * kBasis * M.N;
+  basis.x = W.ens_basis_x.p + slot * kBasis * M.N;
+  basis.gram = W.ens_basis_gram.p + slot * kBasis * kBasis;
+  basis.ring = W.ens_basis_ring.p + 2 * slot;
+  void *args[] = {&a, &cap, &nm, &basis};
+  const void *fn = nm <= 2 ? (const void *)k_cgm<2> : (nm <= 4 ? (const void *)k_cgm<4> : (const void *)k_cgm<8>);
+  NMG_PROF_BEGIN(h, 1 + mode);
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(W.cg_blocks), dim3(kCGThreads), args,
+                                              (size_t)W.cg_smem_bytes, h->stream);
+  NMG_PROF_END(h);
+  ++h->launches;
+  if (e != cudaSuccess) {
+    h->last_error = std::string("ensemble CG launch failed: ") + cudaGetErrorString(e);
+    return 100;
+  }
+  return 0;
+}
+
 }  // namespace
 
 int cg_solve(nmg_handle *h, int slot, const double *b, double *x, double rtol, double atol, int maxits) {
@@ -810,20 +1358,24 @@ int init_workspace(nmg_handle *h, std::string &err) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   const int N = M.N, nb = M.nb;
-  const size_t n3 = 3 * (size_t)N;
+  const int B = h->nrep, BC = std::min(B, kChunk);   // members; members per CG / BEM launch
+  const size_t n3 = 3 * (size_t)N * B, nB = (size_t)N * B;
   for (DevBuf<double> *b : {&W.m, &W.h_ext, &W.h_exch, &W.h_demag, &W.h_anis, &W.h_total, &W.dmdt})
     NMG_CUDA_TRY(b->alloc(n3), "alloc field");
-  for (DevBuf<double> *b : {&W.rho, &W.phi1, &W.phi2, &W.phi, &W.rhs2, &W.cg_r, &W.cg_z, &W.cg_p, &W.cg_q,
-                            &W.dinv_n, &W.dinv_d})
+  for (DevBuf<double> *b : {&W.rho, &W.phi1, &W.phi2, &W.phi, &W.rhs2})
+    NMG_CUDA_TRY(b->alloc(nB), "alloc scalar field");
+  for (DevBuf<double> *b : {&W.cg_r, &W.cg_z, &W.cg_p, &W.cg_q})
+    NMG_CUDA_TRY(b->alloc((size_t)N * BC), "alloc CG vectors");
+  for (DevBuf<double> *b : {&W.dinv_n, &W.dinv_d})
     NMG_CUDA_TRY(b->alloc(N), "alloc scalar field");
-  NMG_CUDA_TRY(W.b1.alloc(nb > 0 ? nb : 1), "alloc");
-  NMG_CUDA_TRY(W.b2.alloc(nb > 0 ? nb : 1), "alloc");
-  NMG_CUDA_TRY(W.E5.alloc(5 * (size_t)N), "alloc");
+  NMG_CUDA_TRY(W.b1.alloc(nb > 0 ? (size_t)nb * B : 1), "alloc");
+  NMG_CUDA_TRY(W.b2.alloc(nb > 0 ? (size_t)nb * B : 1), "alloc");
+  NMG_CUDA_TRY(W.E5.alloc(5 * nB), "alloc");
   cudaMemsetAsync(W.m.p, 0, sizeof(double) * n3, h->stream);
   cudaMemsetAsync(W.h_ext.p, 0, sizeof(double) * n3, h->stream);
-  cudaMemsetAsync(W.phi1.p, 0, sizeof(double) * N, h->stream);
-  cudaMemsetAsync(W.phi2.p, 0, sizeof(double) * N, h->stream);
-  cudaMemsetAsync(W.phi.p, 0, sizeof(double) * N, h->stream);
+  cudaMemsetAsync(W.phi1.p, 0, sizeof(double) * nB, h->stream);
+  cudaMemsetAsync(W.phi2.p, 0, sizeof(double) * nB, h->stream);
+  cudaMemsetAsync(W.phi.p, 0, sizeof(double) * nB, h->stream);
   for (DevBuf<double> *b : {&W.h_exch, &W.h_demag, &W.h_anis, &W.h_total, &W.dmdt})
     cudaMemsetAsync(b->p, 0, sizeof(double) * n3, h->stream);
   // CG grid: one row per thread when it fits in one co-resident wave.
@@ -865,6 +1417,19 @@ int init_workspace(nmg_handle *h, std::string &err) {
             std::to_string(per_sm * h->sm_count * kCGThreads) + " nodes here)";
       return 4;
     }
+    if (B > 1 && h->opt.do_demag) {
+      // the ensemble CG kernels hold up to kChunk members per row in registers
+      for (const void *fn : {(const void *)k_cgm<2>, (const void *)k_cgm<4>, (const void *)k_cgm<8>}) {
+        int per = 0;
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kCGThreads, W.cg_smem_bytes) != cudaSuccess ||
+            per * h->sm_count < W.cg_blocks) {
+          cudaGetLastError();
+          err = "mesh too large for the ensemble CG (" + std::to_string(W.cg_blocks) + " co-resident blocks needed)";
+          return 4;
+        }
+      }
+    }
   }
   // BEM product grid: every resident warp streams an equal share of the
   // flattened matrix (units of 32 bytes; rows of ld entries).
@@ -886,17 +1451,28 @@ int init_workspace(nmg_handle *h, std::string &err) {
       part_n = std::max(part_n, (size_t)(warps * W.gemv_maxr[f]));
     }
   }
-  // partials, then an FP32 copy of x padded to ld (ld/2 doubles of room)
+  // partials (kChunk members for the ensemble), then FP32 copies of x padded to ld
+  part_n *= (B > 1 ? kChunk : 1);
+  if (B > 1 && nb > 0)   // FP32 tiles: one partial per (slab, row, member)
+    part_n = std::max(part_n, (size_t)((M.ld + kTileCols - 1) / kTileCols) * nb * kChunk);
   W.gemv_x32_off = (part_n + 7) / 8 * 8;
-  NMG_CUDA_TRY(W.bpart.alloc(W.gemv_x32_off + (size_t)M.ld / 2 + 8), "alloc gemv partials");
-  size_t red_n = 2 * 8 * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);  // 2 parities x 8 values
+  NMG_CUDA_TRY(W.bpart.alloc(W.gemv_x32_off + (size_t)BC * M.ld / 2 + 8), "alloc gemv partials");
+  // 2 parities x kCG2MaxRed values per block (at least 1024 blocks: averages use it too)
+  size_t red_n = 2 * (size_t)kCG2MaxRed * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);
   NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
   NMG_CUDA_TRY(W.bar.alloc(W.cg_blocks + 2), "alloc barrier");
-  NMG_CUDA_TRY(W.cg_w.alloc(N), "alloc");
+  NMG_CUDA_TRY(W.cg_w.alloc((size_t)N * BC), "alloc");
   NMG_CUDA_TRY(W.basis_b.alloc(kCGSlots * (size_t)kBasis * N), "alloc CG basis");
   NMG_CUDA_TRY(W.basis_x.alloc(kCGSlots * (size_t)kBasis * N), "alloc CG basis");
   NMG_CUDA_TRY(W.basis_gram.alloc(kCGSlots * kBasis * kBasis), "alloc");
   NMG_CUDA_TRY(W.basis_ring.alloc(2 * kCGSlots), "alloc");
+  if (B > 1) {
+    NMG_CUDA_TRY(W.ens_basis_b.alloc(2 * (size_t)B * kBasis * N), "alloc ensemble CG basis");
+    NMG_CUDA_TRY(W.ens_basis_x.alloc(2 * (size_t)B * kBasis * N), "alloc ensemble CG basis");
+    NMG_CUDA_TRY(W.ens_basis_gram.alloc(2 * (size_t)B * kBasis * kBasis), "alloc");
+    NMG_CUDA_TRY(W.ens_basis_ring.alloc(4 * (size_t)B), "alloc");
+    cudaMemsetAsync(W.ens_basis_ring.p, 0, sizeof(int) * 4 * B, h->stream);
+  }
   cudaMemsetAsync(W.basis_ring.p, 0, sizeof(int) * 2 * kCGSlots, h->stream);
   NMG_CUDA_TRY(W.cg_tot.alloc(2 * 4), "alloc");
   NMG_CUDA_TRY(W.iters.alloc(4), "alloc");
@@ -931,6 +1507,49 @@ void bem_gemv(nmg_handle *h, const double *x, double *y) {
   ++h->launches;
 }
 
+// Y = B X for the ensemble (member m at x + m * nb), kChunk members per pass.
+void bem_gemm(nmg_handle *h, const double *x, double *y) {
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  const int nb = M.nb, B = h->nrep;
+  const int f = (h->opt.bem_precision == 1 && M.bem32.p) ? 1 : 0;
+  const long long seg = W.gemv_seg[f];
+  const int maxr = W.gemv_maxr[f];
+  const long long Q = M.ld / (f == 0 ? 4 : 8);
+  const long long nwarps = (long long)W.gemv_blocks * (kGemvThreads / 32);
+  for (int c0 = 0; c0 < B; c0 += kChunk) {
+    const int nm = std::min(kChunk, B - c0);
+    const int MB = nm <= 2 ? 2 : (nm <= 4 ? 4 : 8);
+    const double *xc = x + (size_t)c0 * nb;
+    if (f == 1) {
+      float *x32 = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
+      k_to_f32_vec<<<nblk((long long)M.ld * nm, 256), 256, 0, h->stream>>>(nb, M.ld, xc, x32, nm); ++h->launches;
+      const int nslab = (M.ld + kTileCols - 1) / kTileCols;
+      dim3 grid(nslab, (nb + kTileRows - 1) / kTileRows);
+      NMG_PROF_BEGIN(h, 0);
+      if (MB == 2) k_gemm_f32t<2><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, x32, W.bpart);
+      else if (MB == 4) k_gemm_f32t<4><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, x32, W.bpart);
+      else k_gemm_f32t<8><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, x32, W.bpart);
+      NMG_PROF_END(h);
+      ++h->launches;
+      k_slab_sum_m<<<nblk((long long)nb * nm, 256), 256, 0, h->stream>>>(nb, nslab, nm, MB, W.bpart,
+                                                                         y + (size_t)c0 * nb);
+      ++h->launches;
+      continue;
+    } else {
+      NMG_PROF_BEGIN(h, 0);
+      if (MB == 2) k_gemm_f64<2><<<W.gemv_blocks, kGemvThreads, 0, h->stream>>>(nb, M.ld, seg, maxr, nm, M.bem, xc, W.bpart);
+      else if (MB == 4) k_gemm_f64<4><<<W.gemv_blocks, kGemvThreads, 0, h->stream>>>(nb, M.ld, seg, maxr, nm, M.bem, xc, W.bpart);
+      else k_gemm_f64<8><<<W.gemv_blocks, kGemvThreads, 0, h->stream>>>(nb, M.ld, seg, maxr, nm, M.bem, xc, W.bpart);
+      NMG_PROF_END(h);
+    }
+    ++h->launches;
+    k_row_sum_m<<<nblk((long long)nb * nm, 256), 256, 0, h->stream>>>(nb, Q, seg, maxr, nwarps, nm, MB, W.bpart,
+                                                                      y + (size_t)c0 * nb);
+    ++h->launches;
+  }
+}
+
 int check_device_error(nmg_handle *h, const char *where) {
   int derr = 0;
   cudaError_t e = cudaMemcpyAsync(&derr, h->ws.err.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
@@ -956,7 +1575,24 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
   cudaStream_t s = h->stream;
   const int N = M.N;
   const nmg_material &mt = h->mat;
-  if (h->opt.do_demag && M.nb > 0) {
+  const int B = h->nrep;
+  if (h->opt.do_demag && M.nb > 0 && B > 1) {
+    // ensemble: the same pipeline over B members, kChunk members per CG / BEM launch
+    const long long NB = (long long)N * B;
+    k_div<<<nblk(NB, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, h->ep.active ? h->ep.Dx.p : M.D.p, d_m,
+                                        W.rho, B); ++h->launches;
+    for (int c0 = 0; c0 < B; c0 += kChunk)
+      if (run_cgm(h, 0, c0, W.rho.p + (size_t)c0 * N, W.phi1.p + (size_t)c0 * N, std::min(kChunk, B - c0),
+                  h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
+    k_gather_b<<<nblk((long long)M.nb * B, 256), 256, 0, s>>>(M.nb, M.node_of_b, W.phi1, W.b1, N, B); ++h->launches;
+    bem_gemm(h, W.b1, W.b2);
+    k_dbc_rhs<<<nblk(NB, 256), 256, 0, s>>>(N, M.row_ptr, M.col_idx, M.K, M.b_of_node, W.b2, W.rhs2, W.phi2, M.nb, B);
+    ++h->launches;
+    for (int c0 = 0; c0 < B; c0 += kChunk)
+      if (run_cgm(h, 1, c0, W.rhs2.p + (size_t)c0 * N, W.phi2.p + (size_t)c0 * N, std::min(kChunk, B - c0),
+                  h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)) return 100;
+    k_add<<<nblk(NB, 256), 256, 0, s>>>((int)NB, W.phi1, W.phi2, W.phi); ++h->launches;
+  } else if (h->opt.do_demag && M.nb > 0) {
     k_div<<<nblk(N, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, h->ep.active ? h->ep.Dx.p : M.D.p, d_m,
                                        W.rho); ++h->launches;
     if (run_cg(h, 0, W.rho, W.phi1, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
@@ -967,7 +1603,7 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
     k_add<<<nblk(N, 256), 256, 0, s>>>(N, W.phi1, W.phi2, W.phi); ++h->launches;
   }
   NodeArgs a;
-  a.N = N; a.nnz = M.nnz; a.do_demag = (h->opt.do_demag && M.nb > 0) ? 1 : 0;
+  a.N = N; a.nnz = M.nnz; a.do_demag = (h->opt.do_demag && M.nb > 0) ? 1 : 0; a.nrep = B;
   a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.K = h->exch_K(); a.G = M.G; a.vol = M.vol;
   a.m = d_m; a.phi = W.phi; a.h_ext = W.h_ext;
   a.anis_node = h->ep.active ? h->ep.anis.p : nullptr;
@@ -978,7 +1614,7 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
   a.dmdt = d_dmdt ? d_dmdt : W.dmdt.p;
   {
     NMG_PROF_BEGIN(h, 3);
-    k_heff_llg<<<nblk(N, 128), 128, 0, s>>>(a); ++h->launches;
+    k_heff_llg<<<nblk((long long)N * B, 128), 128, 0, s>>>(a); ++h->launches;
     NMG_PROF_END(h);
   }
   h->n_rhs++;
@@ -989,18 +1625,20 @@ int energy_density(nmg_handle *h, const double *d_m, double *d_E5) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   const nmg_material &mt = h->mat;
-  k_energy<<<nblk(M.N, 256), 256, 0, h->stream>>>(M.N, d_m, W.h_exch, W.h_demag, W.h_ext, mt.E_coeff_half,
+  const int NB = M.N * h->nrep;   // pointwise over all members: E[k * NB + member * N + i]
+  k_energy<<<nblk(NB, 256), 256, 0, h->stream>>>(NB, d_m, W.h_exch, W.h_demag, W.h_ext, mt.E_coeff_half,
                                                   mt.E_coeff_ext, mt.K1, mt.axis[0], mt.axis[1], mt.axis[2], d_E5); ++h->launches;
   return cudaGetLastError() == cudaSuccess ? 0 : 100;
 }
 
-int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5]) {
+int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5], int member) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   const int nblocks = 64;
-  const double *E = energies ? W.E5.p : nullptr;
+  const double *E = energies ? W.E5.p + (size_t)member * M.N : nullptr;
   if (energies && energy_density(h, d_m, W.E5)) return 100;
-  k_avg_partials<<<nblocks, 256, 0, h->stream>>>(M.N, d_m, M.vol, E, W.red); ++h->launches;
+  k_avg_partials<<<nblocks, 256, 0, h->stream>>>(M.N, d_m + (size_t)member * 3 * M.N, M.vol, E, W.red,
+                                                 (size_t)M.N * h->nrep); ++h->launches;
   std::vector<double> part(9 * nblocks);
   if (cudaMemcpyAsync(part.data(), W.red.p, sizeof(double) * 9 * nblocks, cudaMemcpyDeviceToHost, h->stream) ||
       cudaStreamSynchronize(h->stream))
@@ -1015,7 +1653,7 @@ int averages(nmg_handle *h, const double *d_m, double avg[3], double energies[5]
 
 int max_dm(nmg_handle *h, const double *d_m, const double *d_mprev, double *out) {
   const int nblocks = 64;
-  k_maxdm_partials<<<nblocks, 256, 0, h->stream>>>(h->mesh.N, d_m, d_mprev, h->ws.red); ++h->launches;
+  k_maxdm_partials<<<nblocks, 256, 0, h->stream>>>(h->mesh.N * h->nrep, d_m, d_mprev, h->ws.red); ++h->launches;
   double part[nblocks];
   if (cudaMemcpyAsync(part, h->ws.red.p, sizeof(double) * nblocks, cudaMemcpyDeviceToHost, h->stream) ||
       cudaStreamSynchronize(h->stream))

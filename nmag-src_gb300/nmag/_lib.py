@@ -26,7 +26,7 @@ class Options(C.Structure):
     _fields_ = [("do_demag", C.c_int), ("nbc_rtol", C.c_double), ("nbc_atol", C.c_double), ("nbc_maxits", C.c_int),
                 ("dbc_rtol", C.c_double), ("dbc_atol", C.c_double), ("dbc_maxits", C.c_int),
                 ("bem_precision", C.c_int), ("cg_precision", C.c_int), ("cg_no_coarse", C.c_int),
-                ("reserved", C.c_int * 5)]
+                ("n_members", C.c_int), ("reserved", C.c_int * 4)]
 
 
 class TsStats(C.Structure):
@@ -45,7 +45,8 @@ EXPORTS = ["nmg_version", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_me
            "nmg_set_material", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
            "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
            "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_max_dm_static",
-           "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint"]
+           "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
+           "nmg_member_averages"]
 
 PROFILED_KERNELS = ["bem_gemv", "cg_neumann", "cg_dirichlet", "heff_llg", "jv_psolve"]
 
@@ -101,6 +102,7 @@ def lib(build_if_missing=True):
     L.nmg_launch_count.restype = C.c_int64
     L.nmg_cg_iterations.argtypes = [vp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]
     L.nmg_max_dm_static.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_double)]
+    L.nmg_member_averages.argtypes = [vp, C.c_int, _f64p, vp]
     L.nmg_set_element_params.argtypes = [vp, vp, vp, vp, _f64p]
     L.nmg_clear_element_params.argtypes = [vp]
     L.nmg_rk4_forward.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, vp]
@@ -130,6 +132,10 @@ class Engine(object):
         info = np.zeros(6, np.int64)
         L.nmg_mesh_info(h, info)
         self.N, self.T, self.nnz, self.nb, self.ntri, self.nouter = (int(v) for v in info)
+        self.B = max(1, int(options.n_members))   # ensemble members (arrays gain a leading member axis)
+
+    def _shape3(self):
+        return (self.B, self.N, 3) if self.B > 1 else (self.N, 3)
 
     def close(self):
         if getattr(self, "h", None):
@@ -147,12 +153,12 @@ class Engine(object):
         check(lib().nmg_set_m(self.h, np.ascontiguousarray(m, dtype=np.float64).reshape(-1)), self.h, "set_m")
 
     def get_m(self):
-        out = np.zeros(3 * self.N)
+        out = np.zeros(3 * self.N * self.B)
         check(lib().nmg_get_m(self.h, out), self.h, "get_m")
-        return out.reshape(self.N, 3)
+        return out.reshape(self._shape3())
 
     def set_h_ext(self, h):
-        h = np.broadcast_to(np.asarray(h, dtype=np.float64), (self.N, 3))
+        h = np.broadcast_to(np.asarray(h, dtype=np.float64), self._shape3())
         check(lib().nmg_set_h_ext(self.h, np.ascontiguousarray(h).reshape(-1)), self.h, "set_h_ext")
 
     def set_material(self, mat: Material):
@@ -160,23 +166,32 @@ class Engine(object):
 
     # ---- evaluation ----
     def eval_fields(self):
-        f = np.zeros(15 * self.N)
-        s = np.zeros(2 * self.N)
+        n = self.N * self.B
+        f = np.zeros(15 * n)
+        s = np.zeros(2 * n)
         check(lib().nmg_eval_fields(self.h, f.ctypes.data, s.ctypes.data), self.h, "eval_fields")
-        f = f.reshape(5, self.N, 3)
+        f = f.reshape((5,) + self._shape3())
+        sh = (self.B, self.N) if self.B > 1 else (self.N,)
         return {"H_exch": f[0], "H_demag": f[1], "H_anis": f[2], "H_total": f[3], "dmdt": f[4],
-                "phi": s[:self.N], "rho": s[self.N:]}
+                "phi": s[:n].reshape(sh), "rho": s[n:].reshape(sh)}
 
     def energy_density(self):
-        E = np.zeros(5 * self.N)
+        E = np.zeros(5 * self.N * self.B)
         check(lib().nmg_energy_density(self.h, E), self.h, "energy_density")
-        E = E.reshape(5, self.N)
+        E = E.reshape((5, self.B, self.N) if self.B > 1 else (5, self.N))
         return {"E_exch": E[0], "E_demag": E[1], "E_ext": E[2], "E_anis": E[3], "E_total": E[4]}
 
     def averages(self, energies=False):
         a = np.zeros(3)
         e = np.zeros(5)
         check(lib().nmg_averages(self.h, a, e.ctypes.data if energies else None), self.h, "averages")
+        return (a, e) if energies else a
+
+    def member_averages(self, member, energies=False):
+        a = np.zeros(3)
+        e = np.zeros(5)
+        check(lib().nmg_member_averages(self.h, int(member), a, e.ctypes.data if energies else None), self.h,
+              "member_averages")
         return (a, e) if energies else a
 
     # ---- time integration ----

@@ -100,7 +100,7 @@ class Simulation(object):
     def __init__(self, name=None, phi_BEM=None, periodic_bc=None, do_demag=True, do_anisotropy_jacobian=False,
                  temperature=None, thermal_delta_t=None, user_seed_T=0, timestepper_max_order=2,
                  timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
-                 lam_debugfile=None, quirks="nmag", bem_precision="fp64"):
+                 lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1):
         if periodic_bc is not None:
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
@@ -114,6 +114,9 @@ class Simulation(object):
         self.ksp_tolerances = dict(ksp_tolerances or {})
         self.quirks = quirks
         self.bem_precision = bem_precision
+        # ensemble: n_members simulations on one mesh, integrated together;
+        # per-node arrays then carry a leading member axis (GB300 extension)
+        self.n_members = max(1, int(n_members))
         self.ts_rel_tol = 1e-6
         self.ts_abs_tol = 1e-6
         self.stopping_dm_dt = simulation_units.of(_si.degrees_per_ns)   # 1 deg/ns
@@ -156,10 +159,11 @@ class Simulation(object):
         opts.nbc_rtol, opts.nbc_atol, opts.nbc_maxits = tol("NBC.rtol", 1e-5), tol("NBC.atol", 1e-50), int(tol("NBC.maxits", 10000))
         opts.dbc_rtol, opts.dbc_atol, opts.dbc_maxits = tol("DBC.rtol", 1e-5), tol("DBC.atol", 1e-50), int(tol("DBC.maxits", 10000))
         opts.bem_precision = {"fp64": 0, "fp32": 1}[self.bem_precision]
+        opts.n_members = self.n_members if self.n_members > 1 else 0
         self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
-        N = self.engine.N
-        self._m = np.zeros((N, 3))
-        self._h_ext = np.zeros((N, 3))
+        shape = self.engine._shape3()
+        self._m = np.zeros(shape)
+        self._h_ext = np.zeros(shape)
         self._ts_ready = False
         return self.mesh
 
@@ -183,6 +187,19 @@ class Simulation(object):
         return self.mesh.points * simulation_units.conversion_factor_of(SI("m"))
 
     def _vector_values(self, values):
+        B = self.n_members
+        if B > 1:
+            if isinstance(values, (list, tuple)) and len(values) == B and not (
+                    B == 3 and all(np.isscalar(v) or isinstance(v, SI) for v in values)):
+                return np.stack([self._one_vector_values(v) for v in values])
+            arr = None if callable(values) else np.asarray(values, dtype=np.float64)
+            if arr is not None and arr.shape == (B, self.engine.N, 3):
+                return arr.copy()
+            one = self._one_vector_values(values)
+            return np.broadcast_to(one, (B,) + one.shape).copy()
+        return self._one_vector_values(values)
+
+    def _one_vector_values(self, values):
         N = self.engine.N
         if callable(values):
             pos = self._positions_si()
@@ -195,10 +212,10 @@ class Simulation(object):
     def set_m(self, values, subfieldname=None):
         """main.py:1787: set m (auto-normalised)."""
         m = self._vector_values(values)
-        n = np.linalg.norm(m, axis=1)
+        n = np.linalg.norm(m, axis=-1)
         if np.any(n == 0.0):
             raise ValueError("set_m: zero-length magnetisation vector")
-        m = m / n[:, None]
+        m = m / n[..., None]
         self._m = m
         self.engine.set_m(m)
         self._ts_ready = False
@@ -270,7 +287,7 @@ class Simulation(object):
         self.clock.last_step_dt_su = stats["hcur"]
         self.last_stats = stats
         if prev_m is not None and delta_t > 0.0:
-            dm = np.sqrt(((self._m - prev_m) ** 2).sum(axis=1)).max()
+            dm = np.sqrt(((self._m - prev_m) ** 2).sum(axis=-1)).max()
             self.max_dm_dt = dm / delta_t
         return SI(t_stage * simulation_units.conversion_factor_of(SI("s")), "s")
 
@@ -370,7 +387,7 @@ class Simulation(object):
     def get_subfield_average_siv(self, field, subfield=None):
         name = field if subfield is None else field
         if name == "m" or name.startswith("m_"):
-            return list(self.engine.averages())
+            return list(self.engine.averages())   # member 0 of an ensemble
         vals = self.get_subfield(name)
         V = self._volumes()
         if vals.ndim == 2:
@@ -379,6 +396,10 @@ class Simulation(object):
 
     def get_subfield_average(self, field, subfield=None):
         return self.get_subfield_average_siv(field, subfield)
+
+    def get_member_average_m(self, member):
+        """<m> of one ensemble member."""
+        return list(self.engine.member_averages(member))
 
     def _volumes(self):
         if not hasattr(self, "_vol_cache"):
