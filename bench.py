@@ -227,7 +227,7 @@ def config_dict(args, msh):
     return {"workload": WORKLOAD_NAMES[args.workload],
             "relax": "alpha=1, H_ext=0 for %.3g ps before the timed dynamics (untimed)" % args.relax_ps,
             "nodes": int(msh.n_nodes), "tets": int(msh.n_tets), "step": "%.3g ps advance + <m> read" % args.step_ps,
-            "form": args.form, "members": args.members,
+            "form": args.form, "cg": args.cg, "members": args.members,
             "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
             "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % (8 if args.form == "fp64" else 4)}
 
@@ -242,7 +242,8 @@ def run_ours(args):
     torch.cuda.init()
     msh, base, seed = workload(args.workload)
     B = args.members
-    sim = nmag.Simulation("bench", bem_precision=args.form, n_members=B)
+    # fp32 form: FP32 BEM matrix (FP64 sums); --cg fp32: FP32 CG iterations with FP64 residual refinement
+    sim = nmag.Simulation("bench", bem_precision=args.form, cg_precision=args.cg, n_members=B)
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     if B > 1:   # member b starts from the workload's initial state with seed + b
@@ -371,6 +372,8 @@ def main():
     ap.add_argument("--step-ps", type=float, default=1.0)
     ap.add_argument("--relax-ps", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cg", default="fp64", choices=["fp64", "fp32"],
+                    help="Poisson CG: FP64, or FP32 iterations with FP64 residual refinement")
     ap.add_argument("--members", type=int, default=1,
                     help="ensemble size: B films on the one mesh integrated together (value summed over members)")
     args = ap.parse_args()

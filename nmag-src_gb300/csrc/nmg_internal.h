@@ -77,6 +77,8 @@ struct Workspace {
   DevBuf<int> ens_basis_ring;
   DevBuf<int32_t> perm, prow, pcol, pbnd;     // CG solver ordering (spatially binned nodes)
   DevBuf<double> pK, xperm, ainv, rc;         // K in that order, iterate, coarse inverse, coarse residual
+  DevBuf<float> ainv32, rc32, z32;            // FP32 copies / vectors of the mixed-precision CG
+  int cg_smem_mp = 0;                         // dynamic shared memory of the mixed-precision CG
   int nc = 0;                                 // aggregates of the two-level Neumann CG (0: none)
   int cg_blocks = 0;
   int cg_smem_bytes = 0;     // >0: shared-memory CG (one row per thread)

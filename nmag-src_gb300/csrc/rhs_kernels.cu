@@ -37,12 +37,14 @@ __device__ __forceinline__ double warp_sum(double v) {
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double *smem) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
   for (int j = 0; j < NV; ++j) {
     double s = warp_sum(v[j]);
     if (lane == 0) smem[wid * NV + j] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+#pragma unroll
     for (int j = 0; j < NV; ++j) {
       double s = 0.0;
       for (int w = 0; w < nw; ++w) s += smem[w * NV + j];
@@ -72,6 +74,11 @@ struct CGArgs {
   int coarse, nc;
   const double *ainv; // nc x nc inverse of the (regularised) aggregated operator
   double *rc;         // restricted residual, nc
+  // mixed-precision CG: FP32 copies for the inner iterations
+  const float *ainv32;
+  float *rc32, *z32;  // coarse residual (nc x MB), published inner direction (N x MB)
+  float eta;          // inner relative tolerance
+  int max_outer;      // FP64 refinement steps
 };
 constexpr int kAgg = 64;   // rows per aggregate (4 aggregates per 256-row block)
 
@@ -112,6 +119,7 @@ __device__ __forceinline__ bool reduce_all(const CGArgs &a, unsigned epoch, doub
   block_sum<NV>(v, smem);
   double *slot = a.red + (size_t)(epoch & 1) * gridDim.x * kCG2MaxRed;
   if (threadIdx.x == 0)
+#pragma unroll
     for (int j = 0; j < NV; ++j) slot[blockIdx.x * kCG2MaxRed + j] = v[j];
   if (!arrive_wait(a, epoch)) return false;
   {
@@ -126,6 +134,28 @@ __device__ __forceinline__ bool reduce_all(const CGArgs &a, unsigned epoch, doub
   }
   __syncthreads();
   for (int j = 0; j < NV; ++j) out[j] = smem[j];
+  __syncthreads();
+  return true;
+}
+
+// reduce_all with the totals left in shared memory (res[0..NV)) instead of
+// registers: the ensemble CG keeps its per-member values there.
+template <int NV>
+__device__ __forceinline__ bool reduce_all_to(const CGArgs &a, unsigned epoch, double (&v)[NV], double *smem,
+                                              double *res) {
+  block_sum<NV>(v, smem);
+  double *slot = a.red + (size_t)(epoch & 1) * gridDim.x * kCG2MaxRed;
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) slot[blockIdx.x * kCG2MaxRed + j] = v[j];
+  if (!arrive_wait(a, epoch)) return false;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = wid; j < NV; j += nw) {
+    double s = 0.0;
+    for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(slot + b * kCG2MaxRed + j);
+    s = warp_sum(s);
+    if (lane == 0) res[j] = s;
+  }
   __syncthreads();
   return true;
 }
@@ -373,20 +403,26 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
   static_assert(MB * 32 <= kCGThreads, "one warp per member for the scalar work");
   constexpr int P = kBasis + 1;
   extern __shared__ double dyn[];
-  __shared__ double smem[32 * P * MB];
-  __shared__ double sc[4 * MB + 1];
+  __shared__ double smem[kCGThreads / 32 * P * MB];   // block_sum scratch
+  __shared__ double sres[P * MB];                     // totals of the last reduction
+  __shared__ double sbdot[P * MB];                    // projection dots (Gram update at the end)
+  __shared__ double s_al[MB], s_be[MB], s_ga[MB], s_tol[MB];
+  __shared__ int s_st[MB];
+  __shared__ int s_cnt[MB], s_head[MB];               // ring read once: block 0 rewrites it at the end
   __shared__ double scoef[MB * kBasis];
+  __shared__ double sbi[MB][kCGThreads];              // (centred) right-hand sides of this block's rows
   __shared__ double sagg[MB][2 * (kCGThreads / kAgg)], sec[MB][kCGThreads / kAgg];
   double *sK = dyn;
   int *sC = reinterpret_cast<int *>(sK + nnz_cap);
   const int N = a.N;
+  const int tid = threadIdx.x;
   const int row0 = blockIdx.x * blockDim.x;
-  const int r = row0 + threadIdx.x;
+  const int r = row0 + tid;
   const bool active = r < N;
   const int node = active ? a.perm[r] : 0;
   const int base = a.prow[row0];
   const int rend = a.prow[min(row0 + (int)blockDim.x, N)];
-  for (int k = base + threadIdx.x; k < rend; k += blockDim.x) {
+  for (int k = base + tid; k < rend; k += blockDim.x) {
     const int j = a.pcol[k];
     sC[k - base] = j;
     sK[k - base] = (a.mode == 1 && a.pbnd[j]) ? 0.0 : a.pK[k];
@@ -394,33 +430,61 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
   int lo = 0, hi = 0;
   bool ident = false;
   double dinv = 1.0;
-  double xi[MB], ri[MB], ui[MB], pi[MB], si[MB], wi[MB], bi[MB];
+  double xi[MB], ri[MB], ui[MB], pi[MB], si[MB], wi[MB];
 #pragma unroll
-  for (int m = 0; m < MB; ++m) { xi[m] = ri[m] = ui[m] = pi[m] = si[m] = wi[m] = bi[m] = 0.0; }
+  for (int m = 0; m < MB; ++m) {
+    xi[m] = ri[m] = ui[m] = pi[m] = si[m] = wi[m] = 0.0;
+    sbi[m][tid] = (active && m < nm) ? a.b[(size_t)m * N + node] : 0.0;
+  }
   if (active) {
     lo = a.prow[r] - base;
     hi = a.prow[r + 1] - base;
     ident = a.mode == 1 && a.pbnd[r];
     dinv = a.dinv[node];
 #pragma unroll
-    for (int m = 0; m < MB; ++m)
-      if (m < nm) { xi[m] = a.x[(size_t)m * N + node]; bi[m] = a.b[(size_t)m * N + node]; }
+    for (int m = 0; m < MB; ++m) if (m < nm) xi[m] = a.x[(size_t)m * N + node];
+  }
+  if (tid < MB) {
+    s_cnt[tid] = tid < nm ? B.ring[2 * tid] : 0;
+    s_head[tid] = tid < nm ? B.ring[2 * tid + 1] : 0;
   }
   __syncthreads();
-  // s[m] = (A v_m)_r for every member
+  // s[m] = (A v_m)_r for every member; published vectors are member-minor
+  // (v[row * MB + m]) so that one neighbour's members share cache lines
   auto apply = [&](const double *v, double (&s)[MB]) {
 #pragma unroll
     for (int m = 0; m < MB; ++m) s[m] = 0.0;
     if (ident) {
+      const double2 *vr = reinterpret_cast<const double2 *>(v + (size_t)r * MB);
 #pragma unroll
-      for (int m = 0; m < MB; ++m) if (m < nm) s[m] = __ldcg(v + (size_t)m * N + r);
+      for (int q = 0; q < MB / 2; ++q) { const double2 t = __ldcg(vr + q); s[2 * q] = t.x; s[2 * q + 1] = t.y; }
       return;
     }
-    for (int k = lo; k < hi; ++k) {
-      const double kv = sK[k];
-      const int c = sC[k];
+    int k = lo;
+    for (; k + 2 <= hi; k += 2) {   // two neighbours' loads in flight
+      const double kv0 = sK[k], kv1 = sK[k + 1];
+      const double2 *vc0 = reinterpret_cast<const double2 *>(v + (size_t)sC[k] * MB);
+      const double2 *vc1 = reinterpret_cast<const double2 *>(v + (size_t)sC[k + 1] * MB);
+      double2 t0[MB / 2], t1[MB / 2];
 #pragma unroll
-      for (int m = 0; m < MB; ++m) if (m < nm) s[m] += kv * __ldcg(v + (size_t)m * N + c);
+      for (int q = 0; q < MB / 2; ++q) { t0[q] = __ldcg(vc0 + q); t1[q] = __ldcg(vc1 + q); }
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q) {
+        s[2 * q] += kv0 * t0[q].x;
+        s[2 * q + 1] += kv0 * t0[q].y;
+        s[2 * q] += kv1 * t1[q].x;
+        s[2 * q + 1] += kv1 * t1[q].y;
+      }
+    }
+    for (; k < hi; ++k) {
+      const double kv = sK[k];
+      const double2 *vc = reinterpret_cast<const double2 *>(v + (size_t)sC[k] * MB);
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q) {
+        const double2 t = __ldcg(vc + q);
+        s[2 * q] += kv * t.x;
+        s[2 * q + 1] += kv * t.y;
+      }
     }
   };
   unsigned epoch = 0;
@@ -428,30 +492,36 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
 #pragma unroll
     for (int m = 0; m < MB; ++m) uu[m] = dinv * rr[m];
     if (!a.coarse) return true;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int lane = tid & 31, wid = tid >> 5;
 #pragma unroll
     for (int m = 0; m < MB; ++m) {
       const double s = warp_sum(active ? rr[m] : 0.0);
       if (lane == 0) sagg[m][wid] = s;
     }
     __syncthreads();
-    if (threadIdx.x < kCGThreads / kAgg) {
-      const int I = blockIdx.x * (kCGThreads / kAgg) + threadIdx.x;
+    if (tid < kCGThreads / kAgg) {
+      const int I = blockIdx.x * (kCGThreads / kAgg) + tid;
       if (I < a.nc)
-        for (int m = 0; m < nm; ++m) a.rc[(size_t)m * a.nc + I] = sagg[m][2 * threadIdx.x] + sagg[m][2 * threadIdx.x + 1];
+        for (int m = 0; m < MB; ++m) a.rc[(size_t)I * MB + m] = sagg[m][2 * tid] + sagg[m][2 * tid + 1];
     }
     if (!arrive_wait(a, ++epoch)) return false;
-    const int g = threadIdx.x / kAgg, t = threadIdx.x % kAgg;
+    const int g = tid / kAgg, t = tid % kAgg;
     const int I = blockIdx.x * (kCGThreads / kAgg) + g;
     double acc[MB];
 #pragma unroll
     for (int m = 0; m < MB; ++m) acc[m] = 0.0;
     if (I < a.nc) {
       const double *row = a.ainv + (size_t)I * a.nc;
+#pragma unroll 2
       for (int J = t; J < a.nc; J += kAgg) {
         const double w = row[J];
+        const double2 *rcJ = reinterpret_cast<const double2 *>(a.rc + (size_t)J * MB);
 #pragma unroll
-        for (int m = 0; m < MB; ++m) if (m < nm) acc[m] += w * __ldcg(a.rc + (size_t)m * a.nc + J);
+        for (int q = 0; q < MB / 2; ++q) {
+          const double2 t = __ldcg(rcJ + q);
+          acc[2 * q] += w * t.x;
+          acc[2 * q + 1] += w * t.y;
+        }
       }
     }
 #pragma unroll
@@ -460,8 +530,8 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
       if (lane == 0) sagg[m][wid] = s;
     }
     __syncthreads();
-    if (threadIdx.x < kCGThreads / kAgg)
-      for (int m = 0; m < nm; ++m) sec[m][threadIdx.x] = sagg[m][2 * threadIdx.x] + sagg[m][2 * threadIdx.x + 1];
+    if (tid < kCGThreads / kAgg)
+      for (int m = 0; m < nm; ++m) sec[m][tid] = sagg[m][2 * tid] + sagg[m][2 * tid + 1];
     __syncthreads();
 #pragma unroll
     for (int m = 0; m < MB; ++m) uu[m] += sec[m][g];
@@ -469,21 +539,14 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
   };
   // centre b (Neumann)
   if (a.mode == 0) {
-    double v[MB], t[MB];
+    double v[MB];
 #pragma unroll
-    for (int m = 0; m < MB; ++m) v[m] = active ? bi[m] : 0.0;
-    if (!reduce_all<MB>(a, ++epoch, v, smem, t)) return;
+    for (int m = 0; m < MB; ++m) v[m] = sbi[m][tid];
+    if (!reduce_all_to<MB>(a, ++epoch, v, smem, sres)) return;
 #pragma unroll
-    for (int m = 0; m < MB; ++m) if (active) bi[m] -= t[m] / N;
+    for (int m = 0; m < MB; ++m) if (active) sbi[m][tid] -= sres[m] / N;
   }
   // projection of each member's b onto its stored right-hand sides (+ b.b)
-  int count[MB], head[MB];
-#pragma unroll
-  for (int m = 0; m < MB; ++m) {
-    count[m] = m < nm ? B.ring[2 * m] : 0;
-    head[m] = m < nm ? B.ring[2 * m + 1] : 0;
-  }
-  double bdot[P * MB];
   {
     double proj[P * MB];
 #pragma unroll
@@ -491,128 +554,135 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
     if (active) {
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
+        if (m >= nm) break;
+        const int cnt = s_cnt[m];
+        const double bm = sbi[m][tid];
         const double *bb = B.b + (size_t)m * kBasis * N;
-        for (int j = 0; j < count[m]; ++j) proj[P * m + j] = bi[m] * bb[(size_t)j * N + r];
-        proj[P * m + kBasis] = bi[m] * bi[m];
+#pragma unroll
+        for (int j = 0; j < kBasis; ++j) if (j < cnt) proj[P * m + j] = bm * bb[(size_t)j * N + r];
+        proj[P * m + kBasis] = bm * bm;
       }
     }
-    if (!reduce_all<P * MB>(a, ++epoch, proj, smem, bdot)) return;
+    if (!reduce_all_to<P * MB>(a, ++epoch, proj, smem, sbdot)) return;
   }
-  double tol[MB];
-#pragma unroll
-  for (int m = 0; m < MB; ++m) tol[m] = fmax(a.rtol * sqrt(bdot[P * m + kBasis]), a.atol);
-#pragma unroll
-  for (int m = 0; m < MB; ++m) {
-    if (threadIdx.x == 32 * m && count[m] > 0) {
-      double c[kBasis];
-      small_solve(count[m], B.gram + m * kBasis * kBasis, bdot + P * m, c);
-      for (int j = 0; j < count[m]; ++j) scoef[m * kBasis + j] = c[j];
+  if (tid < MB) s_tol[tid] = fmax(a.rtol * sqrt(sbdot[P * tid + kBasis]), a.atol);
+  {
+    const int m = tid >> 5;
+    if ((tid & 31) == 0 && m < nm) {
+      const int cnt = s_cnt[m];
+      if (cnt > 0) {
+        double c[kBasis];
+        small_solve(cnt, B.gram + m * kBasis * kBasis, sbdot + P * m, c);
+        for (int j = 0; j < cnt; ++j) scoef[m * kBasis + j] = c[j];
+      }
     }
   }
   __syncthreads();
   if (active) {
 #pragma unroll
     for (int m = 0; m < MB; ++m) {
-      if (count[m] == 0) continue;
+      if (m >= nm) break;
+      const int cnt = s_cnt[m];
+      if (cnt == 0) continue;
       const double *bx = B.x + (size_t)m * kBasis * N;
       double g = 0.0;
-      for (int j = 0; j < count[m]; ++j) g += scoef[m * kBasis + j] * bx[(size_t)j * N + r];
-      xi[m] = ident ? bi[m] : g;
+      for (int j = 0; j < cnt; ++j) g += scoef[m * kBasis + j] * bx[(size_t)j * N + r];
+      xi[m] = ident ? sbi[m][tid] : g;
     }
 #pragma unroll
-    for (int m = 0; m < MB; ++m) if (m < nm) a.xperm[(size_t)m * N + r] = xi[m];
+    for (int q = 0; q < MB / 2; ++q)
+      reinterpret_cast<double2 *>(a.xperm + (size_t)r * MB)[q] = make_double2(xi[2 * q], xi[2 * q + 1]);
   }
   if (!arrive_wait(a, ++epoch)) return;
   {
     double ax[MB];
     apply(a.xperm, ax);
 #pragma unroll
-    for (int m = 0; m < MB; ++m) ri[m] = active ? bi[m] - ax[m] : 0.0;
+    for (int m = 0; m < MB; ++m) ri[m] = active ? sbi[m][tid] - ax[m] : 0.0;
   }
   if (!precond(ri, ui)) return;
   if (active)
 #pragma unroll
-    for (int m = 0; m < MB; ++m) if (m < nm) a.z[(size_t)m * N + r] = ui[m];
+    for (int q = 0; q < MB / 2; ++q)
+      reinterpret_cast<double2 *>(a.z + (size_t)r * MB)[q] = make_double2(ui[2 * q], ui[2 * q + 1]);
+  if (tid < MB) { s_al[tid] = 0.0; s_ga[tid] = 0.0; s_be[tid] = 0.0; s_st[tid] = tid < nm ? 0 : 1; }
   if (!arrive_wait(a, ++epoch)) return;
-  double alpha[MB], gamma[MB];
-  int state[MB];   // 0 running, 1 converged, 2 failed
-#pragma unroll
-  for (int m = 0; m < MB; ++m) { alpha[m] = gamma[m] = 0.0; state[m] = m < nm ? 0 : 1; }
   int it = 0;
   for (;;) {
-    double v[3 * MB], t[3 * MB];
-    apply(a.z, wi);
+    {
+      double v[3 * MB];
+      apply(a.z, wi);
 #pragma unroll
-    for (int m = 0; m < MB; ++m) {
-      v[3 * m] = active ? ri[m] * ui[m] : 0.0;
-      v[3 * m + 1] = active ? wi[m] * ui[m] : 0.0;
-      v[3 * m + 2] = active ? ri[m] * ri[m] : 0.0;
+      for (int m = 0; m < MB; ++m) {
+        v[3 * m] = active ? ri[m] * ui[m] : 0.0;
+        v[3 * m + 1] = active ? wi[m] * ui[m] : 0.0;
+        v[3 * m + 2] = active ? ri[m] * ri[m] : 0.0;
+      }
+      if (!reduce_all_to<3 * MB>(a, ++epoch, v, smem, sres)) return;
     }
-    if (!reduce_all<3 * MB>(a, ++epoch, v, smem, t)) return;
-#pragma unroll
-    for (int m = 0; m < MB; ++m) {
-      if (threadIdx.x != 32 * m) continue;
-      int st = state[m];
-      double be = 0.0, al = alpha[m];
-      if (st == 0) {
-        if (!(t[3 * m + 2] == t[3 * m + 2]) || isinf(t[3 * m + 2])) st = 2;
-        else if (sqrt(t[3 * m + 2]) <= tol[m]) st = 1;
-        else if (it >= a.maxits) st = 2;
+    {
+      const int m = tid >> 5;   // lane 0 of warp m: member m's scalars
+      if ((tid & 31) == 0 && m < MB) {
+        int st = s_st[m];
+        double be = 0.0, al = s_al[m];
+        const double t0 = sres[3 * m], t1 = sres[3 * m + 1], t2 = sres[3 * m + 2];
+        if (st == 0) {
+          if (!(t2 == t2) || isinf(t2)) st = 2;
+          else if (sqrt(t2) <= s_tol[m]) st = 1;
+          else if (it >= a.maxits) st = 2;
+        }
+        if (st == 0) {
+          if (it == 0) al = t0 / t1;
+          else { be = t0 / s_ga[m]; al = t0 / (t1 - be * t0 / s_al[m]); }
+          s_ga[m] = t0;
+        }
+        s_al[m] = al; s_be[m] = be; s_st[m] = st;
       }
-      if (st == 0) {
-        if (it == 0) al = t[3 * m] / t[3 * m + 1];
-        else { be = t[3 * m] / gamma[m]; al = t[3 * m] / (t[3 * m + 1] - be * t[3 * m] / alpha[m]); }
-      }
-      sc[4 * m] = al; sc[4 * m + 1] = be; sc[4 * m + 2] = st == 0 ? t[3 * m] : gamma[m]; sc[4 * m + 3] = st;
     }
     __syncthreads();
     int running = 0;
-    double beta[MB];
 #pragma unroll
-    for (int m = 0; m < MB; ++m) {
-      alpha[m] = sc[4 * m];
-      beta[m] = sc[4 * m + 1];
-      gamma[m] = sc[4 * m + 2];
-      state[m] = (int)sc[4 * m + 3];
-      running += state[m] == 0;
-    }
-    __syncthreads();
+    for (int m = 0; m < MB; ++m) running += s_st[m] == 0;
     if (running == 0) break;
     if (active) {
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
-        if (state[m] != 0) continue;
-        pi[m] = ui[m] + beta[m] * pi[m];
-        si[m] = wi[m] + beta[m] * si[m];
-        xi[m] += alpha[m] * pi[m];
-        ri[m] -= alpha[m] * si[m];
+        if (s_st[m] != 0) continue;
+        const double al = s_al[m], be = s_be[m];
+        pi[m] = ui[m] + be * pi[m];
+        si[m] = wi[m] + be * si[m];
+        xi[m] += al * pi[m];
+        ri[m] -= al * si[m];
       }
     }
     if (!precond(ri, ui)) return;
     if (active)
 #pragma unroll
-      for (int m = 0; m < MB; ++m) if (m < nm) a.z[(size_t)m * N + r] = ui[m];
+      for (int q = 0; q < MB / 2; ++q)
+        reinterpret_cast<double2 *>(a.z + (size_t)r * MB)[q] = make_double2(ui[2 * q], ui[2 * q + 1]);
     ++it;
     if (!arrive_wait(a, ++epoch)) return;
   }
   bool failed = false;
 #pragma unroll
-  for (int m = 0; m < MB; ++m) failed = failed || state[m] == 2;
+  for (int m = 0; m < MB; ++m) failed = failed || s_st[m] == 2;
+  __syncthreads();
   if (a.mode == 0) {
-    double v[MB], t[MB];
+    double v[MB];
 #pragma unroll
     for (int m = 0; m < MB; ++m) v[m] = active ? xi[m] : 0.0;
-    if (!reduce_all<MB>(a, ++epoch, v, smem, t)) return;
+    if (!reduce_all_to<MB>(a, ++epoch, v, smem, sres)) return;
 #pragma unroll
-    for (int m = 0; m < MB; ++m) xi[m] -= t[m] / N;
+    for (int m = 0; m < MB; ++m) xi[m] -= sres[m] / N;
   }
   if (active) {
 #pragma unroll
     for (int m = 0; m < MB; ++m) {
       if (m >= nm) break;
+      const int head = s_head[m];
       a.x[(size_t)m * N + node] = xi[m];
-      B.b[(size_t)m * kBasis * N + (size_t)head[m] * N + r] = bi[m];   // this solve joins the basis
-      B.x[(size_t)m * kBasis * N + (size_t)head[m] * N + r] = xi[m];
+      B.b[(size_t)m * kBasis * N + (size_t)head * N + r] = sbi[m][tid];   // this solve joins the basis
+      B.x[(size_t)m * kBasis * N + (size_t)head * N + r] = xi[m];
     }
   }
   if (r == 0) {
@@ -620,18 +690,463 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
     a.iters[2 + a.mode] += it;
     if (failed) atomicOr(a.err, ERR_CG_MAXITS);
   }
+  // every block read the ring into shared memory at its start; block 0,
+  // lane 0 of warp m updates member m's Gram row/column and ring
+  {
+    const int m = tid >> 5;
+    if (blockIdx.x == 0 && (tid & 31) == 0 && m < nm) {
+      double *G = B.gram + m * kBasis * kBasis;
+      const int cnt = s_cnt[m], head = s_head[m];
+      const int ncount = cnt < kBasis ? cnt + 1 : kBasis;
+      for (int j = 0; j < ncount; ++j) {
+        const double gv = (j == head) ? sbdot[P * m + kBasis] : sbdot[P * m + j];
+        G[head * kBasis + j] = gv;
+        G[j * kBasis + head] = gv;
+      }
+      B.ring[2 * m] = ncount;
+      B.ring[2 * m + 1] = (head + 1) % kBasis;
+    }
+  }
+}
+
+// Block-wide FP32 sums of NV values (result in thread 0) for the inner CG.
+template <int NV>
+__device__ __forceinline__ void block_sum_f(float (&v)[NV], float *smem) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    float s = v[j];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) smem[wid * NV + j] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      float s = 0.f;
+      for (int w = 0; w < nw; ++w) s += smem[w * NV + j];
+      v[j] = s;
+    }
+  }
+  __syncthreads();
+}
+
+// Cross-block total of NV FP32 block sums, accumulated in FP64 (res, shared).
+template <int NV>
+__device__ __forceinline__ bool reduce_all_f(const CGArgs &a, unsigned epoch, float (&v)[NV], float *smemf,
+                                             double *res) {
+  block_sum_f<NV>(v, smemf);
+  double *slot = a.red + (size_t)(epoch & 1) * gridDim.x * kCG2MaxRed;
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) slot[blockIdx.x * kCG2MaxRed + j] = (double)v[j];
+  if (!arrive_wait(a, epoch)) return false;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = wid; j < NV; j += nw) {
+    double s = 0.0;
+    for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(slot + b * kCG2MaxRed + j);
+    s = warp_sum(s);
+    if (lane == 0) res[j] = s;
+  }
+  __syncthreads();
+  return true;
+}
+
+// Mixed-precision form of k_cgm (nm <= MB right-hand sides): FP64 projection
+// warm start and FP64 true residual r = b - A x; the correction A d = r is
+// solved by the single-reduction CG in FP32 (operator, preconditioner and
+// vectors FP32; dot products summed in FP32 within a block and in FP64
+// across blocks) to a relative tolerance eta; x += d in FP64; repeated until
+// the FP64 residual meets the tolerance (at most max_outer corrections).
+// GB300's FP32 pipe is ~60x its FP64 pipe: the inner iterations, where all
+// the work is, run on it.
+template <int MB>
+__global__ void __launch_bounds__(kCGThreads) k_cgm_mp(CGArgs a, int nnz_cap, int nm, CGBasis B) {
+  static_assert(MB * 32 <= kCGThreads && MB % 2 == 0, "one warp per member; member pairs");
+  constexpr int P = kBasis + 1;
+  extern __shared__ double dyn[];
+  __shared__ double smem[kCGThreads / 32 * P * MB];
+  __shared__ float smemf[kCGThreads / 32 * 3 * MB];
+  __shared__ double sres[P * MB];
+  __shared__ double sbdot[P * MB];
+  __shared__ double s_al[MB], s_be[MB], s_ga[MB], s_tol[MB], s_itol[MB];
+  __shared__ int s_st[MB], s_out[MB];
+  __shared__ int s_cnt[MB], s_head[MB];
+  __shared__ double scoef[MB * kBasis];
+  __shared__ double sbi[MB][kCGThreads];
+  __shared__ float sagg[MB][2 * (kCGThreads / kAgg)], sec[MB][kCGThreads / kAgg];
+  double *sK = dyn;
+  int *sC = reinterpret_cast<int *>(sK + nnz_cap);
+  float *sK32 = reinterpret_cast<float *>(sC + nnz_cap);
+  const int N = a.N;
+  const int tid = threadIdx.x;
+  const int row0 = blockIdx.x * blockDim.x;
+  const int r = row0 + tid;
+  const bool active = r < N;
+  const int node = active ? a.perm[r] : 0;
+  const int base = a.prow[row0];
+  const int rend = a.prow[min(row0 + (int)blockDim.x, N)];
+  for (int k = base + tid; k < rend; k += blockDim.x) {
+    const int j = a.pcol[k];
+    const double kv = (a.mode == 1 && a.pbnd[j]) ? 0.0 : a.pK[k];
+    sC[k - base] = j;
+    sK[k - base] = kv;
+    sK32[k - base] = (float)kv;
+  }
+  int lo = 0, hi = 0;
+  bool ident = false;
+  double dinv = 1.0;
+  double xi[MB];
 #pragma unroll
   for (int m = 0; m < MB; ++m) {
-    if (r != 32 * m || m >= nm) continue;   // block 0, lane 0 of warp m: member m's Gram row/column and ring
-    double *G = B.gram + m * kBasis * kBasis;
-    const int ncount = count[m] < kBasis ? count[m] + 1 : kBasis;
-    for (int j = 0; j < ncount; ++j) {
-      const double gv = (j == head[m]) ? bdot[P * m + kBasis] : bdot[P * m + j];
-      G[head[m] * kBasis + j] = gv;
-      G[j * kBasis + head[m]] = gv;
+    xi[m] = 0.0;
+    sbi[m][tid] = (active && m < nm) ? a.b[(size_t)m * N + node] : 0.0;
+  }
+  if (active) {
+    lo = a.prow[r] - base;
+    hi = a.prow[r + 1] - base;
+    ident = a.mode == 1 && a.pbnd[r];
+    dinv = a.dinv[node];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) if (m < nm) xi[m] = a.x[(size_t)m * N + node];
+  }
+  const float dinv32 = (float)dinv;
+  if (tid < MB) {
+    s_cnt[tid] = tid < nm ? B.ring[2 * tid] : 0;
+    s_head[tid] = tid < nm ? B.ring[2 * tid + 1] : 0;
+  }
+  __syncthreads();
+  // FP64 operator on the published member-minor FP64 vector
+  auto apply64 = [&](const double *v, double (&s)[MB]) {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) s[m] = 0.0;
+    if (ident) {
+      const double2 *vr = reinterpret_cast<const double2 *>(v + (size_t)r * MB);
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q) { const double2 t = __ldcg(vr + q); s[2 * q] = t.x; s[2 * q + 1] = t.y; }
+      return;
     }
-    B.ring[2 * m] = ncount;
-    B.ring[2 * m + 1] = (head[m] + 1) % kBasis;
+    int k = lo;
+    for (; k + 2 <= hi; k += 2) {   // two neighbours' loads in flight
+      const double kv0 = sK[k], kv1 = sK[k + 1];
+      const double2 *vc0 = reinterpret_cast<const double2 *>(v + (size_t)sC[k] * MB);
+      const double2 *vc1 = reinterpret_cast<const double2 *>(v + (size_t)sC[k + 1] * MB);
+      double2 t0[MB / 2], t1[MB / 2];
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q) { t0[q] = __ldcg(vc0 + q); t1[q] = __ldcg(vc1 + q); }
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q) {
+        s[2 * q] += kv0 * t0[q].x;
+        s[2 * q + 1] += kv0 * t0[q].y;
+        s[2 * q] += kv1 * t1[q].x;
+        s[2 * q + 1] += kv1 * t1[q].y;
+      }
+    }
+    for (; k < hi; ++k) {
+      const double kv = sK[k];
+      const double2 *vc = reinterpret_cast<const double2 *>(v + (size_t)sC[k] * MB);
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q) {
+        const double2 t = __ldcg(vc + q);
+        s[2 * q] += kv * t.x;
+        s[2 * q + 1] += kv * t.y;
+      }
+    }
+  };
+  // FP32 operator on the published member-minor FP32 vector
+  auto apply32 = [&](const float *v, float (&s)[MB]) {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) s[m] = 0.f;
+    if (ident) {
+      const float2 *vr = reinterpret_cast<const float2 *>(v + (size_t)r * MB);
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q) { const float2 t = __ldcg(vr + q); s[2 * q] = t.x; s[2 * q + 1] = t.y; }
+      return;
+    }
+    int k = lo;
+    for (; k + 4 <= hi; k += 4) {   // four neighbours' loads in flight
+      float2 t[4][MB / 2];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float2 *vc = reinterpret_cast<const float2 *>(v + (size_t)sC[k + u] * MB);
+#pragma unroll
+        for (int q = 0; q < MB / 2; ++q) t[u][q] = __ldcg(vc + q);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float kv = sK32[k + u];
+#pragma unroll
+        for (int q = 0; q < MB / 2; ++q) {
+          s[2 * q] = fmaf(kv, t[u][q].x, s[2 * q]);
+          s[2 * q + 1] = fmaf(kv, t[u][q].y, s[2 * q + 1]);
+        }
+      }
+    }
+    for (; k < hi; ++k) {
+      const float kv = sK32[k];
+      const float2 *vc = reinterpret_cast<const float2 *>(v + (size_t)sC[k] * MB);
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q) {
+        const float2 t = __ldcg(vc + q);
+        s[2 * q] = fmaf(kv, t.x, s[2 * q]);
+        s[2 * q + 1] = fmaf(kv, t.y, s[2 * q + 1]);
+      }
+    }
+  };
+  unsigned epoch = 0;
+  auto precond32 = [&](const float (&rr)[MB], float (&uu)[MB]) -> bool {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) uu[m] = dinv32 * rr[m];
+    if (!a.coarse) return true;
+    const int lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      float s = active ? rr[m] : 0.f;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) sagg[m][wid] = s;
+    }
+    __syncthreads();
+    if (tid < kCGThreads / kAgg) {
+      const int I = blockIdx.x * (kCGThreads / kAgg) + tid;
+      if (I < a.nc)
+        for (int m = 0; m < MB; ++m) a.rc32[(size_t)I * MB + m] = sagg[m][2 * tid] + sagg[m][2 * tid + 1];
+    }
+    if (!arrive_wait(a, ++epoch)) return false;
+    const int g = tid / kAgg, t = tid % kAgg;
+    const int I = blockIdx.x * (kCGThreads / kAgg) + g;
+    float acc[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) acc[m] = 0.f;
+    if (I < a.nc) {
+      const float *row = a.ainv32 + (size_t)I * a.nc;
+#pragma unroll 4
+      for (int J = t; J < a.nc; J += kAgg) {
+        const float w = row[J];
+        const float2 *rcJ = reinterpret_cast<const float2 *>(a.rc32 + (size_t)J * MB);
+#pragma unroll
+        for (int q = 0; q < MB / 2; ++q) {
+          const float2 tt = __ldcg(rcJ + q);
+          acc[2 * q] = fmaf(w, tt.x, acc[2 * q]);
+          acc[2 * q + 1] = fmaf(w, tt.y, acc[2 * q + 1]);
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      float s = acc[m];
+#pragma unroll
+      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) sagg[m][wid] = s;
+    }
+    __syncthreads();
+    if (tid < kCGThreads / kAgg)
+      for (int m = 0; m < MB; ++m) sec[m][tid] = sagg[m][2 * tid] + sagg[m][2 * tid + 1];
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < MB; ++m) uu[m] += sec[m][g];
+    return true;
+  };
+  // ---- centre b (Neumann), projection warm start (FP64) ----
+  if (a.mode == 0) {
+    double v[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) v[m] = sbi[m][tid];
+    if (!reduce_all_to<MB>(a, ++epoch, v, smem, sres)) return;
+#pragma unroll
+    for (int m = 0; m < MB; ++m) if (active) sbi[m][tid] -= sres[m] / N;
+  }
+  {
+    double proj[P * MB];
+#pragma unroll
+    for (int q = 0; q < P * MB; ++q) proj[q] = 0.0;
+    if (active) {
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        if (m >= nm) break;
+        const int cnt = s_cnt[m];
+        const double bm = sbi[m][tid];
+        const double *bb = B.b + (size_t)m * kBasis * N;
+#pragma unroll
+        for (int j = 0; j < kBasis; ++j) if (j < cnt) proj[P * m + j] = bm * bb[(size_t)j * N + r];
+        proj[P * m + kBasis] = bm * bm;
+      }
+    }
+    if (!reduce_all_to<P * MB>(a, ++epoch, proj, smem, sbdot)) return;
+  }
+  if (tid < MB) s_tol[tid] = fmax(a.rtol * sqrt(sbdot[P * tid + kBasis]), a.atol);
+  {
+    const int m = tid >> 5;
+    if ((tid & 31) == 0 && m < nm) {
+      const int cnt = s_cnt[m];
+      if (cnt > 0) {
+        double c[kBasis];
+        small_solve(cnt, B.gram + m * kBasis * kBasis, sbdot + P * m, c);
+        for (int j = 0; j < cnt; ++j) scoef[m * kBasis + j] = c[j];
+      }
+    }
+  }
+  __syncthreads();
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      if (m >= nm) break;
+      const int cnt = s_cnt[m];
+      if (cnt == 0) continue;
+      const double *bx = B.x + (size_t)m * kBasis * N;
+      double g = 0.0;
+      for (int j = 0; j < cnt; ++j) g += scoef[m * kBasis + j] * bx[(size_t)j * N + r];
+      xi[m] = ident ? sbi[m][tid] : g;
+    }
+  }
+  int it = 0;
+  bool failed = false;
+  // ---- FP64 refinement loop ----
+  for (int outer = 0;; ++outer) {
+    if (active)
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q)
+        reinterpret_cast<double2 *>(a.xperm + (size_t)r * MB)[q] = make_double2(xi[2 * q], xi[2 * q + 1]);
+    if (!arrive_wait(a, ++epoch)) return;
+    double r64[MB];
+    {
+      double ax[MB];
+      apply64(a.xperm, ax);
+      double v[MB];
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        r64[m] = active ? sbi[m][tid] - ax[m] : 0.0;
+        v[m] = r64[m] * r64[m];
+      }
+      if (!reduce_all_to<MB>(a, ++epoch, v, smem, sres)) return;
+    }
+    if (tid < MB) {
+      const double rn = sres[tid];
+      int st = (tid < nm && !(sqrt(rn) <= s_tol[tid])) ? 0 : 1;
+      if (!(rn == rn)) st = 2;
+      s_out[tid] = st;
+      s_itol[tid] = (double)a.eta * sqrt(rn);   // inner target
+    }
+    __syncthreads();
+    int open = 0;
+#pragma unroll
+    for (int m = 0; m < MB; ++m) { open += s_out[m] == 0; failed = failed || s_out[m] == 2; }
+    if (open == 0 || failed) break;
+    if (outer >= a.max_outer) { failed = true; break; }
+    // ---- inner FP32 CG on A d = r for the open members ----
+    float ri[MB], ui[MB], pi[MB], si[MB], wi[MB], di[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      ri[m] = (s_out[m] == 0) ? (float)r64[m] : 0.f;
+      ui[m] = pi[m] = si[m] = wi[m] = di[m] = 0.f;
+    }
+    if (!precond32(ri, ui)) return;
+    if (active)
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q)
+        reinterpret_cast<float2 *>(a.z32 + (size_t)r * MB)[q] = make_float2(ui[2 * q], ui[2 * q + 1]);
+    if (tid < MB) { s_al[tid] = 0.0; s_ga[tid] = 0.0; s_be[tid] = 0.0; s_st[tid] = s_out[tid] == 0 ? 0 : 1; }
+    if (!arrive_wait(a, ++epoch)) return;
+    int iit = 0;
+    for (;;) {
+      {
+        float v[3 * MB];
+        apply32(a.z32, wi);
+#pragma unroll
+        for (int m = 0; m < MB; ++m) {
+          v[3 * m] = active ? ri[m] * ui[m] : 0.f;
+          v[3 * m + 1] = active ? wi[m] * ui[m] : 0.f;
+          v[3 * m + 2] = active ? ri[m] * ri[m] : 0.f;
+        }
+        if (!reduce_all_f<3 * MB>(a, ++epoch, v, smemf, sres)) return;
+      }
+      {
+        const int m = tid >> 5;
+        if ((tid & 31) == 0 && m < MB) {
+          int st = s_st[m];
+          double be = 0.0, al = s_al[m];
+          const double t0 = sres[3 * m], t1 = sres[3 * m + 1], t2 = sres[3 * m + 2];
+          if (st == 0) {
+            if (!(t2 == t2) || isinf(t2)) st = 2;
+            else if (sqrt(t2) <= s_itol[m] || !(t1 > 0.0)) st = 1;
+            else if (it + iit >= a.maxits) st = 2;
+          }
+          if (st == 0) {
+            if (iit == 0) al = t0 / t1;
+            else { be = t0 / s_ga[m]; al = t0 / (t1 - be * t0 / s_al[m]); }
+            s_ga[m] = t0;
+          }
+          s_al[m] = al; s_be[m] = be; s_st[m] = st;
+        }
+      }
+      __syncthreads();
+      int running = 0;
+#pragma unroll
+      for (int m = 0; m < MB; ++m) { running += s_st[m] == 0; failed = failed || s_st[m] == 2; }
+      if (running == 0) break;
+      if (active) {
+#pragma unroll
+        for (int m = 0; m < MB; ++m) {
+          if (s_st[m] != 0) continue;
+          const float al = (float)s_al[m], be = (float)s_be[m];
+          pi[m] = fmaf(be, pi[m], ui[m]);
+          si[m] = fmaf(be, si[m], wi[m]);
+          di[m] = fmaf(al, pi[m], di[m]);
+          ri[m] = fmaf(-al, si[m], ri[m]);
+        }
+      }
+      if (!precond32(ri, ui)) return;
+      if (active)
+#pragma unroll
+        for (int q = 0; q < MB / 2; ++q)
+          reinterpret_cast<float2 *>(a.z32 + (size_t)r * MB)[q] = make_float2(ui[2 * q], ui[2 * q + 1]);
+      ++iit;
+      if (!arrive_wait(a, ++epoch)) return;
+    }
+    it += iit;
+    if (failed) break;
+#pragma unroll
+    for (int m = 0; m < MB; ++m) if (s_out[m] == 0) xi[m] += (double)di[m];
+  }
+  __syncthreads();
+  if (a.mode == 0) {
+    double v[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) v[m] = active ? xi[m] : 0.0;
+    if (!reduce_all_to<MB>(a, ++epoch, v, smem, sres)) return;
+#pragma unroll
+    for (int m = 0; m < MB; ++m) xi[m] -= sres[m] / N;
+  }
+  if (active) {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) {
+      if (m >= nm) break;
+      const int head = s_head[m];
+      a.x[(size_t)m * N + node] = xi[m];
+      B.b[(size_t)m * kBasis * N + (size_t)head * N + r] = sbi[m][tid];
+      B.x[(size_t)m * kBasis * N + (size_t)head * N + r] = xi[m];
+    }
+  }
+  if (r == 0) {
+    a.iters[a.mode] = it;
+    a.iters[2 + a.mode] += it;
+    if (failed) atomicOr(a.err, ERR_CG_MAXITS);
+  }
+  {
+    const int m = tid >> 5;
+    if (blockIdx.x == 0 && (tid & 31) == 0 && m < nm) {
+      double *G = B.gram + m * kBasis * kBasis;
+      const int cnt = s_cnt[m], head = s_head[m];
+      const int ncount = cnt < kBasis ? cnt + 1 : kBasis;
+      for (int j = 0; j < ncount; ++j) {
+        const double gv = (j == head) ? sbdot[P * m + kBasis] : sbdot[P * m + j];
+        G[head * kBasis + j] = gv;
+        G[j * kBasis + head] = gv;
+      }
+      B.ring[2 * m] = ncount;
+      B.ring[2 * m + 1] = (head + 1) % kBasis;
+    }
   }
 }
 
@@ -913,8 +1428,8 @@ constexpr int kTileCols = 1024, kTileRpw = 4, kTileRows = 64;
 
 // Sum each of NV values over the warp with recursive halving (31 shuffles for
 // NV = 32): afterwards lane L holds the total of value L >> (5 - log2 NV).
-template <int NV>
-__device__ __forceinline__ double warp_transpose_sum(double (&v)[NV]) {
+template <typename T, int NV>
+__device__ __forceinline__ T warp_transpose_sum(T (&v)[NV]) {
   const int lane = threadIdx.x & 31;
   int n = NV;
 #pragma unroll
@@ -924,8 +1439,8 @@ __device__ __forceinline__ double warp_transpose_sum(double (&v)[NV]) {
 #pragma unroll
       for (int i = 0; i < NV / 2; ++i) {
         if (i >= n / 2) break;
-        const double send = up ? v[i] : v[i + n / 2];
-        const double keep = up ? v[i + n / 2] : v[i];
+        const T send = up ? v[i] : v[i + n / 2];
+        const T keep = up ? v[i + n / 2] : v[i];
         v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
       }
       n >>= 1;
@@ -985,11 +1500,79 @@ __global__ void __launch_bounds__(256) k_gemm_f32t(int nb, int ld, int nm, const
     double accd[NV];   // lane sums (32 products each in FP32) combined in FP64
 #pragma unroll
     for (int q = 0; q < NV; ++q) accd[q] = (double)acc[q];
-    const double tot = warp_transpose_sum<NV>(accd);
+    const double tot = warp_transpose_sum<double, NV>(accd);
     const int v = lane >> SH;
     const int rr = v / MB, m = v - rr * MB;
     if ((lane & ((1 << SH) - 1)) == 0 && m < nm && r0 + rr < nb)
       part[((size_t)slab * nb + r0 + rr) * MB + m] = tot;
+  }
+}
+
+// FP32 ensemble product, x held in registers: block (slab group, row block)
+// covers kRegSlab columns with its 8 warps, warp w owning 256 columns and
+// lane l the 8 columns at 256 w + 8 l, for which it keeps every member's x
+// in registers.  The warp walks the block's rows kTileRpw at a time (one
+// 32-byte load per row and lane, no shared-memory x traffic), reduces its
+// kTileRpw x MB sums across lanes (FP32: each covers the warp's 256 columns),
+// and parks them in shared memory; the 8 warps' sums are added in FP64 once
+// at the end.  part[(slab group * nb + row) * MB + m].
+constexpr int kRegSlab = 2048, kRegRows = 64;   // 32 KB of shared sums at MB = 8
+
+template <int MB>
+__global__ void __launch_bounds__(256, 2) k_gemm_f32r(int nb, int ld, int nm, const float *__restrict__ B,
+                                                      const float *__restrict__ x, double *__restrict__ part) {
+  constexpr int NV = kTileRpw * MB;
+  constexpr int SH = NV >= 32 ? 0 : (NV >= 16 ? 1 : (NV >= 8 ? 2 : 3));
+  constexpr int STEPS = kRegRows / kTileRpw;
+  __shared__ double sred[8][STEPS][NV];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int c = blockIdx.x * kRegSlab + 256 * warp + 8 * lane;
+  const bool on = c < ld;   // ld is a multiple of 8: a lane's unit is all in or all out
+  float4 xr[MB][2];
+#pragma unroll
+  for (int m = 0; m < MB; ++m) {
+    const bool ok = on && m < nm;
+    const float4 *px = reinterpret_cast<const float4 *>(x + (size_t)m * ld + (ok ? c : 0));
+    xr[m][0] = ok ? __ldg(px) : make_float4(0.f, 0.f, 0.f, 0.f);
+    xr[m][1] = ok ? __ldg(px + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  const int rbeg = blockIdx.y * kRegRows;
+  for (int st = 0; st < STEPS; ++st) {
+    const int r0 = rbeg + st * kTileRpw;
+    if (r0 >= nb) break;   // uniform across the block
+    float4 a[kTileRpw][2];
+#pragma unroll
+    for (int rr = 0; rr < kTileRpw; ++rr) {
+      const float4 *p = reinterpret_cast<const float4 *>(B + (size_t)min(r0 + rr, nb - 1) * ld + (on ? c : 0));
+      a[rr][0] = on ? __ldcs(p) : make_float4(0.f, 0.f, 0.f, 0.f);
+      a[rr][1] = on ? __ldcs(p + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    float acc[NV];
+#pragma unroll
+    for (int rr = 0; rr < kTileRpw; ++rr) {
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        float t = a[rr][0].x * xr[m][0].x;
+        t = fmaf(a[rr][0].y, xr[m][0].y, t); t = fmaf(a[rr][0].z, xr[m][0].z, t);
+        t = fmaf(a[rr][0].w, xr[m][0].w, t); t = fmaf(a[rr][1].x, xr[m][1].x, t);
+        t = fmaf(a[rr][1].y, xr[m][1].y, t); t = fmaf(a[rr][1].z, xr[m][1].z, t);
+        t = fmaf(a[rr][1].w, xr[m][1].w, t);
+        acc[rr * MB + m] = t;
+      }
+    }
+    const float tot = warp_transpose_sum<float, NV>(acc);   // the warp's 256 columns, FP32
+    if ((lane & ((1 << SH) - 1)) == 0) sred[warp][st][lane >> SH] = (double)tot;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < STEPS * NV; e += blockDim.x) {
+    const int st = e / NV, v = e - st * NV;
+    const int rr = v / MB, m = v - rr * MB;
+    const int row = rbeg + st * kTileRpw + rr;
+    if (row >= nb || m >= nm) continue;
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) s += sred[w][st][v];
+    part[((size_t)blockIdx.x * nb + row) * MB + m] = s;
   }
 }
 
@@ -1217,7 +1800,8 @@ int build_cg_ordering(nmg_handle *h, std::string &err) {
   NMG_CUDA_TRY(W.pcol.alloc(nnz), "alloc");
   NMG_CUDA_TRY(W.pbnd.alloc(N), "alloc");
   NMG_CUDA_TRY(W.pK.alloc(nnz), "alloc");
-  NMG_CUDA_TRY(W.xperm.alloc((size_t)N * std::min(h->nrep, kChunk)), "alloc");
+  NMG_CUDA_TRY(W.xperm.alloc((size_t)N * ((h->nrep > 1 || h->opt.cg_precision == 1) ? kChunk : 1)), "alloc");
+  NMG_CUDA_TRY(W.z32.alloc((size_t)N * kChunk), "alloc");
   NMG_CUDA_TRY(cudaMemcpy(W.perm.p, perm.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "h2d");
   NMG_CUDA_TRY(cudaMemcpy(W.prow.p, prow.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice), "h2d");
   NMG_CUDA_TRY(cudaMemcpy(W.pcol.p, pcol.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice), "h2d");
@@ -1262,8 +1846,14 @@ int build_cg_ordering(nmg_handle *h, std::string &err) {
       Ainv[(size_t)j * nc + i] = s;
     }
   NMG_CUDA_TRY(W.ainv.alloc((size_t)nc * nc), "alloc coarse inverse");
-  NMG_CUDA_TRY(W.rc.alloc((size_t)nc * std::min(h->nrep, kChunk)), "alloc");
+  NMG_CUDA_TRY(W.rc.alloc((size_t)nc * ((h->nrep > 1 || h->opt.cg_precision == 1) ? kChunk : 1)), "alloc");
   NMG_CUDA_TRY(cudaMemcpy(W.ainv.p, Ainv.data(), sizeof(double) * nc * nc, cudaMemcpyHostToDevice), "h2d");
+  {
+    std::vector<float> a32(Ainv.begin(), Ainv.end());
+    NMG_CUDA_TRY(W.ainv32.alloc((size_t)nc * nc), "alloc coarse inverse (FP32)");
+    NMG_CUDA_TRY(W.rc32.alloc((size_t)nc * kChunk), "alloc");
+    NMG_CUDA_TRY(cudaMemcpy(W.ainv32.p, a32.data(), sizeof(float) * nc * nc, cudaMemcpyHostToDevice), "h2d");
+  }
   W.nc = nc;
   return 0;
 }
@@ -1322,19 +1912,31 @@ int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm,
   a.perm = W.perm; a.prow = W.prow; a.pcol = W.pcol; a.pbnd = W.pbnd; a.pK = W.pK; a.xperm = W.xperm;
   a.coarse = (mode == 0 && W.nc > 0) ? 1 : 0;
   a.nc = W.nc; a.ainv = W.ainv; a.rc = W.rc;
+  a.ainv32 = W.ainv32; a.rc32 = W.rc32; a.z32 = W.z32;
+  a.eta = 1e-3f; a.max_outer = 10;
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
   int cap = W.cg_nnz_cap;
   CGBasis basis;
-  const size_t slot = (size_t)mode * h->nrep + c0;   // first member of this chunk
-  basis.b = W.ens_basis_b.p + slot * kBasis * M.N;
-  basis.x = W.ens_basis_x.p + slot * kBasis * M.N;
-  basis.gram = W.ens_basis_gram.p + slot * kBasis * kBasis;
-  basis.ring = W.ens_basis_ring.p + 2 * slot;
+  if (h->nrep > 1) {
+    const size_t slot = (size_t)mode * h->nrep + c0;   // first member of this chunk
+    basis.b = W.ens_basis_b.p + slot * kBasis * M.N;
+    basis.x = W.ens_basis_x.p + slot * kBasis * M.N;
+    basis.gram = W.ens_basis_gram.p + slot * kBasis * kBasis;
+    basis.ring = W.ens_basis_ring.p + 2 * slot;
+  } else {   // one simulation: the single-solve bases of slot `mode`
+    basis.b = W.basis_b.p + (size_t)mode * kBasis * M.N;
+    basis.x = W.basis_x.p + (size_t)mode * kBasis * M.N;
+    basis.gram = W.basis_gram.p + mode * kBasis * kBasis;
+    basis.ring = W.basis_ring.p + 2 * mode;
+  }
   void *args[] = {&a, &cap, &nm, &basis};
-  const void *fn = nm <= 2 ? (const void *)k_cgm<2> : (nm <= 4 ? (const void *)k_cgm<4> : (const void *)k_cgm<8>);
+  const bool mp = h->opt.cg_precision == 1;
+  const void *fn;
+  if (mp) fn = nm <= 2 ? (const void *)k_cgm_mp<2> : (nm <= 4 ? (const void *)k_cgm_mp<4> : (const void *)k_cgm_mp<8>);
+  else fn = nm <= 2 ? (const void *)k_cgm<2> : (nm <= 4 ? (const void *)k_cgm<4> : (const void *)k_cgm<8>);
   NMG_PROF_BEGIN(h, 1 + mode);
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(W.cg_blocks), dim3(kCGThreads), args,
-                                              (size_t)W.cg_smem_bytes, h->stream);
+                                              (size_t)(mp ? W.cg_smem_mp : W.cg_smem_bytes), h->stream);
   NMG_PROF_END(h);
   ++h->launches;
   if (e != cudaSuccess) {
@@ -1364,8 +1966,9 @@ int init_workspace(nmg_handle *h, std::string &err) {
     NMG_CUDA_TRY(b->alloc(n3), "alloc field");
   for (DevBuf<double> *b : {&W.rho, &W.phi1, &W.phi2, &W.phi, &W.rhs2})
     NMG_CUDA_TRY(b->alloc(nB), "alloc scalar field");
+  const int BCv = B > 1 ? kChunk : 1;   // ensemble CG vectors are member-minor with stride up to kChunk
   for (DevBuf<double> *b : {&W.cg_r, &W.cg_z, &W.cg_p, &W.cg_q})
-    NMG_CUDA_TRY(b->alloc((size_t)N * BC), "alloc CG vectors");
+    NMG_CUDA_TRY(b->alloc((size_t)N * BCv), "alloc CG vectors");
   for (DevBuf<double> *b : {&W.dinv_n, &W.dinv_d})
     NMG_CUDA_TRY(b->alloc(N), "alloc scalar field");
   NMG_CUDA_TRY(W.b1.alloc(nb > 0 ? (size_t)nb * B : 1), "alloc");
@@ -1417,12 +2020,19 @@ int init_workspace(nmg_handle *h, std::string &err) {
             std::to_string(per_sm * h->sm_count * kCGThreads) + " nodes here)";
       return 4;
     }
-    if (B > 1 && h->opt.do_demag) {
-      // the ensemble CG kernels hold up to kChunk members per row in registers
-      for (const void *fn : {(const void *)k_cgm<2>, (const void *)k_cgm<4>, (const void *)k_cgm<8>}) {
+    W.cg_smem_mp = cap * (int)(sizeof(double) + sizeof(int) + sizeof(float));
+    const bool mp = h->opt.cg_precision == 1;
+    if ((B > 1 || mp) && h->opt.do_demag) {
+      // the ensemble / mixed-precision CG kernels: up to kChunk members per row
+      const void *fns[3] = {mp ? (const void *)k_cgm_mp<2> : (const void *)k_cgm<2>,
+                            mp ? (const void *)k_cgm_mp<4> : (const void *)k_cgm<4>,
+                            mp ? (const void *)k_cgm_mp<8> : (const void *)k_cgm<8>};
+      const int smem_need = mp ? W.cg_smem_mp : W.cg_smem_bytes;
+      for (const void *fn : fns) {
         int per = 0;
-        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kCGThreads, W.cg_smem_bytes) != cudaSuccess ||
+        if (smem_need > 160 * 1024 ||
+            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kCGThreads, smem_need) != cudaSuccess ||
             per * h->sm_count < W.cg_blocks) {
           cudaGetLastError();
           err = "mesh too large for the ensemble CG (" + std::to_string(W.cg_blocks) + " co-resident blocks needed)";
@@ -1524,12 +2134,12 @@ void bem_gemm(nmg_handle *h, const double *x, double *y) {
     if (f == 1) {
       float *x32 = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
       k_to_f32_vec<<<nblk((long long)M.ld * nm, 256), 256, 0, h->stream>>>(nb, M.ld, xc, x32, nm); ++h->launches;
-      const int nslab = (M.ld + kTileCols - 1) / kTileCols;
-      dim3 grid(nslab, (nb + kTileRows - 1) / kTileRows);
+      const int nslab = (M.ld + kRegSlab - 1) / kRegSlab;
+      dim3 grid(nslab, (nb + kRegRows - 1) / kRegRows);
       NMG_PROF_BEGIN(h, 0);
-      if (MB == 2) k_gemm_f32t<2><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, x32, W.bpart);
-      else if (MB == 4) k_gemm_f32t<4><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, x32, W.bpart);
-      else k_gemm_f32t<8><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, x32, W.bpart);
+      if (MB == 2) k_gemm_f32r<2><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, x32, W.bpart);
+      else if (MB == 4) k_gemm_f32r<4><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, x32, W.bpart);
+      else k_gemm_f32r<8><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, x32, W.bpart);
       NMG_PROF_END(h);
       ++h->launches;
       k_slab_sum_m<<<nblk((long long)nb * nm, 256), 256, 0, h->stream>>>(nb, nslab, nm, MB, W.bpart,
@@ -1593,13 +2203,16 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
                   h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)) return 100;
     k_add<<<nblk(NB, 256), 256, 0, s>>>((int)NB, W.phi1, W.phi2, W.phi); ++h->launches;
   } else if (h->opt.do_demag && M.nb > 0) {
+    const bool mp = h->opt.cg_precision == 1;   // mixed-precision CG (one member)
     k_div<<<nblk(N, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, h->ep.active ? h->ep.Dx.p : M.D.p, d_m,
                                        W.rho); ++h->launches;
-    if (run_cg(h, 0, W.rho, W.phi1, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
+    if (mp ? run_cgm(h, 0, 0, W.rho, W.phi1, 1, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)
+           : run_cg(h, 0, W.rho, W.phi1, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
     k_gather_b<<<nblk(M.nb, 256), 256, 0, s>>>(M.nb, M.node_of_b, W.phi1, W.b1); ++h->launches;
     bem_gemv(h, W.b1, W.b2);
     k_dbc_rhs<<<nblk(N, 256), 256, 0, s>>>(N, M.row_ptr, M.col_idx, M.K, M.b_of_node, W.b2, W.rhs2, W.phi2); ++h->launches;
-    if (run_cg(h, 1, W.rhs2, W.phi2, h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)) return 100;
+    if (mp ? run_cgm(h, 1, 0, W.rhs2, W.phi2, 1, h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)
+           : run_cg(h, 1, W.rhs2, W.phi2, h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)) return 100;
     k_add<<<nblk(N, 256), 256, 0, s>>>(N, W.phi1, W.phi2, W.phi); ++h->launches;
   }
   NodeArgs a;

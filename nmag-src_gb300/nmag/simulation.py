@@ -100,7 +100,7 @@ class Simulation(object):
     def __init__(self, name=None, phi_BEM=None, periodic_bc=None, do_demag=True, do_anisotropy_jacobian=False,
                  temperature=None, thermal_delta_t=None, user_seed_T=0, timestepper_max_order=2,
                  timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
-                 lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1):
+                 lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1, cg_precision="fp64"):
         if periodic_bc is not None:
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
@@ -114,6 +114,8 @@ class Simulation(object):
         self.ksp_tolerances = dict(ksp_tolerances or {})
         self.quirks = quirks
         self.bem_precision = bem_precision
+        # "fp32": the Poisson CG iterates in FP32 with FP64 residual refinement
+        self.cg_precision = cg_precision
         # ensemble: n_members simulations on one mesh, integrated together;
         # per-node arrays then carry a leading member axis (GB300 extension)
         self.n_members = max(1, int(n_members))
@@ -159,6 +161,7 @@ class Simulation(object):
         opts.nbc_rtol, opts.nbc_atol, opts.nbc_maxits = tol("NBC.rtol", 1e-5), tol("NBC.atol", 1e-50), int(tol("NBC.maxits", 10000))
         opts.dbc_rtol, opts.dbc_atol, opts.dbc_maxits = tol("DBC.rtol", 1e-5), tol("DBC.atol", 1e-50), int(tol("DBC.maxits", 10000))
         opts.bem_precision = {"fp64": 0, "fp32": 1}[self.bem_precision]
+        opts.cg_precision = {"fp64": 0, "fp32": 1}[self.cg_precision]
         opts.n_members = self.n_members if self.n_members > 1 else 0
         self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
         shape = self.engine._shape3()

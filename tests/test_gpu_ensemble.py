@@ -10,7 +10,7 @@ from test_gpu_parity import make_engine
 pytestmark = pytest.mark.gpu
 
 
-def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0):
+def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0):
     from nmag import _lib
     single = make_engine(msh, mat, tol=tol, bem_precision=bem_precision)
     c = mat.coefficients("nmag")
@@ -25,6 +25,7 @@ def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0):
     op.nbc_atol = op.dbc_atol = 1e-50
     op.nbc_maxits = op.dbc_maxits = 20000
     op.bem_precision = bem_precision
+    op.cg_precision = cg_precision
     op.n_members = B
     return _lib.Engine(msh.points, msh.simplices, mt, op), single
 
@@ -78,3 +79,23 @@ def test_ensemble_integration_matches_single_runs(small_box):
         single.ts_init(0.0, rtol=1e-8, atol=1e-8)
         single.ts_advance(5.0)
         assert np.abs(me[b] - single.get_m()).max() <= 2e-6, b
+
+
+@pytest.mark.parametrize("B", [1, 6])
+def test_mixed_precision_cg_matches_fp64(cube, B):
+    """FP32 CG iterations with FP64 residual refinement, refined to rtol 1e-12,
+    give the FP64 CG's fields (single handle routed through the same kernel)."""
+    mat = permalloy(0.5)
+    ens, single = make_ensemble(cube, mat, B, cg_precision=1)
+    N = len(cube.points)
+    ms, hs = _members(N, max(B, 2), seed0=300)
+    ens.set_m(ms[:B] if B > 1 else ms[0])
+    ens.set_h_ext(hs[:B] if B > 1 else hs[0])
+    f = ens.eval_fields()
+    for b in range(B):
+        single.set_m(ms[b])
+        single.set_h_ext(hs[b])
+        g = single.eval_fields()
+        got = f["H_demag"][b] if B > 1 else f["H_demag"]
+        ref = g["H_demag"]
+        assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max(), b
