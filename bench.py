@@ -1,5 +1,13 @@
 """Benchmark: simulated ns per wall-second of nmag's LLG path on the film.
 
+Default line: the chosen form -- an ensemble of 8 films on the one mesh
+(options n_members = 8), BEM matrix as FP32 + BF16 residual with compensated
+FP32 products (accurate to ~2^-44), FP64 CG -- with
+`value` summed over the members, and beside it (`plain_fp64`) the plain FP64
+single film measured in the same run, their ratio and the chosen form's
+H_eff error against FP64 at the same magnetisation.  `--form fp64
+--members 1` measures the plain form alone.
+
 Workload (the plain-method film configuration): 500 x 125 x 3 nm permalloy
 film, 2.5 x 2.5 x 1.5 nm cells, Kuhn 6-tet split (30,753 nodes, 120,000
 tets, 21,002 boundary nodes, dense 21,002^2 BEM = 3.53 GB FP64), alpha = 0.02,
@@ -15,7 +23,8 @@ stream).  --impl reference: the CPU restatement of the reference's path
 (oracle/, all host cores) on the same workload and metric.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                       [--form fp64|fp32] [--workload film|cube]
+                       [--form fp64|fp32] [--members B] [--cg fp64|fp32] [--no-compare]
+                       [--workload film|cube|film_small]
 """
 from __future__ import annotations
 
@@ -42,7 +51,7 @@ H_EXT_MT = (-24.6, 4.3, 0.0)
 # from one ncu capture on the 8,562-boundary-node profiling film (matrix
 # 586.6 MB > L2; profiles/k_gemv_f64_film_small.txt: 590.04 MB read+written).
 # The traffic grows with the matrix entries, so it scales to the full film.
-NCU_TRAFFIC_RATIO = {"fp64": (586.81 + 3.23) / 586.60}
+NCU_TRAFFIC_RATIO = {("fp64", False): (586.81 + 3.23) / 586.60}
 
 
 def workload(name):
@@ -211,7 +220,8 @@ def run_reference(args):
                                    % (r["steps"], args.step_ps)},
         "e2e": {"value": value, "unit": "ns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's own build (OCaml/Python 2/PETSc/SUNDIALS) cannot run here; this arm times "
-                "the CPU restatement of its algorithms",
+                "the CPU restatement of its algorithms (FP64).  An ensemble's members would run one after "
+                "another on the CPU, so its aggregate rate equals this single-film rate",
     }
     print(json.dumps(line))
 
@@ -229,21 +239,18 @@ def config_dict(args, msh):
             "nodes": int(msh.n_nodes), "tets": int(msh.n_tets), "step": "%.3g ps advance + <m> read" % args.step_ps,
             "form": args.form, "cg": args.cg, "members": args.members,
             "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
-            "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % (8 if args.form == "fp64" else 4)}
+            "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % {"fp64": 8, "fp32": 4,
+                                                                                  "fp32x2": 6}[args.form]}
 
 
-def run_ours(args):
+def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True):
+    """One form on the workload: untimed setup and relax, W warm-up steps,
+    then K timed steps on the device-resident engine (CUDA-event time on the
+    library's stream) and K more through nmag.Simulation (e2e)."""
     import torch
     import nmag
     from nmag import SI
-    rank, world = dist_setup(args.gpus)
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    torch.cuda.init()
-    msh, base, seed = workload(args.workload)
-    B = args.members
-    # fp32 form: FP32 BEM matrix (FP64 sums); --cg fp32: FP32 CG iterations with FP64 residual refinement
-    sim = nmag.Simulation("bench", bem_precision=args.form, cg_precision=args.cg, n_members=B)
+    sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B)
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     if B > 1:   # member b starts from the workload's initial state with seed + b
@@ -266,8 +273,9 @@ def run_ours(args):
         t += ps
         eng.ts_advance(t)
     # ---- timed region: device-resident value leg ----
-    sampler = ClockSampler(local)
-    sampler.start()
+    sampler = ClockSampler(local) if sample_clocks else None
+    if sampler:
+        sampler.start()
     eng.profile(True)
     launches0 = eng.launch_count()
     cg0 = eng.cg_iterations()
@@ -277,12 +285,11 @@ def run_ours(args):
     torch.cuda.synchronize()
     dev_ms = 0.0
     w0 = time.perf_counter()
-    avgs = []
     for _ in range(args.steps):
         t += ps
         _, st = eng.ts_advance(t)
         dev_ms += float(eng.timings()[0])
-        avgs.append(eng.averages())
+        eng.averages()
     torch.cuda.synchronize()
     wall_value = time.perf_counter() - w0
     barrier(world)
@@ -290,9 +297,7 @@ def run_ours(args):
     cg1 = eng.cg_iterations()
     eng.profile(False)
     prof = eng.profile_read()
-    clocks = sampler.stop()
-    nfe = st["nfe"] - st0["nfe"]
-    nst = st["nst"] - st0["nst"]
+    clocks = sampler.stop() if sampler else None
     # ---- e2e leg through the public API (advance_time copies m to the host) ----
     sim.clock.stage_time_su = t
     sim._last_nst = st["nst"]
@@ -308,56 +313,166 @@ def run_ours(args):
     dev_s = max_over_ranks(dev_ms * 1e-3, world)
     wall_e2e = max_over_ranks(wall_e2e, world)
     sim_ns_total = world * B * args.steps * ps * 1e-3   # summed over ensemble members
-    value = sim_ns_total / dev_s
-    e2e_value = sim_ns_total / wall_e2e
-    if rank != 0:
-        return
     nb = eng.nb
-    gl, gms = prof["bem_gemv"]
-    elem = 8 if args.form == "fp64" else 4
+    elem = {"fp64": 8, "fp32": 4, "fp32x2": 6}[form]
     nm = min(B, 8)   # members per BEM launch
+    gl, gms = prof["bem_gemv"]
     bytes_per_launch = nb * nb * elem + 2 * nm * nb * 8
-    hbm, peak_kind = peaks()
     roof = None
     if gl > 0:
+        hbm, peak_kind = peaks()
         avg_ms = gms / gl
         achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
-        kname = ("k_gemv_" if B == 1 else "k_gemm_") + ("f64" if args.form == "fp64" else "f32")
-        roof = {"bound": "hbm" if not (B > 1 and args.form == "fp64") else "fp64 pipe (bytes shown)",
-                "kernel": kname,
-                "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+        if B == 1:
+            kname = {"fp64": "k_gemv_f64", "fp32": "k_gemv_f32", "fp32x2": "k_gemv_df"}[form]
+        else:
+            kname = {"fp64": "k_gemm_f64", "fp32": "k_gemm_f32r", "fp32x2": "k_gemm_df"}[form]
+        roof = {"bound": "hbm" if not (B > 1 and form == "fp64") else "fp64 pipe (bytes shown)",
+                "kernel": kname, "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "peak_kind": peak_kind,
-                "traffic": (NCU_TRAFFIC_RATIO[args.form] * bytes_per_launch / 1e9
-                            if args.form in NCU_TRAFFIC_RATIO else None),
-                "traffic_unit": "GB per launch (ncu dram__bytes_read+write, scaled from the profiling film)",
+                "traffic": (NCU_TRAFFIC_RATIO[(form, B > 1)] * bytes_per_launch / 1e9
+                            if (form, B > 1) in NCU_TRAFFIC_RATIO else None),
+                "traffic_unit": "GB per launch (ncu dram__bytes_read+write, scaled from the profiling capture)",
                 "launches": gl, "avg_launch_ms": avg_ms,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "share_of_step": gms / max(dev_ms, 1e-9)}
-    line = {
-        "metric": "simulated ns/wall-s", "value": value, "unit": "ns/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_dict(args, msh),
-        "rhs_evals_per_s": nfe / dev_s * world, "bdf_steps": nst, "rhs_evals": nfe,
-        "wall_value_s": wall_value,
-        "roofline": roof,
+    return {
+        "sim": sim, "eng": eng, "value": sim_ns_total / dev_s, "e2e": sim_ns_total / wall_e2e,
+        "ms_per_step": dev_s * 1e3 / args.steps, "rhs_evals": st["nfe"] - st0["nfe"],
+        "bdf_steps": st["nst"] - st0["nst"], "rhs_evals_per_s": (st["nfe"] - st0["nfe"]) / dev_s * world,
+        "wall_value_s": wall_value, "roofline": roof, "launches": launches, "clocks": clocks,
         "kernels_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
         "cg_iterations": {"neumann": cg1[0] - cg0[0], "dirichlet": cg1[1] - cg0[1]},
-        "relax_wall_s": relax_wall,
-        "e2e": {"value": e2e_value, "unit": "ns/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": B * msh.n_nodes * 3 * 8 + 24,
-                "call": "nmag.Simulation.advance_time + get_subfield_average_siv('m')"},
-        "gpu_launches": launches,
-        "clocks": clocks,
-        "avg_m_last": [float(x) for x in avgs[-1]] if avgs else None,
+        "relax_wall_s": relax_wall, "d2h": B * msh.n_nodes * 3 * 8 + 24,
     }
+
+
+def heff_error(args, chosen, msh):
+    """Relative H_eff error of the chosen form against FP64 at the same
+    magnetisation (member 0 after the timed steps): max |H - H_fp64| /
+    max |H_fp64|.  Both sides are fresh handles whose Poisson solves are
+    converged to rtol 1e-12, so the figure is the form's own error (FP32
+    matrix entries), not the difference of two CG solves stopped at the
+    reference's default tolerance."""
+    import nmag
+    from nmag import SI
+    m = chosen["eng"].get_m()
+    m0 = m[0] if m.ndim == 3 else m
+    tight = {"NBC.rtol": 1e-12, "DBC.rtol": 1e-12, "NBC.maxits": 20000, "DBC.maxits": 20000}
+    out = {}
+    for form in (args.form, "fp64"):
+        sim = nmag.Simulation("err", bem_precision=form, ksp_tolerances=tight)
+        sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
+        sim.engine.set_m(m0)
+        sim.engine.set_h_ext(np.broadcast_to(h_ext_su(), (sim.engine.N, 3)))
+        out[form] = sim.engine.eval_fields()["H_total"]
+        sim.engine.close()
+    ref = out["fp64"]
+    return float(np.abs(out[args.form] - ref).max() / np.abs(ref).max())
+
+
+def run_precision_report(args):
+    """Precision form against FP64 on the film for N seeded random fields
+    (m = normalise(N(0,1)) per node, numpy default_rng(seed), seeds 100..):
+    H_eff (max-norm relative) and total / demag energy relative errors.  Both
+    sides are 8-member ensembles with Poisson solves converged to 1e-12; the
+    FP64 side is the plain form's arithmetic."""
+    import torch
+    import nmag
+    from nmag import SI
+    torch.cuda.set_device(0)
+    msh, _, _ = workload(args.workload)
+    tight = {"NBC.rtol": 1e-12, "DBC.rtol": 1e-12, "NBC.maxits": 20000, "DBC.maxits": 20000}
+    B = 8
+    sims = {}
+    for form in (args.form, "fp64"):
+        sim = nmag.Simulation("err", bem_precision=form, ksp_tolerances=tight, n_members=B)
+        sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
+        sim.engine.set_h_ext(np.broadcast_to(h_ext_su(), (B, sim.engine.N, 3)))
+        sims[form] = sim.engine
+    N = msh.n_nodes
+    herr, eerr, derr = [], [], []
+    t0 = time.perf_counter()
+    for s0 in range(100, 100 + args.fields, B):
+        seeds = list(range(s0, min(s0 + B, 100 + args.fields)))
+        ms = []
+        for sd in seeds:
+            g = np.random.default_rng(sd).standard_normal((N, 3))
+            ms.append(g / np.linalg.norm(g, axis=1)[:, None])
+        while len(ms) < B:
+            ms.append(ms[-1])
+        res = {}
+        for form, eng in sims.items():
+            eng.set_m(np.stack(ms))
+            f = eng.eval_fields()["H_total"]
+            en = [eng.member_averages(b, energies=True)[1] for b in range(len(seeds))]
+            res[form] = (f, en)
+        for b in range(len(seeds)):
+            h32, h64 = res[args.form][0][b], res["fp64"][0][b]
+            herr.append(float(np.abs(h32 - h64).max() / np.abs(h64).max()))
+            e32, e64 = res[args.form][1][b], res["fp64"][1][b]
+            eerr.append(float(abs(e32[4] - e64[4]) / abs(e64[4])))
+            derr.append(float(abs(e32[1] - e64[1]) / abs(e64[1])))
+    wall = time.perf_counter() - t0
+    line = {"metric": "precision form error vs FP64", "report": "precision", "fields": len(herr),
+            "seeds": [100, 100 + len(herr) - 1], "workload": WORKLOAD_NAMES[args.workload],
+            "form": args.form, "bound": 1e-5,
+            "heff_rel_err": {"max": max(herr), "median": float(np.median(herr)), "p99": float(np.percentile(herr, 99))},
+            "energy_total_rel_err": {"max": max(eerr), "median": float(np.median(eerr))},
+            "energy_demag_rel_err": {"max": max(derr), "median": float(np.median(derr))},
+            "within_bound": bool(max(herr) <= 1e-5), "wall_s": wall}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    rank, world = dist_setup(args.gpus)
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    torch.cuda.init()
+    msh, base, seed = workload(args.workload)
+    B = args.members
+    r = measure(args, args.form, args.cg, B, msh, base, seed, world, local)
+    plain = None
+    if args.compare and not (args.form == "fp64" and args.cg == "fp64" and B == 1):
+        plain = measure(args, "fp64", "fp64", 1, msh, base, seed, world, local, sample_clocks=False)
+    if rank != 0:
+        return
+    line = {
+        "metric": "simulated ns/wall-s", "value": r["value"], "unit": "ns/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "fp32": "f32 matrix, f64 sums",
+                  "fp32x2": "f32+bf16 matrix, compensated f32 products (~2^-44)"}[args.form],
+        "data": "synthetic",
+        "config": config_dict(args, msh),
+        "rhs_evals_per_s": r["rhs_evals_per_s"], "bdf_steps": r["bdf_steps"], "rhs_evals": r["rhs_evals"],
+        "wall_value_s": r["wall_value_s"],
+        "roofline": r["roofline"],
+        "kernels_ms": r["kernels_ms"],
+        "cg_iterations": r["cg_iterations"],
+        "relax_wall_s": r["relax_wall_s"],
+        "e2e": {"value": r["e2e"], "unit": "ns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": r["d2h"],
+                "call": "nmag.Simulation.advance_time + get_subfield_average_siv('m')"},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+    }
+    if plain is not None:
+        line["plain_fp64"] = {"value": plain["value"], "e2e": plain["e2e"], "ms_per_step": plain["ms_per_step"],
+                              "rhs_evals_per_s": plain["rhs_evals_per_s"], "bdf_steps": plain["bdf_steps"],
+                              "roofline": plain["roofline"], "kernels_ms": plain["kernels_ms"],
+                              "gpu_launches": plain["launches"]}
+        line["speedup_vs_plain_fp64"] = r["value"] / plain["value"]
+        line["heff_rel_err_vs_fp64"] = heff_error(args, r, msh)
+        # member 0 starts from the plain run's state and both advanced the same time
+        a0 = np.asarray(r["eng"].member_averages(0) if B > 1 else r["eng"].averages())
+        line["avg_m_diff_vs_plain_fp64"] = float(np.abs(a0 - np.asarray(plain["eng"].averages())).max())
     if world == 1 and not args.no_cpu_baseline:
-        r = cpu_reference_run(args, msh, base, seed, steps=2, warmup=0, max_wall=20.0, sample_ps=0.5 * ps)
-        line["cpu_baseline"] = {"value": (r["sim_ps"] * 1e-3) / r["wall_s"], "unit": "ns/s", "cores": r["cores"],
+        cr = cpu_reference_run(args, msh, base, seed, steps=2, warmup=0, max_wall=20.0, sample_ps=0.5 * args.step_ps)
+        line["cpu_baseline"] = {"value": (cr["sim_ps"] * 1e-3) / cr["wall_s"], "unit": "ns/s", "cores": cr["cores"],
                                 "kind": "port",
-                                "sample": "%d x %.2f ps from the seeded initial state on the CPU restatement"
-                                          % (r["steps"], 0.5 * ps),
-                                "rhs_evals_per_s": r["nfe"] / r["wall_s"]}
+                                "sample": "%d x %.2f ps of one film from the seeded initial state on the CPU "
+                                          "restatement" % (cr["steps"], 0.5 * args.step_ps),
+                                "rhs_evals_per_s": cr["nfe"] / cr["wall_s"]}
     print(json.dumps(line))
 
 
@@ -367,20 +482,29 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--form", default="fp32x2", choices=["fp64", "fp32", "fp32x2"],
+                    help="BEM product: fp64; fp32 (FP32 entries, FP64 sums); fp32x2 (FP32 + BF16 residual "
+                         "entries, compensated FP32 products)")
     ap.add_argument("--workload", default="film", choices=["film", "cube", "film_small"])
     ap.add_argument("--step-ps", type=float, default=1.0)
     ap.add_argument("--relax-ps", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cg", default="fp64", choices=["fp64", "fp32"],
                     help="Poisson CG: FP64, or FP32 iterations with FP64 residual refinement")
-    ap.add_argument("--members", type=int, default=1,
+    ap.add_argument("--members", type=int, default=8,
                     help="ensemble size: B films on the one mesh integrated together (value summed over members)")
+    ap.add_argument("--report", default=None, choices=["precision"],
+                    help="precision: H_eff / energy error of the FP32 form against FP64 over --fields random fields")
+    ap.add_argument("--fields", type=int, default=1000)
+    ap.add_argument("--no-compare", dest="compare", action="store_false",
+                    help="skip the plain FP64 single-film run reported beside the chosen form")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.report == "precision":
+        run_precision_report(args)
     else:
         run_ours(args)
 

@@ -47,7 +47,9 @@ typedef struct nmg_options {
   int do_demag;                          /* 0: skip FEM/BEM demag                      */
   double nbc_rtol, nbc_atol; int nbc_maxits;   /* Neumann Poisson solve              */
   double dbc_rtol, dbc_atol; int dbc_maxits;   /* Dirichlet Poisson solve            */
-  int bem_precision;                     /* 0: FP64 matrix; 1: FP32 matrix, FP64 sums  */
+  int bem_precision;                     /* 0: FP64 matrix; 1: FP32 matrix, FP64 sums;
+                                            2: FP32 + BF16-residual matrix, compensated
+                                               FP32 products (~2^-44)                  */
   int cg_precision;                      /* 0: FP64 CG; reserved                       */
   int cg_no_coarse;                      /* 1: Jacobi only (no two-level Neumann CG)   */
   int n_members;                         /* ensemble size B (0 or 1: one simulation)   */

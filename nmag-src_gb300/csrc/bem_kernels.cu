@@ -13,6 +13,8 @@
 // transpose then stores the matrix row-major with the row stride padded to a
 // multiple of 8 (bem[k*ld + c]), the layout the matrix-vector product streams.
 // Compiled with --fmad=false to follow the written operation order.
+#include <cuda_bf16.h>
+
 #include "nmg_internal.h"
 
 namespace nmg {
@@ -154,6 +156,17 @@ __global__ void k_transpose_pad(int nb, int ld, const double *__restrict__ a, do
   }
 }
 
+// BF16 bits of the FP32 rounding residual B - fp32(B) (round to nearest even).
+__global__ void k_split_lo(size_t n, const double *__restrict__ a, const float *__restrict__ hi,
+                           uint16_t *__restrict__ lo) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) {
+    const __nv_bfloat16 v = __float2bfloat16_rn((float)(a[i] - (double)hi[i]));
+    lo[i] = *reinterpret_cast<const uint16_t *>(&v);
+  }
+}
+
 // FP32 copy of the row-major matrix (same padded stride).
 __global__ void k_to_f32(size_t n, const double *__restrict__ a, float *__restrict__ b) {
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -191,9 +204,13 @@ int fill_bem(nmg_handle *h, std::string &err) {
     NMG_CUDA_TRY(cudaGetLastError(), "bem transpose launch");
     NMG_CUDA_TRY(cudaStreamSynchronize(s), "bem fill");
   }
-  if (h->opt.bem_precision == 1) {
+  if (h->opt.bem_precision >= 1) {
     NMG_CUDA_TRY(M.bem32.alloc(nb * M.ld), "alloc FP32 BEM");
     k_to_f32<<<h->sm_count * 8, 256, 0, s>>>(nb * M.ld, M.bem, M.bem32);
+  }
+  if (h->opt.bem_precision == 2) {
+    NMG_CUDA_TRY(M.bem16lo.alloc(nb * M.ld), "alloc BEM residual (BF16)");
+    k_split_lo<<<h->sm_count * 8, 256, 0, s>>>(nb * M.ld, M.bem, M.bem32, M.bem16lo);
   }
   NMG_CUDA_TRY(cudaStreamSynchronize(s), "bem fill");
   return 0;

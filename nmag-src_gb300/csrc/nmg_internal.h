@@ -58,7 +58,8 @@ struct Mesh {
   DevBuf<double> coords, dL, adet, K, G, D, vol, tri_normal, solid_angle;
   DevBuf<int32_t> tets, nt_ptr, nt_idx, nbr, row_ptr, col_idx, diag_pos, b_of_node, node_of_b, tri;
   DevBuf<double> bem;      // FP64 BEM, row-major with padded row stride ld (bem[k*ld + c] = B[k][c])
-  DevBuf<float> bem32;     // FP32 copy (precision form), same layout
+  DevBuf<float> bem32;     // FP32 copy (precision forms 1, 2), same layout
+  DevBuf<uint16_t> bem16lo; // form 2: BF16 bits of B - fp32(B), same layout (B ~ hi + lo to ~2^-32)
   int ld = 0;              // row stride: nb rounded up to a multiple of 8 (64-byte aligned FP64 rows)
   DevBuf<TriGeo> trigeo;
   DevBuf<double> obs_max;

@@ -1587,6 +1587,142 @@ __global__ void k_slab_sum_m(int nb, int nslab, int nm, int MB, const double *__
   y[(size_t)m * nb + r] = s;
 }
 
+// ---- compensated ("double-float") BEM product: form 2 ----
+// B = hi (FP32) + lo (BF16), x = xh + xl (FP32 pairs).  Per entry: the
+// product hi * xh is split exactly with an FMA (p + e), the second-order
+// terms hi * xl + lo * xh join e, p enters a TwoSum running sum S whose
+// rounding errors are kept in C.  The result carries ~44 bits although
+// every operation runs on the FP32 pipe (the film's potentials cancel
+// ~50x in phi1 + phi2, so FP32 products alone lose 1e-5 there).
+// __fmul_rn / __fadd_rn / __fsub_rn forbid contraction and reassociation.
+__device__ __forceinline__ void df_madd(float h, float l, float a, float b, float &S, float &C) {
+  const float p = __fmul_rn(h, a);
+  const float e = fmaf(h, a, -p);
+  const float t = fmaf(h, b, fmaf(l, a, e));
+  const float s2 = __fadd_rn(S, p);
+  const float bb = __fsub_rn(s2, S);
+  const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s2, bb)), __fsub_rn(p, bb));
+  S = s2;
+  C += err + t;
+}
+
+__device__ __forceinline__ float bf16lo(unsigned w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16hi(unsigned w) { return __uint_as_float(w & 0xffff0000u); }
+
+// x (nm members, member m at m * n) -> FP32 pairs xh + xl, zero-padded to ld.
+__global__ void k_split_x(int n, int ld, int nm, const double *__restrict__ x, float *__restrict__ xh,
+                          float *__restrict__ xl) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ld * nm) return;
+  const int m = g / ld, i = g - m * ld;
+  const double v = i < n ? x[(size_t)m * n + i] : 0.0;
+  const float h = (float)v;
+  xh[g] = h;
+  xl[g] = (float)(v - (double)h);
+}
+
+// One simulation: the warp-segment decomposition of k_gemv_f32 (8-column units).
+__global__ void __launch_bounds__(kGemvThreads) k_gemv_df(int nb, int ld, long long seg, int maxr,
+                                                           const float *__restrict__ Bh,
+                                                           const uint16_t *__restrict__ Bl,
+                                                           const float *__restrict__ xh,
+                                                           const float *__restrict__ xl, double *__restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long Q = ld / 8, total = (long long)nb * Q;
+  const long long q0 = w * seg, q1 = min(total, q0 + seg);
+  if (q0 >= q1) return;
+  const long long rfirst = q0 / Q;
+  for (long long r = rfirst; r * Q < q1; ++r) {
+    const long long a = max(q0, r * Q), e = min(q1, (r + 1) * Q);
+    const float *rh = Bh + r * (long long)ld;
+    const uint16_t *rl = Bl + r * (long long)ld;
+    float S = 0.f, C = 0.f;
+    for (long long q = a + lane; q < e; q += 32) {
+      const long long c = 8 * (q - r * Q);
+      const float4 h0 = __ldcs(reinterpret_cast<const float4 *>(rh + c));
+      const float4 h1 = __ldcs(reinterpret_cast<const float4 *>(rh + c) + 1);
+      const uint4 lq = __ldcs(reinterpret_cast<const uint4 *>(rl + c));
+      const float4 a0 = __ldg(reinterpret_cast<const float4 *>(xh + c));
+      const float4 a1 = __ldg(reinterpret_cast<const float4 *>(xh + c) + 1);
+      const float4 b0 = __ldg(reinterpret_cast<const float4 *>(xl + c));
+      const float4 b1 = __ldg(reinterpret_cast<const float4 *>(xl + c) + 1);
+      df_madd(h0.x, bf16lo(lq.x), a0.x, b0.x, S, C);
+      df_madd(h0.y, bf16hi(lq.x), a0.y, b0.y, S, C);
+      df_madd(h0.z, bf16lo(lq.y), a0.z, b0.z, S, C);
+      df_madd(h0.w, bf16hi(lq.y), a0.w, b0.w, S, C);
+      df_madd(h1.x, bf16lo(lq.z), a1.x, b1.x, S, C);
+      df_madd(h1.y, bf16hi(lq.z), a1.y, b1.y, S, C);
+      df_madd(h1.z, bf16lo(lq.w), a1.z, b1.z, S, C);
+      df_madd(h1.w, bf16hi(lq.w), a1.w, b1.w, S, C);
+    }
+    const double sum = warp_sum((double)S + (double)C);
+    if (lane == 0) part[w * maxr + (r - rfirst)] = sum;
+  }
+}
+
+// Ensemble: tiles of kDfCols columns x kDfRows rows; the slab's xh / xl of
+// every member in shared memory, each warp kDfRpw rows at a time.
+constexpr int kDfCols = 512, kDfRows = 64, kDfRpw = 2;
+
+template <int MB>
+__global__ void __launch_bounds__(256) k_gemm_df(int nb, int ld, int nm, const float *__restrict__ Bh,
+                                                 const uint16_t *__restrict__ Bl, const float *__restrict__ xh,
+                                                 const float *__restrict__ xl, double *__restrict__ part) {
+  __shared__ float4 sh[MB][kDfCols / 4], sl[MB][kDfCols / 4];
+  const int slab = blockIdx.x, c0 = slab * kDfCols;
+  const int ncol = min(kDfCols, ld - c0);   // a multiple of 8
+  for (int i = threadIdx.x; i < MB * (kDfCols / 4); i += blockDim.x) {
+    const int m = i / (kDfCols / 4), q = i - m * (kDfCols / 4);
+    const bool ok = m < nm && 4 * q < ncol;
+    sh[m][q] = ok ? __ldg(reinterpret_cast<const float4 *>(xh + (size_t)m * ld + c0) + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    sl[m][q] = ok ? __ldg(reinterpret_cast<const float4 *>(xl + (size_t)m * ld + c0) + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int units = ncol / 8;
+  const int rend = min(nb, (int)(blockIdx.y + 1) * kDfRows);
+  for (int r0 = blockIdx.y * kDfRows + warp * kDfRpw; r0 < rend; r0 += 8 * kDfRpw) {
+    float S[kDfRpw * MB], C[kDfRpw * MB];
+#pragma unroll
+    for (int q = 0; q < kDfRpw * MB; ++q) S[q] = C[q] = 0.f;
+    for (int u = lane; u < units; u += 32) {
+      float hv[kDfRpw][8], lv[kDfRpw][8];
+#pragma unroll
+      for (int rr = 0; rr < kDfRpw; ++rr) {
+        const size_t off = (size_t)min(r0 + rr, nb - 1) * ld + c0 + 8 * u;
+        const float4 h0 = __ldcs(reinterpret_cast<const float4 *>(Bh + off));
+        const float4 h1 = __ldcs(reinterpret_cast<const float4 *>(Bh + off) + 1);
+        const uint4 lq = __ldcs(reinterpret_cast<const uint4 *>(Bl + off));
+        hv[rr][0] = h0.x; hv[rr][1] = h0.y; hv[rr][2] = h0.z; hv[rr][3] = h0.w;
+        hv[rr][4] = h1.x; hv[rr][5] = h1.y; hv[rr][6] = h1.z; hv[rr][7] = h1.w;
+        lv[rr][0] = bf16lo(lq.x); lv[rr][1] = bf16hi(lq.x); lv[rr][2] = bf16lo(lq.y); lv[rr][3] = bf16hi(lq.y);
+        lv[rr][4] = bf16lo(lq.z); lv[rr][5] = bf16hi(lq.z); lv[rr][6] = bf16lo(lq.w); lv[rr][7] = bf16hi(lq.w);
+      }
+#pragma unroll
+      for (int m = 0; m < MB; ++m) {
+        const float4 a0 = sh[m][2 * u], a1 = sh[m][2 * u + 1], b0 = sl[m][2 * u], b1 = sl[m][2 * u + 1];
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int rr = 0; rr < kDfRpw; ++rr)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) df_madd(hv[rr][j], lv[rr][j], av[j], bv[j], S[rr * MB + m], C[rr * MB + m]);
+      }
+    }
+    constexpr int NV = kDfRpw * MB;
+    constexpr int SH = NV >= 32 ? 0 : (NV >= 16 ? 1 : (NV >= 8 ? 2 : 3));
+    double acc[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc[q] = (double)S[q] + (double)C[q];
+    const double tot = warp_transpose_sum<double, NV>(acc);
+    const int v = lane >> SH;
+    const int rr = v / MB, m = v - rr * MB;
+    if ((lane & ((1 << SH) - 1)) == 0 && m < nm && r0 + rr < nb)
+      part[((size_t)slab * nb + r0 + rr) * MB + m] = tot;
+  }
+}
+
 // y[m * nb + r] = ordered sum of member m's partials of row r.
 __global__ void k_row_sum_m(int nb, long long Q, long long seg, int maxr, long long nwarps, int nm, int MB,
                             const double *__restrict__ part, double *__restrict__ y) {
@@ -2063,10 +2199,12 @@ int init_workspace(nmg_handle *h, std::string &err) {
   }
   // partials (kChunk members for the ensemble), then FP32 copies of x padded to ld
   part_n *= (B > 1 ? kChunk : 1);
-  if (B > 1 && nb > 0)   // FP32 tiles: one partial per (slab, row, member)
-    part_n = std::max(part_n, (size_t)((M.ld + kTileCols - 1) / kTileCols) * nb * kChunk);
+  if (B > 1 && nb > 0)   // FP32 / compensated tiles: one partial per (slab, row, member)
+    part_n = std::max(part_n, (size_t)((M.ld + std::min(kTileCols, kDfCols) - 1) / std::min(kTileCols, kDfCols)) *
+                                  nb * kChunk);
   W.gemv_x32_off = (part_n + 7) / 8 * 8;
-  NMG_CUDA_TRY(W.bpart.alloc(W.gemv_x32_off + (size_t)BC * M.ld / 2 + 8), "alloc gemv partials");
+  // FP32 x copies: BC members, or BC (xh, xl) pairs for the compensated product
+  NMG_CUDA_TRY(W.bpart.alloc(W.gemv_x32_off + (size_t)BC * M.ld + 8), "alloc gemv partials");
   // 2 parities x kCG2MaxRed values per block (at least 1024 blocks: averages use it too)
   size_t red_n = 2 * (size_t)kCG2MaxRed * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);
   NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
@@ -2098,10 +2236,18 @@ void bem_gemv(nmg_handle *h, const double *x, double *y) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   const int nb = M.nb;
-  const int f = (h->opt.bem_precision == 1 && M.bem32.p) ? 1 : 0;
+  const int f = (h->opt.bem_precision >= 1 && M.bem32.p) ? 1 : 0;
   const long long seg = W.gemv_seg[f];
   const int maxr = W.gemv_maxr[f];
-  if (f == 1) {
+  if (f == 1 && M.bem16lo.p) {   // compensated FP32 pair product
+    float *xh = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
+    float *xl = xh + M.ld;
+    k_split_x<<<nblk(M.ld, 256), 256, 0, h->stream>>>(nb, M.ld, 1, x, xh, xl); ++h->launches;
+    NMG_PROF_BEGIN(h, 0);
+    k_gemv_df<<<W.gemv_blocks, kGemvThreads, 0, h->stream>>>(nb, M.ld, seg, maxr, M.bem32, M.bem16lo, xh, xl, W.bpart);
+    ++h->launches;
+    NMG_PROF_END(h);
+  } else if (f == 1) {
     float *x32 = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
     k_to_f32_vec<<<nblk(M.ld, 256), 256, 0, h->stream>>>(nb, M.ld, x, x32); ++h->launches;
     NMG_PROF_BEGIN(h, 0);
@@ -2122,7 +2268,7 @@ void bem_gemm(nmg_handle *h, const double *x, double *y) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   const int nb = M.nb, B = h->nrep;
-  const int f = (h->opt.bem_precision == 1 && M.bem32.p) ? 1 : 0;
+  const int f = (h->opt.bem_precision >= 1 && M.bem32.p) ? 1 : 0;
   const long long seg = W.gemv_seg[f];
   const int maxr = W.gemv_maxr[f];
   const long long Q = M.ld / (f == 0 ? 4 : 8);
@@ -2131,6 +2277,23 @@ void bem_gemm(nmg_handle *h, const double *x, double *y) {
     const int nm = std::min(kChunk, B - c0);
     const int MB = nm <= 2 ? 2 : (nm <= 4 ? 4 : 8);
     const double *xc = x + (size_t)c0 * nb;
+    if (f == 1 && M.bem16lo.p) {   // compensated FP32 pair product on tiles
+      float *xh = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
+      float *xl = xh + (size_t)nm * M.ld;
+      k_split_x<<<nblk((long long)M.ld * nm, 256), 256, 0, h->stream>>>(nb, M.ld, nm, xc, xh, xl); ++h->launches;
+      const int nslab = (M.ld + kDfCols - 1) / kDfCols;
+      dim3 grid(nslab, (nb + kDfRows - 1) / kDfRows);
+      NMG_PROF_BEGIN(h, 0);
+      if (MB == 2) k_gemm_df<2><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, M.bem16lo, xh, xl, W.bpart);
+      else if (MB == 4) k_gemm_df<4><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, M.bem16lo, xh, xl, W.bpart);
+      else k_gemm_df<8><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, M.bem16lo, xh, xl, W.bpart);
+      NMG_PROF_END(h);
+      ++h->launches;
+      k_slab_sum_m<<<nblk((long long)nb * nm, 256), 256, 0, h->stream>>>(nb, nslab, nm, MB, W.bpart,
+                                                                         y + (size_t)c0 * nb);
+      ++h->launches;
+      continue;
+    }
     if (f == 1) {
       float *x32 = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
       k_to_f32_vec<<<nblk((long long)M.ld * nm, 256), 256, 0, h->stream>>>(nb, M.ld, xc, x32, nm); ++h->launches;
