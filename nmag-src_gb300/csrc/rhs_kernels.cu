@@ -1606,6 +1606,43 @@ __device__ __forceinline__ void df_madd(float h, float l, float a, float b, floa
   C += err + t;
 }
 
+// (S, C) += (S2, C2) for FP32 pairs: TwoSum of the heads, the tails added.
+__device__ __forceinline__ void df_add(float &S, float &C, float S2, float C2) {
+  const float s2 = __fadd_rn(S, S2);
+  const float bb = __fsub_rn(s2, S);
+  const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s2, bb)), __fsub_rn(S2, bb));
+  S = s2;
+  C = __fadd_rn(__fadd_rn(C, C2), err);
+}
+
+// warp_transpose_sum for NV (S, C) pairs, all in FP32 pair arithmetic: the
+// FP64 pipe is used only for the one conversion per result afterwards.
+template <int NV>
+__device__ __forceinline__ void warp_transpose_sum_df(float (&S)[NV], float (&C)[NV]) {
+  const int lane = threadIdx.x & 31;
+  int n = NV;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    if (n > 1) {
+      const bool up = (lane & o) != 0;
+#pragma unroll
+      for (int i = 0; i < NV / 2; ++i) {
+        if (i >= n / 2) break;
+        const float sS = up ? S[i] : S[i + n / 2], sC = up ? C[i] : C[i + n / 2];
+        const float kS = up ? S[i + n / 2] : S[i], kC = up ? C[i + n / 2] : C[i];
+        const float rS = __shfl_xor_sync(0xffffffffu, sS, o), rC = __shfl_xor_sync(0xffffffffu, sC, o);
+        S[i] = kS;
+        C[i] = kC;
+        df_add(S[i], C[i], rS, rC);
+      }
+      n >>= 1;
+    } else {
+      const float rS = __shfl_xor_sync(0xffffffffu, S[0], o), rC = __shfl_xor_sync(0xffffffffu, C[0], o);
+      df_add(S[0], C[0], rS, rC);
+    }
+  }
+}
+
 __device__ __forceinline__ float bf16lo(unsigned w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float bf16hi(unsigned w) { return __uint_as_float(w & 0xffff0000u); }
 
@@ -1712,14 +1749,11 @@ __global__ void __launch_bounds__(256) k_gemm_df(int nb, int ld, int nm, const f
     }
     constexpr int NV = kDfRpw * MB;
     constexpr int SH = NV >= 32 ? 0 : (NV >= 16 ? 1 : (NV >= 8 ? 2 : 3));
-    double acc[NV];
-#pragma unroll
-    for (int q = 0; q < NV; ++q) acc[q] = (double)S[q] + (double)C[q];
-    const double tot = warp_transpose_sum<double, NV>(acc);
+    warp_transpose_sum_df<NV>(S, C);
     const int v = lane >> SH;
     const int rr = v / MB, m = v - rr * MB;
     if ((lane & ((1 << SH) - 1)) == 0 && m < nm && r0 + rr < nb)
-      part[((size_t)slab * nb + r0 + rr) * MB + m] = tot;
+      part[((size_t)slab * nb + r0 + rr) * MB + m] = (double)S[0] + (double)C[0];
   }
 }
 
