@@ -424,6 +424,88 @@ def run_precision_report(args):
     print(json.dumps(line))
 
 
+def run_adjoint_report(args):
+    """Differentiation form on the workload: fixed-step RK4 (dt = 0.1 ps) with
+    per-element Ms (Ms (1 + 0.05 N(0,1)), seed 3), per-element K1 (0) and 20
+    pulse amplitudes (N(0, 5 mT), seed 4) as parameters, loss
+    ||<m>(T) - (0,1,0)||^2 + 1e-3 mean_t <m>_x^2; times one forward + adjoint
+    (CUDA-event free: wall time around synchronised calls) and checks the
+    adjoint's directional derivatives against central differences
+    (h = 1e-6 relative) along seeded directions on a shorter trajectory."""
+    import torch
+    import nmag
+    from nmag import SI, adjoint
+    torch.cuda.set_device(0)
+    msh, base, seed = workload(args.workload)
+    mat = material(0.02)
+    sim = nmag.Simulation("adj", ksp_tolerances={"NBC.rtol": 1e-10, "DBC.rtol": 1e-10})
+    sim.load_mesh(msh, [("film", mat)], unit_length=SI(1e-9, "m"))
+    eng = sim.engine
+    c = mat.coefficients("nmag")
+    from nmag.si import simulation_units, mu0 as mu0_si
+    mu0 = simulation_units.of(mu0_si)
+    T = eng.T
+    Ms_T = c["Ms"] * (1.0 + 0.05 * np.random.default_rng(3).standard_normal(T))
+    K1_T = np.zeros(T)
+    pulses = np.random.default_rng(4).standard_normal((20, 3)) * (5e-3 / MU0) * 1e-6
+    m0 = initial_m(msh.n_nodes, base, seed).reshape(-1)
+    eng.set_h_ext(np.broadcast_to(h_ext_su(), (eng.N, 3)))
+    dt = 0.1
+    nsteps, ckpt = args.adj_steps, 50
+    spp = max(1, nsteps // 20)
+    axis = (1.0, 0.0, 0.0)
+
+    def run(Ms, K1, P, steps, grad):
+        tM = torch.tensor(Ms, device="cuda", dtype=torch.float64, requires_grad=grad)
+        tK = torch.tensor(K1, device="cuda", dtype=torch.float64, requires_grad=grad)
+        tP = torch.tensor(P, device="cuda", dtype=torch.float64, requires_grad=grad)
+        tm = torch.tensor(m0, device="cuda", dtype=torch.float64)
+        _, hist = adjoint.rk4_trajectory(eng, tm, tM, tK, tP, axis, c["Ms"], mu0, dt, steps, ckpt,
+                                         max(1, steps // 20))
+        loss = adjoint.film_loss(hist)
+        if grad:
+            loss.backward()
+            return loss.item(), tM.grad.cpu().numpy(), tK.grad.cpu().numpy(), tP.grad.cpu().numpy()
+        return loss.item()
+
+    torch.cuda.synchronize()
+    launches0 = eng.launch_count()
+    w = time.perf_counter()
+    loss, gM, gK, gP = run(Ms_T, K1_T, pulses, nsteps, True)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w
+    launches = eng.launch_count() - launches0
+    # finite differences on a shorter trajectory
+    fd_steps = args.adj_fd_steps
+    _, gM2, gK2, gP2 = run(Ms_T, K1_T, pulses, fd_steps, True)
+    h = 1e-6
+    rng = np.random.default_rng(11)
+    errs = []
+    for _ in range(args.adj_dirs):
+        dM = Ms_T * rng.standard_normal(T)
+        dK = 0.05 * rng.standard_normal(T)
+        dP = np.abs(pulses).mean() * rng.standard_normal(pulses.shape)
+        lp = run(Ms_T + h * dM, K1_T + h * dK, pulses + h * dP, fd_steps, False)
+        lm = run(Ms_T - h * dM, K1_T - h * dK, pulses - h * dP, fd_steps, False)
+        fd = (lp - lm) / (2 * h)
+        ad = gM2 @ dM + gK2 @ dK + (gP2 * dP).sum()
+        errs.append(abs(fd - ad) / max(abs(ad), 1e-30))
+    line = {"metric": "forward + adjoint wall time", "report": "adjoint", "value": wall, "unit": "s",
+            "higher_is_better": False, "workload": WORKLOAD_NAMES[args.workload],
+            "trajectory": {"steps": nsteps, "dt_ps": dt, "checkpoint_every": ckpt, "pulses": 20,
+                           "steps_per_pulse": spp, "rhs_evals": 8 * nsteps, "vjp_evals": 4 * nsteps,
+                           "note": "20 pulses span the trajectory (T/20 each; the configuration's 100 ps "
+                                   "pulses would leave 18 of 20 beyond 2000 x 0.1 ps)"},
+            "params": {"Ms_per_element": T, "K1_per_element": T, "pulse_amplitudes": 60},
+            "loss": loss, "grad_norms": {"Ms": float(np.linalg.norm(gM)), "K1": float(np.linalg.norm(gK)),
+                                         "pulses": float(np.linalg.norm(gP))},
+            "sim_ps_per_s": nsteps * dt / wall,
+            "fd_check": {"steps": fd_steps, "directions": len(errs), "h_rel": h,
+                         "max_rel_err": max(errs) if errs else None, "bound": 1e-5},
+            "gpu_launches": launches}
+    print(json.dumps(line))
+
+
 def run_ours(args):
     import torch
     rank, world = dist_setup(args.gpus)
@@ -493,7 +575,10 @@ def main():
                     help="Poisson CG: FP64, or FP32 iterations with FP64 residual refinement")
     ap.add_argument("--members", type=int, default=8,
                     help="ensemble size: B films on the one mesh integrated together (value summed over members)")
-    ap.add_argument("--report", default=None, choices=["precision"],
+    ap.add_argument("--adj-steps", type=int, default=2000)
+    ap.add_argument("--adj-fd-steps", type=int, default=100)
+    ap.add_argument("--adj-dirs", type=int, default=4)
+    ap.add_argument("--report", default=None, choices=["precision", "adjoint"],
                     help="precision: H_eff / energy error of the FP32 form against FP64 over --fields random fields")
     ap.add_argument("--fields", type=int, default=1000)
     ap.add_argument("--no-compare", dest="compare", action="store_false",
@@ -505,6 +590,8 @@ def main():
         run_reference(args)
     elif args.report == "precision":
         run_precision_report(args)
+    elif args.report == "adjoint":
+        run_adjoint_report(args)
     else:
         run_ours(args)
 
