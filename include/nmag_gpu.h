@@ -199,6 +199,54 @@ int nmg_rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, in
 int nmg_rk4_adjoint(nmg_handle *h, const double *d_m_final_bar, const double *d_avg_hist_bar, double *d_m0_bar,
                     double *d_wK_bar, double *d_wD_bar, double *d_kappa_bar, double *d_pulses_bar);
 
+/* Batching form: many independent particles (each its own mesh, material
+ * and applied-field direction) advanced together in one persistent launch.
+ * No counterpart in the reference (one simulation per process); each particle
+ * follows the RHS of nmag_lam.py:734-832 and the hysteresis loop of
+ * hysteresis.py:244-557 (relax to max |dm/dt| < stop_dmdt twice in a row,
+ * then the next field H_k = h_max (1 - 2k/(n_stages-1)) along h_dir).  Time
+ * integration: embedded Bogacki-Shampine 3(2) with per-particle step control
+ * (or a fixed step when fixed_dt > 0).  The BEM blocks are FP32 with FP64 row
+ * sums.  Arrays of all particles are concatenated in particle order. */
+typedef struct nmg_particle {
+  const double *coords;   /* 3 n_nodes, simulation units */
+  int n_nodes;
+  const int32_t *tets;    /* 4 n_tets */
+  int n_tets;
+  nmg_material mat;
+  double h_dir[3];        /* direction of the field sweep */
+} nmg_particle;
+
+typedef struct nmg_batch_options {
+  double cg_rtol; int cg_maxits;          /* both Poisson solves                         */
+  int n_stages;                           /* fields in the sweep                         */
+  double rtol, atol;                      /* step control (max norm)                     */
+  double stop_dmdt;                       /* convergence, su (1 deg/ns = 1.745e-5)       */
+  double h_max;                           /* sweep amplitude, su                         */
+  double dt0, dt_max, fixed_dt;           /* initial / maximal step; fixed_dt > 0: no control */
+  int threads;                            /* CTA size (0: 256)                           */
+  double budget;                          /* work per particle per launch (0: one step)  */
+  int reserved[4];
+} nmg_batch_options;
+
+typedef struct nmg_batch nmg_batch;
+const char *nmg_batch_last_error(const nmg_batch *b);
+int nmg_batch_create(const nmg_particle *parts, int n, const nmg_batch_options *opt, nmg_batch **out);
+int nmg_batch_destroy(nmg_batch *b);
+int nmg_batch_info(const nmg_batch *b, int64_t *nodes_total, int32_t *nodes, int32_t *nb);
+int nmg_batch_set_m(nmg_batch *b, const double *m);
+int nmg_batch_get_m(const nmg_batch *b, double *m);
+/* dm/dt and H_total of every particle at its current m and stage field. */
+int nmg_batch_eval(nmg_batch *b, double *dmdt, double *h_total);
+/* Replay a CUDA graph of `launches` persistent launches; returns when done. */
+int nmg_batch_run(nmg_batch *b, int launches);
+int nmg_batch_state(const nmg_batch *b, double *t, int32_t *stage, int64_t *steps, int64_t *rhs_evals,
+                    int32_t *done, double *max_dmdt);
+/* CTA size and per-launch work budget; the autotuner times candidates on the
+ * batch (state restored afterwards) and keeps the fastest. */
+int nmg_batch_set_schedule(nmg_batch *b, int threads, double budget);
+int nmg_batch_autotune(nmg_batch *b, int trial_launches, int *threads_out, double *budget_out);
+
 /* Wall-clock split of the last nmg_ts_advance / RHS work, in ms (CUDA events). */
 int nmg_get_timings(const nmg_handle *h, double out[8]);
 

@@ -29,6 +29,18 @@ class Options(C.Structure):
                 ("n_members", C.c_int), ("reserved", C.c_int * 4)]
 
 
+class Particle(C.Structure):
+    _fields_ = [("coords", C.c_void_p), ("n_nodes", C.c_int), ("tets", C.c_void_p), ("n_tets", C.c_int),
+                ("mat", Material), ("h_dir", C.c_double * 3)]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("cg_rtol", C.c_double), ("cg_maxits", C.c_int), ("n_stages", C.c_int), ("rtol", C.c_double),
+                ("atol", C.c_double), ("stop_dmdt", C.c_double), ("h_max", C.c_double), ("dt0", C.c_double),
+                ("dt_max", C.c_double), ("fixed_dt", C.c_double), ("threads", C.c_int), ("budget", C.c_double),
+                ("reserved", C.c_int * 4)]
+
+
 class TsStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("nst", "nfe", "nni", "nli", "ncfn", "netf", "npe", "nps", "njv", "nje")] + \
                [("hcur", C.c_double), ("tcur", C.c_double), ("qcur", C.c_int32), ("last_cg_iters_nbc", C.c_int32),
@@ -46,7 +58,9 @@ EXPORTS = ["nmg_version", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_me
            "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
            "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_max_dm_static",
            "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
-           "nmg_member_averages"]
+           "nmg_member_averages", "nmg_batch_last_error", "nmg_batch_create", "nmg_batch_destroy", "nmg_batch_info",
+           "nmg_batch_set_m", "nmg_batch_get_m", "nmg_batch_eval", "nmg_batch_run", "nmg_batch_state",
+           "nmg_batch_set_schedule", "nmg_batch_autotune"]
 
 PROFILED_KERNELS = ["bem_gemv", "cg_neumann", "cg_dirichlet", "heff_llg", "jv_psolve"]
 
@@ -103,6 +117,18 @@ def lib(build_if_missing=True):
     L.nmg_cg_iterations.argtypes = [vp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]
     L.nmg_max_dm_static.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_double)]
     L.nmg_member_averages.argtypes = [vp, C.c_int, _f64p, vp]
+    L.nmg_batch_last_error.argtypes = [vp]
+    L.nmg_batch_last_error.restype = C.c_char_p
+    L.nmg_batch_create.argtypes = [vp, C.c_int, C.POINTER(BatchOptions), C.POINTER(vp)]
+    L.nmg_batch_destroy.argtypes = [vp]
+    L.nmg_batch_info.argtypes = [vp, vp, vp, vp]
+    L.nmg_batch_set_m.argtypes = [vp, _f64p]
+    L.nmg_batch_get_m.argtypes = [vp, _f64p]
+    L.nmg_batch_eval.argtypes = [vp, vp, vp]
+    L.nmg_batch_run.argtypes = [vp, C.c_int]
+    L.nmg_batch_state.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.nmg_batch_set_schedule.argtypes = [vp, C.c_int, C.c_double]
+    L.nmg_batch_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]
     L.nmg_set_element_params.argtypes = [vp, vp, vp, vp, _f64p]
     L.nmg_clear_element_params.argtypes = [vp]
     L.nmg_rk4_forward.argtypes = [vp, vp, C.c_double, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, vp]

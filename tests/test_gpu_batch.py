@@ -1,0 +1,107 @@
+"""Batching form on the GPU: independent particles of different size,
+material and field direction in one persistent launch (nmag.batch), checked
+particle by particle against the CPU oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import seeded_m
+
+pytestmark = pytest.mark.gpu
+
+
+def _particles(cells, seed=2, alpha=0.1):
+    import nmag
+    from nmag import SI, mesh
+    rng = np.random.default_rng(seed)
+    out, coeffs_list = [], []
+    for k, c in enumerate(cells):
+        msh = mesh.box_mesh(c, c, c, 2.0)
+        Ms = rng.uniform(4e5, 1.7e6)
+        K1 = rng.uniform(0.0, 5e5)
+        ax = rng.standard_normal(3)
+        ax /= np.linalg.norm(ax)
+        mat = nmag.MagMaterial("p%d" % k, Ms=SI(Ms, "A/m"), exchange_coupling=SI(1.3e-11, "J/m"), llg_damping=alpha,
+                               llg_gamma_G=SI(2.211e5, "m/A s"),
+                               anisotropy=nmag.uniaxial_anisotropy(axis=list(ax), K1=SI(K1, "J/m^3")))
+        hd = rng.standard_normal(3)
+        hd /= np.linalg.norm(hd)
+        c_ = mat.coefficients("nmag")
+        out.append((msh.points, msh.simplices, c_, hd))
+        coeffs_list.append((msh, c_, hd))
+    return out, coeffs_list
+
+
+def _oracle_rhs(msh, coeffs, h, m):
+    om = oracle.OracleMesh(msh.points, msh.simplices)
+    sim = oracle.OracleSim(om, coeffs, nbc=(1e-12, 1e-50, 20000), dbc=(1e-12, 1e-50, 20000))
+    sim.set_h_ext(h)
+    return sim, sim.rhs(m).reshape(-1, 3)
+
+
+def test_batch_rhs_matches_oracle():
+    from nmag.batch import ParticleBatch
+    parts, info = _particles([3, 4, 6])
+    hmax = 0.3
+    b = ParticleBatch(parts, n_stages=5, h_max=hmax, cg_rtol=1e-12)
+    ms = [seeded_m(len(p[0]), base=(1.0, 0.5, -0.3), seed=40 + k, noise=0.4) for k, p in enumerate(parts)]
+    b.set_m(ms)
+    f, H = b.eval()
+    for k, (msh, c_, hd) in enumerate(info):
+        _, ref = _oracle_rhs(msh, c_, hmax * hd, ms[k])
+        err = np.abs(f[k] - ref).max() / np.abs(ref).max()
+        assert err <= 1e-5, (k, err)
+    b.close()
+
+
+def test_batch_fixed_step_matches_bs3_reference():
+    """Fixed-step Bogacki-Shampine on the GPU against the same scheme driven
+    by the oracle's RHS (FSAL: the last stage slope starts the next step)."""
+    from nmag.batch import ParticleBatch
+    parts, info = _particles([3, 5], seed=5)
+    hmax, dt, steps = 0.2, 0.02, 4
+    b = ParticleBatch(parts, n_stages=3, h_max=hmax, cg_rtol=1e-12, fixed_dt=dt, budget=0.0)
+    ms = [seeded_m(len(p[0]), base=(0.3, 1.0, 0.2), seed=60 + k, noise=0.3) for k, p in enumerate(parts)]
+    b.set_m(ms)
+    b.run(steps)   # budget 0: one step per particle per launch
+    got = b.get_m()
+    st = b.state()
+    assert (st["steps"] == steps).all()
+    for k, (msh, c_, hd) in enumerate(info):
+        sim, _ = _oracle_rhs(msh, c_, hmax * hd, ms[k])
+        m = ms[k].copy()
+        f = lambda y: sim.rhs(y).reshape(-1, 3)
+        k1 = f(m)
+        for _ in range(steps):
+            k2 = f(m + 0.5 * dt * k1)
+            k3 = f(m + 0.75 * dt * k2)
+            y = m + dt * ((2.0 / 9.0) * k1 + (1.0 / 3.0) * k2 + (4.0 / 9.0) * k3)
+            k1 = f(y)
+            m = y
+        assert np.abs(got[k] - m).max() <= 1e-7, (k, np.abs(got[k] - m).max())
+    b.close()
+
+
+def test_batch_sweep_completes_and_autotune():
+    """Every particle walks its 3-field sweep to the end.  The explicit
+    integrator's error-controlled fluctuation of |dm/dt| is ~tol/dt, so the
+    step tolerance (1e-6) sits well below the convergence threshold."""
+    from nmag.batch import ParticleBatch
+    parts, _ = _particles([3, 4, 3, 5], seed=7, alpha=1.0)
+    b = ParticleBatch(parts, n_stages=3, h_max=0.5, stop_dmdt=5e-3, rtol=1e-6, atol=1e-6)
+    ms = [seeded_m(len(p[0]), base=(1.0, 1.0, 1.0), seed=80 + k, noise=0.2) for k, p in enumerate(parts)]
+    b.set_m(ms)
+    threads, budget = b.autotune(trial_launches=1)
+    assert threads in (128, 256, 512) and budget > 0
+    b.set_schedule(threads, 50 * budget)
+    for _ in range(300):
+        b.run(4)
+        st = b.state()
+        if st["done"].all():
+            break
+    assert st["done"].all(), st
+    assert (st["stage"] == 3).all()
+    m = b.get_m()
+    for k in range(len(parts)):
+        assert np.abs(np.linalg.norm(m[k], axis=1) - 1.0).max() < 1e-2
+    b.close()
