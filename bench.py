@@ -506,6 +506,122 @@ def run_adjoint_report(args):
     print(json.dumps(line))
 
 
+def particle_batch_config(n=256, seed=2):
+    """The batching configuration: cubes with edge U[8, 40] nm at a 2 nm pitch
+    (round(edge/2) cells per side), Ms U[4e5, 1.7e6] A/m, K1 U[0, 5e5] J/m^3
+    along a random unit axis, alpha 0.1, field sweep direction random."""
+    import nmag
+    from nmag import SI, mesh
+    rng = np.random.default_rng(seed)
+    parts = []
+    for k in range(n):
+        c = int(round(rng.uniform(8.0, 40.0) / 2.0))
+        msh = mesh.box_mesh(c, c, c, 2.0)
+        Ms, K1 = rng.uniform(4e5, 1.7e6), rng.uniform(0.0, 5e5)
+        ax = rng.standard_normal(3)
+        ax /= np.linalg.norm(ax)
+        hd = rng.standard_normal(3)
+        hd /= np.linalg.norm(hd)
+        mat = nmag.MagMaterial("p%d" % k, Ms=SI(Ms, "A/m"), exchange_coupling=SI(1.3e-11, "J/m"), llg_damping=0.1,
+                               llg_gamma_G=SI(2.211e5, "m/A s"),
+                               anisotropy=nmag.uniaxial_anisotropy(axis=list(ax), K1=SI(K1, "J/m^3")))
+        parts.append((msh.points, msh.simplices, mat.coefficients("nmag"), hd))
+    return parts
+
+
+def run_batch_report(args):
+    """Batching form on the 256-particle configuration: setup, autotuned
+    schedule, then timed CUDA-graph replays; reports the aggregate RHS and
+    simulated-time throughput and the sweep's progress, and beside it the
+    one-at-a-time RHS rate of a sample of particles on single handles (FP64
+    BEM, same CG tolerance)."""
+    import torch
+    from nmag.batch import ParticleBatch
+    from nmag import _lib
+    torch.cuda.set_device(0)
+    parts = particle_batch_config(args.particles)
+    h_max = (1.0 / MU0) / 1e6   # 1 T / mu0 in simulation units
+    w = time.perf_counter()
+    b = ParticleBatch(parts, n_stages=81, h_max=h_max, rtol=1e-6, atol=1e-6, cg_rtol=1e-6)
+    setup = time.perf_counter() - w
+    sizes = np.array(b.sizes)
+    ms = [initial_m(n, (1.0, 1.0, 1.0), 100 + k) for k, n in enumerate(sizes)]
+    # start along the first field so the sweep begins near saturation
+    ms = [np.broadcast_to(np.asarray(parts[k][3]), (n, 3)) + 0.05 * ms[k] for k, n in enumerate(sizes)]
+    ms = [m / np.linalg.norm(m, axis=1)[:, None] for m in ms]
+    b.set_m(ms)
+    w = time.perf_counter()
+    threads, budget = b.autotune(trial_launches=2)
+    tune = time.perf_counter() - w
+    b.set_schedule(threads, budget)
+    b.run(args.warmup)
+    s0 = b.state()
+    torch.cuda.synchronize()
+    w = time.perf_counter()
+    b.run(args.steps)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w
+    s1 = b.state()
+    rhs = int((s1["rhs"] - s0["rhs"]).sum())
+    node_rhs = float(((s1["rhs"] - s0["rhs"]) * sizes).sum())
+    sim_ps = float((s1["t"] - s0["t"]).sum())
+    # one-at-a-time reference: single handles on a size-stratified sample
+    order = np.argsort(sizes)
+    sample = order[np.linspace(0, len(order) - 1, 8).astype(int)]
+    per_rhs = {}
+    for k in sample:
+        pts, sim, c_, hd = parts[k]
+        mt = _lib.Material()
+        mt.Ms, mt.exch_coeff, mt.C1, mt.C2, mt.C3 = c_["Ms"], c_["exch_coeff"], c_["C1"], c_["C2"], c_["C3"]
+        mt.K1, mt.anis_coeff = c_["K1"], c_["anis_coeff"]
+        for d in range(3):
+            mt.axis[d] = c_["axis"][d]
+        op = _lib.Options()
+        op.do_demag = 1
+        op.nbc_rtol = op.dbc_rtol = 1e-6
+        op.nbc_atol = op.dbc_atol = 1e-50
+        op.nbc_maxits = op.dbc_maxits = 10000
+        eng = _lib.Engine(pts, sim, mt, op)
+        eng.set_m(ms[k])
+        eng.set_h_ext(np.broadcast_to(h_max * hd, (eng.N, 3)))
+        dm = torch.tensor(ms[k].reshape(-1), device="cuda", dtype=torch.float64)
+        out = torch.empty_like(dm)
+        for _ in range(3):
+            eng.rhs_device(dm.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(20):
+            eng.rhs_device(dm.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        per_rhs[int(sizes[k])] = (time.perf_counter() - t0) / 20
+        eng.close()
+    xs = np.array(sorted(per_rhs))
+    ys = np.array([per_rhs[x] for x in xs])
+    est = float(np.interp(sizes, xs, ys).sum())   # seconds for one RHS of every particle, one at a time
+    batch_rhs_rate = rhs / wall
+    line = {"metric": "particle RHS evals/s (aggregate)", "report": "batch", "value": batch_rhs_rate,
+            "unit": "RHS/s", "higher_is_better": True, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "data": "synthetic",
+            "config": {"workload": "%d cubes, edge U[8,40] nm (seed 2), 2 nm pitch, nodes %d..%d (total %d), "
+                                   "81-field +-1 T sweep, alpha 0.1" % (len(sizes), sizes.min(), sizes.max(),
+                                                                         sizes.sum()),
+                       "integrator": "Bogacki-Shampine 3(2), rtol = atol = 1e-6, per particle",
+                       "bem": "FP32 blocks, FP64 row sums", "cg_rtol": 1e-6},
+            "wall_s": wall, "setup_s": setup, "autotune_s": tune,
+            "schedule": {"threads": threads, "budget": budget, "launches_per_graph": args.steps},
+            "node_rhs_per_s": node_rhs / wall, "simulated_ps_per_s_aggregate": sim_ps / wall,
+            "accepted_steps": int((s1["steps"] - s0["steps"]).sum()),
+            "sweep": {"stages_done_total": int(s1["stage"].sum()), "stages_total": 81 * len(sizes),
+                      "particles_done": int(s1["done"].sum())},
+            "one_at_a_time": {"sample_sizes": [int(x) for x in xs], "rhs_s": [float(y) for y in ys],
+                              "rhs_per_s_estimate": len(sizes) / est,
+                              "note": "single handles (FP64 BEM, one launch sequence per RHS), interpolated "
+                                      "over the particle sizes"},
+            "speedup_vs_one_at_a_time": batch_rhs_rate / (len(sizes) / est)}
+    print(json.dumps(line))
+    b.close()
+
+
 def run_ours(args):
     import torch
     rank, world = dist_setup(args.gpus)
@@ -578,7 +694,8 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=2000)
     ap.add_argument("--adj-fd-steps", type=int, default=100)
     ap.add_argument("--adj-dirs", type=int, default=4)
-    ap.add_argument("--report", default=None, choices=["precision", "adjoint"],
+    ap.add_argument("--particles", type=int, default=256)
+    ap.add_argument("--report", default=None, choices=["precision", "adjoint", "batch"],
                     help="precision: H_eff / energy error of the FP32 form against FP64 over --fields random fields")
     ap.add_argument("--fields", type=int, default=1000)
     ap.add_argument("--no-compare", dest="compare", action="store_false",
@@ -592,6 +709,8 @@ def main():
         run_precision_report(args)
     elif args.report == "adjoint":
         run_adjoint_report(args)
+    elif args.report == "batch":
+        run_batch_report(args)
     else:
         run_ours(args)
 
