@@ -48,10 +48,14 @@ MU0 = 4e-7 * np.pi
 H_EXT_MT = (-24.6, 4.3, 0.0)
 
 # DRAM bytes per launch of the BEM product divided by its algorithmic bytes,
-# from one ncu capture on the 8,562-boundary-node profiling film (matrix
-# 586.6 MB > L2; profiles/k_gemv_f64_film_small.txt: 590.04 MB read+written).
-# The traffic grows with the matrix entries, so it scales to the full film.
-NCU_TRAFFIC_RATIO = {("fp64", False): (586.81 + 3.23) / 586.60}
+# from ncu captures on the 8,562-boundary-node profiling film (matrices larger
+# than L2; profiles/k_gemv_f64_film_small.txt: 590.04 MB read+written for
+# 586.6 MB).  The traffic grows with the matrix entries, so it scales to the
+# full film.
+NCU_TRAFFIC_RATIO = {("fp64", False): (586.81 + 3.23) / 586.60,
+                     # k_gemm_df<8>, profiling film, 8 members: 440.75 + 6.60 MB of 440.95 MB algorithmic
+                     # (profiles/k_gemm_df_film_small_ensemble.txt)
+                     ("fp32x2", True): (440.75 + 6.60) / 440.95}
 
 
 def workload(name):
