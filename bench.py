@@ -2,7 +2,8 @@
 
 Default line: the chosen form -- an ensemble of 8 films on the one mesh
 (options n_members = 8), BEM matrix as FP32 + BF16 residual with compensated
-FP32 products (accurate to ~2^-44), FP64 CG -- with
+FP32 products (accurate to ~2^-44), Poisson CG iterating in FP32 with FP64
+residual refinement to the same tolerance -- with
 `value` summed over the members, and beside it (`plain_fp64`) the plain FP64
 single film measured in the same run, their ratio and the chosen form's
 H_eff error against FP64 at the same magnetisation.  `--form fp64
@@ -340,6 +341,9 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
                 "launches": gl, "avg_launch_ms": avg_ms,
                 "algorithmic_bytes_per_launch": bytes_per_launch,
                 "share_of_step": gms / max(dev_ms, 1e-9)}
+        if form == "fp32x2" and B > 1:
+            roof["note"] = ("compute-bound on the FP32 pipe (~11 FP32 ops per member-entry; ncu: FMA pipe 71.5% "
+                            "active, profiles/k_gemm_df_film_small_ensemble.txt); the HBM fraction is shown")
     return {
         "sim": sim, "eng": eng, "value": sim_ns_total / dev_s, "e2e": sim_ns_total / wall_e2e,
         "ms_per_step": dev_s * 1e3 / args.steps, "rhs_evals": st["nfe"] - st0["nfe"],
@@ -691,7 +695,7 @@ def main():
     ap.add_argument("--step-ps", type=float, default=1.0)
     ap.add_argument("--relax-ps", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cg", default="fp64", choices=["fp64", "fp32"],
+    ap.add_argument("--cg", default="fp32", choices=["fp64", "fp32"],
                     help="Poisson CG: FP64, or FP32 iterations with FP64 residual refinement")
     ap.add_argument("--members", type=int, default=8,
                     help="ensemble size: B films on the one mesh integrated together (value summed over members)")

@@ -1026,7 +1026,8 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm_mp(CGArgs a, int nnz_cap, in
       int st = (tid < nm && !(sqrt(rn) <= s_tol[tid])) ? 0 : 1;
       if (!(rn == rn)) st = 2;
       s_out[tid] = st;
-      s_itol[tid] = (double)a.eta * sqrt(rn);   // inner target
+      // inner target: the reduction still needed (with margin), but at least eta
+      s_itol[tid] = fmax(0.5 * s_tol[tid], (double)a.eta * sqrt(rn));
     }
     __syncthreads();
     int open = 0;
@@ -1354,77 +1355,7 @@ __global__ void __launch_bounds__(kGemvThreads) k_gemm_f64(int nb, int ld, long 
   }
 }
 
-template <int MB>
-__global__ void __launch_bounds__(kGemvThreads) k_gemm_f32(int nb, int ld, long long seg, int maxr, int nm,
-                                                            const float *__restrict__ B,
-                                                            const float *__restrict__ x, double *__restrict__ part) {
-  const int lane = threadIdx.x & 31;
-  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const long long Q = ld / 8, total = (long long)nb * Q;
-  const long long q0 = w * seg, q1 = min(total, q0 + seg);
-  if (q0 >= q1) return;
-  const long long rfirst = q0 / Q;
-  for (long long r = rfirst; r * Q < q1; ++r) {
-    const long long a = max(q0, r * Q), e = min(q1, (r + 1) * Q);
-    const float *row = B + r * (long long)ld;
-    double acc[MB];
-#pragma unroll
-    for (int m = 0; m < MB; ++m) acc[m] = 0.0;
-    long long q = a + lane;
-    for (; q + 32 < e; q += 64) {
-      float4 v[2][2];
-#pragma unroll
-      for (int u = 0; u < 2; ++u) {
-        const float4 *p = reinterpret_cast<const float4 *>(row + 8 * (q - r * Q + 32 * u));
-        v[u][0] = __ldcs(p);
-        v[u][1] = __ldcs(p + 1);
-      }
-#pragma unroll
-      for (int m = 0; m < MB; ++m) {
-        if (m >= nm) break;
-        float s0 = 0.f, s1 = 0.f;
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const float4 *px = reinterpret_cast<const float4 *>(x + (size_t)m * ld + 8 * (q - r * Q + 32 * u));
-          const float4 x0 = __ldg(px), x1 = __ldg(px + 1);
-          s0 = fmaf(v[u][0].x, x0.x, s0); s1 = fmaf(v[u][0].y, x0.y, s1);
-          s0 = fmaf(v[u][0].z, x0.z, s0); s1 = fmaf(v[u][0].w, x0.w, s1);
-          s0 = fmaf(v[u][1].x, x1.x, s0); s1 = fmaf(v[u][1].y, x1.y, s1);
-          s0 = fmaf(v[u][1].z, x1.z, s0); s1 = fmaf(v[u][1].w, x1.w, s1);
-        }
-        acc[m] += (double)(s0 + s1);
-      }
-    }
-    for (; q < e; q += 32) {
-      const float4 *p = reinterpret_cast<const float4 *>(row + 8 * (q - r * Q));
-      const float4 v0 = __ldcs(p), v1 = __ldcs(p + 1);
-#pragma unroll
-      for (int m = 0; m < MB; ++m) {
-        if (m >= nm) break;
-        const float4 *px = reinterpret_cast<const float4 *>(x + (size_t)m * ld + 8 * (q - r * Q));
-        const float4 x0 = __ldg(px), x1 = __ldg(px + 1);
-        float s0 = v0.x * x0.x;
-        s0 = fmaf(v0.y, x0.y, s0); s0 = fmaf(v0.z, x0.z, s0); s0 = fmaf(v0.w, x0.w, s0);
-        s0 = fmaf(v1.x, x1.x, s0); s0 = fmaf(v1.y, x1.y, s0); s0 = fmaf(v1.z, x1.z, s0); s0 = fmaf(v1.w, x1.w, s0);
-        acc[m] += (double)s0;
-      }
-    }
-#pragma unroll
-    for (int m = 0; m < MB; ++m) {
-      if (m >= nm) break;
-      const double s = warp_sum(acc[m]);
-      if (lane == 0) part[(w * maxr + (r - rfirst)) * MB + m] = s;
-    }
-  }
-}
-
-// FP32 ensemble product on tiles: block (slab, row block) stages the slab's
-// kTileCols entries of x for every member in shared memory, and each warp
-// streams kTileRpw rows at once, so one shared-memory read of x serves
-// kTileRpw rows.  FP32 sums within the slab, one partial per (slab, row,
-// member) in FP64: part[(slab * nb + row) * MB + m].  A lane's 32 products of
-// a (row, member) are summed in FP32, everything after that in FP64.
-constexpr int kTileCols = 1024, kTileRpw = 4, kTileRows = 64;
+constexpr int kTileRpw = 4;   // rows per warp step of the FP32 ensemble product
 
 // Sum each of NV values over the warp with recursive halving (31 shuffles for
 // NV = 32): afterwards lane L holds the total of value L >> (5 - log2 NV).
@@ -1449,63 +1380,6 @@ __device__ __forceinline__ T warp_transpose_sum(T (&v)[NV]) {
     }
   }
   return v[0];
-}
-
-template <int MB>
-__global__ void __launch_bounds__(256) k_gemm_f32t(int nb, int ld, int nm, const float *__restrict__ B,
-                                                   const float *__restrict__ x, double *__restrict__ part) {
-  __shared__ float4 xs[MB][kTileCols / 4];
-  const int slab = blockIdx.x, c0 = slab * kTileCols;
-  const int ncol = min(kTileCols, ld - c0);   // a multiple of 8 (ld and c0 are)
-  for (int i = threadIdx.x; i < MB * (kTileCols / 4); i += blockDim.x) {
-    const int m = i / (kTileCols / 4), q = i - m * (kTileCols / 4);
-    xs[m][q] = (m < nm && 4 * q < ncol) ? __ldg(reinterpret_cast<const float4 *>(x + (size_t)m * ld + c0) + q)
-                                        : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int units = ncol / 8;
-  const int rend = min(nb, (int)(blockIdx.y + 1) * kTileRows);
-  for (int r0 = blockIdx.y * kTileRows + warp * kTileRpw; r0 < rend; r0 += 8 * kTileRpw) {
-    float acc[kTileRpw * MB];
-#pragma unroll
-    for (int q = 0; q < kTileRpw * MB; ++q) acc[q] = 0.f;
-    const float *rows[kTileRpw];
-#pragma unroll
-    for (int rr = 0; rr < kTileRpw; ++rr) rows[rr] = B + (size_t)min(r0 + rr, nb - 1) * ld + c0;
-    for (int u = lane; u < units; u += 32) {
-      float4 a[kTileRpw][2];
-#pragma unroll
-      for (int rr = 0; rr < kTileRpw; ++rr) {
-        const float4 *p = reinterpret_cast<const float4 *>(rows[rr] + 8 * u);
-        a[rr][0] = __ldcs(p);
-        a[rr][1] = __ldcs(p + 1);
-      }
-#pragma unroll
-      for (int m = 0; m < MB; ++m) {
-        const float4 x0 = xs[m][2 * u], x1 = xs[m][2 * u + 1];
-#pragma unroll
-        for (int rr = 0; rr < kTileRpw; ++rr) {
-          float t = acc[rr * MB + m];
-          t = fmaf(a[rr][0].x, x0.x, t); t = fmaf(a[rr][0].y, x0.y, t);
-          t = fmaf(a[rr][0].z, x0.z, t); t = fmaf(a[rr][0].w, x0.w, t);
-          t = fmaf(a[rr][1].x, x1.x, t); t = fmaf(a[rr][1].y, x1.y, t);
-          t = fmaf(a[rr][1].z, x1.z, t); t = fmaf(a[rr][1].w, x1.w, t);
-          acc[rr * MB + m] = t;
-        }
-      }
-    }
-    constexpr int NV = kTileRpw * MB;
-    constexpr int SH = NV >= 32 ? 0 : (NV >= 16 ? 1 : (NV >= 8 ? 2 : (NV >= 4 ? 3 : (NV >= 2 ? 4 : 5))));
-    double accd[NV];   // lane sums (32 products each in FP32) combined in FP64
-#pragma unroll
-    for (int q = 0; q < NV; ++q) accd[q] = (double)acc[q];
-    const double tot = warp_transpose_sum<double, NV>(accd);
-    const int v = lane >> SH;
-    const int rr = v / MB, m = v - rr * MB;
-    if ((lane & ((1 << SH) - 1)) == 0 && m < nm && r0 + rr < nb)
-      part[((size_t)slab * nb + r0 + rr) * MB + m] = tot;
-  }
 }
 
 // FP32 ensemble product, x held in registers: block (slab group, row block)
@@ -2234,7 +2108,7 @@ int init_workspace(nmg_handle *h, std::string &err) {
   // partials (kChunk members for the ensemble), then FP32 copies of x padded to ld
   part_n *= (B > 1 ? kChunk : 1);
   if (B > 1 && nb > 0)   // FP32 / compensated tiles: one partial per (slab, row, member)
-    part_n = std::max(part_n, (size_t)((M.ld + std::min(kTileCols, kDfCols) - 1) / std::min(kTileCols, kDfCols)) *
+    part_n = std::max(part_n, (size_t)((M.ld + std::min(kRegSlab, kDfCols) - 1) / std::min(kRegSlab, kDfCols)) *
                                   nb * kChunk);
   W.gemv_x32_off = (part_n + 7) / 8 * 8;
   // FP32 x copies: BC members, or BC (xh, xl) pairs for the compensated product
