@@ -83,7 +83,7 @@ struct CGArgs {
 constexpr int kAgg = 64;   // rows per aggregate (4 aggregates per 256-row block)
 
 // ---- single-reduction CG on a counter barrier ----
-constexpr int kCG2MaxRed = 7 * kChunk;   // widest fused reduction (projection dots + b.b per ensemble member)
+constexpr int kCG2MaxRed = 11 * kChunk;   // widest fused reduction (projection dots + b.b per ensemble member)
 
 // gpu-scope acquire load
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
@@ -171,7 +171,7 @@ __device__ __forceinline__ bool reduce_all_to(const CGArgs &a, unsigned epoch, d
 // b.b_j come with the first reduction and also update the Gram matrix; every
 // block solves the small system identically.  With an empty basis the
 // previous solution is the start, like the reference's initial_guess_nonzero.
-constexpr int kBasis = 6;
+constexpr int kBasis = 10;
 constexpr int kCGSlots = 4;   // warm-start bases: 0/1 Neumann/Dirichlet, 2/3 the adjoint solves
 
 struct CGBasis {

@@ -76,6 +76,8 @@ typedef struct om_solver {
   double rtol, atol; int maxits;
 } om_solver;
 
+#define OM_BASIS 10
+
 typedef struct om_state {
   const om_mesh *M;
   om_material mat;
@@ -92,11 +94,10 @@ typedef struct om_state {
   /* initial-guess basis of each solve kind: last OM_BASIS right-hand sides
      and solutions, their Gram matrix, {count, head} */
   double *basis_b[2], *basis_x[2];
-  double gram[2][36];
+  double gram[2][OM_BASIS * OM_BASIS];
   int bcount[2], bhead[2];
 } om_state;
 
-#define OM_BASIS 6
 
 int om_state_init(om_state *S, const om_mesh *M, const om_material *mat, const om_solver *nbc,
                   const om_solver *dbc, int do_demag, int nthreads);

@@ -58,7 +58,7 @@ class OmState(C.Structure):
                 ("last_iters_nbc", C.c_int), ("last_iters_dbc", C.c_int), ("n_rhs", C.c_longlong),
                 ("nthreads", C.c_int),
                 ("basis_b", C.POINTER(C.c_double) * 2), ("basis_x", C.POINTER(C.c_double) * 2),
-                ("gram", (C.c_double * 36) * 2), ("bcount", C.c_int * 2), ("bhead", C.c_int * 2)]
+                ("gram", (C.c_double * 100) * 2), ("bcount", C.c_int * 2), ("bhead", C.c_int * 2)]
 
 
 class OmStats(C.Structure):
