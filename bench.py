@@ -40,6 +40,23 @@ import time
 
 import numpy as np
 
+
+def _pin_rank_device():
+    """Under torchrun each rank sees only its own GPU (set before any CUDA
+    initialisation): the library links the CUDA runtime statically, so its
+    current device does not follow torch.cuda.set_device."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = os.environ.get("LOCAL_RANK")
+    if world > 1 and local is not None and "NMAG_BENCH_PINNED" not in os.environ:
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        devices = [d for d in vis.split(",") if d] if vis else [str(i) for i in range(64)]
+        os.environ["CUDA_VISIBLE_DEVICES"] = devices[int(local) % len(devices)]
+        os.environ["NMAG_BENCH_PINNED"] = "1"
+        os.environ["LOCAL_RANK_DEVICE"] = "0"
+
+
+_pin_rank_device()
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 for _p in (os.path.join(ROOT, "nmag-src_gb300"), os.path.join(ROOT, "oracle")):
     if _p not in sys.path:
@@ -652,9 +669,11 @@ def run_batch_report(args):
 def run_ours(args):
     import torch
     rank, world = dist_setup(args.gpus)
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK_DEVICE", os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(local)
     torch.cuda.init()
+    from nmag import _lib
+    _lib.set_device(local)
     msh, base, seed = workload(args.workload)
     B = args.members
     r = measure(args, args.form, args.cg, B, msh, base, seed, world, local)

@@ -67,6 +67,11 @@ typedef struct nmg_ts_stats {
 /* Library version; replaces nothing (ocaml.version). */
 int nmg_version(void);
 
+/* Select the GPU for the handles this thread creates next (the library keeps
+ * its own CUDA runtime state: the caller's own cudaSetDevice or a framework's
+ * device choice does not carry over).  No counterpart in the reference. */
+int nmg_set_device(int device);
+
 /* Message of the last failing call on this handle (or, when h == NULL, of the
  * last failing nmg_create or handle-less call on this thread). */
 const char *nmg_last_error(const nmg_handle *h);

@@ -33,6 +33,13 @@ extern "C" {
 
 int nmg_version(void) { return NMG_VERSION; }
 
+int nmg_set_device(int device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+    return fail(nullptr, -1, "nmg_set_device: no such CUDA device");
+  return cudaSetDevice(device) == cudaSuccess ? 0 : fail(nullptr, 101, "nmg_set_device: cudaSetDevice failed");
+}
+
 const char *nmg_last_error(const nmg_handle *h) { return h ? h->last_error.c_str() : g_create_error.c_str(); }
 
 int nmg_create(const double *coords, int n_nodes, const int32_t *tets, int n_tets, const nmg_material *mat,

@@ -52,7 +52,7 @@ class TsStats(C.Structure):
 
 
 # every symbol declared in include/nmag_gpu.h
-EXPORTS = ["nmg_version", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_mesh_info", "nmg_get_csr",
+EXPORTS = ["nmg_version", "nmg_set_device", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_mesh_info", "nmg_get_csr",
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
            "nmg_set_material", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
            "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
@@ -87,6 +87,7 @@ def lib(build_if_missing=True):
     L = C.CDLL(_build.LIB)
     vp = C.c_void_p
     L.nmg_version.restype = C.c_int
+    L.nmg_set_device.argtypes = [C.c_int]
     L.nmg_last_error.argtypes = [vp]
     L.nmg_last_error.restype = C.c_char_p
     L.nmg_create.argtypes = [_f64p, C.c_int, _i32p, C.c_int, C.POINTER(Material), C.POINTER(Options), C.POINTER(vp)]
@@ -135,6 +136,12 @@ def lib(build_if_missing=True):
     L.nmg_rk4_adjoint.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
+
+
+def set_device(device):
+    """GPU for the engines created next on this thread (the library's own CUDA
+    runtime does not follow torch.cuda.set_device)."""
+    check(lib().nmg_set_device(int(device)), None, "set_device")
 
 
 def check(rc, handle=None, what="call"):
