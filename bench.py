@@ -67,13 +67,23 @@ H_EXT_MT = (-24.6, 4.3, 0.0)
 
 # DRAM bytes per launch of the BEM product divided by its algorithmic bytes,
 # from ncu captures on the 8,562-boundary-node profiling film (matrices larger
-# than L2; profiles/k_gemv_f64_film_small.txt: 590.04 MB read+written for
+# than L2; profiles/k_gemv_f64_film_small.txt: 590.63 MB read+written for
 # 586.6 MB).  The traffic grows with the matrix entries, so it scales to the
 # full film.
-NCU_TRAFFIC_RATIO = {("fp64", False): (586.81 + 3.23) / 586.60,
+NCU_TRAFFIC_RATIO = {("fp64", False): (587.56 + 3.07) / 586.60,
+                     # k_gemv_df, profiling film, one film: 441.09 + 2.80 MB of 439.98 MB algorithmic
+                     # (profiles/k_gemv_df_film_small.txt)
+                     ("fp32x2", False): (441.09 + 2.80) / 439.98,
                      # k_gemm_df<8>, profiling film, 8 members: 440.75 + 6.60 MB of 440.95 MB algorithmic
                      # (profiles/k_gemm_df_film_small_ensemble.txt)
                      ("fp32x2", True): (440.75 + 6.60) / 440.95}
+# the same figures keyed by kernel (the anchored product reports whichever of
+# its two kernels dominates)
+NCU_TRAFFIC_RATIO[("k_gemv_df", False)] = NCU_TRAFFIC_RATIO[("fp32x2", False)]
+NCU_TRAFFIC_RATIO[("k_gemm_df", True)] = NCU_TRAFFIC_RATIO[("fp32x2", True)]
+# k_gemm_f32r<8> (anchored difference product), profiling film, 8 members: 293.80 + 3.54 MB of
+# 294.30 MB algorithmic (profiles/k_gemm_f32r_film_small_ensemble.txt)
+NCU_TRAFFIC_RATIO[("k_gemm_f32r", True)] = (293.80 + 3.54) / 294.30
 
 
 def workload(name):
@@ -261,19 +271,20 @@ def config_dict(args, msh):
             "relax": "alpha=1, H_ext=0 for %.3g ps before the timed dynamics (untimed)" % args.relax_ps,
             "nodes": int(msh.n_nodes), "tets": int(msh.n_tets), "step": "%.3g ps advance + <m> read" % args.step_ps,
             "form": args.form, "cg": args.cg, "members": args.members,
+            "bem_anchor": args.anchor if args.form == "fp32x2" else 0.0,
             "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
             "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % {"fp64": 8, "fp32": 4,
                                                                                   "fp32x2": 6}[args.form]}
 
 
-def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True):
+def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True, anchor=0.0):
     """One form on the workload: untimed setup and relax, W warm-up steps,
     then K timed steps on the device-resident engine (CUDA-event time on the
     library's stream) and K more through nmag.Simulation (e2e)."""
     import torch
     import nmag
     from nmag import SI
-    sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B)
+    sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor)
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     if B > 1:   # member b starts from the workload's initial state with seed + b
@@ -295,6 +306,7 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
     for _ in range(args.warmup):
         t += ps
         eng.ts_advance(t)
+    m_start = eng.get_m()
     # ---- timed region: device-resident value leg ----
     sampler = ClockSampler(local) if sample_clocks else None
     if sampler:
@@ -302,6 +314,7 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
     eng.profile(True)
     launches0 = eng.launch_count()
     cg0 = eng.cg_iterations()
+    anc0 = eng.bem_anchor_stats()
     _, st0 = eng.ts_advance(t)   # no-op advance to read the counters
     torch.cuda.synchronize()
     barrier(world)
@@ -318,6 +331,7 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
     barrier(world)
     launches = eng.launch_count() - launches0
     cg1 = eng.cg_iterations()
+    anc1 = eng.bem_anchor_stats()
     eng.profile(False)
     prof = eng.profile_read()
     clocks = sampler.stop() if sampler else None
@@ -362,6 +376,37 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
         if form == "fp32x2" and B > 1:
             roof["note"] = ("compute-bound on the FP32 pipe (~11 FP32 ops per member-entry; ncu: FMA pipe 71.5% "
                             "active, profiles/k_gemm_df_film_small_ensemble.txt); the HBM fraction is shown")
+    anchored = None
+    if anchor > 0:
+        # two gated kernels per chunk product: the compensated one runs on a
+        # refresh, the FP32 difference product otherwise (the other exits at
+        # once; its launch time stays in the totals)
+        n_prod, n_ref = anc1[0] - anc0[0], anc1[1] - anc0[1]
+        dl, dms = prof["bem_anchor_delta"]
+        bytes32 = nb * nb * 4 + 2 * nm * nb * 8
+        hbm, peak_kind = peaks()
+        legs = {}
+        for name, kname, execd, tot_ms, nbytes in (
+                ("refresh", "k_gemm_df" if B > 1 else "k_gemv_df", n_ref, gms, bytes_per_launch),
+                ("difference", "k_gemm_f32r" if B > 1 else "k_gemv_f32", n_prod - n_ref, dms, bytes32)):
+            ach = execd * nbytes / (tot_ms * 1e-3) / 1e9 if execd > 0 and tot_ms > 0 else None
+            legs[name] = {"kernel": kname, "executed": int(execd), "total_ms": tot_ms,
+                          "algorithmic_bytes_per_launch": nbytes,
+                          "avg_launch_ms": tot_ms / execd if execd > 0 else None,
+                          "achieved": ach, "frac": ach / hbm if ach else None}
+        anchored = {"tol": anchor, "products": int(n_prod), "refreshes": int(n_ref), "legs": legs}
+        dom = max(legs.values(), key=lambda v: v["total_ms"])
+        if dom["achieved"]:
+            roof = {"bound": "hbm" if dom["kernel"] in ("k_gemm_f32r", "k_gemv_f32") else "hbm (FP32 pipe)",
+                    "kernel": dom["kernel"], "achieved": dom["achieved"], "peak": hbm, "unit": "GB/s",
+                    "frac": dom["frac"], "peak_kind": peak_kind,
+                    "traffic": (NCU_TRAFFIC_RATIO[(dom["kernel"], B > 1)] * dom["algorithmic_bytes_per_launch"] / 1e9
+                                if (dom["kernel"], B > 1) in NCU_TRAFFIC_RATIO else None),
+                    "traffic_unit": "GB per launch (ncu dram__bytes_read+write, scaled from the profiling capture)",
+                    "launches": dom["executed"], "avg_launch_ms": dom["avg_launch_ms"],
+                    "algorithmic_bytes_per_launch": dom["algorithmic_bytes_per_launch"],
+                    "share_of_step": dom["total_ms"] / max(dev_ms, 1e-9),
+                    "note": "anchored product: the dominant of its two kernels; both in 'anchored'"}
     return {
         "sim": sim, "eng": eng, "value": sim_ns_total / dev_s, "e2e": sim_ns_total / wall_e2e,
         "ms_per_step": dev_s * 1e3 / args.steps, "rhs_evals": st["nfe"] - st0["nfe"],
@@ -370,6 +415,7 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
         "kernels_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
         "cg_iterations": {"neumann": cg1[0] - cg0[0], "dirichlet": cg1[1] - cg0[1]},
         "relax_wall_s": relax_wall, "d2h": B * msh.n_nodes * 3 * 8 + 24,
+        "anchored": anchored, "m_start": m_start,
     }
 
 
@@ -395,6 +441,47 @@ def heff_error(args, chosen, msh):
         sim.engine.close()
     ref = out["fp64"]
     return float(np.abs(out[args.form] - ref).max() / np.abs(ref).max())
+
+
+def anchor_path_error(args, chosen, msh, points=48):
+    """H_eff error of the anchored product along the run's own trajectory:
+    for every member the magnetisation moves from its state before the timed
+    steps to its final state through `points` normalised linear blends, the
+    anchored form evaluating each blend with its anchor carried along (so
+    most products are FP32 differences from an earlier blend, refreshed when
+    the drift passes tol).  Against the FP64 form at the same blends; both
+    sides converge their Poisson solves to 1e-12.  Returns the max over
+    blends and members of max |H - H_fp64| / max |H_fp64| and the anchor's
+    product / refresh counts over the walk."""
+    import nmag
+    from nmag import SI
+    B = args.members
+    ma = np.asarray(chosen["m_start"]).reshape(B, -1, 3) if B > 1 else np.asarray(chosen["m_start"])[None]
+    mb = np.asarray(chosen["eng"].get_m()).reshape(B, -1, 3) if B > 1 else np.asarray(chosen["eng"].get_m())[None]
+    tight = {"NBC.rtol": 1e-12, "DBC.rtol": 1e-12, "NBC.maxits": 20000, "DBC.maxits": 20000}
+    sims = {}
+    for key, form, anc in (("anchored", args.form, args.anchor), ("fp64", "fp64", 0.0)):
+        sim = nmag.Simulation("err", bem_precision=form, ksp_tolerances=tight, n_members=B, bem_anchor=anc)
+        sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
+        shape = (B, sim.engine.N, 3) if B > 1 else (sim.engine.N, 3)
+        sim.engine.set_h_ext(np.broadcast_to(h_ext_su(), shape))
+        sims[key] = (sim, shape)
+    worst = 0.0
+    for k in range(points + 1):
+        s = k / points
+        m = (1.0 - s) * ma + s * mb
+        m /= np.linalg.norm(m, axis=-1, keepdims=True)
+        H = {}
+        for key, (sim, shape) in sims.items():
+            sim.engine.set_m(m.reshape(shape))
+            H[key] = np.asarray(sim.engine.eval_fields()["H_total"]).reshape(B, -1, 3)
+        for b in range(B):
+            ref = H["fp64"][b]
+            worst = max(worst, float(np.abs(H["anchored"][b] - ref).max() / np.abs(ref).max()))
+    prod, ref_n = sims["anchored"][0].engine.bem_anchor_stats()
+    for sim, _ in sims.values():
+        sim.engine.close()
+    return worst, prod, ref_n
 
 
 def run_precision_report(args):
@@ -676,7 +763,8 @@ def run_ours(args):
     _lib.set_device(local)
     msh, base, seed = workload(args.workload)
     B = args.members
-    r = measure(args, args.form, args.cg, B, msh, base, seed, world, local)
+    anchor = args.anchor if args.form == "fp32x2" else 0.0
+    r = measure(args, args.form, args.cg, B, msh, base, seed, world, local, anchor=anchor)
     plain = None
     if args.compare and not (args.form == "fp64" and args.cg == "fp64" and B == 1):
         plain = measure(args, "fp64", "fp64", 1, msh, base, seed, world, local, sample_clocks=False)
@@ -686,7 +774,9 @@ def run_ours(args):
         "metric": "simulated ns/wall-s", "value": r["value"], "unit": "ns/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "fp32": "f32 matrix, f64 sums",
-                  "fp32x2": "f32+bf16 matrix, compensated f32 products (~2^-44)"}[args.form],
+                  "fp32x2": "f32+bf16 matrix, compensated f32 products (~2^-44)" + (
+                      "; anchored: f32 products of the drift from the last compensated product"
+                      if anchor > 0 else "")}[args.form],
         "data": "synthetic",
         "config": config_dict(args, msh),
         "rhs_evals_per_s": r["rhs_evals_per_s"], "bdf_steps": r["bdf_steps"], "rhs_evals": r["rhs_evals"],
@@ -700,6 +790,8 @@ def run_ours(args):
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
     }
+    if r["anchored"] is not None:
+        line["anchored"] = r["anchored"]
     if plain is not None:
         line["plain_fp64"] = {"value": plain["value"], "e2e": plain["e2e"], "ms_per_step": plain["ms_per_step"],
                               "rhs_evals_per_s": plain["rhs_evals_per_s"], "bdf_steps": plain["bdf_steps"],
@@ -710,6 +802,11 @@ def run_ours(args):
         # member 0 starts from the plain run's state and both advanced the same time
         a0 = np.asarray(r["eng"].member_averages(0) if B > 1 else r["eng"].averages())
         line["avg_m_diff_vs_plain_fp64"] = float(np.abs(a0 - np.asarray(plain["eng"].averages())).max())
+    if anchor > 0:
+        err, prod, nref = anchor_path_error(args, r, msh)
+        line["anchored"]["path_error"] = {"heff_rel_err_vs_fp64": err, "products": prod, "refreshes": nref,
+                                          "blends": 49}
+        line["heff_rel_err_vs_fp64"] = max(line.get("heff_rel_err_vs_fp64", 0.0), err)
     if world == 1 and not args.no_cpu_baseline:
         cr = cpu_reference_run(args, msh, base, seed, steps=2, warmup=0, max_wall=20.0, sample_ps=0.5 * args.step_ps)
         line["cpu_baseline"] = {"value": (cr["sim_ps"] * 1e-3) / cr["wall_s"], "unit": "ns/s", "cores": cr["cores"],
@@ -735,6 +832,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cg", default="fp32", choices=["fp64", "fp32"],
                     help="Poisson CG: FP64, or FP32 iterations with FP64 residual refinement")
+    ap.add_argument("--anchor", type=float, default=3e-3,
+                    help="fp32x2: anchored product tolerance (B x = B x0 + B32 (x - x0) while the max-norm drift "
+                         "of x from x0 stays below it; 0 = off)")
     ap.add_argument("--members", type=int, default=8,
                     help="ensemble size: B films on the one mesh integrated together (value summed over members)")
     ap.add_argument("--adj-steps", type=int, default=2000)

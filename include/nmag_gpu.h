@@ -53,7 +53,12 @@ typedef struct nmg_options {
   int cg_precision;                      /* 0: FP64 CG; reserved                       */
   int cg_no_coarse;                      /* 1: Jacobi only (no two-level Neumann CG)   */
   int n_members;                         /* ensemble size B (0 or 1: one simulation)   */
-  int reserved[4];
+  double bem_anchor_tol;                 /* bem_precision 2 only; > 0: anchored product
+                                            y = B x0 + B32 (x - x0) while
+                                            max|x - x0| <= tol max|x| per member, a new
+                                            compensated anchor otherwise; 0: off
+                                            (finite, >= 0)                             */
+  int reserved[2];
 } nmg_options;
 
 /* Integrator statistics (CVODE counters; nsim.ml:354-387 timings). */
@@ -259,7 +264,8 @@ int nmg_get_timings(const nmg_handle *h, double out[8]);
  * TSTART/TSTOP timers of nsim.ml:3414-3455).  While profiling is enabled,
  * CUDA events bracket every launch of the hot kernels on the handle's stream:
  * kernel 0 = BEM matrix-vector product, 1 = Neumann CG, 2 = Dirichlet CG,
- * 3 = fused H_eff + LLG node kernel, 4 = Jacobian-vector + preconditioner.
+ * 3 = fused H_eff + LLG node kernel, 4 = Jacobian-vector + preconditioner,
+ * 5 = FP32 difference product of the anchored BEM product (bem_anchor_tol).
  * nmg_profile(h, 1) clears and starts, nmg_profile(h, 0) stops;
  * nmg_profile_read returns launches and summed device milliseconds.
  * nmg_launch_count returns the number of kernels this handle has launched. */
@@ -269,6 +275,10 @@ int64_t nmg_launch_count(const nmg_handle *h);
 /* Total CG iterations since nmg_create: [Neumann, Dirichlet] (the reference
  * reports KSP iteration counts through PETSc logging, nsim.ml:2462-2478). */
 int nmg_cg_iterations(const nmg_handle *h, int64_t total[2]);
+/* Anchored BEM product counters since nmg_create: [products, anchor refreshes
+ * (compensated products)]; zeros when bem_anchor_tol is off.  No counterpart
+ * in the reference. */
+int nmg_bem_anchor_stats(const nmg_handle *h, int64_t out[2]);
 
 /* max over nodes of |m_i - m_prev_i| for device arrays d_m, d_m_prev (3 x
  * n_nodes doubles each), written to the host double *out -- the reduction of

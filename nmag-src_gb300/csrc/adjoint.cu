@@ -587,8 +587,17 @@ int set_element_params(nmg_handle *h, const double *wK, const double *wD, const 
   return 0;
 }
 
+// The anchored BEM product makes an RHS depend on earlier products; the tape
+// runs recompute segments bit for bit, so they suspend it.
+struct AnchorHold {
+  nmg_handle *h;
+  explicit AnchorHold(nmg_handle *hh) : h(hh) { ++h->anchor_hold; }
+  ~AnchorHold() { --h->anchor_hold; }
+};
+
 int rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ckpt, const double *d_pulses,
                 int npulses, int spp, double *d_mT, double *d_hist) {
+  AnchorHold hold(h);
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   cudaStream_t s = h->stream;
@@ -656,6 +665,7 @@ int rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ck
 
 int rk4_adjoint(nmg_handle *h, const double *d_mT_bar, const double *d_hist_bar, double *d_m0_bar, double *d_gwK,
                 double *d_gwD, double *d_gkap, double *d_gpul) {
+  AnchorHold hold(h);
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   cudaStream_t s = h->stream;

@@ -56,6 +56,10 @@ int nmg_create(const double *coords, int n_nodes, const int32_t *tets, int n_tet
   if (mat->Ms == 0.0) return fail(nullptr, -5, "nmg_create: Ms must be non-zero");
   if (opt && (opt->n_members < 0 || opt->n_members > nmg::kMaxMembers))
     return fail(nullptr, -6, "nmg_create: n_members must be in [0, " + std::to_string(nmg::kMaxMembers) + "]");
+  if (opt && !(opt->bem_anchor_tol >= 0.0 && opt->bem_anchor_tol <= 1e300))
+    return fail(nullptr, -6, "nmg_create: bem_anchor_tol must be finite and non-negative");
+  if (opt && opt->bem_anchor_tol > 0.0 && opt->bem_precision != 2)
+    return fail(nullptr, -6, "nmg_create: bem_anchor_tol applies to the compensated product (bem_precision 2)");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(nullptr, 101, "nmg_create: no CUDA device");
   nmg_handle *h = new nmg_handle();
@@ -357,6 +361,15 @@ int nmg_profile_read(nmg_handle *h, int kernel, int64_t *launches, double *total
 }
 
 int64_t nmg_launch_count(const nmg_handle *h) { return h ? h->launches : -1; }
+
+int nmg_bem_anchor_stats(const nmg_handle *h, int64_t out[2]) {
+  if (!h || !out) return -1;
+  long long c[2] = {0, 0};
+  if (h->ws.anc_count.p && d2h(h, c, h->ws.anc_count.p, sizeof(c))) return 100;
+  out[0] = c[0];
+  out[1] = c[1];
+  return 0;
+}
 
 int nmg_cg_iterations(const nmg_handle *h, int64_t total[2]) {
   if (!h || !total) return -1;

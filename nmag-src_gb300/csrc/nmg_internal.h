@@ -91,13 +91,20 @@ struct Workspace {
   long long gemv_seg[2] = {1, 1};
   int gemv_maxr[2] = {1, 1};
   size_t gemv_x32_off = 0;   // offset (doubles) of the padded FP32 x inside bpart
+  // anchored compensated product: per member the anchor x0 and y0 = B x0
+  // (member-major like b1 / b2); per chunk [flag, valid]; drift maxima;
+  // counters [products, refreshes]
+  DevBuf<double> anc_x, anc_y;
+  DevBuf<unsigned long long> anc_mx;
+  DevBuf<int> anc_flag;
+  DevBuf<long long> anc_count;
 };
 
 struct Integrator;
 
 // CUDA-event brackets around hot-kernel launches (resolved after the run).
 struct Profiler {
-  static constexpr int kKernels = 5;
+  static constexpr int kKernels = 6;
   static constexpr int kMaxPairs = 8192;
   bool enabled = false;
   std::vector<cudaEvent_t> pool;   // 2 * kMaxPairs events, created lazily
@@ -143,6 +150,10 @@ struct nmg_handle {
   int nrep = 1;                 // ensemble members B (member-major vectors: member b at b * 3N / b * N)
   nmg::ElemParams ep;
   nmg::Tape *tape = nullptr;
+  int anchor_hold = 0;          // >0: anchored BEM product suspended (RK4 tape runs recompute bit for bit)
+  bool anchored() const {
+    return opt.bem_anchor_tol > 0.0 && opt.bem_precision == 2 && mesh.bem16lo.p && !anchor_hold;
+  }
   const double *exch_K() const { return ep.active ? ep.Kx.p : mesh.K.p; }
 };
 

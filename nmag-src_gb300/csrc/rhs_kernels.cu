@@ -33,6 +33,42 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// Sum each of NV values over the warp with recursive halving (31 shuffles for
+// NV = 32): afterwards lane L holds the total of value L >> (5 - log2 NV).
+template <typename T, int NV>
+__device__ __forceinline__ T warp_transpose_sum(T (&v)[NV]) {
+  const int lane = threadIdx.x & 31;
+  int n = NV;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    if (n > 1) {
+      const bool up = (lane & o) != 0;
+#pragma unroll
+      for (int i = 0; i < NV / 2; ++i) {
+        if (i >= n / 2) break;
+        const T send = up ? v[i] : v[i + n / 2];
+        const T keep = up ? v[i + n / 2] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+      n >>= 1;
+    } else {
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+    }
+  }
+  return v[0];
+}
+
+// Shape of a block reduction of NV values: transpose groups of Q values
+// (a power of two, at most 32), G groups; lane L ends with value L >> SH of
+// each group.
+template <int NV>
+struct RedShape {
+  static constexpr int Q = NV > 16 ? 32 : (NV > 8 ? 16 : (NV > 4 ? 8 : (NV > 2 ? 4 : (NV > 1 ? 2 : 1))));
+  static constexpr int G = (NV + Q - 1) / Q;
+  static constexpr int SH = Q == 32 ? 0 : (Q == 16 ? 1 : (Q == 8 ? 2 : (Q == 4 ? 3 : (Q == 2 ? 4 : 5))));
+  static constexpr int W = G * Q;   // per-warp stride of the scratch
+};
+
 // Block-wide sum of NV values in a fixed order; result valid in thread 0.
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double *smem) {
@@ -51,6 +87,61 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *smem) {
       v[j] = s;
     }
   }
+  __syncthreads();
+}
+
+// Block sum of NV values per thread in a fixed order, the totals written as
+// double to out[0..NV) by threads 0..NV-1 (out may be global).  Each warp
+// reduces its lanes with transpose sums (one shuffle-add per value per
+// stage at the widest, against five for a butterfly per value), then
+// thread j adds value j over the warps.  smem: (kCGThreads/32) x W values.
+template <typename T, int NV>
+__device__ __forceinline__ void block_reduce_out(const T (&v)[NV], T *smem, double *out) {
+  using S = RedShape<NV>;
+  constexpr int NW = kCGThreads / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int g = 0; g < S::G; ++g) {
+    T w[S::Q];
+#pragma unroll
+    for (int i = 0; i < S::Q; ++i) w[i] = (g * S::Q + i < NV) ? v[g * S::Q + i] : T(0);
+    const T t = warp_transpose_sum<T, S::Q>(w);
+    const int j = g * S::Q + (lane >> S::SH);
+    if ((lane & ((1 << S::SH) - 1)) == 0 && j < NV) smem[wid * S::W + j] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    T t = T(0);
+#pragma unroll
+    for (int w = 0; w < NW; ++w) t += smem[w * S::W + threadIdx.x];
+    out[threadIdx.x] = (double)t;
+  }
+}
+
+// res[j] = sum over the grid's blocks of slot[b * stride + j], j < NV, in a
+// fixed order, identical in every block: warp w takes the values j = w,
+// w + 8, ...; its lanes take blocks lane, lane + 32, ... (all of a lane's
+// loads issued together), then one transpose sum per warp.  res: shared.
+template <int NV>
+__device__ __forceinline__ void grid_total(const double *slot, int stride, double *res) {
+  constexpr int NW = kCGThreads / 32;
+  constexpr int JV = (NV + NW - 1) / NW;
+  using S = RedShape<JV>;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double t[S::Q];
+#pragma unroll
+  for (int q = 0; q < S::Q; ++q) t[q] = 0.0;
+#pragma unroll 4
+  for (unsigned b = lane; b < gridDim.x; b += 32) {
+#pragma unroll
+    for (int q = 0; q < JV; ++q) {
+      const int j = wid + q * NW;
+      if (j < NV) t[q] += __ldcg(slot + (size_t)b * stride + j);
+    }
+  }
+  const double tot = warp_transpose_sum<double, S::Q>(t);
+  const int q = lane >> S::SH, j = wid + q * NW;
+  if ((lane & ((1 << S::SH) - 1)) == 0 && q < JV && j < NV) res[j] = tot;
   __syncthreads();
 }
 
@@ -112,28 +203,18 @@ __device__ __forceinline__ bool arrive_wait(const CGArgs &a, unsigned epoch) {
 
 // Reduction fused with the counter barrier: partials double-buffered by
 // epoch parity; after the barrier every block sums all partials in block
-// order (deterministic, identical in every block).
+// order (deterministic, identical in every block).  smem: block_reduce_out
+// scratch ((kCGThreads/32) x RedShape<NV>::W doubles) followed by NV totals.
 template <int NV>
 __device__ __forceinline__ bool reduce_all(const CGArgs &a, unsigned epoch, double (&v)[NV], double *smem,
                                            double (&out)[NV]) {
-  block_sum<NV>(v, smem);
   double *slot = a.red + (size_t)(epoch & 1) * gridDim.x * kCG2MaxRed;
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int j = 0; j < NV; ++j) slot[blockIdx.x * kCG2MaxRed + j] = v[j];
+  block_reduce_out<double, NV>(v, smem, slot + (size_t)blockIdx.x * kCG2MaxRed);
   if (!arrive_wait(a, epoch)) return false;
-  {
-    // value j is summed by warp j % (warps per block): the values proceed in parallel
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int j = wid; j < NV; j += nw) {
-      double s = 0.0;
-      for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(slot + b * kCG2MaxRed + j);
-      s = warp_sum(s);
-      if (lane == 0) smem[j] = s;
-    }
-  }
-  __syncthreads();
-  for (int j = 0; j < NV; ++j) out[j] = smem[j];
+  double *res = smem + (kCGThreads / 32) * RedShape<NV>::W;
+  grid_total<NV>(slot, kCG2MaxRed, res);
+#pragma unroll
+  for (int j = 0; j < NV; ++j) out[j] = res[j];
   __syncthreads();
   return true;
 }
@@ -143,20 +224,10 @@ __device__ __forceinline__ bool reduce_all(const CGArgs &a, unsigned epoch, doub
 template <int NV>
 __device__ __forceinline__ bool reduce_all_to(const CGArgs &a, unsigned epoch, double (&v)[NV], double *smem,
                                               double *res) {
-  block_sum<NV>(v, smem);
   double *slot = a.red + (size_t)(epoch & 1) * gridDim.x * kCG2MaxRed;
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int j = 0; j < NV; ++j) slot[blockIdx.x * kCG2MaxRed + j] = v[j];
+  block_reduce_out<double, NV>(v, smem, slot + (size_t)blockIdx.x * kCG2MaxRed);
   if (!arrive_wait(a, epoch)) return false;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j = wid; j < NV; j += nw) {
-    double s = 0.0;
-    for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(slot + b * kCG2MaxRed + j);
-    s = warp_sum(s);
-    if (lane == 0) res[j] = s;
-  }
-  __syncthreads();
+  grid_total<NV>(slot, kCG2MaxRed, res);
   return true;
 }
 
@@ -180,41 +251,71 @@ struct CGBasis {
   int *ring;       // {count, head}
 };
 
-// Least squares for c: (G + eps diag G) c = v via Cholesky; directions whose
-// pivot collapses (nearly dependent right-hand sides) get c = 0.
-__device__ void small_solve(int n, const double *G, const double *v, double *c) {
-  double L[kBasis][kBasis], y[kBasis];
-  bool on[kBasis];
-  for (int i = 0; i < n; ++i) {
-    on[i] = true;
-    for (int j = 0; j <= i; ++j) {
-      double s = G[i * kBasis + j];
-      if (i == j) s *= 1.0 + 1e-12;
-      for (int k = 0; k < j; ++k) if (on[k]) s -= L[i][k] * L[j][k];
-      if (i == j) {
-        if (!(s > 1e-14 * G[i * kBasis + i]) || !on[i]) { on[i] = false; L[i][i] = 1.0; }
-        else L[i][i] = sqrt(s);
-      } else {
-        L[i][j] = on[j] ? s / L[j][j] : 0.0;
-      }
+// Least squares for c: (G + eps diag G) c = v, one warp (every lane calls;
+// lane i < n owns row i of L): LDL^T factorisation, column by column, with
+// the rows of a column in parallel lanes; a direction whose pivot collapses
+// (nearly dependent right-hand sides) gets c = 0.  Each pivot's reciprocal
+// is formed once and the substitutions multiply: the dependent chain is n
+// reciprocals instead of ~n^2/2 FP64 divisions in one thread.  sD: kBasis
+// doubles of shared scratch for this warp (the pivots); c (shared or
+// global) receives c[0..n) from lanes 0..n-1.
+__device__ void small_solve_warp(int n, const double *G, const double *v, double *c, double *sD) {
+  const int lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
+  double L[kBasis];   // row `lane` of the unit lower factor
+  double rd = 0.0;    // 1 / D_lane (0: dropped direction)
+  unsigned on = 0u;
+#pragma unroll
+  for (int j = 0; j < kBasis; ++j) L[j] = 0.0;
+#pragma unroll
+  for (int j = 0; j < kBasis; ++j) {
+    if (j >= n) break;
+    double s = lane < n ? G[lane * kBasis + j] : 0.0;
+    if (lane == j) s *= 1.0 + 1e-12;
+#pragma unroll
+    for (int k = 0; k < kBasis; ++k) {
+      if (k >= j) break;
+      const double ljk = __shfl_sync(full, L[k], j);
+      if ((on >> k) & 1u) s -= (L[k] * sD[k]) * ljk;
     }
-    if (!on[i]) for (int j = 0; j < i; ++j) L[i][j] = 0.0;
+    const double sjj = __shfl_sync(full, s, j);
+    const bool keep = sjj > 1e-14 * G[j * kBasis + j];
+    const double r = keep ? 1.0 / sjj : 0.0;
+    __syncwarp();
+    if (lane == 0) sD[j] = keep ? sjj : 1.0;
+    __syncwarp();
+    if (keep) on |= 1u << j;
+    if (lane == j) rd = r;
+    if (lane > j) L[j] = s * r;
   }
-  for (int i = 0; i < n; ++i) {
-    double s = v[i];
-    for (int k = 0; k < i; ++k) s -= L[i][k] * y[k];
-    y[i] = on[i] ? s / L[i][i] : 0.0;
+  // L z = v, y = z / D
+  double z = lane < n ? v[lane] : 0.0;
+#pragma unroll
+  for (int k = 0; k < kBasis; ++k) {
+    if (k >= n) break;
+    const double zk = __shfl_sync(full, z, k);
+    if (lane > k && ((on >> k) & 1u)) z -= L[k] * zk;
   }
-  for (int i = n - 1; i >= 0; --i) {
-    double s = y[i];
-    for (int k = i + 1; k < n; ++k) s -= L[k][i] * c[k];
-    c[i] = on[i] ? s / L[i][i] : 0.0;
+  double ci = z * rd;
+  // L^T c = y, descending: lane i takes L_ki from lane k's row
+#pragma unroll
+  for (int k = kBasis - 1; k >= 0; --k) {
+    if (k >= n) continue;
+    if (lane == k && !((on >> k) & 1u)) ci = 0.0;
+    const double ck = __shfl_sync(full, ci, k);
+#pragma unroll
+    for (int i = 0; i < kBasis; ++i) {
+      if (i >= k) break;
+      const double lki = __shfl_sync(full, L[i], k);
+      if (lane == i) ci -= lki * ck;
+    }
   }
+  if (lane < n) c[lane] = ((on >> lane) & 1u) ? ci : 0.0;
 }
 
-__global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBasis B) {
+__global__ void __launch_bounds__(kCGThreads, 4) k_cg3(CGArgs a, int nnz_cap, CGBasis B) {
   extern __shared__ double dyn[];
-  __shared__ double smem[32 * (kBasis + 1)];
+  __shared__ double smem[kCGThreads / 32 * RedShape<kBasis + 1>::W + kBasis + 1];   // reduce_all scratch + totals
   __shared__ double sc[kBasis + 4];
   __shared__ double sagg[2 * (kCGThreads / kAgg)], sec[kCGThreads / kAgg];
   double *sK = dyn;
@@ -297,23 +398,25 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBas
   // ---- projection of b onto the stored right-hand sides ----
   const int count = B.ring[0], head = B.ring[1];
   double proj[kBasis + 1], bdot[kBasis + 1];
+#pragma unroll
   for (int j = 0; j <= kBasis; ++j) proj[j] = 0.0;
   if (active) {
-    for (int j = 0; j < count; ++j) proj[j] = bi * B.b[(size_t)j * a.N + r];
+#pragma unroll
+    for (int j = 0; j < kBasis; ++j) if (j < count) proj[j] = bi * __ldcg(B.b + (size_t)j * a.N + r);
     proj[kBasis] = bi * bi;
   }
   if (!reduce_all<kBasis + 1>(a, ++epoch, proj, smem, bdot)) return;
   const double tol = fmax(a.rtol * sqrt(bdot[kBasis]), a.atol);
   if (count > 0) {
-    if (threadIdx.x == 0) {
-      double c[kBasis];
-      small_solve(count, B.gram, bdot, c);
-      for (int j = 0; j < count; ++j) sc[j] = c[j];
-    }
+    if (threadIdx.x < 32) small_solve_warp(count, B.gram, bdot, sc, smem);   // reduce scratch is free here
     __syncthreads();
     if (active) {
       double g = 0.0;
-      for (int j = 0; j < count; ++j) g += sc[j] * B.x[(size_t)j * a.N + r];
+      double t[kBasis];   // every load in flight before the sum (same order as a plain loop)
+#pragma unroll
+      for (int j = 0; j < kBasis; ++j) t[j] = j < count ? __ldcg(B.x + (size_t)j * a.N + r) : 0.0;
+#pragma unroll
+      for (int j = 0; j < kBasis; ++j) if (j < count) g += sc[j] * t[j];
       xi = ident ? bi : g;   // identity (Dirichlet boundary) rows are exact
     }
   }
@@ -399,11 +502,11 @@ __global__ void __launch_bounds__(kCGThreads) k_cg3(CGArgs a, int nnz_cap, CGBas
 // the loop ends when all members have stopped.  Member m's scalar work runs
 // on lane 0 of warp m, so the members' FP64 divisions proceed in parallel.
 template <int MB>
-__global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int nm, CGBasis B) {
+__global__ void __launch_bounds__(kCGThreads, 1) k_cgm(CGArgs a, int nnz_cap, int nm, CGBasis B) {
   static_assert(MB * 32 <= kCGThreads, "one warp per member for the scalar work");
   constexpr int P = kBasis + 1;
   extern __shared__ double dyn[];
-  __shared__ double smem[kCGThreads / 32 * P * MB];   // block_sum scratch
+  __shared__ double smem[kCGThreads / 32 * RedShape<P * MB>::W];   // block_reduce_out scratch
   __shared__ double sres[P * MB];                     // totals of the last reduction
   __shared__ double sbdot[P * MB];                    // projection dots (Gram update at the end)
   __shared__ double s_al[MB], s_be[MB], s_ga[MB], s_tol[MB];
@@ -568,14 +671,8 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
   if (tid < MB) s_tol[tid] = fmax(a.rtol * sqrt(sbdot[P * tid + kBasis]), a.atol);
   {
     const int m = tid >> 5;
-    if ((tid & 31) == 0 && m < nm) {
-      const int cnt = s_cnt[m];
-      if (cnt > 0) {
-        double c[kBasis];
-        small_solve(cnt, B.gram + m * kBasis * kBasis, sbdot + P * m, c);
-        for (int j = 0; j < cnt; ++j) scoef[m * kBasis + j] = c[j];
-      }
-    }
+    if (m < nm && s_cnt[m] > 0)   // warp m: member m's coefficients
+      small_solve_warp(s_cnt[m], B.gram + m * kBasis * kBasis, sbdot + P * m, scoef + m * kBasis, smem + m * kBasis);
   }
   __syncthreads();
   if (active) {
@@ -586,7 +683,11 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
       if (cnt == 0) continue;
       const double *bx = B.x + (size_t)m * kBasis * N;
       double g = 0.0;
-      for (int j = 0; j < cnt; ++j) g += scoef[m * kBasis + j] * bx[(size_t)j * N + r];
+      double t[kBasis];   // every load in flight before the sum (same order as a plain loop)
+#pragma unroll
+      for (int j = 0; j < kBasis; ++j) t[j] = j < cnt ? __ldcg(bx + (size_t)j * N + r) : 0.0;
+#pragma unroll
+      for (int j = 0; j < kBasis; ++j) if (j < cnt) g += scoef[m * kBasis + j] * t[j];
       xi[m] = ident ? sbi[m][tid] : g;
     }
 #pragma unroll
@@ -709,47 +810,15 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm(CGArgs a, int nnz_cap, int n
   }
 }
 
-// Block-wide FP32 sums of NV values (result in thread 0) for the inner CG.
-template <int NV>
-__device__ __forceinline__ void block_sum_f(float (&v)[NV], float *smem) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int j = 0; j < NV; ++j) {
-    float s = v[j];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) smem[wid * NV + j] = s;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int j = 0; j < NV; ++j) {
-      float s = 0.f;
-      for (int w = 0; w < nw; ++w) s += smem[w * NV + j];
-      v[j] = s;
-    }
-  }
-  __syncthreads();
-}
-
-// Cross-block total of NV FP32 block sums, accumulated in FP64 (res, shared).
+// Cross-block total of NV FP32 values: block sums in FP32, accumulated over
+// the blocks in FP64 (res, shared).
 template <int NV>
 __device__ __forceinline__ bool reduce_all_f(const CGArgs &a, unsigned epoch, float (&v)[NV], float *smemf,
                                              double *res) {
-  block_sum_f<NV>(v, smemf);
   double *slot = a.red + (size_t)(epoch & 1) * gridDim.x * kCG2MaxRed;
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int j = 0; j < NV; ++j) slot[blockIdx.x * kCG2MaxRed + j] = (double)v[j];
+  block_reduce_out<float, NV>(v, smemf, slot + (size_t)blockIdx.x * kCG2MaxRed);
   if (!arrive_wait(a, epoch)) return false;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int j = wid; j < NV; j += nw) {
-    double s = 0.0;
-    for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(slot + b * kCG2MaxRed + j);
-    s = warp_sum(s);
-    if (lane == 0) res[j] = s;
-  }
-  __syncthreads();
+  grid_total<NV>(slot, kCG2MaxRed, res);
   return true;
 }
 
@@ -762,12 +831,12 @@ __device__ __forceinline__ bool reduce_all_f(const CGArgs &a, unsigned epoch, fl
 // GB300's FP32 pipe is ~60x its FP64 pipe: the inner iterations, where all
 // the work is, run on it.
 template <int MB>
-__global__ void __launch_bounds__(kCGThreads) k_cgm_mp(CGArgs a, int nnz_cap, int nm, CGBasis B) {
+__global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap, int nm, CGBasis B) {
   static_assert(MB * 32 <= kCGThreads && MB % 2 == 0, "one warp per member; member pairs");
   constexpr int P = kBasis + 1;
   extern __shared__ double dyn[];
-  __shared__ double smem[kCGThreads / 32 * P * MB];
-  __shared__ float smemf[kCGThreads / 32 * 3 * MB];
+  __shared__ double smem[kCGThreads / 32 * RedShape<P * MB>::W];
+  __shared__ float smemf[kCGThreads / 32 * RedShape<3 * MB>::W];
   __shared__ double sres[P * MB];
   __shared__ double sbdot[P * MB];
   __shared__ double s_al[MB], s_be[MB], s_ga[MB], s_tol[MB], s_itol[MB];
@@ -978,14 +1047,8 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm_mp(CGArgs a, int nnz_cap, in
   if (tid < MB) s_tol[tid] = fmax(a.rtol * sqrt(sbdot[P * tid + kBasis]), a.atol);
   {
     const int m = tid >> 5;
-    if ((tid & 31) == 0 && m < nm) {
-      const int cnt = s_cnt[m];
-      if (cnt > 0) {
-        double c[kBasis];
-        small_solve(cnt, B.gram + m * kBasis * kBasis, sbdot + P * m, c);
-        for (int j = 0; j < cnt; ++j) scoef[m * kBasis + j] = c[j];
-      }
-    }
+    if (m < nm && s_cnt[m] > 0)   // warp m: member m's coefficients
+      small_solve_warp(s_cnt[m], B.gram + m * kBasis * kBasis, sbdot + P * m, scoef + m * kBasis, smem + m * kBasis);
   }
   __syncthreads();
   if (active) {
@@ -996,7 +1059,11 @@ __global__ void __launch_bounds__(kCGThreads) k_cgm_mp(CGArgs a, int nnz_cap, in
       if (cnt == 0) continue;
       const double *bx = B.x + (size_t)m * kBasis * N;
       double g = 0.0;
-      for (int j = 0; j < cnt; ++j) g += scoef[m * kBasis + j] * bx[(size_t)j * N + r];
+      double t[kBasis];   // every load in flight before the sum (same order as a plain loop)
+#pragma unroll
+      for (int j = 0; j < kBasis; ++j) t[j] = j < cnt ? __ldcg(bx + (size_t)j * N + r) : 0.0;
+#pragma unroll
+      for (int j = 0; j < kBasis; ++j) if (j < cnt) g += scoef[m * kBasis + j] * t[j];
       xi[m] = ident ? sbi[m][tid] : g;
     }
   }
@@ -1245,7 +1312,9 @@ __global__ void __launch_bounds__(kGemvThreads) k_gemv_f64(int nb, int ld, long 
 // group of a lane, groups summed in FP64.
 __global__ void __launch_bounds__(kGemvThreads) k_gemv_f32(int nb, int ld, long long seg, int maxr,
                                                             const float *__restrict__ B,
-                                                            const float *__restrict__ x, double *__restrict__ part) {
+                                                            const float *__restrict__ x, double *__restrict__ part,
+                                                            const int *__restrict__ gate = nullptr) {
+  if (gate && *gate) return;   // anchored product: this chunk refreshes its anchor instead
   const int lane = threadIdx.x & 31;
   const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long Q = ld / 8, total = (long long)nb * Q;
@@ -1357,30 +1426,6 @@ __global__ void __launch_bounds__(kGemvThreads) k_gemm_f64(int nb, int ld, long 
 
 constexpr int kTileRpw = 4;   // rows per warp step of the FP32 ensemble product
 
-// Sum each of NV values over the warp with recursive halving (31 shuffles for
-// NV = 32): afterwards lane L holds the total of value L >> (5 - log2 NV).
-template <typename T, int NV>
-__device__ __forceinline__ T warp_transpose_sum(T (&v)[NV]) {
-  const int lane = threadIdx.x & 31;
-  int n = NV;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    if (n > 1) {
-      const bool up = (lane & o) != 0;
-#pragma unroll
-      for (int i = 0; i < NV / 2; ++i) {
-        if (i >= n / 2) break;
-        const T send = up ? v[i] : v[i + n / 2];
-        const T keep = up ? v[i + n / 2] : v[i];
-        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-      }
-      n >>= 1;
-    } else {
-      v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
-    }
-  }
-  return v[0];
-}
 
 // FP32 ensemble product, x held in registers: block (slab group, row block)
 // covers kRegSlab columns with its 8 warps, warp w owning 256 columns and
@@ -1394,7 +1439,9 @@ constexpr int kRegSlab = 2048, kRegRows = 64;   // 32 KB of shared sums at MB = 
 
 template <int MB>
 __global__ void __launch_bounds__(256, 2) k_gemm_f32r(int nb, int ld, int nm, const float *__restrict__ B,
-                                                      const float *__restrict__ x, double *__restrict__ part) {
+                                                      const float *__restrict__ x, double *__restrict__ part,
+                                                      const int *__restrict__ gate = nullptr) {
+  if (gate && *gate) return;   // anchored product: this chunk refreshes its anchor instead
   constexpr int NV = kTileRpw * MB;
   constexpr int SH = NV >= 32 ? 0 : (NV >= 16 ? 1 : (NV >= 8 ? 2 : 3));
   constexpr int STEPS = kRegRows / kTileRpw;
@@ -1522,9 +1569,9 @@ __device__ __forceinline__ float bf16hi(unsigned w) { return __uint_as_float(w &
 
 // x (nm members, member m at m * n) -> FP32 pairs xh + xl, zero-padded to ld.
 __global__ void k_split_x(int n, int ld, int nm, const double *__restrict__ x, float *__restrict__ xh,
-                          float *__restrict__ xl) {
+                          float *__restrict__ xl, const int *__restrict__ gate = nullptr) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ld * nm) return;
+  if (g >= ld * nm || (gate && !*gate)) return;
   const int m = g / ld, i = g - m * ld;
   const double v = i < n ? x[(size_t)m * n + i] : 0.0;
   const float h = (float)v;
@@ -1537,7 +1584,9 @@ __global__ void __launch_bounds__(kGemvThreads) k_gemv_df(int nb, int ld, long l
                                                            const float *__restrict__ Bh,
                                                            const uint16_t *__restrict__ Bl,
                                                            const float *__restrict__ xh,
-                                                           const float *__restrict__ xl, double *__restrict__ part) {
+                                                           const float *__restrict__ xl, double *__restrict__ part,
+                                                           const int *__restrict__ gate = nullptr) {
+  if (gate && !*gate) return;   // anchored product: the FP32 difference product runs instead
   const int lane = threadIdx.x & 31;
   const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long Q = ld / 8, total = (long long)nb * Q;
@@ -1579,7 +1628,9 @@ constexpr int kDfCols = 512, kDfRows = 64, kDfRpw = 2;
 template <int MB>
 __global__ void __launch_bounds__(256) k_gemm_df(int nb, int ld, int nm, const float *__restrict__ Bh,
                                                  const uint16_t *__restrict__ Bl, const float *__restrict__ xh,
-                                                 const float *__restrict__ xl, double *__restrict__ part) {
+                                                 const float *__restrict__ xl, double *__restrict__ part,
+                                                 const int *__restrict__ gate = nullptr) {
+  if (gate && !*gate) return;   // anchored product: the FP32 difference product runs instead
   __shared__ float4 sh[MB][kDfCols / 4], sl[MB][kDfCols / 4];
   const int slab = blockIdx.x, c0 = slab * kDfCols;
   const int ncol = min(kDfCols, ld - c0);   // a multiple of 8
@@ -1641,6 +1692,103 @@ __global__ void k_row_sum_m(int nb, long long Q, long long seg, int maxr, long l
   double s = 0.0;
   for (long long w = w0; w <= w1; ++w) s += part[(w * maxr + (r - (w * seg) / Q)) * MB + m];
   y[(size_t)m * nb + r] = s;
+}
+
+// ---- anchored BEM product (compensated form) ----
+// y = B x is formed as y0 + B32 (x - x0), where (x0, y0 = B x0) is the chunk's
+// last compensated product (the anchor) and B32 the FP32 part of the matrix.
+// The FP32 product's rounding error is ~2^-24 |B| |x - x0| instead of
+// 2^-24 |B| |x|, so while x stays within tol of x0 (max norm, per member) the
+// result keeps (tol x the FP32 error), and the matrix is read at 4 B per entry
+// on an HBM-bound kernel instead of 6 B on an FP32-pipe-bound one.  Every
+// product is computed from its own x; the anchor is a second solution of the
+// same linear map that the difference is added to.
+//
+// k_anchor_drift: d = FP32(x - x0) zero-padded to ld (the FP32 kernels' x
+// layout) and per-member maxima of |x - x0| and |x| (bit patterns of
+// non-negative doubles order like the values; NaN orders above +inf).
+__global__ void k_anchor_drift(int n, int ld, int nm, const double *__restrict__ x, const double *__restrict__ x0,
+                               float *__restrict__ d, unsigned long long *__restrict__ mx) {
+  __shared__ unsigned long long smx[2 * kChunk];
+  if (threadIdx.x < 2 * kChunk) smx[threadIdx.x] = 0ull;
+  __syncthreads();
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < ld * nm) {
+    const int m = g / ld, i = g - m * ld;
+    float dv = 0.f;
+    if (i < n) {
+      const double v = x[(size_t)m * n + i], e = v - x0[(size_t)m * n + i];
+      dv = (float)e;
+      atomicMax(&smx[m], (unsigned long long)__double_as_longlong(fabs(e)));
+      atomicMax(&smx[kChunk + m], (unsigned long long)__double_as_longlong(fabs(v)));
+    }
+    d[g] = dv;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * kChunk && smx[threadIdx.x]) atomicMax(&mx[threadIdx.x], smx[threadIdx.x]);
+}
+
+// One thread: refresh (flag = 1) when the chunk has no anchor yet or a
+// member drifted past tol; clears the maxima for the next chunk and counts
+// products / refreshes.
+__global__ void k_anchor_decide(int nm, double tol, unsigned long long *__restrict__ mx, const int *__restrict__ valid,
+                                int *__restrict__ flag, long long *__restrict__ count) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int refresh = *valid ? 0 : 1;
+  for (int m = 0; m < nm; ++m) {
+    const double dm = __longlong_as_double((long long)mx[m]), xm = __longlong_as_double((long long)mx[kChunk + m]);
+    if (!(dm <= tol * xm)) refresh = 1;
+  }
+  for (int k = 0; k < 2 * kChunk; ++k) mx[k] = 0ull;
+  *flag = refresh;
+  count[0] += 1;
+  count[1] += refresh;
+}
+
+// Ensemble epilogue: sum the slab partials of whichever product ran (the
+// compensated one has nslab_df slabs, the FP32 one nslab_32), then either
+// store the new anchor or add the difference product to the old one.
+__global__ void k_anchor_slab_sum(int nb, int nslab_df, int nslab_32, int nm, int MB, const double *__restrict__ part,
+                                  const int *__restrict__ flag, int *__restrict__ valid, const double *__restrict__ x,
+                                  double *__restrict__ x0, double *__restrict__ y0, double *__restrict__ y) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int refresh = *flag;
+  if (g == 0 && refresh) *valid = 1;
+  if (g >= nb * nm) return;
+  const int m = g / nb, r = g - m * nb;
+  const int nslab = refresh ? nslab_df : nslab_32;
+  double s = 0.0;
+  for (int sl = 0; sl < nslab; ++sl) s += part[((size_t)sl * nb + r) * MB + m];
+  const size_t o = (size_t)m * nb + r;
+  if (refresh) {
+    y0[o] = s;
+    x0[o] = x[o];
+    y[o] = s;
+  } else {
+    y[o] = y0[o] + s;
+  }
+}
+
+// One simulation: k_row_sum over the shared segment partials (the compensated
+// and FP32 single products use the same decomposition), then the anchor step.
+__global__ void k_anchor_row_sum(int nb, long long Q, long long seg, int maxr, long long nwarps,
+                                 const double *__restrict__ part, const int *__restrict__ flag,
+                                 int *__restrict__ valid, const double *__restrict__ x, double *__restrict__ x0,
+                                 double *__restrict__ y0, double *__restrict__ y) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int refresh = *flag;
+  if (r == 0 && refresh) *valid = 1;
+  if (r >= nb) return;
+  const long long w0 = (r * Q) / seg, w1 = min(nwarps - 1, ((r + 1) * Q - 1) / seg);
+  double s = 0.0;
+  for (long long w = w0; w <= w1; ++w) s += part[w * maxr + (r - (w * seg) / Q)];
+  if (refresh) {
+    y0[r] = s;
+    x0[r] = x[r];
+    y[r] = s;
+  } else {
+    y[r] = y0[r] + s;
+  }
 }
 
 // Dirichlet right-hand side (op_load_DBC, sign folded): interior rows
@@ -2131,6 +2279,17 @@ int init_workspace(nmg_handle *h, std::string &err) {
   }
   cudaMemsetAsync(W.basis_ring.p, 0, sizeof(int) * 2 * kCGSlots, h->stream);
   NMG_CUDA_TRY(W.cg_tot.alloc(2 * 4), "alloc");
+  if (h->opt.bem_anchor_tol > 0.0 && h->opt.bem_precision == 2 && nb > 0) {
+    const int nchunk = (B + kChunk - 1) / kChunk;
+    NMG_CUDA_TRY(W.anc_x.alloc((size_t)nb * B), "alloc BEM anchor");
+    NMG_CUDA_TRY(W.anc_y.alloc((size_t)nb * B), "alloc BEM anchor");
+    NMG_CUDA_TRY(W.anc_mx.alloc(2 * kChunk), "alloc");
+    NMG_CUDA_TRY(W.anc_flag.alloc(2 * (size_t)nchunk), "alloc");
+    NMG_CUDA_TRY(W.anc_count.alloc(2), "alloc");
+    cudaMemsetAsync(W.anc_mx.p, 0, sizeof(unsigned long long) * 2 * kChunk, h->stream);
+    cudaMemsetAsync(W.anc_flag.p, 0, sizeof(int) * 2 * nchunk, h->stream);
+    cudaMemsetAsync(W.anc_count.p, 0, sizeof(long long) * 2, h->stream);
+  }
   NMG_CUDA_TRY(W.iters.alloc(4), "alloc");
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * 2, h->stream);
   cudaMemsetAsync(W.iters.p, 0, sizeof(int) * 4, h->stream);
@@ -2147,6 +2306,33 @@ void bem_gemv(nmg_handle *h, const double *x, double *y) {
   const int f = (h->opt.bem_precision >= 1 && M.bem32.p) ? 1 : 0;
   const long long seg = W.gemv_seg[f];
   const int maxr = W.gemv_maxr[f];
+  if (h->anchored() && W.anc_x.p) {   // anchored compensated product (one simulation)
+    float *xh = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
+    float *xl = xh + M.ld;
+    int *flag = W.anc_flag.p, *valid = W.anc_flag.p + 1;
+    k_anchor_drift<<<nblk(M.ld, 256), 256, 0, h->stream>>>(nb, M.ld, 1, x, W.anc_x, xh, W.anc_mx); ++h->launches;
+    k_anchor_decide<<<1, 32, 0, h->stream>>>(1, h->opt.bem_anchor_tol, W.anc_mx, valid, flag, W.anc_count);
+    ++h->launches;
+    k_split_x<<<nblk(M.ld, 256), 256, 0, h->stream>>>(nb, M.ld, 1, x, xh, xl, flag); ++h->launches;
+    {
+      NMG_PROF_BEGIN(h, 0);
+      k_gemv_df<<<W.gemv_blocks, kGemvThreads, 0, h->stream>>>(nb, M.ld, seg, maxr, M.bem32, M.bem16lo, xh, xl,
+                                                               W.bpart, flag);
+      ++h->launches;
+      NMG_PROF_END(h);
+    }
+    {
+      NMG_PROF_BEGIN(h, 5);
+      k_gemv_f32<<<W.gemv_blocks, kGemvThreads, 0, h->stream>>>(nb, M.ld, seg, maxr, M.bem32, xh, W.bpart, flag);
+      ++h->launches;
+      NMG_PROF_END(h);
+    }
+    k_anchor_row_sum<<<nblk(nb, 256), 256, 0, h->stream>>>(nb, (long long)(M.ld / 8), seg, maxr,
+                                                           (long long)W.gemv_blocks * (kGemvThreads / 32), W.bpart,
+                                                           flag, valid, x, W.anc_x, W.anc_y, y);
+    ++h->launches;
+    return;
+  }
   if (f == 1 && M.bem16lo.p) {   // compensated FP32 pair product
     float *xh = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
     float *xl = xh + M.ld;
@@ -2185,6 +2371,41 @@ void bem_gemm(nmg_handle *h, const double *x, double *y) {
     const int nm = std::min(kChunk, B - c0);
     const int MB = nm <= 2 ? 2 : (nm <= 4 ? 4 : 8);
     const double *xc = x + (size_t)c0 * nb;
+    if (h->anchored() && W.anc_x.p) {   // anchored compensated product for this chunk
+      float *xh = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
+      float *xl = xh + (size_t)nm * M.ld;
+      int *flag = W.anc_flag.p + 2 * (c0 / kChunk), *valid = flag + 1;
+      double *ax = W.anc_x.p + (size_t)c0 * nb, *ay = W.anc_y.p + (size_t)c0 * nb;
+      k_anchor_drift<<<nblk((long long)M.ld * nm, 256), 256, 0, h->stream>>>(nb, M.ld, nm, xc, ax, xh, W.anc_mx);
+      ++h->launches;
+      k_anchor_decide<<<1, 32, 0, h->stream>>>(nm, h->opt.bem_anchor_tol, W.anc_mx, valid, flag, W.anc_count);
+      ++h->launches;
+      k_split_x<<<nblk((long long)M.ld * nm, 256), 256, 0, h->stream>>>(nb, M.ld, nm, xc, xh, xl, flag);
+      ++h->launches;
+      const int nslab_df = (M.ld + kDfCols - 1) / kDfCols, nslab_32 = (M.ld + kRegSlab - 1) / kRegSlab;
+      {
+        dim3 grid(nslab_df, (nb + kDfRows - 1) / kDfRows);
+        NMG_PROF_BEGIN(h, 0);
+        if (MB == 2) k_gemm_df<2><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, M.bem16lo, xh, xl, W.bpart, flag);
+        else if (MB == 4) k_gemm_df<4><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, M.bem16lo, xh, xl, W.bpart, flag);
+        else k_gemm_df<8><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, M.bem16lo, xh, xl, W.bpart, flag);
+        NMG_PROF_END(h);
+        ++h->launches;
+      }
+      {
+        dim3 grid(nslab_32, (nb + kRegRows - 1) / kRegRows);
+        NMG_PROF_BEGIN(h, 5);
+        if (MB == 2) k_gemm_f32r<2><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, xh, W.bpart, flag);
+        else if (MB == 4) k_gemm_f32r<4><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, xh, W.bpart, flag);
+        else k_gemm_f32r<8><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, xh, W.bpart, flag);
+        NMG_PROF_END(h);
+        ++h->launches;
+      }
+      k_anchor_slab_sum<<<nblk((long long)nb * nm, 256), 256, 0, h->stream>>>(
+          nb, nslab_df, nslab_32, nm, MB, W.bpart, flag, valid, xc, ax, ay, y + (size_t)c0 * nb);
+      ++h->launches;
+      continue;
+    }
     if (f == 1 && M.bem16lo.p) {   // compensated FP32 pair product on tiles
       float *xh = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
       float *xl = xh + (size_t)nm * M.ld;

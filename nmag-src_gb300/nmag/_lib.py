@@ -26,7 +26,8 @@ class Options(C.Structure):
     _fields_ = [("do_demag", C.c_int), ("nbc_rtol", C.c_double), ("nbc_atol", C.c_double), ("nbc_maxits", C.c_int),
                 ("dbc_rtol", C.c_double), ("dbc_atol", C.c_double), ("dbc_maxits", C.c_int),
                 ("bem_precision", C.c_int), ("cg_precision", C.c_int), ("cg_no_coarse", C.c_int),
-                ("n_members", C.c_int), ("reserved", C.c_int * 4)]
+                ("n_members", C.c_int), ("bem_anchor_tol", C.c_double),
+                ("reserved", C.c_int * 2)]
 
 
 class Particle(C.Structure):
@@ -56,13 +57,13 @@ EXPORTS = ["nmg_version", "nmg_set_device", "nmg_last_error", "nmg_create", "nmg
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
            "nmg_set_material", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
            "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
-           "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_max_dm_static",
+           "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_bem_anchor_stats", "nmg_max_dm_static",
            "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
            "nmg_member_averages", "nmg_batch_last_error", "nmg_batch_create", "nmg_batch_destroy", "nmg_batch_info",
            "nmg_batch_set_m", "nmg_batch_get_m", "nmg_batch_eval", "nmg_batch_run", "nmg_batch_state",
            "nmg_batch_set_schedule", "nmg_batch_autotune"]
 
-PROFILED_KERNELS = ["bem_gemv", "cg_neumann", "cg_dirichlet", "heff_llg", "jv_psolve"]
+PROFILED_KERNELS = ["bem_gemv", "cg_neumann", "cg_dirichlet", "heff_llg", "jv_psolve", "bem_anchor_delta"]
 
 _lib = None
 
@@ -116,6 +117,7 @@ def lib(build_if_missing=True):
     L.nmg_launch_count.argtypes = [vp]
     L.nmg_launch_count.restype = C.c_int64
     L.nmg_cg_iterations.argtypes = [vp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]
+    L.nmg_bem_anchor_stats.argtypes = [vp, np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")]
     L.nmg_max_dm_static.argtypes = [vp, vp, C.c_int, C.POINTER(C.c_double)]
     L.nmg_member_averages.argtypes = [vp, C.c_int, _f64p, vp]
     L.nmg_batch_last_error.argtypes = [vp]
@@ -267,6 +269,12 @@ class Engine(object):
     def cg_iterations(self):
         out = np.zeros(2, np.int64)
         check(lib().nmg_cg_iterations(self.h, out), self.h, "cg_iterations")
+        return int(out[0]), int(out[1])
+
+    def bem_anchor_stats(self):
+        """(BEM products, anchor refreshes) of the anchored compensated product."""
+        out = np.zeros(2, np.int64)
+        check(lib().nmg_bem_anchor_stats(self.h, out), self.h, "bem_anchor_stats")
         return int(out[0]), int(out[1])
 
     # ---- inspection (parity tests) ----

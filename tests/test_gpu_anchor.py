@@ -1,0 +1,101 @@
+"""Anchored compensated BEM product (bem_anchor_tol): B x is formed as
+B x0 + B32 (x - x0) from the last compensated product (x0, B x0) while x
+stays within tol of x0 (max norm, per member).  Checked against the FP64
+form at the same magnetisation, with the anchor's refresh decisions read
+back from the library's counters."""
+import numpy as np
+import pytest
+
+from conftest import permalloy, seeded_m
+from test_gpu_ensemble import make_ensemble
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.mark.parametrize("B", [1, 3, 10])
+def test_anchor_refresh_decisions_and_accuracy(cube, B):
+    mat = permalloy(0.5)
+    anc, _ = make_ensemble(cube, mat, B, bem_precision=2, anchor=0.02)
+    ref, _ = make_ensemble(cube, mat, B, bem_precision=0)
+    N = len(cube.points)
+    shape = (B, N, 3) if B > 1 else (N, 3)
+    ms = np.stack([seeded_m(N, base=(1.0, 0.2 * b, -0.3), seed=300 + b, noise=0.5) for b in range(B)]).reshape(shape)
+    hs = np.broadcast_to([0.02, -0.01, 0.005], shape).copy()
+    for e in (anc, ref):
+        e.set_h_ext(hs)
+    chunks = (B + 7) // 8
+    rng = np.random.default_rng(7)
+
+    def step(m):
+        anc.set_m(m)
+        ref.set_m(m)
+        return anc.eval_fields(), ref.eval_fields()
+
+    # 1: no anchor yet -> every chunk refreshes (compensated product)
+    f, g = step(ms)
+    assert anc.bem_anchor_stats() == (chunks, chunks)
+    assert _rel(f["H_demag"], g["H_demag"]) <= 1e-9
+    # 2: a small move (drift well inside tol) -> the FP32 difference product
+    m2 = ms + 2e-4 * rng.standard_normal(ms.shape)
+    m2 /= np.linalg.norm(m2, axis=-1, keepdims=True)
+    f, g = step(m2)
+    assert anc.bem_anchor_stats() == (2 * chunks, chunks)
+    assert _rel(f["H_demag"], g["H_demag"]) <= 1e-9
+    assert _rel(f["H_total"], g["H_total"]) <= 1e-9
+    # 3: a large move (a new magnetisation) -> refresh again
+    m3 = np.stack([seeded_m(N, base=(-0.4, 1.0, 0.1 * b), seed=400 + b, noise=0.5) for b in range(B)]).reshape(shape)
+    f, g = step(m3)
+    assert anc.bem_anchor_stats() == (3 * chunks, 2 * chunks)
+    assert _rel(f["H_demag"], g["H_demag"]) <= 1e-9
+    anc.close()
+    ref.close()
+
+
+def test_anchor_difference_algebra(cube):
+    """A huge tol: after the first product every product is anchored however
+    far x moves, so the result carries the FP32 product error of the full
+    difference x - x0 (here about twice |x|), bounded like the FP32 form's."""
+    mat = permalloy(0.5)
+    B = 2
+    anc, _ = make_ensemble(cube, mat, B, bem_precision=2, anchor=1e6)
+    ref, _ = make_ensemble(cube, mat, B, bem_precision=0)
+    N = len(cube.points)
+    ma = np.stack([seeded_m(N, base=(1.0, 0.0, 0.0), seed=500 + b, noise=0.3) for b in range(B)])
+    mb = np.stack([seeded_m(N, base=(0.0, 1.0, 0.5), seed=600 + b, noise=0.3) for b in range(B)])
+    hs = np.zeros((B, N, 3))
+    for e in (anc, ref):
+        e.set_h_ext(hs)
+    anc.set_m(ma)
+    anc.eval_fields()
+    anc.set_m(mb)
+    ref.set_m(mb)
+    f, g = anc.eval_fields(), ref.eval_fields()
+    assert anc.bem_anchor_stats() == (2, 1)
+    assert _rel(f["H_demag"], g["H_demag"]) <= 5e-6   # the FP32 form's bound on this mesh, x2
+    anc.close()
+    ref.close()
+
+
+def test_anchor_suspended_on_rk4_tape(cube):
+    """The RK4 tape recomputes segments bit for bit, so its runs bypass the
+    anchor: the counters do not move and two runs agree exactly."""
+    from test_gpu_adjoint import _params, _run
+    mat = permalloy(0.5)
+    eng, _ = make_ensemble(cube, mat, 1, bem_precision=2, anchor=0.02)
+    c = mat.coefficients("nmag")
+    N, T = len(cube.points), len(cube.simplices)
+    eng.set_h_ext(np.zeros(3))
+    m0 = seeded_m(N, seed=11)
+    Ms_T, K1_T, pulses = _params(T, 2)
+    a = _run(eng, c, m0, Ms_T, K1_T, pulses, 6, 2, 3)
+    b = _run(eng, c, m0, Ms_T, K1_T, pulses, 6, 2, 3)
+    assert eng.bem_anchor_stats() == (0, 0)
+    assert a[0] == b[0]
+    for x, y in zip(a[1:], b[1:]):
+        assert np.array_equal(x, y)
+    eng.clear_element_params()
+    eng.close()
