@@ -404,6 +404,13 @@ inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
 }  // namespace
 
+namespace {
+__global__ void k_recip(int n, const double *__restrict__ a, double *__restrict__ b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = 1.0 / a[i];
+}
+}  // namespace
+
 int build_mesh(nmg_handle *h, const double *coords, const int32_t *tets, std::string &err) {
   Mesh &M = h->mesh;
   cudaStream_t s = h->stream;
@@ -465,6 +472,8 @@ int build_mesh(nmg_handle *h, const double *coords, const int32_t *tets, std::st
   NMG_CUDA_TRY(M.vol.alloc(N), "alloc vol");
   k_values<<<nblk(N, 128), 128, 0, s>>>(N, nnz, M.tets, M.nt_ptr, M.nt_idx, M.dL, M.adet, M.nbr, M.row_ptr,
                                         M.col_idx, M.K, M.G, M.D, M.vol);
+  NMG_CUDA_TRY(M.ivol.alloc(N), "alloc");
+  k_recip<<<nblk(N, 256), 256, 0, s>>>(N, M.vol, M.ivol);
 
   // surface triangles
   DevBuf<int32_t> tcnt, toff;

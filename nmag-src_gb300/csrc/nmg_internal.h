@@ -56,6 +56,7 @@ struct TriGeo {
 struct Mesh {
   int N = 0, T = 0, nnz = 0, nb = 0, ntri = 0, nouter = 0;
   DevBuf<double> coords, dL, adet, K, G, D, vol, tri_normal, solid_angle;
+  DevBuf<double> ivol;   // 1 / vol (the node kernels multiply instead of dividing)
   DevBuf<int32_t> tets, nt_ptr, nt_idx, nbr, row_ptr, col_idx, diag_pos, b_of_node, node_of_b, tri;
   DevBuf<double> bem;      // FP64 BEM, row-major with padded row stride ld (bem[k*ld + c] = B[k][c])
   DevBuf<float> bem32;     // FP32 copy (precision forms 1, 2), same layout
@@ -78,7 +79,7 @@ struct Workspace {
   DevBuf<int> ens_basis_ring;
   DevBuf<int32_t> perm, prow, pcol, pbnd;     // CG solver ordering (spatially binned nodes)
   DevBuf<double> pK, xperm, ainv, rc;         // K in that order, iterate, coarse inverse, coarse residual
-  DevBuf<float> ainv32, rc32, z32;            // FP32 copies / vectors of the mixed-precision CG
+  DevBuf<float> ainv32, rc32, z32, rw32;      // FP32 copies / vectors of the mixed-precision CG
   int cg_smem_mp = 0;                         // dynamic shared memory of the mixed-precision CG
   int nc = 0;                                 // aggregates of the two-level Neumann CG (0: none)
   int cg_blocks = 0;

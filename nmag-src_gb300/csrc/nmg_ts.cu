@@ -36,7 +36,7 @@ constexpr int MSBP = 20;
 constexpr double SPILS_DGMAX = 0.2, SPILS_DELT = 0.05;
 constexpr int SPILS_MSBPRE = 50;
 constexpr double UROUND = 2.220446049250313e-16;
-constexpr int kRedBlocks = 120;
+constexpr int kRedBlocks = 304;   // two blocks per SM: enough loads in flight for HBM
 
 inline int nblk(long long n, int t) { return (int)((n + t - 1) / t); }
 
@@ -55,34 +55,62 @@ __global__ void k_scale(int n, double a, double *__restrict__ x) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) x[i] *= a;
 }
-__global__ void k_ewt(int n, double rtol, double atol, const double *__restrict__ y, double *__restrict__ w) {
+// error weights w = 1 / (rtol |y| + atol), and their reciprocals ws (the
+// tolerance scale) so that dividing by a weight is a multiplication
+__global__ void k_ewt(int n, double rtol, double atol, const double *__restrict__ y, double *__restrict__ w,
+                      double *__restrict__ ws) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) w[i] = 1.0 / (rtol * fabs(y[i]) + atol);
+  if (i >= n) return;
+  const double sc = rtol * fabs(y[i]) + atol;
+  w[i] = 1.0 / sc;
+  ws[i] = sc;
 }
 struct ZnPtrs { double *z[QMAXB + 2]; };
 // Nordsieck prediction z <- z * Pascal (sign = +1) or its inverse (sign = -1).
-__global__ void k_predict(int n, int q, ZnPtrs zn, int sign) {
+// (The order q is a template parameter: with compile-time indices the
+// history pointers and values stay in registers.)
+template <int Q>
+__global__ void k_predict(int n, ZnPtrs zn, int sign) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double v[QMAXB + 2];
-  for (int j = 0; j <= q; ++j) v[j] = zn.z[j][i];
-  for (int k = 1; k <= q; ++k)
-    for (int j = q; j >= k; --j) v[j - 1] = sign > 0 ? v[j - 1] + v[j] : v[j - 1] - v[j];
-  for (int j = 0; j < q; ++j) zn.z[j][i] = v[j];
+  double v[Q + 1];
+#pragma unroll
+  for (int j = 0; j <= Q; ++j) v[j] = zn.z[j][i];
+#pragma unroll
+  for (int k = 1; k <= Q; ++k)
+#pragma unroll
+    for (int j = Q; j >= k; --j) v[j - 1] = sign > 0 ? v[j - 1] + v[j] : v[j - 1] - v[j];
+#pragma unroll
+  for (int j = 0; j < Q; ++j) zn.z[j][i] = v[j];
 }
-__global__ void k_rescale(int n, int q, ZnPtrs zn, double eta) {
+template <int Q>
+__global__ void k_rescale(int n, ZnPtrs zn, double eta) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double f = eta;
-  for (int j = 1; j <= q; ++j) { zn.z[j][i] *= f; f *= eta; }
+#pragma unroll
+  for (int j = 1; j <= Q; ++j) { zn.z[j][i] *= f; f *= eta; }
 }
 struct Coef { double c[QMAXB + 2]; };
-__global__ void k_complete(int n, int q, ZnPtrs zn, Coef l, const double *__restrict__ acor) {
+template <int Q>
+__global__ void k_complete(int n, ZnPtrs zn, Coef l, const double *__restrict__ acor) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double a = acor[i];
-  for (int j = 0; j <= q; ++j) zn.z[j][i] += l.c[j] * a;
+#pragma unroll
+  for (int j = 0; j <= Q; ++j) zn.z[j][i] += l.c[j] * a;
 }
+// launch K<q>(args...) for the runtime order q in [1, QMAXB]
+#define NMG_LAUNCH_Q(K, q, grid, blk, st, ...)                            \
+  do {                                                                  \
+    switch (q) {                                                        \
+      case 1: K<1><<<grid, blk, 0, st>>>(__VA_ARGS__); break;           \
+      case 2: K<2><<<grid, blk, 0, st>>>(__VA_ARGS__); break;           \
+      case 3: K<3><<<grid, blk, 0, st>>>(__VA_ARGS__); break;           \
+      case 4: K<4><<<grid, blk, 0, st>>>(__VA_ARGS__); break;           \
+      default: K<5><<<grid, blk, 0, st>>>(__VA_ARGS__); break;          \
+    }                                                                   \
+  } while (0)
 // y(t) = sum_j zn[j] s^j
 __global__ void k_interp(int n, int q, ZnPtrs zn, double s, double *__restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -106,9 +134,10 @@ __global__ void k_newton_upd(int n, const double *__restrict__ b, double *__rest
   acor[i] = a;
   y[i] = zn0[i] + a;
 }
-__global__ void k_div_ewt(int n, const double *__restrict__ v, const double *__restrict__ w, double *__restrict__ o) {
+// o = v / w, given ws = 1 / w
+__global__ void k_div_ewt(int n, const double *__restrict__ v, const double *__restrict__ ws, double *__restrict__ o) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) o[i] = v[i] / w[i];
+  if (i < n) o[i] = v[i] * ws[i];
 }
 __global__ void k_hub(int n, const double *__restrict__ y, const double *__restrict__ yp, const double *__restrict__ w,
                       double *__restrict__ out) {
@@ -122,12 +151,20 @@ __global__ void k_red(int n, int mode, const double *__restrict__ x, const doubl
                       double *__restrict__ part) {
   __shared__ double sm[32];
   double acc = 0.0;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double v = (mode == 0) ? x[i] * y[i] : x[i] * y[i];
+  const int stride = gridDim.x * blockDim.x;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  auto step = [&](double xv, double yv) {
+    const double v = xv * yv;
     if (mode == 0) acc += v * v;
     else if (mode == 1) acc += v;
-    else acc = fmax(acc, x[i]);
+    else acc = fmax(acc, xv);
+  };
+  for (; i + 3 * stride < n; i += 4 * stride) {   // four loads of each vector in flight, same order
+    const double x0 = x[i], x1 = x[i + stride], x2 = x[i + 2 * stride], x3 = x[i + 3 * stride];
+    const double y0 = y[i], y1 = y[i + stride], y2 = y[i + 2 * stride], y3 = y[i + 3 * stride];
+    step(x0, y0); step(x1, y1); step(x2, y2); step(x3, y3);
   }
+  for (; i < n; i += stride) step(x[i], y[i]);
   if (mode == 2) { for (int o = 16; o; o >>= 1) acc = fmax(acc, __shfl_xor_sync(0xffffffffu, acc, o)); }
   else acc = warp_sum(acc);
   if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
@@ -140,16 +177,23 @@ __global__ void k_red(int n, int mode, const double *__restrict__ x, const doubl
 }
 // Multi-dot h[k] = V[k] . w for k < nv (Gram-Schmidt), partials per block.
 struct VecPtrs { const double *v[32]; };
+// NVM: compile-time bound on nv (the accumulators and vector pointers stay
+// in registers).
+template <int NVM>
 __global__ void k_mdot(int n, int nv, VecPtrs V, const double *__restrict__ w, double *__restrict__ part) {
   __shared__ double sm[32][33];
-  double acc[32];
-  for (int k = 0; k < nv; ++k) acc[k] = 0.0;
+  double acc[NVM];
+#pragma unroll
+  for (int k = 0; k < NVM; ++k) acc[k] = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double wi = w[i];
-    for (int k = 0; k < nv; ++k) acc[k] += V.v[k][i] * wi;
+#pragma unroll
+    for (int k = 0; k < NVM; ++k) if (k < nv) acc[k] += V.v[k][i] * wi;
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int k = 0; k < nv; ++k) {
+#pragma unroll
+  for (int k = 0; k < NVM; ++k) {
+    if (k >= nv) break;
     double s = warp_sum(acc[k]);
     if (lane == 0) sm[wid][k] = s;
   }
@@ -160,15 +204,30 @@ __global__ void k_mdot(int n, int nv, VecPtrs V, const double *__restrict__ w, d
     part[(size_t)blockIdx.x * 32 + threadIdx.x] = s;
   }
 }
-// Ordered sum of the multi-dot partials into h (device).
-__global__ void k_mdot_final(int nblocks, int nv, const double *__restrict__ part, double *__restrict__ h) {
-  int k = threadIdx.x;
-  if (k >= nv) return;
+// Ordered sum of the multi-dot partials into h (device), one block of 256
+// threads: thread (chunk c = tid / 32, value k = tid % 32) adds the partials
+// of blocks [c * nblocks / 8, (c + 1) * nblocks / 8) in order, then thread k
+// adds the 8 chunk sums in order.
+__global__ void __launch_bounds__(256) k_mdot_final(int nblocks, int nv, const double *__restrict__ part,
+                                                    double *__restrict__ h) {
+  __shared__ double sc[8][32];
+  const int k = threadIdx.x & 31, c = threadIdx.x >> 5;
+  const int b0 = (int)((long long)c * nblocks / 8), b1 = (int)((long long)(c + 1) * nblocks / 8);
   double s = 0.0;
-  for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * 32 + k];
-  h[k] = s;
+  if (k < nv) {
+#pragma unroll 8
+    for (int b = b0; b < b1; ++b) s += part[(size_t)b * 32 + k];
+  }
+  sc[c][k] = s;
+  __syncthreads();
+  if (threadIdx.x < nv) {
+    double t = 0.0;
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) t += sc[cc][threadIdx.x];
+    h[threadIdx.x] = t;
+  }
 }
-// w -= sum_k h[k] V[k]  and accumulate hacc += h
+template <int NVM>
 __global__ void k_orth(int n, int nv, VecPtrs V, const double *__restrict__ h, double *__restrict__ w) {
   __shared__ double hs[32];
   if (threadIdx.x < nv) hs[threadIdx.x] = h[threadIdx.x];
@@ -176,8 +235,40 @@ __global__ void k_orth(int n, int nv, VecPtrs V, const double *__restrict__ h, d
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double s = w[i];
-  for (int k = 0; k < nv; ++k) s -= hs[k] * V.v[k][i];
+#pragma unroll
+  for (int k = 0; k < NVM; ++k) if (k < nv) s -= hs[k] * V.v[k][i];
   w[i] = s;
+}
+// x += sum_k c_k V_k with the coefficients passed by value (no host-to-device
+// copy, so the host need not wait before reusing its buffer)
+struct Coef32 { double c[32]; };
+template <int NVM>
+__global__ void k_axpy_multi(int n, int nv, VecPtrs V, Coef32 c, double *__restrict__ x) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = x[i];
+#pragma unroll
+  for (int k = 0; k < NVM; ++k) if (k < nv) s -= (-c.c[k]) * V.v[k][i];
+  x[i] = s;
+}
+void launch_axpy_multi(int n, int nv, const VecPtrs &vp, const Coef32 &c, double *x, cudaStream_t st) {
+  const int g = nblk(n, 256);
+  if (nv <= 1) k_axpy_multi<1><<<g, 256, 0, st>>>(n, nv, vp, c, x);
+  else if (nv <= 2) k_axpy_multi<2><<<g, 256, 0, st>>>(n, nv, vp, c, x);
+  else if (nv <= 4) k_axpy_multi<4><<<g, 256, 0, st>>>(n, nv, vp, c, x);
+  else if (nv <= 8) k_axpy_multi<8><<<g, 256, 0, st>>>(n, nv, vp, c, x);
+  else if (nv <= 16) k_axpy_multi<16><<<g, 256, 0, st>>>(n, nv, vp, c, x);
+  else k_axpy_multi<32><<<g, 256, 0, st>>>(n, nv, vp, c, x);
+}
+// k_orth<NVM> for the smallest NVM >= nv
+void launch_orth(int n, int nv, const VecPtrs &vp, const double *h, double *w, cudaStream_t st) {
+  const int g = nblk(n, 256);
+  if (nv <= 1) k_orth<1><<<g, 256, 0, st>>>(n, nv, vp, h, w);
+  else if (nv <= 2) k_orth<2><<<g, 256, 0, st>>>(n, nv, vp, h, w);
+  else if (nv <= 4) k_orth<4><<<g, 256, 0, st>>>(n, nv, vp, h, w);
+  else if (nv <= 8) k_orth<8><<<g, 256, 0, st>>>(n, nv, vp, h, w);
+  else if (nv <= 16) k_orth<16><<<g, 256, 0, st>>>(n, nv, vp, h, w);
+  else k_orth<32><<<g, 256, 0, st>>>(n, nv, vp, h, w);
 }
 __global__ void k_hacc(int nv, const double *__restrict__ h, double *__restrict__ hcol, int first) {
   int k = threadIdx.x;
@@ -190,7 +281,8 @@ __global__ void k_hacc(int nv, const double *__restrict__ h, double *__restrict_
 struct JvArgs {
   int N, nrep;   // nodes per member, ensemble members (member-major vectors)
   const int32_t *row_ptr, *col_idx, *diag_pos;
-  const double *K, *vol, *mJ, *HJ, *t, *ewt;
+  const double *K, *ivol, *mJ, *HJ, *t, *ewt;
+  const double *Pinv;   // per node and member: inverse of the 3x3 preconditioner block (row-major)
   double c_exch, C1, C2, gamma, gammap;
   int psolve, scale_out;
   double *out;
@@ -226,31 +318,16 @@ __global__ void k_jv_psolve(JvArgs a) {
     double kv = a.K[k];
     s0 += kv * tj[0]; s1 += kv * tj[1]; s2 += kv * tj[2];
   }
-  const double V = a.vol[i];
-  const double hv[3] = {-a.c_exch * s0 / V, -a.c_exch * s1 / V, -a.c_exch * s2 / V};
+  const double ce = -a.c_exch * a.ivol[i];
+  const double hv[3] = {ce * s0, ce * s1, ce * s2};
   const double *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g, *w = a.t + 3 * (size_t)g;
   double jw[3];
   jac_apply(m, H, w, hv, a.C1, a.C2, jw);
   double r[3] = {w[0] - a.gamma * jw[0], w[1] - a.gamma * jw[1], w[2] - a.gamma * jw[2]};
   double z[3] = {r[0], r[1], r[2]};
   if (a.psolve) {
-    const double kap = -a.c_exch * a.K[a.diag_pos[i]] / V;
-    double P[3][3];
-    for (int c = 0; c < 3; ++c) {
-      double e[3] = {0.0, 0.0, 0.0};
-      e[c] = 1.0;
-      double he[3] = {kap * e[0], kap * e[1], kap * e[2]}, je[3];
-      jac_apply(m, H, e, he, a.C1, a.C2, je);
-      for (int d = 0; d < 3; ++d) P[d][c] = (d == c ? 1.0 : 0.0) - a.gammap * je[d];
-    }
-    double c00 = P[1][1] * P[2][2] - P[1][2] * P[2][1];
-    double c01 = P[1][2] * P[2][0] - P[1][0] * P[2][2];
-    double c02 = P[1][0] * P[2][1] - P[1][1] * P[2][0];
-    double inv = 1.0 / (P[0][0] * c00 + P[0][1] * c01 + P[0][2] * c02);
-    double Pi[3][3] = {{c00 * inv, (P[0][2] * P[2][1] - P[0][1] * P[2][2]) * inv, (P[0][1] * P[1][2] - P[0][2] * P[1][1]) * inv},
-                       {c01 * inv, (P[0][0] * P[2][2] - P[0][2] * P[2][0]) * inv, (P[0][2] * P[1][0] - P[0][0] * P[1][2]) * inv},
-                       {c02 * inv, (P[0][1] * P[2][0] - P[0][0] * P[2][1]) * inv, (P[0][0] * P[1][1] - P[0][1] * P[1][0]) * inv}};
-    for (int d = 0; d < 3; ++d) z[d] = (Pi[d][0] * r[0] + Pi[d][1] * r[1]) + Pi[d][2] * r[2];
+    const double *Pi = a.Pinv + 9 * (size_t)g;
+    for (int d = 0; d < 3; ++d) z[d] = (Pi[3 * d] * r[0] + Pi[3 * d + 1] * r[1]) + Pi[3 * d + 2] * r[2];
   }
   for (int d = 0; d < 3; ++d) {
     size_t o = 3 * (size_t)g + d;
@@ -258,16 +335,17 @@ __global__ void k_jv_psolve(JvArgs a) {
   }
 }
 
-// Block-Jacobi preconditioner alone: out = ewt * P^{-1} r (r unscaled).
-__global__ void k_psolve(int N, const int32_t *__restrict__ diag_pos, const double *__restrict__ K,
-                         const double *__restrict__ vol, const double *__restrict__ mJ, const double *__restrict__ HJ,
-                         double c_exch, double C1, double C2, double gammap, const double *__restrict__ r,
-                         const double *__restrict__ ewt, double *__restrict__ out, int nrep) {
+// The block-Jacobi preconditioner's 3x3 blocks P = I - gamma_p dF/dm (the
+// exchange diagonal and the site terms at the setup state mJ, HJ), inverted
+// once per preconditioner setup: Pinv[9 g + 3 d + c] = (P^-1)_dc.
+__global__ void k_pprep(int N, const int32_t *__restrict__ diag_pos, const double *__restrict__ K,
+                        const double *__restrict__ vol, const double *__restrict__ mJ, const double *__restrict__ HJ,
+                        double c_exch, double C1, double C2, double gammap, double *__restrict__ Pinv, int nrep) {
   const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (g >= (long long)N * nrep) return;
   const int i = (int)(g % N);
   const double kap = -c_exch * K[diag_pos[i]] / vol[i];
-  const double *m = mJ + 3 * (size_t)g, *H = HJ + 3 * (size_t)g, *ri = r + 3 * (size_t)g;
+  const double *m = mJ + 3 * (size_t)g, *H = HJ + 3 * (size_t)g;
   double P[3][3];
   for (int c = 0; c < 3; ++c) {
     double e[3] = {0.0, 0.0, 0.0};
@@ -280,12 +358,21 @@ __global__ void k_psolve(int N, const int32_t *__restrict__ diag_pos, const doub
   double c01 = P[1][2] * P[2][0] - P[1][0] * P[2][2];
   double c02 = P[1][0] * P[2][1] - P[1][1] * P[2][0];
   double inv = 1.0 / (P[0][0] * c00 + P[0][1] * c01 + P[0][2] * c02);
-  double Pi[3][3] = {{c00 * inv, (P[0][2] * P[2][1] - P[0][1] * P[2][2]) * inv, (P[0][1] * P[1][2] - P[0][2] * P[1][1]) * inv},
-                     {c01 * inv, (P[0][0] * P[2][2] - P[0][2] * P[2][0]) * inv, (P[0][2] * P[1][0] - P[0][0] * P[1][2]) * inv},
-                     {c02 * inv, (P[0][1] * P[2][0] - P[0][0] * P[2][1]) * inv, (P[0][0] * P[1][1] - P[0][1] * P[1][0]) * inv}};
+  double *o = Pinv + 9 * (size_t)g;
+  o[0] = c00 * inv; o[1] = (P[0][2] * P[2][1] - P[0][1] * P[2][2]) * inv; o[2] = (P[0][1] * P[1][2] - P[0][2] * P[1][1]) * inv;
+  o[3] = c01 * inv; o[4] = (P[0][0] * P[2][2] - P[0][2] * P[2][0]) * inv; o[5] = (P[0][2] * P[1][0] - P[0][0] * P[1][2]) * inv;
+  o[6] = c02 * inv; o[7] = (P[0][1] * P[2][0] - P[0][0] * P[2][1]) * inv; o[8] = (P[0][0] * P[1][1] - P[0][1] * P[1][0]) * inv;
+}
+
+// Block-Jacobi preconditioner alone: out = ewt * P^{-1} r (r unscaled).
+__global__ void k_psolve(long long n3, const double *__restrict__ Pinv, const double *__restrict__ r,
+                         const double *__restrict__ ewt, double *__restrict__ out) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (3 * g >= n3) return;
+  const double *Pi = Pinv + 9 * (size_t)g, *ri = r + 3 * (size_t)g;
   for (int d = 0; d < 3; ++d) {
     size_t o = 3 * (size_t)g + d;
-    out[o] = ewt[o] * ((Pi[d][0] * ri[0] + Pi[d][1] * ri[1]) + Pi[d][2] * ri[2]);
+    out[o] = ewt[o] * ((Pi[3 * d] * ri[0] + Pi[3 * d + 1] * ri[1]) + Pi[3 * d + 2] * ri[2]);
   }
 }
 
@@ -296,6 +383,8 @@ struct Integrator {
   int n, qmax, maxl;
   double rtol, atol;
   DevBuf<double> znbuf, ewt, acor, y, tempv, ftemp, xsol, mJ, HJ, Vbuf, tvec, part, hdev, hcol;
+  DevBuf<double> Pinv;   // preconditioner blocks inverted at each setup (9 per node and member)
+  DevBuf<double> ewts;   // 1 / ewt
   double *zn[QMAXB + 2];
   std::vector<double *> V;
   double *hpin = nullptr;  // pinned readback
@@ -338,7 +427,7 @@ struct Integrator {
     if (r) status = r;
     return r;
   }
-  void set_ewt(const double *yv) { k_ewt<<<nblk(n, 256), 256, 0, s()>>>(n, rtol, atol, yv, ewt); ++hd->launches; }
+  void set_ewt(const double *yv) { k_ewt<<<nblk(n, 256), 256, 0, s()>>>(n, rtol, atol, yv, ewt, ewts); ++hd->launches; }
 };
 
 namespace {
@@ -389,8 +478,8 @@ int psetup(Integrator &I, int jok, const double *ypred) {
 JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
   const Mesh &M = I.hd->mesh;
   JvArgs a;
-  a.N = M.N; a.nrep = I.hd->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.vol = M.vol;
-  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt;
+  a.N = M.N; a.nrep = I.hd->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.ivol = M.ivol;
+  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv;
   a.c_exch = I.hd->mat.exch_coeff; a.C1 = I.hd->mat.C1; a.C2 = I.hd->mat.C2;
   a.gamma = I.gamma; a.gammap = I.gammap; a.psolve = psolve; a.scale_out = 1; a.out = out;
   return a;
@@ -404,14 +493,20 @@ void orthogonalise(Integrator &I, int nv, double *w) {
       int cnt = nv - k0 < 32 ? nv - k0 : 32;
       VecPtrs vp;
       for (int k = 0; k < cnt; ++k) vp.v[k] = I.V[k0 + k];
-      k_mdot<<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part); ++I.hd->launches;
-      k_mdot_final<<<1, 32, 0, I.s()>>>(kRedBlocks, cnt, I.part, I.hdev.p + k0); ++I.hd->launches;
+      if (cnt <= 1) k_mdot<1><<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part);
+      else if (cnt <= 2) k_mdot<2><<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part);
+      else if (cnt <= 4) k_mdot<4><<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part);
+      else if (cnt <= 8) k_mdot<8><<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part);
+      else if (cnt <= 16) k_mdot<16><<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part);
+      else k_mdot<32><<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part);
+      ++I.hd->launches;
+      k_mdot_final<<<1, 256, 0, I.s()>>>(kRedBlocks, cnt, I.part, I.hdev.p + k0); ++I.hd->launches;
     }
     for (int k0 = 0; k0 < nv; k0 += 32) {
       int cnt = nv - k0 < 32 ? nv - k0 : 32;
       VecPtrs vp;
       for (int k = 0; k < cnt; ++k) vp.v[k] = I.V[k0 + k];
-      k_orth<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, cnt, vp, I.hdev.p + k0, w); ++I.hd->launches;
+      launch_orth(I.n, cnt, vp, I.hdev.p + k0, w, I.s()); ++I.hd->launches;
       k_hacc<<<1, 32, 0, I.s()>>>(cnt, I.hdev.p + k0, I.hcol.p + k0, pass == 0); ++I.hd->launches;
     }
   }
@@ -425,9 +520,8 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
   const nmg_material &mt = I.hd->mat;
   auto HM = [&](int i, int j) -> double & { return I.Hm[(size_t)i * maxl + j]; };
   *nli_out = 0;
-  k_psolve<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(M.N, M.diag_pos, I.hd->exch_K(), M.vol, I.mJ,
-                                                                       I.HJ, mt.exch_coeff, mt.C1, mt.C2, I.gammap, b,
-                                                                       I.ewt, I.V[0], I.hd->nrep); ++I.hd->launches;
+  k_psolve<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>((long long)n, I.Pinv, b, I.ewt, I.V[0]);
+  ++I.hd->launches;
   I.nps++;
   double rho = 0.0;  // ||V0||_2 (unweighted)
   {
@@ -446,7 +540,7 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
   I.yg[0] = rho;
   int converged = 0, kdim = 0;
   for (int l = 0; l < maxl; ++l) {
-    k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewt, I.tvec); ++I.hd->launches;
+    k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewts, I.tvec); ++I.hd->launches;
     JvArgs a = jv_args(I, I.tvec, I.V[l + 1], 1);
     {
       NMG_PROF_BEGIN(I.hd, 4);
@@ -496,26 +590,26 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
     int cnt = kdim - k0 < 32 ? kdim - k0 : 32;
     VecPtrs vp;
     for (int k = 0; k < cnt; ++k) vp.v[k] = I.V[k0 + k];
-    for (int k = 0; k < cnt; ++k) I.hpin[k] = -I.yg[k0 + k];
-    cudaMemcpyAsync(I.hdev.p, I.hpin, sizeof(double) * cnt, cudaMemcpyHostToDevice, I.s());
-    k_orth<<<nblk(n, 256), 256, 0, I.s()>>>(n, cnt, vp, I.hdev, x);  // x -= (-y) V ++I.hd->launches;
-    cudaStreamSynchronize(I.s());
+    Coef32 c;
+    for (int k = 0; k < cnt; ++k) c.c[k] = I.yg[k0 + k];
+    launch_axpy_multi(n, cnt, vp, c, x, I.s());   // x -= (-y) V, as the Gram-Schmidt update
+    ++I.hd->launches;
   }
-  k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, x, I.ewt, x); ++I.hd->launches;
+  k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, x, I.ewts, x); ++I.hd->launches;
   if (converged) return 0;
   return (rho < I.beta0) ? 2 : 1;
 }
 
 void predict(Integrator &I) {
   I.tn += I.h;
-  k_predict<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), 1); ++I.hd->launches;
+  NMG_LAUNCH_Q(k_predict, I.q, nblk(I.n, 256), 256, I.s(), I.n, I.znp(), 1); ++I.hd->launches;
 }
 void restore(Integrator &I, double saved_t) {
   I.tn = saved_t;
-  k_predict<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), -1); ++I.hd->launches;
+  NMG_LAUNCH_Q(k_predict, I.q, nblk(I.n, 256), 256, I.s(), I.n, I.znp(), -1); ++I.hd->launches;
 }
 void rescale(Integrator &I) {
-  k_rescale<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), I.eta); ++I.hd->launches;
+  NMG_LAUNCH_Q(k_rescale, I.q, nblk(I.n, 256), 256, I.s(), I.n, I.znp(), I.eta); ++I.hd->launches;
   I.h = I.hscale * I.eta;
   I.hprime = I.h;
   I.hscale = I.h;
@@ -589,6 +683,14 @@ int nls(Integrator &I, int nflag_first) {
       I.nsetups++;
       I.crate = 1.0; I.gammap = I.gamma; I.nstlp = I.nst; I.gamrat = 1.0;
       call_setup = 0;
+      {
+        const Mesh &M = I.hd->mesh;
+        const nmg_material &mt = I.hd->mat;
+        k_pprep<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(
+            M.N, M.diag_pos, I.hd->exch_K(), M.vol, I.mJ, I.HJ, mt.exch_coeff, mt.C1, mt.C2, I.gammap, I.Pinv,
+            I.hd->nrep);
+        ++I.hd->launches;
+      }
     }
     cudaMemsetAsync(I.acor.p, 0, sizeof(double) * n, I.s());
     cudaMemcpyAsync(I.y.p, I.zn[0], sizeof(double) * n, cudaMemcpyDeviceToDevice, I.s());
@@ -643,7 +745,7 @@ void complete_step(Integrator &I) {
   I.tau[1] = I.h;
   Coef c;
   for (int j = 0; j < QMAXB + 2; ++j) c.c[j] = j <= QMAXB ? I.l[j] : 0.0;
-  k_complete<<<nblk(I.n, 256), 256, 0, I.s()>>>(I.n, I.q, I.znp(), c, I.acor); ++I.hd->launches;
+  NMG_LAUNCH_Q(k_complete, I.q, nblk(I.n, 256), 256, I.s(), I.n, I.znp(), c, I.acor); ++I.hd->launches;
   I.qwait--;
   if (I.qwait == 1 && I.q != I.qmax) {
     cudaMemcpyAsync(I.zn[I.qmax], I.acor.p, sizeof(double) * I.n, cudaMemcpyDeviceToDevice, I.s());
@@ -801,9 +903,10 @@ Integrator *ts_create(nmg_handle *h, int qmax, int maxl, double rtol, double ato
   I->rtol = rtol; I->atol = atol;
   const size_t n = I->n;
   bool ok = I->znbuf.alloc(n * (I->qmax + 2)) == cudaSuccess;
-  for (DevBuf<double> *b : {&I->ewt, &I->acor, &I->y, &I->tempv, &I->ftemp, &I->xsol, &I->mJ, &I->HJ, &I->tvec})
+  for (DevBuf<double> *b : {&I->ewt, &I->ewts, &I->acor, &I->y, &I->tempv, &I->ftemp, &I->xsol, &I->mJ, &I->HJ, &I->tvec})
     ok = ok && b->alloc(n) == cudaSuccess;
   ok = ok && I->Vbuf.alloc(n * (I->maxl + 1)) == cudaSuccess;
+  ok = ok && I->Pinv.alloc(3 * n) == cudaSuccess;
   ok = ok && I->part.alloc(32 * kRedBlocks) == cudaSuccess;
   ok = ok && I->hdev.alloc(I->maxl + 64) == cudaSuccess;
   ok = ok && I->hcol.alloc(I->maxl + 64) == cudaSuccess;

@@ -91,12 +91,12 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *smem) {
 }
 
 // Block sum of NV values per thread in a fixed order, the totals written as
-// double to out[0..NV) by threads 0..NV-1 (out may be global).  Each warp
+// double to out[j * stride], j < NV, by threads 0..NV-1 (out may be global).  Each warp
 // reduces its lanes with transpose sums (one shuffle-add per value per
 // stage at the widest, against five for a butterfly per value), then
 // thread j adds value j over the warps.  smem: (kCGThreads/32) x W values.
 template <typename T, int NV>
-__device__ __forceinline__ void block_reduce_out(const T (&v)[NV], T *smem, double *out) {
+__device__ __forceinline__ void block_reduce_out(const T (&v)[NV], T *smem, double *out, int stride = 1) {
   using S = RedShape<NV>;
   constexpr int NW = kCGThreads / 32;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -114,16 +114,18 @@ __device__ __forceinline__ void block_reduce_out(const T (&v)[NV], T *smem, doub
     T t = T(0);
 #pragma unroll
     for (int w = 0; w < NW; ++w) t += smem[w * S::W + threadIdx.x];
-    out[threadIdx.x] = (double)t;
+    out[(size_t)threadIdx.x * stride] = (double)t;
   }
 }
 
-// res[j] = sum over the grid's blocks of slot[b * stride + j], j < NV, in a
-// fixed order, identical in every block: warp w takes the values j = w,
-// w + 8, ...; its lanes take blocks lane, lane + 32, ... (all of a lane's
-// loads issued together), then one transpose sum per warp.  res: shared.
+// res[j] = sum over the grid's blocks b of slot[j * gridDim.x + b] (block
+// partials stored value-major, so a warp's loads of one value are
+// contiguous), j < NV, in a fixed order, identical in every block: warp w
+// takes the values j = w, w + 8, ...; its lanes take blocks lane, lane + 32,
+// ... (all of a lane's loads issued together), then one transpose sum per
+// warp.  res: shared.
 template <int NV>
-__device__ __forceinline__ void grid_total(const double *slot, int stride, double *res) {
+__device__ __forceinline__ void grid_total(const double *slot, double *res) {
   constexpr int NW = kCGThreads / 32;
   constexpr int JV = (NV + NW - 1) / NW;
   using S = RedShape<JV>;
@@ -136,7 +138,7 @@ __device__ __forceinline__ void grid_total(const double *slot, int stride, doubl
 #pragma unroll
     for (int q = 0; q < JV; ++q) {
       const int j = wid + q * NW;
-      if (j < NV) t[q] += __ldcg(slot + (size_t)b * stride + j);
+      if (j < NV) t[q] += __ldcg(slot + (size_t)j * gridDim.x + b);
     }
   }
   const double tot = warp_transpose_sum<double, S::Q>(t);
@@ -168,10 +170,15 @@ struct CGArgs {
   // mixed-precision CG: FP32 copies for the inner iterations
   const float *ainv32;
   float *rc32, *z32;  // coarse residual (nc x MB), published inner direction (N x MB)
+  float *rw32;        // R w of every aggregate (nc x MB), published with the inner dot products
   float eta;          // inner relative tolerance
   int max_outer;      // FP64 refinement steps
 };
 constexpr int kAgg = 64;   // rows per aggregate (4 aggregates per 256-row block)
+// float4 groups of the coarse vectors (nc x MB floats) per thread of the
+// mixed-precision CG: nc * kChunk <= kRwPer * 4 * kCGThreads, i.e. up to 640
+// aggregates (40,960 nodes; its one-block-per-SM grid holds 38,912 rows)
+constexpr int kRwPer = 5;
 
 // ---- single-reduction CG on a counter barrier ----
 constexpr int kCG2MaxRed = 11 * kChunk;   // widest fused reduction (projection dots + b.b per ensemble member)
@@ -201,6 +208,24 @@ __device__ __forceinline__ bool arrive_wait(const CGArgs &a, unsigned epoch) {
   return !(*(volatile int *)a.err & ERR_BARRIER);
 }
 
+// arrive_wait in two halves, so that a block can work between its arrival
+// and the wait (same counter, same spin limit and error flag).
+__device__ __forceinline__ void arrive(const CGArgs &a) {
+  __syncthreads();
+  if (threadIdx.x == 0) asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(a.flags) : "memory");
+}
+__device__ __forceinline__ bool wait_epoch(const CGArgs &a, unsigned epoch) {
+  if (threadIdx.x == 0) {
+    const unsigned target = epoch * gridDim.x;
+    unsigned long long spins = 0;
+    while (ld_acquire_gpu(a.flags) < target) {
+      if (++spins > kBarrierSpinLimit || (*(volatile int *)a.err & ERR_BARRIER)) { atomicOr(a.err, ERR_BARRIER); break; }
+    }
+  }
+  __syncthreads();
+  return !(*(volatile int *)a.err & ERR_BARRIER);
+}
+
 // Reduction fused with the counter barrier: partials double-buffered by
 // epoch parity; after the barrier every block sums all partials in block
 // order (deterministic, identical in every block).  smem: block_reduce_out
@@ -209,10 +234,10 @@ template <int NV>
 __device__ __forceinline__ bool reduce_all(const CGArgs &a, unsigned epoch, double (&v)[NV], double *smem,
                                            double (&out)[NV]) {
   double *slot = a.red + (size_t)(epoch & 1) * gridDim.x * kCG2MaxRed;
-  block_reduce_out<double, NV>(v, smem, slot + (size_t)blockIdx.x * kCG2MaxRed);
+  block_reduce_out<double, NV>(v, smem, slot + blockIdx.x, gridDim.x);
   if (!arrive_wait(a, epoch)) return false;
   double *res = smem + (kCGThreads / 32) * RedShape<NV>::W;
-  grid_total<NV>(slot, kCG2MaxRed, res);
+  grid_total<NV>(slot, res);
 #pragma unroll
   for (int j = 0; j < NV; ++j) out[j] = res[j];
   __syncthreads();
@@ -225,9 +250,9 @@ template <int NV>
 __device__ __forceinline__ bool reduce_all_to(const CGArgs &a, unsigned epoch, double (&v)[NV], double *smem,
                                               double *res) {
   double *slot = a.red + (size_t)(epoch & 1) * gridDim.x * kCG2MaxRed;
-  block_reduce_out<double, NV>(v, smem, slot + (size_t)blockIdx.x * kCG2MaxRed);
+  block_reduce_out<double, NV>(v, smem, slot + blockIdx.x, gridDim.x);
   if (!arrive_wait(a, epoch)) return false;
-  grid_total<NV>(slot, kCG2MaxRed, res);
+  grid_total<NV>(slot, res);
   return true;
 }
 
@@ -816,9 +841,9 @@ template <int NV>
 __device__ __forceinline__ bool reduce_all_f(const CGArgs &a, unsigned epoch, float (&v)[NV], float *smemf,
                                              double *res) {
   double *slot = a.red + (size_t)(epoch & 1) * gridDim.x * kCG2MaxRed;
-  block_reduce_out<float, NV>(v, smemf, slot + (size_t)blockIdx.x * kCG2MaxRed);
+  block_reduce_out<float, NV>(v, smemf, slot + blockIdx.x, gridDim.x);
   if (!arrive_wait(a, epoch)) return false;
-  grid_total<NV>(slot, kCG2MaxRed, res);
+  grid_total<NV>(slot, res);
   return true;
 }
 
@@ -839,7 +864,8 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
   __shared__ float smemf[kCGThreads / 32 * RedShape<3 * MB>::W];
   __shared__ double sres[P * MB];
   __shared__ double sbdot[P * MB];
-  __shared__ double s_al[MB], s_be[MB], s_ga[MB], s_tol[MB], s_itol[MB];
+  __shared__ double s_tol[MB], s_itol2[MB];
+  __shared__ float s_al[MB], s_be[MB], s_ga[MB];
   __shared__ int s_st[MB], s_out[MB];
   __shared__ int s_cnt[MB], s_head[MB];
   __shared__ double scoef[MB * kBasis];
@@ -881,11 +907,36 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
     for (int m = 0; m < MB; ++m) if (m < nm) xi[m] = a.x[(size_t)m * N + node];
   }
   const float dinv32 = (float)dinv;
+  float *suS = sK32 + nnz_cap;                        // this block's u, kCGThreads x MB (local SpMV)
+  float *rcS = suS + (size_t)kCGThreads * MB;         // coarse residual R r of every aggregate (nc x MB)
+  float *RsS = rcS + (size_t)a.nc * MB;               // R s of every aggregate (nc x MB)
+  float *ainvS = RsS + (size_t)a.nc * MB;             // this block's rows of the coarse inverse
+  if (a.coarse)
+    for (int e = tid; e < (kCGThreads / kAgg) * a.nc; e += kCGThreads) {
+      const int I = blockIdx.x * (kCGThreads / kAgg) + e / a.nc;
+      ainvS[e] = I < a.nc ? a.ainv32[(size_t)I * a.nc + e % a.nc] : 0.f;
+    }
+
   if (tid < MB) {
     s_cnt[tid] = tid < nm ? B.ring[2 * tid] : 0;
     s_head[tid] = tid < nm ? B.ring[2 * tid + 1] : 0;
   }
   __syncthreads();
+  // each row's columns inside the block's row range first (read from shared
+  // memory while the barrier that publishes u completes); after the barrier
+  // above, every row's entries are in place
+  int mid = lo;
+  for (int k = lo; k < hi; ++k) {
+    const int j = sC[k];
+    if (j >= row0 && j < row0 + kCGThreads) {
+      if (k != mid) {
+        const int tc = sC[mid]; sC[mid] = j; sC[k] = tc;
+        const double td = sK[mid]; sK[mid] = sK[k]; sK[k] = td;
+        const float tf = sK32[mid]; sK32[mid] = sK32[k]; sK32[k] = tf;
+      }
+      ++mid;
+    }
+  }
   // FP64 operator on the published member-minor FP64 vector
   auto apply64 = [&](const double *v, double (&s)[MB]) {
 #pragma unroll
@@ -923,17 +974,33 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
       }
     }
   };
-  // FP32 operator on the published member-minor FP32 vector
-  auto apply32 = [&](const float *v, float (&s)[MB]) {
+  // FP32 operator, in two parts around the barrier that publishes u: the
+  // columns inside this block's row range (put first in each row, above)
+  // from the block's own u in shared memory, before the wait; the other
+  // columns from the published member-minor FP32 vector, after it.
+  auto apply32_local = [&](float (&s)[MB]) {
 #pragma unroll
     for (int m = 0; m < MB; ++m) s[m] = 0.f;
     if (ident) {
-      const float2 *vr = reinterpret_cast<const float2 *>(v + (size_t)r * MB);
+      const float2 *vr = reinterpret_cast<const float2 *>(suS + (size_t)tid * MB);
 #pragma unroll
-      for (int q = 0; q < MB / 2; ++q) { const float2 t = __ldcg(vr + q); s[2 * q] = t.x; s[2 * q + 1] = t.y; }
+      for (int q = 0; q < MB / 2; ++q) { const float2 t = vr[q]; s[2 * q] = t.x; s[2 * q + 1] = t.y; }
       return;
     }
-    int k = lo;
+    for (int k = lo; k < mid; ++k) {
+      const float kv = sK32[k];
+      const float2 *vc = reinterpret_cast<const float2 *>(suS + (size_t)(sC[k] - row0) * MB);
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q) {
+        const float2 t = vc[q];
+        s[2 * q] = fmaf(kv, t.x, s[2 * q]);
+        s[2 * q + 1] = fmaf(kv, t.y, s[2 * q + 1]);
+      }
+    }
+  };
+  auto apply32_halo = [&](const float *v, float (&s)[MB]) {
+    if (ident) return;
+    int k = mid;
     for (; k + 4 <= hi; k += 4) {   // four neighbours' loads in flight
       float2 t[4][MB / 2];
 #pragma unroll
@@ -964,57 +1031,76 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
     }
   };
   unsigned epoch = 0;
-  auto precond32 = [&](const float (&rr)[MB], float (&uu)[MB]) -> bool {
-#pragma unroll
-    for (int m = 0; m < MB; ++m) uu[m] = dinv32 * rr[m];
-    if (!a.coarse) return true;
+  // Two-level preconditioner u = D^-1 r + P A_c^-1 R r (R: sums over the
+  // kAgg-row aggregates; a block's rows form whole aggregates).  Every block
+  // keeps the whole coarse residual R r in shared memory (rcS): precond32
+  // forms it from r (one barrier) at the start of an inner solve; inside the
+  // iteration it follows the recurrence R r -= alpha R s, R s = R w + beta R s,
+  // with R w published alongside the dot products, so the coarse step needs
+  // no barrier of its own.
+  auto coarse_add = [&](float (&uu)[MB]) {
     const int lane = tid & 31, wid = tid >> 5;
-#pragma unroll
-    for (int m = 0; m < MB; ++m) {
-      float s = active ? rr[m] : 0.f;
-#pragma unroll
-      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) sagg[m][wid] = s;
-    }
-    __syncthreads();
-    if (tid < kCGThreads / kAgg) {
-      const int I = blockIdx.x * (kCGThreads / kAgg) + tid;
-      if (I < a.nc)
-        for (int m = 0; m < MB; ++m) a.rc32[(size_t)I * MB + m] = sagg[m][2 * tid] + sagg[m][2 * tid + 1];
-    }
-    if (!arrive_wait(a, ++epoch)) return false;
     const int g = tid / kAgg, t = tid % kAgg;
     const int I = blockIdx.x * (kCGThreads / kAgg) + g;
     float acc[MB];
 #pragma unroll
     for (int m = 0; m < MB; ++m) acc[m] = 0.f;
     if (I < a.nc) {
-      const float *row = a.ainv32 + (size_t)I * a.nc;
+      const float *row = ainvS + (size_t)g * a.nc;
 #pragma unroll 4
       for (int J = t; J < a.nc; J += kAgg) {
         const float w = row[J];
-        const float2 *rcJ = reinterpret_cast<const float2 *>(a.rc32 + (size_t)J * MB);
+        const float2 *rcJ = reinterpret_cast<const float2 *>(rcS + (size_t)J * MB);
 #pragma unroll
         for (int q = 0; q < MB / 2; ++q) {
-          const float2 tt = __ldcg(rcJ + q);
+          const float2 tt = rcJ[q];
           acc[2 * q] = fmaf(w, tt.x, acc[2 * q]);
           acc[2 * q + 1] = fmaf(w, tt.y, acc[2 * q + 1]);
         }
       }
     }
-#pragma unroll
-    for (int m = 0; m < MB; ++m) {
-      float s = acc[m];
-#pragma unroll
-      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) sagg[m][wid] = s;
+    {
+      constexpr int SH = MB == 8 ? 2 : (MB == 4 ? 3 : 4);
+      const float tot = warp_transpose_sum<float, MB>(acc);   // lane L: member L >> SH
+      if ((lane & ((1 << SH) - 1)) == 0) sagg[lane >> SH][wid] = tot;
     }
     __syncthreads();
-    if (tid < kCGThreads / kAgg)
-      for (int m = 0; m < MB; ++m) sec[m][tid] = sagg[m][2 * tid] + sagg[m][2 * tid + 1];
+    if (tid < (kCGThreads / kAgg) * MB) {
+      const int gg = tid / MB, m = tid % MB;
+      sec[m][gg] = sagg[m][2 * gg] + sagg[m][2 * gg + 1];
+    }
     __syncthreads();
 #pragma unroll
     for (int m = 0; m < MB; ++m) uu[m] += sec[m][g];
+  };
+  // block sums of v over this block's aggregates, written to out[I * MB + m]
+  auto aggregate_sums = [&](const float (&v)[MB], float *out) {
+    const int lane = tid & 31, wid = tid >> 5;
+    float w[MB];
+#pragma unroll
+    for (int m = 0; m < MB; ++m) w[m] = active ? v[m] : 0.f;
+    constexpr int SH = MB == 8 ? 2 : (MB == 4 ? 3 : 4);
+    const float tot = warp_transpose_sum<float, MB>(w);
+    if ((lane & ((1 << SH) - 1)) == 0) sagg[lane >> SH][wid] = tot;
+    __syncthreads();
+    if (tid < (kCGThreads / kAgg) * MB) {
+      const int gg = tid / MB, m = tid % MB;
+      const int I = blockIdx.x * (kCGThreads / kAgg) + gg;
+      if (I < a.nc) out[(size_t)I * MB + m] = sagg[m][2 * gg] + sagg[m][2 * gg + 1];
+    }
+  };
+  auto precond32 = [&](const float (&rr)[MB], float (&uu)[MB]) -> bool {
+#pragma unroll
+    for (int m = 0; m < MB; ++m) uu[m] = dinv32 * rr[m];
+    if (!a.coarse) return true;
+    aggregate_sums(rr, a.rc32);
+    if (!arrive_wait(a, ++epoch)) return false;
+    for (int e = tid; e < a.nc * MB; e += kCGThreads) {
+      rcS[e] = __ldcg(a.rc32 + e);
+      RsS[e] = 0.f;
+    }
+    __syncthreads();
+    coarse_add(uu);
     return true;
   };
   // ---- centre b (Neumann), projection warm start (FP64) ----
@@ -1094,7 +1180,8 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
       if (!(rn == rn)) st = 2;
       s_out[tid] = st;
       // inner target: the reduction still needed (with margin), but at least eta
-      s_itol[tid] = fmax(0.5 * s_tol[tid], (double)a.eta * sqrt(rn));
+      const double itol = fmax(0.5 * s_tol[tid], (double)a.eta * sqrt(rn));
+      s_itol2[tid] = itol * itol;
     }
     __syncthreads();
     int open = 0;
@@ -1110,40 +1197,68 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
       ui[m] = pi[m] = si[m] = wi[m] = di[m] = 0.f;
     }
     if (!precond32(ri, ui)) return;
-    if (active)
+    // publish u (global for the other blocks, shared for this block's rows)
+    auto publish = [&]() {
+      if (active)
 #pragma unroll
-      for (int q = 0; q < MB / 2; ++q)
-        reinterpret_cast<float2 *>(a.z32 + (size_t)r * MB)[q] = make_float2(ui[2 * q], ui[2 * q + 1]);
-    if (tid < MB) { s_al[tid] = 0.0; s_ga[tid] = 0.0; s_be[tid] = 0.0; s_st[tid] = s_out[tid] == 0 ? 0 : 1; }
-    if (!arrive_wait(a, ++epoch)) return;
+        for (int q = 0; q < MB / 2; ++q) {
+          const float2 t = make_float2(ui[2 * q], ui[2 * q + 1]);
+          reinterpret_cast<float2 *>(a.z32 + (size_t)r * MB)[q] = t;
+          reinterpret_cast<float2 *>(suS + (size_t)tid * MB)[q] = t;
+        }
+      else
+#pragma unroll
+        for (int q = 0; q < MB / 2; ++q) reinterpret_cast<float2 *>(suS + (size_t)tid * MB)[q] = make_float2(0.f, 0.f);
+    };
+    publish();
+    if (tid < MB) { s_al[tid] = 0.f; s_ga[tid] = 0.f; s_be[tid] = 0.f; s_st[tid] = s_out[tid] == 0 ? 0 : 1; }
+    arrive(a);
+    apply32_local(wi);
+    if (!wait_epoch(a, ++epoch)) return;
     int iit = 0;
     for (;;) {
       {
         float v[3 * MB];
-        apply32(a.z32, wi);
+        apply32_halo(a.z32, wi);
 #pragma unroll
         for (int m = 0; m < MB; ++m) {
           v[3 * m] = active ? ri[m] * ui[m] : 0.f;
           v[3 * m + 1] = active ? wi[m] * ui[m] : 0.f;
           v[3 * m + 2] = active ? ri[m] * ri[m] : 0.f;
         }
+        if (a.coarse) aggregate_sums(wi, a.rw32);   // R w rides on the reduction's barrier
         if (!reduce_all_f<3 * MB>(a, ++epoch, v, smemf, sres)) return;
       }
+      // this thread's share of every aggregate's R w, loaded while the scalars are formed
+      float4 rwq[kRwPer];
+      if (a.coarse)
+#pragma unroll
+        for (int q = 0; q < kRwPer; ++q) {
+          const int e4 = tid + q * kCGThreads;
+          rwq[q] = e4 * 4 < a.nc * MB ? __ldcg(reinterpret_cast<const float4 *>(a.rw32) + e4)
+                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
       {
-        const int m = tid >> 5;
+        const int m = tid >> 5;   // lane 0 of warp m: member m's scalars (FP32, like the vectors)
         if ((tid & 31) == 0 && m < MB) {
           int st = s_st[m];
-          double be = 0.0, al = s_al[m];
+          float be = 0.f, al = s_al[m];
           const double t0 = sres[3 * m], t1 = sres[3 * m + 1], t2 = sres[3 * m + 2];
+          const float f0 = (float)t0, f1 = (float)t1;
           if (st == 0) {
             if (!(t2 == t2) || isinf(t2)) st = 2;
-            else if (sqrt(t2) <= s_itol[m] || !(t1 > 0.0)) st = 1;
+            else if (t2 <= s_itol2[m] || !(f1 > 0.f)) st = 1;
             else if (it + iit >= a.maxits) st = 2;
           }
           if (st == 0) {
-            if (iit == 0) al = t0 / t1;
-            else { be = t0 / s_ga[m]; al = t0 / (t1 - be * t0 / s_al[m]); }
-            s_ga[m] = t0;
+            if (iit == 0) al = f0 / f1;
+            else {
+              be = f0 / s_ga[m];
+              const float den = f1 - be * f0 / s_al[m];
+              if (den > 0.f) al = f0 / den;
+              else st = 1;   // lost positivity in FP32: end this inner solve, the FP64 loop continues
+            }
+            s_ga[m] = f0;
           }
           s_al[m] = al; s_be[m] = be; s_st[m] = st;
         }
@@ -1153,24 +1268,42 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
 #pragma unroll
       for (int m = 0; m < MB; ++m) { running += s_st[m] == 0; failed = failed || s_st[m] == 2; }
       if (running == 0) break;
+      if (a.coarse) {   // R s = R w + beta R s, R r -= alpha R s (every aggregate, every block)
+#pragma unroll
+        for (int q = 0; q < kRwPer; ++q) {
+          const int e4 = tid + q * kCGThreads;
+          if (e4 * 4 >= a.nc * MB) continue;
+          const float rw[4] = {rwq[q].x, rwq[q].y, rwq[q].z, rwq[q].w};
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int e = 4 * e4 + c, m = e & (MB - 1);
+            if (e >= a.nc * MB || s_st[m] != 0) continue;
+            const float rs = fmaf(s_be[m], RsS[e], rw[c]);
+            RsS[e] = rs;
+            rcS[e] = fmaf(-s_al[m], rs, rcS[e]);
+          }
+        }
+        __syncthreads();
+      }
       if (active) {
 #pragma unroll
         for (int m = 0; m < MB; ++m) {
           if (s_st[m] != 0) continue;
-          const float al = (float)s_al[m], be = (float)s_be[m];
+          const float al = s_al[m], be = s_be[m];
           pi[m] = fmaf(be, pi[m], ui[m]);
           si[m] = fmaf(be, si[m], wi[m]);
           di[m] = fmaf(al, pi[m], di[m]);
           ri[m] = fmaf(-al, si[m], ri[m]);
         }
       }
-      if (!precond32(ri, ui)) return;
-      if (active)
 #pragma unroll
-        for (int q = 0; q < MB / 2; ++q)
-          reinterpret_cast<float2 *>(a.z32 + (size_t)r * MB)[q] = make_float2(ui[2 * q], ui[2 * q + 1]);
+      for (int m = 0; m < MB; ++m) ui[m] = dinv32 * ri[m];
+      if (a.coarse) coarse_add(ui);
+      publish();
       ++iit;
-      if (!arrive_wait(a, ++epoch)) return;
+      arrive(a);
+      apply32_local(wi);
+      if (!wait_epoch(a, ++epoch)) return;
     }
     it += iit;
     if (failed) break;
@@ -1820,7 +1953,7 @@ __global__ void k_add(int n, const double *__restrict__ a, const double *__restr
 struct NodeArgs {
   int N, nnz, do_demag, nrep;   // nrep members: m, h_ext and outputs member-major (3N each), phi N each
   const int32_t *row_ptr, *col_idx;
-  const double *K, *G, *vol, *m, *phi, *h_ext;
+  const double *K, *G, *ivol, *m, *phi, *h_ext;   // ivol: 1 / box volume
   const double *anis_node;   // per-node anisotropy coefficient (element parameters) or null
   double c_exch, C1, C2, C3, K1, anis, ax, ay, az;
   double *h_exch, *h_demag, *h_anis, *h_total, *dmdt;
@@ -1845,9 +1978,10 @@ __global__ void k_heff_llg(NodeArgs a) {
       g0 += a.G[k] * pj; g1 += a.G[(size_t)a.nnz + k] * pj; g2 += a.G[2 * (size_t)a.nnz + k] * pj;
     }
   }
-  const double V = a.vol[i];
-  const double hx[3] = {-a.c_exch * s0 / V, -a.c_exch * s1 / V, -a.c_exch * s2 / V};
-  const double hd[3] = {-g0 / V, -g1 / V, -g2 / V};
+  const double iv = a.ivol[i];
+  const double ce = -a.c_exch * iv;
+  const double hx[3] = {ce * s0, ce * s1, ce * s2};
+  const double hd[3] = {-g0 * iv, -g1 * iv, -g2 * iv};
   const double *m = mm + 3 * (size_t)i;
   double ha[3] = {0.0, 0.0, 0.0};
   if (a.K1 != 0.0 || a.anis_node) {
@@ -2044,6 +2178,7 @@ int build_cg_ordering(nmg_handle *h, std::string &err) {
     std::vector<float> a32(Ainv.begin(), Ainv.end());
     NMG_CUDA_TRY(W.ainv32.alloc((size_t)nc * nc), "alloc coarse inverse (FP32)");
     NMG_CUDA_TRY(W.rc32.alloc((size_t)nc * kChunk), "alloc");
+    NMG_CUDA_TRY(W.rw32.alloc((size_t)nc * kChunk), "alloc");
     NMG_CUDA_TRY(cudaMemcpy(W.ainv32.p, a32.data(), sizeof(float) * nc * nc, cudaMemcpyHostToDevice), "h2d");
   }
   W.nc = nc;
@@ -2104,7 +2239,7 @@ int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm,
   a.perm = W.perm; a.prow = W.prow; a.pcol = W.pcol; a.pbnd = W.pbnd; a.pK = W.pK; a.xperm = W.xperm;
   a.coarse = (mode == 0 && W.nc > 0) ? 1 : 0;
   a.nc = W.nc; a.ainv = W.ainv; a.rc = W.rc;
-  a.ainv32 = W.ainv32; a.rc32 = W.rc32; a.z32 = W.z32;
+  a.ainv32 = W.ainv32; a.rc32 = W.rc32; a.z32 = W.z32; a.rw32 = W.rw32;
   a.eta = 1e-3f; a.max_outer = 10;
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
   int cap = W.cg_nnz_cap;
@@ -2212,7 +2347,11 @@ int init_workspace(nmg_handle *h, std::string &err) {
             std::to_string(per_sm * h->sm_count * kCGThreads) + " nodes here)";
       return 4;
     }
-    W.cg_smem_mp = cap * (int)(sizeof(double) + sizeof(int) + sizeof(float));
+    // CSR (FP64 + FP32 values, columns), the block's u, and with the coarse
+    // level the whole coarse residual and its direction term plus this
+    // block's rows of the coarse inverse (FP32)
+    W.cg_smem_mp = cap * (int)(sizeof(double) + sizeof(int) + sizeof(float)) +
+                   (int)sizeof(float) * (kCGThreads * kChunk + (W.nc > 0 ? 2 * W.nc * kChunk + (kCGThreads / kAgg) * W.nc : 0));
     const bool mp = h->opt.cg_precision == 1;
     if ((B > 1 || mp) && h->opt.do_demag) {
       // the ensemble / mixed-precision CG kernels: up to kChunk members per row
@@ -2220,6 +2359,11 @@ int init_workspace(nmg_handle *h, std::string &err) {
                             mp ? (const void *)k_cgm_mp<4> : (const void *)k_cgm<4>,
                             mp ? (const void *)k_cgm_mp<8> : (const void *)k_cgm<8>};
       const int smem_need = mp ? W.cg_smem_mp : W.cg_smem_bytes;
+      if (mp && W.nc * kChunk > kRwPer * 4 * kCGThreads) {
+        err = "mesh too large for the mixed-precision CG (" + std::to_string(W.nc) + " aggregates, at most " +
+              std::to_string(kRwPer * 4 * kCGThreads / kChunk) + ")";
+        return 4;
+      }
       for (const void *fn : fns) {
         int per = 0;
         if (smem_need > 160 * 1024 ||
@@ -2509,7 +2653,7 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
   }
   NodeArgs a;
   a.N = N; a.nnz = M.nnz; a.do_demag = (h->opt.do_demag && M.nb > 0) ? 1 : 0; a.nrep = B;
-  a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.K = h->exch_K(); a.G = M.G; a.vol = M.vol;
+  a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.K = h->exch_K(); a.G = M.G; a.ivol = M.ivol;
   a.m = d_m; a.phi = W.phi; a.h_ext = W.h_ext;
   a.anis_node = h->ep.active ? h->ep.anis.p : nullptr;
   a.c_exch = mt.exch_coeff; a.C1 = mt.C1; a.C2 = mt.C2; a.C3 = mt.C3; a.K1 = mt.K1; a.anis = mt.anis_coeff;
