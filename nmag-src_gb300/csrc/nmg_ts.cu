@@ -209,7 +209,7 @@ __global__ void k_mdot(int n, int nv, VecPtrs V, const double *__restrict__ w, d
 // of blocks [c * nblocks / 8, (c + 1) * nblocks / 8) in order, then thread k
 // adds the 8 chunk sums in order.
 __global__ void __launch_bounds__(256) k_mdot_final(int nblocks, int nv, const double *__restrict__ part,
-                                                    double *__restrict__ h) {
+                                                    double *__restrict__ h, double *__restrict__ hcol, int first) {
   __shared__ double sc[8][32];
   const int k = threadIdx.x & 31, c = threadIdx.x >> 5;
   const int b0 = (int)((long long)c * nblocks / 8), b1 = (int)((long long)(c + 1) * nblocks / 8);
@@ -225,6 +225,7 @@ __global__ void __launch_bounds__(256) k_mdot_final(int nblocks, int nv, const d
 #pragma unroll
     for (int cc = 0; cc < 8; ++cc) t += sc[cc][threadIdx.x];
     h[threadIdx.x] = t;
+    hcol[threadIdx.x] = first ? t : hcol[threadIdx.x] + t;   // the Hessenberg column, summed over the passes
   }
 }
 template <int NVM>
@@ -260,6 +261,40 @@ void launch_axpy_multi(int n, int nv, const VecPtrs &vp, const Coef32 &c, double
   else if (nv <= 16) k_axpy_multi<16><<<g, 256, 0, st>>>(n, nv, vp, c, x);
   else k_axpy_multi<32><<<g, 256, 0, st>>>(n, nv, vp, c, x);
 }
+// k_orth followed by the block partials of |w|^2, in k_red's grid, order and
+// tree (mode 1), so the norm is the same number k_red would give.
+template <int NVM>
+__global__ void k_orth_norm(int n, int nv, VecPtrs V, const double *__restrict__ h, double *__restrict__ w,
+                            double *__restrict__ part) {
+  __shared__ double hs[32], sm[32];
+  if (threadIdx.x < nv) hs[threadIdx.x] = h[threadIdx.x];
+  __syncthreads();
+  double acc = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double s = w[i];
+#pragma unroll
+    for (int k = 0; k < NVM; ++k) if (k < nv) s -= hs[k] * V.v[k][i];
+    w[i] = s;
+    const double v = s * s;
+    acc += v;
+  }
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) t = t + sm[wv];
+    part[blockIdx.x] = t;
+  }
+}
+void launch_orth_norm(int n, int nv, const VecPtrs &vp, const double *h, double *w, double *part, cudaStream_t st) {
+  if (nv <= 1) k_orth_norm<1><<<kRedBlocks, 256, 0, st>>>(n, nv, vp, h, w, part);
+  else if (nv <= 2) k_orth_norm<2><<<kRedBlocks, 256, 0, st>>>(n, nv, vp, h, w, part);
+  else if (nv <= 4) k_orth_norm<4><<<kRedBlocks, 256, 0, st>>>(n, nv, vp, h, w, part);
+  else if (nv <= 8) k_orth_norm<8><<<kRedBlocks, 256, 0, st>>>(n, nv, vp, h, w, part);
+  else if (nv <= 16) k_orth_norm<16><<<kRedBlocks, 256, 0, st>>>(n, nv, vp, h, w, part);
+  else k_orth_norm<32><<<kRedBlocks, 256, 0, st>>>(n, nv, vp, h, w, part);
+}
 // k_orth<NVM> for the smallest NVM >= nv
 void launch_orth(int n, int nv, const VecPtrs &vp, const double *h, double *w, cudaStream_t st) {
   const int g = nblk(n, 256);
@@ -270,10 +305,6 @@ void launch_orth(int n, int nv, const VecPtrs &vp, const double *h, double *w, c
   else if (nv <= 16) k_orth<16><<<g, 256, 0, st>>>(n, nv, vp, h, w);
   else k_orth<32><<<g, 256, 0, st>>>(n, nv, vp, h, w);
 }
-__global__ void k_hacc(int nv, const double *__restrict__ h, double *__restrict__ hcol, int first) {
-  int k = threadIdx.x;
-  if (k < nv) hcol[k] = first ? h[k] : hcol[k] + h[k];
-}
 
 // J v with frozen (mJ, HJ), fused with  w = t - gamma J t  and the block-Jacobi
 // preconditioner and the ewt scaling:  out = ewt * P^{-1} (t - gamma J t),
@@ -283,6 +314,7 @@ struct JvArgs {
   const int32_t *row_ptr, *col_idx, *diag_pos;
   const double *K, *ivol, *mJ, *HJ, *t, *ewt;
   const double *Pinv;   // per node and member: inverse of the 3x3 preconditioner block (row-major)
+  const double *ws;     // non-null: the vector is t * ws (the GMRES basis vector over the error weights)
   double c_exch, C1, C2, gamma, gammap;
   int psolve, scale_out;
   double *out;
@@ -312,15 +344,21 @@ __global__ void k_jv_psolve(JvArgs a) {
   if (g >= (long long)a.N * a.nrep) return;
   const int mbr = (int)(g / a.N), i = (int)(g - (long long)mbr * a.N);
   const double *tm = a.t + (size_t)mbr * 3 * a.N;
+  const double *wsm = a.ws ? a.ws + (size_t)mbr * 3 * a.N : nullptr;
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
   for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; ++k) {
-    const double *tj = tm + 3 * (size_t)a.col_idx[k];
+    const size_t j3 = 3 * (size_t)a.col_idx[k];
+    const double *tj = tm + j3;
+    double t0 = tj[0], t1 = tj[1], t2 = tj[2];
+    if (wsm) { t0 *= wsm[j3]; t1 *= wsm[j3 + 1]; t2 *= wsm[j3 + 2]; }
     double kv = a.K[k];
-    s0 += kv * tj[0]; s1 += kv * tj[1]; s2 += kv * tj[2];
+    s0 += kv * t0; s1 += kv * t1; s2 += kv * t2;
   }
   const double ce = -a.c_exch * a.ivol[i];
   const double hv[3] = {ce * s0, ce * s1, ce * s2};
-  const double *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g, *w = a.t + 3 * (size_t)g;
+  const double *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g;
+  double w[3] = {a.t[3 * (size_t)g], a.t[3 * (size_t)g + 1], a.t[3 * (size_t)g + 2]};
+  if (a.ws) for (int d = 0; d < 3; ++d) w[d] *= a.ws[3 * (size_t)g + d];
   double jw[3];
   jac_apply(m, H, w, hv, a.C1, a.C2, jw);
   double r[3] = {w[0] - a.gamma * jw[0], w[1] - a.gamma * jw[1], w[2] - a.gamma * jw[2]};
@@ -382,7 +420,7 @@ struct Integrator {
   nmg_handle *hd;
   int n, qmax, maxl;
   double rtol, atol;
-  DevBuf<double> znbuf, ewt, acor, y, tempv, ftemp, xsol, mJ, HJ, Vbuf, tvec, part, hdev, hcol;
+  DevBuf<double> znbuf, ewt, acor, y, tempv, ftemp, xsol, mJ, HJ, Vbuf, part, hdev, hcol;
   DevBuf<double> Pinv;   // preconditioner blocks inverted at each setup (9 per node and member)
   DevBuf<double> ewts;   // 1 / ewt
   double *zn[QMAXB + 2];
@@ -479,7 +517,7 @@ JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
   const Mesh &M = I.hd->mesh;
   JvArgs a;
   a.N = M.N; a.nrep = I.hd->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.ivol = M.ivol;
-  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv;
+  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv; a.ws = nullptr;
   a.c_exch = I.hd->mat.exch_coeff; a.C1 = I.hd->mat.C1; a.C2 = I.hd->mat.C2;
   a.gamma = I.gamma; a.gammap = I.gammap; a.psolve = psolve; a.scale_out = 1; a.out = out;
   return a;
@@ -487,7 +525,10 @@ JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
 
 // Gram-Schmidt of w against V[0..nv): two classical passes (CGS2); the
 // coefficients stay on the device in hcol.
-void orthogonalise(Integrator &I, int nv, double *w) {
+// Returns true when the second pass also left the block partials of |w|^2
+// in I.part (nv <= 32: one chunk).
+bool orthogonalise(Integrator &I, int nv, double *w) {
+  bool normed = false;
   for (int pass = 0; pass < 2; ++pass) {
     for (int k0 = 0; k0 < nv; k0 += 32) {
       int cnt = nv - k0 < 32 ? nv - k0 : 32;
@@ -500,16 +541,23 @@ void orthogonalise(Integrator &I, int nv, double *w) {
       else if (cnt <= 16) k_mdot<16><<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part);
       else k_mdot<32><<<kRedBlocks, 256, 0, I.s()>>>(I.n, cnt, vp, w, I.part);
       ++I.hd->launches;
-      k_mdot_final<<<1, 256, 0, I.s()>>>(kRedBlocks, cnt, I.part, I.hdev.p + k0); ++I.hd->launches;
+      k_mdot_final<<<1, 256, 0, I.s()>>>(kRedBlocks, cnt, I.part, I.hdev.p + k0, I.hcol.p + k0, pass == 0);
+      ++I.hd->launches;
     }
     for (int k0 = 0; k0 < nv; k0 += 32) {
       int cnt = nv - k0 < 32 ? nv - k0 : 32;
       VecPtrs vp;
       for (int k = 0; k < cnt; ++k) vp.v[k] = I.V[k0 + k];
-      launch_orth(I.n, cnt, vp, I.hdev.p + k0, w, I.s()); ++I.hd->launches;
-      k_hacc<<<1, 32, 0, I.s()>>>(cnt, I.hdev.p + k0, I.hcol.p + k0, pass == 0); ++I.hd->launches;
+      if (pass == 1 && nv <= 32) {
+        launch_orth_norm(I.n, cnt, vp, I.hdev.p + k0, w, I.part, I.s());
+        normed = true;
+      } else {
+        launch_orth(I.n, cnt, vp, I.hdev.p + k0, w, I.s());
+      }
+      ++I.hd->launches;
     }
   }
+  return normed;
 }
 
 // SPGMR, left preconditioned, scaled by ewt; x = 0 initial guess.
@@ -540,16 +588,18 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
   I.yg[0] = rho;
   int converged = 0, kdim = 0;
   for (int l = 0; l < maxl; ++l) {
-    k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewts, I.tvec); ++I.hd->launches;
-    JvArgs a = jv_args(I, I.tvec, I.V[l + 1], 1);
+    JvArgs a = jv_args(I, I.V[l], I.V[l + 1], 1);   // t = V_l / ewt formed inside the kernel
+    a.ws = I.ewts;
     {
       NMG_PROF_BEGIN(I.hd, 4);
       k_jv_psolve<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(a); ++I.hd->launches;
       NMG_PROF_END(I.hd);
     }
     I.njv++; I.nps++;
-    orthogonalise(I, l + 1, I.V[l + 1]);
-    k_red<<<kRedBlocks, 256, 0, I.s()>>>(n, 1, I.V[l + 1], I.V[l + 1], I.part); ++I.hd->launches;
+    if (!orthogonalise(I, l + 1, I.V[l + 1])) {
+      k_red<<<kRedBlocks, 256, 0, I.s()>>>(n, 1, I.V[l + 1], I.V[l + 1], I.part);
+      ++I.hd->launches;
+    }
     cudaMemcpyAsync(I.hpin, I.hcol.p, sizeof(double) * (l + 1), cudaMemcpyDeviceToHost, I.s());
     double *hp2 = I.hpin + maxl + 1;
     cudaMemcpyAsync(hp2, I.part.p, sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, I.s());
@@ -903,7 +953,7 @@ Integrator *ts_create(nmg_handle *h, int qmax, int maxl, double rtol, double ato
   I->rtol = rtol; I->atol = atol;
   const size_t n = I->n;
   bool ok = I->znbuf.alloc(n * (I->qmax + 2)) == cudaSuccess;
-  for (DevBuf<double> *b : {&I->ewt, &I->ewts, &I->acor, &I->y, &I->tempv, &I->ftemp, &I->xsol, &I->mJ, &I->HJ, &I->tvec})
+  for (DevBuf<double> *b : {&I->ewt, &I->ewts, &I->acor, &I->y, &I->tempv, &I->ftemp, &I->xsol, &I->mJ, &I->HJ})
     ok = ok && b->alloc(n) == cudaSuccess;
   ok = ok && I->Vbuf.alloc(n * (I->maxl + 1)) == cudaSuccess;
   ok = ok && I->Pinv.alloc(3 * n) == cudaSuccess;
