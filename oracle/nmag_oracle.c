@@ -4,8 +4,8 @@
  * (Fredkin-Koehler) demagnetisation with Lindholm double-layer weights,
  * exchange, uniaxial anisotropy, Zeeman and the LLG equation.
  *
- * It is the checker for the CUDA library and the CPU baseline of bench.py,
- * never part of the product.  Parity with the reference is UNPINNED (the
+ * It supplies the expected results of the CUDA library's parity tests and the
+ * CPU baseline of bench.py, never part of the product.  Parity with the reference is UNPINNED (the
  * reference cannot run here and ships no golden vectors); see the header.
  *
  * Floating-point contract: compiled with -ffp-contract=off so the per-tet

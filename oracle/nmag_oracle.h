@@ -1,7 +1,7 @@
 /*
  * nmag_oracle.h -- CPU restatement of nmag/nsim's LLG right-hand side and its
- * time integration, used ONLY as test infrastructure: the checker for the CUDA
- * library's parity tests and the timed CPU baseline of bench.py.  Nothing in
+ * time integration, used ONLY as test infrastructure: the reference results of
+ * the CUDA library's parity tests and the timed CPU baseline of bench.py.  Nothing in
  * the product links, imports or calls this code.
  *
  * Parity status: the reference (OCaml + Python 2 + PETSc 2.3.3 + SUNDIALS

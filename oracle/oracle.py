@@ -1,7 +1,8 @@
 """ctypes wrapper of the CPU oracle (oracle/_build/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's CPU-baseline leg as the checker.  The product never imports it.
+bench.py's CPU-baseline leg, to produce expected results.  The product never
+imports it.
 
 The oracle restates nsim's LLG right-hand side and CVODE-style integrator on
 the CPU (see nmag_oracle.h for the reference citations).  Parity with the
