@@ -168,6 +168,11 @@ int nmg_ts_advance(nmg_handle *h, double t_final, int exact_tstop, int64_t max_s
 /* max_i |m_i - m_prev_i| over nodes (Euclidean norm of the 3-vector); the
  * reference's mwe_norm_dist_fun (nsimexec.ml:2332-2368, fem.ml:4717-4793). */
 int nmg_max_dm(nmg_handle *h, const double *m_prev, double *out);
+/* The same distance between the current m and m at the previous call (or at
+ * the last nmg_set_m, whichever came later), without a host copy; then
+ * remembers the current m.  0 on the first call after nmg_create.  Serves
+ * the convergence check after each advance (main.py:1383-1455). */
+int nmg_max_dm_step(nmg_handle *h, double *out);
 
 /* Device-pointer entry points (pointers are CUDA device addresses, e.g. from
  * torch tensors): one RHS evaluation dmdt = f(m) on the handle's stream and

@@ -167,6 +167,10 @@ int nmg_set_m(nmg_handle *h, const double *m) {
     if (!(m[k] == m[k])) return fail(h, -4, "nmg_set_m: non-finite magnetisation");
   if (cudaMemcpyAsync(h->ws.m.p, m, sizeof(double) * 3 * h->mesh.N * h->nrep, cudaMemcpyHostToDevice, h->stream))
     return fail(h, 100, "nmg_set_m: copy failed");
+  if (h->ws.m_mark.p &&
+      cudaMemcpyAsync(h->ws.m_mark.p, h->ws.m.p, sizeof(double) * 3 * h->mesh.N * h->nrep, cudaMemcpyDeviceToDevice,
+                      h->stream))
+    return fail(h, 100, "nmg_set_m: copy failed");
   h->ts_ready = 0;
   return cudaStreamSynchronize(h->stream) == cudaSuccess ? 0 : fail(h, 100, "nmg_set_m: sync failed");
 }
@@ -280,6 +284,21 @@ int nmg_max_dm(nmg_handle *h, const double *m_prev, double *out) {
   if (tmp.alloc(3 * (size_t)h->mesh.N * h->nrep)) return 100;
   cudaMemcpyAsync(tmp.p, m_prev, sizeof(double) * 3 * h->mesh.N * h->nrep, cudaMemcpyHostToDevice, h->stream);
   return nmg::max_dm(h, h->ws.m, tmp, out);
+}
+
+int nmg_max_dm_step(nmg_handle *h, double *out) {
+  if (!h || !out) return -1;
+  const size_t n3 = 3 * (size_t)h->mesh.N * h->nrep;
+  *out = 0.0;
+  if (!h->ws.m_mark.p) {
+    if (h->ws.m_mark.alloc(n3)) return fail(h, 100, "nmg_max_dm_step: device allocation failed");
+  } else {
+    int rc = nmg::max_dm(h, h->ws.m, h->ws.m_mark, out);
+    if (rc) return fail(h, rc, "nmg_max_dm_step: reduction failed");
+  }
+  if (cudaMemcpyAsync(h->ws.m_mark.p, h->ws.m.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, h->stream))
+    return fail(h, 100, "nmg_max_dm_step: copy failed");
+  return 0;
 }
 
 int nmg_rhs_device(nmg_handle *h, const double *d_m, double *d_dmdt) {

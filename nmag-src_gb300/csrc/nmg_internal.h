@@ -99,6 +99,8 @@ struct Workspace {
   DevBuf<unsigned long long> anc_mx;
   DevBuf<int> anc_flag;
   DevBuf<long long> anc_count;
+  // m at the last nmg_max_dm_step / nmg_set_m (allocated on first use)
+  DevBuf<double> m_mark;
 };
 
 struct Integrator;

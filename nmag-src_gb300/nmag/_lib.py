@@ -56,7 +56,7 @@ class TsStats(C.Structure):
 EXPORTS = ["nmg_version", "nmg_set_device", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_mesh_info", "nmg_get_csr",
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
            "nmg_set_material", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
-           "nmg_ts_advance", "nmg_max_dm", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
+           "nmg_ts_advance", "nmg_max_dm", "nmg_max_dm_step", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
            "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_bem_anchor_stats", "nmg_max_dm_static",
            "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
            "nmg_member_averages", "nmg_batch_last_error", "nmg_batch_create", "nmg_batch_destroy", "nmg_batch_info",
@@ -109,6 +109,7 @@ def lib(build_if_missing=True):
     L.nmg_ts_init.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]
     L.nmg_ts_advance.argtypes = [vp, C.c_double, C.c_int, C.c_int64, C.POINTER(C.c_double), C.POINTER(TsStats)]
     L.nmg_max_dm.argtypes = [vp, _f64p, C.POINTER(C.c_double)]
+    L.nmg_max_dm_step.argtypes = [vp, C.POINTER(C.c_double)]
     L.nmg_rhs_device.argtypes = [vp, vp, vp]
     L.nmg_rk4_device.argtypes = [vp, vp, C.c_double, C.c_int]
     L.nmg_get_timings.argtypes = [vp, _f64p]
@@ -244,6 +245,12 @@ class Engine(object):
         out = C.c_double()
         check(lib().nmg_max_dm(self.h, np.ascontiguousarray(m_prev, dtype=np.float64).reshape(-1), C.byref(out)),
               self.h, "max_dm")
+        return out.value
+
+    def max_dm_step(self):
+        """max |m - m at the previous call or set_m| on the device (0 the first time)."""
+        out = C.c_double()
+        check(lib().nmg_max_dm_step(self.h, C.byref(out)), self.h, "max_dm_step")
         return out.value
 
     def timings(self):

@@ -172,6 +172,7 @@ class Simulation(object):
         self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
         shape = self.engine._shape3()
         self._m = np.zeros(shape)
+        self.engine.max_dm_step()   # the device's reference m for the first convergence check
         self._h_ext = np.zeros(shape)
         self._ts_ready = False
         return self.mesh
@@ -295,8 +296,10 @@ class Simulation(object):
         self.clock.stage_step += max(delta_steps, 0)
         self.clock.last_step_dt_su = stats["hcur"]
         self.last_stats = stats
+        # max |m - m before this advance| (the device remembers m at each
+        # set_m and each advance), as the reference's mwe_norm_dist_fun
+        dm = self.engine.max_dm_step()
         if prev_m is not None and delta_t > 0.0:
-            dm = np.sqrt(((self._m - prev_m) ** 2).sum(axis=-1)).max()
             self.max_dm_dt = dm / delta_t
         return SI(t_stage * simulation_units.conversion_factor_of(SI("s")), "s")
 

@@ -187,3 +187,24 @@ def test_simulation_api_advance_and_relax(small_box):
     assert sim.max_dm_dt < sim.stopping_dm_dt
     avg = sim.get_subfield_average_siv("m")
     assert avg[2] > 0.99
+
+
+def test_max_dm_step_tracks_previous_m(small_box):
+    """nmg_max_dm_step: distance to m at the previous call or set_m, on the
+    device; equal to the host computation on the same arrays."""
+    eng = make_engine(small_box, permalloy(0.5), do_demag=False)
+    n = small_box.n_nodes
+    m0 = seeded_m(n, seed=5, noise=0.3)
+    eng.set_m(m0)
+    assert eng.max_dm_step() == 0.0                      # first call: nothing to compare with
+    eng.set_h_ext(np.zeros(3))
+    eng.ts_init(0.0, 1e-6, 1e-6, 2, 300)
+    eng.ts_advance(0.5)
+    m1 = eng.get_m()
+    d = eng.max_dm_step()
+    assert d == pytest.approx(np.sqrt(((m1 - m0) ** 2).sum(1)).max(), rel=1e-15)
+    assert d > 0.0
+    assert eng.max_dm_step() == 0.0                      # nothing moved since the last call
+    m2 = seeded_m(n, seed=6, noise=0.3)
+    eng.set_m(m2)                                        # set_m becomes the reference
+    assert eng.max_dm_step() == 0.0
