@@ -314,7 +314,6 @@ struct JvArgs {
   const int32_t *row_ptr, *col_idx, *diag_pos;
   const double *K, *ivol, *mJ, *HJ, *t, *ewt;
   const double *Pinv;   // per node and member: inverse of the 3x3 preconditioner block (row-major)
-  const double *ws;     // non-null: the vector is t * ws (the GMRES basis vector over the error weights)
   double c_exch, C1, C2, gamma, gammap;
   int psolve, scale_out;
   double *out;
@@ -344,21 +343,15 @@ __global__ void k_jv_psolve(JvArgs a) {
   if (g >= (long long)a.N * a.nrep) return;
   const int mbr = (int)(g / a.N), i = (int)(g - (long long)mbr * a.N);
   const double *tm = a.t + (size_t)mbr * 3 * a.N;
-  const double *wsm = a.ws ? a.ws + (size_t)mbr * 3 * a.N : nullptr;
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
   for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; ++k) {
-    const size_t j3 = 3 * (size_t)a.col_idx[k];
-    const double *tj = tm + j3;
-    double t0 = tj[0], t1 = tj[1], t2 = tj[2];
-    if (wsm) { t0 *= wsm[j3]; t1 *= wsm[j3 + 1]; t2 *= wsm[j3 + 2]; }
+    const double *tj = tm + 3 * (size_t)a.col_idx[k];
     double kv = a.K[k];
-    s0 += kv * t0; s1 += kv * t1; s2 += kv * t2;
+    s0 += kv * tj[0]; s1 += kv * tj[1]; s2 += kv * tj[2];
   }
   const double ce = -a.c_exch * a.ivol[i];
   const double hv[3] = {ce * s0, ce * s1, ce * s2};
-  const double *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g;
-  double w[3] = {a.t[3 * (size_t)g], a.t[3 * (size_t)g + 1], a.t[3 * (size_t)g + 2]};
-  if (a.ws) for (int d = 0; d < 3; ++d) w[d] *= a.ws[3 * (size_t)g + d];
+  const double *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g, *w = a.t + 3 * (size_t)g;
   double jw[3];
   jac_apply(m, H, w, hv, a.C1, a.C2, jw);
   double r[3] = {w[0] - a.gamma * jw[0], w[1] - a.gamma * jw[1], w[2] - a.gamma * jw[2]};
@@ -420,7 +413,7 @@ struct Integrator {
   nmg_handle *hd;
   int n, qmax, maxl;
   double rtol, atol;
-  DevBuf<double> znbuf, ewt, acor, y, tempv, ftemp, xsol, mJ, HJ, Vbuf, part, hdev, hcol;
+  DevBuf<double> znbuf, ewt, acor, y, tempv, ftemp, xsol, mJ, HJ, Vbuf, tvec, part, hdev, hcol;
   DevBuf<double> Pinv;   // preconditioner blocks inverted at each setup (9 per node and member)
   DevBuf<double> ewts;   // 1 / ewt
   double *zn[QMAXB + 2];
@@ -517,7 +510,7 @@ JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
   const Mesh &M = I.hd->mesh;
   JvArgs a;
   a.N = M.N; a.nrep = I.hd->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.ivol = M.ivol;
-  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv; a.ws = nullptr;
+  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv;
   a.c_exch = I.hd->mat.exch_coeff; a.C1 = I.hd->mat.C1; a.C2 = I.hd->mat.C2;
   a.gamma = I.gamma; a.gammap = I.gammap; a.psolve = psolve; a.scale_out = 1; a.out = out;
   return a;
@@ -588,8 +581,10 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
   I.yg[0] = rho;
   int converged = 0, kdim = 0;
   for (int l = 0; l < maxl; ++l) {
-    JvArgs a = jv_args(I, I.V[l], I.V[l + 1], 1);   // t = V_l / ewt formed inside the kernel
-    a.ws = I.ewts;
+    // t = V_l / ewt in its own pass: inside the FP64-bound Jv kernel the
+    // division would be repeated for every neighbour reference
+    k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewts, I.tvec); ++I.hd->launches;
+    JvArgs a = jv_args(I, I.tvec, I.V[l + 1], 1);
     {
       NMG_PROF_BEGIN(I.hd, 4);
       k_jv_psolve<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(a); ++I.hd->launches;
@@ -953,7 +948,7 @@ Integrator *ts_create(nmg_handle *h, int qmax, int maxl, double rtol, double ato
   I->rtol = rtol; I->atol = atol;
   const size_t n = I->n;
   bool ok = I->znbuf.alloc(n * (I->qmax + 2)) == cudaSuccess;
-  for (DevBuf<double> *b : {&I->ewt, &I->ewts, &I->acor, &I->y, &I->tempv, &I->ftemp, &I->xsol, &I->mJ, &I->HJ})
+  for (DevBuf<double> *b : {&I->ewt, &I->ewts, &I->acor, &I->y, &I->tempv, &I->ftemp, &I->xsol, &I->mJ, &I->HJ, &I->tvec})
     ok = ok && b->alloc(n) == cudaSuccess;
   ok = ok && I->Vbuf.alloc(n * (I->maxl + 1)) == cudaSuccess;
   ok = ok && I->Pinv.alloc(3 * n) == cudaSuccess;

@@ -181,7 +181,7 @@ constexpr int kAgg = 64;   // rows per aggregate (4 aggregates per 256-row block
 constexpr int kRwPer = 5;
 
 // ---- single-reduction CG on a counter barrier ----
-constexpr int kCG2MaxRed = 11 * kChunk;   // widest fused reduction (projection dots + b.b per ensemble member)
+constexpr int kCG2MaxRed = 12 * kChunk;   // widest fused reduction (projection dots, b.b and sum b per member)
 
 // gpu-scope acquire load
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p) {
@@ -860,9 +860,10 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
   static_assert(MB * 32 <= kCGThreads && MB % 2 == 0, "one warp per member; member pairs");
   constexpr int P = kBasis + 1;
   extern __shared__ double dyn[];
-  __shared__ double smem[kCGThreads / 32 * RedShape<P * MB>::W];
+  __shared__ double smem[kCGThreads / 32 * RedShape<(P + 1) * MB>::W];
   __shared__ float smemf[kCGThreads / 32 * RedShape<3 * MB>::W];
-  __shared__ double sres[P * MB];
+  __shared__ double sres[(P + 1) * MB];
+  __shared__ double s_xsum[MB];   // sum of x per member at the last FP64 residual (Neumann centring)
   __shared__ double sbdot[P * MB];
   __shared__ double s_tol[MB], s_itol2[MB];
   __shared__ float s_al[MB], s_be[MB], s_ga[MB];
@@ -1103,19 +1104,14 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
     coarse_add(uu);
     return true;
   };
-  // ---- centre b (Neumann), projection warm start (FP64) ----
-  if (a.mode == 0) {
-    double v[MB];
-#pragma unroll
-    for (int m = 0; m < MB; ++m) v[m] = sbi[m][tid];
-    if (!reduce_all_to<MB>(a, ++epoch, v, smem, sres)) return;
-#pragma unroll
-    for (int m = 0; m < MB; ++m) if (active) sbi[m][tid] -= sres[m] / N;
-  }
+  // ---- projection warm start (FP64).  For the Neumann problem the sum of b
+  // rides on the same reduction: the stored right-hand sides are centred, so
+  // (b - mean) . b_j = b . b_j to rounding and |b - mean|^2 = b . b - N mean^2.
   {
-    double proj[P * MB];
+    constexpr int PP = P + 1;
+    double proj[PP * MB];
 #pragma unroll
-    for (int q = 0; q < P * MB; ++q) proj[q] = 0.0;
+    for (int q = 0; q < PP * MB; ++q) proj[q] = 0.0;
     if (active) {
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
@@ -1124,11 +1120,21 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
         const double bm = sbi[m][tid];
         const double *bb = B.b + (size_t)m * kBasis * N;
 #pragma unroll
-        for (int j = 0; j < kBasis; ++j) if (j < cnt) proj[P * m + j] = bm * bb[(size_t)j * N + r];
-        proj[P * m + kBasis] = bm * bm;
+        for (int j = 0; j < kBasis; ++j) if (j < cnt) proj[PP * m + j] = bm * bb[(size_t)j * N + r];
+        proj[PP * m + kBasis] = bm * bm;
+        proj[PP * m + kBasis + 1] = bm;
       }
     }
-    if (!reduce_all_to<P * MB>(a, ++epoch, proj, smem, sbdot)) return;
+    if (!reduce_all_to<PP * MB>(a, ++epoch, proj, smem, sres)) return;
+    for (int q = tid; q < P * MB; q += kCGThreads) {
+      const int m = q / P, j = q - m * P;
+      const double mean = a.mode == 0 ? sres[PP * m + kBasis + 1] / N : 0.0;
+      sbdot[q] = j < kBasis ? sres[PP * m + j] : sres[PP * m + kBasis] - N * mean * mean;
+    }
+    if (a.mode == 0)
+#pragma unroll
+      for (int m = 0; m < MB; ++m) if (active) sbi[m][tid] -= sres[PP * m + kBasis + 1] / N;
+    __syncthreads();
   }
   if (tid < MB) s_tol[tid] = fmax(a.rtol * sqrt(sbdot[P * tid + kBasis]), a.atol);
   {
@@ -1166,16 +1172,18 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
     {
       double ax[MB];
       apply64(a.xperm, ax);
-      double v[MB];
+      double v[2 * MB];   // |r|^2, and sum of x for the Neumann centring at the end
 #pragma unroll
       for (int m = 0; m < MB; ++m) {
         r64[m] = active ? sbi[m][tid] - ax[m] : 0.0;
         v[m] = r64[m] * r64[m];
+        v[MB + m] = (a.mode == 0 && active) ? xi[m] : 0.0;
       }
-      if (!reduce_all_to<MB>(a, ++epoch, v, smem, sres)) return;
+      if (!reduce_all_to<2 * MB>(a, ++epoch, v, smem, sres)) return;
     }
     if (tid < MB) {
       const double rn = sres[tid];
+      s_xsum[tid] = sres[MB + tid];
       int st = (tid < nm && !(sqrt(rn) <= s_tol[tid])) ? 0 : 1;
       if (!(rn == rn)) st = 2;
       s_out[tid] = st;
@@ -1311,14 +1319,9 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
     for (int m = 0; m < MB; ++m) if (s_out[m] == 0) xi[m] += (double)di[m];
   }
   __syncthreads();
-  if (a.mode == 0) {
-    double v[MB];
+  if (a.mode == 0)   // x is unchanged since the last residual reduction summed it
 #pragma unroll
-    for (int m = 0; m < MB; ++m) v[m] = active ? xi[m] : 0.0;
-    if (!reduce_all_to<MB>(a, ++epoch, v, smem, sres)) return;
-#pragma unroll
-    for (int m = 0; m < MB; ++m) xi[m] -= sres[m] / N;
-  }
+    for (int m = 0; m < MB; ++m) xi[m] -= s_xsum[m] / N;
   if (active) {
 #pragma unroll
     for (int m = 0; m < MB; ++m) {
