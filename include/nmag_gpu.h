@@ -241,7 +241,11 @@ typedef struct nmg_batch_options {
   double dt0, dt_max, fixed_dt;           /* initial / maximal step; fixed_dt > 0: no control */
   int threads;                            /* CTA size (0: 256)                           */
   double budget;                          /* work per particle per launch (0: one step)  */
-  int reserved[4];
+  int integrator;                         /* 0: Bogacki-Shampine 3(2), explicit;
+                                             1: ROS2, linearly implicit (L-stable) with
+                                                BiCGSTAB solves of I - gamma tau J    */
+  int krylov_maxits;                      /* ROS2 linear-solve cap (0: 200)              */
+  int reserved[2];
 } nmg_batch_options;
 
 typedef struct nmg_batch nmg_batch;

@@ -46,10 +46,12 @@ struct PState {
   double t, dt, hmag, maxdmdt;
   int stage, done, conv, have_k1;
   long long steps, rejects, rhs, cg_iters;
+  long long krylov_iters;   // ROS2 linear-solve iterations
 };
 
 struct BatchArgs {
   int P, n_stages, cg_maxits, adaptive;
+  int integrator, krylov_maxits;   // 0: Bogacki-Shampine 3(2); 1: ROS2 (linearly implicit)
   double hmax, rtol, atol, cg_rtol, stop_dmdt, dt_max;
   const int *order;
   int *queue;                      // next queue position (reset before each launch)
@@ -59,6 +61,8 @@ struct BatchArgs {
   const double *K, *Gx, *Gy, *Gz, *Dx, *Dy, *Dz, *vol;
   const float *bem;
   double *m, *k0, *k1, *k2, *k3, *y, *phi1, *phi2, *rho, *rhs2, *cr, *cz, *cp, *cq, *b2, *hout;
+  // ROS2: field at the step's start, 3x3 block inverses of W, Krylov vectors (3N per particle)
+  double *hn, *pinv, *kr, *krh, *kp, *kv, *ks, *kt, *kph, *ksh;
   int *err;
 };
 
@@ -363,6 +367,244 @@ __device__ void particle_run(const BatchArgs &a, int p, double *sm, float *xs, P
   }
 }
 
+// ---- linearly implicit integrator: ROS2 ----
+// The two-stage Rosenbrock W-method of Verwer, Spee, Blom and Hundsdorfer
+// (1999): gamma = 1 + 1/sqrt(2), W = I - gamma tau J,
+//   W k1 = f(y_n),  W k2 = f(y_n + tau k1) - 2 k1,
+//   y_{n+1} = y_n + tau (3/2 k1 + 1/2 k2),  error estimate tau/2 (k1 + k2).
+// It is L-stable and second order for any matrix J, so J is the exchange and
+// site linearisation of f at (y_n, H_n) with the demagnetising and
+// anisotropy fields frozen -- the Jacobian of the single-film path
+// (nsim.ml:967-1050) -- and the step is limited by accuracy, not by the
+// exchange stiffness that bounds the explicit integrator.  W k = b is solved
+// by block-level BiCGSTAB preconditioned with the 3x3 node blocks of W.
+constexpr double kRos2Gamma = 1.7071067811865475;   // 1 + 1/sqrt(2)
+
+__device__ __forceinline__ void bcross(const double *a, const double *b, double *c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+// dF = C1 (w x H + m x hv) + C2 (w x (m x H) + m x (w x H + m x hv))
+__device__ __forceinline__ void bjac(const double *m, const double *H, const double *w, const double *hv, double C1,
+                                     double C2, double *out) {
+  double wxH[3], mxhv[3], mxH[3], t1[3], u[3], t2[3];
+  bcross(w, H, wxH);
+  bcross(m, hv, mxhv);
+  bcross(m, H, mxH);
+  bcross(w, mxH, t1);
+  for (int c = 0; c < 3; ++c) u[c] = wxH[c] + mxhv[c];
+  bcross(m, u, t2);
+  for (int c = 0; c < 3; ++c) out[c] = C1 * (wxH[c] + mxhv[c]) + C2 * (t1[c] + t2[c]);
+}
+// (W x)_i = x_i - gt (J x)_i
+__device__ __forceinline__ void wapply(const PView &v, const PDesc &d, int i, const double *m, const double *H,
+                                       double gt, const double *x, double *out) {
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
+    const double *xj = x + 3 * (size_t)v.ci[k];
+    const double kv = v.K[k];
+    s0 += kv * xj[0]; s1 += kv * xj[1]; s2 += kv * xj[2];
+  }
+  const double V = v.vol[i];
+  const double hv[3] = {-d.c_exch * s0 / V, -d.c_exch * s1 / V, -d.c_exch * s2 / V};
+  double jx[3];
+  bjac(m + 3 * (size_t)i, H + 3 * (size_t)i, x + 3 * (size_t)i, hv, d.C1, d.C2, jx);
+  for (int c = 0; c < 3; ++c) out[c] = x[3 * (size_t)i + c] - gt * jx[c];
+}
+// Pinv_i = inverse of node i's 3x3 block of W (row-major, 9 values)
+__device__ void pblock(const PView &v, const PDesc &d, int i, const double *m, const double *H, double gt,
+                       double *Pi) {
+  const double kap = -d.c_exch * v.K[v.diag[i]] / v.vol[i];
+  double P[3][3];
+  for (int c = 0; c < 3; ++c) {
+    double e[3] = {0.0, 0.0, 0.0};
+    e[c] = 1.0;
+    const double he[3] = {kap * e[0], kap * e[1], kap * e[2]};
+    double je[3];
+    bjac(m + 3 * (size_t)i, H + 3 * (size_t)i, e, he, d.C1, d.C2, je);
+    for (int r = 0; r < 3; ++r) P[r][c] = (r == c ? 1.0 : 0.0) - gt * je[r];
+  }
+  const double c00 = P[1][1] * P[2][2] - P[1][2] * P[2][1];
+  const double c01 = P[1][2] * P[2][0] - P[1][0] * P[2][2];
+  const double c02 = P[1][0] * P[2][1] - P[1][1] * P[2][0];
+  const double inv = 1.0 / (P[0][0] * c00 + P[0][1] * c01 + P[0][2] * c02);
+  Pi[0] = c00 * inv; Pi[1] = (P[0][2] * P[2][1] - P[0][1] * P[2][2]) * inv; Pi[2] = (P[0][1] * P[1][2] - P[0][2] * P[1][1]) * inv;
+  Pi[3] = c01 * inv; Pi[4] = (P[0][0] * P[2][2] - P[0][2] * P[2][0]) * inv; Pi[5] = (P[0][2] * P[1][0] - P[0][0] * P[1][2]) * inv;
+  Pi[6] = c02 * inv; Pi[7] = (P[0][1] * P[2][0] - P[0][0] * P[2][1]) * inv; Pi[8] = (P[0][0] * P[1][1] - P[0][1] * P[1][0]) * inv;
+}
+__device__ __forceinline__ void pmul(const double *Pinv, int i, const double *x, double *out) {
+  const double *Pi = Pinv + 9 * (size_t)i, *xi = x + 3 * (size_t)i;
+  for (int r = 0; r < 3; ++r) out[3 * (size_t)i + r] = (Pi[3 * r] * xi[0] + Pi[3 * r + 1] * xi[1]) + Pi[3 * r + 2] * xi[2];
+}
+
+struct KrylovVecs { double *r, *rh, *p, *v, *s, *t, *ph, *sh; };
+
+// W x = b by right-preconditioned BiCGSTAB on one particle (block); x holds
+// the initial guess.  Stops at |r| <= rtol |b|; returns iterations, sets
+// *failed on breakdown or when maxits is reached.
+__device__ int block_bicgstab(const PView &v, const PDesc &d, const double *m, const double *H, double gt,
+                              const double *Pinv, const double *b, double *x, double rtol, int maxits,
+                              const KrylovVecs &K, double *sm, bool *failed) {
+  const int N = v.N, tid = threadIdx.x, nt = blockDim.x;
+  double bb = 0.0, rr = 0.0;
+  for (int i = tid; i < N; i += nt) {
+    double wx[3];
+    wapply(v, d, i, m, H, gt, x, wx);
+    for (int c = 0; c < 3; ++c) {
+      const size_t o = 3 * (size_t)i + c;
+      const double r = b[o] - wx[c];
+      K.r[o] = r; K.rh[o] = r; K.p[o] = 0.0; K.v[o] = 0.0;
+      bb += b[o] * b[o];
+      rr += r * r;
+    }
+  }
+  bsum2(bb, rr, sm);
+  const double tol = rtol * sqrt(bb);
+  double rho = 1.0, alpha = 1.0, omega = 1.0;
+  int it = 0;
+  while (sqrt(rr) > tol) {
+    if (it >= maxits || !(rr == rr)) { *failed = true; break; }
+    double rho1 = 0.0, dum = 0.0;
+    for (int o = tid; o < 3 * N; o += nt) rho1 += K.rh[o] * K.r[o];
+    bsum2(rho1, dum, sm);
+    if (rho1 == 0.0 || omega == 0.0) { *failed = true; break; }
+    const double beta = (rho1 / rho) * (alpha / omega);
+    for (int o = tid; o < 3 * N; o += nt) K.p[o] = K.r[o] + beta * (K.p[o] - omega * K.v[o]);
+    __syncthreads();
+    for (int i = tid; i < N; i += nt) pmul(Pinv, i, K.p, K.ph);
+    __syncthreads();
+    double rv = 0.0;
+    for (int i = tid; i < N; i += nt) {
+      double w[3];
+      wapply(v, d, i, m, H, gt, K.ph, w);
+      for (int c = 0; c < 3; ++c) {
+        const size_t o = 3 * (size_t)i + c;
+        K.v[o] = w[c];
+        rv += K.rh[o] * w[c];
+      }
+    }
+    bsum2(rv, dum, sm);
+    if (rv == 0.0) { *failed = true; break; }
+    alpha = rho1 / rv;
+    double ss = 0.0;
+    for (int o = tid; o < 3 * N; o += nt) {
+      const double sv = K.r[o] - alpha * K.v[o];
+      K.s[o] = sv;
+      ss += sv * sv;
+    }
+    bsum2(ss, dum, sm);
+    ++it;
+    if (sqrt(ss) <= tol) {
+      for (int o = tid; o < 3 * N; o += nt) x[o] += alpha * K.ph[o];
+      rr = ss;
+      __syncthreads();
+      break;
+    }
+    for (int i = tid; i < N; i += nt) pmul(Pinv, i, K.s, K.sh);
+    __syncthreads();
+    double ts = 0.0, tt = 0.0;
+    for (int i = tid; i < N; i += nt) {
+      double w[3];
+      wapply(v, d, i, m, H, gt, K.sh, w);
+      for (int c = 0; c < 3; ++c) {
+        const size_t o = 3 * (size_t)i + c;
+        K.t[o] = w[c];
+        ts += w[c] * K.s[o];
+        tt += w[c] * w[c];
+      }
+    }
+    bsum2(ts, tt, sm);
+    omega = tt > 0.0 ? ts / tt : 0.0;
+    double rn = 0.0;
+    for (int o = tid; o < 3 * N; o += nt) {
+      x[o] += alpha * K.ph[o] + omega * K.sh[o];
+      const double r = K.s[o] - omega * K.t[o];
+      K.r[o] = r;
+      rn += r * r;
+    }
+    bsum2(rn, dum, sm);
+    rr = rn;
+    rho = rho1;
+  }
+  __syncthreads();
+  return it;
+}
+
+// Up to d.steps_cap ROS2 steps (with the hysteresis stage logic) for particle p.
+__device__ void particle_run_ros2(const BatchArgs &a, int p, double *sm, float *xs, PState &st) {
+  const PDesc d = a.desc[p];
+  const PView v = view(a, p, d);
+  const int n3 = 3 * d.N, N = d.N, tid = threadIdx.x, nt = blockDim.x;
+  const size_t o3 = 3 * (size_t)d.on;
+  double *m = a.m + o3, *f0 = a.k0 + o3, *k1 = a.k1 + o3, *k2 = a.k2 + o3, *f1 = a.k3 + o3, *y = a.y + o3;
+  double *H = a.hn + o3, *Pinv = a.pinv + 3 * o3;
+  const KrylovVecs K = {a.kr + o3, a.krh + o3, a.kp + o3, a.kv + o3, a.ks + o3, a.kt + o3, a.kph + o3, a.ksh + o3};
+  const double krtol = 1e-3 * fmin(a.rtol, a.atol) > 1e-12 ? 1e-3 * fmin(a.rtol, a.atol) : 1e-12;
+  bool failed = false;
+  for (int s = 0; s < d.steps_cap && !st.done; ++s) {
+    if (!st.have_k1) {   // f and H at the step's start (after a new field of the sweep)
+      prhs(a, p, d, v, st.hmag, m, f0, H, sm, xs, st, &failed);
+      st.have_k1 = 1;
+    }
+    const double tau = st.dt, gt = kRos2Gamma * tau;
+    for (int i = tid; i < N; i += nt) pblock(v, d, i, m, H, gt, Pinv + 9 * (size_t)i);
+    for (int o = tid; o < n3; o += nt) k1[o] = f0[o];
+    __syncthreads();
+    st.krylov_iters += block_bicgstab(v, d, m, H, gt, Pinv, f0, k1, krtol, a.krylov_maxits, K, sm, &failed);
+    for (int o = tid; o < n3; o += nt) y[o] = m[o] + tau * k1[o];
+    __syncthreads();
+    prhs(a, p, d, v, st.hmag, y, f1, nullptr, sm, xs, st, &failed);
+    for (int o = tid; o < n3; o += nt) {
+      f1[o] -= 2.0 * k1[o];
+      k2[o] = f1[o];
+    }
+    __syncthreads();
+    st.krylov_iters += block_bicgstab(v, d, m, H, gt, Pinv, f1, k2, krtol, a.krylov_maxits, K, sm, &failed);
+    double en = 0.0;
+    for (int o = tid; o < n3; o += nt) {
+      const double yn = m[o] + tau * (1.5 * k1[o] + 0.5 * k2[o]);
+      y[o] = yn;
+      if (a.adaptive) en = fmax(en, fabs(0.5 * tau * (k1[o] + k2[o])) / (a.atol + a.rtol * fmax(fabs(m[o]), fabs(yn))));
+    }
+    if (a.adaptive) en = bmax(en, sm);
+    else __syncthreads();
+    if (failed || !(en == en)) {
+      if (tid == 0) atomicOr(a.err, failed ? ERR_CG_MAXITS : ERR_NONFINITE);
+      st.done = 1;
+      break;
+    }
+    if (en <= 1.0) {   // accept: m <- y, then f and H there (the next step's start)
+      for (int o = tid; o < n3; o += nt) m[o] = y[o];
+      __syncthreads();
+      prhs(a, p, d, v, st.hmag, m, f0, H, sm, xs, st, &failed);
+      double mx = 0.0;
+      for (int i = tid; i < N; i += nt) {
+        const double *f = f0 + 3 * (size_t)i;
+        mx = fmax(mx, sqrt((f[0] * f[0] + f[1] * f[1]) + f[2] * f[2]));
+      }
+      mx = bmax(mx, sm);
+      st.t += tau;
+      st.steps++;
+      st.maxdmdt = mx;
+      st.conv = mx < a.stop_dmdt ? st.conv + 1 : 0;
+      if (st.conv >= 2) {
+        st.conv = 0;
+        st.stage++;
+        if (st.stage >= a.n_stages) st.done = 1;
+        else { st.hmag = stage_field(a, st.stage); st.have_k1 = 0; }
+      }
+    } else {
+      st.rejects++;
+    }
+    if (a.adaptive) {   // first-order error estimate
+      const double fac = en > 0.0 ? 0.9 * sqrt(1.0 / en) : 5.0;
+      st.dt = fmin(a.dt_max, tau * fmin(5.0, fmax(0.2, fac)));
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_batch_run(BatchArgs a) {
   extern __shared__ float xs[];
   __shared__ double sm[2 * kMaxWarps];
@@ -379,7 +621,10 @@ __global__ void k_batch_run(BatchArgs a) {
     if (p < 0) break;
     // every thread works on a private copy of the scalars; thread 0's is stored
     PState mine = st;
-    if (!mine.done) particle_run(a, p, sm, xs, mine);
+    if (!mine.done) {
+      if (a.integrator == 1) particle_run_ros2(a, p, sm, xs, mine);
+      else particle_run(a, p, sm, xs, mine);
+    }
     __syncthreads();
     if (threadIdx.x == 0) a.st[p] = mine;
     __syncthreads();
@@ -426,6 +671,7 @@ struct nmg_batch {
   nmg::DevBuf<double> K, Gx, Gy, Gz, Dx, Dy, Dz, vol;
   nmg::DevBuf<float> bem;
   nmg::DevBuf<double> m, k0, k1, k2, k3, y, phi1, phi2, rho, rhs2, cr, cz, cp, cq, b2, hout, dmdt;
+  nmg::DevBuf<double> hn, pinv, kr, krh, kp, kv, ks, kt, kph, ksh;   // ROS2 integrator only
   nmg::DevBuf<nmg::PDesc> desc;
   nmg::DevBuf<nmg::PState> st;
   nmg::DevBuf<int> err;
@@ -452,6 +698,10 @@ int bfail(nmg_batch *b, int code, const std::string &msg) {
 nmg::BatchArgs nmg_batch::args() const {
   nmg::BatchArgs a{};
   a.P = P; a.n_stages = opt.n_stages; a.cg_maxits = opt.cg_maxits; a.adaptive = opt.fixed_dt > 0.0 ? 0 : 1;
+  a.integrator = opt.integrator;
+  a.krylov_maxits = opt.krylov_maxits > 0 ? opt.krylov_maxits : 200;
+  a.hn = hn; a.pinv = pinv; a.kr = kr; a.krh = krh; a.kp = kp; a.kv = kv; a.ks = ks; a.kt = kt; a.kph = kph;
+  a.ksh = ksh;
   a.hmax = opt.h_max; a.rtol = opt.rtol; a.atol = opt.atol; a.cg_rtol = opt.cg_rtol;
   a.stop_dmdt = opt.stop_dmdt; a.dt_max = opt.dt_max;
   a.order = order; a.queue = queue; a.desc = desc; a.st = st;
@@ -529,6 +779,8 @@ int nmg_batch_create(const nmg_particle *parts, int n, const nmg_batch_options *
   *out = nullptr;
   if (opt->n_stages < 1 || opt->cg_maxits < 1 || !(opt->cg_rtol > 0.0))
     return bfail(nullptr, -2, "nmg_batch_create: need n_stages >= 1, cg_maxits >= 1, cg_rtol > 0");
+  if (opt->integrator < 0 || opt->integrator > 1 || opt->krylov_maxits < 0)
+    return bfail(nullptr, -2, "nmg_batch_create: integrator must be 0 (Bogacki-Shampine) or 1 (ROS2)");
   nmg_batch *b = new nmg_batch();
   b->P = n;
   b->opt = *opt;
@@ -654,6 +906,11 @@ int nmg_batch_create(const nmg_particle *parts, int n, const nmg_batch_options *
   const size_t n3 = 3 * (size_t)on;
   for (nmg::DevBuf<double> *v : {&b->m, &b->k0, &b->k1, &b->k2, &b->k3, &b->y, &b->hout, &b->dmdt})
     if (v->alloc(n3)) rc = 100;
+  if (opt->integrator == 1) {
+    for (nmg::DevBuf<double> *v : {&b->hn, &b->kr, &b->krh, &b->kp, &b->kv, &b->ks, &b->kt, &b->kph, &b->ksh})
+      if (v->alloc(n3)) rc = 100;
+    if (b->pinv.alloc(3 * n3)) rc = 100;
+  }
   for (nmg::DevBuf<double> *v : {&b->phi1, &b->phi2, &b->rho, &b->rhs2, &b->cr, &b->cz, &b->cp, &b->cq})
     if (v->alloc(on) || cudaMemset(v->p, 0, sizeof(double) * on)) rc = 100;
   if (b->b2.alloc(std::max<long long>(onb, 1))) rc = 100;
@@ -806,11 +1063,12 @@ int nmg_batch_autotune(nmg_batch *b, int trial_launches, int *threads_out, doubl
   const double cmax = std::max_element(b->hdesc.begin(), b->hdesc.end(),
                                        [](const nmg::PDesc &x, const nmg::PDesc &y) { return x.cost < y.cost; })->cost;
   const size_t n3 = 3 * (size_t)b->Ntot;
-  nmg::DevBuf<double> save_m, save_k0, save_p1, save_p2;
+  nmg::DevBuf<double> save_m, save_k0, save_p1, save_p2, save_hn;
   nmg::DevBuf<nmg::PState> save_st;
   if (save_m.alloc(n3) || save_k0.alloc(n3) || save_p1.alloc(b->Ntot) || save_p2.alloc(b->Ntot) ||
-      save_st.alloc(b->P))
+      save_st.alloc(b->P) || (b->hn.p && save_hn.alloc(n3)))
     return bfail(b, 100, "nmg_batch_autotune: allocation failed");
+  if (b->hn.p) cudaMemcpy(save_hn.p, b->hn.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
   cudaMemcpy(save_m.p, b->m.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
   cudaMemcpy(save_k0.p, b->k0.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
   cudaMemcpy(save_p1.p, b->phi1.p, sizeof(double) * b->Ntot, cudaMemcpyDeviceToDevice);
@@ -838,6 +1096,7 @@ int nmg_batch_autotune(nmg_batch *b, int trial_launches, int *threads_out, doubl
       cudaMemcpy(b->phi1.p, save_p1.p, sizeof(double) * b->Ntot, cudaMemcpyDeviceToDevice);
       cudaMemcpy(b->phi2.p, save_p2.p, sizeof(double) * b->Ntot, cudaMemcpyDeviceToDevice);
       cudaMemcpy(b->st.p, save_st.p, sizeof(nmg::PState) * b->P, cudaMemcpyDeviceToDevice);
+      if (b->hn.p) cudaMemcpy(b->hn.p, save_hn.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
     }
   }
   int rc = nmg_batch_set_schedule(b, best_t, best_b);

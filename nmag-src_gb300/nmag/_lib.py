@@ -39,7 +39,7 @@ class BatchOptions(C.Structure):
     _fields_ = [("cg_rtol", C.c_double), ("cg_maxits", C.c_int), ("n_stages", C.c_int), ("rtol", C.c_double),
                 ("atol", C.c_double), ("stop_dmdt", C.c_double), ("h_max", C.c_double), ("dt0", C.c_double),
                 ("dt_max", C.c_double), ("fixed_dt", C.c_double), ("threads", C.c_int), ("budget", C.c_double),
-                ("reserved", C.c_int * 4)]
+                ("integrator", C.c_int), ("krylov_maxits", C.c_int), ("reserved", C.c_int * 2)]
 
 
 class TsStats(C.Structure):

@@ -6,8 +6,12 @@ Each particle runs the reference's hysteresis protocol
 (interface/nmag/hysteresis.py:244-557): at each field of the sweep it relaxes
 until max |dm/dt| < stop_dmdt twice in a row, then moves to the next field,
 H_k = h_max (1 - 2k/(n-1)) along its direction.  The right-hand side is the
-single path's (nmag_lam.py:734-832); time integration is the embedded
-Bogacki-Shampine 3(2) pair with per-particle step control.
+single path's (nmag_lam.py:734-832); time integration is either the embedded
+Bogacki-Shampine 3(2) pair (integrator="bs3", explicit) or the linearly
+implicit ROS2 W-method (integrator="ros2": L-stable, steps limited by accuracy
+rather than by the exchange stiffness; each stage solves I - gamma tau J by
+BiCGSTAB with the exchange + site Jacobian of nsim.ml:967-1050), both with
+per-particle step control.
 """
 import ctypes as C
 
@@ -35,7 +39,8 @@ class ParticleBatch(object):
     units (stop_dmdt default 1 deg/ns, h_max the sweep amplitude)."""
 
     def __init__(self, particles, n_stages=81, h_max=0.0, stop_dmdt=1.7453292519943295e-05, rtol=1e-5, atol=1e-5,
-                 cg_rtol=1e-6, cg_maxits=5000, dt0=0.01, dt_max=5.0, fixed_dt=0.0, threads=256, budget=0.0):
+                 cg_rtol=1e-6, cg_maxits=5000, dt0=0.01, dt_max=5.0, fixed_dt=0.0, threads=256, budget=0.0,
+                 integrator="bs3", krylov_maxits=200):
         L = lib()
         self._keep = []
         arr = (Particle * len(particles))()
@@ -56,6 +61,8 @@ class ParticleBatch(object):
         o.cg_rtol, o.cg_maxits, o.n_stages = cg_rtol, cg_maxits, n_stages
         o.rtol, o.atol, o.stop_dmdt, o.h_max = rtol, atol, stop_dmdt, h_max
         o.dt0, o.dt_max, o.fixed_dt, o.threads, o.budget = dt0, dt_max, fixed_dt, threads, budget
+        o.integrator = {"bs3": 0, "ros2": 1}[integrator]
+        o.krylov_maxits = krylov_maxits
         h = C.c_void_p()
         rc = L.nmg_batch_create(arr, len(particles), C.byref(o), C.byref(h))
         if rc != 0:
