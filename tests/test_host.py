@@ -95,6 +95,45 @@ def test_create_rejects_bad_input_without_gpu():
     assert b"missing node" in L.nmg_last_error(None)
 
 
+def test_create_rejects_bad_anchor_options_without_gpu():
+    # the anchored product's tolerance: finite, non-negative, compensated form only
+    L = _lib.lib()
+    import ctypes as C
+    mt = _lib.Material()
+    mt.Ms = 1.0
+    h = C.c_void_p()
+    pts = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1], dtype=np.float64)
+    tet = np.array([0, 1, 2, 3], dtype=np.int32)
+    for prec, tol, msg in ((2, -1.0, b"finite and non-negative"), (2, float("nan"), b"finite and non-negative"),
+                           (0, 1e-3, b"compensated product"), (1, 1e-3, b"compensated product")):
+        op = _lib.Options()
+        op.do_demag = 1
+        op.bem_precision = prec
+        op.bem_anchor_tol = tol
+        rc = L.nmg_create(pts, 4, tet, 1, C.byref(mt), C.byref(op), C.byref(h))
+        assert rc == -6, (prec, tol, rc)
+        assert msg in L.nmg_last_error(None), L.nmg_last_error(None)
+
+
+def test_batch_rejects_bad_integrator_without_gpu():
+    import ctypes as C
+    L = _lib.lib()
+    pts = np.array([0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0, 1], dtype=np.float64)
+    tet = np.array([0, 1, 2, 3], dtype=np.int32)
+    part = (_lib.Particle * 1)()
+    part[0].coords = pts.ctypes.data
+    part[0].n_nodes = 4
+    part[0].tets = tet.ctypes.data
+    part[0].n_tets = 1
+    o = _lib.BatchOptions()
+    o.n_stages, o.cg_maxits, o.cg_rtol = 1, 10, 1e-6
+    o.integrator = 2
+    b = C.c_void_p()
+    rc = L.nmg_batch_create(part, 1, C.byref(o), C.byref(b))
+    assert rc == -2
+    assert b"integrator" in L.nmg_batch_last_error(None)
+
+
 def test_product_does_not_import_oracle():
     pkg = os.path.join(ROOT, "nmag-src_gb300")
     for dirpath, _, files in os.walk(pkg):
