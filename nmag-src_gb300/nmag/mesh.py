@@ -106,6 +106,19 @@ def save_ascii(mesh, filename):
         f.write("0\n0\n")
 
 
+def magnetic_part(mesh):
+    """The simplices of the magnetic regions (region id >= 1; region 0 is
+    vacuum, main.py:1190,1297) and the nodes they use, renumbered in their
+    original order.  Returns (Mesh, node_map): node k of the result is
+    mesh.points[node_map[k]]."""
+    keep = mesh.regions >= 1
+    simp = mesh.simplices[keep]
+    used = np.unique(simp.reshape(-1))
+    renum = np.full(mesh.n_nodes, -1, dtype=np.int64)
+    renum[used] = np.arange(len(used))
+    return Mesh(mesh.points[used], renum[simp].astype(np.int32), mesh.regions[keep]), used
+
+
 def load_ascii(filename):
     """Read an nmesh ASCII file (points, region+simplices; surfaces ignored)."""
     if not os.path.exists(filename):

@@ -134,6 +134,7 @@ class Simulation(object):
         self._countdown = 2
         self.engine = None
         self.mesh = None
+        self.node_map = None    # magnetic nodes -> nodes of the loaded mesh (vacuum present)
         self.material = None
         self._m = None          # host master buffer of m (N,3)
         self._h_ext = None
@@ -145,14 +146,25 @@ class Simulation(object):
     def load_mesh(self, filename, region_names_and_mag_mats, unit_length, do_reorder=False, manual_distribution=None):
         """main.py:1075.  ``filename`` is an nmesh ASCII file or a ``nmag.mesh.Mesh``."""
         m = _mesh.load(filename)
+        # region ids 1, 2, ... name the listed regions in order; 0 is vacuum
         mats = []
         for entry in region_names_and_mag_mats:
             region_name, mat = entry
             mats.extend(mat if isinstance(mat, (list, tuple)) else [mat])
-        if len(mats) != 1:
-            raise NotImplementedError("exactly one magnetic material is supported on this path")
+        if not mats:
+            raise ValueError("load_mesh: no magnetic material given")
+        c0 = mats[0].coefficients(self.quirks)
+        if any(mt.coefficients(self.quirks) != c0 for mt in mats[1:]):
+            raise NotImplementedError("one magnetic material (possibly over several regions) is supported on this path")
+        if np.any(m.regions > len(region_names_and_mag_mats)):
+            raise ValueError("load_mesh: the mesh has region ids beyond the %d regions named"
+                             % len(region_names_and_mag_mats))
+        # vacuum simplices carry no magnetisation; the magnetic part alone is
+        # simulated (its open-boundary potential comes from the BEM), and
+        # per-site arrays refer to its nodes, as nmag's m subfields do
+        self.node_map = None
         if np.any(m.regions <= 0):
-            raise NotImplementedError("vacuum (region 0) simplices are not supported on this path")
+            m, self.node_map = _mesh.magnetic_part(m)
         self.material = mats[0]
         scale = simulation_units.of(unit_length, compatible_with=SI("m"))
         self.mesh = _mesh.Mesh(m.points * scale, m.simplices, m.regions)

@@ -208,3 +208,28 @@ def test_max_dm_step_tracks_previous_m(small_box):
     m2 = seeded_m(n, seed=6, noise=0.3)
     eng.set_m(m2)                                        # set_m becomes the reference
     assert eng.max_dm_step() == 0.0
+
+
+def test_vacuum_region_simulates_the_magnetic_part():
+    """A mesh with vacuum (region 0) simplices: the Simulation runs on its
+    magnetic part, whose per-site arrays are those of the magnetic nodes."""
+    import nmag
+    from nmag import SI, mesh
+    from test_host import _shelled_box
+    shelled = _shelled_box()
+    part, node_map = mesh.magnetic_part(shelled)
+    mat = permalloy(0.5)
+    tight = {"NBC.rtol": 1e-12, "DBC.rtol": 1e-12}
+    sims = []
+    for msh in (shelled, part):
+        s = nmag.Simulation("vac", ksp_tolerances=tight)
+        s.load_mesh(msh, [("a", mat)], unit_length=SI(1e-9, "m"))
+        sims.append(s)
+    assert sims[0].engine.N == part.n_nodes
+    np.testing.assert_array_equal(sims[0].node_map, node_map)
+    m = seeded_m(part.n_nodes, seed=3, noise=0.3)
+    H = []
+    for s in sims:
+        s.set_m(m)
+        H.append(s.engine.eval_fields()["H_total"])
+    assert np.array_equal(H[0], H[1])

@@ -141,3 +141,40 @@ def test_product_does_not_import_oracle():
             if f.endswith((".py", ".cu", ".h")):
                 txt = open(os.path.join(dirpath, f)).read()
                 assert "import oracle" not in txt and "liboracle" not in txt, f
+
+
+def _shelled_box():
+    """A 6x6x4 box whose outer layer of cells is vacuum (region 0): the
+    magnetic part is the inner 4x4x2 box."""
+    from nmag import mesh
+    outer = mesh.box_mesh(6, 6, 4, 2.0)
+    cen = outer.points[outer.simplices].mean(axis=1)
+    inside = np.all((cen > 2.0) & (cen < np.array([10.0, 10.0, 6.0])), axis=1)
+    return mesh.Mesh(outer.points, outer.simplices, np.where(inside, 1, 0))
+
+
+def test_magnetic_part_drops_vacuum():
+    from nmag import mesh
+    shelled = _shelled_box()
+    part, node_map = mesh.magnetic_part(shelled)
+    inner = mesh.box_mesh(4, 4, 2, 2.0, origin=(2.0, 2.0, 2.0))
+    assert part.n_nodes == inner.n_nodes and part.n_tets == inner.n_tets
+    assert (part.regions == 1).all()
+    np.testing.assert_array_equal(part.points, shelled.points[node_map])
+    # same tetrahedra (as coordinate sets) as the inner box built directly
+    key = lambda m: sorted(tuple(sorted(map(tuple, np.round(m.points[t], 9)))) for t in m.simplices)
+    assert key(part) == key(inner)
+
+
+def test_load_mesh_region_checks_without_gpu():
+    import nmag
+    from nmag import SI
+    shelled = _shelled_box()
+    a = nmag.MagMaterial("A", Ms=SI(8e5, "A/m"), exchange_coupling=SI(1.3e-11, "J/m"))
+    b = nmag.MagMaterial("B", Ms=SI(1e6, "A/m"), exchange_coupling=SI(1.3e-11, "J/m"))
+    sim = nmag.Simulation("regions")
+    with pytest.raises(NotImplementedError):
+        sim.load_mesh(shelled, [("a", a), ("b", b)], unit_length=SI(1e-9, "m"))
+    two = nmag.mesh.Mesh(shelled.points, shelled.simplices, np.where(shelled.regions == 1, 2, 1))
+    with pytest.raises(ValueError):
+        sim.load_mesh(two, [("a", a)], unit_length=SI(1e-9, "m"))
