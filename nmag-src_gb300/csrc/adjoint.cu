@@ -47,6 +47,9 @@ struct Tape {
   DevBuf<double> hbase, pulses;  // 3N, 3 x npulses
   DevBuf<double> Hbar, sanis, hsum, phibar, rhs, z, y2b, y1b, rhobar, tpart, avgpart, vt;
   int t_groups = 1, t_slabs = 1, t_rows = 1;
+  // compensated form: B^T with the FP32 + BF16 planes, 8-column units
+  int d_groups = 1, d_slabs = 1, d_rows = 1;
+  DevBuf<float> yhl;             // y as FP32 pairs (2 x nb)
 };
 
 namespace {
@@ -337,6 +340,53 @@ __global__ void __launch_bounds__(kT) k_gemv_t_f64(int nb, int ld, int groups, i
   o[0] = a0; o[1] = a1; o[2] = a2; o[3] = a3;
 }
 
+// y (FP64) -> FP32 pairs yh + yl
+__global__ void k_split_y(int nb, const double *__restrict__ y, float *__restrict__ yh, float *__restrict__ yl) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nb) return;
+  const double v = y[k];
+  const float h = (float)v;
+  yh[k] = h;
+  yl[k] = (float)(v - (double)h);
+}
+
+// B^T y in the compensated form (B = hi + lo, y = yh + yl): the transpose of
+// the forward compensated product, so the adjoint differentiates the same
+// linear map.  Warp (group g, slab s) owns 256 columns (one 8-column unit per
+// lane) and the rows of slab s; every column keeps an (S, C) pair.
+__global__ void __launch_bounds__(kT) k_gemv_t_df(int nb, int ld, int groups, int slabs, int rows,
+                                                   const float *__restrict__ Bh, const uint16_t *__restrict__ Bl,
+                                                   const float *__restrict__ yh, const float *__restrict__ yl,
+                                                   double *__restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int g = (int)(w % groups), sl = (int)(w / groups);
+  const int Q = ld / 8, q = g * 32 + lane;
+  if (sl >= slabs || q >= Q) return;
+  const int k0 = sl * rows, k1 = min(nb, k0 + rows);
+  float S[8], C[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) S[c] = C[c] = 0.f;
+  for (int k = k0; k < k1; ++k) {
+    const size_t o = (size_t)k * ld + 8 * (size_t)q;
+    const float4 h0 = __ldcs(reinterpret_cast<const float4 *>(Bh + o));
+    const float4 h1 = __ldcs(reinterpret_cast<const float4 *>(Bh + o) + 1);
+    const uint4 lq = __ldcs(reinterpret_cast<const uint4 *>(Bl + o));
+    const float a = __ldg(yh + k), b = __ldg(yl + k);
+    const float hv[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+    const unsigned lw[4] = {lq.x, lq.y, lq.z, lq.w};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const unsigned u = lw[c >> 1];
+      const float l = __uint_as_float((c & 1) ? (u & 0xffff0000u) : (u << 16));
+      df_madd(hv[c], l, a, b, S[c], C[c]);
+    }
+  }
+  double *out = part + (size_t)sl * ld + 8 * (size_t)q;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) out[c] = (double)S[c] + (double)C[c];
+}
+
 __global__ void k_col_sum(int nb, int ld, int slabs, const double *__restrict__ part, double *__restrict__ out) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nb) return;
@@ -520,10 +570,19 @@ int stage_vjp(nmg_handle *h, Tape &T, const double *u, const double *H, const do
     k_adj_bnd<<<nblk(M.nb, kT), kT, 0, s>>>(M.nb, M.node_of_b, M.b_of_node, M.row_ptr, M.col_idx, M.K, T.z, T.phibar,
                                            T.y2b);
     ADJ_TRY(launched(h, "adjoint boundary"));
-    k_gemv_t_f64<<<nblk((long long)T.t_groups * T.t_slabs * 32, kT), kT, 0, s>>>(M.nb, M.ld, T.t_groups, T.t_slabs,
-                                                                                  T.t_rows, M.bem, T.y2b, T.tpart);
+    const bool df = h->opt.bem_precision == 2 && M.bem16lo.p && T.yhl.p;
+    if (df) {   // the transpose of the compensated forward product
+      float *yh = T.yhl.p, *yl = T.yhl.p + M.nb;
+      k_split_y<<<nblk(M.nb, kT), kT, 0, s>>>(M.nb, T.y2b, yh, yl);
+      ADJ_TRY(launched(h, "BEM transpose split"));
+      k_gemv_t_df<<<nblk((long long)T.d_groups * T.d_slabs * 32, kT), kT, 0, s>>>(
+          M.nb, M.ld, T.d_groups, T.d_slabs, T.d_rows, M.bem32, M.bem16lo, yh, yl, T.tpart);
+    } else {
+      k_gemv_t_f64<<<nblk((long long)T.t_groups * T.t_slabs * 32, kT), kT, 0, s>>>(M.nb, M.ld, T.t_groups, T.t_slabs,
+                                                                                    T.t_rows, M.bem, T.y2b, T.tpart);
+    }
     ADJ_TRY(launched(h, "BEM transpose product"));
-    k_col_sum<<<nblk(M.nb, kT), kT, 0, s>>>(M.nb, M.ld, T.t_slabs, T.tpart, T.y1b);
+    k_col_sum<<<nblk(M.nb, kT), kT, 0, s>>>(M.nb, M.ld, df ? T.d_slabs : T.t_slabs, T.tpart, T.y1b);
     ADJ_TRY(launched(h, "BEM transpose sum"));
     k_adj_scatter<<<nblk(N, kT), kT, 0, s>>>(N, M.b_of_node, T.phibar, T.y1b, T.rhs);
     ADJ_TRY(launched(h, "adjoint neumann rhs"));
@@ -627,7 +686,16 @@ int rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ck
       int slabs = std::max(1, std::min(M.nb, target / std::max(1, T.t_groups)));
       T.t_rows = (M.nb + slabs - 1) / slabs;
       T.t_slabs = (M.nb + T.t_rows - 1) / T.t_rows;
-      if (T.tpart.alloc((size_t)T.t_slabs * M.ld)) return 100;
+      size_t part_slabs = T.t_slabs;
+      if (h->opt.bem_precision == 2 && M.bem16lo.p) {   // compensated transpose: 8-column units
+        T.d_groups = (M.ld / 8 + 31) / 32;
+        int dsl = std::max(1, std::min(M.nb, target / std::max(1, T.d_groups)));
+        T.d_rows = (M.nb + dsl - 1) / dsl;
+        T.d_slabs = (M.nb + T.d_rows - 1) / T.d_rows;
+        part_slabs = std::max<size_t>(part_slabs, T.d_slabs);
+        if (T.yhl.alloc(2 * (size_t)M.nb)) return 100;
+      }
+      if (T.tpart.alloc(part_slabs * M.ld)) return 100;
     }
   }
   cudaMemcpyAsync(T.hbase.p, W.h_ext.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice, s);

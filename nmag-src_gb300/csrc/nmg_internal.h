@@ -168,6 +168,22 @@ struct nmg_handle {
   if (prof_slot__ >= 0) (h)->prof.end((h)->stream, prof_slot__)
 
 namespace nmg {
+// Compensated FP32 multiply-add of the BEM products: (S, C) += (h + l)(a + b)
+// with h*a split exactly by an FMA, the second-order terms h*b + l*a added to
+// the error term, and S updated by TwoSum (~44 bits in FP32 operations).
+__device__ __forceinline__ void df_madd(float h, float l, float a, float b, float &S, float &C) {
+  const float p = __fmul_rn(h, a);
+  const float e = fmaf(h, a, -p);
+  const float t = fmaf(h, b, fmaf(l, a, e));
+  const float s2 = __fadd_rn(S, p);
+  const float bb = __fsub_rn(s2, S);
+  const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s2, bb)), __fsub_rn(p, bb));
+  S = s2;
+  C += err + t;
+}
+}  // namespace nmg
+
+namespace nmg {
 // ---- launchers (mesh_kernels.cu) ----
 int build_mesh(nmg_handle *h, const double *coords, const int32_t *tets, std::string &err);
 int export_operator(const nmg_handle *h, int which, double coeff, int *rows, int *cols, int *nnz,

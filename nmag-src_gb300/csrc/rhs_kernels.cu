@@ -1652,16 +1652,8 @@ __global__ void k_slab_sum_m(int nb, int nslab, int nm, int MB, const double *__
 // every operation runs on the FP32 pipe (the film's potentials cancel
 // ~50x in phi1 + phi2, so FP32 products alone lose 1e-5 there).
 // __fmul_rn / __fadd_rn / __fsub_rn forbid contraction and reassociation.
-__device__ __forceinline__ void df_madd(float h, float l, float a, float b, float &S, float &C) {
-  const float p = __fmul_rn(h, a);
-  const float e = fmaf(h, a, -p);
-  const float t = fmaf(h, b, fmaf(l, a, e));
-  const float s2 = __fadd_rn(S, p);
-  const float bb = __fsub_rn(s2, S);
-  const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s2, bb)), __fsub_rn(p, bb));
-  S = s2;
-  C += err + t;
-}
+// df_madd (the compensated multiply-add) is in nmg_internal.h: the adjoint's
+// transpose product uses it too.
 
 // (S, C) += (S2, C2) for FP32 pairs: TwoSum of the heads, the tails added.
 __device__ __forceinline__ void df_add(float &S, float &C, float S2, float C2) {

@@ -79,7 +79,19 @@ def test_uniform_weights_match_plain_rk4(cube_setup):
 
 
 def test_adjoint_matches_dense_autograd(cube_setup):
-    eng, c, cube = cube_setup
+    _check_dense(*cube_setup)
+
+
+def test_adjoint_matches_dense_autograd_compensated(cube):
+    """Compensated BEM form: forward product and its transpose in FP32 +
+    BF16 pairs (the adjoint differentiates the same map); same bounds."""
+    mat = permalloy(0.5)
+    eng = make_engine(cube, mat, tol=1e-12, bem_precision=2)
+    _check_dense(eng, mat.coefficients("nmag"), cube)
+    eng.close()
+
+
+def _check_dense(eng, c, cube):
     N, T = len(cube.points), len(cube.simplices)
     nsteps, ckpt, spp, npul = 12, 5, 3, 4
     m0 = seeded_m(N, seed=0)
