@@ -552,7 +552,8 @@ def run_adjoint_report(args):
     msh, base, seed = workload(args.workload)
     mat = material(0.02)
     sim = nmag.Simulation("adj", ksp_tolerances={"NBC.rtol": 1e-10, "DBC.rtol": 1e-10},
-                          bem_precision=args.adj_form, cg_precision=args.adj_cg)
+                          bem_precision=args.adj_form, cg_precision=args.adj_cg,
+                          adjoint_cg_precision=args.adj_bwd_cg)
     sim.load_mesh(msh, [("film", mat)], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     c = mat.coefficients("nmag")
@@ -614,7 +615,7 @@ def run_adjoint_report(args):
             "loss": loss, "grad_norms": {"Ms": float(np.linalg.norm(gM)), "K1": float(np.linalg.norm(gK)),
                                          "pulses": float(np.linalg.norm(gP))},
             "sim_ps_per_s": nsteps * dt / wall,
-            "forward_form": {"bem": args.adj_form, "cg": args.adj_cg},
+            "forward_form": {"bem": args.adj_form, "cg": args.adj_cg}, "backward_cg": args.adj_bwd_cg,
             "fd_check": {"steps": fd_steps, "directions": len(errs), "h_rel": h,
                          "max_rel_err": max(errs) if errs else None, "bound": 1e-5},
             "gpu_launches": launches}
@@ -845,7 +846,9 @@ def main():
     ap.add_argument("--adj-form", default="fp32x2", choices=["fp64", "fp32x2"],
                     help="BEM product of the RK4 forward pass (the adjoint's B^T product is FP64)")
     ap.add_argument("--adj-cg", default="fp64", choices=["fp64", "fp32"],
-                    help="Poisson CG of the RK4 forward pass (the adjoint's transposed solves are FP64)")
+                    help="Poisson CG of the RK4 forward pass")
+    ap.add_argument("--adj-bwd-cg", default="fp32", choices=["fp64", "fp32"],
+                    help="Poisson CG of the adjoint's backward pass (fp32: FP64-refined to the same tolerance)")
     ap.add_argument("--particles", type=int, default=256)
     ap.add_argument("--batch-tol", type=float, default=1e-7)
     ap.add_argument("--batch-seconds", type=float, default=0.0,

@@ -58,7 +58,10 @@ typedef struct nmg_options {
                                             max|x - x0| <= tol max|x| per member, a new
                                             compensated anchor otherwise; 0: off
                                             (finite, >= 0)                             */
-  int reserved[2];
+  int adjoint_cg_precision;              /* Poisson solves of nmg_rk4_adjoint's backward
+                                            pass: 0 FP64 CG; 1 FP32 CG with FP64 residual
+                                            refinement (to the same tolerance)         */
+  int reserved[1];
 } nmg_options;
 
 /* Integrator statistics (CVODE counters; nsim.ml:354-387 timings). */

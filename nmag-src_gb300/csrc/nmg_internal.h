@@ -154,6 +154,8 @@ struct nmg_handle {
   nmg::ElemParams ep;
   nmg::Tape *tape = nullptr;
   int anchor_hold = 0;          // >0: anchored BEM product suspended (RK4 tape runs recompute bit for bit)
+  // the mixed-precision CG is used by the forward solves or the adjoint's
+  bool mixed_cg() const { return opt.cg_precision == 1 || opt.adjoint_cg_precision == 1; }
   bool anchored() const {
     return opt.bem_anchor_tol > 0.0 && opt.bem_precision == 2 && mesh.bem16lo.p && !anchor_hold;
   }

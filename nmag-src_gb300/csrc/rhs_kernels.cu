@@ -2121,7 +2121,7 @@ int build_cg_ordering(nmg_handle *h, std::string &err) {
   NMG_CUDA_TRY(W.pcol.alloc(nnz), "alloc");
   NMG_CUDA_TRY(W.pbnd.alloc(N), "alloc");
   NMG_CUDA_TRY(W.pK.alloc(nnz), "alloc");
-  NMG_CUDA_TRY(W.xperm.alloc((size_t)N * ((h->nrep > 1 || h->opt.cg_precision == 1) ? kChunk : 1)), "alloc");
+  NMG_CUDA_TRY(W.xperm.alloc((size_t)N * ((h->nrep > 1 || h->mixed_cg()) ? kChunk : 1)), "alloc");
   NMG_CUDA_TRY(W.z32.alloc((size_t)N * kChunk), "alloc");
   NMG_CUDA_TRY(cudaMemcpy(W.perm.p, perm.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "h2d");
   NMG_CUDA_TRY(cudaMemcpy(W.prow.p, prow.data(), sizeof(int32_t) * (N + 1), cudaMemcpyHostToDevice), "h2d");
@@ -2167,7 +2167,7 @@ int build_cg_ordering(nmg_handle *h, std::string &err) {
       Ainv[(size_t)j * nc + i] = s;
     }
   NMG_CUDA_TRY(W.ainv.alloc((size_t)nc * nc), "alloc coarse inverse");
-  NMG_CUDA_TRY(W.rc.alloc((size_t)nc * ((h->nrep > 1 || h->opt.cg_precision == 1) ? kChunk : 1)), "alloc");
+  NMG_CUDA_TRY(W.rc.alloc((size_t)nc * ((h->nrep > 1 || h->mixed_cg()) ? kChunk : 1)), "alloc");
   NMG_CUDA_TRY(cudaMemcpy(W.ainv.p, Ainv.data(), sizeof(double) * nc * nc, cudaMemcpyHostToDevice), "h2d");
   {
     std::vector<float> a32(Ainv.begin(), Ainv.end());
@@ -2219,8 +2219,10 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
 }
 
 // Ensemble CG: nm <= kChunk right-hand sides (member m at b + m * N).
+// bslot: warm-start basis slot of a single simulation (-1: `mode`); mp: 1
+// mixed precision, 0 FP64, -1 the handle's forward choice.
 int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm, double rtol, double atol,
-            int maxits) {
+            int maxits, int bslot = -1, int mp_sel = -1) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   CGArgs a;
@@ -2245,14 +2247,15 @@ int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm,
     basis.x = W.ens_basis_x.p + slot * kBasis * M.N;
     basis.gram = W.ens_basis_gram.p + slot * kBasis * kBasis;
     basis.ring = W.ens_basis_ring.p + 2 * slot;
-  } else {   // one simulation: the single-solve bases of slot `mode`
-    basis.b = W.basis_b.p + (size_t)mode * kBasis * M.N;
-    basis.x = W.basis_x.p + (size_t)mode * kBasis * M.N;
-    basis.gram = W.basis_gram.p + mode * kBasis * kBasis;
-    basis.ring = W.basis_ring.p + 2 * mode;
+  } else {   // one simulation: the single-solve bases of slot bslot (default `mode`)
+    const int sl = bslot >= 0 ? bslot : mode;
+    basis.b = W.basis_b.p + (size_t)sl * kBasis * M.N;
+    basis.x = W.basis_x.p + (size_t)sl * kBasis * M.N;
+    basis.gram = W.basis_gram.p + sl * kBasis * kBasis;
+    basis.ring = W.basis_ring.p + 2 * sl;
   }
   void *args[] = {&a, &cap, &nm, &basis};
-  const bool mp = h->opt.cg_precision == 1;
+  const bool mp = mp_sel >= 0 ? mp_sel == 1 : h->opt.cg_precision == 1;
   const void *fn;
   if (mp) fn = nm <= 2 ? (const void *)k_cgm_mp<2> : (nm <= 4 ? (const void *)k_cgm_mp<4> : (const void *)k_cgm_mp<8>);
   else fn = nm <= 2 ? (const void *)k_cgm<2> : (nm <= 4 ? (const void *)k_cgm<4> : (const void *)k_cgm<8>);
@@ -2271,6 +2274,8 @@ int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm,
 }  // namespace
 
 int cg_solve(nmg_handle *h, int slot, const double *b, double *x, double rtol, double atol, int maxits) {
+  if (slot >= 2 && h->opt.adjoint_cg_precision == 1)   // the adjoint's solves, mixed precision
+    return run_cgm(h, slot & 1, 0, b, x, 1, rtol, atol, maxits, slot, 1);
   return run_cg(h, slot, b, x, rtol, atol, maxits);
 }
 
@@ -2347,23 +2352,27 @@ int init_workspace(nmg_handle *h, std::string &err) {
     // block's rows of the coarse inverse (FP32)
     W.cg_smem_mp = cap * (int)(sizeof(double) + sizeof(int) + sizeof(float)) +
                    (int)sizeof(float) * (kCGThreads * kChunk + (W.nc > 0 ? 2 * W.nc * kChunk + (kCGThreads / kAgg) * W.nc : 0));
-    const bool mp = h->opt.cg_precision == 1;
+    const bool mp = h->mixed_cg();
     if ((B > 1 || mp) && h->opt.do_demag) {
       // the ensemble / mixed-precision CG kernels: up to kChunk members per row
-      const void *fns[3] = {mp ? (const void *)k_cgm_mp<2> : (const void *)k_cgm<2>,
-                            mp ? (const void *)k_cgm_mp<4> : (const void *)k_cgm<4>,
-                            mp ? (const void *)k_cgm_mp<8> : (const void *)k_cgm<8>};
-      const int smem_need = mp ? W.cg_smem_mp : W.cg_smem_bytes;
       if (mp && W.nc * kChunk > kRwPer * 4 * kCGThreads) {
         err = "mesh too large for the mixed-precision CG (" + std::to_string(W.nc) + " aggregates, at most " +
               std::to_string(kRwPer * 4 * kCGThreads / kChunk) + ")";
         return 4;
       }
-      for (const void *fn : fns) {
+      struct Need { const void *fn; int smem; };
+      std::vector<Need> needs;
+      if (mp)   // forward mixed CG, or the adjoint's
+        for (const void *fn : {(const void *)k_cgm_mp<2>, (const void *)k_cgm_mp<4>, (const void *)k_cgm_mp<8>})
+          needs.push_back({fn, W.cg_smem_mp});
+      if (B > 1 && h->opt.cg_precision != 1)   // FP64 ensemble CG
+        for (const void *fn : {(const void *)k_cgm<2>, (const void *)k_cgm<4>, (const void *)k_cgm<8>})
+          needs.push_back({fn, W.cg_smem_bytes});
+      for (const Need &nd : needs) {
         int per = 0;
-        if (smem_need > 160 * 1024 ||
-            cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, kCGThreads, smem_need) != cudaSuccess ||
+        if (nd.smem > 160 * 1024 ||
+            cudaFuncSetAttribute(nd.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, nd.fn, kCGThreads, nd.smem) != cudaSuccess ||
             per * h->sm_count < W.cg_blocks) {
           cudaGetLastError();
           err = "mesh too large for the ensemble CG (" + std::to_string(W.cg_blocks) + " co-resident blocks needed)";

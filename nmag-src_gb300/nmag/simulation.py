@@ -101,7 +101,7 @@ class Simulation(object):
                  temperature=None, thermal_delta_t=None, user_seed_T=0, timestepper_max_order=2,
                  timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
                  lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1, cg_precision="fp64",
-                 bem_anchor=0.0):
+                 bem_anchor=0.0, adjoint_cg_precision="fp64"):
         if periodic_bc is not None:
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
@@ -120,6 +120,9 @@ class Simulation(object):
         # fp32x2 only: > 0 forms B x as B x0 + B32 (x - x0) while x stays within
         # this relative max-norm distance of the last compensated product's x0
         self.bem_anchor = float(bem_anchor)
+        # Poisson solves of the RK4 adjoint's backward pass ("fp32": FP32 CG
+        # iterations with FP64 residual refinement to the same tolerance)
+        self.adjoint_cg_precision = adjoint_cg_precision
         # ensemble: n_members simulations on one mesh, integrated together;
         # per-node arrays then carry a leading member axis (GB300 extension)
         self.n_members = max(1, int(n_members))
@@ -181,6 +184,7 @@ class Simulation(object):
         opts.cg_precision = {"fp64": 0, "fp32": 1}[self.cg_precision]
         opts.n_members = self.n_members if self.n_members > 1 else 0
         opts.bem_anchor_tol = self.bem_anchor
+        opts.adjoint_cg_precision = {"fp64": 0, "fp32": 1}[self.adjoint_cg_precision]
         self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
         shape = self.engine._shape3()
         self._m = np.zeros(shape)

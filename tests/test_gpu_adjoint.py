@@ -91,6 +91,16 @@ def test_adjoint_matches_dense_autograd_compensated(cube):
     eng.close()
 
 
+def test_adjoint_matches_dense_autograd_mixed_backward_cg(cube):
+    """The backward pass's Poisson solves by the mixed-precision CG (FP64
+    residual refinement to 1e-12): same bounds."""
+    from test_gpu_ensemble import make_ensemble
+    mat = permalloy(0.5)
+    eng, _ = make_ensemble(cube, mat, 1, bem_precision=2, adjoint_cg=1)
+    _check_dense(eng, mat.coefficients("nmag"), cube)
+    eng.close()
+
+
 def _check_dense(eng, c, cube):
     N, T = len(cube.points), len(cube.simplices)
     nsteps, ckpt, spp, npul = 12, 5, 3, 4

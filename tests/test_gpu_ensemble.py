@@ -10,7 +10,7 @@ from test_gpu_parity import make_engine
 pytestmark = pytest.mark.gpu
 
 
-def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0, anchor=0.0):
+def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0, anchor=0.0, adjoint_cg=0):
     from nmag import _lib
     single = make_engine(msh, mat, tol=tol, bem_precision=bem_precision)
     c = mat.coefficients("nmag")
@@ -28,6 +28,7 @@ def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0, ancho
     op.cg_precision = cg_precision
     op.n_members = B
     op.bem_anchor_tol = anchor
+    op.adjoint_cg_precision = adjoint_cg
     return _lib.Engine(msh.points, msh.simplices, mt, op), single
 
 
