@@ -135,6 +135,21 @@ int nmg_set_h_ext(nmg_handle *h, const double *h_ext);
  * reinitialise. */
 int nmg_set_material(nmg_handle *h, const nmg_material *mat);
 
+/* A general anisotropy in the polynomial form the reference generates for it
+ * (src/nsim_anisotropy.ml:207-236 anisotropy_equations, called from
+ * interface/nmag/nmag_lam.py:485-502 for every anisotropy other than the
+ * closed-form uniaxial K1 term of nmg_material):
+ *   E_anis   = sum_{t < n_e} e_coef[t] mx^a my^b mz^c,       a,b,c from e_pow[t]
+ *   H_anis,d = sum_{t < n_h} h_coef[3t + d] mx^a my^b mz^c,  a,b,c from h_pow[t]
+ * with the exponents packed a | b << 4 | c << 8 (each 0..13) and at most 1024
+ * terms each.  The host forms both polynomials (fit of the energy on the unit
+ * sphere, tangential gradient times -1/(mu0 Ms)); the field is added to the
+ * K1 term (set K1 = 0 to use the polynomial alone) in every member of an
+ * ensemble.  n_e = n_h = 0 removes it.  Invalidates the integrator.  The RK4
+ * adjoint refuses handles with a polynomial anisotropy (-2). */
+int nmg_set_anisotropy_poly(nmg_handle *h, int n_e, const int32_t *e_pow, const double *e_coef, int n_h,
+                            const int32_t *h_pow, const double *h_coef);
+
 /* Evaluate the RHS at the current m (program update_dmdt, nmag_lam.py:784-
  * 795) and copy fields out: fields = [H_exch | H_demag | H_anis | H_total |
  * dmdt] (5 x 3N), scalars = [phi | rho] (2 x N).  Either may be NULL. */

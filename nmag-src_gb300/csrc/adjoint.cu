@@ -665,6 +665,10 @@ int rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ck
     h->last_error = "the RK4 adjoint applies to single simulations (n_members <= 1)";
     return -2;
   }
+  if (h->ap.nh > 0 || h->ap.ne > 0) {   // the backward pass differentiates the closed-form uniaxial term only
+    h->last_error = "the RK4 adjoint does not differentiate a polynomial anisotropy";
+    return -2;
+  }
   if (!h->tape) h->tape = new Tape();
   Tape &T = *h->tape;
   const bool same = T.n3 == n3 && T.ckpt == ckpt && T.nsteps == nsteps && T.npulses == npulses;
@@ -740,6 +744,10 @@ int rk4_adjoint(nmg_handle *h, const double *d_mT_bar, const double *d_hist_bar,
   if (!h->tape || h->tape->nsteps <= 0) {
     h->last_error = "rk4 adjoint: no forward trajectory on this handle";
     return -3;
+  }
+  if (h->ap.nh > 0 || h->ap.ne > 0) {
+    h->last_error = "the RK4 adjoint does not differentiate a polynomial anisotropy";
+    return -2;
   }
   Tape &T = *h->tape;
   const int n3 = T.n3, N = M.N;

@@ -1,6 +1,7 @@
 // nmg_api.cu -- the extern "C" boundary of libnmaggpu.so (declared in
 // include/nmag_gpu.h).  Argument checking, handle lifetime, host<->device
 // copies and error reporting; the numerical work is in the *_kernels.cu files.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -195,6 +196,41 @@ int nmg_set_material(nmg_handle *h, const nmg_material *mat) {
   if (!h || !mat) return -1;
   if (!finite_material(mat) || mat->Ms == 0.0) return fail(h, -5, "nmg_set_material: invalid constants");
   h->mat = *mat;
+  h->ts_ready = 0;
+  return 0;
+}
+
+int nmg_set_anisotropy_poly(nmg_handle *h, int n_e, const int32_t *e_pow, const double *e_coef, int n_h,
+                            const int32_t *h_pow, const double *h_coef) {
+  if (!h) return -1;
+  if (n_e < 0 || n_h < 0 || n_e > nmg::kAnisMaxTerms || n_h > nmg::kAnisMaxTerms)
+    return fail(h, -2, "nmg_set_anisotropy_poly: term counts must be 0.." + std::to_string(nmg::kAnisMaxTerms));
+  if ((n_e > 0 && (!e_pow || !e_coef)) || (n_h > 0 && (!h_pow || !h_coef)))
+    return fail(h, -1, "nmg_set_anisotropy_poly: null term array");
+  auto bad_pow = [](int32_t p) {
+    return p < 0 || (p >> 12) != 0 || (p & 15) > nmg::kAnisMaxPow || ((p >> 4) & 15) > nmg::kAnisMaxPow ||
+           ((p >> 8) & 15) > nmg::kAnisMaxPow;
+  };
+  for (int t = 0; t < n_e; ++t)
+    if (bad_pow(e_pow[t]) || !std::isfinite(e_coef[t]))
+      return fail(h, -2, "nmg_set_anisotropy_poly: bad energy term " + std::to_string(t));
+  for (int t = 0; t < n_h; ++t)
+    if (bad_pow(h_pow[t]) || !std::isfinite(h_coef[3 * t]) || !std::isfinite(h_coef[3 * t + 1]) ||
+        !std::isfinite(h_coef[3 * t + 2]))
+      return fail(h, -2, "nmg_set_anisotropy_poly: bad field term " + std::to_string(t));
+  nmg::AnisPoly &ap = h->ap;
+  ap.ne = ap.nh = 0;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess)   // no launch in flight still reads the old tables
+    return fail(h, 100, "nmg_set_anisotropy_poly: sync failed");
+  if (ap.epow.alloc(n_e) || ap.ecoef.alloc(n_e) || ap.hpow.alloc(n_h) || ap.hcoef.alloc(3 * (size_t)n_h))
+    return fail(h, 100, "nmg_set_anisotropy_poly: device allocation failed");
+  if ((n_e > 0 && (cudaMemcpy(ap.epow.p, e_pow, sizeof(int32_t) * n_e, cudaMemcpyHostToDevice) ||
+                   cudaMemcpy(ap.ecoef.p, e_coef, sizeof(double) * n_e, cudaMemcpyHostToDevice))) ||
+      (n_h > 0 && (cudaMemcpy(ap.hpow.p, h_pow, sizeof(int32_t) * n_h, cudaMemcpyHostToDevice) ||
+                   cudaMemcpy(ap.hcoef.p, h_coef, sizeof(double) * 3 * n_h, cudaMemcpyHostToDevice))))
+    return fail(h, 100, "nmg_set_anisotropy_poly: copy failed");
+  ap.ne = n_e;
+  ap.nh = n_h;
   h->ts_ready = 0;
   return 0;
 }

@@ -132,6 +132,16 @@ struct ElemParams {
   double axis[3] = {0, 0, 1};
 };
 struct Tape;                     // RK4 checkpoints of the differentiation form (adjoint.cu)
+// Anisotropy given as polynomials in m (nsim_anisotropy.ml:207-236): energy
+// density terms (ne) and field terms (nh, three coefficients each); exponents
+// packed a | b << 4 | c << 8, each at most kAnisMaxPow.
+constexpr int kAnisMaxPow = 13;
+constexpr int kAnisMaxTerms = 1024;
+struct AnisPoly {
+  int ne = 0, nh = 0;
+  DevBuf<int32_t> epow, hpow;
+  DevBuf<double> ecoef, hcoef;   // ne, 3 x nh (term-major)
+};
 }  // namespace nmg
 
 struct nmg_handle {
@@ -152,6 +162,7 @@ struct nmg_handle {
   nmg::Profiler prof;
   int nrep = 1;                 // ensemble members B (member-major vectors: member b at b * 3N / b * N)
   nmg::ElemParams ep;
+  nmg::AnisPoly ap;
   nmg::Tape *tape = nullptr;
   int anchor_hold = 0;          // >0: anchored BEM product suspended (RK4 tape runs recompute bit for bit)
   // the mixed-precision CG is used by the forward solves or the adjoint's

@@ -13,6 +13,8 @@
 //   k_dbc_rhs      rhs = -K_IB phi2b (interior), phi2b (boundary)  (op_load_DBC)
 //   k_heff_llg     H_exch (K SpMV), H_demag (G SpMV on phi1+phi2), H_anis,
 //                  H_total and dm/dt fused in one node kernel (CFBOX = / V_i)
+//   k_anis_poly    H_anis from the polynomial form of a general anisotropy
+//                  energy (uniaxial K2, cubic, user functions), before k_heff_llg
 #include <algorithm>
 #include <cmath>
 
@@ -1945,11 +1947,45 @@ __global__ void k_add(int n, const double *__restrict__ a, const double *__restr
   if (i < n) c[i] = a[i] + b[i];
 }
 
+// Monomial mx^a my^b mz^c of a packed exponent triple from per-node power tables.
+__device__ __forceinline__ double anis_monomial(int p, const double *px, const double *py, const double *pz) {
+  return px[p & 15] * py[(p >> 4) & 15] * pz[(p >> 8) & 15];
+}
+
+__device__ __forceinline__ void anis_powers(double x, double y, double z, double *px, double *py, double *pz) {
+  px[0] = py[0] = pz[0] = 1.0;
+#pragma unroll
+  for (int k = 1; k <= kAnisMaxPow; ++k) {
+    px[k] = px[k - 1] * x; py[k] = py[k - 1] * y; pz[k] = pz[k - 1] * z;
+  }
+}
+
+// Anisotropy field from its polynomial form (nsim_anisotropy.ml:143-206: the
+// tangential gradient -(1/mu0 Ms)(grad E - (m.grad E) m) expanded into
+// monomials by the host): H_d = sum_t c_{t,d} m^{p_t}, written to h (3 per
+// node, all members).  The term table is read uniformly by every thread.
+__global__ void k_anis_poly(long long n, const double *__restrict__ m, int nt, const int32_t *__restrict__ pw,
+                            const double *__restrict__ c, double *__restrict__ h) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double px[kAnisMaxPow + 1], py[kAnisMaxPow + 1], pz[kAnisMaxPow + 1];
+  anis_powers(m[3 * i], m[3 * i + 1], m[3 * i + 2], px, py, pz);
+  double h0 = 0.0, h1 = 0.0, h2 = 0.0;
+  for (int t = 0; t < nt; ++t) {
+    const double mono = anis_monomial(__ldg(pw + t), px, py, pz);
+    h0 = fma(__ldg(c + 3 * t), mono, h0);
+    h1 = fma(__ldg(c + 3 * t + 1), mono, h1);
+    h2 = fma(__ldg(c + 3 * t + 2), mono, h2);
+  }
+  h[3 * i] = h0; h[3 * i + 1] = h1; h[3 * i + 2] = h2;
+}
+
 struct NodeArgs {
   int N, nnz, do_demag, nrep;   // nrep members: m, h_ext and outputs member-major (3N each), phi N each
   const int32_t *row_ptr, *col_idx;
   const double *K, *G, *ivol, *m, *phi, *h_ext;   // ivol: 1 / box volume
   const double *anis_node;   // per-node anisotropy coefficient (element parameters) or null
+  const double *anis_in;     // polynomial anisotropy field (3 per node, all members) or null
   double c_exch, C1, C2, C3, K1, anis, ax, ay, az;
   double *h_exch, *h_demag, *h_anis, *h_total, *dmdt;
 };
@@ -1979,12 +2015,16 @@ __global__ void k_heff_llg(NodeArgs a) {
   const double hd[3] = {-g0 * iv, -g1 * iv, -g2 * iv};
   const double *m = mm + 3 * (size_t)i;
   double ha[3] = {0.0, 0.0, 0.0};
+  if (a.anis_in) {
+    const double *p = a.anis_in + 3 * (size_t)gi;
+    ha[0] = p[0]; ha[1] = p[1]; ha[2] = p[2];
+  }
   if (a.K1 != 0.0 || a.anis_node) {
     const double c = a.anis_node ? a.anis_node[i] : a.anis;
     double am = (a.ax * m[0] + a.ay * m[1]) + a.az * m[2];
-    ha[0] = c * am * (a.ax - am * m[0]);
-    ha[1] = c * am * (a.ay - am * m[1]);
-    ha[2] = c * am * (a.az - am * m[2]);
+    ha[0] += c * am * (a.ax - am * m[0]);
+    ha[1] += c * am * (a.ay - am * m[1]);
+    ha[2] += c * am * (a.az - am * m[2]);
   }
   const double *he = a.h_ext + 3 * (size_t)gi;
   double H[3];
@@ -2003,7 +2043,8 @@ __global__ void k_heff_llg(NodeArgs a) {
 // Energy densities (nmag_lam.py:454-460): E_exch, E_demag, E_ext, E_anis, E_total.
 __global__ void k_energy(int N, const double *__restrict__ m, const double *__restrict__ hx,
                          const double *__restrict__ hd, const double *__restrict__ he, double ch, double ce,
-                         double K1, double ax, double ay, double az, double *__restrict__ E) {
+                         double K1, double ax, double ay, double az, int ne, const int32_t *__restrict__ epow,
+                         const double *__restrict__ ecoef, double *__restrict__ E) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const double *mi = m + 3 * (size_t)i, *x = hx + 3 * (size_t)i, *d = hd + 3 * (size_t)i, *e = he + 3 * (size_t)i;
@@ -2012,6 +2053,11 @@ __global__ void k_energy(int N, const double *__restrict__ m, const double *__re
   double ez = ce * ((mi[0] * e[0] + mi[1] * e[1]) + mi[2] * e[2]);
   double an = 0.0;
   if (K1 != 0.0) { double am = (ax * mi[0] + ay * mi[1]) + az * mi[2]; an = -K1 * am * am; }
+  if (ne > 0) {   // polynomial energy density E_anis = sum_t e_t m^{p_t}
+    double px[kAnisMaxPow + 1], py[kAnisMaxPow + 1], pz[kAnisMaxPow + 1];
+    anis_powers(mi[0], mi[1], mi[2], px, py, pz);
+    for (int t = 0; t < ne; ++t) an = fma(__ldg(ecoef + t), anis_monomial(__ldg(epow + t), px, py, pz), an);
+  }
   E[i] = ex; E[N + i] = dm; E[2 * (size_t)N + i] = ez; E[3 * (size_t)N + i] = an;
   E[4 * (size_t)N + i] = ((dm + ex) + ez) + an;
 }
@@ -2660,6 +2706,12 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
   a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.K = h->exch_K(); a.G = M.G; a.ivol = M.ivol;
   a.m = d_m; a.phi = W.phi; a.h_ext = W.h_ext;
   a.anis_node = h->ep.active ? h->ep.anis.p : nullptr;
+  a.anis_in = nullptr;
+  if (h->ap.nh > 0) {
+    k_anis_poly<<<nblk((long long)N * B, 128), 128, 0, s>>>((long long)N * B, d_m, h->ap.nh, h->ap.hpow, h->ap.hcoef,
+                                                             W.h_anis); ++h->launches;
+    a.anis_in = W.h_anis;
+  }
   a.c_exch = mt.exch_coeff; a.C1 = mt.C1; a.C2 = mt.C2; a.C3 = mt.C3; a.K1 = mt.K1; a.anis = mt.anis_coeff;
   a.ax = mt.axis[0]; a.ay = mt.axis[1]; a.az = mt.axis[2];
   if (h->ep.active) { a.ax = h->ep.axis[0]; a.ay = h->ep.axis[1]; a.az = h->ep.axis[2]; }
@@ -2680,7 +2732,8 @@ int energy_density(nmg_handle *h, const double *d_m, double *d_E5) {
   const nmg_material &mt = h->mat;
   const int NB = M.N * h->nrep;   // pointwise over all members: E[k * NB + member * N + i]
   k_energy<<<nblk(NB, 256), 256, 0, h->stream>>>(NB, d_m, W.h_exch, W.h_demag, W.h_ext, mt.E_coeff_half,
-                                                  mt.E_coeff_ext, mt.K1, mt.axis[0], mt.axis[1], mt.axis[2], d_E5); ++h->launches;
+                                                  mt.E_coeff_ext, mt.K1, mt.axis[0], mt.axis[1], mt.axis[2],
+                                                  h->ap.ne, h->ap.epow, h->ap.ecoef, d_E5); ++h->launches;
   return cudaGetLastError() == cudaSuccess ? 0 : 100;
 }
 

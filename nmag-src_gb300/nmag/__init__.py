@@ -11,9 +11,11 @@ nmag/nsim on hand-written sm_103a CUDA kernels, behind nmag's Python API.
 """
 from . import mesh
 from .si import SI, simulation_units
-from .material import MagMaterial, uniaxial_anisotropy
+from .material import MagMaterial
+from .anisotropy import PredefinedAnisotropy, uniaxial_anisotropy, cubic_anisotropy
 from .simulation import Simulation, every, at
 from ._lib import NmagGpuError
 
-__all__ = ["SI", "simulation_units", "MagMaterial", "uniaxial_anisotropy", "Simulation", "every", "at", "mesh",
+__all__ = ["SI", "simulation_units", "MagMaterial", "PredefinedAnisotropy", "uniaxial_anisotropy", "cubic_anisotropy",
+           "Simulation", "every", "at", "mesh",
            "NmagGpuError"]

@@ -55,7 +55,7 @@ class TsStats(C.Structure):
 # every symbol declared in include/nmag_gpu.h
 EXPORTS = ["nmg_version", "nmg_set_device", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_mesh_info", "nmg_get_csr",
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
-           "nmg_set_material", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
+           "nmg_set_material", "nmg_set_anisotropy_poly", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
            "nmg_ts_advance", "nmg_max_dm", "nmg_max_dm_step", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
            "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_bem_anchor_stats", "nmg_max_dm_static",
            "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
@@ -103,6 +103,7 @@ def lib(build_if_missing=True):
     L.nmg_get_m.argtypes = [vp, _f64p]
     L.nmg_set_h_ext.argtypes = [vp, _f64p]
     L.nmg_set_material.argtypes = [vp, C.POINTER(Material)]
+    L.nmg_set_anisotropy_poly.argtypes = [vp, C.c_int, vp, vp, C.c_int, vp, vp]
     L.nmg_eval_fields.argtypes = [vp, vp, vp]
     L.nmg_energy_density.argtypes = [vp, _f64p]
     L.nmg_averages.argtypes = [vp, _f64p, vp]
@@ -199,6 +200,19 @@ class Engine(object):
 
     def set_material(self, mat: Material):
         check(lib().nmg_set_material(self.h, C.byref(mat)), self.h, "set_material")
+
+    def set_anisotropy_poly(self, e_pow=(), e_coef=(), h_pow=(), h_coef=()):
+        """Polynomial anisotropy (nmg_set_anisotropy_poly): exponents packed
+        a | b << 4 | c << 8; h_coef holds three coefficients per field term.
+        Empty tables remove it."""
+        ep = np.ascontiguousarray(e_pow, dtype=np.int32)
+        ec = np.ascontiguousarray(e_coef, dtype=np.float64)
+        hp = np.ascontiguousarray(h_pow, dtype=np.int32)
+        hc = np.ascontiguousarray(h_coef, dtype=np.float64).reshape(-1)
+        if ec.size != ep.size or hc.size != 3 * hp.size:
+            raise ValueError("set_anisotropy_poly: coefficient and exponent tables differ in length")
+        check(lib().nmg_set_anisotropy_poly(self.h, ep.size, ep.ctypes.data, ec.ctypes.data, hp.size, hp.ctypes.data,
+                                            hc.ctypes.data), self.h, "set_anisotropy_poly")
 
     # ---- evaluation ----
     def eval_fields(self):

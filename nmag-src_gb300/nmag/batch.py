@@ -23,6 +23,8 @@ __all__ = ["ParticleBatch"]
 
 
 def _material_struct(coeffs):
+    if coeffs.get("anis_poly") is not None:
+        raise NotImplementedError("particle batches take the second-order uniaxial anisotropy only")
     mt = Material()
     mt.Ms, mt.exch_coeff, mt.C1, mt.C2, mt.C3 = (coeffs["Ms"], coeffs["exch_coeff"], coeffs["C1"], coeffs["C2"],
                                                  coeffs["C3"])

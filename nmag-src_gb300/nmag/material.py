@@ -1,5 +1,5 @@
-"""MagMaterial and predefined anisotropies (interface/nmag/main.py:257-495,
-interface/nmag/anisotropy.py:92-137).
+"""MagMaterial (interface/nmag/main.py:257-495); the anisotropies it takes
+are in ``anisotropy.py`` (interface/nmag/anisotropy.py).
 
 Material constants are converted to simulation units exactly as the
 reference does (main.py:419-465) and then turned into the coefficients its
@@ -10,7 +10,10 @@ generated code computes with:
 * local-equation coefficients (the LLG C1, C2, C3 and the energy factors) are
   printed with ``%g`` -- 6 significant digits -- into generated C
   (nsim.ml:846);
-* the energy factor mu0 is printed with ``%f`` (nmag_lam.py:454-459).
+* the energy factor mu0 is printed with ``%f`` (nmag_lam.py:454-459);
+* anisotropy polynomials (every anisotropy but the second-order uniaxial one,
+  which the engine evaluates in closed form) are printed with ``%f``
+  (nsim_anisotropy.ml:189-206).
 
 ``quirks="nmag"`` (the default) reproduces these roundings; ``quirks=None``
 keeps the exact double values.
@@ -20,38 +23,10 @@ from __future__ import annotations
 import math
 
 from . import si as _si
+from .anisotropy import PredefinedAnisotropy, cubic_anisotropy, polynomial_tables, uniaxial_anisotropy
 from .si import SI, g6, py2str, f6, simulation_units
 
-
-class PredefinedAnisotropy(object):
-    def __init__(self, function, order, anis_type="uniaxial", axis1=None, K1=None, K2=0, stringifier=None):
-        self.function = function
-        self.order = order
-        self.anis_type = anis_type
-        self.axis1 = axis1
-        self.K1 = K1
-        self.K2 = K2
-
-
-def _normalised(v):
-    v = [float(x) for x in v]
-    n = math.sqrt(sum(x * x for x in v))
-    if n == 0.0:
-        raise ValueError("zero-length anisotropy axis")
-    return [x / n for x in v]
-
-
-def uniaxial_anisotropy(axis, K1, K2=0):
-    """E_anis = -K1 <axis, m>^2 - K2 <axis, m>^4 (anisotropy.py:92-137)."""
-    axis = _normalised(axis)
-
-    def f(m):
-        a = sum(x * y for x, y in zip(axis, m))
-        return -K1 * a ** 2 - K2 * a ** 4
-
-    if K2:
-        raise NotImplementedError("fourth-order uniaxial anisotropy (K2) is not implemented on this path")
-    return PredefinedAnisotropy(f, 2, "uniaxial", axis, K1, K2)
+__all__ = ["MagMaterial", "PredefinedAnisotropy", "uniaxial_anisotropy", "cubic_anisotropy"]
 
 
 class MagMaterial(object):
@@ -74,13 +49,18 @@ class MagMaterial(object):
         self.scale_volume_charges = float(scale_volume_charges)
         if self.scale_volume_charges != 1.0:
             raise NotImplementedError("scale_volume_charges != 1 (a developer debugging knob) is not supported")
+        # main.py:408-421: a predefined anisotropy brings its order; a custom
+        # energy function E(m) (J/m^3) needs anisotropy_order
         if isinstance(anisotropy, PredefinedAnisotropy):
             if anisotropy_order:
                 raise ValueError("Cannot specify custom anisotropy_order when using a predefined anisotropy.")
             self.anisotropy = anisotropy
             self.anisotropy_order = anisotropy.order
         elif anisotropy is not None:
-            raise NotImplementedError("only predefined uniaxial anisotropy is supported on this path")
+            if not anisotropy_order:
+                raise ValueError("You need to specify the anisotropy_order when using a custom anisotropy function.")
+            self.anisotropy = PredefinedAnisotropy(anisotropy, int(anisotropy_order))
+            self.anisotropy_order = int(anisotropy_order)
         else:
             self.anisotropy = None
             self.anisotropy_order = None
@@ -106,10 +86,23 @@ class MagMaterial(object):
         self.su_exch_prefactor = 2.0 * self.su_exchange_coupling / (self.su_mu0 * self.su_Ms)
         self.su_K1 = 0.0
         self.axis = (0.0, 0.0, 1.0)
-        if self.anisotropy is not None:
+        self._poly = {}
+        if self.anisotropy is not None and self.anisotropy.closed_form_uniaxial():
             K1 = self.anisotropy.K1
             self.su_K1 = su.of(K1, compatible_with=SI("J/m^3")) if isinstance(K1, SI) else float(K1)
             self.axis = tuple(self.anisotropy.axis1)
+
+    def anisotropy_polynomial(self, quirks="nmag"):
+        """Tables of nmg_set_anisotropy_poly for every anisotropy other than
+        the closed-form second-order uniaxial one, else None
+        (nmag_lam.py:485-502: energy fitted on the unit sphere, field =
+        -(1/mu0 Ms) times its tangential gradient)."""
+        if self.anisotropy is None or self.anisotropy.closed_form_uniaxial():
+            return None
+        if quirks not in self._poly:
+            self._poly[quirks] = polynomial_tables(self.anisotropy.function, self.anisotropy_order,
+                                                   1.0 / (self.su_mu0 * self.su_Ms), quirks)
+        return self._poly[quirks]
 
     def set_damping(self, llg_damping):
         self.llg_damping = llg_damping
@@ -131,6 +124,7 @@ class MagMaterial(object):
             "anis_coeff": 2.0 * self.su_K1 / (self.su_mu0 * self.su_Ms),
             "E_coeff_half": g6(-0.5 * Ms * mu0f) if q else -0.5 * Ms * mu0f,
             "E_coeff_ext": g6(-1.0 * Ms * mu0f) if q else -1.0 * Ms * mu0f,
+            "anis_poly": self.anisotropy_polynomial(quirks),
         }
         return c
 

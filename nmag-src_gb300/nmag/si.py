@@ -111,12 +111,29 @@ class SI(object):
         return self._new(float(o) / self.value, {k: -v for k, v in self.dims.items()})
 
     def __add__(self, o):
-        if not isinstance(o, SI) or o.dims != self.dims:
+        # a zero of any dimension is neutral (lib.py:380-399 accepts it too),
+        # so that e.g. -K1 a^2 - K2 a^4 with K2 = 0 stays an energy density
+        if not isinstance(o, SI):
+            if float(o) == 0.0:
+                return self
+            if not self.dims:
+                return self._new(self.value + float(o), self.dims)
+            raise ValueError("incompatible SI addition")
+        if o.dims != self.dims:
+            if o.value == 0.0:
+                return self
+            if self.value == 0.0:
+                return o
             raise ValueError("incompatible SI addition")
         return self._new(self.value + o.value, self.dims)
 
+    __radd__ = __add__
+
     def __sub__(self, o):
         return self + (-1.0) * o
+
+    def __rsub__(self, o):
+        return (-self) + o
 
     def __neg__(self):
         return self._new(-self.value, self.dims)

@@ -106,8 +106,12 @@ class Simulation(object):
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
             raise NotImplementedError("thermal (Heun) integration is disabled in the reference (main.py:797-806)")
-        if do_anisotropy_jacobian:
-            raise NotImplementedError("do_anisotropy_jacobian is not implemented on this path")
+        # kept for the API: in the reference this flag only extends the
+        # jacobian plan (nmag_lam.py:665-679), and jacobian plans are never
+        # built ("old relic", nsim.ml:3266) -- the timestepper's Jacobian takes
+        # its derivatives from phys_field_derivs, which ignore H_anis
+        # (nmag_lam.py:689-693) -- so it changes no result
+        self._do_anisotropy_jacobian = bool(do_anisotropy_jacobian)
         self.name = name or "nmag"
         self._do_demag = bool(do_demag)
         self.max_order = int(timestepper_max_order)
@@ -186,6 +190,9 @@ class Simulation(object):
         opts.bem_anchor_tol = self.bem_anchor
         opts.adjoint_cg_precision = {"fp64": 0, "fp32": 1}[self.adjoint_cg_precision]
         self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
+        poly = self.material.anisotropy_polynomial(self.quirks)
+        if poly is not None:
+            self.engine.set_anisotropy_poly(*poly)
         shape = self.engine._shape3()
         self._m = np.zeros(shape)
         self.engine.max_dm_step()   # the device's reference m for the first convergence check

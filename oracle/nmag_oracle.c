@@ -480,7 +480,37 @@ void om_state_free(om_state *S) {
   free(S->phi1); free(S->phi2); free(S->phi); free(S->rho); free(S->h_ext); free(S->h_exch); free(S->h_demag);
   free(S->h_anis); free(S->h_total); free(S->dmdt); free(S->tmp_b1); free(S->tmp_b2);
   for (int k = 0; k < 2; ++k) { free(S->basis_b[k]); free(S->basis_x[k]); }
+  free(S->an_epow); free(S->an_hpow); free(S->an_ecoef); free(S->an_hcoef);
   memset(S, 0, sizeof(*S));
+}
+
+int om_set_anisotropy_poly(om_state *S, int ne, const int32_t *epow, const double *ecoef, int nh,
+                           const int32_t *hpow, const double *hcoef) {
+  if (ne < 0 || nh < 0) return -1;
+  free(S->an_epow); free(S->an_hpow); free(S->an_ecoef); free(S->an_hcoef);
+  S->an_epow = xcalloc(ne + 1, sizeof(int32_t)); S->an_ecoef = xcalloc(ne + 1, sizeof(double));
+  S->an_hpow = xcalloc(nh + 1, sizeof(int32_t)); S->an_hcoef = xcalloc(3 * (size_t)nh + 1, sizeof(double));
+  if (ne) { memcpy(S->an_epow, epow, sizeof(int32_t) * ne); memcpy(S->an_ecoef, ecoef, sizeof(double) * ne); }
+  if (nh) { memcpy(S->an_hpow, hpow, sizeof(int32_t) * nh); memcpy(S->an_hcoef, hcoef, sizeof(double) * 3 * nh); }
+  S->an_ne = ne; S->an_nh = nh;
+  return 0;
+}
+
+/* One generated polynomial: sum over the terms with a non-zero coefficient
+ * (stride apart in coef) of (c)*m(0)^a*m(1)^b*m(2)^c, multiplied left to
+ * right, summed in order. */
+static double poly_eval(int nt, const int32_t *pw, const double *coef, int stride, const double *m) {
+  double sum = 0.0;
+  for (int t = 0; t < nt; ++t) {
+    const double c = coef[(size_t)t * stride];
+    if (c == 0.0) continue;
+    double v = c;
+    const int e[3] = {pw[t] & 15, (pw[t] >> 4) & 15, (pw[t] >> 8) & 15};
+    for (int d = 0; d < 3; ++d)
+      for (int k = 0; k < e[d]; ++k) v *= m[d];
+    sum += v;
+  }
+  return sum;
 }
 
 /* Sparse A x where A is K restricted by a mask: mode 0 = full K; mode 1 =
@@ -731,6 +761,8 @@ int om_rhs(om_state *S, const double *m, double *dmdt_out) {
       double am = (mt->axis[0] * mi[0] + mt->axis[1] * mi[1]) + mt->axis[2] * mi[2];
       for (int d = 0; d < 3; ++d) ha[d] = mt->anis_coeff * am * (mt->axis[d] - am * mi[d]);
     } else ha[0] = ha[1] = ha[2] = 0.0;
+    if (S->an_nh)
+      for (int d = 0; d < 3; ++d) ha[d] += poly_eval(S->an_nh, S->an_hpow, S->an_hcoef + d, 3, mi);
     double *ht = S->h_total + 3 * (size_t)i;
     for (int d = 0; d < 3; ++d)
       ht[d] = ((S->h_ext[3 * i + d] + S->h_exch[3 * i + d]) + ha[d]) + S->h_demag[3 * i + d];
@@ -756,6 +788,7 @@ int om_energy_density(const om_state *S, const double *m, double *E5) {
       double am = (mt->axis[0] * mi[0] + mt->axis[1] * mi[1]) + mt->axis[2] * mi[2];
       e_an = -mt->K1 * am * am;
     }
+    if (S->an_ne) e_an += poly_eval(S->an_ne, S->an_epow, S->an_ecoef, 1, mi);
     E5[i] = e_ex; E5[N + i] = e_dm; E5[2 * N + i] = e_ext; E5[3 * N + i] = e_an;
     E5[4 * N + i] = ((e_dm + e_ex) + e_ext) + e_an;
   }

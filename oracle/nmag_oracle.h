@@ -96,12 +96,24 @@ typedef struct om_state {
   double *basis_b[2], *basis_x[2];
   double gram[2][OM_BASIS * OM_BASIS];
   int bcount[2], bhead[2];
+  /* anisotropy in polynomial form (om_set_anisotropy_poly); owned copies */
+  int an_ne, an_nh;
+  int32_t *an_epow, *an_hpow;
+  double *an_ecoef, *an_hcoef;
 } om_state;
 
 
 int om_state_init(om_state *S, const om_mesh *M, const om_material *mat, const om_solver *nbc,
                   const om_solver *dbc, int do_demag, int nthreads);
 void om_state_free(om_state *S);
+/* Anisotropy as the polynomials the reference generates for it
+ * (nsim_anisotropy.ml:189-236, equations E_anis and H_anis(d) of
+ * nmag_lam.py:485-502): E = sum_t e_t m^p_t, H_d = sum_t h_{t,d} m^p_t with
+ * exponents packed a | b << 4 | c << 8; added to the closed-form K1 term.
+ * Evaluated like the generated C: per component, terms in table order,
+ * each (c)*m(0)*...*m(2) left to right.  ne = nh = 0 removes it. */
+int om_set_anisotropy_poly(om_state *S, int ne, const int32_t *epow, const double *ecoef, int nh,
+                           const int32_t *hpow, const double *hcoef);
 /* Full RHS: H_exch, H_demag (FEM/BEM), H_anis, H_total, dm/dt (nmag_lam.py:734-832). */
 int om_rhs(om_state *S, const double *m, double *dmdt_out);
 /* Energy densities E_exch, E_demag, E_ext, E_anis, E_total (5 x N) from the last fields. */

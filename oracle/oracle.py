@@ -59,7 +59,10 @@ class OmState(C.Structure):
                 ("last_iters_nbc", C.c_int), ("last_iters_dbc", C.c_int), ("n_rhs", C.c_longlong),
                 ("nthreads", C.c_int),
                 ("basis_b", C.POINTER(C.c_double) * 2), ("basis_x", C.POINTER(C.c_double) * 2),
-                ("gram", (C.c_double * 100) * 2), ("bcount", C.c_int * 2), ("bhead", C.c_int * 2)]
+                ("gram", (C.c_double * 100) * 2), ("bcount", C.c_int * 2), ("bhead", C.c_int * 2),
+                ("an_ne", C.c_int), ("an_nh", C.c_int), ("an_epow", C.POINTER(C.c_int32)),
+                ("an_hpow", C.POINTER(C.c_int32)), ("an_ecoef", C.POINTER(C.c_double)),
+                ("an_hcoef", C.POINTER(C.c_double))]
 
 
 class OmStats(C.Structure):
@@ -93,6 +96,8 @@ def lib():
                                     C.POINTER(OmSolver), C.POINTER(OmSolver), C.c_int, C.c_int]
         L.om_state_free.argtypes = [C.POINTER(OmState)]
         L.om_rhs.argtypes = [C.POINTER(OmState), _f64p, C.c_void_p]
+        L.om_set_anisotropy_poly.argtypes = [C.POINTER(OmState), C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                             C.c_void_p, C.c_void_p]
         L.om_energy_density.argtypes = [C.POINTER(OmState), _f64p, _f64p]
         L.om_jv.argtypes = [C.POINTER(OmState), _f64p, _f64p, _f64p, _f64p]
         L.om_bdf_create.argtypes = [C.POINTER(OmState), C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -210,6 +215,12 @@ class OracleSim(object):
         n2 = OmSolver(dbc[0], dbc[1], int(dbc[2]))
         L.om_state_init(C.byref(self._s), C.byref(omesh._m), C.byref(mat), C.byref(n1), C.byref(n2),
                         int(bool(do_demag)), nthreads)
+        poly = coeffs.get("anis_poly")
+        if poly is not None:
+            ep, ec, hp, hc = (np.ascontiguousarray(poly[0], dtype=np.int32), np.ascontiguousarray(poly[1], dtype=np.float64),
+                              np.ascontiguousarray(poly[2], dtype=np.int32), np.ascontiguousarray(poly[3], dtype=np.float64))
+            L.om_set_anisotropy_poly(C.byref(self._s), ep.size, ep.ctypes.data, ec.ctypes.data, hp.size,
+                                     hp.ctypes.data, hc.ctypes.data)
         self.N = omesh.n_nodes
         self._bdf = None
 

@@ -29,7 +29,10 @@ def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0, ancho
     op.n_members = B
     op.bem_anchor_tol = anchor
     op.adjoint_cg_precision = adjoint_cg
-    return _lib.Engine(msh.points, msh.simplices, mt, op), single
+    ens = _lib.Engine(msh.points, msh.simplices, mt, op)
+    if c.get("anis_poly") is not None:
+        ens.set_anisotropy_poly(*c["anis_poly"])
+    return ens, single
 
 
 def _members(N, B, seed0=100):

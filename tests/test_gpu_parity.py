@@ -34,7 +34,10 @@ def make_engine(msh, mat, do_demag=True, tol=1e-12, bem_precision=0):
     op.nbc_atol = op.dbc_atol = 1e-50
     op.nbc_maxits = op.dbc_maxits = 20000
     op.bem_precision = bem_precision
-    return _lib.Engine(msh.points, msh.simplices, mt, op)
+    eng = _lib.Engine(msh.points, msh.simplices, mt, op)
+    if c.get("anis_poly") is not None:
+        eng.set_anisotropy_poly(*c["anis_poly"])
+    return eng
 
 
 @pytest.fixture(scope="module")
