@@ -150,6 +150,29 @@ int nmg_set_material(nmg_handle *h, const nmg_material *mat);
 int nmg_set_anisotropy_poly(nmg_handle *h, int n_e, const int32_t *e_pow, const double *e_coef, int n_h,
                             const int32_t *h_pow, const double *h_coef);
 
+/* Spin-transfer torque (Zhang-Li form of interface/nmag/nmag_lam.py:417-424,
+ * 872-903): dm/dt gains c4 m x (m x u) + c5 m x u with u = dm_dcurrent =
+ * (J . grad) m, computed every RHS as G_j m (the op_grad_phi pattern without
+ * its sign) dotted with the current density J per node and divided by the box
+ * volume.  c4 = su_llg_stt_adiab, c5 = su_llg_stt_nadiab of the material
+ * (main.py:440-451), rounded like the other LLG coefficients; 0, 0 switches
+ * it off.  The timestepper's Jacobian ignores these terms, as the
+ * reference's (nmag_lam.py:432-436).  The RK4 adjoint refuses a handle with
+ * it switched on (-2). */
+int nmg_set_stt(nmg_handle *h, double c4, double c5);
+
+/* Current density J (3N per member, simulation units of A/m^2; NULL = zero),
+ * v_current_density of main.py:1934-1960.  Invalidates the integrator. */
+int nmg_set_current_density(nmg_handle *h, const double *j);
+
+/* Pinning field (N values, one per node, shared by the members of an
+ * ensemble; NULL = 1 everywhere): the factor `pin` of every term of dm/dt and
+ * of the timestepper's Jacobian rows (interface/nmag/nmag_lam.py:417-436;
+ * Simulation.set_pinning, main.py:1918-1935).  0 fixes the magnetisation of a
+ * node.  Invalidates the integrator.  The RK4 adjoint refuses a handle with a
+ * pinning field (-2). */
+int nmg_set_pinning(nmg_handle *h, const double *pin);
+
 /* Evaluate the RHS at the current m (program update_dmdt, nmag_lam.py:784-
  * 795) and copy fields out: fields = [H_exch | H_demag | H_anis | H_total |
  * dmdt] (5 x 3N), scalars = [phi | rho] (2 x N).  Either may be NULL. */

@@ -669,6 +669,14 @@ int rk4_forward(nmg_handle *h, const double *d_m0, double dt, int nsteps, int ck
     h->last_error = "the RK4 adjoint does not differentiate a polynomial anisotropy";
     return -2;
   }
+  if (h->stt.on()) {
+    h->last_error = "the RK4 adjoint does not differentiate the spin-transfer torque";
+    return -2;
+  }
+  if (h->pin.p) {
+    h->last_error = "the RK4 adjoint does not take a pinning field";
+    return -2;
+  }
   if (!h->tape) h->tape = new Tape();
   Tape &T = *h->tape;
   const bool same = T.n3 == n3 && T.ckpt == ckpt && T.nsteps == nsteps && T.npulses == npulses;
@@ -745,8 +753,8 @@ int rk4_adjoint(nmg_handle *h, const double *d_mT_bar, const double *d_hist_bar,
     h->last_error = "rk4 adjoint: no forward trajectory on this handle";
     return -3;
   }
-  if (h->ap.nh > 0 || h->ap.ne > 0) {
-    h->last_error = "the RK4 adjoint does not differentiate a polynomial anisotropy";
+  if (h->ap.nh > 0 || h->ap.ne > 0 || h->stt.on() || h->pin.p) {
+    h->last_error = "the RK4 adjoint takes no polynomial anisotropy, spin-transfer torque or pinning field";
     return -2;
   }
   Tape &T = *h->tape;

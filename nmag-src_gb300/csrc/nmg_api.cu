@@ -235,6 +235,55 @@ int nmg_set_anisotropy_poly(nmg_handle *h, int n_e, const int32_t *e_pow, const 
   return 0;
 }
 
+int nmg_set_stt(nmg_handle *h, double c4, double c5) {
+  if (!h) return -1;
+  if (!std::isfinite(c4) || !std::isfinite(c5)) return fail(h, -5, "nmg_set_stt: non-finite coefficient");
+  const size_t n3 = 3 * (size_t)h->mesh.N * h->nrep;
+  if ((c4 != 0.0 || c5 != 0.0) && !h->stt.j.p) {   // current density starts at zero
+    if (h->stt.j.alloc(n3) || h->stt.dmdc.alloc(n3) || cudaMemset(h->stt.j.p, 0, sizeof(double) * n3))
+      return fail(h, 100, "nmg_set_stt: device allocation failed");
+  }
+  h->stt.c4 = c4;
+  h->stt.c5 = c5;
+  h->ts_ready = 0;
+  return 0;
+}
+
+int nmg_set_current_density(nmg_handle *h, const double *j) {
+  if (!h) return -1;
+  const size_t n3 = 3 * (size_t)h->mesh.N * h->nrep;
+  if (j)
+    for (size_t k = 0; k < n3; ++k)
+      if (!std::isfinite(j[k])) return fail(h, -4, "nmg_set_current_density: non-finite value");
+  if (!h->stt.j.p && (h->stt.j.alloc(n3) || h->stt.dmdc.alloc(n3)))
+    return fail(h, 100, "nmg_set_current_density: device allocation failed");
+  cudaError_t e = j ? cudaMemcpyAsync(h->stt.j.p, j, sizeof(double) * n3, cudaMemcpyHostToDevice, h->stream)
+                    : cudaMemsetAsync(h->stt.j.p, 0, sizeof(double) * n3, h->stream);
+  if (e != cudaSuccess || cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return fail(h, 100, "nmg_set_current_density: copy failed");
+  h->ts_ready = 0;
+  return 0;
+}
+
+int nmg_set_pinning(nmg_handle *h, const double *pin) {
+  if (!h) return -1;
+  const int N = h->mesh.N;
+  if (!pin) {   // 1 everywhere: no factor
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail(h, 100, "nmg_set_pinning: sync failed");
+    h->pin.release();
+    h->ts_ready = 0;
+    return 0;
+  }
+  for (int i = 0; i < N; ++i)
+    if (!std::isfinite(pin[i])) return fail(h, -4, "nmg_set_pinning: non-finite value");
+  if (!h->pin.p && h->pin.alloc(N)) return fail(h, 100, "nmg_set_pinning: device allocation failed");
+  if (cudaMemcpyAsync(h->pin.p, pin, sizeof(double) * N, cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return fail(h, 100, "nmg_set_pinning: copy failed");
+  h->ts_ready = 0;
+  return 0;
+}
+
 int nmg_eval_fields(nmg_handle *h, double *fields, double *scalars) {
   if (!h) return -1;
   int rc = nmg::rhs_eval(h, h->ws.m, h->ws.dmdt);

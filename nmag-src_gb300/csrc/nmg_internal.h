@@ -142,6 +142,14 @@ struct AnisPoly {
   DevBuf<int32_t> epow, hpow;
   DevBuf<double> ecoef, hcoef;   // ne, 3 x nh (term-major)
 };
+// Spin-transfer torque (Zhang-Li): coefficients LLG_C4 (adiabatic) and LLG_C5
+// (non-adiabatic) of the material, the current density (3 per node, all
+// members) and the per-RHS dm_dcurrent = (J . grad) m.
+struct Stt {
+  double c4 = 0.0, c5 = 0.0;
+  DevBuf<double> j, dmdc;
+  bool on() const { return (c4 != 0.0 || c5 != 0.0) && j.p; }
+};
 }  // namespace nmg
 
 struct nmg_handle {
@@ -163,6 +171,8 @@ struct nmg_handle {
   int nrep = 1;                 // ensemble members B (member-major vectors: member b at b * 3N / b * N)
   nmg::ElemParams ep;
   nmg::AnisPoly ap;
+  nmg::Stt stt;
+  nmg::DevBuf<double> pin;      // per-node factor of dm/dt and of the Jacobian rows (null: 1 everywhere)
   nmg::Tape *tape = nullptr;
   int anchor_hold = 0;          // >0: anchored BEM product suspended (RK4 tape runs recompute bit for bit)
   // the mixed-precision CG is used by the forward solves or the adjoint's

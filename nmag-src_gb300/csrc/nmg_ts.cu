@@ -314,6 +314,7 @@ struct JvArgs {
   const int32_t *row_ptr, *col_idx, *diag_pos;
   const double *K, *ivol, *mJ, *HJ, *t, *ewt;
   const double *Pinv;   // per node and member: inverse of the 3x3 preconditioner block (row-major)
+  const double *pin;    // per-node factor of the Jacobian rows (the pin field) or null
   double c_exch, C1, C2, gamma, gammap;
   int psolve, scale_out;
   double *out;
@@ -354,6 +355,10 @@ __global__ void k_jv_psolve(JvArgs a) {
   const double *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g, *w = a.t + 3 * (size_t)g;
   double jw[3];
   jac_apply(m, H, w, hv, a.C1, a.C2, jw);
+  if (a.pin) {
+    const double p = a.pin[i];
+    jw[0] *= p; jw[1] *= p; jw[2] *= p;
+  }
   double r[3] = {w[0] - a.gamma * jw[0], w[1] - a.gamma * jw[1], w[2] - a.gamma * jw[2]};
   double z[3] = {r[0], r[1], r[2]};
   if (a.psolve) {
@@ -371,11 +376,13 @@ __global__ void k_jv_psolve(JvArgs a) {
 // once per preconditioner setup: Pinv[9 g + 3 d + c] = (P^-1)_dc.
 __global__ void k_pprep(int N, const int32_t *__restrict__ diag_pos, const double *__restrict__ K,
                         const double *__restrict__ vol, const double *__restrict__ mJ, const double *__restrict__ HJ,
-                        double c_exch, double C1, double C2, double gammap, double *__restrict__ Pinv, int nrep) {
+                        double c_exch, double C1, double C2, double gammap, double *__restrict__ Pinv, int nrep,
+                        const double *__restrict__ pin) {
   const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (g >= (long long)N * nrep) return;
   const int i = (int)(g % N);
   const double kap = -c_exch * K[diag_pos[i]] / vol[i];
+  const double pf = pin ? pin[i] : 1.0;
   const double *m = mJ + 3 * (size_t)g, *H = HJ + 3 * (size_t)g;
   double P[3][3];
   for (int c = 0; c < 3; ++c) {
@@ -383,7 +390,7 @@ __global__ void k_pprep(int N, const int32_t *__restrict__ diag_pos, const doubl
     e[c] = 1.0;
     double he[3] = {kap * e[0], kap * e[1], kap * e[2]}, je[3];
     jac_apply(m, H, e, he, C1, C2, je);
-    for (int d = 0; d < 3; ++d) P[d][c] = (d == c ? 1.0 : 0.0) - gammap * je[d];
+    for (int d = 0; d < 3; ++d) P[d][c] = (d == c ? 1.0 : 0.0) - gammap * (pin ? pf * je[d] : je[d]);
   }
   double c00 = P[1][1] * P[2][2] - P[1][2] * P[2][1];
   double c01 = P[1][2] * P[2][0] - P[1][0] * P[2][2];
@@ -510,7 +517,7 @@ JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
   const Mesh &M = I.hd->mesh;
   JvArgs a;
   a.N = M.N; a.nrep = I.hd->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.ivol = M.ivol;
-  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv;
+  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv; a.pin = I.hd->pin.p;
   a.c_exch = I.hd->mat.exch_coeff; a.C1 = I.hd->mat.C1; a.C2 = I.hd->mat.C2;
   a.gamma = I.gamma; a.gammap = I.gammap; a.psolve = psolve; a.scale_out = 1; a.out = out;
   return a;
@@ -733,7 +740,7 @@ int nls(Integrator &I, int nflag_first) {
         const nmg_material &mt = I.hd->mat;
         k_pprep<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(
             M.N, M.diag_pos, I.hd->exch_K(), M.vol, I.mJ, I.HJ, mt.exch_coeff, mt.C1, mt.C2, I.gammap, I.Pinv,
-            I.hd->nrep);
+            I.hd->nrep, I.hd->pin.p);
         ++I.hd->launches;
       }
     }

@@ -15,6 +15,7 @@
 //                  H_total and dm/dt fused in one node kernel (CFBOX = / V_i)
 //   k_anis_poly    H_anis from the polynomial form of a general anisotropy
 //                  energy (uniaxial K2, cubic, user functions), before k_heff_llg
+//   k_stt_dmdc     spin-transfer dm_dcurrent = (J . grad) m, before k_heff_llg
 #include <algorithm>
 #include <cmath>
 
@@ -1980,12 +1981,40 @@ __global__ void k_anis_poly(long long n, const double *__restrict__ m, int nt, c
   h[3 * i] = h0; h[3 * i + 1] = h1; h[3 * i + 2] = h2;
 }
 
+// dm_dcurrent = (J . grad) m (program set_dm_dcurrent, nmag_lam.py:872-903):
+// op_grad_m = <grad_m(i,j)||d/dxj m(i)> is G_j applied to m_i (the pattern
+// and values of op_grad_phi without its sign), then site-wise
+// grad_m(i,j) current_density(j) summed over j in order, then CFBOX.
+__global__ void k_stt_dmdc(int N, int nrep, int nnz, const int32_t *__restrict__ row_ptr,
+                           const int32_t *__restrict__ col_idx, const double *__restrict__ G,
+                           const double *__restrict__ ivol, const double *__restrict__ m,
+                           const double *__restrict__ J, double *__restrict__ out) {
+  const long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (gi >= (long long)N * nrep) return;
+  const int mbr = (int)(gi / N), i = (int)(gi - (long long)mbr * N);
+  const double *mm = m + (size_t)mbr * 3 * N;
+  double g[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};   // g[comp][direction]
+  for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+    const double gx = G[k], gy = G[(size_t)nnz + k], gz = G[2 * (size_t)nnz + k];
+    const double *mj = mm + 3 * (size_t)col_idx[k];
+    for (int c = 0; c < 3; ++c) {
+      g[c][0] += gx * mj[c]; g[c][1] += gy * mj[c]; g[c][2] += gz * mj[c];
+    }
+  }
+  const double *jp = J + 3 * (size_t)gi;
+  const double iv = ivol[i];
+  for (int c = 0; c < 3; ++c) out[3 * (size_t)gi + c] = ((g[c][0] * jp[0] + g[c][1] * jp[1]) + g[c][2] * jp[2]) * iv;
+}
+
 struct NodeArgs {
   int N, nnz, do_demag, nrep;   // nrep members: m, h_ext and outputs member-major (3N each), phi N each
   const int32_t *row_ptr, *col_idx;
   const double *K, *G, *ivol, *m, *phi, *h_ext;   // ivol: 1 / box volume
   const double *anis_node;   // per-node anisotropy coefficient (element parameters) or null
   const double *anis_in;     // polynomial anisotropy field (3 per node, all members) or null
+  const double *dmdc;        // spin-transfer dm_dcurrent (3 per node, all members) or null
+  const double *pin;         // per-node factor of dm/dt (one per node, shared by members) or null
+  double C4, C5;             // its LLG coefficients
   double c_exch, C1, C2, C3, K1, anis, ax, ay, az;
   double *h_exch, *h_demag, *h_anis, *h_total, *dmdt;
 };
@@ -2033,10 +2062,23 @@ __global__ void k_heff_llg(NodeArgs a) {
   const double mxmxH[3] = {m[1] * mxH[2] - m[2] * mxH[1], m[2] * mxH[0] - m[0] * mxH[2],
                            m[0] * mxH[1] - m[1] * mxH[0]};
   const double c3 = a.C3 * (1.0 - ((m[0] * m[0] + m[1] * m[1]) + m[2] * m[2]));
+  double f[3];
+  for (int d = 0; d < 3; ++d) f[d] = (a.C1 * mxH[d] + a.C2 * mxmxH[d]) + c3 * m[d];
+  if (a.dmdc) {   // + C4 m x (m x dm_dcurrent) + C5 m x dm_dcurrent (nmag_lam.py:417-424)
+    const double *u = a.dmdc + 3 * (size_t)gi;
+    const double mxu[3] = {m[1] * u[2] - m[2] * u[1], m[2] * u[0] - m[0] * u[2], m[0] * u[1] - m[1] * u[0]};
+    const double mxmxu[3] = {m[1] * mxu[2] - m[2] * mxu[1], m[2] * mxu[0] - m[0] * mxu[2],
+                             m[0] * mxu[1] - m[1] * mxu[0]};
+    for (int d = 0; d < 3; ++d) f[d] = (f[d] + a.C4 * mxmxu[d]) + a.C5 * mxu[d];
+  }
+  if (a.pin) {   // every LLG term carries the factor pin (nmag_lam.py:417-424)
+    const double p = a.pin[i];
+    for (int d = 0; d < 3; ++d) f[d] *= p;
+  }
   for (int d = 0; d < 3; ++d) {
     const size_t o = 3 * (size_t)gi + d;
     a.h_exch[o] = hx[d]; a.h_demag[o] = hd[d]; a.h_anis[o] = ha[d]; a.h_total[o] = H[d];
-    a.dmdt[o] = (a.C1 * mxH[d] + a.C2 * mxmxH[d]) + c3 * m[d];
+    a.dmdt[o] = f[d];
   }
 }
 
@@ -2711,6 +2753,14 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
     k_anis_poly<<<nblk((long long)N * B, 128), 128, 0, s>>>((long long)N * B, d_m, h->ap.nh, h->ap.hpow, h->ap.hcoef,
                                                              W.h_anis); ++h->launches;
     a.anis_in = W.h_anis;
+  }
+  a.dmdc = nullptr;
+  a.pin = h->pin.p;
+  a.C4 = h->stt.c4; a.C5 = h->stt.c5;
+  if (h->stt.on()) {
+    k_stt_dmdc<<<nblk((long long)N * B, 128), 128, 0, s>>>(N, B, M.nnz, M.row_ptr, M.col_idx, M.G, M.ivol, d_m,
+                                                            h->stt.j, h->stt.dmdc); ++h->launches;
+    a.dmdc = h->stt.dmdc;
   }
   a.c_exch = mt.exch_coeff; a.C1 = mt.C1; a.C2 = mt.C2; a.C3 = mt.C3; a.K1 = mt.K1; a.anis = mt.anis_coeff;
   a.ax = mt.axis[0]; a.ay = mt.axis[1]; a.az = mt.axis[2];

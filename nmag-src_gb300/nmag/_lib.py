@@ -55,7 +55,7 @@ class TsStats(C.Structure):
 # every symbol declared in include/nmag_gpu.h
 EXPORTS = ["nmg_version", "nmg_set_device", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_mesh_info", "nmg_get_csr",
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
-           "nmg_set_material", "nmg_set_anisotropy_poly", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
+           "nmg_set_material", "nmg_set_anisotropy_poly", "nmg_set_stt", "nmg_set_current_density", "nmg_set_pinning", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
            "nmg_ts_advance", "nmg_max_dm", "nmg_max_dm_step", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
            "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_bem_anchor_stats", "nmg_max_dm_static",
            "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
@@ -104,6 +104,9 @@ def lib(build_if_missing=True):
     L.nmg_set_h_ext.argtypes = [vp, _f64p]
     L.nmg_set_material.argtypes = [vp, C.POINTER(Material)]
     L.nmg_set_anisotropy_poly.argtypes = [vp, C.c_int, vp, vp, C.c_int, vp, vp]
+    L.nmg_set_stt.argtypes = [vp, C.c_double, C.c_double]
+    L.nmg_set_current_density.argtypes = [vp, vp]
+    L.nmg_set_pinning.argtypes = [vp, vp]
     L.nmg_eval_fields.argtypes = [vp, vp, vp]
     L.nmg_energy_density.argtypes = [vp, _f64p]
     L.nmg_averages.argtypes = [vp, _f64p, vp]
@@ -200,6 +203,26 @@ class Engine(object):
 
     def set_material(self, mat: Material):
         check(lib().nmg_set_material(self.h, C.byref(mat)), self.h, "set_material")
+
+    def set_stt(self, c4, c5):
+        """Spin-transfer coefficients LLG_C4 (adiabatic), LLG_C5 (non-adiabatic)."""
+        check(lib().nmg_set_stt(self.h, float(c4), float(c5)), self.h, "set_stt")
+
+    def set_current_density(self, j=None):
+        """Current density (simulation units), broadcast like set_h_ext; None = zero."""
+        if j is None:
+            check(lib().nmg_set_current_density(self.h, None), self.h, "set_current_density")
+            return
+        j = np.ascontiguousarray(np.broadcast_to(np.asarray(j, dtype=np.float64), self._shape3())).reshape(-1)
+        check(lib().nmg_set_current_density(self.h, j.ctypes.data), self.h, "set_current_density")
+
+    def set_pinning(self, pin=None):
+        """Pinning factor per node (N values, shared by ensemble members); None = 1."""
+        if pin is None:
+            check(lib().nmg_set_pinning(self.h, None), self.h, "set_pinning")
+            return
+        p = np.ascontiguousarray(np.broadcast_to(np.asarray(pin, dtype=np.float64), (self.N,)))
+        check(lib().nmg_set_pinning(self.h, p.ctypes.data), self.h, "set_pinning")
 
     def set_anisotropy_poly(self, e_pow=(), e_coef=(), h_pow=(), h_coef=()):
         """Polynomial anisotropy (nmg_set_anisotropy_poly): exponents packed

@@ -25,6 +25,8 @@ __all__ = ["ParticleBatch"]
 def _material_struct(coeffs):
     if coeffs.get("anis_poly") is not None:
         raise NotImplementedError("particle batches take the second-order uniaxial anisotropy only")
+    if coeffs.get("C4", 0.0) != 0.0 or coeffs.get("C5", 0.0) != 0.0:
+        raise NotImplementedError("particle batches have no spin-transfer torque")
     mt = Material()
     mt.Ms, mt.exch_coeff, mt.C1, mt.C2, mt.C3 = (coeffs["Ms"], coeffs["exch_coeff"], coeffs["C1"], coeffs["C2"],
                                                  coeffs["C3"])

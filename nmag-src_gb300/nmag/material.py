@@ -7,7 +7,7 @@ generated code computes with:
 
 * operator-string constants (Ms, the exchange prefactor) pass through Python
   2's ``str(float)`` -- 12 significant digits (preprocess.py substitutor);
-* local-equation coefficients (the LLG C1, C2, C3 and the energy factors) are
+* local-equation coefficients (the LLG C1 ... C5 and the energy factors) are
   printed with ``%g`` -- 6 significant digits -- into generated C
   (nsim.ml:846);
 * the energy factor mu0 is printed with ``%f`` (nmag_lam.py:454-459);
@@ -64,8 +64,6 @@ class MagMaterial(object):
         else:
             self.anisotropy = None
             self.anisotropy_order = None
-        if float(llg_polarisation) != 0.0:
-            raise NotImplementedError("spin-transfer torque (llg_polarisation != 0) is outside this path")
         self._compute_su()
 
     def _compute_su(self):
@@ -82,6 +80,15 @@ class MagMaterial(object):
         self.su_llg_coeff2 = self.su_llg_coeff1 * self.su_llg_damping
         if not self.do_precession:
             self.su_llg_coeff1 = 0.0
+        # spin-transfer torque (main.py:440-451): Zhang-Li coefficients of
+        # m x (m x (J.grad)m) (adiabatic) and m x (J.grad)m (non-adiabatic)
+        su_xi = su.of(self.llg_xi, compatible_with=SI(""))
+        su_pol = su.of(self.llg_polarisation, compatible_with=SI(""))
+        su_f = -gilbert_to_ll * (su_pol * su.of(_si.bohr_magneton)
+                                 / (su.of(_si.positron_charge) * self.su_Ms * (1.0 + su_xi * su_xi)))
+        self.su_llg_stt_prefactor = 0.0 if su_f == 0.0 else 1.0
+        self.su_llg_stt_nadiab = su_f * (su_xi - self.su_llg_damping)
+        self.su_llg_stt_adiab = su_f * (1.0 + self.su_llg_damping * su_xi)
         self.su_mu0 = su.of(_si.mu0)
         self.su_exch_prefactor = 2.0 * self.su_exchange_coupling / (self.su_mu0 * self.su_Ms)
         self.su_K1 = 0.0
@@ -125,6 +132,9 @@ class MagMaterial(object):
             "E_coeff_half": g6(-0.5 * Ms * mu0f) if q else -0.5 * Ms * mu0f,
             "E_coeff_ext": g6(-1.0 * Ms * mu0f) if q else -1.0 * Ms * mu0f,
             "anis_poly": self.anisotropy_polynomial(quirks),
+            # LLG_C4 / LLG_C5 (nmag_lam.py:260-261), 0 without a polarisation
+            "C4": g6(py2str(self.su_llg_stt_adiab)) if q else self.su_llg_stt_adiab,
+            "C5": g6(py2str(self.su_llg_stt_nadiab)) if q else self.su_llg_stt_nadiab,
         }
         return c
 

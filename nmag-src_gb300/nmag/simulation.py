@@ -26,7 +26,7 @@ from .si import SI, simulation_units
 log = logging.getLogger("nmag")
 
 _FIELD_SI = {"H": SI(1.0, "A/m"), "E": SI(1.0, "J/m^3"), "phi": SI(1.0, "A"), "rho": SI(1.0, "A/m^2"),
-             "dmdt": SI(1.0, "1/s")}
+             "dmdt": SI(1.0, "1/s"), "J": SI(1.0, "A/m^2")}
 
 
 def _su_factor(kind):
@@ -193,6 +193,11 @@ class Simulation(object):
         poly = self.material.anisotropy_polynomial(self.quirks)
         if poly is not None:
             self.engine.set_anisotropy_poly(*poly)
+        self._j = None
+        if self.material.su_llg_stt_prefactor != 0.0:   # llg_polarisation given: J starts at zero
+            c = self.material.coefficients(self.quirks)
+            self.engine.set_stt(c["C4"], c["C5"])
+            self._j = np.zeros(self.engine._shape3())
         shape = self.engine._shape3()
         self._m = np.zeros(shape)
         self.engine.max_dm_step()   # the device's reference m for the first convergence check
@@ -266,6 +271,34 @@ class Simulation(object):
             h = self._vector_values(values) * simulation_units.of(unit, compatible_with=SI("A/m"))
         self._h_ext = h
         self.engine.set_h_ext(h)
+        self._ts_ready = False
+
+    def set_pinning(self, values):
+        """main.py:1918-1935: the pinning factor of dm/dt per site (1 free,
+        0 fixed): a number, a function of the position (SI) or N values.
+        Shared by the members of an ensemble."""
+        N = self.engine.N
+        if callable(values):
+            p = np.array([float(values(x)) for x in self._positions_si()], dtype=np.float64)
+        else:
+            p = np.broadcast_to(np.asarray(values, dtype=np.float64), (N,)).copy()
+        self._pin = p
+        self.engine.set_pinning(None if np.all(p == 1.0) else p)
+        self._ts_ready = False
+
+    def set_current_density(self, values, unit=None):
+        """main.py:1934-1960: the current density of the spin-transfer
+        torque, values times unit (SI, compatible with A/m^2; SI values or
+        numbers in A/m^2 without a unit)."""
+        if unit is None:
+            if isinstance(values, (list, tuple)) and values and isinstance(values[0], SI):
+                j = self._vector_values([simulation_units.of(v, compatible_with=SI("A/m^2")) for v in values])
+            else:
+                j = self._vector_values(values) / _su_factor("J")
+        else:
+            j = self._vector_values(values) * simulation_units.of(unit, compatible_with=SI("A/m^2"))
+        self._j = j
+        self.engine.set_current_density(j)
         self._ts_ready = False
 
     def set_params(self, stopping_dm_dt=None, ts_rel_tol=None, ts_abs_tol=None, exact_tstop=None):
@@ -402,6 +435,12 @@ class Simulation(object):
             return self._m.copy()
         if subfieldname.startswith("H_ext"):
             return self._h_ext * _su_factor("H")
+        if subfieldname == "pin":
+            p = getattr(self, "_pin", None)
+            return p.copy() if p is not None else np.ones(self.engine.N)
+        if subfieldname.startswith("current_density"):
+            j = self._j if getattr(self, "_j", None) is not None else np.zeros_like(self._h_ext)
+            return j * _su_factor("J")
         f = self.engine.eval_fields()
         for key in ("H_exch", "H_demag", "H_anis", "H_total"):
             if subfieldname.startswith(key):

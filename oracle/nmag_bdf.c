@@ -195,6 +195,8 @@ static void block_of_J(const om_bdf *B, int i, double Jb[3][3]) {
     double t2[3] = {m[1] * u[2] - m[2] * u[1], m[2] * u[0] - m[0] * u[2], m[0] * u[1] - m[1] * u[0]};
     for (int d = 0; d < 3; ++d) Jb[d][c] = C1 * a[d] + C2 * (t1[d] + t2[d]);
   }
+  if (S->pin) /* the Jacobian rows carry the pin factor (nmag_lam.py:432-436) */
+    for (int d = 0; d < 3; ++d) for (int c = 0; c < 3; ++c) Jb[d][c] *= S->pin[i];
 }
 
 static void psolve(om_bdf *B, const double *r, double *z) {

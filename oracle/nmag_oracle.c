@@ -481,7 +481,42 @@ void om_state_free(om_state *S) {
   free(S->h_anis); free(S->h_total); free(S->dmdt); free(S->tmp_b1); free(S->tmp_b2);
   for (int k = 0; k < 2; ++k) { free(S->basis_b[k]); free(S->basis_x[k]); }
   free(S->an_epow); free(S->an_hpow); free(S->an_ecoef); free(S->an_hcoef);
+  free(S->stt_j); free(S->stt_dmdc); free(S->pin);
   memset(S, 0, sizeof(*S));
+}
+
+int om_set_pinning(om_state *S, const double *pin) {
+  const int N = S->M->n_nodes;
+  free(S->pin);
+  S->pin = NULL;
+  if (pin) { S->pin = xcalloc(N, sizeof(double)); memcpy(S->pin, pin, sizeof(double) * N); }
+  return 0;
+}
+
+int om_set_stt(om_state *S, double c4, double c5, const double *j) {
+  const int N = S->M->n_nodes;
+  if (!S->stt_j) { S->stt_j = xcalloc(3 * (size_t)N, sizeof(double)); S->stt_dmdc = xcalloc(3 * (size_t)N, sizeof(double)); }
+  if (j) memcpy(S->stt_j, j, sizeof(double) * 3 * N);
+  else memset(S->stt_j, 0, sizeof(double) * 3 * N);
+  S->stt_c4 = c4; S->stt_c5 = c5;
+  return 0;
+}
+
+/* set_dm_dcurrent (nmag_lam.py:892-903): SM*V op_grad_m, site-wise
+ * grad_m(i,j) current_density(j), CFBOX. */
+static void dm_dcurrent(const om_state *S, const double *m, double *out) {
+  const om_mesh *M = S->M;
+  const int N = M->n_nodes;
+  for (int a = 0; a < N; ++a) {
+    double g[3][3] = {{0}};
+    for (int k = M->row_ptr[a]; k < M->row_ptr[a + 1]; ++k) {
+      const double *mb = m + 3 * (size_t)M->col_idx[k];
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 3; ++d) g[c][d] += M->G[d][k] * mb[c];
+    }
+    const double *J = S->stt_j + 3 * (size_t)a;
+    for (int c = 0; c < 3; ++c) out[3 * (size_t)a + c] = ((g[c][0] * J[0] + g[c][1] * J[1]) + g[c][2] * J[2]) / M->vol[a];
+  }
 }
 
 int om_set_anisotropy_poly(om_state *S, int ne, const int32_t *epow, const double *ecoef, int nh,
@@ -754,6 +789,8 @@ int om_rhs(om_state *S, const double *m, double *dmdt_out) {
   if (st) return st;
   exch(S, m, S->h_exch);
   const om_material *mt = &S->mat;
+  const int stt = S->stt_j && (S->stt_c4 != 0.0 || S->stt_c5 != 0.0);
+  if (stt) dm_dcurrent(S, m, S->stt_dmdc);
   for (int i = 0; i < N; ++i) {
     const double *mi = m + 3 * (size_t)i;
     double *ha = S->h_anis + 3 * (size_t)i;
@@ -767,6 +804,15 @@ int om_rhs(om_state *S, const double *m, double *dmdt_out) {
     for (int d = 0; d < 3; ++d)
       ht[d] = ((S->h_ext[3 * i + d] + S->h_exch[3 * i + d]) + ha[d]) + S->h_demag[3 * i + d];
     llg(mi, ht, mt->C1, mt->C2, mt->C3, S->dmdt + 3 * (size_t)i);
+    if (stt) {   /* + C4 m x (m x u) + C5 m x u, after the C1..C3 terms */
+      const double *u = S->stt_dmdc + 3 * (size_t)i;
+      double mxu[3] = {mi[1] * u[2] - mi[2] * u[1], mi[2] * u[0] - mi[0] * u[2], mi[0] * u[1] - mi[1] * u[0]};
+      double mxmxu[3] = {mi[1] * mxu[2] - mi[2] * mxu[1], mi[2] * mxu[0] - mi[0] * mxu[2],
+                         mi[0] * mxu[1] - mi[1] * mxu[0]};
+      double *o = S->dmdt + 3 * (size_t)i;
+      for (int d = 0; d < 3; ++d) o[d] = (o[d] + S->stt_c4 * mxmxu[d]) + S->stt_c5 * mxu[d];
+    }
+    if (S->pin) for (int d = 0; d < 3; ++d) S->dmdt[3 * (size_t)i + d] *= S->pin[i];
   }
   if (dmdt_out) memcpy(dmdt_out, S->dmdt, sizeof(double) * 3 * N);
   S->n_rhs++;
@@ -827,6 +873,7 @@ void om_jv(const om_state *S, const double *mJ, const double *HJ, const double *
     double u[3] = {wxH[0] + mxhv[0], wxH[1] + mxhv[1], wxH[2] + mxhv[2]};
     double t2[3] = {m[1] * u[2] - m[2] * u[1], m[2] * u[0] - m[0] * u[2], m[0] * u[1] - m[1] * u[0]};
     for (int d = 0; d < 3; ++d) out[3 * i + d] = C1 * a[d] + C2 * (t1[d] + t2[d]);
+    if (S->pin) for (int d = 0; d < 3; ++d) out[3 * i + d] *= S->pin[i];
   }
 }
 

@@ -100,6 +100,11 @@ typedef struct om_state {
   int an_ne, an_nh;
   int32_t *an_epow, *an_hpow;
   double *an_ecoef, *an_hcoef;
+  /* spin-transfer torque (om_set_stt): LLG_C4, LLG_C5, current density (3N,
+     owned) and the last dm_dcurrent (3N) */
+  double stt_c4, stt_c5;
+  double *stt_j, *stt_dmdc;
+  double *pin;   /* N, owned; NULL = 1 everywhere (om_set_pinning) */
 } om_state;
 
 
@@ -114,6 +119,15 @@ void om_state_free(om_state *S);
  * each (c)*m(0)*...*m(2) left to right.  ne = nh = 0 removes it. */
 int om_set_anisotropy_poly(om_state *S, int ne, const int32_t *epow, const double *ecoef, int nh,
                            const int32_t *hpow, const double *hcoef);
+/* Spin-transfer torque (nmag_lam.py:417-424,872-903): dm/dt gains
+ * c4 m x (m x u) + c5 m x u, u = dm_dcurrent computed each RHS as
+ * op_grad_m (G_d m_c, no sign), site-wise grad_m(c,d) J(d) summed over d in
+ * order, then divided by the box volume.  j: 3N current density (NULL =
+ * zero). */
+int om_set_stt(om_state *S, double c4, double c5, const double *j);
+/* Pinning field (nmag_lam.py:417-436): every dm/dt term and the Jacobian
+ * rows carry the factor pin of their node.  NULL = 1 everywhere. */
+int om_set_pinning(om_state *S, const double *pin);
 /* Full RHS: H_exch, H_demag (FEM/BEM), H_anis, H_total, dm/dt (nmag_lam.py:734-832). */
 int om_rhs(om_state *S, const double *m, double *dmdt_out);
 /* Energy densities E_exch, E_demag, E_ext, E_anis, E_total (5 x N) from the last fields. */

@@ -62,7 +62,9 @@ class OmState(C.Structure):
                 ("gram", (C.c_double * 100) * 2), ("bcount", C.c_int * 2), ("bhead", C.c_int * 2),
                 ("an_ne", C.c_int), ("an_nh", C.c_int), ("an_epow", C.POINTER(C.c_int32)),
                 ("an_hpow", C.POINTER(C.c_int32)), ("an_ecoef", C.POINTER(C.c_double)),
-                ("an_hcoef", C.POINTER(C.c_double))]
+                ("an_hcoef", C.POINTER(C.c_double)), ("stt_c4", C.c_double), ("stt_c5", C.c_double),
+                ("stt_j", C.POINTER(C.c_double)), ("stt_dmdc", C.POINTER(C.c_double)),
+                ("pin", C.POINTER(C.c_double))]
 
 
 class OmStats(C.Structure):
@@ -98,6 +100,8 @@ def lib():
         L.om_rhs.argtypes = [C.POINTER(OmState), _f64p, C.c_void_p]
         L.om_set_anisotropy_poly.argtypes = [C.POINTER(OmState), C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                              C.c_void_p, C.c_void_p]
+        L.om_set_stt.argtypes = [C.POINTER(OmState), C.c_double, C.c_double, C.c_void_p]
+        L.om_set_pinning.argtypes = [C.POINTER(OmState), C.c_void_p]
         L.om_energy_density.argtypes = [C.POINTER(OmState), _f64p, _f64p]
         L.om_jv.argtypes = [C.POINTER(OmState), _f64p, _f64p, _f64p, _f64p]
         L.om_bdf_create.argtypes = [C.POINTER(OmState), C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
@@ -224,6 +228,19 @@ class OracleSim(object):
         self.N = omesh.n_nodes
         self._bdf = None
 
+    def set_stt(self, c4, c5, j=None):
+        """Spin-transfer coefficients and current density (3N or broadcast)."""
+        jj = None if j is None else np.ascontiguousarray(np.broadcast_to(np.asarray(j, dtype=np.float64),
+                                                                         (self.N, 3))).reshape(-1)
+        lib().om_set_stt(C.byref(self._s), float(c4), float(c5), None if jj is None else jj.ctypes.data)
+
+    def set_pinning(self, pin=None):
+        """Pinning factor per node (N values; None = 1 everywhere)."""
+        pp = None if pin is None else np.ascontiguousarray(np.broadcast_to(np.asarray(pin, dtype=np.float64),
+                                                                           (self.N,)))
+        self._pin = pp   # the C side copies; kept for reference
+        lib().om_set_pinning(C.byref(self._s), None if pp is None else pp.ctypes.data)
+
     def set_h_ext(self, h):
         h = np.broadcast_to(np.asarray(h, dtype=np.float64), (self.N, 3)).reshape(-1)
         np.ctypeslib.as_array(self._s.h_ext, shape=(3 * self.N,))[:] = h
@@ -239,7 +256,8 @@ class OracleSim(object):
     def field(self, name):
         n = self.N
         ptr = getattr(self._s, {"H_exch": "h_exch", "H_demag": "h_demag", "H_anis": "h_anis",
-                                "H_total": "h_total", "H_ext": "h_ext", "dmdt": "dmdt"}[name])
+                                "H_total": "h_total", "H_ext": "h_ext", "dmdt": "dmdt",
+                                "dm_dcurrent": "stt_dmdc"}[name])
         return np.ctypeslib.as_array(ptr, shape=(3 * n,)).copy().reshape(n, 3)
 
     def scalar_field(self, name):

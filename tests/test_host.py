@@ -40,8 +40,9 @@ def test_material_coefficients_and_quirks():
         assert abs(q["C1"] / g["C1"] - 1) < 5e-6
     m = nmag.MagMaterial("x", do_precession=False)
     assert m.coefficients()["C1"] == 0.0
-    with pytest.raises(NotImplementedError):
-        nmag.MagMaterial("stt", llg_polarisation=0.5)
+    # a polarisation switches the spin-transfer coefficients on
+    stt = nmag.MagMaterial("stt", llg_polarisation=0.5).coefficients()
+    assert stt["C4"] != 0.0 and stt["C5"] != 0.0
 
 
 @pytest.mark.parametrize("n", [4, 8])
