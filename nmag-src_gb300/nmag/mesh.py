@@ -48,6 +48,38 @@ class Mesh(object):
     def scaled(self, factor):
         return Mesh(self.points * factor, self.simplices, self.regions)
 
+    def tet_volumes(self):
+        """|det| / 6 per simplex."""
+        p = self.points[self.simplices]
+        return np.abs(np.linalg.det(p[:, 1:] - p[:, :1])) / 6.0
+
+    def locate(self, pos, eps=1e-10):
+        """(simplex, barycentric coordinates (4,)) of a point, or None when it
+        lies outside every simplex; on a shared face or edge the first
+        simplex containing it is taken (P1 fields agree there)."""
+        if getattr(self, "_inv", None) is None:
+            p = self.points[self.simplices]
+            self._p0 = p[:, 0]
+            self._inv = np.linalg.inv(np.transpose(p[:, 1:] - p[:, :1], (0, 2, 1)))
+        x = np.asarray(pos, dtype=np.float64).reshape(3)
+        lam = np.einsum("tij,tj->ti", self._inv, x[None, :] - self._p0)
+        bary = np.concatenate([1.0 - lam.sum(1, keepdims=True), lam], axis=1)
+        inside = np.nonzero(bary.min(1) >= -eps)[0]
+        if len(inside) == 0:
+            return None
+        t = int(inside[0])
+        return t, bary[t]
+
+    def interpolate(self, values, pos, eps=1e-10):
+        """Value of the P1 (nodal) field ``values`` (N, ...) at ``pos``, or None
+        outside the mesh."""
+        hit = self.locate(pos, eps)
+        if hit is None:
+            return None
+        t, bary = hit
+        v = np.asarray(values, dtype=np.float64)[self.simplices[t]]
+        return np.tensordot(bary, v, axes=(0, 0))
+
 
 _PERMS = list(itertools.permutations((0, 1, 2)))
 

@@ -140,6 +140,7 @@ class Simulation(object):
         self._countdown_initial = 2
         self._countdown = 2
         self.engine = None
+        self._timers = {}
         self.mesh = None
         self.node_map = None    # magnetic nodes -> nodes of the loaded mesh (vacuum present)
         self.material = None
@@ -173,6 +174,11 @@ class Simulation(object):
         if np.any(m.regions <= 0):
             m, self.node_map = _mesh.magnetic_part(m)
         self.material = mats[0]
+        # regions of each material name (main.py:1182-1191: region ids 1, 2, ...)
+        self._regions_by_material = {}
+        for rid, (region_name, mat) in enumerate(region_names_and_mag_mats, start=1):
+            for mt in (mat if isinstance(mat, (list, tuple)) else [mat]):
+                self._regions_by_material.setdefault(mt.name, []).append(rid)
         scale = simulation_units.of(unit_length, compatible_with=SI("m"))
         self.mesh = _mesh.Mesh(m.points * scale, m.simplices, m.regions)
         opts = Options()
@@ -341,6 +347,7 @@ class Simulation(object):
             return target_time
         prev_m = self._m
         t_stage, stats = self.engine.ts_advance(target_su, exact_tstop, max_it)
+        self._timers["advance_time"] = self._timers.get("advance_time", 0.0) + self.engine.timings()[0] * 1e-3
         self._m = self.engine.get_m()
         delta_steps = stats["nst"] - self._last_nst
         self._last_nst = stats["nst"]
@@ -457,6 +464,84 @@ class Simulation(object):
                 if subfieldname.startswith(key):
                     return E[key] * _su_factor("E")
         raise KeyError("unknown subfield %r" % subfieldname)
+
+    _UNITS = {"m": SI(1.0), "M": SI(1.0, "A/m"), "H": SI(1.0, "A/m"), "E": SI(1.0, "J/m^3"),
+              "phi": SI(1.0, "A"), "rho": SI(1.0, "A/m^2"), "dmdt": SI(1.0, "1/s"), "pin": SI(1.0),
+              "current_density": SI(1.0, "A/m^2")}
+
+    def _unit_of(self, subfieldname):
+        for key in ("current_density", "dmdt", "phi", "rho", "pin"):
+            if subfieldname.startswith(key):
+                return self._UNITS[key]
+        return self._UNITS[subfieldname.split("_")[0] if subfieldname[0] in "mMHE" else subfieldname]
+
+    def probe_subfield_siv(self, subfieldname, pos, unit=None):
+        """main.py:1651-1700: the subfield at a position given in metres
+        (floats), linearly interpolated in the simplex containing it; a float
+        for scalar subfields, a list for vectors; None outside the magnetic
+        mesh."""
+        vals = self.get_subfield(subfieldname)
+        if vals.ndim == 3:   # an ensemble: member 0, as get_subfield_average_siv
+            vals = vals[0]
+        pos_su = np.asarray(pos, dtype=np.float64) * simulation_units.of(SI(1.0, "m"))
+        v = self.mesh.interpolate(vals, pos_su)
+        if v is None:
+            return None
+        return float(v) if np.ndim(v) == 0 else [float(x) for x in v]
+
+    def probe_subfield(self, subfieldname, pos, unit=None):
+        """main.py:1570-1650: as probe_subfield_siv with the position a list of
+        SI objects (or an SI vector) and the result SI objects."""
+        pos_m = [simulation_units.of(p, compatible_with=SI("m")) * simulation_units.conversion_factor_of(SI("m"))
+                 for p in pos]
+        data = self.probe_subfield_siv(subfieldname, pos_m)
+        if data is None:
+            return None
+        u = unit if unit is not None else self._unit_of(subfieldname)
+        return [x * u for x in data] if isinstance(data, list) else data * u
+
+    def get_subfield_sites(self, subfieldname):
+        """main.py:2055-2077: node indices (of the loaded mesh) of the sites,
+        one list per site."""
+        self._unit_of(subfieldname)   # KeyError for unknown subfields
+        nodes = self.node_map if self.node_map is not None else np.arange(self.mesh.n_nodes)
+        return np.asarray(nodes, dtype=np.int64).reshape(-1, 1)
+
+    def get_subfield_positions(self, subfieldname, pos_units=SI("m")):
+        """main.py:2079-2103: site positions (site order, as get_subfield)
+        in units of pos_units."""
+        self._unit_of(subfieldname)
+        return self.mesh.points / simulation_units.of(pos_units, compatible_with=SI("m"))
+
+    def material_volume(self, material_name):
+        """main.py:2189-2226: volume (simulation units) of the regions of a
+        material; None: the whole magnetic mesh."""
+        vol = self.mesh.tet_volumes()
+        if material_name is None:
+            return float(vol.sum())
+        regions = self._regions_by_material[material_name]
+        return float(vol[np.isin(self.mesh.regions, regions)].sum())
+
+    def get_timers(self, timers=()):
+        """main.py:1904-1916: (name, None, seconds) per timer; the device time
+        of advance_time accumulated over the calls."""
+        names = list(timers) or sorted(self._timers)
+        return [(k, None, self._timers.get(k, 0.0)) for k in names]
+
+    def save_mesh(self, filename):
+        """main.py:1228-1232: the magnetic mesh in nmesh ASCII, in simulation
+        units of length (as the reference's mesh object stores it)."""
+        _mesh.save_ascii(self.mesh, filename)
+
+    def do_next_stage(self, stage=None):
+        """main.py:2733-2735 / clock.py:84-94: start the next stage (or the
+        given one)."""
+        self.max_dm_dt = None
+        self.clock.stage = self.clock.stage + 1 if stage is None else stage
+        self.clock.stage_step = 0
+        self.clock.stage_time_su = 0.0
+        self.clock.convergence = False
+        self._ts_ready = False
 
     def get_subfield_average_siv(self, field, subfield=None):
         name = field if subfield is None else field

@@ -192,6 +192,44 @@ def test_simulation_api_advance_and_relax(small_box):
     assert avg[2] > 0.99
 
 
+def test_simulation_probe_sites_volumes_timers(small_box, tmp_path):
+    """probe_subfield(_siv), get_subfield_sites/positions, material_volume,
+    get_timers, save_mesh and do_next_stage (main.py:1228,1570-1700,1904,
+    2055-2103,2189,2733)."""
+    import nmag
+    from nmag import SI
+    mat = permalloy(0.5)
+    sim = nmag.Simulation("probe")
+    sim.load_mesh(small_box, [("box", mat)], unit_length=SI(1e-9, "m"))
+    sim.set_m(lambda p: [1.0, 0.2 + 1e8 * p[0], 0.1])     # normalised by set_m
+    sim.set_H_ext([0.0, 0.0, 1e5], SI(1.0, "A/m"))
+    m = sim.get_subfield("m")
+    x = sim.get_subfield_positions("m")                   # metres, site order
+    assert np.allclose(x, small_box.points * 1e-9)
+    assert np.array_equal(sim.get_subfield_sites("m_Py")[:, 0], np.arange(small_box.n_nodes))
+    # at a node the probe returns the node's value; between nodes the P1 interpolant
+    k = 5
+    assert np.allclose(sim.probe_subfield_siv("m_Py", list(x[k])), m[k], atol=1e-14)
+    tet = small_box.simplices[3]
+    c = x[tet].mean(0)
+    assert np.allclose(sim.probe_subfield_siv("m_Py", list(c)), m[tet].mean(0), atol=1e-14)
+    h = sim.get_subfield("H_demag")
+    got = sim.probe_subfield("H_demag", [SI(v, "m") for v in c])
+    assert np.allclose([g.value for g in got], h[tet].mean(0), rtol=1e-9)
+    assert sim.probe_subfield_siv("m", [1.0, 1.0, 1.0]) is None
+    lo, hi = small_box.points.min(0), small_box.points.max(0)
+    assert abs(sim.material_volume("Py") - np.prod(hi - lo)) < 1e-9
+    assert sim.material_volume(None) == sim.material_volume("Py")
+    sim.advance_time(SI(2e-12, "s"))
+    (name, _, secs), = sim.get_timers()
+    assert name == "advance_time" and secs > 0.0
+    sim.save_mesh(str(tmp_path / "m.nmesh"))
+    back = nmag.mesh.load(str(tmp_path / "m.nmesh"))
+    assert np.allclose(back.points, small_box.points) and np.array_equal(back.simplices, small_box.simplices)
+    sim.do_next_stage()
+    assert sim.clock.stage == 2 and sim.clock.stage_step == 0 and sim.clock.stage_time_su == 0.0
+
+
 def test_max_dm_step_tracks_previous_m(small_box):
     """nmg_max_dm_step: distance to m at the previous call or set_m, on the
     device; equal to the host computation on the same arrays."""
