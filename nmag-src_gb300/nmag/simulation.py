@@ -500,6 +500,20 @@ class Simulation(object):
         u = unit if unit is not None else self._unit_of(subfieldname)
         return [x * u for x in data] if isinstance(data, list) else data * u
 
+    def probe_H_demag_siv(self, pos, pos_unit=SI("m"), epsilon=1e-7):
+        """main.py:2124-2187: H_demag (A/m) at a position given in units of
+        pos_unit.  Inside the magnetic mesh this is the probed H_demag field
+        (nsimexec.ml:4248-4285 probes the field first); outside, the
+        reference's parallel linalg machine has no potential evaluation
+        (nsim.ml:3703, get_potential fails), and neither is there one here."""
+        pos_m = np.asarray(pos, dtype=np.float64) * (simulation_units.of(pos_unit, compatible_with=SI("m"))
+                                                     * simulation_units.conversion_factor_of(SI("m")))
+        v = self.probe_subfield_siv("H_demag", list(pos_m))
+        if v is None:
+            raise NotImplementedError("probe_H_demag_siv: the exterior demag field (get_potential) is not "
+                                      "available, as in the reference's parallel linalg machine")
+        return v
+
     def get_subfield_sites(self, subfieldname):
         """main.py:2055-2077: node indices (of the loaded mesh) of the sites,
         one list per site."""

@@ -217,6 +217,9 @@ def test_simulation_probe_sites_volumes_timers(small_box, tmp_path):
     got = sim.probe_subfield("H_demag", [SI(v, "m") for v in c])
     assert np.allclose([g.value for g in got], h[tet].mean(0), rtol=1e-9)
     assert sim.probe_subfield_siv("m", [1.0, 1.0, 1.0]) is None
+    assert np.allclose(sim.probe_H_demag_siv(list(c / 1e-9), pos_unit=SI(1e-9, "m")), h[tet].mean(0), rtol=1e-9)
+    with pytest.raises(NotImplementedError):
+        sim.probe_H_demag_siv([1.0, 1.0, 1.0])
     lo, hi = small_box.points.min(0), small_box.points.max(0)
     assert abs(sim.material_volume("Py") - np.prod(hi - lo)) < 1e-9
     assert sim.material_volume(None) == sim.material_volume("Py")
