@@ -13,6 +13,7 @@ from __future__ import annotations
 import logging
 import math
 import os
+import re
 import time as _time
 
 import numpy as np
@@ -21,6 +22,7 @@ from . import mesh as _mesh
 from . import si as _si
 from ._lib import Engine, Material, Options, NmagGpuError
 from .material import MagMaterial
+from .when import at, every, never
 from .si import SI, simulation_units
 
 log = logging.getLogger("nmag")
@@ -39,7 +41,15 @@ class Clock(dict):
     def __init__(self):
         super().__init__(id=-1, stage=1, step=0, time_su=0.0, stage_step=0, stage_time_su=0.0,
                          real_time=0.0, stage_end=False, convergence=False, exit_hysteresis=False,
-                         last_step_dt_su=0.0, time_reached_su=0.0)
+                         last_step_dt_su=0.0, time_reached_su=0.0, zero_stage_step=0, zero_stage_time_su=0.0)
+
+    def view(self):
+        """The counters the save / do schedules read (times in simulation
+        units, real time in seconds)."""
+        return {"step": self.step, "stage_step": self.stage_step, "time": self.time_su,
+                "stage_time": self.stage_time_su, "real_time": self.real_time, "stage": self.stage,
+                "convergence": bool(self.convergence), "stage_end": bool(self.stage_end),
+                "zero_stage_step": self.zero_stage_step, "zero_stage_time": self.zero_stage_time_su}
 
     def __getattr__(self, k):
         try:
@@ -51,47 +61,44 @@ class Clock(dict):
         self[k] = v
 
 
-class every(object):
-    """Schedule: every('step', 5), every('time', SI(1e-12, 's')) (nsim/when.py)."""
-
-    def __init__(self, what, value, first=0):
-        self.what, self.value, self.first = what, value, first
-
-    def next_delta(self, clock):
-        if self.what == "step":
-            n = int(self.value)
-            return ("step", n - (clock.stage_step % n) if clock.stage_step % n else n)
-        if self.what == "time":
-            dt = simulation_units.of(self.value, compatible_with=SI("s")) if isinstance(self.value, SI) else float(self.value)
-            k = math.floor(clock.stage_time_su / dt + 1e-9) + 1
-            return ("time", k * dt - clock.stage_time_su)
-        return (None, None)
-
-    def match(self, clock):
-        if self.what == "step":
-            return clock.stage_step % int(self.value) == 0
-        if self.what == "time":
-            dt = simulation_units.of(self.value, compatible_with=SI("s")) if isinstance(self.value, SI) else float(self.value)
-            r = clock.stage_time_su / dt
-            return abs(r - round(r)) < 1e-9
-        return False
+_SPACES = re.compile(r"[ \t]+")
 
 
-class at(object):
-    """Schedule at an event: at('stage_end'), at('convergence'), at('step', n)."""
+def _normalise_action(name):
+    """hysteresis.py:42-54: 'Save  Fields' -> 'save_fields'."""
+    return _SPACES.sub("_", name.lower())
 
-    def __init__(self, what, value=None):
-        self.what, self.value = what, value
 
-    def next_delta(self, clock):
-        return (None, None)
+def _next_deltas(event, view, suggest=None, tols=None):
+    """hysteresis.py:132-159: (steps, simulation time, real time) to the next
+    firing of event, each None when it does not constrain that counter; the
+    minimum with ``suggest``."""
+    def delta(name):
+        n = event.next_time(name, view, tols=tols)
+        return None if isinstance(n, bool) else n - view[name]
 
-    def match(self, clock):
-        if self.what in ("stage_end", "convergence"):
-            return bool(clock.stage_end)
-        if self.what == "step":
-            return clock.stage_step == self.value
-        return False
+    def least(vals):
+        vals = [v for v in vals if v is not None]
+        return min(vals) if vals else None
+    ds, dt, dr = suggest if suggest is not None else (None, None, None)
+    return (least([delta("step"), delta("stage_step"), ds]), least([delta("time"), delta("stage_time"), dt]),
+            least([delta("real_time"), dr]))
+
+
+def _next_time(event, view, tols=None):
+    """hysteresis.py:161-198: (step, time, real time) of the next firing,
+    counted from the start of the stage."""
+    def at_(name, zero=None):
+        n = event.next_time(name, view, tols=tols)
+        if isinstance(n, bool):
+            return None
+        return n - view[zero] if zero else n
+
+    def least(vals):
+        vals = [v for v in vals if v is not None]
+        return min(vals) if vals else None
+    return (least([at_("step", "zero_stage_step"), at_("stage_step")]),
+            least([at_("time", "zero_stage_time"), at_("stage_time")]), at_("real_time"))
 
 
 class Simulation(object):
@@ -346,7 +353,9 @@ class Simulation(object):
         if target_su == 0:
             return target_time
         prev_m = self._m
+        wall0 = _time.time()
         t_stage, stats = self.engine.ts_advance(target_su, exact_tstop, max_it)
+        self.clock.real_time += _time.time() - wall0   # clock.py: real time spent advancing
         self._timers["advance_time"] = self._timers.get("advance_time", 0.0) + self.engine.timings()[0] * 1e-3
         self._m = self.engine.get_m()
         delta_steps = stats["nst"] - self._last_nst
@@ -367,72 +376,126 @@ class Simulation(object):
         return SI(t_stage * simulation_units.conversion_factor_of(SI("s")), "s")
 
     def is_converged(self):
-        """convergence.py:54-100: max dm/dt below stopping_dm_dt twice in a row."""
+        """convergence.py:54-100 / main.py:2737-2760: max dm/dt below
+        stopping_dm_dt twice in a row; sets clock.convergence."""
+        self.clock.convergence = False
         if self.max_dm_dt is None:
             return False
         if self.max_dm_dt < self.stopping_dm_dt:
             self._countdown -= 1
             if self._countdown < 1:
                 self._countdown = self._countdown_initial
+                self.clock.convergence = True
                 return True
             return False
         self._countdown = self._countdown_initial
         return False
 
-    def hysteresis(self, H_ext_list, save=None, do=None, convergence_check=every("step", 5)):
-        """hysteresis.py:244-557: for each field, relax until converged."""
-        save = list(save or [])
-        do = list(do or [])
-        for stage_idx, H in enumerate(H_ext_list):
-            self.clock.stage = stage_idx + 1
+    # predefined things to save / do (simulation_core.py:180-200,256-271)
+    @staticmethod
+    def hysteresis_next_stage(sim):
+        """End the current stage (the 'next_stage' action)."""
+        sim.clock.stage_end = True
+
+    @staticmethod
+    def hysteresis_exit(sim):
+        """Leave the hysteresis loop (the 'exit' action)."""
+        sim.clock.exit_hysteresis = True
+        sim.clock.stage_end = True
+
+    _ACTIONS = {"save_averages": lambda sim: sim.save_data(avoid_same_step=True),
+                "save_fields": lambda sim: sim.save_data(fields="all", avoid_same_step=True),
+                "save_field_m": lambda sim: sim.save_data(fields=["m"], avoid_same_step=True),
+                "save_restart": lambda sim: sim.save_restart_file(),
+                "do_next_stage": lambda sim: Simulation.hysteresis_next_stage(sim),
+                "do_exit": lambda sim: Simulation.hysteresis_exit(sim)}
+
+    def _join_save_and_do(self, save, do):
+        """hysteresis.py:56-130: (function, when, key) for every thing of the
+        (thing, ..., when) tuples, the do list first; strings name the
+        predefined actions ('averages', 'save fields', 'next_stage', ...)."""
+        joint, keys = [], set()
+        for prefix, items in (("do", do), ("save", save)):
+            try:
+                items = [list(t) for t in items]
+            except TypeError:
+                raise ValueError("hysteresis: '%s' must be a list of (thing, ..., when) tuples" % prefix)
+            for item in items:
+                if len(item) < 2:
+                    raise ValueError("hysteresis: '%s' must be a list of (thing, ..., when) tuples" % prefix)
+                when = item[-1]
+                for thing in item[:-1]:
+                    if callable(thing):
+                        fn, key = thing, ("fn", id(thing))
+                    elif isinstance(thing, str):
+                        name = _normalise_action(prefix + " " + thing)
+                        if name not in self._ACTIONS:
+                            name = _normalise_action(thing)
+                        if name not in self._ACTIONS:
+                            raise ValueError("hysteresis: you want to %s '%s' but I don't know how to do it; "
+                                             "available: %s" % (prefix, thing, ", ".join(sorted(self._ACTIONS))))
+                        fn, key = self._ACTIONS[name], name
+                    else:
+                        raise ValueError("hysteresis: things to %s are strings or functions, not %r" % (prefix, thing))
+                    if key in keys:
+                        raise ValueError("hysteresis: %s is given twice in 'save' / 'do'; combine the schedules "
+                                         "with | instead" % (thing,))
+                    keys.add(key)
+                    joint.append((fn, when, key))
+        return joint
+
+    def hysteresis(self, H_ext_list, save=(("averages", "fields", at("stage_end")),), do=(),
+                   convergence_check=every("step", 5)):
+        """hysteresis.py:244-557: for each applied field (None keeps the
+        current one) start a stage and integrate until converged, running
+        the save / do actions whenever their schedules fire."""
+        actions = self._join_save_and_do(save, do)
+        tol_time = simulation_units.of(SI(1e-20, "s"))   # hysteresis.py:420-423
+        tols = {"time": tol_time, "stage_time": tol_time}
+        next_save = {}
+        stage = self.clock.stage
+        self.clock.exit_hysteresis = False
+        for H in list(H_ext_list)[stage - 1:]:
+            self.do_next_stage(stage=stage)
+            stage = None
             self.clock.stage_end = False
             if H is not None:
-                if isinstance(H, (list, tuple)) and len(H) == 3 and all(isinstance(v, SI) for v in H):
-                    self.set_H_ext(H)
-                elif isinstance(H, tuple) and len(H) == 2 and isinstance(H[1], SI):
+                if isinstance(H, tuple) and len(H) == 2 and isinstance(H[1], SI):
                     self.set_H_ext(H[0], H[1])
                 else:
                     self.set_H_ext(H)
-            self.max_dm_dt = None
             self._countdown = self._countdown_initial
-            self._last_nst = 0
             self.reinitialise(initial_time=0)
+            for _, when, key in actions:
+                next_save[key] = _next_time(when, self.clock.view(), tols)
             while True:
                 self.clock.stage_end = self.is_converged()
-                for what, when in save + do:
-                    if when.match(self.clock):
-                        self._do_action(what)
+                deltas = _next_deltas(convergence_check, self.clock.view(), tols=tols)
+                for fn, when, key in actions:
+                    v = self.clock.view()
+                    nst = _next_time(when, v, tols)
+                    if when.match_time(v) or nst != next_save[key]:
+                        fn(self)
+                    next_save[key] = nst
+                    deltas = _next_deltas(when, self.clock.view(), suggest=deltas, tols=tols)
+                d_step, d_time, _ = deltas
+                if d_time is None:
+                    target, max_it = self.max_time_reached, d_step
+                else:
+                    target, max_it = self.clock.stage_time_su + d_time, (-1 if d_step is None else d_step)
                 if self.clock.exit_hysteresis:
                     return
                 if self.clock.stage_end:
                     break
-                kind, delta = convergence_check.next_delta(self.clock)
-                if kind == "step":
-                    target, max_it = self.max_time_reached, int(delta)
-                elif kind == "time":
-                    target, max_it = self.clock.stage_time_su + delta, -1
-                else:
-                    target, max_it = self.max_time_reached, -1
                 t = self.advance_time(target, max_it=max_it)
                 if simulation_units.of(t, compatible_with=SI("s")) > 0.99 * self.max_time_reached:
                     raise RuntimeError("Simulation time reached %s: are you starting from a zero torque "
                                        "configuration?" % self.max_time_reached)
 
-    def relax(self, save=None, do=None, convergence_check=every("step", 5)):
-        """hysteresis.py:207-242: hysteresis([None])."""
-        return self.hysteresis([None], save=save, do=do, convergence_check=convergence_check)
-
-    def _do_action(self, what):
-        if callable(what):
-            what(self)
-        elif what == "averages":
-            self.save_data()
-        elif what == "fields":
-            self.save_data(fields="all")
-        elif what == "restart":
-            self.save_restart_file()
-        elif what == "exit":
-            self.clock.exit_hysteresis = True
+    def relax(self, H_applied=None, save=(("averages", "fields", at("stage_end")),), do=(),
+              convergence_check=every("step", 5)):
+        """hysteresis.py:207-242: hysteresis([H_applied])."""
+        return self.hysteresis([H_applied], save=save, do=do, convergence_check=convergence_check)
 
     # ---- read-out ------------------------------------------------------------
     def get_subfield(self, subfieldname, units=None):
@@ -555,6 +618,8 @@ class Simulation(object):
         self.clock.stage_step = 0
         self.clock.stage_time_su = 0.0
         self.clock.convergence = False
+        self.clock.zero_stage_step = self.clock.step
+        self.clock.zero_stage_time_su = self.clock.time_su
         self._ts_ready = False
 
     def get_subfield_average_siv(self, field, subfield=None):
@@ -586,16 +651,25 @@ class Simulation(object):
         return e * _su_factor("E") * (simulation_units.conversion_factor_of(SI("m")) ** 3)
 
     def save_data(self, fields=None, avoid_same_step=False):
-        """Append averages to <name>_dat.ndt (main.py:2481-2636 column subset)."""
+        """main.py:2481-2536: append the averages to <name>_dat.ndt (a new
+        clock id per row; with avoid_same_step a step already written is not
+        written again) and, when fields are given ('all' or names), save
+        them (here m, as <name>_fields_<step>.npz)."""
         fn = "%s_dat.ndt" % self.name
-        avg = self.engine.averages()
-        new = not os.path.exists(fn)
-        with open(fn, "a") as f:
-            if new:
-                f.write("#%9s %12s %16s %16s %16s %16s\n" % ("step", "stage", "time", "m_Py_0", "m_Py_1", "m_Py_2"))
-            f.write(" %9d %12d %16.9e %16.9e %16.9e %16.9e\n" % (
-                self.clock.step, self.clock.stage, self.clock.time_su * 1e-12, avg[0], avg[1], avg[2]))
-        if fields == "all":
+        saved = getattr(self, "_saved_steps", None)
+        if saved is None:
+            saved = self._saved_steps = set()
+        if not (avoid_same_step and self.clock.step in saved):
+            self.clock.id += 1
+            saved.add(self.clock.step)
+            avg = self.engine.averages()
+            new = not os.path.exists(fn)
+            with open(fn, "a") as f:
+                if new:
+                    f.write("#%9s %12s %16s %16s %16s %16s\n" % ("step", "stage", "time", "m_Py_0", "m_Py_1", "m_Py_2"))
+                f.write(" %9d %12d %16.9e %16.9e %16.9e %16.9e\n" % (
+                    self.clock.step, self.clock.stage, self.clock.time_su * 1e-12, avg[0], avg[1], avg[2]))
+        if fields:
             np.savez("%s_fields_%06d.npz" % (self.name, self.clock.step), m=self._m)
 
     def save_restart_file(self, filename=None):

@@ -174,7 +174,8 @@ def test_fp32_bem_precision_form_error(cube_pair, cube):
     assert rel_err(f32["H_total"], f64["H_total"]) < 1e-5
 
 
-def test_simulation_api_advance_and_relax(small_box):
+def test_simulation_api_advance_and_relax(small_box, tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)   # relax saves averages and fields at the stage end
     import nmag
     from nmag import SI
     mat = nmag.MagMaterial("Py", Ms=SI(8.6e5, "A/m"), exchange_coupling=SI(1.3e-11, "J/m"), llg_damping=1.0)
@@ -188,6 +189,7 @@ def test_simulation_api_advance_and_relax(small_box):
     assert np.abs(np.linalg.norm(m, axis=1) - 1).max() < 1e-4
     sim.relax()
     assert sim.max_dm_dt < sim.stopping_dm_dt
+    assert (tmp_path / "api_test_dat.ndt").exists()
     avg = sim.get_subfield_average_siv("m")
     assert avg[2] > 0.99
 

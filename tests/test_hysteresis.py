@@ -1,0 +1,144 @@
+"""Save / do schedules (interface/nsim/when.py) and the hysteresis loop
+(interface/nmag/hysteresis.py:244-557) on the host, with a stand-in engine
+that relaxes exponentially, so the control logic runs without a GPU."""
+import math
+
+import numpy as np
+import pytest
+
+import nmag
+from nmag import SI
+from nmag.when import at, every, never
+
+
+def test_every_and_at_next_times():
+    c = {"step": 3, "stage_step": 3, "time": 0.0, "stage_time": 0.0, "real_time": 0.0, "stage": 1,
+         "convergence": False, "stage_end": False}
+    w = every("step", 5)
+    assert w.next_time("step", c) == 5 and not w.match_time(c)
+    assert w.next_time("time", c) is False          # other counter: does it match now?
+    c["step"] = 10
+    assert w.match_time(c) and w.next_time("step", c) == 15
+    w = every("step", 5, first=12, last=30)
+    assert w.next_time("step", c) == 12
+    c["step"] = 30
+    assert w.next_time("step", c) is False
+    # SI times become simulation units (1e-12 s)
+    t = every("time", SI(2e-12, "s"))
+    c["time"] = 3.0
+    assert t.next_time("time", c) == pytest.approx(4.0)
+    assert at("time", SI(5e-12, "s")).next_time("time", c) == pytest.approx(5.0)
+    assert at("convergence").next_time("step", c) is True
+    c["convergence"] = True
+    assert at("convergence").match_time(c)
+    # combinations (when.py:71-128)
+    c["step"] = 0
+    assert (every("step", 4) | every("step", 6)).next_time("step", c) == 4
+    assert (every("step", 4) & every("step", 6)).next_time("step", c) == 12
+    assert (every("step", 4) | at("convergence")).next_time("step", c) == 4
+    assert never.next_time("step", c) is False and not never.match_time(c)
+    with pytest.raises(ValueError):
+        every("step", 0)
+    with pytest.raises(ValueError):
+        every("step", 5, first=10, last=5)
+
+
+class RelaxingEngine(object):
+    """Stand-in for nmag._lib.Engine: fixed steps of h, m relaxing towards
+    +z with rate 1 (simulation units)."""
+
+    def __init__(self, N=4, h=0.25):
+        self.N, self.B, self.h = N, 1, h
+        self.t, self.nst = 0.0, 0
+        self.m = np.tile([1.0, 0.0, 0.0], (N, 1))
+        self.mark = self.m.copy()
+        self.H = None
+        self.inits = 0
+
+    def _shape3(self):
+        return (self.N, 3)
+
+    def set_m(self, m):
+        self.m = np.array(m, dtype=float).reshape(self.N, 3)
+        self.mark = self.m.copy()
+
+    def get_m(self):
+        return self.m.copy()
+
+    def set_h_ext(self, h):
+        self.H = np.array(h, dtype=float)
+
+    def ts_init(self, t0, rtol, atol, q, k):
+        self.t, self.nst, self.inits = t0, 0, self.inits + 1
+
+    def ts_advance(self, target, exact_tstop, max_it):
+        n = math.ceil((target - self.t) / self.h - 1e-12)
+        if max_it is not None and max_it > 0:
+            n = min(n, max_it)
+        n = max(n, 0)
+        self.t = min(self.t + n * self.h, target)
+        self.nst += n
+        a = math.exp(-self.t)
+        self.m = np.tile([a, 0.0, math.sqrt(1 - a * a)], (self.N, 1))
+        return self.t, {"nst": self.nst, "hcur": self.h}
+
+    def timings(self):
+        return np.zeros(8)
+
+    def max_dm_step(self):
+        d = float(np.abs(self.m - self.mark).max())
+        self.mark = self.m.copy()
+        return d
+
+    def averages(self):
+        return self.m.mean(0)
+
+
+def make_sim(tmp_path, monkeypatch, stop=1e-3):
+    monkeypatch.chdir(tmp_path)
+    sim = nmag.Simulation("hyst")
+    eng = RelaxingEngine()
+    sim.engine = eng
+    sim._m = eng.get_m()
+    sim._h_ext = np.zeros((eng.N, 3))
+    sim.stopping_dm_dt = stop
+    return sim, eng
+
+
+def test_relax_runs_to_convergence_and_saves_at_stage_end(tmp_path, monkeypatch):
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    sim.relax()
+    assert sim.clock.stage_end and sim.clock.convergence
+    assert sim.max_dm_dt < sim.stopping_dm_dt
+    rows = [l for l in open("hyst_dat.ndt") if not l.startswith("#")]
+    assert len(rows) == 1                        # averages at stage end only (the default save)
+    assert len(list(tmp_path.glob("hyst_fields_*.npz"))) == 1
+    assert sim.clock.id == 0                     # ids start at -1; one new id per averages row
+
+
+def test_hysteresis_schedules(tmp_path, monkeypatch):
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    seen = []
+
+    def record(s):
+        seen.append((s.clock.stage, s.clock.stage_step))
+    H = [[0, 0, 1e5], [0, 0, 2e5], [0, 0, 3e5]]
+    sim.hysteresis(H, save=[(record, every("stage_step", 6))],
+                   do=[("next stage", at("stage_step", 12)), ("exit", at("step", 30))])
+    # stage 1: steps 0, 6, 12 (ended by next_stage at 12); stage 2 likewise;
+    # stage 3 exits at step 30 = stage step 6
+    assert seen == [(1, 0), (1, 6), (1, 12), (2, 0), (2, 6), (2, 12), (3, 0), (3, 6)]
+    assert sim.clock.exit_hysteresis and sim.clock.step == 30
+    assert eng.inits == 3 and np.allclose(eng.H[0], [0, 0, 3e5 * 1e-6])
+
+
+def test_hysteresis_time_schedule_and_errors(tmp_path, monkeypatch):
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    times = []
+    sim.relax(save=[(lambda s: times.append(round(s.clock.stage_time_su, 9)), every("time", SI(0.5e-12, "s")))],
+              do=[("exit", at("stage_time", SI(2e-12, "s")))])
+    assert times == [0.0, 0.5, 1.0, 1.5, 2.0]
+    with pytest.raises(ValueError):
+        sim.relax(save=[("teleport", at("stage_end"))])
+    with pytest.raises(ValueError):
+        sim.relax(save=[("averages", at("stage_end")), ("save averages", every("step", 3))])
