@@ -150,6 +150,23 @@ class SI(object):
         u = " ".join("%s^%d" % (k, v) if v != 1 else k for k, v in sorted(self.dims.items()))
         return "SI(%r, %r)" % (self.value, u)
 
+    def dens_str(self, angles=True):
+        """si_units/lib.py:304-340: '<A/m>', '<kg/ms^2>', '<1e-09m>': positive
+        then negative powers in the order m kg s A K mol cd, no separators."""
+        def part(sign):
+            out = ""
+            for u in ("m", "kg", "s", "A", "K", "mol", "cd"):
+                p = self.dims.get(u, 0)
+                if p and (p > 0) == (sign > 0):
+                    out += u if abs(p) == 1 else "%s^%d" % (u, abs(p))
+            return out
+        powers = part(+1)
+        neg = part(-1)
+        if neg:
+            powers = "%s/%s" % (powers, neg)
+        body = (powers or "1") if self.value == 1.0 else "%g%s" % (self.value, powers)
+        return "<%s>" % body if angles else body
+
 
 # physical constants (interface/nsim/si_units/si.py)
 mu0 = SI(4.0e-7 * math.pi, "N/A^2")

@@ -27,8 +27,17 @@ from .si import SI, simulation_units
 
 log = logging.getLogger("nmag")
 
+# SI units of the fields as the reference converts them (main.py:208-231),
+# including its unit for dm/dt, SI("A/m s")
 _FIELD_SI = {"H": SI(1.0, "A/m"), "E": SI(1.0, "J/m^3"), "phi": SI(1.0, "A"), "rho": SI(1.0, "A/m^2"),
-             "dmdt": SI(1.0, "1/s"), "J": SI(1.0, "A/m^2")}
+             "dmdt": SI(1.0, "A/m s"), "J": SI(1.0, "A/m^2"), "M": SI(1.0, "A/m"), "m": SI(1.0, ""),
+             "pin": SI(1.0, "")}
+# averages written to the .ndt file (main.py:2313-2480): per material (the
+# fields_on_space of main.py:202-204) and over the mesh (fields_on_materials)
+_NDT_PER_MATERIAL = [("m", "m"), ("M", "M"), ("H_total", "H"), ("H_exch", "H"), ("H_anis", "H"), ("dmdt", "dmdt"),
+                     ("E_total", "E"), ("E_exch", "E"), ("E_anis", "E"), ("E_demag", "E"), ("E_ext", "E")]
+_NDT_MESH = [("H_demag", "H"), ("H_ext", "H"), ("phi", "phi"), ("rho", "rho"), ("pin", "pin")]
+_NDT_HEADERS_DONE = set()
 
 
 def _su_factor(kind):
@@ -650,25 +659,98 @@ class Simulation(object):
         _, e = self.engine.averages(energies=True)
         return e * _su_factor("E") * (simulation_units.conversion_factor_of(SI("m")) ** 3)
 
+    def _compute_averages(self):
+        """main.py:2313-2480: (names, values, units) of one .ndt row: the
+        clock, the volume average in SI of every field (member 0 of an
+        ensemble), the largest angle between m at neighbouring nodes,
+        the local and the unix time."""
+        ck = self.clock
+        to_si = simulation_units.conversion_factor_of(SI(1.0, "s"))
+        names = ["time", "id", "step", "last_step_dt", "stage_time", "stage_step", "stage"]
+        units = [SI(1.0, "s"), SI(1.0), SI(1.0), SI(1.0, "s"), SI(1.0, "s"), SI(1.0), SI(1.0)]
+        values = [ck.time_su * to_si, int(ck.id), int(ck.step), ck.last_step_dt_su * to_si,
+                  ck.stage_time_su * to_si, float(ck.stage_step), int(ck.stage)]
+        f = self.engine.eval_fields()
+        E = self.engine.energy_density()
+        first = (lambda a: a[0]) if self.n_members > 1 else (lambda a: a)
+        m = first(np.asarray(self._m))
+        c = self.material.coefficients(self.quirks)
+        su = {"m": m, "M": c["Ms"] * m, "H_ext": first(np.asarray(self._h_ext)),
+              "phi": first(f["phi"]), "rho": first(f["rho"]),
+              "pin": getattr(self, "_pin", None) if getattr(self, "_pin", None) is not None else np.ones(len(m))}
+        for k in ("H_total", "H_exch", "H_anis", "H_demag", "dmdt"):
+            su[k] = first(f[k])
+        for k in ("E_total", "E_exch", "E_anis", "E_demag", "E_ext"):
+            su[k] = first(E[k])
+        mesh_fields = list(_NDT_MESH)
+        if getattr(self, "_j", None) is not None:
+            su["current_density"] = first(np.asarray(self._j))
+            mesh_fields.append(("current_density", "J"))
+        V = self._volumes()
+
+        def average(a, kind):
+            a = np.asarray(a, dtype=np.float64)
+            s_ = (a * V[:, None]).sum(0) if a.ndim == 2 else (a * V).sum()
+            return s_ / V.sum() * (1.0 / simulation_units.of(_FIELD_SI[kind]))
+        mat = self.material.name
+        for fname, kind in _NDT_PER_MATERIAL:
+            names.append("%s_%s" % (fname, mat)); units.append(_FIELD_SI[kind]); values.append(average(su[fname], kind))
+        for fname, kind in mesh_fields:
+            names.append(fname); units.append(_FIELD_SI[kind]); values.append(average(su[fname], kind))
+        # largest angle between m at the two ends of a mesh edge (degrees)
+        t = self.mesh.simplices
+        e = np.concatenate([t[:, [a, b]] for a in range(4) for b in range(a + 1, 4)])
+        mn = m / np.linalg.norm(m, axis=1)[:, None]
+        cosang = np.clip(np.einsum("ij,ij->i", mn[e[:, 0]], mn[e[:, 1]]), -1.0, 1.0)
+        names.append("maxangle_m_%s" % mat); units.append("<deg>")
+        values.append(float(np.degrees(np.arccos(cosang.min()))) if len(cosang) else 0.0)
+        lt = _time.localtime()
+        names += ["localtime", "unixtime"]
+        units += ["<>", SI(1.0, "s")]
+        values += ["%04d/%02d/%02d-%02d:%02d:%02d" % lt[:6], _time.time()]
+        return names, values, units
+
+    @staticmethod
+    def _save_data_table_to_ndt(names, values, units, filename):
+        """main.py:2571-2634: one row of 25-character columns; a name line and
+        a unit line first (once per file and process)."""
+        cols = []
+        for name, value, unit in zip(names, values, units):
+            ustr = unit if isinstance(unit, str) else unit.dens_str()
+            if np.ndim(value) == 0:
+                cols.append((name, value, ustr))
+            else:
+                cols += [("%s_%d" % (name, k), float(v), ustr) for k, v in enumerate(value)]
+        key = os.path.abspath(filename)
+        new = not os.path.exists(filename)
+        with open(filename, "a") as fh:
+            if new or key not in _NDT_HEADERS_DONE:
+                fh.write("#" + "".join("%-25s " % n for n, _, _ in cols) + "\n")
+                fh.write("#" + "".join("%-25s " % u for _, _, u in cols) + "\n")
+                _NDT_HEADERS_DONE.add(key)
+            row = []
+            for _, v, _ in cols:
+                if isinstance(v, str):
+                    row.append("% 25s " % v)
+                elif isinstance(v, (int, np.integer)):
+                    row.append("% 25d " % v)
+                else:
+                    row.append("% 25.13g " % float(v))
+            fh.write("".join(row) + "\n")
+
     def save_data(self, fields=None, avoid_same_step=False):
         """main.py:2481-2536: append the averages to <name>_dat.ndt (a new
         clock id per row; with avoid_same_step a step already written is not
         written again) and, when fields are given ('all' or names), save
         them (here m, as <name>_fields_<step>.npz)."""
-        fn = "%s_dat.ndt" % self.name
         saved = getattr(self, "_saved_steps", None)
         if saved is None:
             saved = self._saved_steps = set()
         if not (avoid_same_step and self.clock.step in saved):
             self.clock.id += 1
             saved.add(self.clock.step)
-            avg = self.engine.averages()
-            new = not os.path.exists(fn)
-            with open(fn, "a") as f:
-                if new:
-                    f.write("#%9s %12s %16s %16s %16s %16s\n" % ("step", "stage", "time", "m_Py_0", "m_Py_1", "m_Py_2"))
-                f.write(" %9d %12d %16.9e %16.9e %16.9e %16.9e\n" % (
-                    self.clock.step, self.clock.stage, self.clock.time_su * 1e-12, avg[0], avg[1], avg[2]))
+            names, values, units = self._compute_averages()
+            self._save_data_table_to_ndt(names, values, units, "%s_dat.ndt" % self.name)
         if fields:
             np.savez("%s_fields_%06d.npz" % (self.name, self.clock.step), m=self._m)
 

@@ -93,12 +93,25 @@ class RelaxingEngine(object):
     def averages(self):
         return self.m.mean(0)
 
+    def eval_fields(self):
+        z = np.zeros((self.N, 3))
+        return {"H_exch": z, "H_demag": z + 0.1, "H_anis": z, "H_total": z + 0.1, "dmdt": z,
+                "phi": np.zeros(self.N), "rho": np.zeros(self.N)}
+
+    def energy_density(self):
+        return {k: np.full(self.N, 0.5) for k in ("E_exch", "E_demag", "E_ext", "E_anis", "E_total")}
+
+    def csr(self):
+        return (None,) * 5 + (np.array([1.0, 2.0, 3.0, 4.0]),)
+
 
 def make_sim(tmp_path, monkeypatch, stop=1e-3):
     monkeypatch.chdir(tmp_path)
     sim = nmag.Simulation("hyst")
     eng = RelaxingEngine()
     sim.engine = eng
+    sim.material = nmag.MagMaterial("Py")
+    sim.mesh = nmag.mesh.Mesh([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], [[0, 1, 2, 3]])
     sim._m = eng.get_m()
     sim._h_ext = np.zeros((eng.N, 3))
     sim.stopping_dm_dt = stop
@@ -142,3 +155,32 @@ def test_hysteresis_time_schedule_and_errors(tmp_path, monkeypatch):
         sim.relax(save=[("teleport", at("stage_end"))])
     with pytest.raises(ValueError):
         sim.relax(save=[("averages", at("stage_end")), ("save averages", every("step", 3))])
+
+
+def test_ndt_row_layout(tmp_path, monkeypatch):
+    """main.py:2313-2480,2571-2634: a names line, a units line, then one
+    row per save with the clock, the SI averages and the extra columns."""
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    sim.relax(save=[("averages", every("step", 10) | at("stage_end"))])
+    lines = open("hyst_dat.ndt").read().splitlines()
+    names, units = lines[0][1:].split(), lines[1][1:].split()
+    rows = [l.split() for l in lines[2:]]
+    assert names[:7] == ["time", "id", "step", "last_step_dt", "stage_time", "stage_step", "stage"]
+    for col in ("m_Py_0", "m_Py_2", "M_Py_1", "H_total_Py_2", "dmdt_Py_0", "E_total_Py", "E_demag_Py",
+                "H_demag_0", "H_ext_2", "phi", "rho", "pin", "maxangle_m_Py", "localtime", "unixtime"):
+        assert col in names, col
+    assert len(units) == len(names) and all(len(r) == len(names) for r in rows)
+    u = dict(zip(names, units))
+    assert u["time"] == "<s>" and u["H_demag_0"] == "<A/m>" and u["E_total_Py"] == "<kg/ms^2>" and u["m_Py_0"] == "<1>"
+    assert u["dmdt_Py_0"] == "<A/ms>" and u["maxangle_m_Py"] == "<deg>"
+    steps = [int(r[names.index("step")]) for r in rows]
+    assert steps[:3] == [0, 10, 20] and steps == sorted(set(steps))     # every 10 steps, no step twice
+    ids = [int(r[names.index("id")]) for r in rows]
+    assert ids == list(range(len(rows)))
+    last = dict(zip(names, rows[-1]))
+    m = eng.get_m()
+    V = np.array([1.0, 2.0, 3.0, 4.0])
+    assert float(last["m_Py_2"]) == pytest.approx((m[:, 2] * V).sum() / V.sum(), rel=1e-12)
+    assert float(last["H_demag_1"]) == pytest.approx(0.1 * 1e6, rel=1e-12)    # A/m from 0.1 su
+    assert float(last["E_exch_Py"]) == pytest.approx(0.5 * 1e6, rel=1e-12)    # J/m^3 from 0.5 su
+    assert float(last["pin"]) == 1.0 and float(last["maxangle_m_Py"]) == pytest.approx(0.0, abs=1e-6)
