@@ -509,9 +509,10 @@ class Simulation(object):
     # ---- read-out ------------------------------------------------------------
     def get_subfield(self, subfieldname, units=None):
         """Field values per node in SI (m is dimensionless)."""
-        name = subfieldname.split("_")[0] if subfieldname.startswith("m_") else subfieldname
         if subfieldname == "m" or subfieldname.startswith("m_"):
             return self._m.copy()
+        if subfieldname == "M" or subfieldname.startswith("M_"):   # M = Ms m (nmag_lam.py:463)
+            return self._m * self.material.coefficients(self.quirks)["Ms"] * _su_factor("M")
         if subfieldname.startswith("H_ext"):
             return self._h_ext * _su_factor("H")
         if subfieldname == "pin":
@@ -632,17 +633,27 @@ class Simulation(object):
         self._ts_ready = False
 
     def get_subfield_average_siv(self, field, subfield=None):
-        name = field if subfield is None else field
-        if name == "m" or name.startswith("m_"):
-            return list(self.engine.averages())   # member 0 of an ensemble
-        vals = self.get_subfield(name)
+        """main.py:2234-2290: volume average of a field in SI numbers (a
+        list for vectors); ``subfield`` names the material of per-material
+        fields ('m', 'Py' -> m_Py).  Member 0 of an ensemble."""
+        if subfield is not None and subfield != self.material.name:
+            raise ValueError("You want to compute the average of '%s', but the subfield you specified (%s) is "
+                             "not one of its subfields" % (field, subfield))
+        if field == "m" or field.startswith("m_"):
+            return list(self.engine.averages())
+        vals = self.get_subfield(field)
+        if vals.ndim == 3 or (vals.ndim == 2 and self.n_members > 1 and vals.shape[0] == self.n_members):
+            vals = vals[0]
         V = self._volumes()
         if vals.ndim == 2:
             return list((vals * V[:, None]).sum(0) / V.sum())
         return float((vals * V).sum() / V.sum())
 
     def get_subfield_average(self, field, subfield=None):
-        return self.get_subfield_average_siv(field, subfield)
+        """main.py:2292-2312: as get_subfield_average_siv, as SI objects."""
+        v = self.get_subfield_average_siv(field, subfield)
+        u = self._unit_of(field)
+        return [x * u for x in v] if isinstance(v, list) else v * u
 
     def get_member_average_m(self, member):
         """<m> of one ensemble member."""

@@ -184,3 +184,16 @@ def test_ndt_row_layout(tmp_path, monkeypatch):
     assert float(last["H_demag_1"]) == pytest.approx(0.1 * 1e6, rel=1e-12)    # A/m from 0.1 su
     assert float(last["E_exch_Py"]) == pytest.approx(0.5 * 1e6, rel=1e-12)    # J/m^3 from 0.5 su
     assert float(last["pin"]) == 1.0 and float(last["maxangle_m_Py"]) == pytest.approx(0.0, abs=1e-6)
+
+
+def test_subfield_averages(tmp_path, monkeypatch):
+    """main.py:2234-2312: averages in SI numbers or objects; the subfield is
+    the material name; M = Ms m."""
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    assert sim.get_subfield_average_siv("H_demag") == pytest.approx([0.1e6] * 3, rel=1e-12)
+    E = sim.get_subfield_average("E_total", "Py")
+    assert E.value == pytest.approx(0.5e6, rel=1e-12) and E.dims == SI("J/m^3").dims
+    with pytest.raises(ValueError):
+        sim.get_subfield_average_siv("m", "Co")
+    M = sim.get_subfield("M_Py")
+    assert np.allclose(M, eng.get_m() * 0.86e6, rtol=1e-11)
