@@ -284,7 +284,8 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
     import torch
     import nmag
     from nmag import SI
-    sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor)
+    sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor,
+                          anchor_product=args.anchor_product)
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     if B > 1:   # member b starts from the workload's initial state with seed + b
@@ -383,21 +384,27 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
         # once; its launch time stays in the totals)
         n_prod, n_ref = anc1[0] - anc0[0], anc1[1] - anc0[1]
         dl, dms = prof["bem_anchor_delta"]
-        bytes32 = nb * nb * 4 + 2 * nm * nb * 8
+        h16 = B > 1 and args.anchor_product == "fp16"
+        # difference product: the FP32 matrix, or the FP16 fragment copy (16 x 16
+        # tiles covering nb rounded up to 16); x - x0 in and y out per member
+        kt = (nb + 15) // 16
+        bytes_d = (kt * kt * 512 if h16 else nb * nb * 4) + 2 * nm * nb * 8
         hbm, peak_kind = peaks()
         legs = {}
         for name, kname, execd, tot_ms, nbytes in (
                 ("refresh", "k_gemm_df" if B > 1 else "k_gemv_df", n_ref, gms, bytes_per_launch),
-                ("difference", "k_gemm_f32r" if B > 1 else "k_gemv_f32", n_prod - n_ref, dms, bytes32)):
+                ("difference", ("k_gemm_h16mma" if h16 else "k_gemm_f32r") if B > 1 else "k_gemv_f32",
+                 n_prod - n_ref, dms, bytes_d)):
             ach = execd * nbytes / (tot_ms * 1e-3) / 1e9 if execd > 0 and tot_ms > 0 else None
             legs[name] = {"kernel": kname, "executed": int(execd), "total_ms": tot_ms,
                           "algorithmic_bytes_per_launch": nbytes,
                           "avg_launch_ms": tot_ms / execd if execd > 0 else None,
                           "achieved": ach, "frac": ach / hbm if ach else None}
-        anchored = {"tol": anchor, "products": int(n_prod), "refreshes": int(n_ref), "legs": legs}
+        anchored = {"tol": anchor, "products": int(n_prod), "refreshes": int(n_ref), "legs": legs,
+                    "difference_product": "fp16 fragments (mma.m16n8k16)" if h16 else "fp32"}
         dom = max(legs.values(), key=lambda v: v["total_ms"])
         if dom["achieved"]:
-            roof = {"bound": "hbm" if dom["kernel"] in ("k_gemm_f32r", "k_gemv_f32") else "hbm (FP32 pipe)",
+            roof = {"bound": "hbm" if dom["kernel"] in ("k_gemm_f32r", "k_gemv_f32", "k_gemm_h16mma") else "hbm (FP32 pipe)",
                     "kernel": dom["kernel"], "achieved": dom["achieved"], "peak": hbm, "unit": "GB/s",
                     "frac": dom["frac"], "peak_kind": peak_kind,
                     "traffic": (NCU_TRAFFIC_RATIO[(dom["kernel"], B > 1)] * dom["algorithmic_bytes_per_launch"] / 1e9
@@ -461,7 +468,8 @@ def anchor_path_error(args, chosen, msh, points=48):
     tight = {"NBC.rtol": 1e-12, "DBC.rtol": 1e-12, "NBC.maxits": 20000, "DBC.maxits": 20000}
     sims = {}
     for key, form, anc in (("anchored", args.form, args.anchor), ("fp64", "fp64", 0.0)):
-        sim = nmag.Simulation("err", bem_precision=form, ksp_tolerances=tight, n_members=B, bem_anchor=anc)
+        sim = nmag.Simulation("err", bem_precision=form, ksp_tolerances=tight, n_members=B, bem_anchor=anc,
+                              anchor_product=args.anchor_product)
         sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
         shape = (B, sim.engine.N, 3) if B > 1 else (sim.engine.N, 3)
         sim.engine.set_h_ext(np.broadcast_to(h_ext_su(), shape))
@@ -835,6 +843,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cg", default="fp32", choices=["fp64", "fp32"],
                     help="Poisson CG: FP64, or FP32 iterations with FP64 residual refinement")
+    ap.add_argument("--anchor-product", default="fp32", choices=["fp32", "fp16"],
+                    help="difference product of the anchored ensemble form: FP32 matrix copy or FP16 copy "
+                         "in tensor-core fragment order")
     ap.add_argument("--anchor", type=float, default=3e-3,
                     help="fp32x2: anchored product tolerance (B x = B x0 + B32 (x - x0) while the max-norm drift "
                          "of x from x0 stays below it; 0 = off)")

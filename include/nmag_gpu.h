@@ -61,7 +61,10 @@ typedef struct nmg_options {
   int adjoint_cg_precision;              /* Poisson solves of nmg_rk4_adjoint's backward
                                             pass: 0 FP64 CG; 1 FP32 CG with FP64 residual
                                             refinement (to the same tolerance)         */
-  int reserved[1];
+  int anchor_product;                    /* anchored ensemble product's difference
+                                            B (x - x0): 0 FP32 copy of B; 1 FP16 copy of
+                                            B in tensor-core fragment order (FP32
+                                            accumulation; ~2^-11 of |B||x - x0|)        */
 } nmg_options;
 
 /* Integrator statistics (CVODE counters; nsim.ml:354-387 timings). */

@@ -14,6 +14,10 @@
 // multiple of 8 (bem[k*ld + c]), the layout the matrix-vector product streams.
 // Compiled with --fmad=false to follow the written operation order.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cmath>
+#include <cstring>
 
 #include "nmg_internal.h"
 
@@ -174,6 +178,46 @@ __global__ void k_to_f32(size_t n, const double *__restrict__ a, float *__restri
   for (; i < n; i += stride) b[i] = (float)a[i];
 }
 
+// max |B| as float bits (non-negative floats order like their bit patterns).
+__global__ void k_absmax_f32(long long n, const float *__restrict__ v, unsigned *__restrict__ out) {
+  unsigned m = 0u;
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    m = max(m, __float_as_uint(fabsf(v[k])));
+  for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+// FP16 copy of B (times scale) in the A-operand fragment order of
+// mma.m16n8k16 (row-major): tile (rb, kb) holds rows 16 rb .. +15 and
+// columns 16 kb .. +15 as 32 lanes x 8 halves; lane 4 g + t carries
+// (g, 2t), (g, 2t+1), (g+8, 2t), (g+8, 2t+1), (g, 2t+8), (g, 2t+9),
+// (g+8, 2t+8), (g+8, 2t+9) -- the PTX fragment elements a0..a7 -- so one
+// 16-byte load per lane fills the operand.  Entries beyond nb are 0.
+__global__ void k_pack_bem16f(int nb, int ld, int KT, long long ntiles, const float *__restrict__ B32, float scale,
+                              uint4 *__restrict__ out) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= ntiles * 32) return;
+  const long long tile = g >> 5;
+  const int lane = (int)(g & 31);
+  const int rb = (int)(tile / KT), kb = (int)(tile - (long long)rb * KT);
+  const int gq = lane >> 2, t = lane & 3;
+  unsigned w[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    float v[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int i = 2 * j + h;
+      const int r = 16 * rb + gq + ((i & 2) ? 8 : 0);
+      const int c = 16 * kb + 2 * t + (i & 1) + (i >= 4 ? 8 : 0);
+      v[h] = (r < nb && c < nb) ? B32[(size_t)r * ld + c] * scale : 0.f;
+    }
+    const __half2 p = __floats2half2_rn(v[0], v[1]);   // v[0] in the low half
+    memcpy(&w[j], &p, sizeof(unsigned));
+  }
+  out[g] = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
 }  // namespace
 
 int fill_bem(nmg_handle *h, std::string &err) {
@@ -211,6 +255,28 @@ int fill_bem(nmg_handle *h, std::string &err) {
   if (h->opt.bem_precision == 2) {
     NMG_CUDA_TRY(M.bem16lo.alloc(nb * M.ld), "alloc BEM residual (BF16)");
     k_split_lo<<<h->sm_count * 8, 256, 0, s>>>(nb * M.ld, M.bem, M.bem32, M.bem16lo);
+  }
+  if (h->opt.bem_precision == 2 && h->opt.bem_anchor_tol > 0.0 && h->nrep > 1 && h->opt.anchor_product == 1) {
+    // FP16 fragment copy for the anchored ensemble product, scaled by a power
+    // of two that puts max|B| in [2^13, 2^14) (FP16 normal range for the rest)
+    DevBuf<unsigned> amax;
+    NMG_CUDA_TRY(amax.alloc(1), "alloc");
+    NMG_CUDA_TRY(cudaMemsetAsync(amax.p, 0, sizeof(unsigned), s), "zero");
+    k_absmax_f32<<<h->sm_count * 4, 256, 0, s>>>((long long)nb * M.ld, M.bem32, amax);
+    unsigned bits = 0;
+    NMG_CUDA_TRY(cudaMemcpyAsync(&bits, amax.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "copy");
+    NMG_CUDA_TRY(cudaStreamSynchronize(s), "absmax");
+    float mx;
+    std::memcpy(&mx, &bits, sizeof(float));
+    int e = 0;
+    if (mx > 0.f && std::isfinite(mx)) std::frexp(mx, &e);
+    M.h16_scale = std::ldexp(1.f, 14 - e);
+    M.h16_kt = (nb + 15) / 16;
+    const long long ntiles = (long long)M.h16_kt * M.h16_kt;   // row blocks = column tiles
+    NMG_CUDA_TRY(M.bem16f.alloc((size_t)ntiles * 256), "alloc FP16 fragment BEM");
+    k_pack_bem16f<<<(unsigned)((ntiles * 32 + 255) / 256), 256, 0, s>>>(
+        nb, M.ld, M.h16_kt, ntiles, M.bem32, M.h16_scale, reinterpret_cast<uint4 *>(M.bem16f.p));
+    NMG_CUDA_TRY(cudaGetLastError(), "pack FP16 fragment BEM");
   }
   NMG_CUDA_TRY(cudaStreamSynchronize(s), "bem fill");
   return 0;

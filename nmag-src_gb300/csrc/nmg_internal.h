@@ -61,6 +61,11 @@ struct Mesh {
   DevBuf<double> bem;      // FP64 BEM, row-major with padded row stride ld (bem[k*ld + c] = B[k][c])
   DevBuf<float> bem32;     // FP32 copy (precision forms 1, 2), same layout
   DevBuf<uint16_t> bem16lo; // form 2: BF16 bits of B - fp32(B), same layout (B ~ hi + lo to ~2^-32)
+  // anchored ensemble product: FP16 bits of B * h16_scale in the m16n8k16
+  // A-fragment order, tiles of 16 x 16 (h16_kt tiles per row block)
+  DevBuf<uint16_t> bem16f;
+  int h16_kt = 0;
+  float h16_scale = 1.f;
   int ld = 0;              // row stride: nb rounded up to a multiple of 8 (64-byte aligned FP64 rows)
   DevBuf<TriGeo> trigeo;
   DevBuf<double> obs_max;
@@ -101,6 +106,12 @@ struct Workspace {
   DevBuf<long long> anc_count;
   // m at the last nmg_max_dm_step / nmg_set_m (allocated on first use)
   DevBuf<double> m_mark;
+  // FP16 fragment product: x - x0 of 8 members in B-fragment order, the
+  // per-member power-of-two scales, the warps' row-block partials
+  DevBuf<uint16_t> x16f;
+  DevBuf<float> x16scale, h16part;
+  int h16_blocks = 0, h16_maxr = 0;
+  long long h16_seg = 0;
 };
 
 struct Integrator;

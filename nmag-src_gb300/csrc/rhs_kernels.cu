@@ -20,6 +20,8 @@
 #include <cmath>
 
 #include <cooperative_groups.h>
+#include <cuda_fp16.h>
+#include <cstring>
 
 #include "nmg_internal.h"
 
@@ -1863,12 +1865,18 @@ __global__ void k_anchor_drift(int n, int ld, int nm, const double *__restrict__
 // member drifted past tol; clears the maxima for the next chunk and counts
 // products / refreshes.
 __global__ void k_anchor_decide(int nm, double tol, unsigned long long *__restrict__ mx, const int *__restrict__ valid,
-                                int *__restrict__ flag, long long *__restrict__ count) {
+                                int *__restrict__ flag, long long *__restrict__ count, float *__restrict__ scale = nullptr) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   int refresh = *valid ? 0 : 1;
   for (int m = 0; m < nm; ++m) {
     const double dm = __longlong_as_double((long long)mx[m]), xm = __longlong_as_double((long long)mx[kChunk + m]);
     if (!(dm <= tol * xm)) refresh = 1;
+    if (scale) {   // FP16 fragment product: 2^k with max|x - x0| 2^k in [2^13, 2^14)
+      int e = 0;
+      if (dm > 0.0 && dm <= 1e300) frexp(dm, &e);
+      e = max(-100, min(100, e));
+      scale[m] = (float)ldexp(1.0, 14 - e);
+    }
   }
   for (int k = 0; k < 2 * kChunk; ++k) mx[k] = 0ull;
   *flag = refresh;
@@ -1898,6 +1906,121 @@ __global__ void k_anchor_slab_sum(int nb, int nslab_df, int nslab_32, int nm, in
   } else {
     y[o] = y0[o] + s;
   }
+}
+
+// ---- anchored ensemble product, FP16 fragment form ----
+// The difference product B (x - x0) of 8 members on the tensor cores:
+// mma.m16n8k16 with B's 16 x 16 tiles as the A operand (FP16, stored in
+// fragment order by k_pack_bem16f, scaled by 2^sB), the members' x - x0 as
+// the 16 x 8 B operand (FP16, scaled per member by 2^sX), FP32 accumulation.
+// One 16-byte load per lane and tile and one mma per tile replace 128 FP32
+// FMAs per lane, so the 2-byte matrix streams at the memory rate.
+//
+// k_pack_x16f: x - x0 (FP32, [member][ld]) times the member scales in the
+// B-operand fragment order: k-tile kb, lane 4 n + t holds rows 2t, 2t+1,
+// 2t+8, 2t+9 of column n (member n; 0 beyond nm or nb).
+__global__ void k_pack_x16f(int nb, int ld, int nm, int KT, const float *__restrict__ xh,
+                            const float *__restrict__ scale, uint2 *__restrict__ out, const int *__restrict__ gate) {
+  if (gate && *gate) return;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= KT * 32) return;
+  const int kb = g >> 5, lane = g & 31, n = lane >> 2, t = lane & 3;
+  const float sc = n < nm ? scale[n] : 0.f;
+  unsigned w[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    float v[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = 16 * kb + 2 * t + h + 8 * j;
+      v[h] = (n < nm && k < nb) ? xh[(size_t)n * ld + k] * sc : 0.f;
+    }
+    const __half2 p = __floats2half2_rn(v[0], v[1]);
+    memcpy(&w[j], &p, sizeof(unsigned));
+  }
+  out[g] = make_uint2(w[0], w[1]);
+}
+
+// k_gemm_h16mma: warp w streams tiles [w seg, (w+1) seg) of the row-block-
+// major tile sequence (KT tiles per row block), kH16Unroll tiles of loads in
+// flight, and stores its 16 x 8 accumulator (C-fragment order, a float4 per
+// lane) whenever the row block changes: part[(w maxr + local block) 32 + lane].
+constexpr int kH16Unroll = 8;
+__global__ void __launch_bounds__(256) k_gemm_h16mma(long long TT, int KT, long long seg, int maxr,
+                                                     const uint4 *__restrict__ A, const uint2 *__restrict__ X,
+                                                     float4 *__restrict__ part, const int *__restrict__ gate) {
+  if (gate && *gate) return;
+  const int lane = threadIdx.x & 31;
+  const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long t0 = w * seg, t1 = min(t0 + seg, TT);
+  if (t0 >= t1) return;   // warp-uniform
+  const int rfirst = (int)(t0 / KT);
+  int cur = rfirst, lrb = rfirst, lkb = (int)(t0 - (long long)rfirst * KT);
+  float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+  for (long long tb = t0; tb < t1; tb += kH16Unroll) {
+    uint4 a[kH16Unroll];
+    uint2 b[kH16Unroll];
+    int rbu[kH16Unroll];
+#pragma unroll
+    for (int u = 0; u < kH16Unroll; ++u) {
+      const bool in = tb + u < t1;
+      rbu[u] = lrb;
+      a[u] = in ? __ldcs(A + (tb + u) * 32 + lane) : make_uint4(0u, 0u, 0u, 0u);
+      b[u] = in ? __ldg(X + (size_t)lkb * 32 + lane) : make_uint2(0u, 0u);
+      if (++lkb == KT) { lkb = 0; ++lrb; }
+    }
+#pragma unroll
+    for (int u = 0; u < kH16Unroll; ++u) {
+      if (tb + u < t1) {   // warp-uniform
+        if (rbu[u] != cur) {
+          part[((size_t)w * maxr + (cur - rfirst)) * 32 + lane] = make_float4(c0, c1, c2, c3);
+          c0 = c1 = c2 = c3 = 0.f;
+          cur = rbu[u];
+        }
+        asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+            "{%0,%1,%2,%3};\n"
+            : "+f"(c0), "+f"(c1), "+f"(c2), "+f"(c3)
+            : "r"(a[u].x), "r"(a[u].y), "r"(a[u].z), "r"(a[u].w), "r"(b[u].x), "r"(b[u].y));
+      }
+    }
+  }
+  part[((size_t)w * maxr + (cur - rfirst)) * 32 + lane] = make_float4(c0, c1, c2, c3);
+}
+
+// Ensemble epilogue of the FP16 fragment form: on a refresh, the compensated
+// product's slab partials (as k_anchor_slab_sum); otherwise row r of member m
+// sums its row block's partials over the warps that streamed it, in warp
+// order (element (r mod 16, m) of the C fragment: lane 4 (r mod 8) + m/2,
+// component 2 [r mod 16 >= 8] + m mod 2), undoes the two scales and adds y0.
+__global__ void k_anchor_h16_sum(int nb, int nslab_df, int nm, int MB, const double *__restrict__ part_df,
+                                 const float *__restrict__ part16, int KT, long long seg, int maxr, long long nwarps,
+                                 double inv_scale_b, const float *__restrict__ scale_x, const int *__restrict__ flag,
+                                 int *__restrict__ valid, const double *__restrict__ x, double *__restrict__ x0,
+                                 double *__restrict__ y0, double *__restrict__ y) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int refresh = *flag;
+  if (g == 0 && refresh) *valid = 1;
+  if (g >= nb * nm) return;
+  const int m = g / nb, r = g - m * nb;
+  const size_t o = (size_t)m * nb + r;
+  if (refresh) {
+    double s = 0.0;
+    for (int sl = 0; sl < nslab_df; ++sl) s += part_df[((size_t)sl * nb + r) * MB + m];
+    y0[o] = s;
+    x0[o] = x[o];
+    y[o] = s;
+    return;
+  }
+  const int rb = r >> 4, rr = r & 15;
+  const int lane = (rr & 7) * 4 + (m >> 1), comp = (rr >= 8 ? 2 : 0) + (m & 1);
+  const long long w0 = ((long long)rb * KT) / seg, w1 = min(nwarps - 1, ((long long)(rb + 1) * KT - 1) / seg);
+  double s = 0.0;
+  for (long long w = w0; w <= w1; ++w) {
+    const long long loc = rb - (w * seg) / KT;
+    s += (double)part16[(((size_t)w * maxr + loc) * 32 + lane) * 4 + comp];
+  }
+  y[o] = y0[o] + s * (inv_scale_b / (double)scale_x[m]);
 }
 
 // One simulation: k_row_sum over the shared segment partials (the compensated
@@ -2497,6 +2620,20 @@ int init_workspace(nmg_handle *h, std::string &err) {
   W.gemv_x32_off = (part_n + 7) / 8 * 8;
   // FP32 x copies: BC members, or BC (xh, xl) pairs for the compensated product
   NMG_CUDA_TRY(W.bpart.alloc(W.gemv_x32_off + (size_t)BC * M.ld + 8), "alloc gemv partials");
+  // anchored ensemble product in the FP16 fragment form (the matrix copy is
+  // packed by fill_bem): warps stream equal shares of the KT x KT tiles
+  if (nb > 0 && B > 1 && h->opt.bem_precision == 2 && h->opt.bem_anchor_tol > 0.0 && h->opt.anchor_product == 1) {
+    M.h16_kt = (nb + 15) / 16;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_h16mma, 256, 0);
+    W.h16_blocks = std::max(1, std::min(per_sm, 8)) * h->sm_count;
+    const long long nwarps = (long long)W.h16_blocks * 8, TT = (long long)M.h16_kt * M.h16_kt;
+    W.h16_seg = std::max<long long>(1, (TT + nwarps - 1) / nwarps);
+    W.h16_maxr = (int)((W.h16_seg + M.h16_kt - 1) / M.h16_kt + 1);
+    NMG_CUDA_TRY(W.x16f.alloc((size_t)M.h16_kt * 32 * 4), "alloc FP16 x fragments");
+    NMG_CUDA_TRY(W.x16scale.alloc(kChunk), "alloc");
+    NMG_CUDA_TRY(W.h16part.alloc((size_t)nwarps * W.h16_maxr * 128), "alloc FP16 product partials");
+  }
   // 2 parities x kCG2MaxRed values per block (at least 1024 blocks: averages use it too)
   size_t red_n = 2 * (size_t)kCG2MaxRed * (size_t)(W.cg_blocks > 1024 ? W.cg_blocks : 1024);
   NMG_CUDA_TRY(W.red.alloc(red_n), "alloc reductions");
@@ -2614,7 +2751,9 @@ void bem_gemm(nmg_handle *h, const double *x, double *y) {
       double *ax = W.anc_x.p + (size_t)c0 * nb, *ay = W.anc_y.p + (size_t)c0 * nb;
       k_anchor_drift<<<nblk((long long)M.ld * nm, 256), 256, 0, h->stream>>>(nb, M.ld, nm, xc, ax, xh, W.anc_mx);
       ++h->launches;
-      k_anchor_decide<<<1, 32, 0, h->stream>>>(nm, h->opt.bem_anchor_tol, W.anc_mx, valid, flag, W.anc_count);
+      const bool h16 = M.bem16f.p && W.h16part.p;   // FP16 fragment difference product
+      k_anchor_decide<<<1, 32, 0, h->stream>>>(nm, h->opt.bem_anchor_tol, W.anc_mx, valid, flag, W.anc_count,
+                                               h16 ? W.x16scale.p : nullptr);
       ++h->launches;
       k_split_x<<<nblk((long long)M.ld * nm, 256), 256, 0, h->stream>>>(nb, M.ld, nm, xc, xh, xl, flag);
       ++h->launches;
@@ -2627,6 +2766,26 @@ void bem_gemm(nmg_handle *h, const double *x, double *y) {
         else k_gemm_df<8><<<grid, 256, 0, h->stream>>>(nb, M.ld, nm, M.bem32, M.bem16lo, xh, xl, W.bpart, flag);
         NMG_PROF_END(h);
         ++h->launches;
+      }
+      if (h16) {
+        const int KT = M.h16_kt;
+        const long long nwarps = (long long)W.h16_blocks * 8;
+        uint2 *x16 = reinterpret_cast<uint2 *>(W.x16f.p);
+        k_pack_x16f<<<nblk((long long)KT * 32, 256), 256, 0, h->stream>>>(nb, M.ld, nm, KT, xh, W.x16scale, x16, flag);
+        ++h->launches;
+        {
+          NMG_PROF_BEGIN(h, 5);
+          k_gemm_h16mma<<<W.h16_blocks, 256, 0, h->stream>>>((long long)KT * KT, KT, W.h16_seg, W.h16_maxr,
+                                                            reinterpret_cast<const uint4 *>(M.bem16f.p), x16,
+                                                            reinterpret_cast<float4 *>(W.h16part.p), flag);
+          NMG_PROF_END(h);
+          ++h->launches;
+        }
+        k_anchor_h16_sum<<<nblk((long long)nb * nm, 256), 256, 0, h->stream>>>(
+            nb, nslab_df, nm, MB, W.bpart, W.h16part, KT, W.h16_seg, W.h16_maxr, nwarps, 1.0 / (double)M.h16_scale,
+            W.x16scale, flag, valid, xc, ax, ay, y + (size_t)c0 * nb);
+        ++h->launches;
+        continue;
       }
       {
         dim3 grid(nslab_32, (nb + kRegRows - 1) / kRegRows);

@@ -117,7 +117,7 @@ class Simulation(object):
                  temperature=None, thermal_delta_t=None, user_seed_T=0, timestepper_max_order=2,
                  timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
                  lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1, cg_precision="fp64",
-                 bem_anchor=0.0, adjoint_cg_precision="fp64"):
+                 bem_anchor=0.0, adjoint_cg_precision="fp64", anchor_product="fp32"):
         if periodic_bc is not None:
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
@@ -140,6 +140,9 @@ class Simulation(object):
         # fp32x2 only: > 0 forms B x as B x0 + B32 (x - x0) while x stays within
         # this relative max-norm distance of the last compensated product's x0
         self.bem_anchor = float(bem_anchor)
+        # ensemble anchored product's difference B (x - x0): "fp32" or "fp16"
+        # (FP16 copy of B in tensor-core fragment order, FP32 accumulation)
+        self.anchor_product = anchor_product
         # Poisson solves of the RK4 adjoint's backward pass ("fp32": FP32 CG
         # iterations with FP64 residual refinement to the same tolerance)
         self.adjoint_cg_precision = adjoint_cg_precision
@@ -211,6 +214,7 @@ class Simulation(object):
         opts.n_members = self.n_members if self.n_members > 1 else 0
         opts.bem_anchor_tol = self.bem_anchor
         opts.adjoint_cg_precision = {"fp64": 0, "fp32": 1}[self.adjoint_cg_precision]
+        opts.anchor_product = {"fp32": 0, "fp16": 1}[self.anchor_product]
         self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
         poly = self.material.anisotropy_polynomial(self.quirks)
         if poly is not None:

@@ -122,3 +122,43 @@ def test_anchored_ensemble_integration_matches_fp64(small_box):
     assert np.abs(anc.get_m() - ref.get_m()).max() <= 2e-6
     anc.close()
     ref.close()
+
+
+def test_fp16_fragment_difference_product(cube):
+    """anchor_product 1: the difference B (x - x0) of the anchored ensemble
+    product from the FP16 fragment copy of B on the tensor cores
+    (mma.m16n8k16, FP32 accumulation).  Ten members (a chunk of 8 and one of
+    2, so unused operand columns are exercised).  A refresh is the
+    compensated product itself; after a small move the result stays within
+    FP16 rounding of |B||x - x0| of the FP32-difference form, and a wrong
+    fragment order would be off by O(1)."""
+    mat = permalloy(0.5)
+    B = 10
+    h16, _ = make_ensemble(cube, mat, B, bem_precision=2, anchor=0.02, anchor_product=1)
+    f32, _ = make_ensemble(cube, mat, B, bem_precision=2, anchor=0.02, anchor_product=0)
+    ref, _ = make_ensemble(cube, mat, B, bem_precision=0)
+    N = len(cube.points)
+    ms = np.stack([seeded_m(N, base=(1.0, 0.2 * b, -0.3), seed=700 + b, noise=0.5) for b in range(B)])
+    hs = np.broadcast_to([0.02, -0.01, 0.005], (B, N, 3)).copy()
+    for e in (h16, f32, ref):
+        e.set_h_ext(hs)
+        e.set_m(ms)
+    f, g = h16.eval_fields(), ref.eval_fields()
+    assert h16.bem_anchor_stats() == (2, 2)
+    assert _rel(f["H_demag"], g["H_demag"]) <= 1e-9          # refresh: the compensated product
+    f32.eval_fields()
+    rng = np.random.default_rng(8)
+    m2 = ms + 1e-3 * rng.standard_normal(ms.shape)
+    m2 /= np.linalg.norm(m2, axis=-1, keepdims=True)
+    for e in (h16, f32, ref):
+        e.set_m(m2)
+    f, f3, g = h16.eval_fields(), f32.eval_fields(), ref.eval_fields()
+    assert h16.bem_anchor_stats() == (4, 2)                   # both chunks anchored
+    e16 = _rel(f["H_demag"], g["H_demag"])
+    assert _rel(f3["H_demag"], g["H_demag"]) <= 1e-9
+    assert e16 <= 2e-5, e16
+    for b in range(B):                                        # every member, both chunks
+        assert _rel(f["H_demag"][b], g["H_demag"][b]) <= 2e-5, b
+    h16.close()
+    f32.close()
+    ref.close()

@@ -10,7 +10,8 @@ from test_gpu_parity import make_engine
 pytestmark = pytest.mark.gpu
 
 
-def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0, anchor=0.0, adjoint_cg=0):
+def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0, anchor=0.0, adjoint_cg=0,
+                  anchor_product=0):
     from nmag import _lib
     single = make_engine(msh, mat, tol=tol, bem_precision=bem_precision)
     c = mat.coefficients("nmag")
@@ -29,6 +30,7 @@ def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0, ancho
     op.n_members = B
     op.bem_anchor_tol = anchor
     op.adjoint_cg_precision = adjoint_cg
+    op.anchor_product = anchor_product
     ens = _lib.Engine(msh.points, msh.simplices, mt, op)
     if c.get("anis_poly") is not None:
         ens.set_anisotropy_poly(*c["anis_poly"])
