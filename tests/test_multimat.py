@@ -2,13 +2,12 @@
 multi-material right-hand side (oracle/multimat.py), pinned against the
 single-material C oracle and by known answers.  CPU only."""
 import numpy as np
-import pytest
 
 import nmag
 from nmag import SI
 from nmag.mesh import Mesh, box_mesh
 from nmag.sites import SiteLayer
-from conftest import permalloy, seeded_m
+from conftest import seeded_m
 
 TIGHT = (1e-13, 1e-50, 20000)
 
