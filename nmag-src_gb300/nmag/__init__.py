@@ -13,9 +13,9 @@ from . import mesh
 from .si import SI, simulation_units
 from .material import MagMaterial
 from .anisotropy import PredefinedAnisotropy, uniaxial_anisotropy, cubic_anisotropy
-from .simulation import Simulation, every, at
+from .simulation import Simulation, every, at, never
 from ._lib import NmagGpuError
 
 __all__ = ["SI", "simulation_units", "MagMaterial", "PredefinedAnisotropy", "uniaxial_anisotropy", "cubic_anisotropy",
-           "Simulation", "every", "at", "mesh",
+           "Simulation", "every", "at", "never", "mesh",
            "NmagGpuError"]

@@ -150,6 +150,72 @@ class SI(object):
         u = " ".join("%s^%d" % (k, v) if v != 1 else k for k, v in sorted(self.dims.items()))
         return "SI(%r, %r)" % (self.value, u)
 
+    # the rest of the reference's Physical interface (si_units/lib.py:330-470)
+    def in_units_of(self, unit):
+        """This quantity as a multiple of ``unit`` (compatible units)."""
+        u = unit if isinstance(unit, SI) else SI(float(unit))
+        if u.dims != self.dims:
+            raise ValueError("%r is not compatible with %r" % (self, u))
+        return self.value / u.value
+
+    def get_units(self):
+        """The units of this quantity (value 1)."""
+        return self._new(1.0, self.dims)
+
+    def copy(self):
+        return self._new(self.value, self.dims)
+
+    def _cmp_value(self, o):
+        # zero compares with any dimension (lib.py:364-374)
+        if not isinstance(o, SI):
+            o = SI(float(o))
+        if o.dims != self.dims and self.value != 0.0 and o.value != 0.0:
+            raise ValueError("Expected quantities of matching dimensions: %r and %r" % (self, o))
+        return o.value
+
+    def __lt__(self, o):
+        return self.value < self._cmp_value(o)
+
+    def __le__(self, o):
+        return self.value <= self._cmp_value(o)
+
+    def __gt__(self, o):
+        return self.value > self._cmp_value(o)
+
+    def __ge__(self, o):
+        return self.value >= self._cmp_value(o)
+
+    def __eq__(self, o):
+        if not isinstance(o, SI):
+            return False
+        return self.dims == o.dims and self.value == o.value
+
+    def __ne__(self, o):
+        return not self.__eq__(o)
+
+    __hash__ = None
+
+    def __abs__(self):
+        return self._new(abs(self.value), self.dims)
+
+    def __pos__(self):
+        return self.copy()
+
+    def __str__(self):
+        """'<SI: 1e+06  A / m >' (lib.py:376-395)."""
+        def part(sign):
+            out = ""
+            for u in ("m", "kg", "s", "A", "K", "mol", "cd"):
+                p = self.dims.get(u, 0)
+                if p and (p > 0) == (sign > 0):
+                    out += " %s" % u if abs(p) == 1 else " %s^%d" % (u, abs(p))
+            return out
+        powers = part(+1)
+        neg = part(-1)
+        if neg:
+            powers = "%s /%s" % (powers, neg)
+        return "<SI: %g %s >" % (self.value, powers)
+
     def dens_str(self, angles=True):
         """si_units/lib.py:304-340: '<A/m>', '<kg/ms^2>', '<1e-09m>': positive
         then negative powers in the order m kg s A K mol cd, no separators."""

@@ -179,3 +179,22 @@ def test_load_mesh_region_checks_without_gpu():
     two = nmag.mesh.Mesh(shelled.points, shelled.simplices, np.where(shelled.regions == 1, 2, 1))
     with pytest.raises(ValueError):
         sim.load_mesh(two, [("a", a)], unit_length=SI(1e-9, "m"))
+
+
+def test_si_physical_interface():
+    """si_units/lib.py: in_units_of, get_units, comparisons (zero against any
+    dimension), abs, str."""
+    from nmag import SI
+    d = SI(10.0, "m")
+    assert d.in_units_of(SI(2.54e-2, "m")) == pytest.approx(393.7007874015748)
+    with pytest.raises(ValueError):
+        d.in_units_of(SI(1.0, "s"))
+    assert d.get_units().value == 1.0 and d.get_units().dims == d.dims
+    assert SI(1.0, "m") < SI(2.0, "m") and SI(3.0, "m") >= SI(3.0, "m") and SI(0.0, "s") < SI(1.0, "m")
+    with pytest.raises(ValueError):
+        SI(1.0, "m") < SI(2.0, "s")
+    assert SI(2.0, "A/m") == SI(2.0, "A/m") and SI(2.0, "A/m") != SI(2.0, "m")
+    assert abs(SI(-3.0, "s")).value == 3.0
+    assert str(SI(1e6, "A/m")) == "<SI: 1e+06  A / m >"
+    import nmag
+    assert nmag.never.match_time({"step": 0}) is False
