@@ -183,9 +183,11 @@ class Simulation(object):
         c0 = mats[0].coefficients(self.quirks)
         if any(mt.coefficients(self.quirks) != c0 for mt in mats[1:]):
             raise NotImplementedError("one magnetic material (possibly over several regions) is supported on this path")
-        if np.any(m.regions > len(region_names_and_mag_mats)):
-            raise ValueError("load_mesh: the mesh has region ids beyond the %d regions named"
-                             % len(region_names_and_mag_mats))
+        nreg = int(m.regions.max()) if len(m.regions) else 0
+        if nreg != len(region_names_and_mag_mats):   # main.py:1174-1180
+            raise ValueError("Found inconsistency between the mesh you loaded and the provided list of "
+                             "(region_name, materials). The mesh has %d regions but the provided list has "
+                             "%d pairs." % (nreg, len(region_names_and_mag_mats)))
         # vacuum simplices carry no magnetisation; the magnetic part alone is
         # simulated (its open-boundary potential comes from the BEM), and
         # per-site arrays refer to its nodes, as nmag's m subfields do

@@ -179,6 +179,9 @@ def test_load_mesh_region_checks_without_gpu():
     two = nmag.mesh.Mesh(shelled.points, shelled.simplices, np.where(shelled.regions == 1, 2, 1))
     with pytest.raises(ValueError):
         sim.load_mesh(two, [("a", a)], unit_length=SI(1e-9, "m"))
+    # one (region, materials) pair per region of the mesh (main.py:1174-1180)
+    with pytest.raises(ValueError):
+        sim.load_mesh(two, [("a", a), ("b", a), ("c", a)], unit_length=SI(1e-9, "m"))
 
 
 def test_si_physical_interface():
