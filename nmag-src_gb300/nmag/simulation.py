@@ -276,7 +276,10 @@ class Simulation(object):
         return arr.reshape(N, 3).copy()
 
     def set_m(self, values, subfieldname=None):
-        """main.py:1787: set m (auto-normalised)."""
+        """main.py:1787: set m (auto-normalised); subfieldname 'm_<material>'
+        or None (every material)."""
+        if subfieldname is not None and self._field_of(subfieldname) != "m":
+            raise KeyError("set_m: '%s' is not a magnetisation subfield" % subfieldname)
         m = self._vector_values(values)
         n = np.linalg.norm(m, axis=-1)
         if np.any(n == 0.0):
@@ -513,46 +516,52 @@ class Simulation(object):
         return self.hysteresis([H_applied], save=save, do=do, convergence_check=convergence_check)
 
     # ---- read-out ------------------------------------------------------------
+    # fields per material (subfields <field>_<material>) and over the mesh
+    # (main.py:199-206); the bare field name is accepted for the one material
+    _PER_MATERIAL = ("E_total", "E_demag", "E_exch", "E_anis", "E_ext", "H_total", "H_exch", "H_anis", "dmdt",
+                     "m", "M")
+    _ON_MESH = ("H_demag", "H_ext", "phi", "rho", "pin", "current_density")
+    _KIND = {"m": "m", "M": "M", "H_total": "H", "H_exch": "H", "H_anis": "H", "H_demag": "H", "H_ext": "H",
+             "dmdt": "dmdt", "E_total": "E", "E_demag": "E", "E_exch": "E", "E_anis": "E", "E_ext": "E",
+             "phi": "phi", "rho": "rho", "pin": "pin", "current_density": "J"}
+
+    def _field_of(self, subfieldname):
+        """The field of a subfield name; KeyError for names that name no
+        subfield of this simulation (main.py:612-628)."""
+        if subfieldname in self._ON_MESH:
+            return subfieldname
+        for f in self._PER_MATERIAL:
+            if subfieldname == f:
+                return f
+            if subfieldname.startswith(f + "_"):
+                if self.material is None or subfieldname[len(f) + 1:] != self.material.name:
+                    break
+                return f
+        raise KeyError("Couldn't find field for subfieldname '%s'" % subfieldname)
+
     def get_subfield(self, subfieldname, units=None):
-        """Field values per node in SI (m is dimensionless)."""
-        if subfieldname == "m" or subfieldname.startswith("m_"):
+        """main.py:1480-1568: field values per site in SI (the reference's unit
+        table); m is dimensionless."""
+        field = self._field_of(subfieldname)
+        if field == "m":
             return self._m.copy()
-        if subfieldname == "M" or subfieldname.startswith("M_"):   # M = Ms m (nmag_lam.py:463)
+        if field == "M":   # M = Ms m (nmag_lam.py:463)
             return self._m * self.material.coefficients(self.quirks)["Ms"] * _su_factor("M")
-        if subfieldname.startswith("H_ext"):
+        if field == "H_ext":
             return self._h_ext * _su_factor("H")
-        if subfieldname == "pin":
+        if field == "pin":
             p = getattr(self, "_pin", None)
             return p.copy() if p is not None else np.ones(self.engine.N)
-        if subfieldname.startswith("current_density"):
+        if field == "current_density":
             j = self._j if getattr(self, "_j", None) is not None else np.zeros_like(self._h_ext)
             return j * _su_factor("J")
+        if field.startswith("E_"):
+            return self.engine.energy_density()[field] * _su_factor("E")
         f = self.engine.eval_fields()
-        for key in ("H_exch", "H_demag", "H_anis", "H_total"):
-            if subfieldname.startswith(key):
-                return f[key] * _su_factor("H")
-        if subfieldname.startswith("dmdt"):
-            return f["dmdt"] * _su_factor("dmdt")
-        if subfieldname == "phi":
-            return f["phi"] * _su_factor("phi")
-        if subfieldname == "rho":
-            return f["rho"] * _su_factor("rho")
-        if subfieldname.startswith("E_"):
-            E = self.engine.energy_density()
-            for key in E:
-                if subfieldname.startswith(key):
-                    return E[key] * _su_factor("E")
-        raise KeyError("unknown subfield %r" % subfieldname)
-
-    _UNITS = {"m": SI(1.0), "M": SI(1.0, "A/m"), "H": SI(1.0, "A/m"), "E": SI(1.0, "J/m^3"),
-              "phi": SI(1.0, "A"), "rho": SI(1.0, "A/m^2"), "dmdt": SI(1.0, "1/s"), "pin": SI(1.0),
-              "current_density": SI(1.0, "A/m^2")}
+        return f[field] * _su_factor(self._KIND[field])
 
     def _unit_of(self, subfieldname):
-        for key in ("current_density", "dmdt", "phi", "rho", "pin"):
-            if subfieldname.startswith(key):
-                return self._UNITS[key]
-        return self._UNITS[subfieldname.split("_")[0] if subfieldname[0] in "mMHE" else subfieldname]
+        return _FIELD_SI[self._KIND[self._field_of(subfieldname)]]
 
     def probe_subfield_siv(self, subfieldname, pos, unit=None):
         """main.py:1651-1700: the subfield at a position given in metres

@@ -197,3 +197,26 @@ def test_subfield_averages(tmp_path, monkeypatch):
         sim.get_subfield_average_siv("m", "Co")
     M = sim.get_subfield("M_Py")
     assert np.allclose(M, eng.get_m() * 0.86e6, rtol=1e-11)
+
+
+def test_subfield_names_probe_and_units(tmp_path, monkeypatch):
+    """Subfield names as the reference resolves them (main.py:612-628): a
+    per-material field with this material's suffix or bare, mesh fields bare;
+    the probe interpolates in the simplex (None outside) and carries the
+    reference's units."""
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    assert np.allclose(sim.get_subfield("m_Py"), eng.get_m())
+    for bad in ("m_Co", "H_demag_Py", "E_total_Co", "Hdemag", "H_ext_x"):
+        with pytest.raises(KeyError):
+            sim.get_subfield(bad)
+    with pytest.raises(KeyError):
+        sim.set_m([1.0, 0.0, 0.0], "m_Co")
+    assert np.allclose(sim.get_subfield("H_demag"), 0.1e6)
+    inside = [0.2e-9, 0.2e-9, 0.2e-9]
+    assert sim.probe_subfield_siv("H_demag", inside) == pytest.approx([0.1e6] * 3)
+    assert sim.probe_subfield_siv("E_exch_Py", inside) == pytest.approx(0.5e6)
+    assert sim.probe_subfield_siv("m", [5e-9, 0.0, 0.0]) is None
+    d = sim.probe_subfield("dmdt_Py", [SI(v, "m") for v in inside])
+    assert d[0].dims == SI("A/m s").dims
+    H = sim.probe_subfield("H_total", [SI(v, "m") for v in inside])
+    assert H[2].dims == SI("A/m").dims and H[2].value == pytest.approx(0.1e6)
