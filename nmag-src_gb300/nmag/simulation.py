@@ -539,9 +539,10 @@ class Simulation(object):
                 return f
         raise KeyError("Couldn't find field for subfieldname '%s'" % subfieldname)
 
-    def get_subfield(self, subfieldname, units=None):
+    def get_subfield(self, subfieldname, units=None, _snap=None):
         """main.py:1480-1568: field values per site in SI (the reference's unit
-        table); m is dimensionless."""
+        table); m is dimensionless.  (_snap: fields and energy densities of
+        one evaluation, for callers reading several subfields.)"""
         field = self._field_of(subfieldname)
         if field == "m":
             return self._m.copy()
@@ -556,8 +557,9 @@ class Simulation(object):
             j = self._j if getattr(self, "_j", None) is not None else np.zeros_like(self._h_ext)
             return j * _su_factor("J")
         if field.startswith("E_"):
-            return self.engine.energy_density()[field] * _su_factor("E")
-        f = self.engine.eval_fields()
+            E = _snap["E"] if _snap else self.engine.energy_density()
+            return E[field] * _su_factor("E")
+        f = _snap["f"] if _snap else self.engine.eval_fields()
         return f[field] * _su_factor(self._KIND[field])
 
     def _unit_of(self, subfieldname):
@@ -778,7 +780,19 @@ class Simulation(object):
             names, values, units = self._compute_averages()
             self._save_data_table_to_ndt(names, values, units, "%s_dat.ndt" % self.name)
         if fields:
-            np.savez("%s_fields_%06d.npz" % (self.name, self.clock.step), m=self._m)
+            # the reference writes the fields into <name>_dat.h5 (main.py:2527-2534,
+            # _save_fields); here one .npz per save, arrays per site in SI
+            names = list(self._PER_MATERIAL) + list(self._ON_MESH) if fields == "all" else (
+                [fields] if isinstance(fields, str) else list(fields))
+            for name in names:
+                self._field_of(name)   # KeyError for unknown fields
+            snap = {"f": self.engine.eval_fields(), "E": self.engine.energy_density()}
+            out = {name: self.get_subfield(name, _snap=snap) for name in names}
+            np.savez("%s_fields_%06d.npz" % (self.name, self.clock.step), **out)
+
+    def get_restart_file_name(self):
+        """The default restart file (simulation_core.py:343-345; .npz here)."""
+        return "%s_restart.npz" % self.name
 
     def save_restart_file(self, filename=None):
         """main.py:2764-2857: m and the clock, written via a temp file + rename."""

@@ -220,3 +220,18 @@ def test_subfield_names_probe_and_units(tmp_path, monkeypatch):
     assert d[0].dims == SI("A/m s").dims
     H = sim.probe_subfield("H_total", [SI(v, "m") for v in inside])
     assert H[2].dims == SI("A/m").dims and H[2].value == pytest.approx(0.1e6)
+
+
+def test_save_fields_and_restart_name(tmp_path, monkeypatch):
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    sim.save_data(fields="all")
+    d = np.load(list(tmp_path.glob("hyst_fields_*.npz"))[0])
+    assert {"m", "M", "H_demag", "E_total", "phi", "pin"} <= set(d.files)
+    assert np.allclose(d["H_demag"], 0.1e6)
+    sim.clock.step = 7
+    sim.save_data(fields=["m"])
+    d = np.load(str(tmp_path / "hyst_fields_000007.npz"))
+    assert d.files == ["m"]
+    with pytest.raises(KeyError):
+        sim.save_data(fields=["B_field"])
+    assert sim.get_restart_file_name() == "hyst_restart.npz"
