@@ -320,7 +320,11 @@ class Simulation(object):
     def set_current_density(self, values, unit=None):
         """main.py:1934-1960: the current density of the spin-transfer
         torque, values times unit (SI, compatible with A/m^2; SI values or
-        numbers in A/m^2 without a unit)."""
+        numbers in A/m^2 without a unit).  The field exists only when the
+        material has a spin polarisation (nmag_lam.py:195-202; main.py:570)."""
+        if self.material is None or self.material.su_llg_stt_prefactor == 0.0:
+            raise KeyError("set_current_density: no 'current_density' field (the material has no "
+                           "llg_polarisation)")
         if unit is None:
             if isinstance(values, (list, tuple)) and values and isinstance(values[0], SI):
                 j = self._vector_values([simulation_units.of(v, compatible_with=SI("A/m^2")) for v in values])

@@ -235,3 +235,9 @@ def test_save_fields_and_restart_name(tmp_path, monkeypatch):
     with pytest.raises(KeyError):
         sim.save_data(fields=["B_field"])
     assert sim.get_restart_file_name() == "hyst_restart.npz"
+
+
+def test_current_density_needs_a_polarisation(tmp_path, monkeypatch):
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    with pytest.raises(KeyError):
+        sim.set_current_density([1e12, 0, 0], unit=SI("A/m^2"))
