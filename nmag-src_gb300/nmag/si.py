@@ -267,6 +267,24 @@ class SimulationUnits(object):
 simulation_units = SimulationUnits({"A": 1e-3, "kg": 1e-27, "m": 1e-9, "s": 1e-12, "cd": 1.0, "K": 1.0, "mol": 1.0})
 
 
+def str_of_SI_vector(v):
+    """'[1e+06 0 0]<A/m>' (si_units/lib.py str_of_SI_vector): the values with
+    %g and the common unit once; plain zeros may stand among SI values."""
+    if v is None:
+        return "None"
+    dims = None
+    vals = []
+    for x in v:
+        if isinstance(x, SI):
+            if dims is None or (not any(dims.values()) and x.dims):
+                dims = x.dims
+            vals.append(x.value)
+        else:
+            vals.append(float(x))
+    unit = SI(1.0, dict(dims or {})).dens_str()
+    return "[%s]%s" % (" ".join("%g" % x for x in vals), unit)
+
+
 def g6(x: float) -> float:
     """Round like C's printf("%g") (6 significant digits).
 

@@ -201,3 +201,15 @@ def test_si_physical_interface():
     assert str(SI(1e6, "A/m")) == "<SI: 1e+06  A / m >"
     import nmag
     assert nmag.never.match_time({"step": 0}) is False
+
+
+def test_str_of_si_vector():
+    """The expectations of si_units/test_lib.py."""
+    from nmag.si import SI, str_of_SI_vector
+    H = [SI(1000000, ["m", -1.0, "A", 1.0]), SI(0, ["m", -1.0, "A", 1.0]), SI(0, ["m", -1.0, "A", 1.0])]
+    assert str_of_SI_vector([SI(0, "A/m"), SI(100, "A/m")]) == "[0 100]<A/m>"
+    assert str_of_SI_vector([0, SI(123, "A/m")]) == "[0 123]<A/m>"
+    assert str_of_SI_vector([0, SI(123, "A/m"), 0]) == "[0 123 0]<A/m>"
+    assert str_of_SI_vector(H) == "[1e+06 0 0]<A/m>"
+    assert str_of_SI_vector([SI(1, "A/m")]) == "[1]<A/m>"
+    assert str_of_SI_vector(None) == "None"
