@@ -72,6 +72,15 @@ class SiteLayer(object):
         k = self.material_index(name)
         return np.arange(self.offset[k], self.offset[k] + len(self.nodes[k]))
 
+    def site_index(self, name, node):
+        """The site of a material at a mesh node; KeyError where the
+        material is not defined (as fefields.set_field_at_site fails there)."""
+        k = self.material_index(name)
+        j = np.searchsorted(self.nodes[k], node)
+        if j >= len(self.nodes[k]) or self.nodes[k][j] != node:
+            raise KeyError("material %r has no site at node %d" % (name, node))
+        return self.offset[k] + int(j)
+
     def submesh(self, name, points):
         """(points, simplices) of a material's sites: its own mesh, whose
         outer surface is where the material ends (regions of other materials

@@ -2,6 +2,7 @@
 multi-material right-hand side (oracle/multimat.py), pinned against the
 single-material C oracle and by known answers.  CPU only."""
 import numpy as np
+import pytest
 
 import nmag
 from nmag import SI
@@ -143,3 +144,22 @@ def test_no_exchange_across_the_interface():
     b_sites = L.sites_of("B")
     assert np.array_equal(h1[b_sites], h0[b_sites])
     assert np.abs(h1[L.sites_of("A")] - h0[L.sites_of("A")]).max() > 0.0
+
+
+def test_sites_where_each_material_is_defined():
+    """The expectations of interface/nmag/test_fefields.py on a two-region
+    mesh: a subfield on region A, one on region B and one on both; setting
+    one at a node works exactly where its material is defined (interface
+    nodes belong to both regions)."""
+    msh = halves()
+    L = SiteLayer(msh, [["ab", "a"], ["ab", "b"]])
+    x = msh.points[:, 0]
+    for node in range(msh.n_nodes):
+        in_a, in_b = x[node] <= 6.0, x[node] >= 6.0
+        assert L.site_node[L.site_index("ab", node)] == node
+        for name, defined in (("a", in_a), ("b", in_b)):
+            if defined:
+                assert L.site_node[L.site_index(name, node)] == node
+            else:
+                with pytest.raises(KeyError):
+                    L.site_index(name, node)
