@@ -738,7 +738,8 @@ int sync_check(nmg_batch *b, const char *where) {
   int derr = 0;
   cudaMemcpy(&derr, b->err.p, sizeof(int), cudaMemcpyDeviceToHost);
   if (derr) {
-    cudaMemset(b->err.p, 0, sizeof(int));
+    cudaMemsetAsync(b->err.p, 0, sizeof(int), b->stream);
+    cudaStreamSynchronize(b->stream);
     return bfail(b, (derr & nmg::ERR_NONFINITE) ? 6 : 5,
                  std::string(where) + ((derr & nmg::ERR_NONFINITE) ? ": non-finite state or CG failure"
                                                                     : ": CG reached its iteration limit"));
@@ -942,7 +943,9 @@ int nmg_batch_create(const nmg_particle *parts, int n, const nmg_batch_options *
     nmg_batch_destroy(b);
     return bfail(nullptr, rc, e);
   }
-  if (cudaStreamSynchronize(b->stream) != cudaSuccess) {
+  // the setup copies above ran on the legacy stream, which the batch's
+  // non-blocking stream does not wait for: finish them before any launch
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
     nmg_batch_destroy(b);
     return bfail(nullptr, 100, "nmg_batch_create: setup failed");
   }
@@ -979,7 +982,7 @@ int nmg_batch_set_m(nmg_batch *b, const double *m) {
   cudaMemcpyAsync(st.data(), b->st.p, sizeof(nmg::PState) * b->P, cudaMemcpyDeviceToHost, b->stream);
   cudaStreamSynchronize(b->stream);
   for (auto &s : st) s.have_k1 = 0;
-  cudaMemcpy(b->st.p, st.data(), sizeof(nmg::PState) * b->P, cudaMemcpyHostToDevice);
+  cudaMemcpyAsync(b->st.p, st.data(), sizeof(nmg::PState) * b->P, cudaMemcpyHostToDevice, b->stream);
   return sync_check(b, "nmg_batch_set_m");
 }
 

@@ -224,10 +224,13 @@ int nmg_set_anisotropy_poly(nmg_handle *h, int n_e, const int32_t *e_pow, const 
     return fail(h, 100, "nmg_set_anisotropy_poly: sync failed");
   if (ap.epow.alloc(n_e) || ap.ecoef.alloc(n_e) || ap.hpow.alloc(n_h) || ap.hcoef.alloc(3 * (size_t)n_h))
     return fail(h, 100, "nmg_set_anisotropy_poly: device allocation failed");
-  if ((n_e > 0 && (cudaMemcpy(ap.epow.p, e_pow, sizeof(int32_t) * n_e, cudaMemcpyHostToDevice) ||
-                   cudaMemcpy(ap.ecoef.p, e_coef, sizeof(double) * n_e, cudaMemcpyHostToDevice))) ||
-      (n_h > 0 && (cudaMemcpy(ap.hpow.p, h_pow, sizeof(int32_t) * n_h, cudaMemcpyHostToDevice) ||
-                   cudaMemcpy(ap.hcoef.p, h_coef, sizeof(double) * 3 * n_h, cudaMemcpyHostToDevice))))
+  // on the handle's (non-blocking) stream, completed before returning
+  cudaStream_t s = h->stream;
+  if ((n_e > 0 && (cudaMemcpyAsync(ap.epow.p, e_pow, sizeof(int32_t) * n_e, cudaMemcpyHostToDevice, s) ||
+                   cudaMemcpyAsync(ap.ecoef.p, e_coef, sizeof(double) * n_e, cudaMemcpyHostToDevice, s))) ||
+      (n_h > 0 && (cudaMemcpyAsync(ap.hpow.p, h_pow, sizeof(int32_t) * n_h, cudaMemcpyHostToDevice, s) ||
+                   cudaMemcpyAsync(ap.hcoef.p, h_coef, sizeof(double) * 3 * n_h, cudaMemcpyHostToDevice, s))) ||
+      cudaStreamSynchronize(s) != cudaSuccess)
     return fail(h, 100, "nmg_set_anisotropy_poly: copy failed");
   ap.ne = n_e;
   ap.nh = n_h;
@@ -240,7 +243,8 @@ int nmg_set_stt(nmg_handle *h, double c4, double c5) {
   if (!std::isfinite(c4) || !std::isfinite(c5)) return fail(h, -5, "nmg_set_stt: non-finite coefficient");
   const size_t n3 = 3 * (size_t)h->mesh.N * h->nrep;
   if ((c4 != 0.0 || c5 != 0.0) && !h->stt.j.p) {   // current density starts at zero
-    if (h->stt.j.alloc(n3) || h->stt.dmdc.alloc(n3) || cudaMemset(h->stt.j.p, 0, sizeof(double) * n3))
+    if (h->stt.j.alloc(n3) || h->stt.dmdc.alloc(n3) ||
+        cudaMemsetAsync(h->stt.j.p, 0, sizeof(double) * n3, h->stream) || cudaStreamSynchronize(h->stream))
       return fail(h, 100, "nmg_set_stt: device allocation failed");
   }
   h->stt.c4 = c4;
