@@ -14,8 +14,9 @@ from .si import SI, simulation_units
 from .material import MagMaterial
 from .anisotropy import PredefinedAnisotropy, uniaxial_anisotropy, cubic_anisotropy
 from .simulation import Simulation, every, at, never
+from .sets import float_set, vector_set
 from ._lib import NmagGpuError
 
 __all__ = ["SI", "simulation_units", "MagMaterial", "PredefinedAnisotropy", "uniaxial_anisotropy", "cubic_anisotropy",
            "Simulation", "every", "at", "never", "mesh",
-           "NmagGpuError"]
+           "float_set", "vector_set", "NmagGpuError"]
