@@ -466,8 +466,27 @@ class Simulation(object):
                     joint.append((fn, when, key))
         return joint
 
+    def _update_progress_file(self, H, filename, min_delay):
+        """hysteresis.py:25-40: at most every min_delay seconds, the time, the
+        clock and the convergence state into <name>_progress.txt, and a log
+        line."""
+        now = _time.time()
+        if now - getattr(self, "_progress_t", -1e300) < min_delay:
+            return
+        self._progress_t = now
+        with open(filename, "w") as f:
+            f.write(_time.asctime() + "\n")
+            for k in ("id", "stage", "step", "stage_step", "time_su", "stage_time_su", "real_time",
+                      "last_step_dt_su", "convergence", "stage_end"):
+                f.write("%-16s %s\n" % (k, self.clock[k]))
+            f.write("max_dm_dt %s (stop below %s, simulation units)\n" % (self.max_dm_dt, self.stopping_dm_dt))
+        Hs = "None" if H is None else _si.str_of_SI_vector(
+            H if isinstance(H, (list, tuple)) and H and isinstance(H[0], SI) else list(np.ravel(H))[:3])
+        log.info("it %d, time %g s; stage %d; H_ext=%s" % (self.clock.step, self.clock.time_su * 1e-12,
+                                                          self.clock.stage, Hs))
+
     def hysteresis(self, H_ext_list, save=(("averages", "fields", at("stage_end")),), do=(),
-                   convergence_check=every("step", 5)):
+                   convergence_check=every("step", 5), progress_message_minimum_delay=60):
         """hysteresis.py:244-557: for each applied field (None keeps the
         current one) start a stage and integrate until converged, running
         the save / do actions whenever their schedules fire."""
@@ -513,11 +532,16 @@ class Simulation(object):
                 if simulation_units.of(t, compatible_with=SI("s")) > 0.99 * self.max_time_reached:
                     raise RuntimeError("Simulation time reached %s: are you starting from a zero torque "
                                        "configuration?" % self.max_time_reached)
+                try:   # progress reports never stop the loop (hysteresis.py:541-551)
+                    self._update_progress_file(H, self.name + "_progress.txt", progress_message_minimum_delay)
+                except Exception as exc:
+                    log.info("Problem when generating progress file: %s" % exc)
 
     def relax(self, H_applied=None, save=(("averages", "fields", at("stage_end")),), do=(),
-              convergence_check=every("step", 5)):
+              convergence_check=every("step", 5), progress_message_minimum_delay=60):
         """hysteresis.py:207-242: hysteresis([H_applied])."""
-        return self.hysteresis([H_applied], save=save, do=do, convergence_check=convergence_check)
+        return self.hysteresis([H_applied], save=save, do=do, convergence_check=convergence_check,
+                               progress_message_minimum_delay=progress_message_minimum_delay)
 
     # ---- read-out ------------------------------------------------------------
     # fields per material (subfields <field>_<material>) and over the mesh

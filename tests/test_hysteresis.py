@@ -241,3 +241,14 @@ def test_current_density_needs_a_polarisation(tmp_path, monkeypatch):
     sim, eng = make_sim(tmp_path, monkeypatch)
     with pytest.raises(KeyError):
         sim.set_current_density([1e12, 0, 0], unit=SI("A/m^2"))
+
+
+def test_progress_file(tmp_path, monkeypatch):
+    """hysteresis.py:25-40: <name>_progress.txt with the clock and the
+    convergence state, at most every progress_message_minimum_delay seconds."""
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    sim.hysteresis([[0, 0, 1e5]], save=[], progress_message_minimum_delay=0)
+    text = (tmp_path / "hyst_progress.txt").read_text()
+    assert "stage_step" in text and "max_dm_dt" in text
+    step_line = [l for l in text.splitlines() if l.startswith("step ")][0]
+    assert int(step_line.split()[1]) == sim.clock.step
