@@ -234,10 +234,25 @@ class SI(object):
         return "<%s>" % body if angles else body
 
 
-# physical constants (interface/nsim/si_units/si.py)
+# units and physical constants (interface/nsim/si_units/si.py)
+kilogram = SI(1.0, "kg")
+meter = metre = SI(1.0, "m")
+Ampere = SI(1.0, "A")
+Kelvin = SI(1.0, "K")
+second = SI(1.0, "s")
+candela = SI(1.0, "cd")
+mol = SI(1.0, "mol")
+Newton = kilogram * meter / second ** 2
+Joule = SI(1.0, "J")
+Tesla = kilogram / Ampere / second ** 2
+Gauss = 1e-4 * Tesla
 mu0 = SI(4.0e-7 * math.pi, "N/A^2")
+Oersted = Oe = Gauss / mu0
 gamma0 = SI(-2.2137286285040001e5, "m/A s")
 positron_charge = SI(1.6021765314e-19, "C")
+electron_charge = -positron_charge
+plank_constant = 6.6260689633e-34 * Joule * second
+reduced_plank_constant = plank_constant / (2 * math.pi)
 bohr_magneton = SI(9.2740094980e-24, "J/T")
 boltzmann_constant = SI(1.3806504e-23, "J/K")
 degrees_per_ns = SI(math.pi / 180.0 / 1e-9, "1/s")

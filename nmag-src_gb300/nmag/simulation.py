@@ -290,14 +290,14 @@ class Simulation(object):
         self._ts_ready = False
 
     def set_H_ext(self, values, unit=None):
-        """main.py:1726: values times unit (SI, compatible with A/m)."""
+        """main.py:1726-1785: values times unit (SI, compatible with A/m), or
+        SI values; plain numbers without a unit are dimensionless, i.e.
+        simulation units (map_terminals.SI_vector takes SI(""))."""
         if unit is None:
-            vals = values
             if isinstance(values, (list, tuple)) and values and isinstance(values[0], SI):
-                vals = [simulation_units.of(v, compatible_with=SI("A/m")) for v in values]
-                h = self._vector_values(vals)
+                h = self._vector_values([simulation_units.of(v, compatible_with=SI("A/m")) for v in values])
             else:
-                h = self._vector_values(vals) / _su_factor("H")
+                h = self._vector_values(values)
         else:
             h = self._vector_values(values) * simulation_units.of(unit, compatible_with=SI("A/m"))
         self._h_ext = h
@@ -319,17 +319,17 @@ class Simulation(object):
 
     def set_current_density(self, values, unit=None):
         """main.py:1934-1960: the current density of the spin-transfer
-        torque, values times unit (SI, compatible with A/m^2; SI values or
-        numbers in A/m^2 without a unit).  The field exists only when the
+        torque, values times unit (SI, compatible with A/m^2), SI values, or
+        plain numbers in simulation units.  The field exists only when the
         material has a spin polarisation (nmag_lam.py:195-202; main.py:570)."""
         if self.material is None or self.material.su_llg_stt_prefactor == 0.0:
             raise KeyError("set_current_density: no 'current_density' field (the material has no "
                            "llg_polarisation)")
-        if unit is None:
+        if unit is None:   # SI values, or plain numbers in simulation units (as set_H_ext)
             if isinstance(values, (list, tuple)) and values and isinstance(values[0], SI):
                 j = self._vector_values([simulation_units.of(v, compatible_with=SI("A/m^2")) for v in values])
             else:
-                j = self._vector_values(values) / _su_factor("J")
+                j = self._vector_values(values)
         else:
             j = self._vector_values(values) * simulation_units.of(unit, compatible_with=SI("A/m^2"))
         self._j = j

@@ -135,14 +135,18 @@ def test_hysteresis_schedules(tmp_path, monkeypatch):
 
     def record(s):
         seen.append((s.clock.stage, s.clock.stage_step))
-    H = [[0, 0, 1e5], [0, 0, 2e5], [0, 0, 3e5]]
+    H = [[0, 0, 0.1], [0, 0, 0.2], [0, 0, 0.3]]      # plain numbers: simulation units
     sim.hysteresis(H, save=[(record, every("stage_step", 6))],
                    do=[("next stage", at("stage_step", 12)), ("exit", at("step", 30))])
     # stage 1: steps 0, 6, 12 (ended by next_stage at 12); stage 2 likewise;
     # stage 3 exits at step 30 = stage step 6
     assert seen == [(1, 0), (1, 6), (1, 12), (2, 0), (2, 6), (2, 12), (3, 0), (3, 6)]
     assert sim.clock.exit_hysteresis and sim.clock.step == 30
-    assert eng.inits == 3 and np.allclose(eng.H[0], [0, 0, 3e5 * 1e-6])
+    assert eng.inits == 3 and np.allclose(eng.H[0], [0, 0, 0.3])
+    sim.set_H_ext([0, 0, 2e5], SI("A/m"))
+    assert np.allclose(eng.H[0], [0, 0, 0.2])                 # 1 A/m = 1e-6 simulation units
+    sim.set_H_ext([SI(0, "A/m"), SI(0, "A/m"), SI(1e5, "A/m")])
+    assert np.allclose(eng.H[0], [0, 0, 0.1])
 
 
 def test_hysteresis_time_schedule_and_errors(tmp_path, monkeypatch):
@@ -247,7 +251,7 @@ def test_progress_file(tmp_path, monkeypatch):
     """hysteresis.py:25-40: <name>_progress.txt with the clock and the
     convergence state, at most every progress_message_minimum_delay seconds."""
     sim, eng = make_sim(tmp_path, monkeypatch)
-    sim.hysteresis([[0, 0, 1e5]], save=[], progress_message_minimum_delay=0)
+    sim.hysteresis([[0, 0, 0.1]], save=[], progress_message_minimum_delay=0)
     text = (tmp_path / "hyst_progress.txt").read_text()
     assert "stage_step" in text and "max_dm_dt" in text
     step_line = [l for l in text.splitlines() if l.startswith("step ")][0]
