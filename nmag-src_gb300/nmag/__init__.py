@@ -15,8 +15,9 @@ from .material import MagMaterial
 from .anisotropy import PredefinedAnisotropy, uniaxial_anisotropy, cubic_anisotropy
 from .simulation import Simulation, every, at, never
 from .sets import float_set, vector_set
+from .vectools import normalised_vector, vector3_dot, vector3_cross
 from ._lib import NmagGpuError
 
 __all__ = ["SI", "simulation_units", "MagMaterial", "PredefinedAnisotropy", "uniaxial_anisotropy", "cubic_anisotropy",
            "Simulation", "every", "at", "never", "mesh",
-           "float_set", "vector_set", "NmagGpuError"]
+           "float_set", "vector_set", "normalised_vector", "vector3_dot", "vector3_cross", "NmagGpuError"]

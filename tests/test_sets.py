@@ -58,3 +58,10 @@ def test_vector_set():
     assert close(v[1], [0.2672612419124244, 0.5345224838248488, 0.8017837257372732])
     assert close(v[4], [1.0690449676496976, 2.1380899352993952, 3.2071349029490928])
     assert vector_set([0, 2], [1, 2], normalize=False, units=3) == [[0.0, 0.0], [6.0, 12.0]]
+
+
+def test_vectools():
+    import nmag
+    assert nmag.normalised_vector([3.0, 0.0, 4.0]) == [0.6, 0.0, 0.8]
+    assert nmag.vector3_dot([1, 2, 3], [4, 5, 6]) == 32
+    assert nmag.vector3_cross([1, 0, 0], [0, 1, 0]) == (0, 0, 1)
