@@ -62,6 +62,6 @@ def test_vector_set():
 
 def test_vectools():
     import nmag
-    assert nmag.normalised_vector([3.0, 0.0, 4.0]) == [0.6, 0.0, 0.8]
+    assert close(nmag.normalised_vector([3.0, 0.0, 4.0]), [0.6, 0.0, 0.8])
     assert nmag.vector3_dot([1, 2, 3], [4, 5, 6]) == 32
     assert nmag.vector3_cross([1, 0, 0], [0, 1, 0]) == (0, 0, 1)
