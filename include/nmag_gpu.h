@@ -342,8 +342,12 @@ int nmg_bem_anchor_stats(const nmg_handle *h, int64_t out[2]);
  * 8 KB static device array (kept by every GPU that loads the library), which
  * limits n_nodes to 2,097,152; larger sizes return -2.  The first call on a
  * device sets that device up (make it before any stream capture); calls that
- * overlap on the GPU share the scratch and race.  Runs on the default stream
- * and returns after the result is on the host; errors via nmg_last_error(NULL). */
+ * overlap on the GPU share the scratch and race.  Runs on the legacy default
+ * stream and returns after the result is on the host; errors via
+ * nmg_last_error(NULL).  The legacy stream is not ordered with non-blocking
+ * streams (every handle's and batch's own stream is one), so d_m and d_m_prev
+ * must be complete when the call is made: synchronise any stream that wrote
+ * them first (e.g. after nmg_rhs_device or nmg_rk4_device on a handle). */
 int nmg_max_dm_static(const double *d_m, const double *d_m_prev, int n_nodes, double *out);
 
 #ifdef __cplusplus

@@ -1038,7 +1038,10 @@ int nmg_batch_state(const nmg_batch *b, double *t, int32_t *stage, int64_t *step
                     double *max_dmdt) {
   if (!b) return -1;
   std::vector<nmg::PState> st(b->P);
-  if (cudaMemcpy(st.data(), b->st.p, sizeof(nmg::PState) * b->P, cudaMemcpyDeviceToHost) != cudaSuccess)
+  // ordered after the batch's own launches, which run on its non-blocking stream
+  if (cudaMemcpyAsync(st.data(), b->st.p, sizeof(nmg::PState) * b->P, cudaMemcpyDeviceToHost, b->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess)
     return bfail(const_cast<nmg_batch *>(b), 100, "nmg_batch_state: copy failed");
   for (int p = 0; p < b->P; ++p) {
     if (t) t[p] = st[p].t;
@@ -1071,14 +1074,28 @@ int nmg_batch_autotune(nmg_batch *b, int trial_launches, int *threads_out, doubl
   if (save_m.alloc(n3) || save_k0.alloc(n3) || save_p1.alloc(b->Ntot) || save_p2.alloc(b->Ntot) ||
       save_st.alloc(b->P) || (b->hn.p && save_hn.alloc(n3)))
     return bfail(b, 100, "nmg_batch_autotune: allocation failed");
-  if (b->hn.p) cudaMemcpy(save_hn.p, b->hn.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
-  cudaMemcpy(save_m.p, b->m.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
-  cudaMemcpy(save_k0.p, b->k0.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
-  cudaMemcpy(save_p1.p, b->phi1.p, sizeof(double) * b->Ntot, cudaMemcpyDeviceToDevice);
-  cudaMemcpy(save_p2.p, b->phi2.p, sizeof(double) * b->Ntot, cudaMemcpyDeviceToDevice);
-  cudaMemcpy(save_st.p, b->st.p, sizeof(nmg::PState) * b->P, cudaMemcpyDeviceToDevice);
+  // Every copy is ordered on the batch's own (non-blocking) stream, so the
+  // trial launches on that stream see the saved state and each restore.
+  auto d2d = [b](void *dst, const void *src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, b->stream) == cudaSuccess;
+  };
+  auto copy_state = [&](bool save) {
+    bool ok = true;
+    if (b->hn.p) ok &= save ? d2d(save_hn.p, b->hn.p, sizeof(double) * n3) : d2d(b->hn.p, save_hn.p, sizeof(double) * n3);
+    ok &= save ? d2d(save_m.p, b->m.p, sizeof(double) * n3) : d2d(b->m.p, save_m.p, sizeof(double) * n3);
+    ok &= save ? d2d(save_k0.p, b->k0.p, sizeof(double) * n3) : d2d(b->k0.p, save_k0.p, sizeof(double) * n3);
+    ok &= save ? d2d(save_p1.p, b->phi1.p, sizeof(double) * b->Ntot) : d2d(b->phi1.p, save_p1.p, sizeof(double) * b->Ntot);
+    ok &= save ? d2d(save_p2.p, b->phi2.p, sizeof(double) * b->Ntot) : d2d(b->phi2.p, save_p2.p, sizeof(double) * b->Ntot);
+    ok &= save ? d2d(save_st.p, b->st.p, sizeof(nmg::PState) * b->P) : d2d(b->st.p, save_st.p, sizeof(nmg::PState) * b->P);
+    return ok;
+  };
+  auto read_state = [b](std::vector<nmg::PState> &out) {
+    return cudaMemcpyAsync(out.data(), b->st.p, sizeof(nmg::PState) * b->P, cudaMemcpyDeviceToHost, b->stream) ==
+               cudaSuccess &&
+           cudaStreamSynchronize(b->stream) == cudaSuccess;
+  };
   std::vector<nmg::PState> st0(b->P), st1(b->P);
-  cudaMemcpy(st0.data(), b->st.p, sizeof(nmg::PState) * b->P, cudaMemcpyDeviceToHost);
+  if (!copy_state(true) || !read_state(st0)) return bfail(b, 100, "nmg_batch_autotune: saving the state failed");
   double best = -1.0;
   int best_t = b->threads;
   double best_b = b->budget;
@@ -1087,21 +1104,23 @@ int nmg_batch_autotune(nmg_batch *b, int trial_launches, int *threads_out, doubl
       if (nmg_batch_set_schedule(b, threads, f * cmax)) continue;
       auto t0 = std::chrono::steady_clock::now();
       for (int k = 0; k < trial_launches; ++k) launch_run(b);
-      if (sync_check(b, "nmg_batch_autotune")) break;
+      if (sync_check(b, "nmg_batch_autotune")) {
+        copy_state(false);
+        break;
+      }
       const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-      cudaMemcpy(st1.data(), b->st.p, sizeof(nmg::PState) * b->P, cudaMemcpyDeviceToHost);
+      if (!read_state(st1)) return bfail(b, 100, "nmg_batch_autotune: reading the state failed");
       double work = 0.0;
       for (int p = 0; p < b->P; ++p) work += (double)(st1[p].rhs - st0[p].rhs) * b->hdesc[p].cost;
       const double score = work / sec;
       if (score > best) { best = score; best_t = threads; best_b = f * cmax; }
-      cudaMemcpy(b->m.p, save_m.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
-      cudaMemcpy(b->k0.p, save_k0.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
-      cudaMemcpy(b->phi1.p, save_p1.p, sizeof(double) * b->Ntot, cudaMemcpyDeviceToDevice);
-      cudaMemcpy(b->phi2.p, save_p2.p, sizeof(double) * b->Ntot, cudaMemcpyDeviceToDevice);
-      cudaMemcpy(b->st.p, save_st.p, sizeof(nmg::PState) * b->P, cudaMemcpyDeviceToDevice);
-      if (b->hn.p) cudaMemcpy(b->hn.p, save_hn.p, sizeof(double) * n3, cudaMemcpyDeviceToDevice);
+      if (!copy_state(false)) return bfail(b, 100, "nmg_batch_autotune: restoring the state failed");
     }
   }
+  // the last restore (and every copy from the save buffers) completes before
+  // they are freed and before the next launch on any stream
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess)
+    return bfail(b, 100, "nmg_batch_autotune: restoring the state failed");
   int rc = nmg_batch_set_schedule(b, best_t, best_b);
   if (threads_out) *threads_out = best_t;
   if (budget_out) *budget_out = best_b;

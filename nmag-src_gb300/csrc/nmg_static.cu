@@ -16,7 +16,10 @@
 // and caches it; make that first call before any stream capture.  All calls
 // share the array: calls that overlap on the GPU (from several host threads
 // or streams) race on it and must be serialised by the caller.  Every call
-// overwrites each partial it reads, so nothing has to be cleared.
+// overwrites each partial it reads, so nothing has to be cleared.  The kernel
+// and the read-back run on the legacy default stream, which is not ordered
+// with non-blocking streams (a handle's own stream is one): the caller makes
+// sure that whatever wrote m and m_prev has finished before the call.
 #include <mutex>
 
 #include "nmg_internal.h"
@@ -92,8 +95,13 @@ extern "C" int nmg_max_dm_static(const double *d_m, const double *d_m_prev, int 
   const long long per_block = (long long)kStaticThreads * kNodesPerThread;
   const int blocks = (int)((n_nodes + per_block - 1) / per_block);
   k_maxdm_static<<<blocks, kStaticThreads>>>(n_nodes, d_m, d_m_prev, part);
+  // a launch that did not start leaves the previous call's partials in the
+  // array: report it instead of returning their stale maximum
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess)
+    return static_fail(100, std::string("nmg_max_dm_static: launch failed: ") + cudaGetErrorString(e));
   double host[kStaticPartials];
-  cudaError_t e = cudaMemcpy(host, part, sizeof(double) * blocks, cudaMemcpyDeviceToHost);
+  e = cudaMemcpy(host, part, sizeof(double) * blocks, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess)
     return static_fail(100, std::string("nmg_max_dm_static: ") + cudaGetErrorString(e));
   double mx = 0.0;

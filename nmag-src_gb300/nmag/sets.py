@@ -39,8 +39,9 @@ def _continue(out, first, second, last, scale):
 
 
 def float_set(float_list, units=None):
-    """The numbers the list describes (see the module docstring), each
-    multiplied by units when given."""
+    """The numbers the list describes (see the module docstring), multiplied
+    by units when given -- except those of an ``[a, [n], b]`` range, which the
+    reference leaves unscaled (sets.py:88-97)."""
     scale = _scaled(units)
     out = []
     prev2 = prev1 = None   # the last two numbers read
@@ -67,11 +68,13 @@ def float_set(float_list, units=None):
             _continue(out, prev2, prev1, last, scale)
             prev2, prev1, mode = None, last, None
         else:   # n equal steps from prev1 to token (sets.py:88-97)
+            # the reference appends these values without units (only its
+            # other two branches scale), and a drop-in gives the same list
             last = float(token)
             h = (last - prev1) / steps
             start = prev1 + h
             for i in range(steps):
-                out.append(scale(start + i * h))
+                out.append(start + i * h)
             prev2, prev1, mode = None, last, None
     if mode is not None:
         raise ValueError('float_set: the list cannot end with "...", [] or [n]')

@@ -107,6 +107,29 @@ def test_batch_sweep_completes_and_autotune():
     b.close()
 
 
+def test_batch_autotune_leaves_state_unchanged():
+    """The autotuner's trial launches run on a saved copy of the state, which
+    is restored afterwards: m and every particle's clock and counters are bit
+    for bit what they were (the trials advance them)."""
+    from nmag.batch import ParticleBatch
+    parts, _ = _particles([3, 4, 5], seed=9, alpha=0.5)
+    b = ParticleBatch(parts, n_stages=3, h_max=0.5, stop_dmdt=5e-3, rtol=1e-6, atol=1e-6)
+    ms = [seeded_m(len(p[0]), base=(1.0, 0.3, 0.2), seed=90 + k, noise=0.2) for k, p in enumerate(parts)]
+    b.set_m(ms)
+    b.run(1)   # a state in mid-stage, with the FSAL slope held
+    m0, st0 = b.get_m(), b.state()
+    b.autotune(trial_launches=1)
+    m1, st1 = b.get_m(), b.state()
+    for k in range(len(parts)):
+        assert np.array_equal(m0[k], m1[k])
+    for key in ("t", "stage", "steps", "rhs", "done", "max_dmdt"):
+        assert np.array_equal(st0[key], st1[key]), key
+    # and the trials did move it, so the comparison is not vacuous
+    b.run(1)
+    assert (b.state()["rhs"] > st0["rhs"]).all()
+    b.close()
+
+
 def test_batch_ros2_fixed_step_matches_reference():
     """Fixed-step ROS2 on the GPU against the same scheme on the CPU with the
     oracle's RHS, its H_total at the step's start and its Jacobian-vector

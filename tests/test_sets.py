@@ -65,3 +65,10 @@ def test_vectools():
     assert close(nmag.normalised_vector([3.0, 0.0, 4.0]), [0.6, 0.0, 0.8])
     assert nmag.vector3_dot([1, 2, 3], [4, 5, 6]) == 32
     assert nmag.vector3_cross([1, 0, 0], [0, 1, 0]) == (0, 0, 1)
+
+
+def test_float_set_units_scale_all_but_the_n_step_range():
+    # the reference's [a, [n], b] branch appends its values without units
+    # (interface/nsim/sets.py:88-97); its other branches scale them
+    assert float_set([1, 2, [], 4], units=10) == [10.0, 20.0, 30.0, 40.0]
+    assert float_set([1, [3], 4], units=10) == [10.0, 2.0, 3.0, 4.0]

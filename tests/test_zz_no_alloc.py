@@ -38,9 +38,14 @@ def test_static_max_dm_matches_allocating_entry_point(small_box):
         d_now = torch.tensor(m_now, dtype=torch.float64, device="cuda")
         d_prev = torch.tensor(m_prev, dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         out = C.c_double(-1.0)
         rc = L.nmg_max_dm_static(C.c_void_p(d_now.data_ptr()), C.c_void_p(d_prev.data_ptr()), n, C.byref(out))
         assert rc == 0, L.nmg_last_error(None)
+        if call > 0:
+            # the first call sets the device up (symbol lookup, module load);
+            # after that a call leaves the device's free memory as it found it
+            assert torch.cuda.mem_get_info()[0] == free_before
         assert out.value == pytest.approx(expected, rel=1e-15, abs=0.0)
         assert out.value == pytest.approx(np.sqrt(((m_now - m_prev) ** 2).sum(1)).max(), rel=1e-15)
 
