@@ -83,6 +83,52 @@ def build(force=False):
         subprocess.check_call(["make", "-s", "-C", HERE])
 
 
+REF_SRC = os.environ.get("NMAG_REFERENCE_SRC", "/root/reference/src")
+REF_LIB = os.path.join(HERE, "_ref", "libref_bem.so")
+_ref = None
+
+
+def build_ref():
+    """Compile the reference's own Lindholm stub (REF_SRC/bem3d_stubs.c,
+    unmodified) with the harness into _ref/ when the reference tree is
+    present; return whether the library exists afterwards."""
+    if os.path.exists(os.path.join(REF_SRC, "bem3d_stubs.c")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF_SRC=" + REF_SRC])
+    return os.path.exists(REF_LIB)
+
+
+def ref_lib():
+    """The reference-built BEM library, or None when it was not built (the
+    reference tree is absent, e.g. where only the committed fixtures exist)."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_LIB):
+            return None
+        L = C.CDLL(REF_LIB)
+        L.ref_fill_bem.argtypes = [C.c_int, _f64p, C.c_int, _i32p, _f64p, _f64p, _f64p]
+        L.ref_fill_bem.restype = C.c_int
+        _ref = L
+    return _ref
+
+
+def ref_bem(omesh):
+    """The BEM matrix of an OracleMesh as the reference's own stub fills it
+    (bem3d.ml:938-1047 around bem3d_stubs.c:413-610), from the oracle's
+    boundary numbering, surface triangles, normals and solid angles."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("reference BEM library not built (oracle/_ref)")
+    nb = omesh.nb
+    obs = np.ascontiguousarray(omesh.points[omesh.node_of_b], dtype=np.float64)
+    out = np.zeros((nb, nb))
+    rc = L.ref_fill_bem(nb, obs.reshape(-1), omesh.ntri, np.ascontiguousarray(omesh.tri, np.int32).reshape(-1),
+                        np.ascontiguousarray(omesh.tri_normal).reshape(-1), np.ascontiguousarray(omesh.solid_angle),
+                        out.reshape(-1))
+    if rc != 0:
+        raise MemoryError("ref_fill_bem failed")
+    return out
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -154,6 +200,7 @@ class OracleMesh(object):
         m = self._m
         N, T, nnz, nb = m.n_nodes, m.n_tets, m.nnz, m.nb
         self.n_nodes, self.n_tets, self.nnz, self.nb, self.ntri = N, T, nnz, nb, m.ntri
+        self.points = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
         self.row_ptr = _arr(m.row_ptr, N + 1, np.int32)
         self.col_idx = _arr(m.col_idx, nnz, np.int32)
         self.K = _arr(m.K, nnz, np.float64)
