@@ -196,9 +196,12 @@ def barrier(world):
 
 
 def cpu_reference_run(args, msh, base, seed, steps, warmup, max_wall=25.0, sample_ps=None):
-    """Time the oracle (CPU restatement, all host threads) on the workload:
-    the same relax stage (alpha = 1, no field, RELAX_PS), then the timed
-    alpha = 0.02 dynamics under H_ext."""
+    """Time the oracle (CPU restatement, all host threads) on a bounded
+    sample of the workload: the seeded state relaxed at alpha = 1 without
+    field for args.relax_ps (the full relaxation to 1 deg/ns would take the
+    CPU longer than the whole run may), then alpha = 0.02 under H_ext,
+    `warmup` untimed records and up to `steps` timed records of sample_ps
+    (default: record_ps), stopping early after max_wall seconds."""
     import oracle
     t0 = time.perf_counter()
     om = oracle.OracleMesh(msh.points, msh.simplices, nthreads=0)
@@ -213,7 +216,7 @@ def cpu_reference_run(args, msh, base, seed, steps, warmup, max_wall=25.0, sampl
     s.ts_init(m, rtol=1e-6, atol=1e-6)
     setup = time.perf_counter() - t0
     t = 0.0
-    dt = sample_ps or args.step_ps
+    dt = sample_ps or args.record_ps
     for _ in range(warmup):
         t += dt
         s.ts_advance(t)
@@ -231,7 +234,7 @@ def cpu_reference_run(args, msh, base, seed, steps, warmup, max_wall=25.0, sampl
             break
     st = s.ts_stats()
     return {"sim_ps": done, "wall_s": wall, "steps": n, "nfe": st["nfe"] - nfe0, "setup_s": setup,
-            "cores": os.cpu_count()}
+            "cores": os.cpu_count(), "dt": dt}
 
 
 def run_reference(args):
@@ -249,8 +252,9 @@ def run_reference(args):
         "config": config_dict(args, msh),
         "rhs_evals_per_s": r["nfe"] / r["wall_s"],
         "cpu_baseline": {"value": value, "unit": "ns/s", "cores": r["cores"], "kind": "port",
-                         "sample": "%d x %.2f ps of the workload on the CPU restatement (oracle/, OpenMP)"
-                                   % (r["steps"], args.step_ps)},
+                         "sample": "%d x %.2f ps records of the workload's dynamics on the CPU restatement "
+                                   "(oracle/, OpenMP), after a %g ps relax at alpha=1 (the relax to 1 deg/ns "
+                                   "is beyond a bounded CPU run)" % (r["steps"], r["dt"], args.relax_ps)},
         "e2e": {"value": value, "unit": "ns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's own build (OCaml/Python 2/PETSc/SUNDIALS) cannot run here; this arm times "
                 "the CPU restatement of its algorithms (FP64).  An ensemble's members would run one after "
@@ -268,8 +272,12 @@ WORKLOAD_NAMES = {
 
 def config_dict(args, msh):
     return {"workload": WORKLOAD_NAMES[args.workload],
-            "relax": "alpha=1, H_ext=0 for %.3g ps before the timed dynamics (untimed)" % args.relax_ps,
-            "nodes": int(msh.n_nodes), "tets": int(msh.n_tets), "step": "%.3g ps advance + <m> read" % args.step_ps,
+            "relax": ("alpha=1, H_ext=0, nmag relax() until max |dm/dt| < 1 deg/ns twice in a row (checked every "
+                      "5 BDF steps; capped at %g ps), untimed; the timed dynamics start from the relaxed state"
+                      % args.relax_cap_ps),
+            "nodes": int(msh.n_nodes), "tets": int(msh.n_tets),
+            "step": "%g ps advance in %g ps records, each followed by an <m> read" % (args.step_ps, args.record_ps),
+            "interval_ps": args.steps * args.step_ps,
             "form": args.form, "cg": args.cg, "members": args.members,
             "bem_anchor": args.anchor if args.form == "fp32x2" else 0.0,
             "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
@@ -277,10 +285,49 @@ def config_dict(args, msh):
                                                                                   "fp32x2": 6}[args.form]}
 
 
-def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True, anchor=0.0):
-    """One form on the workload: untimed setup and relax, W warm-up steps,
-    then K timed steps on the device-resident engine (CUDA-event time on the
-    library's stream) and K more through nmag.Simulation (e2e)."""
+def relax_states(args, form, cg, B, msh, base, seed, anchor):
+    """The workload's relaxation, untimed: each member's seeded initial state
+    relaxed at alpha = 1 without field by nmag's own relax() -- integrate,
+    check max |dm/dt| every 5 steps, stop once it is below 1 deg/ns twice in
+    a row (convergence.py:54-100, hysteresis.py:207-242) -- capped at
+    args.relax_cap_ps of simulated time.  Returns the relaxed states and a
+    record of the relaxation."""
+    import nmag
+    from nmag import SI, every
+    sim = nmag.Simulation("relax", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor,
+                          anchor_product=args.anchor_product)
+    sim.load_mesh(msh, [("film", material(1.0))], unit_length=SI(1e-9, "m"))
+    if B > 1:   # member b starts from the workload's initial state with seed + b
+        sim.set_m(np.stack([initial_m(msh.n_nodes, base, seed + b) for b in range(B)]))
+    else:
+        sim.set_m(initial_m(msh.n_nodes, base, seed))
+    cap = args.relax_cap_ps
+
+    def stop_at_cap(s):
+        if s.clock.stage_time_su >= cap:
+            s.hysteresis_exit(s)
+
+    w = time.perf_counter()
+    sim.relax(save=(), do=((stop_at_cap, every("step", 5)),))
+    wall = time.perf_counter() - w
+    rec = {"sim_ps": float(sim.clock.stage_time_su), "wall_s": wall, "bdf_steps": int(sim.clock.stage_step),
+           "converged": bool(sim.clock.convergence), "final_max_dm_dt_deg_per_ns": float(sim.max_dm_dt) / 1.7453292519943296e-05,
+           "form": form if B > 1 or form != "fp64" else "fp64", "members": B}
+    m = sim.engine.get_m()
+    sim.engine.close()
+    return m, rec
+
+
+def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anchor=0.0, warmup=None,
+            e2e=True):
+    """One form on the workload from the relaxed states `start`: alpha =
+    0.02 and the applied field; W untimed warm-up steps, then the state is
+    put back and K timed steps run on the device-resident engine (value:
+    CUDA-event time of the advances on the library's stream), then the state
+    is put back again and the same K steps run through nmag.Simulation (e2e:
+    advance_time, which copies m to the host, and <m> read on the host).  A
+    step advances step_ps in records of record_ps, each followed by an <m>
+    read, so K steps from t = 0 cover exactly the configured interval."""
     import torch
     import nmag
     from nmag import SI
@@ -288,26 +335,23 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
                           anchor_product=args.anchor_product)
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
-    if B > 1:   # member b starts from the workload's initial state with seed + b
-        sim.set_m(np.stack([initial_m(msh.n_nodes, base, seed + b) for b in range(B)]))
-    else:
-        sim.set_m(initial_m(msh.n_nodes, base, seed))
-    relax_wall = 0.0
-    if args.relax_ps > 0:   # relax stage: alpha = 1, no applied field
-        w = time.perf_counter()
-        sim.set_damping(1.0)
-        sim.reinitialise(initial_time=0)
-        sim.advance_time(SI(args.relax_ps * 1e-12, "s"))
-        sim.set_damping(0.02)
-        relax_wall = time.perf_counter() - w
     sim.set_H_ext(h_ext_su() * 1e6, SI(1.0, "A/m"))
-    sim.reinitialise(initial_time=0)
-    ps = args.step_ps
+    rec = args.record_ps
+    per_step = int(round(args.step_ps / rec))
+    warmup = args.warmup if warmup is None else warmup
+
+    def restart():
+        sim.set_m(start)
+        sim.reinitialise(initial_time=0)
+
+    restart()
     t = 0.0
-    for _ in range(args.warmup):
-        t += ps
+    for _ in range(warmup * per_step):
+        t += rec
         eng.ts_advance(t)
-    m_start = eng.get_m()
+        eng.averages()
+    restart()
+    t = 0.0
     # ---- timed region: device-resident value leg ----
     sampler = ClockSampler(local) if sample_clocks else None
     if sampler:
@@ -321,12 +365,14 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
     barrier(world)
     torch.cuda.synchronize()
     dev_ms = 0.0
+    trace = []
     w0 = time.perf_counter()
     for _ in range(args.steps):
-        t += ps
-        _, st = eng.ts_advance(t)
-        dev_ms += float(eng.timings()[0])
-        eng.averages()
+        for _ in range(per_step):
+            t += rec
+            _, st = eng.ts_advance(t)
+            dev_ms += float(eng.timings()[0])
+            trace.append(eng.averages())
     torch.cuda.synchronize()
     wall_value = time.perf_counter() - w0
     barrier(world)
@@ -336,21 +382,24 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
     eng.profile(False)
     prof = eng.profile_read()
     clocks = sampler.stop() if sampler else None
-    # ---- e2e leg through the public API (advance_time copies m to the host) ----
-    sim.clock.stage_time_su = t
-    sim._last_nst = st["nst"]
-    torch.cuda.synchronize()
-    barrier(world)
-    w1 = time.perf_counter()
-    for _ in range(args.steps):
-        t += ps
-        sim.advance_time(SI(t * 1e-12, "s"))
-        sim.get_subfield_average_siv("m")
-    torch.cuda.synchronize()
-    wall_e2e = time.perf_counter() - w1
+    m_final = eng.get_m()
+    # ---- e2e leg through the public API, over the same interval from the same state ----
+    wall_e2e = None
+    if e2e:
+        restart()
+        torch.cuda.synchronize()
+        barrier(world)
+        w1 = time.perf_counter()
+        t = 0.0
+        for _ in range(args.steps):
+            for _ in range(per_step):
+                t += rec
+                sim.advance_time(SI(t * 1e-12, "s"))
+                sim.get_subfield_average_siv("m")
+        torch.cuda.synchronize()
+        wall_e2e = max_over_ranks(time.perf_counter() - w1, world)
     dev_s = max_over_ranks(dev_ms * 1e-3, world)
-    wall_e2e = max_over_ranks(wall_e2e, world)
-    sim_ns_total = world * B * args.steps * ps * 1e-3   # summed over ensemble members
+    sim_ns_total = world * B * args.steps * args.step_ps * 1e-3   # summed over ensemble members
     nb = eng.nb
     elem = {"fp64": 8, "fp32": 4, "fp32x2": 6}[form]
     nm = min(B, 8)   # members per BEM launch
@@ -415,14 +464,16 @@ def measure(args, form, cg, B, msh, base, seed, world, local, sample_clocks=True
                     "share_of_step": dom["total_ms"] / max(dev_ms, 1e-9),
                     "note": "anchored product: the dominant of its two kernels; both in 'anchored'"}
     return {
-        "sim": sim, "eng": eng, "value": sim_ns_total / dev_s, "e2e": sim_ns_total / wall_e2e,
+        "sim": sim, "eng": eng, "value": sim_ns_total / dev_s,
+        "e2e": sim_ns_total / wall_e2e if wall_e2e else None,
         "ms_per_step": dev_s * 1e3 / args.steps, "rhs_evals": st["nfe"] - st0["nfe"],
         "bdf_steps": st["nst"] - st0["nst"], "rhs_evals_per_s": (st["nfe"] - st0["nfe"]) / dev_s * world,
         "wall_value_s": wall_value, "roofline": roof, "launches": launches, "clocks": clocks,
         "kernels_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
         "cg_iterations": {"neumann": cg1[0] - cg0[0], "dirichlet": cg1[1] - cg0[1]},
-        "relax_wall_s": relax_wall, "d2h": B * msh.n_nodes * 3 * 8 + 24,
-        "anchored": anchored, "m_start": m_start,
+        # per step: B members' m copied to the host (advance_time) + <m> (24 B) per record
+        "d2h": per_step * (B * msh.n_nodes * 3 * 8 + 24),
+        "anchored": anchored, "m_start": start, "m_final": m_final, "trace": np.asarray(trace),
     }
 
 
@@ -464,7 +515,7 @@ def anchor_path_error(args, chosen, msh, points=48):
     from nmag import SI
     B = args.members
     ma = np.asarray(chosen["m_start"]).reshape(B, -1, 3) if B > 1 else np.asarray(chosen["m_start"])[None]
-    mb = np.asarray(chosen["eng"].get_m()).reshape(B, -1, 3) if B > 1 else np.asarray(chosen["eng"].get_m())[None]
+    mb = np.asarray(chosen["m_final"]).reshape(B, -1, 3) if B > 1 else np.asarray(chosen["m_final"])[None]
     tight = {"NBC.rtol": 1e-12, "DBC.rtol": 1e-12, "NBC.maxits": 20000, "DBC.maxits": 20000}
     sims = {}
     for key, form, anc in (("anchored", args.form, args.anchor), ("fp64", "fp64", 0.0)):
@@ -775,10 +826,15 @@ def run_ours(args):
     msh, base, seed = workload(args.workload)
     B = args.members
     anchor = args.anchor if args.form == "fp32x2" else 0.0
-    r = measure(args, args.form, args.cg, B, msh, base, seed, world, local, anchor=anchor)
+    # one relaxation for both forms (untimed setup): the ensemble's members
+    # from seeds seed..seed+B-1; the plain film starts from member 0's state
+    start, relax_rec = relax_states(args, args.form, args.cg, B, msh, base, seed, anchor)
+    r = measure(args, args.form, args.cg, B, msh, start, world, local, anchor=anchor)
     plain = None
     if args.compare and not (args.form == "fp64" and args.cg == "fp64" and B == 1):
-        plain = measure(args, "fp64", "fp64", 1, msh, base, seed, world, local, sample_clocks=False)
+        start0 = start[0] if B > 1 else start
+        plain = measure(args, "fp64", "fp64", 1, msh, start0, world, local, sample_clocks=False,
+                        warmup=1, e2e=False)
     if rank != 0:
         return
     line = {
@@ -795,9 +851,12 @@ def run_ours(args):
         "roofline": r["roofline"],
         "kernels_ms": r["kernels_ms"],
         "cg_iterations": r["cg_iterations"],
-        "relax_wall_s": r["relax_wall_s"],
+        "relax": relax_rec,
+        "per_member_value": r["value"] / B,
         "e2e": {"value": r["e2e"], "unit": "ns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": r["d2h"],
-                "call": "nmag.Simulation.advance_time + get_subfield_average_siv('m')"},
+                "call": "nmag.Simulation.advance_time + get_subfield_average_siv('m'), same interval and start "
+                        "state as value"},
+        "avg_m_final": [float(v) for v in r["trace"][-1]],
         "gpu_launches": r["launches"],
         "clocks": r["clocks"],
     }
@@ -810,36 +869,47 @@ def run_ours(args):
                               "gpu_launches": plain["launches"]}
         line["speedup_vs_plain_fp64"] = r["value"] / plain["value"]
         line["heff_rel_err_vs_fp64"] = heff_error(args, r, msh)
-        # member 0 starts from the plain run's state and both advanced the same time
-        a0 = np.asarray(r["eng"].member_averages(0) if B > 1 else r["eng"].averages())
-        line["avg_m_diff_vs_plain_fp64"] = float(np.abs(a0 - np.asarray(plain["eng"].averages())).max())
+        # member 0 starts from the plain run's state: <m> at every record of the interval
+        line["avg_m_diff_vs_plain_fp64"] = float(np.abs(r["trace"] - plain["trace"]).max())
     if anchor > 0:
         err, prod, nref = anchor_path_error(args, r, msh)
         line["anchored"]["path_error"] = {"heff_rel_err_vs_fp64": err, "products": prod, "refreshes": nref,
                                           "blends": 49}
         line["heff_rel_err_vs_fp64"] = max(line.get("heff_rel_err_vs_fp64", 0.0), err)
     if world == 1 and not args.no_cpu_baseline:
-        cr = cpu_reference_run(args, msh, base, seed, steps=2, warmup=0, max_wall=20.0, sample_ps=0.5 * args.step_ps)
-        line["cpu_baseline"] = {"value": (cr["sim_ps"] * 1e-3) / cr["wall_s"], "unit": "ns/s", "cores": cr["cores"],
+        cr = cpu_reference_run(args, msh, base, seed, steps=args.cpu_records, warmup=0, max_wall=20.0)
+        cpu_value = (cr["sim_ps"] * 1e-3) / cr["wall_s"]
+        line["cpu_baseline"] = {"value": cpu_value, "unit": "ns/s", "cores": cr["cores"],
                                 "kind": "port",
-                                "sample": "%d x %.2f ps of one film from the seeded initial state on the CPU "
-                                          "restatement" % (cr["steps"], 0.5 * args.step_ps),
+                                "sample": "%d x %.2f ps records of one film's dynamics on the CPU restatement, "
+                                          "after a %g ps relax at alpha=1" % (cr["steps"], cr["dt"], args.relax_ps),
                                 "rhs_evals_per_s": cr["nfe"] / cr["wall_s"]}
+        if plain is not None:
+            line["plain_fp64"]["vs_cpu_baseline"] = plain["value"] / cpu_value
+            line["plain_fp64"]["rhs_evals_per_s_vs_cpu_baseline"] = (plain["rhs_evals_per_s"]
+                                                                     / line["cpu_baseline"]["rhs_evals_per_s"])
     print(json.dumps(line))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="fp32x2", choices=["fp64", "fp32", "fp32x2"],
                     help="BEM product: fp64; fp32 (FP32 entries, FP64 sums); fp32x2 (FP32 + BF16 residual "
                          "entries, compensated FP32 products)")
     ap.add_argument("--workload", default="film", choices=["film", "cube", "film_small"])
-    ap.add_argument("--step-ps", type=float, default=1.0)
-    ap.add_argument("--relax-ps", type=float, default=10.0)
+    ap.add_argument("--step-ps", type=float, default=50.0,
+                    help="simulated time per step (20 steps: the configured 1 ns)")
+    ap.add_argument("--record-ps", type=float, default=1.0, help="<m> is read every record_ps")
+    ap.add_argument("--relax-cap-ps", type=float, default=5000.0,
+                    help="cap of the simulated time of the (untimed) relaxation to 1 deg/ns")
+    ap.add_argument("--relax-ps", type=float, default=10.0,
+                    help="the CPU arms' truncated relax at alpha=1 before their sampled records")
+    ap.add_argument("--cpu-records", type=int, default=20,
+                    help="records of the CPU baseline sample in our line (bounded by 20 s of CPU work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cg", default="fp32", choices=["fp64", "fp32"],
                     help="Poisson CG: FP64, or FP32 iterations with FP64 residual refinement")

@@ -1,0 +1,191 @@
+"""Trajectory parity: m(t) of the device integrator against the oracle's.
+
+The metric's bound is m(t) within 1e-4 of the reference trajectory.  Both
+sides run the same BDF family (orders 1-2, Newton, left-preconditioned
+GMRES, rtol = atol = 1e-6 as the configurations ask), each with its own step
+control, so their step sequences differ and m(t) agrees to the integrators'
+global error, not to rounding.
+
+The Poisson solves are fixed at a tight tolerance on both sides.  The
+configurations leave them at the reference's default (PETSc rtol 1e-5), under
+which the two solvers' different stopping points alone move the cube's m(t)
+by up to 1.3e-4 over 1 ns (oracle against oracle, rtol 1e-5 against 1e-10),
+so a loose tolerance would measure the solvers' stopping points rather than
+the integrators.
+
+* Cube (30 nm, 1331 nodes), alpha 0.5, no field, m0 = normalise((1,1,1) +
+  0.01 N(0,1)), seed 0: 1 ns with m(t) and the energies every 10 ps.
+* Film (500 x 125 x 3 nm, 30,753 nodes) at the film workload's parameters:
+  each member's seeded state (seeds 1..8) is first damped on the device for
+  10 ps at alpha 1 without field (a short stand-in for the relaxation, which
+  removes the seeded noise's spin waves), then alpha 0.02 and
+  mu0 H = (-24.6, 4.3, 0) mT.  From those states the plain FP64 path and the
+  chosen form (8 members in one ensemble: compensated BEM product anchored
+  at 3e-3 with FP32 difference products, FP32 CG with FP64 refinement) run
+  50 ps with m(t) and <m>(t) every 1 ps and the energies every 10 ps, each
+  member against an oracle run from its own state: member 0 over the 50 ps,
+  members 1-7 over their first 10 ps.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import permalloy, seeded_m
+from test_gpu_parity import make_engine
+
+pytestmark = pytest.mark.gpu
+
+M_TOL = 1e-4          # the metric's bound on m(t)
+E_TOL = 1e-4          # energies, relative to the largest |E| of the run
+MU0 = 4e-7 * np.pi
+# mu0 H = (-24.6, 4.3, 0) mT as a field in simulation units (1e-3 A / 1e-9 m)
+H_FILM = np.array([-24.6, 4.3, 0.0]) * 1e-3 / MU0 * 1e-6
+
+
+def _material(mat):
+    from nmag import _lib
+    c = mat.coefficients("nmag")
+    mt = _lib.Material()
+    mt.Ms, mt.exch_coeff, mt.C1, mt.C2, mt.C3 = c["Ms"], c["exch_coeff"], c["C1"], c["C2"], c["C3"]
+    mt.K1, mt.anis_coeff, mt.E_coeff_half, mt.E_coeff_ext = c["K1"], c["anis_coeff"], c["E_coeff_half"], c["E_coeff_ext"]
+    for d in range(3):
+        mt.axis[d] = c["axis"][d]
+    return mt
+
+
+def _oracle_run(om, mat, m0, h, times, tol, energy_every=None):
+    """m(t) (and energy totals) of the oracle's BDF at the given times."""
+    s = oracle.OracleSim(om, mat.coefficients("nmag"), nbc=(tol, 1e-50, 50000), dbc=(tol, 1e-50, 50000))
+    s.set_h_ext(h)
+    s.ts_init(m0, rtol=1e-6, atol=1e-6, max_order=2, krylov_max=300)
+    ms, es = [], {}
+    for k, t in enumerate(times):
+        _, m = s.ts_advance(t)
+        ms.append(m.reshape(-1, 3).copy())
+        if energy_every and (k + 1) % energy_every == 0:
+            es[k] = s.energy_density(m) @ om.vol
+    return np.array(ms), es, s.ts_stats()
+
+
+def _avg(m, vol):
+    return (m * vol[:, None]).sum(0) / vol.sum()
+
+
+def test_cube_trajectory_1ns_matches_oracle(cube):
+    mat = permalloy(0.5)
+    eng = make_engine(cube, mat, tol=1e-10)
+    om = oracle.OracleMesh(cube.points, cube.simplices)
+    m0 = seeded_m(om.n_nodes, seed=0)
+    times = [10.0 * k for k in range(1, 101)]
+    mo, eo, so = _oracle_run(om, mat, m0, np.zeros(3), times, 1e-10, energy_every=1)
+    eng.set_h_ext(np.zeros(3))
+    eng.set_m(m0)
+    eng.ts_init(0.0, 1e-6, 1e-6, 2, 300)
+    dm, de = [], []
+    emax = max(np.abs(e).max() for e in eo.values())
+    for k, t in enumerate(times):
+        tr, st = eng.ts_advance(t)
+        assert abs(tr - t) < 1e-9
+        mg = eng.get_m()
+        dm.append(np.abs(mg - mo[k]).max())
+        _, e = eng.averages(energies=True)
+        de.append(np.abs(e - eo[k]).max() / emax)
+    print("cube 1 ns: max |dm| %.2e, max energy diff %.2e of max |E|, BDF steps %d (oracle %d)"
+          % (max(dm), max(de), st["nst"], so["nst"]))
+    assert max(dm) <= M_TOL, (max(dm), int(np.argmax(dm)))
+    assert max(de) <= E_TOL, max(de)
+    # the state has moved well beyond the tolerance (the comparison is not vacuous)
+    assert np.abs(mo[-1] - m0).max() > 100 * M_TOL
+    eng.close()
+
+
+@pytest.fixture(scope="module")
+def film_setup():
+    from nmag import mesh
+    from test_gpu_ensemble import make_ensemble
+    film = mesh.film_mesh()
+    N = len(film.points)
+    B = 8
+    seeds = [seeded_m(N, base=(1.0, 0.25, 0.1), seed=1 + b) for b in range(B)]
+    ens, single = make_ensemble(film, permalloy(1.0), B, tol=1e-8, bem_precision=2, cg_precision=1, anchor=3e-3)
+    single.close()
+    ens.set_h_ext(np.zeros(3))
+    ens.set_m(np.stack(seeds))
+    ens.ts_init(0.0, 1e-6, 1e-6, 2, 300)
+    ens.ts_advance(10.0)
+    starts = ens.get_m()
+    ens.set_material(_material(permalloy(0.02)))
+    ens.set_h_ext(H_FILM)
+    om = oracle.OracleMesh(film.points, film.simplices)
+    cache = {}
+
+    def oracle_member(b, n_ps):
+        key = (b, n_ps)
+        if key not in cache:
+            times = [float(k) for k in range(1, n_ps + 1)]
+            cache[key] = _oracle_run(om, permalloy(0.02), starts[b], H_FILM, times, 1e-8, energy_every=10)
+        return cache[key]
+
+    yield {"film": film, "om": om, "ens": ens, "starts": starts, "oracle": oracle_member}
+    ens.close()
+
+
+def _compare(label, get_m, get_avg_e, ref, vol, n_ps, energies=True):
+    mo, eo, so = ref
+    dm, da, de = [], [], []
+    emax = max(np.abs(e).max() for e in eo.values()) if eo else 1.0
+    for k in range(n_ps):
+        mg = get_m(k)
+        dm.append(np.abs(mg - mo[k]).max())
+        da.append(np.abs(_avg(mg, vol) - _avg(mo[k], vol)).max())
+        if energies and k in eo:
+            de.append(np.abs(get_avg_e() - eo[k]).max() / emax)
+    print("%s: %d ps, max |dm| %.2e, max |d<m>| %.2e, max energy diff %.2e of max |E| (oracle %d BDF steps)"
+          % (label, n_ps, max(dm), max(da), max(de) if de else 0.0, so["nst"]))
+    assert max(dm) <= M_TOL, (label, max(dm), int(np.argmax(dm)))
+    if de:
+        assert max(de) <= E_TOL, (label, max(de))
+    return max(dm)
+
+
+def test_film_plain_fp64_trajectory_matches_oracle(film_setup):
+    S = film_setup
+    eng = make_engine(S["film"], permalloy(0.02), tol=1e-8)
+    eng.set_h_ext(H_FILM)
+    eng.set_m(S["starts"][0])
+    eng.ts_init(0.0, 1e-6, 1e-6, 2, 300)
+
+    def get_m(k):
+        eng.ts_advance(float(k + 1))
+        return eng.get_m()
+
+    def get_e():
+        return eng.averages(energies=True)[1]
+
+    _compare("film plain FP64", get_m, get_e, S["oracle"](0, 50), S["om"].vol, 50)
+    eng.close()
+
+
+def test_film_chosen_form_members_match_oracle(film_setup):
+    S = film_setup
+    ens = S["ens"]
+    ens.set_m(S["starts"])
+    ens.ts_init(0.0, 1e-6, 1e-6, 2, 300)
+    hist, ehist = [], {}
+    for k in range(50):
+        ens.ts_advance(float(k + 1))
+        hist.append(ens.get_m())
+        if (k + 1) % 10 == 0:
+            ehist[k] = [ens.member_averages(b, energies=True)[1] for b in range(8)]
+    for b in range(8):
+        n_ps = 50 if b == 0 else 10
+        ref = S["oracle"](b, n_ps)
+        _compare("film chosen form, member %d" % b, lambda k, b=b: hist[k][b],
+                 None, ref, S["om"].vol, n_ps, energies=False)
+        mo, eo, _ = ref
+        emax = max(np.abs(e).max() for e in eo.values())
+        for k, e in eo.items():
+            assert np.abs(ehist[k][b] - e).max() / emax <= E_TOL, (b, k)
+    # the anchored product was in use along the run (not every product a refresh)
+    prods, refreshes = ens.bem_anchor_stats()
+    assert refreshes < prods
