@@ -115,6 +115,15 @@ def h_ext_su():
     return np.array([v * 1e-3 / MU0 for v in H_EXT_MT]) / 1e6
 
 
+def peaks_tensor():
+    """Dense bf16 tensor peak (TFLOP/s): the measured burst figure, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -282,7 +291,7 @@ def config_dict(args, msh):
             "bem_anchor": args.anchor if args.form == "fp32x2" else 0.0,
             "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
             "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % {"fp64": 8, "fp32": 4,
-                                                                                  "fp32x2": 6}[args.form]}
+                                                                                  "fp32x2": 6, "bf16x3": 6}[args.form]}
 
 
 def relax_states(args, form, cg, B, msh, base, seed, anchor):
@@ -401,7 +410,7 @@ def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anc
     dev_s = max_over_ranks(dev_ms * 1e-3, world)
     sim_ns_total = world * B * args.steps * args.step_ps * 1e-3   # summed over ensemble members
     nb = eng.nb
-    elem = {"fp64": 8, "fp32": 4, "fp32x2": 6}[form]
+    elem = {"fp64": 8, "fp32": 4, "fp32x2": 6, "bf16x3": 6}[form]
     nm = min(B, 8)   # members per BEM launch
     gl, gms = prof["bem_gemv"]
     bytes_per_launch = nb * nb * elem + 2 * nm * nb * 8
@@ -547,21 +556,25 @@ def run_precision_report(args):
     """Precision form against FP64 on the film for N seeded random fields
     (m = normalise(N(0,1)) per node, numpy default_rng(seed), seeds 100..):
     H_eff (max-norm relative) and total / demag energy relative errors.  Both
-    sides are 8-member ensembles with Poisson solves converged to 1e-12; the
-    FP64 side is the plain form's arithmetic."""
+    sides are ensembles (--precision-members fields each; every field of an
+    ensemble goes through one BEM product) with Poisson solves converged to
+    1e-12; the FP64 side is the plain form's arithmetic.  For the tensor-core
+    form (bf16x3) the BEM products are timed with CUDA events and reported
+    against the measured bf16 tensor peak."""
     import torch
     import nmag
     from nmag import SI
     torch.cuda.set_device(0)
     msh, _, _ = workload(args.workload)
     tight = {"NBC.rtol": 1e-12, "DBC.rtol": 1e-12, "NBC.maxits": 20000, "DBC.maxits": 20000}
-    B = 8
+    B = args.precision_members or (128 if args.form == "bf16x3" else 8)
     sims = {}
     for form in (args.form, "fp64"):
         sim = nmag.Simulation("err", bem_precision=form, ksp_tolerances=tight, n_members=B)
         sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
         sim.engine.set_h_ext(np.broadcast_to(h_ext_su(), (B, sim.engine.N, 3)))
         sims[form] = sim.engine
+    sims[args.form].profile(True)
     N = msh.n_nodes
     herr, eerr, derr = [], [], []
     t0 = time.perf_counter()
@@ -586,13 +599,90 @@ def run_precision_report(args):
             eerr.append(float(abs(e32[4] - e64[4]) / abs(e64[4])))
             derr.append(float(abs(e32[1] - e64[1]) / abs(e64[1])))
     wall = time.perf_counter() - t0
+    eng = sims[args.form]
+    eng.profile(False)
+    launches, ms_tot = eng.profile_read()["bem_gemv"]
     line = {"metric": "precision form error vs FP64", "report": "precision", "fields": len(herr),
             "seeds": [100, 100 + len(herr) - 1], "workload": WORKLOAD_NAMES[args.workload],
-            "form": args.form, "bound": 1e-5,
+            "form": args.form, "members_per_product": B, "bound": 1e-5,
             "heff_rel_err": {"max": max(herr), "median": float(np.median(herr)), "p99": float(np.percentile(herr, 99))},
             "energy_total_rel_err": {"max": max(eerr), "median": float(np.median(eerr))},
             "energy_demag_rel_err": {"max": max(derr), "median": float(np.median(derr))},
             "within_bound": bool(max(herr) <= 1e-5), "wall_s": wall}
+    if launches:
+        nb = eng.nb
+        avg_ms = ms_tot / launches
+        line["bem_product"] = {"kernel": {"bf16x3": "k_bem_tc", "fp32x2": "k_gemm_df", "fp32": "k_gemm_f32r",
+                                          "fp64": "k_gemm_f64"}[args.form],
+                               "launches": launches, "avg_launch_ms": avg_ms,
+                               "right_hand_sides_per_launch": B,
+                               "fields_per_s": B / (avg_ms * 1e-3)}
+        if args.form == "bf16x3":
+            flop = 6 * 2.0 * nb * nb * B   # six BF16 products per term on the tensor pipe
+            peak = peaks_tensor()
+            line["bem_product"]["roofline"] = {
+                "bound": "tensor", "achieved": flop / (avg_ms * 1e-3) / 1e12, "peak": peak[0], "unit": "TFLOP/s",
+                "frac": flop / (avg_ms * 1e-3) / 1e12 / peak[0], "peak_kind": peak[1],
+                "flop_per_launch": flop, "algorithmic_flop_per_launch": 2.0 * nb * nb * B,
+                "note": "tensor FLOPs = 6 split products x 2 nb^2 R; the product itself is 2 nb^2 R"}
+    print(json.dumps(line))
+
+
+def run_bem_report(args):
+    """The BEM product alone: y_n = B x_n for --rhs right-hand sides (smooth
+    boundary potentials of different wavelengths) in the chosen form, W
+    warm-up products, then K timed products (CUDA events around the product
+    kernel on the library's stream); error against the FP64 product of the
+    same vectors; tensor-pipe (bf16x3) or HBM fraction of the measured peaks."""
+    import torch
+    import nmag
+    from nmag import SI
+    torch.cuda.set_device(0)
+    msh, _, _ = workload(args.workload)
+    engines = {}
+    for form in dict.fromkeys((args.form, "fp64")):
+        sim = nmag.Simulation("bem", bem_precision=form)
+        sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
+        engines[form] = sim.engine
+    eng = engines[args.form]
+    nb, R = eng.nb, args.rhs
+    k = np.arange(nb)
+    X = np.stack([100.0 * np.sin(k * w + ph) for ph, w in enumerate(np.geomspace(1e-4, 3e-1, R))])
+    dx = torch.tensor(X, dtype=torch.float64, device="cuda")
+    dy = torch.empty_like(dx)
+    dr = torch.empty_like(dx)
+    engines["fp64"].bem_apply_device(dx.data_ptr(), dr.data_ptr(), R)
+    for _ in range(args.warmup):
+        eng.bem_apply_device(dx.data_ptr(), dy.data_ptr(), R)
+    torch.cuda.synchronize()
+    eng.profile(True)
+    w = time.perf_counter()
+    for _ in range(args.steps):
+        eng.bem_apply_device(dx.data_ptr(), dy.data_ptr(), R)
+    wall = time.perf_counter() - w
+    eng.profile(False)
+    launches, ms_tot = eng.profile_read()["bem_gemv"]
+    err = float((dy - dr).abs().max() / dr.abs().max())
+    avg_ms = ms_tot / max(launches, 1)
+    line = {"metric": "BEM product", "report": "bem", "workload": WORKLOAD_NAMES[args.workload], "nb": nb,
+            "form": args.form, "right_hand_sides": R, "steps": args.steps, "warmup": args.warmup,
+            "profiled_launches": launches, "avg_launch_ms": avg_ms, "wall_ms_per_product": 1e3 * wall / args.steps,
+            "rel_err_vs_fp64": err}
+    if args.form == "bf16x3":
+        flop = 6 * 2.0 * nb * nb * R
+        peak, kind = peaks_tensor()
+        line["roofline"] = {"bound": "tensor", "achieved": flop / (avg_ms * 1e-3) / 1e12, "peak": peak,
+                            "unit": "TFLOP/s", "frac": flop / (avg_ms * 1e-3) / 1e12 / peak, "peak_kind": kind,
+                            "flop_per_launch": flop,
+                            "bytes_per_launch": 3 * 2.0 * nb * nb + 3 * 2.0 * nb * R,
+                            "note": "six BF16 tensor products per term (tensor FLOPs = 6 x 2 nb^2 R)"}
+    else:
+        elem = {"fp64": 8, "fp32": 4, "fp32x2": 6}[args.form]
+        hbm, kind = peaks()
+        nbytes = elem * nb * nb * R + 16 * nb * R
+        line["roofline"] = {"bound": "hbm", "achieved": nbytes / (avg_ms * 1e-3) / 1e9, "peak": hbm,
+                            "unit": "GB/s", "frac": nbytes / (avg_ms * 1e-3) / 1e9 / hbm, "peak_kind": kind,
+                            "note": "one product per vector (the single-film kernels)"}
     print(json.dumps(line))
 
 
@@ -897,9 +987,11 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="fp32x2", choices=["fp64", "fp32", "fp32x2"],
+    ap.add_argument("--form", default="fp32x2", choices=["fp64", "fp32", "fp32x2", "bf16x3"],
                     help="BEM product: fp64; fp32 (FP32 entries, FP64 sums); fp32x2 (FP32 + BF16 residual "
-                         "entries, compensated FP32 products)")
+                         "entries, compensated FP32 products); bf16x3 (three BF16 planes, tensor cores)")
+    ap.add_argument("--precision-members", type=int, default=0,
+                    help="--report precision: fields per ensemble (0: 128 for bf16x3, else 8)")
     ap.add_argument("--workload", default="film", choices=["film", "cube", "film_small"])
     ap.add_argument("--step-ps", type=float, default=50.0,
                     help="simulated time per step (20 steps: the configured 1 ns)")
@@ -934,7 +1026,8 @@ def main():
     ap.add_argument("--batch-tol", type=float, default=1e-7)
     ap.add_argument("--batch-seconds", type=float, default=0.0,
                     help="after the timed launches, keep sweeping for this wall time and report the progress")
-    ap.add_argument("--report", default=None, choices=["precision", "adjoint", "batch"],
+    ap.add_argument("--rhs", type=int, default=128, help="--report bem: right-hand sides per product")
+    ap.add_argument("--report", default=None, choices=["precision", "adjoint", "batch", "bem"],
                     help="precision: H_eff / energy error of the FP32 form against FP64 over --fields random fields")
     ap.add_argument("--fields", type=int, default=1000)
     ap.add_argument("--no-compare", dest="compare", action="store_false",
@@ -948,6 +1041,8 @@ def main():
         run_precision_report(args)
     elif args.report == "adjoint":
         run_adjoint_report(args)
+    elif args.report == "bem":
+        run_bem_report(args)
     elif args.report == "batch":
         run_batch_report(args)
     else:

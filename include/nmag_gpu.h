@@ -49,7 +49,12 @@ typedef struct nmg_options {
   double dbc_rtol, dbc_atol; int dbc_maxits;   /* Dirichlet Poisson solve            */
   int bem_precision;                     /* 0: FP64 matrix; 1: FP32 matrix, FP64 sums;
                                             2: FP32 + BF16-residual matrix, compensated
-                                               FP32 products (~2^-44)                  */
+                                               FP32 products (~2^-44);
+                                            3: tensor cores: B and x split into three
+                                               BF16 planes each, six tcgen05 products
+                                               per term, FP32 sums over 2048 terms
+                                               added in FP64 (~2^-24); an ensemble's
+                                               members form one product              */
   int cg_precision;                      /* 0: FP64 CG; reserved                       */
   int cg_no_coarse;                      /* 1: Jacobi only (no two-level Neumann CG)   */
   int n_members;                         /* ensemble size B (0 or 1: one simulation)   */
@@ -222,6 +227,13 @@ int nmg_max_dm_step(nmg_handle *h, double *out);
  * torch tensors): one RHS evaluation dmdt = f(m) on the handle's stream and
  * one fixed-step RK4 trajectory.  No host copies.  */
 int nmg_rhs_device(nmg_handle *h, const double *d_m, double *d_dmdt);
+/* y_n = B x_n for n_rhs boundary vectors (device arrays, member-major: x_n at
+ * d_x + n * nb) with the handle's BEM in its bem_precision form -- the
+ * reference's dense BEM MatMult (nsim.ml:3128-3140) for many right-hand sides
+ * at once (with bem_precision 3 one tensor-core product).  On the handle's
+ * stream; returns after the product is complete.  Not with the anchored
+ * product. */
+int nmg_bem_apply(nmg_handle *h, const double *d_x, double *d_y, int n_rhs);
 int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps);
 
 /* Differentiation form.  No counterpart in the reference, whose material

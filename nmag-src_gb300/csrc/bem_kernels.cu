@@ -248,7 +248,10 @@ int fill_bem(nmg_handle *h, std::string &err) {
     NMG_CUDA_TRY(cudaGetLastError(), "bem transpose launch");
     NMG_CUDA_TRY(cudaStreamSynchronize(s), "bem fill");
   }
-  if (h->opt.bem_precision >= 1) {
+  if (h->opt.bem_precision == 3) {   // tensor-core product: BF16 planes of the FP64 matrix
+    if (int rc = bem_tc_setup(h, err)) return rc;
+  }
+  if (h->opt.bem_precision == 1 || h->opt.bem_precision == 2) {
     NMG_CUDA_TRY(M.bem32.alloc(nb * M.ld), "alloc FP32 BEM");
     k_to_f32<<<h->sm_count * 8, 256, 0, s>>>(nb * M.ld, M.bem, M.bem32);
   }

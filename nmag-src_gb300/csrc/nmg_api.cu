@@ -59,6 +59,8 @@ int nmg_create(const double *coords, int n_nodes, const int32_t *tets, int n_tet
     return fail(nullptr, -6, "nmg_create: n_members must be in [0, " + std::to_string(nmg::kMaxMembers) + "]");
   if (opt && !(opt->bem_anchor_tol >= 0.0 && opt->bem_anchor_tol <= 1e300))
     return fail(nullptr, -6, "nmg_create: bem_anchor_tol must be finite and non-negative");
+  if (opt && (opt->bem_precision < 0 || opt->bem_precision > 3))
+    return fail(nullptr, -6, "nmg_create: bem_precision must be 0, 1, 2 or 3");
   if (opt && opt->bem_anchor_tol > 0.0 && opt->bem_precision != 2)
     return fail(nullptr, -6, "nmg_create: bem_anchor_tol applies to the compensated product (bem_precision 2)");
   int dev = 0;
@@ -397,6 +399,21 @@ int nmg_rhs_device(nmg_handle *h, const double *d_m, double *d_dmdt) {
   return nmg::check_device_error(h, "nmg_rhs_device");
 }
 
+int nmg_bem_apply(nmg_handle *h, const double *d_x, double *d_y, int n_rhs) {
+  if (!h || !d_x || !d_y) return -1;
+  if (n_rhs < 1) return fail(h, -2, "nmg_bem_apply: n_rhs must be positive");
+  if (h->mesh.nb == 0) return fail(h, -2, "nmg_bem_apply: the mesh has no boundary");
+  if (h->anchored()) return fail(h, -2, "nmg_bem_apply: not available with the anchored product (bem_anchor_tol)");
+  const size_t nb = h->mesh.nb;
+  if (h->opt.bem_precision == 3) {
+    if (nmg::bem_tc(h, d_x, d_y, n_rhs)) return fail(h, 100, "nmg_bem_apply: " + h->last_error);
+  } else {
+    for (int n = 0; n < n_rhs; ++n) nmg::bem_gemv(h, d_x + n * nb, d_y + n * nb);
+  }
+  if (cudaGetLastError() != cudaSuccess) return fail(h, 100, "nmg_bem_apply: launch failed");
+  return nmg::check_device_error(h, "nmg_bem_apply");
+}
+
 int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps) {
   if (!h || !d_m || nsteps < 0) return -1;
   return nmg::rk4_device(h, d_m, dt, nsteps);
@@ -453,18 +470,9 @@ int nmg_profile(nmg_handle *h, int enable) {
 int nmg_profile_read(nmg_handle *h, int kernel, int64_t *launches, double *total_ms) {
   if (!h || !launches || !total_ms || kernel < 0 || kernel >= nmg::Profiler::kKernels) return -1;
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return 100;
-  int64_t n = 0;
-  double ms = 0.0;
-  for (int k = 0; k < h->prof.used; ++k) {
-    if (h->prof.kernel_of[k] != kernel) continue;
-    float t = 0.f;
-    if (cudaEventElapsedTime(&t, h->prof.pool[2 * k], h->prof.pool[2 * k + 1]) == cudaSuccess) {
-      ms += t;
-      ++n;
-    }
-  }
-  *launches = n;
-  *total_ms = ms;
+  h->prof.fold();
+  *launches = h->prof.done_n[kernel];
+  *total_ms = h->prof.done_ms[kernel];
   return 0;
 }
 
@@ -491,9 +499,20 @@ int nmg_cg_iterations(const nmg_handle *h, int64_t total[2]) {
 }  // extern "C"
 
 namespace nmg {
+void Profiler::fold() {
+  if (used > 0) cudaEventSynchronize(pool[2 * (used - 1) + 1]);
+  for (int k = 0; k < used; ++k) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, pool[2 * k], pool[2 * k + 1]) == cudaSuccess) {
+      done_ms[kernel_of[k]] += t;
+      ++done_n[kernel_of[k]];
+    }
+  }
+  used = 0;
+}
 void Profiler::begin(cudaStream_t s, int kernel, int *slot) {
   *slot = -1;
-  if (used >= kMaxPairs) return;
+  if (used >= kMaxPairs) fold();   // a long profiled run: resolve the full pool (one wait) and reuse it
   if (pool.empty()) {
     pool.resize(2 * kMaxPairs);
     for (auto &e : pool) cudaEventCreate(&e);

@@ -21,7 +21,7 @@ enum DeviceError : int {
 };
 
 constexpr int kMaxRowLen = 64;     // max distinct neighbours (incl. self) per node
-constexpr int kMaxMembers = 64;    // ensemble members per handle
+constexpr int kMaxMembers = 256;   // ensemble members per handle
 constexpr int kChunk = 8;          // members per CG / BEM launch
 constexpr int kMaxNodeTets = 128;  // max tets around one node
 
@@ -114,6 +114,19 @@ struct Workspace {
   long long h16_seg = 0;
 };
 
+// Tensor-core BEM product (bem_precision 3): three BF16 planes of B (rows
+// padded to Mpad, columns to ldk; plane p at p * Mpad rows), the right-hand
+// sides' planes (Rcap rows each), the FP32 per-split partials and the TMA
+// tensor maps (CUtensorMap, 128 bytes) over the two plane sets.
+struct TcState {
+  int Mpad = 0, ldk = 0, nt = 0, Rcap = 0;
+  int failed = 0;   // a product could not be formed (host-side set-up); rhs_eval reports it
+  DevBuf<uint16_t> bplanes, xplanes;
+  DevBuf<float> part;
+  alignas(64) unsigned char mapA[128];
+  alignas(64) unsigned char mapX[128];
+};
+
 struct Integrator;
 
 // CUDA-event brackets around hot-kernel launches (resolved after the run).
@@ -124,9 +137,16 @@ struct Profiler {
   std::vector<cudaEvent_t> pool;   // 2 * kMaxPairs events, created lazily
   int used = 0;
   int kernel_of[kMaxPairs];
+  // totals of the pairs already resolved (the pool is folded into these when it fills)
+  long long done_n[kKernels] = {0};
+  double done_ms[kKernels] = {0.0};
   void begin(cudaStream_t s, int kernel, int *slot);
   void end(cudaStream_t s, int slot);
-  void reset() { used = 0; }
+  void fold();   // wait for the recorded pairs, add them to the totals, empty the pool
+  void reset() {
+    used = 0;
+    for (int k = 0; k < kKernels; ++k) { done_n[k] = 0; done_ms[k] = 0.0; }
+  }
   ~Profiler();
 };
 
@@ -184,6 +204,7 @@ struct nmg_handle {
   nmg::AnisPoly ap;
   nmg::Stt stt;
   nmg::DevBuf<double> pin;      // per-node factor of dm/dt and of the Jacobian rows (null: 1 everywhere)
+  nmg::TcState tc;              // tensor-core BEM product (bem_precision 3)
   nmg::Tape *tape = nullptr;
   int anchor_hold = 0;          // >0: anchored BEM product suspended (RK4 tape runs recompute bit for bit)
   // the mixed-precision CG is used by the forward solves or the adjoint's
@@ -225,6 +246,9 @@ int export_operator(const nmg_handle *h, int which, double coeff, int *rows, int
 // ---- bem_kernels.cu ----
 int fill_bem(nmg_handle *h, std::string &err);
 void bem_gemv(nmg_handle *h, const double *x, double *y);
+// ---- bem_tc.cu ----
+int bem_tc_setup(nmg_handle *h, std::string &err);
+int bem_tc(nmg_handle *h, const double *x, double *y, int R);   // Y = B X, R member-major right-hand sides
 // ---- rhs_kernels.cu ----
 int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt);  // full RHS on device vectors
 // CG on slot 0/2 (Neumann operator) or 1/3 (Dirichlet operator); slots 2/3

@@ -2676,6 +2676,10 @@ void bem_gemv(nmg_handle *h, const double *x, double *y) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   const int nb = M.nb;
+  if (h->opt.bem_precision == 3) {   // tensor cores, split BF16
+    if (bem_tc(h, x, y, 1)) h->tc.failed = 1;   // reported by rhs_eval
+    return;
+  }
   const int f = (h->opt.bem_precision >= 1 && M.bem32.p) ? 1 : 0;
   const long long seg = W.gemv_seg[f];
   const int maxr = W.gemv_maxr[f];
@@ -2735,6 +2739,10 @@ void bem_gemm(nmg_handle *h, const double *x, double *y) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   const int nb = M.nb, B = h->nrep;
+  if (h->opt.bem_precision == 3) {   // every member in one tensor-core product
+    if (bem_tc(h, x, y, B)) h->tc.failed = 1;   // reported by rhs_eval
+    return;
+  }
   const int f = (h->opt.bem_precision >= 1 && M.bem32.p) ? 1 : 0;
   const long long seg = W.gemv_seg[f];
   const int maxr = W.gemv_maxr[f];
@@ -2932,6 +2940,10 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
     NMG_PROF_END(h);
   }
   h->n_rhs++;
+  if (h->tc.failed) {   // the tensor-core product could not be set up (message in last_error)
+    h->tc.failed = 0;
+    return 100;
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : 100;
 }
 

@@ -56,7 +56,7 @@ class TsStats(C.Structure):
 EXPORTS = ["nmg_version", "nmg_set_device", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_mesh_info", "nmg_get_csr",
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
            "nmg_set_material", "nmg_set_anisotropy_poly", "nmg_set_stt", "nmg_set_current_density", "nmg_set_pinning", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
-           "nmg_ts_advance", "nmg_max_dm", "nmg_max_dm_step", "nmg_rhs_device", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
+           "nmg_ts_advance", "nmg_max_dm", "nmg_max_dm_step", "nmg_rhs_device", "nmg_bem_apply", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
            "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_bem_anchor_stats", "nmg_max_dm_static",
            "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
            "nmg_member_averages", "nmg_batch_last_error", "nmg_batch_create", "nmg_batch_destroy", "nmg_batch_info",
@@ -115,6 +115,7 @@ def lib(build_if_missing=True):
     L.nmg_max_dm.argtypes = [vp, _f64p, C.POINTER(C.c_double)]
     L.nmg_max_dm_step.argtypes = [vp, C.POINTER(C.c_double)]
     L.nmg_rhs_device.argtypes = [vp, vp, vp]
+    L.nmg_bem_apply.argtypes = [vp, vp, vp, C.c_int]
     L.nmg_rk4_device.argtypes = [vp, vp, C.c_double, C.c_int]
     L.nmg_get_timings.argtypes = [vp, _f64p]
     L.nmg_profile.argtypes = [vp, C.c_int]
@@ -355,6 +356,10 @@ class Engine(object):
     # ---- device pointers (torch tensors) ----
     def rhs_device(self, d_m, d_dmdt):
         check(lib().nmg_rhs_device(self.h, C.c_void_p(d_m), C.c_void_p(d_dmdt)), self.h, "rhs_device")
+
+    def bem_apply_device(self, d_x, d_y, n_rhs):
+        """y_n = B x_n for n_rhs member-major boundary vectors (device addresses)."""
+        check(lib().nmg_bem_apply(self.h, C.c_void_p(d_x), C.c_void_p(d_y), int(n_rhs)), self.h, "bem_apply")
 
     def rk4_device(self, d_m, dt, nsteps):
         check(lib().nmg_rk4_device(self.h, C.c_void_p(d_m), dt, nsteps), self.h, "rk4_device")

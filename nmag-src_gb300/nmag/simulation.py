@@ -210,8 +210,9 @@ class Simulation(object):
             return default if v is None else v
         opts.nbc_rtol, opts.nbc_atol, opts.nbc_maxits = tol("NBC.rtol", 1e-5), tol("NBC.atol", 1e-50), int(tol("NBC.maxits", 10000))
         opts.dbc_rtol, opts.dbc_atol, opts.dbc_maxits = tol("DBC.rtol", 1e-5), tol("DBC.atol", 1e-50), int(tol("DBC.maxits", 10000))
-        # fp32: FP32 matrix; fp32x2: FP32 + BF16 residual matrix with compensated FP32 products
-        opts.bem_precision = {"fp64": 0, "fp32": 1, "fp32x2": 2}[self.bem_precision]
+        # fp32: FP32 matrix; fp32x2: FP32 + BF16 residual matrix with compensated FP32 products;
+        # bf16x3: three BF16 planes of matrix and vectors, six tensor-core products per term
+        opts.bem_precision = {"fp64": 0, "fp32": 1, "fp32x2": 2, "bf16x3": 3}[self.bem_precision]
         opts.cg_precision = {"fp64": 0, "fp32": 1}[self.cg_precision]
         opts.n_members = self.n_members if self.n_members > 1 else 0
         opts.bem_anchor_tol = self.bem_anchor
