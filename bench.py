@@ -287,11 +287,17 @@ def config_dict(args, msh):
             "nodes": int(msh.n_nodes), "tets": int(msh.n_tets),
             "step": "%g ps advance in %g ps records, each followed by an <m> read" % (args.step_ps, args.record_ps),
             "interval_ps": args.steps * args.step_ps,
-            "form": args.form, "cg": args.cg, "members": args.members,
+            "form": args.form, "cg": args.cg, "cg_local_sweeps": args.cg_sweeps, "members": args.members,
             "bem_anchor": args.anchor if args.form == "fp32x2" else 0.0,
             "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
             "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % {"fp64": 8, "fp32": 4,
                                                                                   "fp32x2": 6, "bf16x3": 6}[args.form]}
+
+
+# records (1-based, in record_ps units) where the e2e leg keeps WINDOW_LEN
+# consecutive states for the anchored product's error walk
+WINDOW_RECORDS = (100, 500, 900)
+WINDOW_LEN = 6
 
 
 def relax_states(args, form, cg, B, msh, base, seed, anchor):
@@ -304,7 +310,7 @@ def relax_states(args, form, cg, B, msh, base, seed, anchor):
     import nmag
     from nmag import SI, every
     sim = nmag.Simulation("relax", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor,
-                          anchor_product=args.anchor_product)
+                          anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps)
     sim.load_mesh(msh, [("film", material(1.0))], unit_length=SI(1e-9, "m"))
     if B > 1:   # member b starts from the workload's initial state with seed + b
         sim.set_m(np.stack([initial_m(msh.n_nodes, base, seed + b) for b in range(B)]))
@@ -341,7 +347,7 @@ def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anc
     import nmag
     from nmag import SI
     sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor,
-                          anchor_product=args.anchor_product)
+                          anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps)
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     sim.set_H_ext(h_ext_su() * 1e6, SI(1.0, "A/m"))
@@ -394,19 +400,28 @@ def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anc
     m_final = eng.get_m()
     # ---- e2e leg through the public API, over the same interval from the same state ----
     wall_e2e = None
+    windows = []
     if e2e:
         restart()
         torch.cuda.synchronize()
         barrier(world)
         w1 = time.perf_counter()
         t = 0.0
+        keep = {k for first in WINDOW_RECORDS for k in range(first, first + WINDOW_LEN)}
+        snaps = {}
+        nrec = 0
         for _ in range(args.steps):
             for _ in range(per_step):
                 t += rec
                 sim.advance_time(SI(t * 1e-12, "s"))
                 sim.get_subfield_average_siv("m")
+                nrec += 1
+                if anchor > 0 and nrec in keep:   # m is on the host already (advance_time copied it)
+                    snaps[nrec] = np.array(sim._m, copy=True)
         torch.cuda.synchronize()
         wall_e2e = max_over_ranks(time.perf_counter() - w1, world)
+        windows = [[snaps[k] for k in range(first, first + WINDOW_LEN) if k in snaps] for first in WINDOW_RECORDS]
+        windows = [w for w in windows if len(w) >= 2]
     dev_s = max_over_ranks(dev_ms * 1e-3, world)
     sim_ns_total = world * B * args.steps * args.step_ps * 1e-3   # summed over ensemble members
     nb = eng.nb
@@ -483,6 +498,7 @@ def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anc
         # per step: B members' m copied to the host (advance_time) + <m> (24 B) per record
         "d2h": per_step * (B * msh.n_nodes * 3 * 8 + 24),
         "anchored": anchored, "m_start": start, "m_final": m_final, "trace": np.asarray(trace),
+        "windows": windows,
     }
 
 
@@ -510,46 +526,51 @@ def heff_error(args, chosen, msh):
     return float(np.abs(out[args.form] - ref).max() / np.abs(ref).max())
 
 
-def anchor_path_error(args, chosen, msh, points=48):
-    """H_eff error of the anchored product along the run's own trajectory:
-    for every member the magnetisation moves from its state before the timed
-    steps to its final state through `points` normalised linear blends, the
-    anchored form evaluating each blend with its anchor carried along (so
-    most products are FP32 differences from an earlier blend, refreshed when
-    the drift passes tol).  Against the FP64 form at the same blends; both
-    sides converge their Poisson solves to 1e-12.  Returns the max over
-    blends and members of max |H - H_fp64| / max |H_fp64| and the anchor's
-    product / refresh counts over the walk."""
+def anchor_path_error(args, chosen, msh, blends=4):
+    """H_eff error of the anchored product along the run's own trajectory.
+    The e2e leg keeps the members' states of a few windows of consecutive
+    records (chosen["windows"]); each window is walked in order, with
+    `blends` normalised linear blends per record interval, through the
+    anchored form (its anchor carried along, so most products are FP32
+    differences from an earlier state, a refresh when the drift passes tol)
+    and through the FP64 form; both converge their Poisson solves to 1e-12.
+    Returns the max over the walk and the members of max |H - H_fp64| /
+    max |H_fp64|, the anchor's product / refresh counts over the walk and
+    the number of evaluations."""
     import nmag
     from nmag import SI
     B = args.members
-    ma = np.asarray(chosen["m_start"]).reshape(B, -1, 3) if B > 1 else np.asarray(chosen["m_start"])[None]
-    mb = np.asarray(chosen["m_final"]).reshape(B, -1, 3) if B > 1 else np.asarray(chosen["m_final"])[None]
     tight = {"NBC.rtol": 1e-12, "DBC.rtol": 1e-12, "NBC.maxits": 20000, "DBC.maxits": 20000}
     sims = {}
     for key, form, anc in (("anchored", args.form, args.anchor), ("fp64", "fp64", 0.0)):
         sim = nmag.Simulation("err", bem_precision=form, ksp_tolerances=tight, n_members=B, bem_anchor=anc,
-                              anchor_product=args.anchor_product)
+                              anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps)
         sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
         shape = (B, sim.engine.N, 3) if B > 1 else (sim.engine.N, 3)
         sim.engine.set_h_ext(np.broadcast_to(h_ext_su(), shape))
         sims[key] = (sim, shape)
-    worst = 0.0
-    for k in range(points + 1):
-        s = k / points
-        m = (1.0 - s) * ma + s * mb
-        m /= np.linalg.norm(m, axis=-1, keepdims=True)
-        H = {}
-        for key, (sim, shape) in sims.items():
-            sim.engine.set_m(m.reshape(shape))
-            H[key] = np.asarray(sim.engine.eval_fields()["H_total"]).reshape(B, -1, 3)
-        for b in range(B):
-            ref = H["fp64"][b]
-            worst = max(worst, float(np.abs(H["anchored"][b] - ref).max() / np.abs(ref).max()))
+    worst, evals = 0.0, 0
+    for window in chosen["windows"]:
+        states = [np.asarray(w).reshape(B, -1, 3) for w in window]
+        path = []
+        for a, b in zip(states[:-1], states[1:]):
+            for j in range(blends):
+                path.append((1.0 - j / blends) * a + (j / blends) * b)
+        path.append(states[-1])
+        for m in path:
+            m = m / np.linalg.norm(m, axis=-1, keepdims=True)
+            H = {}
+            for key, (sim, shape) in sims.items():
+                sim.engine.set_m(m.reshape(shape))
+                H[key] = np.asarray(sim.engine.eval_fields()["H_total"]).reshape(B, -1, 3)
+            for b in range(B):
+                ref = H["fp64"][b]
+                worst = max(worst, float(np.abs(H["anchored"][b] - ref).max() / np.abs(ref).max()))
+            evals += 1
     prod, ref_n = sims["anchored"][0].engine.bem_anchor_stats()
     for sim, _ in sims.values():
         sim.engine.close()
-    return worst, prod, ref_n
+    return worst, prod, ref_n, evals
 
 
 def run_precision_report(args):
@@ -962,9 +983,11 @@ def run_ours(args):
         # member 0 starts from the plain run's state: <m> at every record of the interval
         line["avg_m_diff_vs_plain_fp64"] = float(np.abs(r["trace"] - plain["trace"]).max())
     if anchor > 0:
-        err, prod, nref = anchor_path_error(args, r, msh)
+        err, prod, nref, nev = anchor_path_error(args, r, msh)
         line["anchored"]["path_error"] = {"heff_rel_err_vs_fp64": err, "products": prod, "refreshes": nref,
-                                          "blends": 49}
+                                          "evaluations": nev,
+                                          "windows": "records %s (ps): consecutive states of the e2e leg, 4 blends "
+                                                     "per 1 ps record interval" % (WINDOW_RECORDS,)}
         line["heff_rel_err_vs_fp64"] = max(line.get("heff_rel_err_vs_fp64", 0.0), err)
     if world == 1 and not args.no_cpu_baseline:
         cr = cpu_reference_run(args, msh, base, seed, steps=args.cpu_records, warmup=0, max_wall=20.0)
@@ -1008,6 +1031,8 @@ def main():
     ap.add_argument("--anchor-product", default="fp32", choices=["fp32", "fp16"],
                     help="difference product of the anchored ensemble form: FP32 matrix copy or FP16 copy "
                          "in tensor-core fragment order")
+    ap.add_argument("--cg-sweeps", type=int, default=0,
+                    help="FP32 inner CG: damped Jacobi sweeps on each block's rows in the preconditioner")
     ap.add_argument("--anchor", type=float, default=3e-3,
                     help="fp32x2: anchored product tolerance (B x = B x0 + B32 (x - x0) while the max-norm drift "
                          "of x from x0 stays below it; 0 = off)")

@@ -70,6 +70,9 @@ typedef struct nmg_options {
                                             B (x - x0): 0 FP32 copy of B; 1 FP16 copy of
                                             B in tensor-core fragment order (FP32
                                             accumulation; ~2^-11 of |B||x - x0|)        */
+  int cg_local_sweeps;                   /* FP32 inner CG (cg_precision 1): damped Jacobi
+                                            sweeps on each thread block's own rows in
+                                            the preconditioner (0 or 1: Jacobi alone) */
 } nmg_options;
 
 /* Integrator statistics (CVODE counters; nsim.ml:354-387 timings). */

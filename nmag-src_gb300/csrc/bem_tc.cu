@@ -12,9 +12,10 @@
 // operands staged in shared memory by TMA (cp.async.bulk.tensor, 128-byte
 // swizzle).  The K dimension (the boundary nodes the matrix sums over) is
 // split over CTAs, each accumulating at most kKbPerSplit x 64 terms of every
-// sum in FP32; the per-split partial sums are added in FP64, in split order,
-// by a second kernel.  So the FP32 accumulation error stays at the level of a
-// few thousand terms, not of nb.
+// sum in FP32 (the hi.hi term and the five smaller terms in two separate TMEM
+// accumulators); the per-split partial sums are added in FP64, in split
+// order, by a second kernel.  So the FP32 accumulation error stays at the
+// level of a thousand terms, not of nb.
 //
 // Tiles: 128 rows of B (one TMEM lane each) x NT right-hand sides (TMEM
 // columns) x 64 entries of K per stage; one thread issues the TMA loads, one
@@ -34,7 +35,7 @@ namespace {
 
 constexpr int kTcRows = 128;           // rows of B per CTA (MMA M)
 constexpr int kTcK = 64;               // K entries per stage (one 128-byte swizzle span of BF16)
-constexpr int kKbPerSplit = 32;        // K stages accumulated in TMEM per split (2048 terms)
+constexpr int kKbPerSplit = 16;        // K stages accumulated in TMEM per split (1024 terms)
 constexpr unsigned long long kTcSpinLimit = 1ull << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -146,9 +147,12 @@ __global__ void __launch_bounds__(128, 1)
     n_issued = n_consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {   // NT TMEM columns (a power of two >= 32) hold the 128 x NT accumulator
+  // 2 NT TMEM columns (a power of two >= 64): two 128 x NT FP32 accumulators,
+  // columns [0, NT) for the hi.hi term, [NT, 2 NT) for the five smaller ones,
+  // so the small terms' rounding is relative to their own (2^-8 smaller) sums
+  if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                 "r"((uint32_t)NT));
+                 "r"((uint32_t)(2 * NT)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -181,7 +185,8 @@ __global__ void __launch_bounds__(128, 1)
       for (int kk = 0; kk < kTcK / 16; ++kk)   // 16 entries (32 bytes) per MMA: +2 in the encoded address
 #pragma unroll
         for (int t = 0; t < 6; ++t)
-          mma_bf16(tmem, da[kPairA[t]] + 2 * kk, dx[kPairX[t]] + 2 * kk, idesc, (i | kk | t) != 0);
+          mma_bf16(t == 0 ? tmem : tmem + NT, da[kPairA[t]] + 2 * kk, dx[kPairX[t]] + 2 * kk, idesc,
+                   (i | kk | (t > 1 ? 1 : 0)) != 0);
       mma_commit(&empty[s]);   // the stage is free once these MMAs have read it
       n_consumed = i + 1;
     }
@@ -196,10 +201,12 @@ __global__ void __launch_bounds__(128, 1)
     float *out = part + ((size_t)blockIdx.z * Rstride + (size_t)blockIdx.y * NT) * Mpad + row;
 #pragma unroll 1
     for (int c0 = 0; c0 < NT; c0 += 32) {
-      uint32_t r[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+      uint32_t r0[32], r1[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r0);
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(NT + c0), r1);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) out[(size_t)(c0 + j) * Mpad] = __uint_as_float(r[j]);
+      for (int j = 0; j < 32; ++j)
+        out[(size_t)(c0 + j) * Mpad] = (float)((double)__uint_as_float(r0[j]) + (double)__uint_as_float(r1[j]));
     }
   } else if (threadIdx.x == 0) {
     atomicOr(err, ERR_BARRIER);
@@ -217,7 +224,8 @@ __global__ void __launch_bounds__(128, 1)
       }
   }
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)NT));
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * NT)));
 }
 
 // y[n * nb + row] = sum over the splits, in split order, of the FP32 partials (FP64 adds).

@@ -178,6 +178,7 @@ struct CGArgs {
   float *rw32;        // R w of every aggregate (nc x MB), published with the inner dot products
   float eta;          // inner relative tolerance
   int max_outer;      // FP64 refinement steps
+  int local_sweeps;   // mixed-precision CG: damped Jacobi sweeps on the block's own rows (1: plain Jacobi)
 };
 constexpr int kAgg = 64;   // rows per aggregate (4 aggregates per 256-row block)
 // float4 groups of the coarse vectors (nc x MB floats) per thread of the
@@ -1095,9 +1096,31 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
       if (I < a.nc) out[(size_t)I * MB + m] = sagg[m][2 * gg] + sagg[m][2 * gg + 1];
     }
   };
-  auto precond32 = [&](const float (&rr)[MB], float (&uu)[MB]) -> bool {
+  // Local part of the preconditioner: u = D^-1 r, then local_sweeps - 1
+  // damped Jacobi sweeps u += (2/3) D^-1 (r - A_loc u) with A_loc the
+  // block's own rows and columns (its subdomain, the other blocks' values
+  // taken as zero): a polynomial in D^-1 A_loc times D^-1, so the
+  // preconditioner stays symmetric positive definite (additive Schwarz with
+  // an inexact subdomain solve; the coarse level is added to it).  Uses suS
+  // as scratch; with one sweep it is the Jacobi step alone.
+  auto local_smooth = [&](const float (&rr)[MB], float (&uu)[MB]) {
 #pragma unroll
     for (int m = 0; m < MB; ++m) uu[m] = dinv32 * rr[m];
+    for (int sw = 1; sw < a.local_sweeps; ++sw) {
+#pragma unroll
+      for (int q = 0; q < MB / 2; ++q)
+        reinterpret_cast<float2 *>(suS + (size_t)tid * MB)[q] =
+            active ? make_float2(uu[2 * q], uu[2 * q + 1]) : make_float2(0.f, 0.f);
+      __syncthreads();
+      float au[MB];
+      apply32_local(au);
+      __syncthreads();
+#pragma unroll
+      for (int m = 0; m < MB; ++m) uu[m] = fmaf((2.f / 3.f) * dinv32, rr[m] - au[m], uu[m]);
+    }
+  };
+  auto precond32 = [&](const float (&rr)[MB], float (&uu)[MB]) -> bool {
+    local_smooth(rr, uu);
     if (!a.coarse) return true;
     aggregate_sums(rr, a.rc32);
     if (!arrive_wait(a, ++epoch)) return false;
@@ -1309,8 +1332,7 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
           ri[m] = fmaf(-al, si[m], ri[m]);
         }
       }
-#pragma unroll
-      for (int m = 0; m < MB; ++m) ui[m] = dinv32 * ri[m];
+      local_smooth(ri, ui);
       if (a.coarse) coarse_add(ui);
       publish();
       ++iit;
@@ -2449,6 +2471,7 @@ int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm,
   a.nc = W.nc; a.ainv = W.ainv; a.rc = W.rc;
   a.ainv32 = W.ainv32; a.rc32 = W.rc32; a.z32 = W.z32; a.rw32 = W.rw32;
   a.eta = 1e-3f; a.max_outer = 10;
+  a.local_sweeps = h->opt.cg_local_sweeps > 1 ? h->opt.cg_local_sweeps : 1;
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
   int cap = W.cg_nnz_cap;
   CGBasis basis;

@@ -117,7 +117,7 @@ class Simulation(object):
                  temperature=None, thermal_delta_t=None, user_seed_T=0, timestepper_max_order=2,
                  timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
                  lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1, cg_precision="fp64",
-                 bem_anchor=0.0, adjoint_cg_precision="fp64", anchor_product="fp32"):
+                 bem_anchor=0.0, adjoint_cg_precision="fp64", anchor_product="fp32", cg_local_sweeps=0):
         if periodic_bc is not None:
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
@@ -146,6 +146,9 @@ class Simulation(object):
         # Poisson solves of the RK4 adjoint's backward pass ("fp32": FP32 CG
         # iterations with FP64 residual refinement to the same tolerance)
         self.adjoint_cg_precision = adjoint_cg_precision
+        # FP32 inner CG: damped Jacobi sweeps on each thread block's own rows
+        # in its preconditioner (0 or 1: Jacobi alone)
+        self.cg_local_sweeps = int(cg_local_sweeps)
         # ensemble: n_members simulations on one mesh, integrated together;
         # per-node arrays then carry a leading member axis (GB300 extension)
         self.n_members = max(1, int(n_members))
@@ -218,6 +221,7 @@ class Simulation(object):
         opts.bem_anchor_tol = self.bem_anchor
         opts.adjoint_cg_precision = {"fp64": 0, "fp32": 1}[self.adjoint_cg_precision]
         opts.anchor_product = {"fp32": 0, "fp16": 1}[self.anchor_product]
+        opts.cg_local_sweeps = self.cg_local_sweeps
         self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
         poly = self.material.anisotropy_polynomial(self.quirks)
         if poly is not None:
