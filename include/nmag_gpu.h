@@ -205,6 +205,36 @@ int nmg_averages(nmg_handle *h, double avg_m[3], double energies[5]);
  * reference, which runs one simulation per process. */
 int nmg_member_averages(nmg_handle *h, int member, double avg_m[3], double energies[5]);
 
+/* Several magnetic materials (main.py:1182-1191 region -> material mapping;
+ * nmag_lam.py:183-470 one m field per material).  Replaces ocaml.raw_make_lam
+ * for a mesh whose regions carry different materials.  tet_region[t] in
+ * 1..n_regions is the region of tetrahedron t (vacuum simplices are not
+ * passed); region r carries the materials region_mats[region_ptr[r-1] ..
+ * region_ptr[r]) (indices into mats).  Every material X has its own m_X on
+ * its sites -- the nodes of the simplices of its regions -- so a node on an
+ * interface carries one m per material, and the exchange acts within each
+ * material only; the demagnetising potential lives on every node and sees
+ * all materials' charges.  Sites are numbered material by material (mats
+ * order), nodes ascending within a material: nmg_mesh_info reports the site
+ * count as info[0], and every per-node array of the calls above (m, H_ext,
+ * fields, energies, pinning) then holds one entry per site.  Options as
+ * nmg_create (precision forms, ensembles); closed-form uniaxial anisotropy
+ * per material; polynomial anisotropy, spin-transfer torque and element
+ * parameters are refused. */
+int nmg_create_materials(const double *coords, int n_nodes, const int32_t *tets, int n_tets,
+                         const int32_t *tet_region, int n_regions, const int32_t *region_ptr,
+                         const int32_t *region_mats, const nmg_material *mats, int n_mats,
+                         const nmg_options *opt, nmg_handle **out);
+/* The mesh node and the material of every site (n_sites entries each). */
+int nmg_site_info(const nmg_handle *h, int32_t *site_node, int32_t *site_material);
+/* Change material k's constants (e.g. its damping between relax and dynamics). */
+int nmg_set_site_material(nmg_handle *h, int material, const nmg_material *mat);
+/* <m> of one material (volume average over its sites) and its energies
+ * (sum of E_i V_i over its sites: exchange, demag, Zeeman, anisotropy,
+ * total), of ensemble member `member`; one material: material 0 is the
+ * mesh (main.py:2313-2480 averages per material). */
+int nmg_material_averages(nmg_handle *h, int material, int member, double avg_m[3], double energies[5]);
+
 /* Timestepper (re)initialisation at t0 from the current m; replaces
  * ocaml.lam_ts_init -> timestepper_set_initial_from_phys (nsim.ml:2485-2535). */
 int nmg_ts_init(nmg_handle *h, double t0, double rtol, double atol, int max_order, int krylov_max);

@@ -103,8 +103,10 @@ int nmg_destroy(nmg_handle *h) {
   nmg::ts_destroy(h->ts);
   h->ts = nullptr;
   nmg::tape_free(h);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  nmg_handle *pot = h->pot;
+  if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
   delete h;  // member destructors release the device buffers
+  if (pot) nmg_destroy(pot);   // several materials: the potential mesh's handle (and the shared stream)
   return 0;
 }
 
@@ -205,6 +207,7 @@ int nmg_set_material(nmg_handle *h, const nmg_material *mat) {
 int nmg_set_anisotropy_poly(nmg_handle *h, int n_e, const int32_t *e_pow, const double *e_coef, int n_h,
                             const int32_t *h_pow, const double *h_coef) {
   if (!h) return -1;
+  if (h->pot) return fail(h, -2, "nmg_set_anisotropy_poly: not available with several materials");
   if (n_e < 0 || n_h < 0 || n_e > nmg::kAnisMaxTerms || n_h > nmg::kAnisMaxTerms)
     return fail(h, -2, "nmg_set_anisotropy_poly: term counts must be 0.." + std::to_string(nmg::kAnisMaxTerms));
   if ((n_e > 0 && (!e_pow || !e_coef)) || (n_h > 0 && (!h_pow || !h_coef)))
@@ -242,6 +245,7 @@ int nmg_set_anisotropy_poly(nmg_handle *h, int n_e, const int32_t *e_pow, const 
 
 int nmg_set_stt(nmg_handle *h, double c4, double c5) {
   if (!h) return -1;
+  if (h->pot) return fail(h, -2, "nmg_set_stt: not available with several materials");
   if (!std::isfinite(c4) || !std::isfinite(c5)) return fail(h, -5, "nmg_set_stt: non-finite coefficient");
   const size_t n3 = 3 * (size_t)h->mesh.N * h->nrep;
   if ((c4 != 0.0 || c5 != 0.0) && !h->stt.j.p) {   // current density starts at zero
@@ -257,6 +261,7 @@ int nmg_set_stt(nmg_handle *h, double c4, double c5) {
 
 int nmg_set_current_density(nmg_handle *h, const double *j) {
   if (!h) return -1;
+  if (h->pot) return fail(h, -2, "nmg_set_current_density: not available with several materials");
   const size_t n3 = 3 * (size_t)h->mesh.N * h->nrep;
   if (j)
     for (size_t k = 0; k < n3; ++k)
@@ -422,6 +427,7 @@ int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps) {
 int nmg_set_element_params(nmg_handle *h, const double *d_wK, const double *d_wD, const double *d_kappa,
                            const double axis[3]) {
   if (!h || !axis) return -1;
+  if (h->pot) return fail(h, -2, "nmg_set_element_params: not available with several materials");
   int rc = nmg::set_element_params(h, d_wK, d_wD, d_kappa, axis);
   return rc ? fail(h, rc, "nmg_set_element_params: " + h->last_error) : 0;
 }

@@ -127,6 +127,25 @@ struct TcState {
   alignas(64) unsigned char mapX[128];
 };
 
+// Several magnetic materials (nmag_lam.py:183-330): every material X has its
+// own m_X on its sites -- the nodes of the simplices of the regions carrying
+// X.  The handle's mesh is then the site mesh, the disjoint union of the
+// materials' sub-meshes (sites numbered material by material, nodes
+// ascending within a material): its exchange operator, box volumes and weak
+// divergence (with the surface term where X ends) are X's own, block by
+// block.  The potential lives on the nodes of the whole magnetic mesh, held
+// by an inner handle (pot) that owns the Poisson solves and the BEM.
+struct SiteMat {   // one material's coefficients (nmg_material, simulation units)
+  double Ms, c_exch, C1, C2, C3, K1, ax, ay, az, anis, E_half, E_ext;
+};
+struct Sites {
+  int n_mats = 0;
+  std::vector<int> offset, count;     // sites of material k: [offset[k], offset[k] + count[k])
+  DevBuf<int32_t> site_node, site_mat; // per site: node of the magnetic mesh, material
+  DevBuf<int32_t> node_ptr, node_sites; // node -> its sites (CSR, sites ascending)
+  DevBuf<SiteMat> mtab;                // per material
+};
+
 struct Integrator;
 
 // CUDA-event brackets around hot-kernel launches (resolved after the run).
@@ -205,6 +224,9 @@ struct nmg_handle {
   nmg::Stt stt;
   nmg::DevBuf<double> pin;      // per-node factor of dm/dt and of the Jacobian rows (null: 1 everywhere)
   nmg::TcState tc;              // tensor-core BEM product (bem_precision 3)
+  nmg::Sites sites;             // several materials: the site layout (n_mats == 0: one material)
+  nmg_handle *pot = nullptr;    // several materials: the handle of the potential mesh (owns BEM, CG)
+  bool own_stream = true;       // false: the stream belongs to pot
   nmg::Tape *tape = nullptr;
   int anchor_hold = 0;          // >0: anchored BEM product suspended (RK4 tape runs recompute bit for bit)
   // the mixed-precision CG is used by the forward solves or the adjoint's
@@ -246,6 +268,11 @@ int export_operator(const nmg_handle *h, int which, double coeff, int *rows, int
 // ---- bem_kernels.cu ----
 int fill_bem(nmg_handle *h, std::string &err);
 void bem_gemv(nmg_handle *h, const double *x, double *y);
+// ---- nmg_sites.cu (several materials) ----
+int rhs_eval_sites(nmg_handle *h, const double *d_m, double *d_dmdt);
+int energy_density_sites(nmg_handle *h, const double *d_m, double *d_E5);
+// ---- rhs_kernels.cu: the demag pipeline from W.rho to W.phi (one handle) ----
+int demag_from_rho(nmg_handle *h);
 // ---- bem_tc.cu ----
 int bem_tc_setup(nmg_handle *h, std::string &err);
 int bem_tc(nmg_handle *h, const double *x, double *y, int R);   // Y = B X, R member-major right-hand sides

@@ -315,6 +315,8 @@ struct JvArgs {
   const double *K, *ivol, *mJ, *HJ, *t, *ewt;
   const double *Pinv;   // per node and member: inverse of the 3x3 preconditioner block (row-major)
   const double *pin;    // per-node factor of the Jacobian rows (the pin field) or null
+  const int32_t *site_mat;   // several materials: each site's material (null: one material)
+  const SiteMat *mt;         //   and the materials' coefficients
   double c_exch, C1, C2, gamma, gammap;
   int psolve, scale_out;
   double *out;
@@ -350,11 +352,16 @@ __global__ void k_jv_psolve(JvArgs a) {
     double kv = a.K[k];
     s0 += kv * tj[0]; s1 += kv * tj[1]; s2 += kv * tj[2];
   }
-  const double ce = -a.c_exch * a.ivol[i];
+  double c_exch = a.c_exch, C1 = a.C1, C2 = a.C2;
+  if (a.site_mat) {
+    const SiteMat &c = a.mt[a.site_mat[i]];
+    c_exch = c.c_exch; C1 = c.C1; C2 = c.C2;
+  }
+  const double ce = -c_exch * a.ivol[i];
   const double hv[3] = {ce * s0, ce * s1, ce * s2};
   const double *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g, *w = a.t + 3 * (size_t)g;
   double jw[3];
-  jac_apply(m, H, w, hv, a.C1, a.C2, jw);
+  jac_apply(m, H, w, hv, C1, C2, jw);
   if (a.pin) {
     const double p = a.pin[i];
     jw[0] *= p; jw[1] *= p; jw[2] *= p;
@@ -377,10 +384,15 @@ __global__ void k_jv_psolve(JvArgs a) {
 __global__ void k_pprep(int N, const int32_t *__restrict__ diag_pos, const double *__restrict__ K,
                         const double *__restrict__ vol, const double *__restrict__ mJ, const double *__restrict__ HJ,
                         double c_exch, double C1, double C2, double gammap, double *__restrict__ Pinv, int nrep,
-                        const double *__restrict__ pin) {
+                        const double *__restrict__ pin, const int32_t *__restrict__ site_mat,
+                        const SiteMat *__restrict__ mt) {
   const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (g >= (long long)N * nrep) return;
   const int i = (int)(g % N);
+  if (site_mat) {   // several materials: the site's own coefficients
+    const SiteMat &c = mt[site_mat[i]];
+    c_exch = c.c_exch; C1 = c.C1; C2 = c.C2;
+  }
   const double kap = -c_exch * K[diag_pos[i]] / vol[i];
   const double pf = pin ? pin[i] : 1.0;
   const double *m = mJ + 3 * (size_t)g, *H = HJ + 3 * (size_t)g;
@@ -518,6 +530,8 @@ JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
   JvArgs a;
   a.N = M.N; a.nrep = I.hd->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.ivol = M.ivol;
   a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv; a.pin = I.hd->pin.p;
+  a.site_mat = I.hd->pot ? I.hd->sites.site_mat.p : nullptr;
+  a.mt = I.hd->sites.mtab.p;
   a.c_exch = I.hd->mat.exch_coeff; a.C1 = I.hd->mat.C1; a.C2 = I.hd->mat.C2;
   a.gamma = I.gamma; a.gammap = I.gammap; a.psolve = psolve; a.scale_out = 1; a.out = out;
   return a;
@@ -740,7 +754,7 @@ int nls(Integrator &I, int nflag_first) {
         const nmg_material &mt = I.hd->mat;
         k_pprep<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(
             M.N, M.diag_pos, I.hd->exch_K(), M.vol, I.mJ, I.HJ, mt.exch_coeff, mt.C1, mt.C2, I.gammap, I.Pinv,
-            I.hd->nrep, I.hd->pin.p);
+            I.hd->nrep, I.hd->pin.p, I.hd->pot ? I.hd->sites.site_mat.p : nullptr, I.hd->sites.mtab.p);
         ++I.hd->launches;
       }
     }

@@ -2879,6 +2879,13 @@ void bem_gemm(nmg_handle *h, const double *x, double *y) {
 }
 
 int check_device_error(nmg_handle *h, const char *where) {
+  if (h->pot) {   // several materials: the potential mesh's solves flag their errors there
+    const int rc = check_device_error(h->pot, where);
+    if (rc) {
+      h->last_error = h->pot->last_error;
+      return rc;
+    }
+  }
   int derr = 0;
   cudaError_t e = cudaMemcpyAsync(&derr, h->ws.err.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -2897,18 +2904,18 @@ int check_device_error(nmg_handle *h, const char *where) {
   return 0;
 }
 
-int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
+// The demag pipeline from the charges in W.rho (all members) to the
+// potential W.phi: Neumann solve, boundary gather, BEM product, Dirichlet
+// load and solve, phi = phi1 + phi2 (nmag_lam.py:740-760).
+int demag_from_rho(nmg_handle *h) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   cudaStream_t s = h->stream;
   const int N = M.N;
-  const nmg_material &mt = h->mat;
   const int B = h->nrep;
-  if (h->opt.do_demag && M.nb > 0 && B > 1) {
+  if (B > 1) {
     // ensemble: the same pipeline over B members, kChunk members per CG / BEM launch
     const long long NB = (long long)N * B;
-    k_div<<<nblk(NB, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, h->ep.active ? h->ep.Dx.p : M.D.p, d_m,
-                                        W.rho, B); ++h->launches;
     for (int c0 = 0; c0 < B; c0 += kChunk)
       if (run_cgm(h, 0, c0, W.rho.p + (size_t)c0 * N, W.phi1.p + (size_t)c0 * N, std::min(kChunk, B - c0),
                   h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
@@ -2920,10 +2927,8 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
       if (run_cgm(h, 1, c0, W.rhs2.p + (size_t)c0 * N, W.phi2.p + (size_t)c0 * N, std::min(kChunk, B - c0),
                   h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)) return 100;
     k_add<<<nblk(NB, 256), 256, 0, s>>>((int)NB, W.phi1, W.phi2, W.phi); ++h->launches;
-  } else if (h->opt.do_demag && M.nb > 0) {
+  } else {
     const bool mp = h->opt.cg_precision == 1;   // mixed-precision CG (one member)
-    k_div<<<nblk(N, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx, h->ep.active ? h->ep.Dx.p : M.D.p, d_m,
-                                       W.rho); ++h->launches;
     if (mp ? run_cgm(h, 0, 0, W.rho, W.phi1, 1, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)
            : run_cg(h, 0, W.rho, W.phi1, h->opt.nbc_rtol, h->opt.nbc_atol, h->opt.nbc_maxits)) return 100;
     k_gather_b<<<nblk(M.nb, 256), 256, 0, s>>>(M.nb, M.node_of_b, W.phi1, W.b1); ++h->launches;
@@ -2932,6 +2937,23 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
     if (mp ? run_cgm(h, 1, 0, W.rhs2, W.phi2, 1, h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)
            : run_cg(h, 1, W.rhs2, W.phi2, h->opt.dbc_rtol, h->opt.dbc_atol, h->opt.dbc_maxits)) return 100;
     k_add<<<nblk(N, 256), 256, 0, s>>>(N, W.phi1, W.phi2, W.phi); ++h->launches;
+  }
+  return 0;
+}
+
+int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
+  if (h->pot) return rhs_eval_sites(h, d_m, d_dmdt);   // several materials
+  Mesh &M = h->mesh;
+  Workspace &W = h->ws;
+  cudaStream_t s = h->stream;
+  const int N = M.N;
+  const nmg_material &mt = h->mat;
+  const int B = h->nrep;
+  if (h->opt.do_demag && M.nb > 0) {
+    k_div<<<nblk((long long)N * B, 256), 256, 0, s>>>(N, M.nnz, mt.Ms, M.row_ptr, M.col_idx,
+                                                       h->ep.active ? h->ep.Dx.p : M.D.p, d_m, W.rho, B);
+    ++h->launches;
+    if (demag_from_rho(h)) return 100;
   }
   NodeArgs a;
   a.N = N; a.nnz = M.nnz; a.do_demag = (h->opt.do_demag && M.nb > 0) ? 1 : 0; a.nrep = B;
@@ -2971,6 +2993,7 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
 }
 
 int energy_density(nmg_handle *h, const double *d_m, double *d_E5) {
+  if (h->pot) return energy_density_sites(h, d_m, d_E5);   // several materials
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
   const nmg_material &mt = h->mat;

@@ -22,7 +22,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr"]
 NO_FMA = {"mesh_kernels.cu", "bem_kernels.cu", "adjoint.cu"}
 SOURCES = ["mesh_kernels.cu", "bem_kernels.cu", "rhs_kernels.cu", "nmg_ts.cu", "nmg_api.cu", "nmg_static.cu",
-           "adjoint.cu", "batch.cu", "bem_tc.cu"]
+           "adjoint.cu", "batch.cu", "bem_tc.cu", "nmg_sites.cu"]
 
 
 def nvcc():

@@ -59,7 +59,8 @@ EXPORTS = ["nmg_version", "nmg_set_device", "nmg_last_error", "nmg_create", "nmg
            "nmg_ts_advance", "nmg_max_dm", "nmg_max_dm_step", "nmg_rhs_device", "nmg_bem_apply", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
            "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_bem_anchor_stats", "nmg_max_dm_static",
            "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
-           "nmg_member_averages", "nmg_batch_last_error", "nmg_batch_create", "nmg_batch_destroy", "nmg_batch_info",
+           "nmg_member_averages", "nmg_create_materials", "nmg_site_info", "nmg_set_site_material",
+           "nmg_material_averages", "nmg_batch_last_error", "nmg_batch_create", "nmg_batch_destroy", "nmg_batch_info",
            "nmg_batch_set_m", "nmg_batch_get_m", "nmg_batch_eval", "nmg_batch_run", "nmg_batch_state",
            "nmg_batch_set_schedule", "nmg_batch_autotune"]
 
@@ -116,6 +117,11 @@ def lib(build_if_missing=True):
     L.nmg_max_dm_step.argtypes = [vp, C.POINTER(C.c_double)]
     L.nmg_rhs_device.argtypes = [vp, vp, vp]
     L.nmg_bem_apply.argtypes = [vp, vp, vp, C.c_int]
+    L.nmg_create_materials.argtypes = [_f64p, C.c_int, _i32p, C.c_int, _i32p, C.c_int, _i32p, _i32p, vp, C.c_int,
+                                       C.POINTER(Options), C.POINTER(vp)]
+    L.nmg_site_info.argtypes = [vp, vp, vp]
+    L.nmg_set_site_material.argtypes = [vp, C.c_int, C.POINTER(Material)]
+    L.nmg_material_averages.argtypes = [vp, C.c_int, C.c_int, _f64p, vp]
     L.nmg_rk4_device.argtypes = [vp, vp, C.c_double, C.c_int]
     L.nmg_get_timings.argtypes = [vp, _f64p]
     L.nmg_profile.argtypes = [vp, C.c_int]
@@ -174,6 +180,52 @@ class Engine(object):
         L.nmg_mesh_info(h, info)
         self.N, self.T, self.nnz, self.nb, self.ntri, self.nouter = (int(v) for v in info)
         self.B = max(1, int(options.n_members))   # ensemble members (arrays gain a leading member axis)
+
+    @classmethod
+    def materials(cls, points, simplices, regions, region_materials, materials, options: Options):
+        """Several magnetic materials (nmg_create_materials): regions (T,) of
+        ids 1..R; region_materials[r - 1] lists the material indices region
+        r carries; materials: Material structs.  Per-site arrays then hold
+        one entry per site (self.N sites, material by material)."""
+        L = lib()
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1)
+        sim = np.ascontiguousarray(simplices, dtype=np.int32).reshape(-1)
+        reg = np.ascontiguousarray(regions, dtype=np.int32).reshape(-1)
+        ptr = np.zeros(len(region_materials) + 1, np.int32)
+        for r, ms in enumerate(region_materials):
+            ptr[r + 1] = ptr[r] + len(ms)
+        idx = np.ascontiguousarray([k for ms in region_materials for k in ms], dtype=np.int32)
+        arr = (Material * len(materials))(*materials)
+        h = C.c_void_p()
+        rc = L.nmg_create_materials(pts, len(pts) // 3, sim, len(sim) // 4, reg, len(region_materials), ptr, idx,
+                                    C.cast(arr, C.c_void_p), len(materials), C.byref(options), C.byref(h))
+        if rc != 0:
+            raise NmagGpuError("nmg_create_materials failed (status %d): %s" % (rc, L.nmg_last_error(None).decode()))
+        self = cls.__new__(cls)
+        self.h = h
+        info = np.zeros(6, np.int64)
+        L.nmg_mesh_info(h, info)
+        self.N, self.T, self.nnz, self.nb, self.ntri, self.nouter = (int(v) for v in info)
+        self.B = max(1, int(options.n_members))
+        self.n_materials = len(materials)
+        return self
+
+    def site_info(self):
+        """(site_node, site_material) of a several-materials handle."""
+        node = np.zeros(self.N, np.int32)
+        mat = np.zeros(self.N, np.int32)
+        check(lib().nmg_site_info(self.h, node.ctypes.data, mat.ctypes.data), self.h, "site_info")
+        return node, mat
+
+    def set_site_material(self, k, mat: Material):
+        check(lib().nmg_set_site_material(self.h, int(k), C.byref(mat)), self.h, "set_site_material")
+
+    def material_averages(self, k, member=0, energies=False):
+        a = np.zeros(3)
+        e = np.zeros(5)
+        check(lib().nmg_material_averages(self.h, int(k), int(member), a, e.ctypes.data if energies else None),
+              self.h, "material_averages")
+        return (a, e) if energies else a
 
     def _shape3(self):
         return (self.B, self.N, 3) if self.B > 1 else (self.N, 3)

@@ -4,11 +4,13 @@
  * the CUDA library's parity tests and the timed CPU baseline of bench.py.  Nothing in
  * the product links, imports or calls this code.
  *
- * Parity status: the reference (OCaml + Python 2 + PETSc 2.3.3 + SUNDIALS
- * CVODE 2.3.0) cannot be built or run here, and the reference tree holds no
- * golden vectors for this path, so parity is UNPINNED against reference
- * outputs.  The restatement is pinned instead against known-answer
- * invariants (uniform-m exchange field, cube demag factor 1/3, BEM row sums,
+ * Parity status: the reference as a whole (OCaml + Python 2 + PETSc 2.3.3 +
+ * SUNDIALS CVODE 2.3.0) cannot be built or run here, and the reference tree
+ * holds no golden vectors for this path.  Its one plain-C piece on the path,
+ * the Lindholm stub src/bem3d_stubs.c, is compiled unmodified against a
+ * minimal caml shim (ref_bem_harness.c, oracle/_ref): om_fill_bem equals its
+ * fill bit for bit.  The rest is pinned against known-answer invariants
+ * (uniform-m exchange field, cube demag factor 1/3, BEM row sums,
  * single-spin LLG solution, SI<->su conversions).
  *
  * Every routine cites the reference file:line it restates (paths relative to

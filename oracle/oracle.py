@@ -5,9 +5,12 @@ bench.py's CPU-baseline leg, to produce expected results.  The product never
 imports it.
 
 The oracle restates nsim's LLG right-hand side and CVODE-style integrator on
-the CPU (see nmag_oracle.h for the reference citations).  Parity with the
-reference's own outputs is unpinned (the reference cannot run here and ships
-no golden vectors); known-answer tests pin the restatement instead.
+the CPU (see nmag_oracle.h for the reference citations).  Its BEM fill is
+pinned to the reference's own code: the reference's plain-C Lindholm stub
+(src/bem3d_stubs.c), compiled unmodified against a minimal caml shim into
+_ref/ (ref_bem), fills the same matrix bit for bit.  The rest of the path has
+no compilable reference (OCaml, PETSc, SUNDIALS are absent), so known-answer
+tests pin the restatement there.
 """
 from __future__ import annotations
 

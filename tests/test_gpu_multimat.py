@@ -1,0 +1,170 @@
+"""Several magnetic materials on the GPU (nmg_create_materials) against the
+oracle's multi-material right-hand side (oracle/multimat.py: every material's
+own m on its sites, exchange within a material, charges of all materials on
+one potential; interface/nmag/nmag_lam.py:183-470, 587-606, 734-832).
+
+Poisson solves at 1e-12 on the device (the oracle solves directly), so the
+fields agree to 1e-9 relative (max norm); the BDF trajectory at rtol = atol =
+1e-8 against the oracle's right-hand side integrated by scipy (rtol 1e-11) to
+1e-6."""
+import numpy as np
+import pytest
+
+import nmag
+from nmag import SI
+from nmag.mesh import Mesh, box_mesh
+from nmag.sites import SiteLayer
+from conftest import seeded_m
+
+pytestmark = pytest.mark.gpu
+
+
+def halves():
+    """A 12 x 6 x 4 nm box split at x = 6 nm into regions 1 and 2."""
+    b = box_mesh(6, 3, 2, 2.0)
+    cx = b.points[b.simplices].mean(1)[:, 0]
+    return Mesh(b.points, b.simplices, np.where(cx < 6.0, 1, 2))
+
+
+def two_boxes():
+    a = box_mesh(3, 3, 2, 2.0)
+    b = box_mesh(3, 3, 2, 2.0, origin=(10.0, 0.0, 0.0))
+    pts = np.concatenate([a.points, b.points])
+    sim = np.concatenate([a.simplices, b.simplices + a.n_nodes])
+    reg = np.concatenate([np.ones(a.n_tets, np.int32), np.full(b.n_tets, 2, np.int32)])
+    return Mesh(pts, sim, reg)
+
+
+def materials():
+    py = nmag.MagMaterial("Py", Ms=SI(8.6e5, "A/m"), exchange_coupling=SI(1.3e-11, "J/m"), llg_damping=0.3,
+                          llg_gamma_G=SI(2.211e5, "m/A s"))
+    co = nmag.MagMaterial("Co", Ms=SI(1.4e6, "A/m"), exchange_coupling=SI(3.0e-11, "J/m"), llg_damping=0.1,
+                          llg_gamma_G=SI(2.211e5, "m/A s"),
+                          anisotropy=nmag.uniaxial_anisotropy(axis=[0.0, 0.6, 0.8], K1=SI(5e5, "J/m^3")))
+    return py, co
+
+
+def struct(mat):
+    from nmag import _lib
+    c = mat.coefficients("nmag")
+    mt = _lib.Material()
+    mt.Ms, mt.exch_coeff, mt.C1, mt.C2, mt.C3 = c["Ms"], c["exch_coeff"], c["C1"], c["C2"], c["C3"]
+    mt.K1, mt.anis_coeff, mt.E_coeff_half, mt.E_coeff_ext = c["K1"], c["anis_coeff"], c["E_coeff_half"], c["E_coeff_ext"]
+    for d in range(3):
+        mt.axis[d] = c["axis"][d]
+    return mt
+
+
+def options(B=1, tol=1e-12):
+    from nmag import _lib
+    op = _lib.Options()
+    op.do_demag = 1
+    op.nbc_rtol = op.dbc_rtol = tol
+    op.nbc_atol = op.dbc_atol = 1e-50
+    op.nbc_maxits = op.dbc_maxits = 20000
+    op.n_members = B if B > 1 else 0
+    return op
+
+
+def engine(msh, region_mats, mats, B=1):
+    from nmag import _lib
+    return _lib.Engine.materials(msh.points, msh.simplices, msh.regions, region_mats, [struct(m) for m in mats],
+                                 options(B))
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.mark.parametrize("geometry", ["halves", "two_boxes"])
+def test_fields_match_multimaterial_oracle(geometry):
+    from multimat import MultiOracle
+    msh = halves() if geometry == "halves" else two_boxes()
+    py, co = materials()
+    eng = engine(msh, [[0], [1]], [py, co])
+    L = SiteLayer(msh, [["Py"], ["Co"]])
+    node, mat = eng.site_info()
+    assert eng.N == L.n_sites
+    assert np.array_equal(node, L.site_node) and np.array_equal(mat, L.site_material)
+    mo = MultiOracle(msh.points, msh.simplices, L, {"Py": py.coefficients("nmag"), "Co": co.coefficients("nmag")})
+    h = np.array([0.02, -0.01, 0.03])
+    mo.set_h_ext(h)
+    eng.set_h_ext(h)
+    m = seeded_m(L.n_sites, base=(0.3, 1.0, -0.2), seed=71, noise=0.4)
+    eng.set_m(m)
+    f = eng.eval_fields()
+    d = mo.rhs(m)
+    for key in ("H_exch", "H_anis", "H_demag", "H_total"):
+        assert rel(f[key], mo.fields[key]) < 1e-9, (key, rel(f[key], mo.fields[key]))
+    assert rel(f["dmdt"], d) < 1e-9
+    assert rel(f["rho"], mo.fields["rho_sites"]) < 1e-9
+    assert rel(f["phi"], mo.fields["phi"][L.site_node]) < 1e-9
+    # per-material averages and energies: volume sums over each material's sites
+    E = eng.energy_density()
+    for k, name in enumerate(("Py", "Co")):
+        s = L.sites_of(name)
+        V = np.asarray(eng.csr()[5])[s]
+        a, e = eng.material_averages(k, energies=True)
+        assert np.allclose(a, (m[s] * V[:, None]).sum(0) / V.sum(), rtol=1e-12)
+        assert np.allclose(e[4], (E["E_total"][s] * V).sum(), rtol=1e-12)
+    eng.close()
+
+
+def test_one_material_over_two_regions_equals_the_single_handle():
+    from test_gpu_parity import make_engine
+    msh = halves()
+    py, _ = materials()
+    eng = engine(msh, [[0], [0]], [py])
+    single = make_engine(msh, py)
+    assert eng.N == msh.n_nodes
+    m = seeded_m(msh.n_nodes, seed=72, noise=0.4)
+    for e in (eng, single):
+        e.set_h_ext([0.01, 0.0, -0.02])
+        e.set_m(m)
+    f, g = eng.eval_fields(), single.eval_fields()
+    assert rel(f["dmdt"], g["dmdt"]) < 1e-12
+    eng.close()
+    single.close()
+
+
+def test_bdf_trajectory_matches_multimaterial_oracle():
+    from scipy.integrate import solve_ivp
+    from multimat import MultiOracle
+    msh = halves()
+    py, co = materials()
+    eng = engine(msh, [[0], [1]], [py, co])
+    L = SiteLayer(msh, [["Py"], ["Co"]])
+    mo = MultiOracle(msh.points, msh.simplices, L, {"Py": py.coefficients("nmag"), "Co": co.coefficients("nmag")})
+    h = np.array([0.0, 0.05, 0.0])
+    mo.set_h_ext(h)
+    eng.set_h_ext(h)
+    m0 = seeded_m(L.n_sites, base=(1.0, 0.2, 0.1), seed=73, noise=0.2)
+    eng.set_m(m0)
+    eng.ts_init(0.0, 1e-8, 1e-8, 2, 300)
+    ref = solve_ivp(lambda t, y: mo.rhs(y).reshape(-1), (0.0, 5.0), m0.reshape(-1), method="DOP853",
+                    rtol=1e-11, atol=1e-11, t_eval=[1.0, 2.5, 5.0])
+    for k, t in enumerate((1.0, 2.5, 5.0)):
+        eng.ts_advance(t)
+        diff = np.abs(eng.get_m() - ref.y[:, k].reshape(-1, 3)).max()
+        assert diff < 1e-6, (t, diff)
+    assert np.abs(ref.y[:, -1].reshape(-1, 3) - m0).max() > 1e-2   # the state moved
+    eng.close()
+
+
+def test_ensemble_members_equal_single_multimaterial_handles():
+    msh = halves()
+    py, co = materials()
+    ens = engine(msh, [[0], [1]], [py, co], B=2)
+    S = ens.N
+    ms = np.stack([seeded_m(S, base=(1.0, 0.1 * b, 0.3), seed=80 + b, noise=0.3) for b in range(2)])
+    ens.set_h_ext(np.zeros(3))
+    ens.set_m(ms)
+    f = ens.eval_fields()
+    for b in range(2):
+        one = engine(msh, [[0], [1]], [py, co])
+        one.set_h_ext(np.zeros(3))
+        one.set_m(ms[b])
+        g = one.eval_fields()
+        assert rel(f["dmdt"][b], g["dmdt"]) < 1e-9
+        one.close()
+    ens.close()

@@ -1,8 +1,9 @@
 """Known-answer pins of the CPU oracle (runs on CPU).
 
-The reference cannot run here and ships no golden vectors (parity with its
-outputs is unpinned); these tests pin the oracle against facts that hold for
-the reference's method: closed-form mesh counts, the BEM row-sum identity,
+The reference as a whole cannot run here and ships no golden vectors (its
+plain-C BEM stub is compiled and pins the BEM fill: test_oracle_ref.py);
+these tests pin the rest of the oracle against facts that hold for the
+reference's method: closed-form mesh counts, the BEM row-sum identity,
 Lindholm weights against quadrature, the exchange field of a uniform state,
 the cube's demagnetising factor and the analytic single-spin LLG solution.
 """
