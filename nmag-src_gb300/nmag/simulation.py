@@ -19,6 +19,7 @@ import time as _time
 import numpy as np
 
 from . import mesh as _mesh
+from . import sites as _sites
 from . import si as _si
 from ._lib import Engine, Material, Options, NmagGpuError
 from .material import MagMaterial
@@ -149,6 +150,9 @@ class Simulation(object):
         # FP32 inner CG: damped Jacobi sweeps on each thread block's own rows
         # in its preconditioner (0 or 1: Jacobi alone)
         self.cg_local_sweeps = int(cg_local_sweeps)
+        # several magnetic materials: the site layout (None: one material)
+        self.layer = None
+        self.materials = []
         # ensemble: n_members simulations on one mesh, integrated together;
         # per-node arrays then carry a leading member axis (GB300 extension)
         self.n_members = max(1, int(n_members))
@@ -183,9 +187,17 @@ class Simulation(object):
             mats.extend(mat if isinstance(mat, (list, tuple)) else [mat])
         if not mats:
             raise ValueError("load_mesh: no magnetic material given")
+        # distinct materials in order of appearance; several (or a region with
+        # several) give every material its own m on its sites
+        self.materials = []
+        for mt in mats:
+            if all(mt is not x for x in self.materials):
+                self.materials.append(mt)
         c0 = mats[0].coefficients(self.quirks)
-        if any(mt.coefficients(self.quirks) != c0 for mt in mats[1:]):
-            raise NotImplementedError("one magnetic material (possibly over several regions) is supported on this path")
+        several_in_a_region = any(isinstance(e[1], (list, tuple)) and len(e[1]) > 1 for e in region_names_and_mag_mats)
+        self._multi = several_in_a_region or any(mt.coefficients(self.quirks) != c0 for mt in mats[1:])
+        if not self._multi:
+            self.materials = [mats[0]]
         nreg = int(m.regions.max()) if len(m.regions) else 0
         if nreg != len(region_names_and_mag_mats):   # main.py:1174-1180
             raise ValueError("Found inconsistency between the mesh you loaded and the provided list of "
@@ -222,6 +234,26 @@ class Simulation(object):
         opts.adjoint_cg_precision = {"fp64": 0, "fp32": 1}[self.adjoint_cg_precision]
         opts.anchor_product = {"fp32": 0, "fp16": 1}[self.anchor_product]
         opts.cg_local_sweeps = self.cg_local_sweeps
+        self.layer = None
+        if self._multi:
+            names = [mt.name for mt in self.materials]
+            per_region = [[mt.name for mt in (mat if isinstance(mat, (list, tuple)) else [mat])]
+                          for _, mat in region_names_and_mag_mats]
+            for mt in self.materials:
+                if mt.anisotropy_polynomial(self.quirks) is not None or mt.su_llg_stt_prefactor != 0.0:
+                    raise NotImplementedError("several materials: polynomial anisotropies and spin-transfer "
+                                              "torque are not available (material '%s')" % mt.name)
+            self.layer = _sites.SiteLayer(self.mesh, per_region)
+            self.engine = Engine.materials(self.mesh.points, self.mesh.simplices, self.mesh.regions,
+                                           [[names.index(n) for n in r] for r in per_region],
+                                           [self._material_struct(mt) for mt in self.materials], opts)
+            self._j = None
+            shape = self.engine._shape3()
+            self._m = np.zeros(shape)
+            self.engine.max_dm_step()
+            self._h_ext = np.zeros(shape)
+            self._ts_ready = False
+            return self.mesh
         self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
         poly = self.material.anisotropy_polynomial(self.quirks)
         if poly is not None:
@@ -238,8 +270,8 @@ class Simulation(object):
         self._ts_ready = False
         return self.mesh
 
-    def _material_struct(self):
-        c = self.material.coefficients(self.quirks)
+    def _material_struct(self, material=None):
+        c = (material or self.material).coefficients(self.quirks)
         mt = Material()
         mt.Ms, mt.exch_coeff, mt.C1, mt.C2, mt.C3 = c["Ms"], c["exch_coeff"], c["C1"], c["C2"], c["C3"]
         mt.K1 = c["K1"]
@@ -249,13 +281,37 @@ class Simulation(object):
         return mt
 
     def set_damping(self, llg_damping):
-        """Change the material's damping (e.g. between relax and dynamics)."""
+        """Change the material's damping (e.g. between relax and dynamics);
+        with several materials, every material's."""
+        if self.layer is not None:
+            for k, mt in enumerate(self.materials):
+                mt.set_damping(llg_damping)
+                self.engine.set_site_material(k, self._material_struct(mt))
+            self._ts_ready = False
+            return
         self.material.set_damping(llg_damping)
         self.engine.set_material(self._material_struct())
         self._ts_ready = False
 
     def _positions_si(self):
-        return self.mesh.points * simulation_units.conversion_factor_of(SI("m"))
+        """Positions (m) of the sites: the mesh nodes, or with several
+        materials every material's nodes in site order."""
+        pts = self.mesh.points if self.layer is None else self.mesh.points[self.layer.site_node]
+        return pts * simulation_units.conversion_factor_of(SI("m"))
+
+    def _material_of(self, subfieldname, field):
+        """With several materials: the material named by '<field>_<name>'
+        (None for the bare field name, i.e. every material)."""
+        if self.layer is None or subfieldname in (None, field):
+            return None
+        name = subfieldname[len(field) + 1:]
+        for mt in self.materials:
+            if mt.name == name:
+                return mt
+        raise KeyError("Couldn't find field for subfieldname '%s'" % subfieldname)
+
+    def _sites_of(self, material):
+        return self.layer.sites_of(material.name)
 
     def _vector_values(self, values):
         B = self.n_members
@@ -290,6 +346,12 @@ class Simulation(object):
         if np.any(n == 0.0):
             raise ValueError("set_m: zero-length magnetisation vector")
         m = m / n[..., None]
+        mat = self._material_of(subfieldname, "m") if subfieldname is not None else None
+        if mat is not None:   # only that material's sites change
+            s_ = self._sites_of(mat)
+            full = np.array(self._m, copy=True)
+            full[..., s_, :] = m[..., s_, :]
+            m = full
         self._m = m
         self.engine.set_m(m)
         self._ts_ready = False
@@ -563,11 +625,12 @@ class Simulation(object):
         subfield of this simulation (main.py:612-628)."""
         if subfieldname in self._ON_MESH:
             return subfieldname
+        names = [mt.name for mt in getattr(self, "materials", None) or ([self.material] if self.material else [])]
         for f in self._PER_MATERIAL:
             if subfieldname == f:
                 return f
             if subfieldname.startswith(f + "_"):
-                if self.material is None or subfieldname[len(f) + 1:] != self.material.name:
+                if subfieldname[len(f) + 1:] not in names:
                     break
                 return f
         raise KeyError("Couldn't find field for subfieldname '%s'" % subfieldname)
@@ -577,6 +640,8 @@ class Simulation(object):
         table); m is dimensionless.  (_snap: fields and energy densities of
         one evaluation, for callers reading several subfields.)"""
         field = self._field_of(subfieldname)
+        if self.layer is not None:
+            return self._get_subfield_sites(subfieldname, field, _snap)
         if field == "m":
             return self._m.copy()
         if field == "M":   # M = Ms m (nmag_lam.py:463)
@@ -594,6 +659,38 @@ class Simulation(object):
             return E[field] * _su_factor("E")
         f = _snap["f"] if _snap else self.engine.eval_fields()
         return f[field] * _su_factor(self._KIND[field])
+
+    _VECTOR = ("m", "M", "H_total", "H_exch", "H_anis", "H_demag", "H_ext", "dmdt", "current_density")
+
+    def _get_subfield_sites(self, subfieldname, field, _snap):
+        """Several materials: a per-material subfield on its material's sites
+        (all sites for the bare name); a mesh field on the mesh nodes (the
+        value of each node's first site)."""
+        mat = self._material_of(subfieldname, field) if field in self._PER_MATERIAL else None
+        if field in ("m", "M"):
+            vals = np.array(self._m, copy=True)
+            if field == "M":
+                ms = np.array([mt.coefficients(self.quirks)["Ms"] for mt in self.materials])[self.layer.site_material]
+                vals = vals * ms[:, None] * _su_factor("M")
+        elif field == "H_ext":
+            vals = self._h_ext * _su_factor("H")
+        elif field == "pin":
+            p = getattr(self, "_pin", None)
+            vals = p.copy() if p is not None else np.ones(self.engine.N)
+        elif field == "current_density":   # no spin-transfer torque with several materials: zero
+            vals = np.zeros_like(np.asarray(self._h_ext))
+        elif field.startswith("E_"):
+            E = _snap["E"] if _snap else self.engine.energy_density()
+            vals = E[field] * _su_factor("E")
+        else:
+            f = _snap["f"] if _snap else self.engine.eval_fields()
+            vals = f[field] * _su_factor(self._KIND[field])
+        axis = -2 if field in self._VECTOR else -1
+        if field in self._ON_MESH:   # node values: each node's first site
+            return np.take(vals, self.layer.node_site_idx[self.layer.node_site_ptr[:-1]], axis=axis)
+        if mat is not None:
+            return np.take(vals, self._sites_of(mat), axis=axis)
+        return vals
 
     def _unit_of(self, subfieldname):
         return _FIELD_SI[self._KIND[self._field_of(subfieldname)]]
@@ -686,6 +783,30 @@ class Simulation(object):
         """main.py:2234-2290: volume average of a field in SI numbers (a
         list for vectors); ``subfield`` names the material of per-material
         fields ('m', 'Py' -> m_Py).  Member 0 of an ensemble."""
+        if self.layer is not None:   # several materials: averages over one material's sites
+            names = [mt.name for mt in self.materials]
+            name, base = subfield, field
+            if name is None:
+                for f in self._PER_MATERIAL:
+                    if field.startswith(f + "_") and field[len(f) + 1:] in names:
+                        name, base = field[len(f) + 1:], f
+            if name is not None and name not in names:
+                raise ValueError("You want to compute the average of '%s', but the subfield you specified (%s) is "
+                                 "not one of its subfields" % (field, subfield))
+            if base == "m" and name is not None:
+                return list(self.engine.material_averages(names.index(name)))
+            vals = self.get_subfield(base if name is None else "%s_%s" % (base, name))
+            if self.n_members > 1:
+                vals = vals[0]
+            if name is not None:
+                V = self._volumes()[self.layer.sites_of(name)]
+            elif base in self._ON_MESH:
+                V = self.layer.scatter(self._volumes())   # node volumes: the sum over each node's sites
+            else:
+                V = self._volumes()
+            if vals.ndim == 2:
+                return list((vals * V[:, None]).sum(0) / V.sum())
+            return float((vals * V).sum() / V.sum())
         if subfield is not None and subfield != self.material.name:
             raise ValueError("You want to compute the average of '%s', but the subfield you specified (%s) is "
                              "not one of its subfields" % (field, subfield))
@@ -734,6 +855,8 @@ class Simulation(object):
         f = self.engine.eval_fields()
         E = self.engine.energy_density()
         first = (lambda a: a[0]) if self.n_members > 1 else (lambda a: a)
+        if self.layer is not None:
+            return self._averages_sites(names, units, values, f, E, first)
         m = first(np.asarray(self._m))
         c = self.material.coefficients(self.quirks)
         su = {"m": m, "M": c["Ms"] * m, "H_ext": first(np.asarray(self._h_ext)),
@@ -765,6 +888,48 @@ class Simulation(object):
         cosang = np.clip(np.einsum("ij,ij->i", mn[e[:, 0]], mn[e[:, 1]]), -1.0, 1.0)
         names.append("maxangle_m_%s" % mat); units.append("<deg>")
         values.append(float(np.degrees(np.arccos(cosang.min()))) if len(cosang) else 0.0)
+        lt = _time.localtime()
+        names += ["localtime", "unixtime"]
+        units += ["<>", SI(1.0, "s")]
+        values += ["%04d/%02d/%02d-%02d:%02d:%02d" % lt[:6], _time.time()]
+        return names, values, units
+
+    def _averages_sites(self, names, units, values, f, E, first):
+        """The .ndt row with several materials: every material's columns
+        (averages over its sites with its box volumes, its largest
+        neighbour angle), then the mesh fields over the nodes."""
+        L = self.layer
+        Vs = self._volumes()
+        m = first(np.asarray(self._m))
+        su = {"m": m, "H_ext": first(np.asarray(self._h_ext)), "phi": first(f["phi"]), "rho": first(f["rho"]),
+              "pin": getattr(self, "_pin", None) if getattr(self, "_pin", None) is not None else np.ones(len(m))}
+        ms = np.array([mt.coefficients(self.quirks)["Ms"] for mt in self.materials])[L.site_material]
+        su["M"] = ms[:, None] * m
+        for k in ("H_total", "H_exch", "H_anis", "H_demag", "dmdt"):
+            su[k] = first(f[k])
+        for k in ("E_total", "E_exch", "E_anis", "E_demag", "E_ext"):
+            su[k] = first(E[k])
+
+        def average(a, V, kind):
+            a = np.asarray(a, dtype=np.float64)
+            s_ = (a * V[:, None]).sum(0) if a.ndim == 2 else (a * V).sum()
+            return s_ / V.sum() * (1.0 / simulation_units.of(_FIELD_SI[kind]))
+        for k, mt in enumerate(self.materials):
+            sx = L.sites_of(mt.name)
+            for fname, kind in _NDT_PER_MATERIAL:
+                names.append("%s_%s" % (fname, mt.name)); units.append(_FIELD_SI[kind])
+                values.append(average(su[fname][sx], Vs[sx], kind))
+        first_site = L.node_site_idx[L.node_site_ptr[:-1]]
+        Vn = L.scatter(Vs)
+        for fname, kind in _NDT_MESH:
+            names.append(fname); units.append(_FIELD_SI[kind]); values.append(average(su[fname][first_site], Vn, kind))
+        for k, mt in enumerate(self.materials):   # largest angle between m at the ends of an edge of the material
+            t = L.site_tets[k] + L.offset[k]
+            e = np.concatenate([t[:, [a, b]] for a in range(4) for b in range(a + 1, 4)])
+            mn = m / np.linalg.norm(m, axis=1)[:, None]
+            cosang = np.clip(np.einsum("ij,ij->i", mn[e[:, 0]], mn[e[:, 1]]), -1.0, 1.0)
+            names.append("maxangle_m_%s" % mt.name); units.append("<deg>")
+            values.append(float(np.degrees(np.arccos(cosang.min()))) if len(cosang) else 0.0)
         lt = _time.localtime()
         names += ["localtime", "unixtime"]
         units += ["<>", SI(1.0, "s")]
@@ -815,7 +980,9 @@ class Simulation(object):
         if fields:
             # the reference writes the fields into <name>_dat.h5 (main.py:2527-2534,
             # _save_fields); here one .npz per save, arrays per site in SI
-            names = list(self._PER_MATERIAL) + list(self._ON_MESH) if fields == "all" else (
+            per_mat = list(self._PER_MATERIAL) if self.layer is None else [
+                "%s_%s" % (f, mt.name) for f in self._PER_MATERIAL for mt in self.materials]
+            names = per_mat + list(self._ON_MESH) if fields == "all" else (
                 [fields] if isinstance(fields, str) else list(fields))
             for name in names:
                 self._field_of(name)   # KeyError for unknown fields

@@ -168,3 +168,35 @@ def test_ensemble_members_equal_single_multimaterial_handles():
         assert rel(f["dmdt"][b], g["dmdt"]) < 1e-9
         one.close()
     ens.close()
+
+
+def test_simulation_api_with_two_materials(tmp_path, monkeypatch):
+    """nmag.Simulation with two materials on two regions: m per material,
+    per-material subfields and averages, advance_time, the .ndt row."""
+    monkeypatch.chdir(tmp_path)
+    msh = halves()
+    py, co = materials()
+    sim = nmag.Simulation("two", ksp_tolerances={"NBC.rtol": 1e-10, "DBC.rtol": 1e-10})
+    sim.load_mesh(msh, [("left", py), ("right", co)], unit_length=SI(1e-9, "m"))
+    L = SiteLayer(msh, [["Py"], ["Co"]])
+    assert sim.engine.N == L.n_sites
+    sim.set_m([1.0, 0.0, 0.0])
+    sim.set_m([0.0, 1.0, 0.0], subfieldname="m_Co")
+    assert np.allclose(sim.get_subfield("m_Py"), [1.0, 0.0, 0.0])
+    assert np.allclose(sim.get_subfield("m_Co"), [0.0, 1.0, 0.0])
+    assert np.allclose(sim.get_subfield_average_siv("m", "Co"), [0.0, 1.0, 0.0])
+    assert sim.get_subfield("H_demag").shape == (msh.n_nodes, 3)
+    sim.set_H_ext([0.0, 0.0, 1e5], SI(1.0, "A/m"))
+    t = sim.advance_time(SI(2e-12, "s"))
+    assert abs(t.value - 2e-12) < 1e-24
+    mpy, mco = sim.get_subfield("m_Py"), sim.get_subfield("m_Co")
+    assert np.abs(np.linalg.norm(mpy, axis=1) - 1).max() < 1e-4 and np.abs(np.linalg.norm(mco, axis=1) - 1).max() < 1e-4
+    sim.save_data()
+    header = open("two_dat.ndt").readline()
+    for col in ("m_Py_0", "m_Co_1", "H_demag_0", "maxangle_m_Py", "maxangle_m_Co"):
+        assert col in header
+    sim.set_damping(1.0)
+    sim.relax()   # the default saves: averages and every field at the stage end
+    assert sim.clock.convergence
+    saved = np.load(sorted(tmp_path.glob("two_fields_*.npz"))[-1])
+    assert saved["m_Co"].shape == (len(L.sites_of("Co")), 3) and saved["H_demag"].shape == (msh.n_nodes, 3)

@@ -174,7 +174,8 @@ def test_load_mesh_region_checks_without_gpu():
     a = nmag.MagMaterial("A", Ms=SI(8e5, "A/m"), exchange_coupling=SI(1.3e-11, "J/m"))
     b = nmag.MagMaterial("B", Ms=SI(1e6, "A/m"), exchange_coupling=SI(1.3e-11, "J/m"))
     sim = nmag.Simulation("regions")
-    with pytest.raises(NotImplementedError):
+    # two materials are fine (one m each), but this mesh has one magnetic region
+    with pytest.raises(ValueError):
         sim.load_mesh(shelled, [("a", a), ("b", b)], unit_length=SI(1e-9, "m"))
     two = nmag.mesh.Mesh(shelled.points, shelled.simplices, np.where(shelled.regions == 1, 2, 1))
     with pytest.raises(ValueError):
