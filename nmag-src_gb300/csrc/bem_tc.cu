@@ -33,9 +33,18 @@
 namespace nmg {
 namespace {
 
-constexpr int kTcRows = 128;           // rows of B per CTA (MMA M)
-constexpr int kTcK = 64;               // K entries per stage (one 128-byte swizzle span of BF16)
-constexpr int kKbPerSplit = 16;        // K stages accumulated in TMEM per split (1024 terms)
+// K entries per stage: 64 (rows of 128 bytes, 128-byte swizzle) or, built
+// with -DNMG_TC_KB=32, 32 (64-byte rows and swizzle: half the bytes per
+// stage, so twice the stages fit in shared memory)
+#ifndef NMG_TC_KB
+#define NMG_TC_KB 64
+#endif
+constexpr int kTcRows = 128;                      // rows of B per CTA (MMA M)
+constexpr int kTcK = NMG_TC_KB;
+static_assert(kTcK == 64 || kTcK == 32, "K block of 64 or 32 BF16 entries");
+constexpr int kRowBytes = 2 * kTcK;               // one swizzle span
+constexpr int kKbPerSplit = 1024 / kTcK;          // K stages accumulated in TMEM per split (1024 terms)
+constexpr int kStMul = 64 / kTcK;                 // stages: twice as many with the 32-entry block
 constexpr unsigned long long kTcSpinLimit = 1ull << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -79,13 +88,15 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
       : "memory");
 }
 
-// Shared-memory matrix descriptor of a K-major tile with the 128-byte swizzle
-// (rows of 128 bytes, groups of 8 rows 1024 bytes apart): start address,
-// leading offset 0 (unused for this layout), stride offset 1024 B,
-// the fixed version bits (0b001 at bit 46) and swizzle mode 2 (128 B).
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+// Shared-memory matrix descriptor of a K-major tile with the swizzle of its
+// row length (rows of kRowBytes, groups of 8 rows 8 kRowBytes apart): start
+// address, leading offset 0 (unused for these layouts), stride offset
+// 8 kRowBytes, the fixed version bits (0b001 at bit 46) and the swizzle mode
+// (2: 128 bytes, 4: 64 bytes).
+__device__ __forceinline__ uint64_t desc_sw(uint32_t saddr) {
+  constexpr uint64_t mode = kRowBytes == 128 ? 2 : 4;
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((8 * kRowBytes) >> 4) << 32) | ((uint64_t)1 << 46) |
+         (mode << 61);
 }
 
 // Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16
@@ -180,7 +191,7 @@ __global__ void __launch_bounds__(128, 1)
       if (!mbar_wait(&full[s], (i / ST) & 1, abort_v)) { *abort_v = 1; break; }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       uint64_t da[3], dx[3];
-      for (int p = 0; p < 3; ++p) { da[p] = desc_sw128(smem_u32(tileA(s, p))); dx[p] = desc_sw128(smem_u32(tileX(s, p))); }
+      for (int p = 0; p < 3; ++p) { da[p] = desc_sw(smem_u32(tileA(s, p))); dx[p] = desc_sw(smem_u32(tileX(s, p))); }
 #pragma unroll
       for (int kk = 0; kk < kTcK / 16; ++kk)   // 16 entries (32 bytes) per MMA: +2 in the encoded address
 #pragma unroll
@@ -270,7 +281,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 2D BF16 tensor map over rows x ldk (row-major), box 64 x box_rows, 128-byte swizzle.
+// 2D BF16 tensor map over rows x ldk (row-major), box kTcK x box_rows, swizzled like the tiles.
 bool encode_planes(CUtensorMap *map, void *base, int ldk, int rows, int box_rows) {
   auto fn = encode_fn();
   if (!fn) return false;
@@ -279,8 +290,8 @@ bool encode_planes(CUtensorMap *map, void *base, int ldk, int rows, int box_rows
   const cuuint32_t box[2] = {(cuuint32_t)kTcK, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+            kRowBytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 int nt_for(int R) { return R <= 32 ? 32 : (R <= 64 ? 64 : 128); }
@@ -298,7 +309,7 @@ int bem_tc_setup(nmg_handle *h, std::string &err) {
   TcState &T = h->tc;
   const int nb = M.nb;
   T.Mpad = (nb + kTcRows - 1) / kTcRows * kTcRows;
-  T.ldk = (nb + kTcK - 1) / kTcK * kTcK;
+  T.ldk = (nb + 63) / 64 * 64;   // a whole number of K blocks of either size
   const size_t plane = (size_t)T.Mpad * T.ldk;
   NMG_CUDA_TRY(T.bplanes.alloc(3 * plane), "alloc BF16 BEM planes");
   NMG_CUDA_TRY(cudaMemsetAsync(T.bplanes.p, 0, sizeof(uint16_t) * 3 * plane, h->stream), "zero BF16 planes");
@@ -367,17 +378,17 @@ int bem_tc(nmg_handle *h, const double *x, double *y, int R) {
   {
     NMG_PROF_BEGIN(h, 0);
     if (NT == 32) {
-      const size_t sm = tc_smem<32, 3>();
-      cudaFuncSetAttribute(k_bem_tc<32, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      k_bem_tc<32, 3><<<grid, 128, sm, h->stream>>>(mA, mX, T.Mpad, Rpad, kb_total, T.part, h->ws.err);
+      const size_t sm = tc_smem<32, 3 * kStMul>();
+      cudaFuncSetAttribute(k_bem_tc<32, 3 * kStMul>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_bem_tc<32, 3 * kStMul><<<grid, 128, sm, h->stream>>>(mA, mX, T.Mpad, Rpad, kb_total, T.part, h->ws.err);
     } else if (NT == 64) {
-      const size_t sm = tc_smem<64, 3>();
-      cudaFuncSetAttribute(k_bem_tc<64, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      k_bem_tc<64, 3><<<grid, 128, sm, h->stream>>>(mA, mX, T.Mpad, Rpad, kb_total, T.part, h->ws.err);
+      const size_t sm = tc_smem<64, 3 * kStMul>();
+      cudaFuncSetAttribute(k_bem_tc<64, 3 * kStMul>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_bem_tc<64, 3 * kStMul><<<grid, 128, sm, h->stream>>>(mA, mX, T.Mpad, Rpad, kb_total, T.part, h->ws.err);
     } else {
-      const size_t sm = tc_smem<128, 2>();
-      cudaFuncSetAttribute(k_bem_tc<128, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      k_bem_tc<128, 2><<<grid, 128, sm, h->stream>>>(mA, mX, T.Mpad, Rpad, kb_total, T.part, h->ws.err);
+      const size_t sm = tc_smem<128, 2 * kStMul>();
+      cudaFuncSetAttribute(k_bem_tc<128, 2 * kStMul>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      k_bem_tc<128, 2 * kStMul><<<grid, 128, sm, h->stream>>>(mA, mX, T.Mpad, Rpad, kb_total, T.part, h->ws.err);
     }
     ++h->launches;
     NMG_PROF_END(h);
