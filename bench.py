@@ -782,9 +782,9 @@ def run_adjoint_report(args):
     # finite differences on a shorter trajectory
     fd_steps = args.adj_fd_steps
     _, gM2, gK2, gP2 = run(Ms_T, K1_T, pulses, fd_steps, True)
-    h = 1e-6
+    h = args.adj_h
     rng = np.random.default_rng(11)
-    errs = []
+    errs, pairs = [], []
     for _ in range(args.adj_dirs):
         dM = Ms_T * rng.standard_normal(T)
         dK = 0.05 * rng.standard_normal(T)
@@ -794,6 +794,7 @@ def run_adjoint_report(args):
         fd = (lp - lm) / (2 * h)
         ad = gM2 @ dM + gK2 @ dK + (gP2 * dP).sum()
         errs.append(abs(fd - ad) / max(abs(ad), 1e-30))
+        pairs.append([float(fd), float(ad)])
     line = {"metric": "forward + adjoint wall time", "report": "adjoint", "value": wall, "unit": "s",
             "higher_is_better": False, "workload": WORKLOAD_NAMES[args.workload],
             "trajectory": {"steps": nsteps, "dt_ps": dt, "checkpoint_every": ckpt, "pulses": 20,
@@ -806,7 +807,7 @@ def run_adjoint_report(args):
             "sim_ps_per_s": nsteps * dt / wall,
             "forward_form": {"bem": args.adj_form, "cg": args.adj_cg}, "backward_cg": args.adj_bwd_cg,
             "poisson_rtol": args.adj_ksp,
-            "fd_check": {"steps": fd_steps, "directions": len(errs), "h_rel": h,
+            "fd_check": {"steps": fd_steps, "directions": len(errs), "h_rel": h, "fd_ad_pairs": pairs,
                          "max_rel_err": max(errs) if errs else None, "bound": 1e-5},
             "gpu_launches": launches}
     print(json.dumps(line))
@@ -1055,7 +1056,7 @@ def main():
                          "in tensor-core fragment order")
     ap.add_argument("--cg-sweeps", type=int, default=0,
                     help="FP32 inner CG: damped Jacobi sweeps on each block's rows in the preconditioner")
-    ap.add_argument("--anchor", type=float, default=3e-3,
+    ap.add_argument("--anchor", type=float, default=1e-2,
                     help="fp32x2: anchored product tolerance (B x = B x0 + B32 (x - x0) while the max-norm drift "
                          "of x from x0 stays below it; 0 = off)")
     ap.add_argument("--members", type=int, default=8,
@@ -1063,6 +1064,7 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=2000)
     ap.add_argument("--adj-fd-steps", type=int, default=100)
     ap.add_argument("--adj-dirs", type=int, default=32)
+    ap.add_argument("--adj-h", type=float, default=1e-6, help="relative step of the central differences")
     ap.add_argument("--adj-ksp", type=float, default=1e-12,
                     help="Poisson solves' rtol in the differentiation report (the finite differences at "
                          "h = 1e-6 need the loss accurate well beyond 1e-6 relative)")

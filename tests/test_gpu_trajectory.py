@@ -21,7 +21,7 @@ the integrators.
   removes the seeded noise's spin waves), then alpha 0.02 and
   mu0 H = (-24.6, 4.3, 0) mT.  From those states the plain FP64 path and the
   chosen form (8 members in one ensemble: compensated BEM product anchored
-  at 3e-3 with FP32 difference products, FP32 CG with FP64 refinement) run
+  at 1e-2 with FP32 difference products, FP32 CG with FP64 refinement) run
   50 ps with m(t) and <m>(t) every 1 ps and the energies every 10 ps, each
   member against an oracle run from its own state: member 0 over the 50 ps,
   members 1-7 over their first 10 ps.
@@ -107,7 +107,7 @@ def film_setup():
     N = len(film.points)
     B = 8
     seeds = [seeded_m(N, base=(1.0, 0.25, 0.1), seed=1 + b) for b in range(B)]
-    ens, single = make_ensemble(film, permalloy(1.0), B, tol=1e-8, bem_precision=2, cg_precision=1, anchor=3e-3)
+    ens, single = make_ensemble(film, permalloy(1.0), B, tol=1e-8, bem_precision=2, cg_precision=1, anchor=1e-2)
     single.close()
     ens.set_h_ext(np.zeros(3))
     ens.set_m(np.stack(seeds))
