@@ -33,11 +33,11 @@
 namespace nmg {
 namespace {
 
-// K entries per stage: 64 (rows of 128 bytes, 128-byte swizzle) or, built
-// with -DNMG_TC_KB=32, 32 (64-byte rows and swizzle: half the bytes per
-// stage, so twice the stages fit in shared memory)
+// K entries per stage: 32 (rows of 64 bytes, 64-byte swizzle: 4-6 stages
+// fit in shared memory; 0.532 ms per 128-vector film product) or, built with
+// -DNMG_TC_KB=64, 64 (128-byte rows and swizzle, half as many stages; 0.568 ms)
 #ifndef NMG_TC_KB
-#define NMG_TC_KB 64
+#define NMG_TC_KB 32
 #endif
 constexpr int kTcRows = 128;                      // rows of B per CTA (MMA M)
 constexpr int kTcK = NMG_TC_KB;
