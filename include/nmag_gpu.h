@@ -225,6 +225,15 @@ int nmg_create_materials(const double *coords, int n_nodes, const int32_t *tets,
                          const int32_t *tet_region, int n_regions, const int32_t *region_ptr,
                          const int32_t *region_mats, const nmg_material *mats, int n_mats,
                          const nmg_options *opt, nmg_handle **out);
+/* Local magnetic coupling between two materials whose sites share nodes
+ * (two magnetic species in one crystal, e.g. the sublattices of DyFe2):
+ * replaces Simulation.set_local_magnetic_coupling (main.py:1234-1263) and
+ * its generated local equations (nmag_lam.py:16-62).  At every node that
+ * carries both, H_lc of mat1 gains h_coeff m_mat2 (added to H_total) and
+ * E_lc of mat1 gains e_coeff m_mat1 . m_mat2 (added to E_total); call it
+ * once per ordered pair.  The timestepper's Jacobian leaves it out, as the
+ * reference's does. */
+int nmg_set_local_coupling(nmg_handle *h, int mat1, int mat2, double h_coeff, double e_coeff);
 /* The mesh node and the material of every site (n_sites entries each). */
 int nmg_site_info(const nmg_handle *h, int32_t *site_node, int32_t *site_material);
 /* Change material k's constants (e.g. its damping between relax and dynamics). */

@@ -144,6 +144,11 @@ struct Sites {
   DevBuf<int32_t> site_node, site_mat; // per site: node of the magnetic mesh, material
   DevBuf<int32_t> node_ptr, node_sites; // node -> its sites (CSR, sites ascending)
   DevBuf<SiteMat> mtab;                // per material
+  // local magnetic coupling between materials sharing a node (nmag_lam.py:
+  // 16-62): lc[2 (X n_mats + Y)] = the field coefficient of m_Y in H_lc_X,
+  // lc[... + 1] the energy coefficient of m_X . m_Y in E_lc_X (null: none)
+  std::vector<double> lc_host;
+  DevBuf<double> lc;
 };
 
 struct Integrator;

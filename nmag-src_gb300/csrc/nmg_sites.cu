@@ -24,6 +24,7 @@
 // V_s, uniaxial anisotropy of X, H_total = ((H_ext + H_exch) + H_anis) +
 // H_demag and the LLG equation with X's coefficients (nmag_lam.py:377-430).
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -79,9 +80,26 @@ struct SiteArgs {
   const double *G, *pivol, *phi;
   const int32_t *site_node, *site_mat;
   const SiteMat *mt;
+  const int32_t *node_ptr, *node_sites;       // node -> sites, for the local coupling
+  const double *lc;                           // local coupling coefficients or null
+  int n_mats;
   const double *m, *h_ext, *pin;
   double *h_exch, *h_demag, *h_anis, *h_total, *dmdt;
 };
+
+// H_lc of site s (material X at node i): sum over the node's other sites s'
+// (material Y) of lc[X][Y] m_s' (nmag_lam.py:16-62, "have_m_Y" = node i
+// carries a site of Y).
+__device__ __forceinline__ void local_coupling(const SiteArgs &a, int s, int X, const double *mm, double *hl) {
+  const int i = a.site_node[s];
+  for (int k = a.node_ptr[i]; k < a.node_ptr[i + 1]; ++k) {
+    const int s2 = a.node_sites[k];
+    if (s2 == s) continue;
+    const double c = a.lc[2 * (X * a.n_mats + a.site_mat[s2])];
+    const double *m2 = mm + 3 * (size_t)s2;
+    hl[0] += c * m2[0]; hl[1] += c * m2[1]; hl[2] += c * m2[2];
+  }
+}
 
 __global__ void k_heff_llg_sites(SiteArgs a) {
   const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -120,6 +138,11 @@ __global__ void k_heff_llg_sites(SiteArgs a) {
   const double *he = a.h_ext + 3 * (size_t)g;
   double H[3];
   for (int d = 0; d < 3; ++d) H[d] = ((he[d] + hx[d]) + ha[d]) + hd[d];
+  if (a.lc) {   // H_total = ... + H_lc (nmag_lam.py:404)
+    double hl[3] = {0.0, 0.0, 0.0};
+    local_coupling(a, s, a.site_mat[s], mm, hl);
+    for (int d = 0; d < 3; ++d) H[d] += hl[d];
+  }
   const double mxH[3] = {m[1] * H[2] - m[2] * H[1], m[2] * H[0] - m[0] * H[2], m[0] * H[1] - m[1] * H[0]};
   const double mxmxH[3] = {m[1] * mxH[2] - m[2] * mxH[1], m[2] * mxH[0] - m[0] * mxH[2],
                            m[0] * mxH[1] - m[1] * mxH[0]};
@@ -140,10 +163,13 @@ __global__ void k_heff_llg_sites(SiteArgs a) {
 // Energy densities per site with the site's material (nmag_lam.py:454-460).
 __global__ void k_energy_sites(long long SB, int S, const SiteMat *__restrict__ mt, const int32_t *__restrict__ site_mat,
                                const double *__restrict__ m, const double *__restrict__ hx,
-                               const double *__restrict__ hd, const double *__restrict__ he, double *__restrict__ E) {
+                               const double *__restrict__ hd, const double *__restrict__ he, double *__restrict__ E,
+                               const int32_t *__restrict__ site_node, const int32_t *__restrict__ node_ptr,
+                               const int32_t *__restrict__ node_sites, const double *__restrict__ lc, int n_mats) {
   const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (g >= SB) return;
-  const SiteMat c = mt[site_mat[g % S]];
+  const int s = (int)(g % S), X = site_mat[s];
+  const SiteMat c = mt[X];
   const double *mi = m + 3 * (size_t)g, *x = hx + 3 * (size_t)g, *d = hd + 3 * (size_t)g, *e = he + 3 * (size_t)g;
   const double ex = c.E_half * ((mi[0] * x[0] + mi[1] * x[1]) + mi[2] * x[2]);
   const double dm = c.E_half * ((mi[0] * d[0] + mi[1] * d[1]) + mi[2] * d[2]);
@@ -153,8 +179,19 @@ __global__ void k_energy_sites(long long SB, int S, const SiteMat *__restrict__ 
     const double am = (c.ax * mi[0] + c.ay * mi[1]) + c.az * mi[2];
     an = -c.K1 * am * am;
   }
+  double el = 0.0;   // E_lc = sum over the node's other sites of lc_e[X][Y] m_X . m_Y, added to E_total
+  if (lc) {
+    const double *mb = m + 3 * (size_t)(g - s);
+    const int i = site_node[s];
+    for (int k = node_ptr[i]; k < node_ptr[i + 1]; ++k) {
+      const int s2 = node_sites[k];
+      if (s2 == s) continue;
+      const double *m2 = mb + 3 * (size_t)s2;
+      el += lc[2 * (X * n_mats + site_mat[s2]) + 1] * ((mi[0] * m2[0] + mi[1] * m2[1]) + mi[2] * m2[2]);
+    }
+  }
   E[g] = ex; E[SB + g] = dm; E[2 * SB + g] = ez; E[3 * SB + g] = an;
-  E[4 * SB + g] = ((dm + ex) + ez) + an;
+  E[4 * SB + g] = (((dm + ex) + ez) + an) + el;
 }
 
 // Block partials over sites [s0, s0 + n) of member b: V, V m (3), V E_k (5).
@@ -220,6 +257,8 @@ int rhs_eval_sites(nmg_handle *h, const double *d_m, double *d_dmdt) {
   a.prow = P->mesh.row_ptr; a.pcol = P->mesh.col_idx; a.G = P->mesh.G; a.pivol = P->mesh.ivol;
   a.phi = demag ? P->ws.phi.p : nullptr;
   a.site_node = h->sites.site_node; a.site_mat = h->sites.site_mat; a.mt = h->sites.mtab;
+  a.node_ptr = h->sites.node_ptr; a.node_sites = h->sites.node_sites; a.lc = h->sites.lc.p;
+  a.n_mats = h->sites.n_mats;
   a.m = d_m; a.h_ext = W.h_ext; a.pin = h->pin.p;
   a.h_exch = W.h_exch; a.h_demag = W.h_demag; a.h_anis = W.h_anis; a.h_total = W.h_total;
   a.dmdt = d_dmdt ? d_dmdt : W.dmdt.p;
@@ -237,7 +276,9 @@ int energy_density_sites(nmg_handle *h, const double *d_m, double *d_E5) {
   Workspace &W = h->ws;
   const long long SB = (long long)h->mesh.N * h->nrep;
   k_energy_sites<<<nblk_s(SB, 256), 256, 0, h->stream>>>(SB, h->mesh.N, h->sites.mtab, h->sites.site_mat, d_m,
-                                                          W.h_exch, W.h_demag, W.h_ext, d_E5);
+                                                          W.h_exch, W.h_demag, W.h_ext, d_E5, h->sites.site_node,
+                                                          h->sites.node_ptr, h->sites.node_sites, h->sites.lc.p,
+                                                          h->sites.n_mats);
   ++h->launches;
   return cudaGetLastError() == cudaSuccess ? 0 : 100;
 }
@@ -380,6 +421,25 @@ int nmg_set_site_material(nmg_handle *h, int material, const nmg_material *mat) 
       cudaStreamSynchronize(h->stream) != cudaSuccess)
     return 100;
   if (material == 0) h->mat = *mat;
+  h->ts_ready = 0;
+  return 0;
+}
+
+int nmg_set_local_coupling(nmg_handle *h, int mat1, int mat2, double h_coeff, double e_coeff) {
+  if (!h) return -1;
+  if (!h->pot) return -2;
+  const int n = h->sites.n_mats;
+  if (mat1 < 0 || mat1 >= n || mat2 < 0 || mat2 >= n || mat1 == mat2) return -2;
+  if (!std::isfinite(h_coeff) || !std::isfinite(e_coeff)) return -5;
+  nmg::Sites &St = h->sites;
+  if (St.lc_host.empty()) St.lc_host.assign(2 * (size_t)n * n, 0.0);
+  St.lc_host[2 * ((size_t)mat1 * n + mat2)] = h_coeff;
+  St.lc_host[2 * ((size_t)mat1 * n + mat2) + 1] = e_coeff;
+  if (!St.lc.p && St.lc.alloc(St.lc_host.size()) != cudaSuccess) return 100;
+  if (cudaMemcpyAsync(St.lc.p, St.lc_host.data(), sizeof(double) * St.lc_host.size(), cudaMemcpyHostToDevice,
+                      h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return 100;
   h->ts_ready = 0;
   return 0;
 }

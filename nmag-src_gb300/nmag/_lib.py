@@ -59,7 +59,7 @@ EXPORTS = ["nmg_version", "nmg_set_device", "nmg_last_error", "nmg_create", "nmg
            "nmg_ts_advance", "nmg_max_dm", "nmg_max_dm_step", "nmg_rhs_device", "nmg_bem_apply", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
            "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_bem_anchor_stats", "nmg_max_dm_static",
            "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
-           "nmg_member_averages", "nmg_create_materials", "nmg_site_info", "nmg_set_site_material",
+           "nmg_member_averages", "nmg_create_materials", "nmg_site_info", "nmg_set_site_material", "nmg_set_local_coupling",
            "nmg_material_averages", "nmg_batch_last_error", "nmg_batch_create", "nmg_batch_destroy", "nmg_batch_info",
            "nmg_batch_set_m", "nmg_batch_get_m", "nmg_batch_eval", "nmg_batch_run", "nmg_batch_state",
            "nmg_batch_set_schedule", "nmg_batch_autotune"]
@@ -121,6 +121,7 @@ def lib(build_if_missing=True):
                                        C.POINTER(Options), C.POINTER(vp)]
     L.nmg_site_info.argtypes = [vp, vp, vp]
     L.nmg_set_site_material.argtypes = [vp, C.c_int, C.POINTER(Material)]
+    L.nmg_set_local_coupling.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double]
     L.nmg_material_averages.argtypes = [vp, C.c_int, C.c_int, _f64p, vp]
     L.nmg_rk4_device.argtypes = [vp, vp, C.c_double, C.c_int]
     L.nmg_get_timings.argtypes = [vp, _f64p]
@@ -219,6 +220,11 @@ class Engine(object):
 
     def set_site_material(self, k, mat: Material):
         check(lib().nmg_set_site_material(self.h, int(k), C.byref(mat)), self.h, "set_site_material")
+
+    def set_local_coupling(self, k1, k2, h_coeff, e_coeff):
+        """H_lc of material k1 gains h_coeff m_k2, E_lc gains e_coeff m_k1 . m_k2 (shared nodes)."""
+        check(lib().nmg_set_local_coupling(self.h, int(k1), int(k2), float(h_coeff), float(e_coeff)), self.h,
+              "set_local_coupling")
 
     def material_averages(self, k, member=0, energies=False):
         a = np.zeros(3)

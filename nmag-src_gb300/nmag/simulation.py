@@ -280,6 +280,32 @@ class Simulation(object):
         mt.anis_coeff, mt.E_coeff_half, mt.E_coeff_ext = c["anis_coeff"], c["E_coeff_half"], c["E_coeff_ext"]
         return mt
 
+    def set_local_magnetic_coupling(self, mat1, mat2, coupling):
+        """main.py:1234-1263: couple the magnetisations of two materials
+        whose sites share nodes (two species in one crystal).  coupling: an
+        SI value in units of mu0 (or a pair, one per direction); H_lc of mat1
+        gains (coupling/mu0) Ms_2 m_2, its energy density
+        (coupling/mu0) (mu0 Ms_1 Ms_2 / 2) m_1 . m_2, and the other way round."""
+        if self.layer is None:
+            raise KeyError("set_local_magnetic_coupling: the simulation has one material")
+        names = [mt.name for mt in self.materials]
+        if mat1.name not in names or mat2.name not in names or mat1.name == mat2.name:
+            raise ValueError("set_local_magnetic_coupling: two different materials of the simulation")
+        done = getattr(self, "_couplings", set())
+        if (mat1.name, mat2.name) in done or (mat2.name, mat1.name) in done:
+            raise ValueError("A coupling %s-%s has been already specified!" % (mat1.name, mat2.name))
+        pair = coupling if isinstance(coupling, (list, tuple)) else (coupling, coupling)
+        c1, c2 = (float((x / _si.mu0).value) if isinstance(x, SI) else float(x) for x in pair)
+        en_dens = simulation_units.of(0.5 * _si.mu0 * mat1.Ms * mat2.Ms, compatible_with=SI("J/m^3"))
+        Ms1 = simulation_units.of(mat1.Ms, compatible_with=SI("A/m"))
+        Ms2 = simulation_units.of(mat2.Ms, compatible_with=SI("A/m"))
+        k1, k2 = names.index(mat1.name), names.index(mat2.name)
+        self.engine.set_local_coupling(k1, k2, c1 * Ms2, en_dens * c1)
+        self.engine.set_local_coupling(k2, k1, c2 * Ms1, en_dens * c2)
+        done.add((mat1.name, mat2.name))
+        self._couplings = done
+        self._ts_ready = False
+
     def set_damping(self, llg_damping):
         """Change the material's damping (e.g. between relax and dynamics);
         with several materials, every material's."""

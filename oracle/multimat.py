@@ -61,6 +61,12 @@ class MultiOracle(object):
             om = oracle.OracleMesh(p, t, fill_bem=False)
             self.sub[name] = (om, _csr(om, om.K), [_csr(om, om.D[d]) for d in range(3)])
         self.h_ext = np.zeros((self.N, 3))
+        self.local_couplings = {}
+
+    def set_local_coupling(self, name1, name2, h_coeff, e_coeff):
+        """H_lc of name1 gains h_coeff m_name2 at the nodes carrying both
+        (nmag_lam.py:16-62); its energy density e_coeff m_name1 . m_name2."""
+        self.local_couplings[(name1, name2)] = (h_coeff, e_coeff)
 
     def set_h_ext(self, h):
         self.h_ext = np.broadcast_to(np.asarray(h, dtype=np.float64), (self.N, 3)).copy()
@@ -108,6 +114,22 @@ class MultiOracle(object):
             H_exch[s] = -c["exch_coeff"] * (K @ m[s]) / om.vol[:, None]
             H_anis[s] = self._anis(c, m[s])
         H_total = ((L.gather(self.h_ext) + H_exch) + H_anis) + L.gather(hd)
+        # local couplings: at every node, each site's H_lc from the node's other sites
+        H_lc = np.zeros_like(m)
+        E_lc = np.zeros(L.n_sites)
+        if self.local_couplings:
+            names = L.materials
+            for i in range(self.N):
+                sites = L.node_site_idx[L.node_site_ptr[i]:L.node_site_ptr[i + 1]]
+                for s1 in sites:
+                    for s2 in sites:
+                        if s1 == s2:
+                            continue
+                        c = self.local_couplings.get((names[L.site_material[s1]], names[L.site_material[s2]]))
+                        if c is not None:
+                            H_lc[s1] += c[0] * m[s2]
+                            E_lc[s1] += c[1] * float(m[s1] @ m[s2])
+            H_total = H_total + H_lc
         dmdt = np.zeros_like(m)
         for name in L.materials:
             s = L.sites_of(name)
@@ -116,5 +138,5 @@ class MultiOracle(object):
             mxH = np.cross(ms, H)
             dmdt[s] = (c["C1"] * mxH + c["C2"] * np.cross(ms, mxH)) + (c["C3"] * (1.0 - np.sum(ms * ms, 1)))[:, None] * ms
         self.fields = {"rho": rho, "rho_sites": rho_s, "phi": phi, "H_demag": hd, "H_exch": H_exch,
-                       "H_anis": H_anis, "H_total": H_total, "dmdt": dmdt}
+                       "H_anis": H_anis, "H_total": H_total, "dmdt": dmdt, "H_lc": H_lc, "E_lc": E_lc}
         return dmdt

@@ -220,3 +220,77 @@ def test_simulation_api_with_two_materials(tmp_path, monkeypatch):
     assert sim.clock.convergence
     saved = np.load(sorted(tmp_path.glob("two_fields_*.npz"))[-1])
     assert saved["m_Co"].shape == (len(L.sites_of("Co")), 3) and saved["H_demag"].shape == (msh.n_nodes, 3)
+
+
+def test_local_coupling_matches_oracle():
+    """Two species on the same nodes (region 1 carries A and B, region 2
+    only B) coupled locally (nmag_lam.py:16-62): H_lc of each species from
+    the other's m at the shared nodes, in H_total and dm/dt against the
+    oracle (1e-9); the energy density's E_lc against the oracle's."""
+    from multimat import MultiOracle
+    msh = halves()
+    a = nmag.MagMaterial("A", Ms=SI(6e5, "A/m"), exchange_coupling=SI(1.0e-11, "J/m"), llg_damping=0.2,
+                         llg_gamma_G=SI(2.211e5, "m/A s"))
+    b = nmag.MagMaterial("B", Ms=SI(1.0e6, "A/m"), exchange_coupling=SI(1.5e-11, "J/m"), llg_damping=0.2,
+                         llg_gamma_G=SI(2.211e5, "m/A s"))
+    L = SiteLayer(msh, [["A", "B"], ["B"]])
+    coup = {("A", "B"): (-0.3, -0.12), ("B", "A"): (-0.2, -0.08)}
+    engs = []
+    for couple in (False, True):
+        e = engine(msh, [[0, 1], [1]], [a, b])
+        if couple:
+            for (x, y), (hc, ec) in coup.items():
+                e.set_local_coupling("AB".index(x), "AB".index(y), hc, ec)
+        engs.append(e)
+    mo = MultiOracle(msh.points, msh.simplices, L, {"A": a.coefficients("nmag"), "B": b.coefficients("nmag")})
+    for (x, y), (hc, ec) in coup.items():
+        mo.set_local_coupling(x, y, hc, ec)
+    m = seeded_m(L.n_sites, base=(0.2, 1.0, 0.4), seed=91, noise=0.5)
+    h = np.array([0.01, 0.0, -0.02])
+    mo.set_h_ext(h)
+    for e in engs:
+        e.set_h_ext(h)
+        e.set_m(m)
+    f0, f = engs[0].eval_fields(), engs[1].eval_fields()
+    d = mo.rhs(m)
+    assert np.abs(mo.fields["H_lc"]).max() > 0.05   # the coupling is felt
+    assert rel(f["H_total"], mo.fields["H_total"]) < 1e-9
+    assert rel(f["dmdt"], d) < 1e-9
+    assert np.abs((f["H_total"] - f0["H_total"]) - mo.fields["H_lc"]).max() < 1e-12
+    E0, E1 = engs[0].energy_density()["E_total"], engs[1].energy_density()["E_total"]
+    assert np.abs((E1 - E0) - mo.fields["E_lc"]).max() < 1e-12
+    for e in engs:
+        e.close()
+
+
+def test_simulation_local_magnetic_coupling(tmp_path, monkeypatch):
+    """Simulation.set_local_magnetic_coupling (main.py:1234-1263) on two
+    species sharing region 1: the coefficients reach the device (the H_total
+    difference from an uncoupled run is the coupling field) and the
+    dynamics run."""
+    monkeypatch.chdir(tmp_path)
+    msh = halves()
+    a = nmag.MagMaterial("A", Ms=SI(6e5, "A/m"), exchange_coupling=SI(1.0e-11, "J/m"), llg_damping=0.2)
+    b = nmag.MagMaterial("B", Ms=SI(1.0e6, "A/m"), exchange_coupling=SI(1.5e-11, "J/m"), llg_damping=0.2)
+    sims = []
+    for couple in (False, True):
+        sim = nmag.Simulation("lc%d" % couple, ksp_tolerances={"NBC.rtol": 1e-12, "DBC.rtol": 1e-12})
+        sim.load_mesh(msh, [("r1", [a, b]), ("r2", b)], unit_length=SI(1e-9, "m"))
+        if couple:
+            sim.set_local_magnetic_coupling(a, b, SI(-0.5e-6, "N/A^2"))
+            with pytest.raises(ValueError):
+                sim.set_local_magnetic_coupling(b, a, SI(-0.5e-6, "N/A^2"))
+        sim.set_m([1.0, 0.2, 0.0], subfieldname="m_A")
+        sim.set_m([-0.3, 1.0, 0.1], subfieldname="m_B")
+        sims.append(sim)
+    L = SiteLayer(msh, [["A", "B"], ["B"]])
+    mA = sims[1].get_subfield("m_A")
+    dH = sims[1].get_subfield("H_total_A") - sims[0].get_subfield("H_total_A")
+    nodeB = {L.site_node[s]: k for k, s in enumerate(L.sites_of("B"))}
+    mB = sims[1].get_subfield("m_B")
+    c = (-0.5e-6 / (4e-7 * np.pi)) * 1.0e6   # (coupling / mu0) Ms_B in A/m per unit m_B
+    exp = np.array([c * mB[nodeB[L.site_node[s]]] for s in L.sites_of("A")])
+    assert np.abs(dH - exp).max() <= 1e-9 * np.abs(exp).max()
+    t = sims[1].advance_time(SI(1e-12, "s"))
+    assert abs(t.value - 1e-12) < 1e-24
+    assert np.abs(np.linalg.norm(sims[1].get_subfield("m_A"), axis=1) - 1).max() < 1e-4
