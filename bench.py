@@ -334,7 +334,7 @@ def relax_states(args, form, cg, B, msh, base, seed, anchor):
 
 
 def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anchor=0.0, warmup=None,
-            e2e=True):
+            e2e=True, jacobian="approximate"):
     """One form on the workload from the relaxed states `start`: alpha =
     0.02 and the applied field; W untimed warm-up steps, then the state is
     put back and K timed steps run on the device-resident engine (value:
@@ -347,7 +347,8 @@ def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anc
     import nmag
     from nmag import SI
     sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor,
-                          anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps)
+                          anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps,
+                          jacobian=jacobian, jacobian_demag_rtol=args.jac_rtol)
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     sim.set_H_ext(h_ext_su() * 1e6, SI(1.0, "A/m"))
@@ -511,6 +512,7 @@ def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anc
         "e2e": sim_ns_total / wall_e2e if wall_e2e else None,
         "ms_per_step": dev_s * 1e3 / args.steps, "rhs_evals": st["nfe"] - st0["nfe"],
         "bdf_steps": st["nst"] - st0["nst"], "rhs_evals_per_s": (st["nfe"] - st0["nfe"]) / dev_s * world,
+        "newton": {k: st[k] - st0[k] for k in ("nni", "nli", "ncfn", "netf", "njv", "npe")},
         "wall_value_s": wall_value, "roofline": roof, "launches": launches, "clocks": clocks,
         "kernels_ms": {k: {"launches": v[0], "total_ms": v[1]} for k, v in prof.items()},
         "cg_iterations": {"neumann": cg1[0] - cg0[0], "dirichlet": cg1[1] - cg0[1]},
@@ -824,6 +826,42 @@ def run_adjoint_report(args):
     print(json.dumps(line))
 
 
+def run_jacobian_report(args):
+    """The BDF's Newton matrix at each Jacobian level on the workload's
+    chosen form: the reference's approximate Jacobian (exchange only), the
+    local terms added, and the exact one (the demag response of every Krylov
+    direction from its own Poisson solves at --jac-rtol).  Same relaxed start,
+    same interval as the headline; device time, BDF / Newton / Krylov counts,
+    and the final states' difference from the approximate Jacobian's."""
+    import torch
+    rank, world = dist_setup(1)
+    torch.cuda.set_device(0)
+    from nmag import _lib
+    _lib.set_device(0)
+    msh, base, seed = workload(args.workload)
+    B = args.members
+    anchor = args.anchor if args.form == "fp32x2" else 0.0
+    start, relax_rec = relax_states(args, args.form, args.cg, B, msh, base, seed, anchor)
+    out = {"report": "jacobian", "workload": WORKLOAD_NAMES[args.workload], "form": args.form, "cg": args.cg,
+           "members": B, "interval_ps": args.steps * args.step_ps, "jacobian_demag_rtol": args.jac_rtol,
+           "relax": relax_rec, "levels": {}}
+    ref_final = None
+    for level in ("approximate", "local", "exact"):
+        r = measure(args, args.form, args.cg, B, msh, start, world, 0, sample_clocks=False, anchor=anchor,
+                    warmup=1, e2e=False, jacobian=level)
+        row = {"value_ns_per_s": r["value"], "ms_per_step": r["ms_per_step"], "bdf_steps": r["bdf_steps"],
+               "rhs_evals": r["rhs_evals"], "cg_iterations": r["cg_iterations"], "newton": r["newton"],
+               "kernels_ms": {k: v["total_ms"] for k, v in r["kernels_ms"].items() if v["launches"]}}
+        if ref_final is None:
+            ref_final = r["m_final"]
+        else:
+            row["max_dm_final_vs_approximate"] = float(np.abs(r["m_final"] - ref_final).max())
+        out["levels"][level] = row
+        r["eng"].close()
+        print(level, json.dumps(row), flush=True)
+    print(json.dumps(out))
+
+
 def particle_batch_config(n=256, seed=2):
     """The batching configuration: cubes with edge U[8, 40] nm at a 2 nm pitch
     (round(edge/2) cells per side), Ms U[4e5, 1.7e6] A/m, K1 U[0, 5e5] J/m^3
@@ -1090,7 +1128,9 @@ def main():
     ap.add_argument("--batch-seconds", type=float, default=0.0,
                     help="after the timed launches, keep sweeping for this wall time and report the progress")
     ap.add_argument("--rhs", type=int, default=128, help="--report bem: right-hand sides per product")
-    ap.add_argument("--report", default=None, choices=["precision", "adjoint", "batch", "bem"],
+    ap.add_argument("--jac-rtol", type=float, default=1e-5,
+                    help="Poisson tolerance of the exact Jacobian's demag response (--report jacobian)")
+    ap.add_argument("--report", default=None, choices=["precision", "adjoint", "batch", "bem", "jacobian"],
                     help="precision: H_eff / energy error of the FP32 form against FP64 over --fields random fields")
     ap.add_argument("--fields", type=int, default=1000)
     ap.add_argument("--no-compare", dest="compare", action="store_false",
@@ -1108,6 +1148,8 @@ def main():
         run_bem_report(args)
     elif args.report == "batch":
         run_batch_report(args)
+    elif args.report == "jacobian":
+        run_jacobian_report(args)
     else:
         run_ours(args)
 

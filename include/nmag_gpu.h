@@ -278,6 +278,26 @@ int nmg_rhs_device(nmg_handle *h, const double *d_m, double *d_dmdt);
 int nmg_bem_apply(nmg_handle *h, const double *d_x, double *d_y, int n_rhs);
 int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps);
 
+/* The Jacobian of the BDF's Newton iteration.  The reference's is
+ * approximate: the derivative of C1 m x H + C2 m x (m x H) with H frozen plus
+ * the exchange operator's dH/dm, nothing else (nmag_lam.py:665-704; its
+ * do_anisotropy_jacobian adds a plan the timestepper never uses,
+ * nmag_lam.py:684-693).  level 0 is that Jacobian (the default); level 1
+ * adds the local terms: the anisotropy field's derivative (uniaxial, per
+ * element or polynomial), the C3 length term's, and with several materials
+ * the local couplings; level 2 adds the demag field's response, the demag
+ * field of each Krylov direction from one Neumann + BEM + Dirichlet pipeline
+ * at Poisson tolerance demag_rtol (in (0, 1)) on buffers of its own.  The
+ * block-Jacobi preconditioner takes the local terms from level 1 on.  The
+ * spin-torque terms are in none.  Changes the Newton iteration only: the
+ * solution is the same to the integrator's tolerances. */
+int nmg_set_jacobian(nmg_handle *h, int level, double demag_rtol);
+/* d_out = J(d_m) d_v at the handle's level (device arrays, 3 per node or site
+ * and member): one RHS evaluation at d_m for the frozen field, then the
+ * Jacobian-vector product.  For tests of the Newton matrix against finite
+ * differences of nmg_rhs_device. */
+int nmg_jacobian_apply(nmg_handle *h, const double *d_m, const double *d_v, double *d_out);
+
 /* Differentiation form.  No counterpart in the reference, whose material
  * constants are one scalar Ms and K1 per material (main.py:347-465); these
  * entry points extend its RHS (nmag_lam.py:734-832) with per-element weights,

@@ -419,6 +419,23 @@ int nmg_bem_apply(nmg_handle *h, const double *d_x, double *d_y, int n_rhs) {
   return nmg::check_device_error(h, "nmg_bem_apply");
 }
 
+int nmg_set_jacobian(nmg_handle *h, int level, double demag_rtol) {
+  if (!h) return -1;
+  if (level < 0 || level > 2) return fail(h, -2, "nmg_set_jacobian: level must be 0, 1 or 2");
+  if (!(demag_rtol > 0.0 && demag_rtol < 1.0)) return fail(h, -2, "nmg_set_jacobian: demag_rtol must be in (0, 1)");
+  h->jac_level = level;
+  h->jac_rtol = demag_rtol;
+  return 0;
+}
+
+int nmg_jacobian_apply(nmg_handle *h, const double *d_m, const double *d_v, double *d_out) {
+  if (!h || !d_m || !d_v || !d_out) return -1;
+  h->last_error.clear();
+  const int rc = nmg::jacobian_apply(h, d_m, d_v, d_out);
+  if (rc && h->last_error.empty()) return fail(h, rc, "nmg_jacobian_apply: launch failed");
+  return rc;
+}
+
 int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps) {
   if (!h || !d_m || nsteps < 0) return -1;
   return nmg::rk4_device(h, d_m, dt, nsteps);

@@ -44,6 +44,10 @@ struct DevBuf {
     n = 0;
   }
   ~DevBuf() { release(); }
+  void swap(DevBuf &o) {
+    T *q = p; p = o.p; o.p = q;
+    size_t m = n; n = o.n; o.n = m;
+  }
   operator T *() const { return p; }
 };
 
@@ -191,6 +195,19 @@ struct Tape;                     // RK4 checkpoints of the differentiation form 
 // density terms (ne) and field terms (nh, three coefficients each); exponents
 // packed a | b << 4 | c << 8, each at most kAnisMaxPow.
 constexpr int kAnisMaxPow = 13;
+
+// Monomial mx^a my^b mz^c of a packed exponent triple from per-node power tables.
+__device__ __forceinline__ double anis_monomial(int p, const double *px, const double *py, const double *pz) {
+  return px[p & 15] * py[(p >> 4) & 15] * pz[(p >> 8) & 15];
+}
+
+__device__ __forceinline__ void anis_powers(double x, double y, double z, double *px, double *py, double *pz) {
+  px[0] = py[0] = pz[0] = 1.0;
+#pragma unroll
+  for (int k = 1; k <= kAnisMaxPow; ++k) {
+    px[k] = px[k - 1] * x; py[k] = py[k - 1] * y; pz[k] = pz[k - 1] * z;
+  }
+}
 constexpr int kAnisMaxTerms = 1024;
 struct AnisPoly {
   int ne = 0, nh = 0;
@@ -204,6 +221,19 @@ struct Stt {
   double c4 = 0.0, c5 = 0.0;
   DevBuf<double> j, dmdc;
   bool on() const { return (c4 != 0.0 || c5 != 0.0) && j.p; }
+};
+// The demag part of the exact Jacobian (Jacobian level 2): H_demag is linear
+// in m, so its derivative along a direction v is the demag field of v itself.
+// The pipeline's buffers for v are swapped into the potential handle's
+// workspace for those solves, so the RHS's warm starts (previous potentials
+// and initial-guess bases) stay as they were; hdv = H_demag(v), 3 per node of
+// the potential mesh and member.
+struct JacDemag {
+  DevBuf<double> rho, phi1, phi2, phi, rhs2, b1, b2;
+  DevBuf<double> basis_b, basis_x, basis_gram, ens_basis_b, ens_basis_x, ens_basis_gram;
+  DevBuf<int> basis_ring, ens_basis_ring, iters;
+  DevBuf<double> hdv;
+  bool ready = false;
 };
 }  // namespace nmg
 
@@ -234,6 +264,13 @@ struct nmg_handle {
   bool own_stream = true;       // false: the stream belongs to pot
   nmg::Tape *tape = nullptr;
   int anchor_hold = 0;          // >0: anchored BEM product suspended (RK4 tape runs recompute bit for bit)
+  // Jacobian of the BDF's Newton iteration: 0 the exchange part only (the
+  // reference's); 1 also the local terms (anisotropy, the C3 length term,
+  // local couplings); 2 also the demag response, from Poisson solves at
+  // jac_rtol (one pair per Jacobian-vector product)
+  int jac_level = 0;
+  double jac_rtol = 1e-5;
+  nmg::JacDemag jd;
   // the mixed-precision CG is used by the forward solves or the adjoint's
   bool mixed_cg() const { return opt.cg_precision == 1 || opt.adjoint_cg_precision == 1; }
   bool anchored() const {
@@ -278,6 +315,15 @@ int rhs_eval_sites(nmg_handle *h, const double *d_m, double *d_dmdt);
 int energy_density_sites(nmg_handle *h, const double *d_m, double *d_E5);
 // ---- rhs_kernels.cu: the demag pipeline from W.rho to W.phi (one handle) ----
 int demag_from_rho(nmg_handle *h);
+// The exact Jacobian's demag response: h->jd.hdv = H_demag(d_v) for the
+// member-major direction d_v (3 per node or site and member); the RHS's
+// solver state is left as it was.  demag_response_sites: several materials.
+int demag_response(nmg_handle *h, const double *d_v);
+int demag_response_sites(nmg_handle *h, const double *d_v);
+// J.rho (charges on P's nodes, all members) -> J.phi -> J.hdv, Poisson solves
+// at rtol; jac_prepare allocates J (zeroed) for P's workspace once
+int jac_prepare(nmg_handle *P, JacDemag &J);
+int jac_demag_solve(nmg_handle *P, JacDemag &J, double rtol);
 // ---- bem_tc.cu ----
 int bem_tc_setup(nmg_handle *h, std::string &err);
 int bem_tc(nmg_handle *h, const double *x, double *y, int R);   // Y = B X, R member-major right-hand sides
@@ -308,6 +354,7 @@ int ts_init(nmg_handle *h, double t0);
 int ts_advance(nmg_handle *h, double tout, int exact_tstop, int64_t max_steps, double *t_reached,
                nmg_ts_stats *st);
 int rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps);
+int jacobian_apply(nmg_handle *h, const double *d_m, const double *d_v, double *d_out);
 // ---- nmg_api.cu ----
 void set_handleless_error(const std::string &msg);  // what nmg_last_error(NULL) reports
 }  // namespace nmg

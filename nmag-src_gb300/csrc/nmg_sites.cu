@@ -272,6 +272,31 @@ int rhs_eval_sites(nmg_handle *h, const double *d_m, double *d_dmdt) {
   return cudaGetLastError() == cudaSuccess ? 0 : 100;
 }
 
+// The demag response of a site direction v: its charges per site, summed onto
+// the potential mesh's nodes, through the potential handle's pipeline on the
+// Jacobian's own buffers; hdv per node of the potential mesh.
+int demag_response_sites(nmg_handle *h, const double *d_v) {
+  Mesh &M = h->mesh;
+  nmg_handle *P = h->pot;
+  JacDemag &J = h->jd;
+  if (jac_prepare(P, J)) {
+    h->last_error = "exact Jacobian: cannot allocate the demag response buffers";
+    return 100;
+  }
+  const int S = M.N, B = h->nrep;
+  cudaStream_t st = h->stream;
+  k_div_sites<<<nblk_s((long long)S * B, 256), 256, 0, st>>>(S, M.nnz, h->sites.mtab, h->sites.site_mat, M.row_ptr,
+                                                              M.col_idx, M.D, d_v, h->ws.rho, B);
+  k_scatter_sites<<<nblk_s((long long)P->mesh.N * B, 256), 256, 0, st>>>(P->mesh.N, h->sites.node_ptr,
+                                                                          h->sites.node_sites, h->ws.rho, J.rho, S, B);
+  h->launches += 2;
+  const int rc = jac_demag_solve(P, J, h->jac_rtol);
+  h->launches += P->launches;
+  P->launches = 0;
+  if (rc) h->last_error = P->last_error.empty() ? "exact Jacobian: demag response failed" : P->last_error;
+  return rc;
+}
+
 int energy_density_sites(nmg_handle *h, const double *d_m, double *d_E5) {
   Workspace &W = h->ws;
   const long long SB = (long long)h->mesh.N * h->nrep;

@@ -306,9 +306,75 @@ void launch_orth(int n, int nv, const VecPtrs &vp, const double *h, double *w, c
   else k_orth<32><<<g, 256, 0, st>>>(n, nv, vp, h, w);
 }
 
+// The local terms of dF/dm . w beyond the exchange (Jacobian level >= 1):
+// the anisotropy field's derivative (uniaxial, per-node, or polynomial), the
+// C3 length term's, and (several materials) the local couplings to the other
+// sites of the node.  The reference's Jacobian has none of them
+// (nmag_lam.py:665-704: H_exch is its only field derivative).
+struct LocalJac {
+  int on = 0;
+  double C3 = 0.0, K1 = 0.0, anis = 0.0, ax = 0.0, ay = 0.0, az = 1.0;   // one material
+  const double *anis_node = nullptr;   // element parameters: per-node anisotropy coefficient
+  int nh = 0;                          // polynomial anisotropy field H_d = sum_t c_{t,d} m^{p_t}
+  const int32_t *hpow = nullptr;
+  const double *hcoef = nullptr;
+  const int32_t *site_mat = nullptr;   // several materials: per-site coefficients
+  const SiteMat *mt = nullptr;
+  const int32_t *site_node = nullptr, *node_ptr = nullptr, *node_sites = nullptr;
+  const double *lc = nullptr;          // local coupling table (null: none)
+  int n_mats = 0;
+};
+
+// dh += dH_local(m) . w (anisotropy; local couplings when tm, the member's
+// direction at every site, is given), fw = C3 [(1 - |m|^2) w - 2 (m . w) m]
+// (the derivative of C3 (1 - |m|^2) m, nmag_lam.py:417-424).
+__device__ __forceinline__ void local_jac(const LocalJac &L, int i, const double *m, const double *w,
+                                          const double *tm, double *dh, double *fw) {
+  double C3 = L.C3, K1 = L.K1, c = L.anis, ax = L.ax, ay = L.ay, az = L.az;
+  bool uni;
+  if (L.site_mat) {
+    const SiteMat &s = L.mt[L.site_mat[i]];
+    C3 = s.C3; K1 = s.K1; c = s.anis; ax = s.ax; ay = s.ay; az = s.az;
+    uni = K1 != 0.0;
+  } else {
+    uni = K1 != 0.0 || L.anis_node;
+    if (L.anis_node) c = L.anis_node[i];
+  }
+  if (uni) {   // H = c am (a - am m), am = a.m
+    const double am = (ax * m[0] + ay * m[1]) + az * m[2], aw = (ax * w[0] + ay * w[1]) + az * w[2];
+    const double a[3] = {ax, ay, az};
+    for (int d = 0; d < 3; ++d) dh[d] += c * ((aw * a[d] - 2.0 * am * aw * m[d]) - am * am * w[d]);
+  }
+  if (L.nh > 0) {   // d(x^a y^b z^c) = a x^(a-1) y^b z^c dx + ...
+    double px[kAnisMaxPow + 1], py[kAnisMaxPow + 1], pz[kAnisMaxPow + 1];
+    anis_powers(m[0], m[1], m[2], px, py, pz);
+    for (int t = 0; t < L.nh; ++t) {
+      const int p = __ldg(L.hpow + t), e0 = p & 15, e1 = (p >> 4) & 15, e2 = (p >> 8) & 15;
+      double dm = 0.0;
+      if (e0) dm += e0 * px[e0 - 1] * py[e1] * pz[e2] * w[0];
+      if (e1) dm += e1 * px[e0] * py[e1 - 1] * pz[e2] * w[1];
+      if (e2) dm += e2 * px[e0] * py[e1] * pz[e2 - 1] * w[2];
+      for (int d = 0; d < 3; ++d) dh[d] = fma(__ldg(L.hcoef + 3 * t + d), dm, dh[d]);
+    }
+  }
+  if (L.lc && tm) {   // H_lc of site i = sum over the node's other sites s2 of c(X, X2) m_s2
+    const int X = L.site_mat[i], nd = L.site_node[i];
+    for (int k = L.node_ptr[nd]; k < L.node_ptr[nd + 1]; ++k) {
+      const int s2 = L.node_sites[k];
+      if (s2 == i) continue;
+      const double cc = L.lc[2 * (X * L.n_mats + L.site_mat[s2])];
+      const double *w2 = tm + 3 * (size_t)s2;
+      dh[0] += cc * w2[0]; dh[1] += cc * w2[1]; dh[2] += cc * w2[2];
+    }
+  }
+  const double mm = (m[0] * m[0] + m[1] * m[1]) + m[2] * m[2], mw = (m[0] * w[0] + m[1] * w[1]) + m[2] * w[2];
+  for (int d = 0; d < 3; ++d) fw[d] = C3 * ((1.0 - mm) * w[d] - 2.0 * mw * m[d]);
+}
+
 // J v with frozen (mJ, HJ), fused with  w = t - gamma J t  and the block-Jacobi
 // preconditioner and the ewt scaling:  out = ewt * P^{-1} (t - gamma J t),
-// t = v / ewt (materialised by the caller).  If psolve == 0, out = t - gamma J t.
+// t = v / ewt (materialised by the caller).  If psolve == 0, out = t - gamma J t;
+// raw != 0: out = J t.
 struct JvArgs {
   int N, nrep;   // nodes per member, ensemble members (member-major vectors)
   const int32_t *row_ptr, *col_idx, *diag_pos;
@@ -317,8 +383,11 @@ struct JvArgs {
   const double *pin;    // per-node factor of the Jacobian rows (the pin field) or null
   const int32_t *site_mat;   // several materials: each site's material (null: one material)
   const SiteMat *mt;         //   and the materials' coefficients
+  LocalJac L;                // Jacobian level >= 1
+  const double *hdv;         // Jacobian level 2: H_demag(t), 3 per node of the potential mesh and member
+  int Np;                    //   nodes of that mesh (the site's node: L.site_node)
   double c_exch, C1, C2, gamma, gammap;
-  int psolve, scale_out;
+  int psolve, scale_out, raw;
   double *out;
 };
 
@@ -341,6 +410,9 @@ __device__ __forceinline__ void jac_apply(const double *m, const double *H, cons
   for (int d = 0; d < 3; ++d) out[d] = C1 * (wxH[d] + mxhv[d]) + C2 * (t1[d] + t2[d]);
 }
 
+// kLocal: Jacobian level >= 1 (local terms, demag response); the default
+// level 0 keeps the lean exchange-only form
+template <bool kLocal>
 __global__ void k_jv_psolve(JvArgs a) {
   const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (g >= (long long)a.N * a.nrep) return;
@@ -358,13 +430,29 @@ __global__ void k_jv_psolve(JvArgs a) {
     c_exch = c.c_exch; C1 = c.C1; C2 = c.C2;
   }
   const double ce = -c_exch * a.ivol[i];
-  const double hv[3] = {ce * s0, ce * s1, ce * s2};
+  double hv[3] = {ce * s0, ce * s1, ce * s2};
   const double *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g, *w = a.t + 3 * (size_t)g;
+  double fl[3] = {0.0, 0.0, 0.0};
+  if constexpr (kLocal) {
+    local_jac(a.L, i, m, w, tm, hv, fl);
+    if (a.hdv) {
+      const int nd = a.L.site_node ? a.L.site_node[i] : i;
+      const double *q = a.hdv + 3 * ((size_t)mbr * a.Np + nd);
+      hv[0] += q[0]; hv[1] += q[1]; hv[2] += q[2];
+    }
+  }
   double jw[3];
   jac_apply(m, H, w, hv, C1, C2, jw);
+  if constexpr (kLocal) {
+    for (int d = 0; d < 3; ++d) jw[d] += fl[d];
+  }
   if (a.pin) {
     const double p = a.pin[i];
     jw[0] *= p; jw[1] *= p; jw[2] *= p;
+  }
+  if (a.raw) {
+    for (int d = 0; d < 3; ++d) a.out[3 * (size_t)g + d] = jw[d];
+    return;
   }
   double r[3] = {w[0] - a.gamma * jw[0], w[1] - a.gamma * jw[1], w[2] - a.gamma * jw[2]};
   double z[3] = {r[0], r[1], r[2]};
@@ -379,13 +467,14 @@ __global__ void k_jv_psolve(JvArgs a) {
 }
 
 // The block-Jacobi preconditioner's 3x3 blocks P = I - gamma_p dF/dm (the
-// exchange diagonal and the site terms at the setup state mJ, HJ), inverted
-// once per preconditioner setup: Pinv[9 g + 3 d + c] = (P^-1)_dc.
+// exchange diagonal and the site terms at the setup state mJ, HJ; at
+// Jacobian level >= 1 also the local anisotropy and C3 terms), inverted once
+// per preconditioner setup: Pinv[9 g + 3 d + c] = (P^-1)_dc.
 __global__ void k_pprep(int N, const int32_t *__restrict__ diag_pos, const double *__restrict__ K,
                         const double *__restrict__ vol, const double *__restrict__ mJ, const double *__restrict__ HJ,
                         double c_exch, double C1, double C2, double gammap, double *__restrict__ Pinv, int nrep,
                         const double *__restrict__ pin, const int32_t *__restrict__ site_mat,
-                        const SiteMat *__restrict__ mt) {
+                        const SiteMat *__restrict__ mt, LocalJac L) {
   const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (g >= (long long)N * nrep) return;
   const int i = (int)(g % N);
@@ -400,8 +489,10 @@ __global__ void k_pprep(int N, const int32_t *__restrict__ diag_pos, const doubl
   for (int c = 0; c < 3; ++c) {
     double e[3] = {0.0, 0.0, 0.0};
     e[c] = 1.0;
-    double he[3] = {kap * e[0], kap * e[1], kap * e[2]}, je[3];
+    double he[3] = {kap * e[0], kap * e[1], kap * e[2]}, je[3], fe[3] = {0.0, 0.0, 0.0};
+    if (L.on) local_jac(L, i, m, e, nullptr, he, fe);
     jac_apply(m, H, e, he, C1, C2, je);
+    for (int d = 0; d < 3; ++d) je[d] += fe[d];
     for (int d = 0; d < 3; ++d) P[d][c] = (d == c ? 1.0 : 0.0) - gammap * (pin ? pf * je[d] : je[d]);
   }
   double c00 = P[1][1] * P[2][2] - P[1][2] * P[2][1];
@@ -525,14 +616,54 @@ int psetup(Integrator &I, int jok, const double *ypred) {
   return 1;
 }
 
-JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
-  const Mesh &M = I.hd->mesh;
+// The local Jacobian terms of the handle's model (level >= 1), else off.
+LocalJac local_jac_args(const nmg_handle *h) {
+  LocalJac L;
+  if (h->jac_level < 1) return L;
+  L.on = 1;
+  if (h->pot) {   // several materials
+    L.site_mat = h->sites.site_mat.p; L.mt = h->sites.mtab.p;
+    L.site_node = h->sites.site_node.p; L.node_ptr = h->sites.node_ptr.p; L.node_sites = h->sites.node_sites.p;
+    L.lc = h->sites.lc.p; L.n_mats = h->sites.n_mats;
+    return L;
+  }
+  const nmg_material &mt = h->mat;
+  L.C3 = mt.C3; L.K1 = mt.K1; L.anis = mt.anis_coeff;
+  L.ax = mt.axis[0]; L.ay = mt.axis[1]; L.az = mt.axis[2];
+  if (h->ep.active) {
+    L.anis_node = h->ep.anis.p;
+    L.ax = h->ep.axis[0]; L.ay = h->ep.axis[1]; L.az = h->ep.axis[2];
+  }
+  L.nh = h->ap.nh; L.hpow = h->ap.hpow.p; L.hcoef = h->ap.hcoef.p;
+  return L;
+}
+
+bool demag_in_jacobian(const nmg_handle *h) {
+  return h->jac_level >= 2 && h->opt.do_demag && (h->pot ? h->pot->mesh.nb : h->mesh.nb) > 0;
+}
+
+// The handle's part of the J v arguments (no integrator state).
+JvArgs jv_base(nmg_handle *h) {
+  const Mesh &M = h->mesh;
   JvArgs a;
-  a.N = M.N; a.nrep = I.hd->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos; a.K = I.hd->exch_K(); a.ivol = M.ivol;
-  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv; a.pin = I.hd->pin.p;
-  a.site_mat = I.hd->pot ? I.hd->sites.site_mat.p : nullptr;
-  a.mt = I.hd->sites.mtab.p;
-  a.c_exch = I.hd->mat.exch_coeff; a.C1 = I.hd->mat.C1; a.C2 = I.hd->mat.C2;
+  a.N = M.N; a.nrep = h->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx; a.diag_pos = M.diag_pos;
+  a.K = h->exch_K(); a.ivol = M.ivol;
+  a.pin = h->pin.p;
+  a.site_mat = h->pot ? h->sites.site_mat.p : nullptr;
+  a.mt = h->sites.mtab.p;
+  a.L = local_jac_args(h);
+  a.hdv = nullptr;
+  a.Np = h->pot ? h->pot->mesh.N : M.N;
+  if (!a.L.site_node && h->pot) a.L.site_node = h->sites.site_node.p;   // the demag response's node of a site
+  a.c_exch = h->mat.exch_coeff; a.C1 = h->mat.C1; a.C2 = h->mat.C2;
+  a.mJ = a.HJ = a.t = a.ewt = a.Pinv = nullptr;
+  a.gamma = a.gammap = 0.0; a.psolve = 0; a.scale_out = 0; a.raw = 0; a.out = nullptr;
+  return a;
+}
+
+JvArgs jv_args(Integrator &I, const double *t, double *out, int psolve) {
+  JvArgs a = jv_base(I.hd);
+  a.mJ = I.mJ; a.HJ = I.HJ; a.t = t; a.ewt = I.ewt; a.Pinv = I.Pinv;
   a.gamma = I.gamma; a.gammap = I.gammap; a.psolve = psolve; a.scale_out = 1; a.out = out;
   return a;
 }
@@ -606,9 +737,15 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
     // division would be repeated for every neighbour reference
     k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewts, I.tvec); ++I.hd->launches;
     JvArgs a = jv_args(I, I.tvec, I.V[l + 1], 1);
+    if (demag_in_jacobian(I.hd)) {   // exact Jacobian: the demag field of the direction
+      if (demag_response(I.hd, I.tvec)) return -1;
+      a.hdv = I.hd->jd.hdv;
+    }
     {
       NMG_PROF_BEGIN(I.hd, 4);
-      k_jv_psolve<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(a); ++I.hd->launches;
+      if (a.L.on) k_jv_psolve<true><<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(a);
+      else k_jv_psolve<false><<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(a);
+      ++I.hd->launches;
       NMG_PROF_END(I.hd);
     }
     I.njv++; I.nps++;
@@ -754,7 +891,8 @@ int nls(Integrator &I, int nflag_first) {
         const nmg_material &mt = I.hd->mat;
         k_pprep<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(
             M.N, M.diag_pos, I.hd->exch_K(), M.vol, I.mJ, I.HJ, mt.exch_coeff, mt.C1, mt.C2, I.gammap, I.Pinv,
-            I.hd->nrep, I.hd->pin.p, I.hd->pot ? I.hd->sites.site_mat.p : nullptr, I.hd->sites.mtab.p);
+            I.hd->nrep, I.hd->pin.p, I.hd->pot ? I.hd->sites.site_mat.p : nullptr, I.hd->sites.mtab.p,
+            local_jac_args(I.hd));
         ++I.hd->launches;
       }
     }
@@ -1083,6 +1221,24 @@ int rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps) {
     k_lin<<<nblk(n, 256), 256, 0, s>>>(n, 1.0, d_m, dt / 6.0, y, d_m); ++h->launches;
   }
   return check_device_error(h, "rk4");
+}
+
+// d_out = J(d_m) d_v with the handle's Jacobian level: the RHS at d_m gives
+// H_total (the frozen field of the Newton matrix), then the fused J v kernel
+// without the preconditioner.
+int jacobian_apply(nmg_handle *h, const double *d_m, const double *d_v, double *d_out) {
+  if (rhs_eval(h, d_m, nullptr)) return 100;
+  JvArgs a = jv_base(h);
+  a.mJ = d_m; a.HJ = h->ws.h_total; a.t = d_v; a.raw = 1; a.out = d_out;
+  if (demag_in_jacobian(h)) {
+    if (demag_response(h, d_v)) return 100;
+    a.hdv = h->jd.hdv;
+  }
+  if (a.L.on) k_jv_psolve<true><<<nblk((long long)h->mesh.N * h->nrep, 128), 128, 0, h->stream>>>(a);
+  else k_jv_psolve<false><<<nblk((long long)h->mesh.N * h->nrep, 128), 128, 0, h->stream>>>(a);
+  ++h->launches;
+  if (cudaGetLastError() != cudaSuccess) return 100;
+  return check_device_error(h, "nmg_jacobian_apply");
 }
 
 }  // namespace nmg

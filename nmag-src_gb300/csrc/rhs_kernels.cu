@@ -22,6 +22,7 @@
 #include <cooperative_groups.h>
 #include <cuda_fp16.h>
 #include <cstring>
+#include <utility>
 
 #include "nmg_internal.h"
 
@@ -2093,19 +2094,6 @@ __global__ void k_add(int n, const double *__restrict__ a, const double *__restr
   if (i < n) c[i] = a[i] + b[i];
 }
 
-// Monomial mx^a my^b mz^c of a packed exponent triple from per-node power tables.
-__device__ __forceinline__ double anis_monomial(int p, const double *px, const double *py, const double *pz) {
-  return px[p & 15] * py[(p >> 4) & 15] * pz[(p >> 8) & 15];
-}
-
-__device__ __forceinline__ void anis_powers(double x, double y, double z, double *px, double *py, double *pz) {
-  px[0] = py[0] = pz[0] = 1.0;
-#pragma unroll
-  for (int k = 1; k <= kAnisMaxPow; ++k) {
-    px[k] = px[k - 1] * x; py[k] = py[k - 1] * y; pz[k] = pz[k - 1] * z;
-  }
-}
-
 // Anisotropy field from its polynomial form (nsim_anisotropy.ml:143-206: the
 // tangential gradient -(1/mu0 Ms)(grad E - (m.grad E) m) expanded into
 // monomials by the host): H_d = sum_t c_{t,d} m^{p_t}, written to h (3 per
@@ -2990,6 +2978,103 @@ int rhs_eval(nmg_handle *h, const double *d_m, double *d_dmdt) {
     return 100;
   }
   return cudaGetLastError() == cudaSuccess ? 0 : 100;
+}
+
+namespace {
+// H_demag at the nodes from a potential: -(G_j phi)_i / vol_i (the demag
+// term of k_heff_llg), 3 per node and member.
+__global__ void k_neg_grad(int N, int nrep, int nnz, const int32_t *__restrict__ row_ptr,
+                           const int32_t *__restrict__ col_idx, const double *__restrict__ G,
+                           const double *__restrict__ ivol, const double *__restrict__ phi, double *__restrict__ out) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= (long long)N * nrep) return;
+  const int b = (int)(g / N), i = (int)(g - (long long)b * N);
+  const double *ph = phi + (size_t)b * N;
+  double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+  for (int k = row_ptr[i]; k < row_ptr[i + 1]; ++k) {
+    const double pj = ph[col_idx[k]];
+    g0 += G[k] * pj; g1 += G[(size_t)nnz + k] * pj; g2 += G[2 * (size_t)nnz + k] * pj;
+  }
+  const double iv = ivol[i];
+  out[3 * (size_t)g] = -g0 * iv; out[3 * (size_t)g + 1] = -g1 * iv; out[3 * (size_t)g + 2] = -g2 * iv;
+}
+
+void swap_jac_buffers(Workspace &W, JacDemag &J) {
+  W.rho.swap(J.rho); W.phi1.swap(J.phi1); W.phi2.swap(J.phi2); W.phi.swap(J.phi); W.rhs2.swap(J.rhs2);
+  W.b1.swap(J.b1); W.b2.swap(J.b2);
+  W.basis_b.swap(J.basis_b); W.basis_x.swap(J.basis_x); W.basis_gram.swap(J.basis_gram);
+  W.basis_ring.swap(J.basis_ring);
+  W.ens_basis_b.swap(J.ens_basis_b); W.ens_basis_x.swap(J.ens_basis_x); W.ens_basis_gram.swap(J.ens_basis_gram);
+  W.ens_basis_ring.swap(J.ens_basis_ring);
+  W.iters.swap(J.iters);
+}
+
+// J's buffers with the sizes of P's workspace, zeroed (empty bases, zero
+// initial potentials).
+int jac_alloc(nmg_handle *P, JacDemag &J) {
+  Workspace &W = P->ws;
+  std::pair<DevBuf<double> *, size_t> d[] = {
+      {&J.rho, W.rho.n}, {&J.phi1, W.phi1.n}, {&J.phi2, W.phi2.n}, {&J.phi, W.phi.n}, {&J.rhs2, W.rhs2.n},
+      {&J.b1, W.b1.n}, {&J.b2, W.b2.n}, {&J.basis_b, W.basis_b.n}, {&J.basis_x, W.basis_x.n},
+      {&J.basis_gram, W.basis_gram.n}, {&J.ens_basis_b, W.ens_basis_b.n}, {&J.ens_basis_x, W.ens_basis_x.n},
+      {&J.ens_basis_gram, W.ens_basis_gram.n}, {&J.hdv, 3 * (size_t)P->mesh.N * P->nrep}};
+  for (auto &e : d) {
+    if (e.first->alloc(e.second) != cudaSuccess) return 100;
+    if (e.second) cudaMemsetAsync(e.first->p, 0, sizeof(double) * e.second, P->stream);
+  }
+  std::pair<DevBuf<int> *, size_t> k[] = {
+      {&J.basis_ring, W.basis_ring.n}, {&J.ens_basis_ring, W.ens_basis_ring.n}, {&J.iters, W.iters.n}};
+  for (auto &e : k) {
+    if (e.first->alloc(e.second) != cudaSuccess) return 100;
+    if (e.second) cudaMemsetAsync(e.first->p, 0, sizeof(int) * e.second, P->stream);
+  }
+  J.ready = true;
+  return 0;
+}
+}  // namespace
+
+int jac_demag_solve(nmg_handle *P, JacDemag &J, double rtol) {
+  Workspace &W = P->ws;
+  const double nr = P->opt.nbc_rtol, dr = P->opt.dbc_rtol;
+  swap_jac_buffers(W, J);
+  P->anchor_hold++;   // the direction is no small change of the anchored state: plain product
+  P->opt.nbc_rtol = rtol;
+  P->opt.dbc_rtol = rtol;
+  const int rc = demag_from_rho(P);
+  P->opt.nbc_rtol = nr;
+  P->opt.dbc_rtol = dr;
+  P->anchor_hold--;
+  swap_jac_buffers(W, J);
+  if (rc) return rc;
+  const Mesh &M = P->mesh;
+  k_neg_grad<<<nblk((long long)M.N * P->nrep, 256), 256, 0, P->stream>>>(M.N, P->nrep, M.nnz, M.row_ptr, M.col_idx,
+                                                                          M.G, M.ivol, J.phi, J.hdv);
+  ++P->launches;
+  if (P->tc.failed) {
+    P->tc.failed = 0;
+    return 100;
+  }
+  return cudaGetLastError() == cudaSuccess ? 0 : 100;
+}
+
+int demag_response(nmg_handle *h, const double *d_v) {
+  if (h->pot) return demag_response_sites(h, d_v);
+  Mesh &M = h->mesh;
+  JacDemag &J = h->jd;
+  if (!J.ready && jac_alloc(h, J)) {
+    h->last_error = "exact Jacobian: cannot allocate the demag response buffers";
+    return 100;
+  }
+  k_div<<<nblk((long long)M.N * h->nrep, 256), 256, 0, h->stream>>>(M.N, M.nnz, h->mat.Ms, M.row_ptr, M.col_idx,
+                                                                     h->ep.active ? h->ep.Dx.p : M.D.p, d_v, J.rho,
+                                                                     h->nrep);
+  ++h->launches;
+  return jac_demag_solve(h, J, h->jac_rtol);
+}
+
+int jac_prepare(nmg_handle *P, JacDemag &J) {
+  if (J.ready) return 0;
+  return jac_alloc(P, J);
 }
 
 int energy_density(nmg_handle *h, const double *d_m, double *d_E5) {

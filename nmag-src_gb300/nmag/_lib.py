@@ -56,7 +56,8 @@ class TsStats(C.Structure):
 EXPORTS = ["nmg_version", "nmg_set_device", "nmg_last_error", "nmg_create", "nmg_destroy", "nmg_mesh_info", "nmg_get_csr",
            "nmg_export_operator", "nmg_get_boundary", "nmg_get_bem", "nmg_set_m", "nmg_get_m", "nmg_set_h_ext",
            "nmg_set_material", "nmg_set_anisotropy_poly", "nmg_set_stt", "nmg_set_current_density", "nmg_set_pinning", "nmg_eval_fields", "nmg_energy_density", "nmg_averages", "nmg_ts_init",
-           "nmg_ts_advance", "nmg_max_dm", "nmg_max_dm_step", "nmg_rhs_device", "nmg_bem_apply", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
+           "nmg_ts_advance", "nmg_max_dm", "nmg_max_dm_step", "nmg_rhs_device", "nmg_bem_apply", "nmg_set_jacobian",
+           "nmg_jacobian_apply", "nmg_rk4_device", "nmg_get_timings", "nmg_profile",
            "nmg_profile_read", "nmg_launch_count", "nmg_cg_iterations", "nmg_bem_anchor_stats", "nmg_max_dm_static",
            "nmg_set_element_params", "nmg_clear_element_params", "nmg_rk4_forward", "nmg_rk4_adjoint",
            "nmg_member_averages", "nmg_create_materials", "nmg_site_info", "nmg_set_site_material", "nmg_set_local_coupling",
@@ -117,6 +118,8 @@ def lib(build_if_missing=True):
     L.nmg_max_dm_step.argtypes = [vp, C.POINTER(C.c_double)]
     L.nmg_rhs_device.argtypes = [vp, vp, vp]
     L.nmg_bem_apply.argtypes = [vp, vp, vp, C.c_int]
+    L.nmg_set_jacobian.argtypes = [vp, C.c_int, C.c_double]
+    L.nmg_jacobian_apply.argtypes = [vp, vp, vp, vp]
     L.nmg_create_materials.argtypes = [_f64p, C.c_int, _i32p, C.c_int, _i32p, C.c_int, _i32p, _i32p, vp, C.c_int,
                                        C.POINTER(Options), C.POINTER(vp)]
     L.nmg_site_info.argtypes = [vp, vp, vp]
@@ -418,6 +421,16 @@ class Engine(object):
     def bem_apply_device(self, d_x, d_y, n_rhs):
         """y_n = B x_n for n_rhs member-major boundary vectors (device addresses)."""
         check(lib().nmg_bem_apply(self.h, C.c_void_p(d_x), C.c_void_p(d_y), int(n_rhs)), self.h, "bem_apply")
+
+    def set_jacobian(self, level, demag_rtol=1e-5):
+        """The Newton matrix's Jacobian: 0 the reference's (exchange only), 1 + the local
+        terms, 2 + the demag response (Poisson solves at demag_rtol)."""
+        check(lib().nmg_set_jacobian(self.h, int(level), float(demag_rtol)), self.h, "set_jacobian")
+
+    def jacobian_apply_device(self, d_m, d_v, d_out):
+        """out = J(m) v at the handle's Jacobian level (device addresses)."""
+        check(lib().nmg_jacobian_apply(self.h, C.c_void_p(d_m), C.c_void_p(d_v), C.c_void_p(d_out)), self.h,
+              "jacobian_apply")
 
     def rk4_device(self, d_m, dt, nsteps):
         check(lib().nmg_rk4_device(self.h, C.c_void_p(d_m), dt, nsteps), self.h, "rk4_device")

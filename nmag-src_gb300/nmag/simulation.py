@@ -111,6 +111,10 @@ def _next_time(event, view, tols=None):
             least([at_("time", "zero_stage_time"), at_("stage_time")]), at_("real_time"))
 
 
+# Newton-matrix Jacobians of the BDF timestepper, by level
+JACOBIAN_LEVELS = ("approximate", "local", "exact")
+
+
 class Simulation(object):
     """Micromagnetic simulation (main.py:776-845 constructor arguments)."""
 
@@ -118,7 +122,8 @@ class Simulation(object):
                  temperature=None, thermal_delta_t=None, user_seed_T=0, timestepper_max_order=2,
                  timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
                  lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1, cg_precision="fp64",
-                 bem_anchor=0.0, adjoint_cg_precision="fp64", anchor_product="fp32", cg_local_sweeps=0):
+                 bem_anchor=0.0, adjoint_cg_precision="fp64", anchor_product="fp32", cg_local_sweeps=0,
+                 jacobian="approximate", jacobian_demag_rtol=1e-5):
         if periodic_bc is not None:
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
@@ -150,6 +155,15 @@ class Simulation(object):
         # FP32 inner CG: damped Jacobi sweeps on each thread block's own rows
         # in its preconditioner (0 or 1: Jacobi alone)
         self.cg_local_sweeps = int(cg_local_sweeps)
+        # the BDF's Newton matrix: "approximate" (the reference's: exchange
+        # only), "local" (+ anisotropy, C3 length term, local couplings) or
+        # "exact" (+ the demag response, Poisson solves at jacobian_demag_rtol)
+        if jacobian not in JACOBIAN_LEVELS:
+            raise ValueError("jacobian must be one of %s" % ", ".join(JACOBIAN_LEVELS))
+        self.jacobian = jacobian
+        self.jacobian_demag_rtol = float(jacobian_demag_rtol)
+        if not 0.0 < self.jacobian_demag_rtol < 1.0:
+            raise ValueError("jacobian_demag_rtol must be in (0, 1)")
         # several magnetic materials: the site layout (None: one material)
         self.layer = None
         self.materials = []
@@ -247,6 +261,7 @@ class Simulation(object):
             self.engine = Engine.materials(self.mesh.points, self.mesh.simplices, self.mesh.regions,
                                            [[names.index(n) for n in r] for r in per_region],
                                            [self._material_struct(mt) for mt in self.materials], opts)
+            self.engine.set_jacobian(JACOBIAN_LEVELS.index(self.jacobian), self.jacobian_demag_rtol)
             self._j = None
             shape = self.engine._shape3()
             self._m = np.zeros(shape)
@@ -255,6 +270,7 @@ class Simulation(object):
             self._ts_ready = False
             return self.mesh
         self.engine = Engine(self.mesh.points, self.mesh.simplices, self._material_struct(), opts)
+        self.engine.set_jacobian(JACOBIAN_LEVELS.index(self.jacobian), self.jacobian_demag_rtol)
         poly = self.material.anisotropy_polynomial(self.quirks)
         if poly is not None:
             self.engine.set_anisotropy_poly(*poly)

@@ -116,6 +116,21 @@ def test_create_rejects_bad_anchor_options_without_gpu():
         assert msg in L.nmg_last_error(None), L.nmg_last_error(None)
 
 
+def test_jacobian_option_checks_without_gpu():
+    # the Newton matrix's Jacobian: three named levels, a Poisson tolerance in (0, 1)
+    import nmag
+    from nmag.simulation import JACOBIAN_LEVELS
+    assert JACOBIAN_LEVELS == ("approximate", "local", "exact")
+    for bad in ({"jacobian": "full"}, {"jacobian_demag_rtol": 0.0}, {"jacobian_demag_rtol": 1.5}):
+        with pytest.raises(ValueError):
+            nmag.Simulation("j", **bad)
+    sim = nmag.Simulation("j", jacobian="exact", jacobian_demag_rtol=1e-6)
+    assert (sim.jacobian, sim.jacobian_demag_rtol) == ("exact", 1e-6)
+    L = _lib.lib()
+    assert L.nmg_set_jacobian(None, 2, 1e-6) == -1
+    assert L.nmg_jacobian_apply(None, None, None, None) == -1
+
+
 def test_batch_rejects_bad_integrator_without_gpu():
     import ctypes as C
     L = _lib.lib()
