@@ -288,6 +288,7 @@ def config_dict(args, msh):
             "step": "%g ps advance in %g ps records, each followed by an <m> read" % (args.step_ps, args.record_ps),
             "interval_ps": args.steps * args.step_ps,
             "form": args.form, "cg": args.cg, "cg_local_sweeps": args.cg_sweeps, "members": args.members,
+            "jv": args.jv,
             "bem_anchor": args.anchor if args.form == "fp32x2" else 0.0,
             "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
             "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % {"fp64": 8, "fp32": 4,
@@ -334,7 +335,7 @@ def relax_states(args, form, cg, B, msh, base, seed, anchor):
 
 
 def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anchor=0.0, warmup=None,
-            e2e=True, jacobian="approximate"):
+            e2e=True, jacobian="approximate", jv=None):
     """One form on the workload from the relaxed states `start`: alpha =
     0.02 and the applied field; W untimed warm-up steps, then the state is
     put back and K timed steps run on the device-resident engine (value:
@@ -348,7 +349,8 @@ def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anc
     from nmag import SI
     sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor,
                           anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps,
-                          jacobian=jacobian, jacobian_demag_rtol=args.jac_rtol)
+                          jacobian=jacobian, jacobian_demag_rtol=args.jac_rtol,
+                          jv_precision=jv if jv is not None else args.jv)
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     sim.set_H_ext(h_ext_su() * 1e6, SI(1.0, "A/m"))
@@ -844,6 +846,7 @@ def run_jacobian_report(args):
     start, relax_rec = relax_states(args, args.form, args.cg, B, msh, base, seed, anchor)
     out = {"report": "jacobian", "workload": WORKLOAD_NAMES[args.workload], "form": args.form, "cg": args.cg,
            "members": B, "interval_ps": args.steps * args.step_ps, "jacobian_demag_rtol": args.jac_rtol,
+           "jv_at_level_0": args.jv,
            "relax": relax_rec, "levels": {}}
     ref_final = None
     for level in ("approximate", "local", "exact"):
@@ -1016,7 +1019,7 @@ def run_ours(args):
     if args.compare and not (args.form == "fp64" and args.cg == "fp64" and B == 1):
         start0 = start[0] if B > 1 else start
         plain = measure(args, "fp64", "fp64", 1, msh, start0, world, local, sample_clocks=False,
-                        warmup=1, e2e=False)
+                        warmup=1, e2e=False, jv="fp64")
     if rank != 0:
         return
     line = {
@@ -1025,7 +1028,8 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": {"fp64": "f64", "fp32": "f32 matrix, f64 sums",
                   "fp32x2": "f32+bf16 matrix, compensated f32 products (~2^-44)" + (
                       "; anchored: f32 products of the drift from the last compensated product"
-                      if anchor > 0 else "")}[args.form],
+                      if anchor > 0 else "")}[args.form] + (
+                      "; f32 Jacobian-vector products" if args.jv == "fp32" else ""),
         "data": "synthetic",
         "config": config_dict(args, msh),
         "rhs_evals_per_s": r["rhs_evals_per_s"], "bdf_steps": r["bdf_steps"], "rhs_evals": r["rhs_evals"],
@@ -1128,6 +1132,9 @@ def main():
     ap.add_argument("--batch-seconds", type=float, default=0.0,
                     help="after the timed launches, keep sweeping for this wall time and report the progress")
     ap.add_argument("--rhs", type=int, default=128, help="--report bem: right-hand sides per product")
+    ap.add_argument("--jv", default="fp32", choices=["fp64", "fp32"],
+                    help="arithmetic of the BDF's Jacobian-vector products and block preconditioner "
+                         "(the chosen form; the plain FP64 comparison always uses fp64)")
     ap.add_argument("--jac-rtol", type=float, default=1e-5,
                     help="Poisson tolerance of the exact Jacobian's demag response (--report jacobian)")
     ap.add_argument("--report", default=None, choices=["precision", "adjoint", "batch", "bem", "jacobian"],

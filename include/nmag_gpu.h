@@ -73,6 +73,12 @@ typedef struct nmg_options {
   int cg_local_sweeps;                   /* FP32 inner CG (cg_precision 1): damped Jacobi
                                             sweeps on each thread block's own rows in
                                             the preconditioner (0 or 1: Jacobi alone) */
+  int jv_precision;                      /* the BDF's Jacobian-vector products and block
+                                            preconditioner at Jacobian level 0: 0 FP64;
+                                            1 FP32 arithmetic on FP32 copies of the
+                                            frozen state, the exchange matrix and the
+                                            direction (the Newton matrix only: the
+                                            residual stays FP64)                      */
 } nmg_options;
 
 /* Integrator statistics (CVODE counters; nsim.ml:354-387 timings). */
@@ -287,7 +293,8 @@ int nmg_rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps);
  * element or polynomial), the C3 length term's, and with several materials
  * the local couplings; level 2 adds the demag field's response, the demag
  * field of each Krylov direction from one Neumann + BEM + Dirichlet pipeline
- * at Poisson tolerance demag_rtol (in (0, 1)) on buffers of its own.  The
+ * at Poisson tolerance demag_rtol (in (0, 1)) on buffers of its own (with
+ * the plain FP32 BEM product where the handle has an FP32 plane).  The
  * block-Jacobi preconditioner takes the local terms from level 1 on.  The
  * spin-torque terms are in none.  Changes the Newton iteration only: the
  * solution is the same to the integrator's tolerances. */

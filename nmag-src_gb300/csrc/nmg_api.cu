@@ -63,6 +63,8 @@ int nmg_create(const double *coords, int n_nodes, const int32_t *tets, int n_tet
     return fail(nullptr, -6, "nmg_create: bem_precision must be 0, 1, 2 or 3");
   if (opt && opt->bem_anchor_tol > 0.0 && opt->bem_precision != 2)
     return fail(nullptr, -6, "nmg_create: bem_anchor_tol applies to the compensated product (bem_precision 2)");
+  if (opt && (opt->jv_precision < 0 || opt->jv_precision > 1))
+    return fail(nullptr, -6, "nmg_create: jv_precision must be 0 or 1");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(nullptr, 101, "nmg_create: no CUDA device");
   nmg_handle *h = new nmg_handle();
@@ -423,6 +425,7 @@ int nmg_set_jacobian(nmg_handle *h, int level, double demag_rtol) {
   if (!h) return -1;
   if (level < 0 || level > 2) return fail(h, -2, "nmg_set_jacobian: level must be 0, 1 or 2");
   if (!(demag_rtol > 0.0 && demag_rtol < 1.0)) return fail(h, -2, "nmg_set_jacobian: demag_rtol must be in (0, 1)");
+  if (level != h->jac_level) nmg::ts_invalidate_setup(h->ts);   // the preconditioner follows the level
   h->jac_level = level;
   h->jac_rtol = demag_rtol;
   return 0;

@@ -264,6 +264,7 @@ struct nmg_handle {
   bool own_stream = true;       // false: the stream belongs to pot
   nmg::Tape *tape = nullptr;
   int anchor_hold = 0;          // >0: anchored BEM product suspended (RK4 tape runs recompute bit for bit)
+  int bem_fp32_only = 0;        // >0: the plain FP32 product even where the compensated one is set up
   // Jacobian of the BDF's Newton iteration: 0 the exchange part only (the
   // reference's); 1 also the local terms (anisotropy, the C3 length term,
   // local couplings); 2 also the demag response, from Poisson solves at
@@ -350,6 +351,7 @@ Integrator *ts_create(nmg_handle *h, int qmax, int maxl, double rtol, double ato
 void ts_destroy(Integrator *t);
 bool ts_matches(const Integrator *t, int qmax, int maxl);
 void ts_set_tolerances(Integrator *t, double rtol, double atol);
+void ts_invalidate_setup(Integrator *t);
 int ts_init(nmg_handle *h, double t0);
 int ts_advance(nmg_handle *h, double tout, int exact_tstop, int64_t max_steps, double *t_reached,
                nmg_ts_stats *st);

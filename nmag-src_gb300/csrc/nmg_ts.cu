@@ -391,16 +391,17 @@ struct JvArgs {
   double *out;
 };
 
-__device__ __forceinline__ void cross(const double *a, const double *b, double *c) {
+template <class T>
+__device__ __forceinline__ void cross(const T *a, const T *b, T *c) {
   c[0] = a[1] * b[2] - a[2] * b[1];
   c[1] = a[2] * b[0] - a[0] * b[2];
   c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
 // dF = C1 (w x H + m x hv) + C2 (w x (m x H) + m x (w x H + m x hv))
-__device__ __forceinline__ void jac_apply(const double *m, const double *H, const double *w, const double *hv,
-                                          double C1, double C2, double *out) {
-  double wxH[3], mxhv[3], mxH[3], t1[3], u[3], t2[3];
+template <class T>
+__device__ __forceinline__ void jac_apply(const T *m, const T *H, const T *w, const T *hv, T C1, T C2, T *out) {
+  T wxH[3], mxhv[3], mxH[3], t1[3], u[3], t2[3];
   cross(w, H, wxH);
   cross(m, hv, mxhv);
   cross(m, H, mxH);
@@ -466,6 +467,76 @@ __global__ void k_jv_psolve(JvArgs a) {
   }
 }
 
+// FP32 form of the level-0 J v (jv_precision 1): the same products in FP32
+// arithmetic on FP32 copies of the frozen state (mJ, HJ), the preconditioner
+// blocks, the exchange matrix and the direction t; out (FP64) as k_jv_psolve's.
+// The Newton matrix only needs the accuracy of an approximate Jacobian; its
+// FP64 form is bound by the FP64 pipe.
+struct Jv32Args {
+  int N, nrep;
+  const int32_t *row_ptr, *col_idx;
+  const float *K, *mJ, *HJ, *t, *Pinv;
+  const double *ivol, *ewt, *pin;
+  const int32_t *site_mat;
+  const SiteMat *mt;
+  double c_exch, C1, C2, gamma;
+  int psolve, scale_out, raw;
+  double *out;
+};
+
+__global__ void k_jv32(Jv32Args a) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= (long long)a.N * a.nrep) return;
+  const int mbr = (int)(g / a.N), i = (int)(g - (long long)mbr * a.N);
+  const float *tm = a.t + (size_t)mbr * 3 * a.N;
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  for (int k = a.row_ptr[i]; k < a.row_ptr[i + 1]; ++k) {
+    const float *tj = tm + 3 * (size_t)a.col_idx[k];
+    const float kv = a.K[k];
+    s0 = fmaf(kv, tj[0], s0); s1 = fmaf(kv, tj[1], s1); s2 = fmaf(kv, tj[2], s2);
+  }
+  double c_exch = a.c_exch, C1 = a.C1, C2 = a.C2;
+  if (a.site_mat) {
+    const SiteMat &c = a.mt[a.site_mat[i]];
+    c_exch = c.c_exch; C1 = c.C1; C2 = c.C2;
+  }
+  const float ce = (float)(-c_exch * a.ivol[i]);
+  const float hv[3] = {ce * s0, ce * s1, ce * s2};
+  const float *m = a.mJ + 3 * (size_t)g, *H = a.HJ + 3 * (size_t)g, *w = a.t + 3 * (size_t)g;
+  float jw[3];
+  jac_apply<float>(m, H, w, hv, (float)C1, (float)C2, jw);
+  if (a.pin) {
+    const float p = (float)a.pin[i];
+    jw[0] *= p; jw[1] *= p; jw[2] *= p;
+  }
+  if (a.raw) {
+    for (int d = 0; d < 3; ++d) a.out[3 * (size_t)g + d] = (double)jw[d];
+    return;
+  }
+  const float gm = (float)a.gamma;
+  const float r[3] = {w[0] - gm * jw[0], w[1] - gm * jw[1], w[2] - gm * jw[2]};
+  float z[3] = {r[0], r[1], r[2]};
+  if (a.psolve) {
+    const float *Pi = a.Pinv + 9 * (size_t)g;
+    for (int d = 0; d < 3; ++d) z[d] = fmaf(Pi[3 * d], r[0], fmaf(Pi[3 * d + 1], r[1], Pi[3 * d + 2] * r[2]));
+  }
+  for (int d = 0; d < 3; ++d) {
+    const size_t o = 3 * (size_t)g + d;
+    a.out[o] = a.scale_out ? a.ewt[o] * (double)z[d] : (double)z[d];
+  }
+}
+
+// t32 = (float)(v / ewt): the FP32 direction of k_jv32
+__global__ void k_div_ewt32(int n, const double *__restrict__ v, const double *__restrict__ ws, float *__restrict__ o) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) o[i] = (float)(v[i] * ws[i]);
+}
+
+__global__ void k_to_f32(long long n, const double *__restrict__ x, float *__restrict__ y) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = (float)x[i];
+}
+
 // The block-Jacobi preconditioner's 3x3 blocks P = I - gamma_p dF/dm (the
 // exchange diagonal and the site terms at the setup state mJ, HJ; at
 // Jacobian level >= 1 also the local anisotropy and C3 terms), inverted once
@@ -474,7 +545,8 @@ __global__ void k_pprep(int N, const int32_t *__restrict__ diag_pos, const doubl
                         const double *__restrict__ vol, const double *__restrict__ mJ, const double *__restrict__ HJ,
                         double c_exch, double C1, double C2, double gammap, double *__restrict__ Pinv, int nrep,
                         const double *__restrict__ pin, const int32_t *__restrict__ site_mat,
-                        const SiteMat *__restrict__ mt, LocalJac L) {
+                        const SiteMat *__restrict__ mt, LocalJac L, float *__restrict__ Pinv32,
+                        float *__restrict__ mJ32, float *__restrict__ HJ32) {
   const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (g >= (long long)N * nrep) return;
   const int i = (int)(g % N);
@@ -503,6 +575,13 @@ __global__ void k_pprep(int N, const int32_t *__restrict__ diag_pos, const doubl
   o[0] = c00 * inv; o[1] = (P[0][2] * P[2][1] - P[0][1] * P[2][2]) * inv; o[2] = (P[0][1] * P[1][2] - P[0][2] * P[1][1]) * inv;
   o[3] = c01 * inv; o[4] = (P[0][0] * P[2][2] - P[0][2] * P[2][0]) * inv; o[5] = (P[0][2] * P[1][0] - P[0][0] * P[1][2]) * inv;
   o[6] = c02 * inv; o[7] = (P[0][1] * P[2][0] - P[0][0] * P[2][1]) * inv; o[8] = (P[0][0] * P[1][1] - P[0][1] * P[1][0]) * inv;
+  if (Pinv32) {   // jv_precision 1: the FP32 copies k_jv32 reads
+    for (int q = 0; q < 9; ++q) Pinv32[9 * (size_t)g + q] = (float)o[q];
+    for (int d = 0; d < 3; ++d) {
+      mJ32[3 * (size_t)g + d] = (float)m[d];
+      HJ32[3 * (size_t)g + d] = (float)H[d];
+    }
+  }
 }
 
 // Block-Jacobi preconditioner alone: out = ewt * P^{-1} r (r unscaled).
@@ -525,6 +604,9 @@ struct Integrator {
   double rtol, atol;
   DevBuf<double> znbuf, ewt, acor, y, tempv, ftemp, xsol, mJ, HJ, Vbuf, tvec, part, hdev, hcol;
   DevBuf<double> Pinv;   // preconditioner blocks inverted at each setup (9 per node and member)
+  // jv_precision 1: FP32 copies of the preconditioner blocks, the frozen
+  // state, the exchange matrix, and the direction
+  DevBuf<float> Pinv32, mJ32, HJ32, K32, t32;
   DevBuf<double> ewts;   // 1 / ewt
   double *zn[QMAXB + 2];
   std::vector<double *> V;
@@ -638,6 +720,22 @@ LocalJac local_jac_args(const nmg_handle *h) {
   return L;
 }
 
+// The FP32 J v form: jv_precision 1 at Jacobian level 0
+bool jv_fp32(const nmg_handle *h) { return h->opt.jv_precision == 1 && h->jac_level == 0; }
+
+Jv32Args jv32_base(nmg_handle *h) {
+  const Mesh &M = h->mesh;
+  Jv32Args a;
+  a.N = M.N; a.nrep = h->nrep; a.row_ptr = M.row_ptr; a.col_idx = M.col_idx;
+  a.K = a.mJ = a.HJ = a.t = a.Pinv = nullptr;
+  a.ivol = M.ivol; a.ewt = nullptr; a.pin = h->pin.p;
+  a.site_mat = h->pot ? h->sites.site_mat.p : nullptr;
+  a.mt = h->sites.mtab.p;
+  a.c_exch = h->mat.exch_coeff; a.C1 = h->mat.C1; a.C2 = h->mat.C2; a.gamma = 0.0;
+  a.psolve = 0; a.scale_out = 0; a.raw = 0; a.out = nullptr;
+  return a;
+}
+
 bool demag_in_jacobian(const nmg_handle *h) {
   return h->jac_level >= 2 && h->opt.do_demag && (h->pot ? h->pot->mesh.nb : h->mesh.nb) > 0;
 }
@@ -735,13 +833,23 @@ int spgmr(Integrator &I, const double *b, double *x, double delta, int *nli_out)
   for (int l = 0; l < maxl; ++l) {
     // t = V_l / ewt in its own pass: inside the FP64-bound Jv kernel the
     // division would be repeated for every neighbour reference
-    k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewts, I.tvec); ++I.hd->launches;
-    JvArgs a = jv_args(I, I.tvec, I.V[l + 1], 1);
-    if (demag_in_jacobian(I.hd)) {   // exact Jacobian: the demag field of the direction
-      if (demag_response(I.hd, I.tvec)) return -1;
-      a.hdv = I.hd->jd.hdv;
-    }
-    {
+    if (jv_fp32(I.hd)) {
+      if (!I.K32.p) return -1;   // set up with every preconditioner setup (never reached)
+      k_div_ewt32<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewts, I.t32); ++I.hd->launches;
+      Jv32Args a = jv32_base(I.hd);
+      a.K = I.K32; a.mJ = I.mJ32; a.HJ = I.HJ32; a.t = I.t32; a.Pinv = I.Pinv32; a.ewt = I.ewt;
+      a.gamma = I.gamma; a.psolve = 1; a.scale_out = 1; a.out = I.V[l + 1];
+      NMG_PROF_BEGIN(I.hd, 4);
+      k_jv32<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(a);
+      ++I.hd->launches;
+      NMG_PROF_END(I.hd);
+    } else {
+      k_div_ewt<<<nblk(n, 256), 256, 0, I.s()>>>(n, I.V[l], I.ewts, I.tvec); ++I.hd->launches;
+      JvArgs a = jv_args(I, I.tvec, I.V[l + 1], 1);
+      if (demag_in_jacobian(I.hd)) {   // exact Jacobian: the demag field of the direction
+        if (demag_response(I.hd, I.tvec)) return -1;
+        a.hdv = I.hd->jd.hdv;
+      }
       NMG_PROF_BEGIN(I.hd, 4);
       if (a.L.on) k_jv_psolve<true><<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(a);
       else k_jv_psolve<false><<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(a);
@@ -869,7 +977,7 @@ int nls(Integrator &I, int nflag_first) {
   const int n = I.n;
   int convfail_bad_j = 0;
   int call_setup = (nflag_first == 2) || (nflag_first == 3) || (I.nst == 0) || (I.nst >= I.nstlp + MSBP) ||
-                   (std::fabs(I.gamrat - 1.0) > DGMAX);
+                   (std::fabs(I.gamrat - 1.0) > DGMAX) || !I.setup_done;
   const int convfail_other = !(nflag_first == 1 || nflag_first == 3);
   for (;;) {
     if (I.rhs(I.zn[0], I.ftemp)) return -2;
@@ -889,10 +997,23 @@ int nls(Integrator &I, int nflag_first) {
       {
         const Mesh &M = I.hd->mesh;
         const nmg_material &mt = I.hd->mat;
+        const bool f32 = jv_fp32(I.hd);
+        if (f32) {
+          if (!I.K32.p) {   // the FP32 copies, once per integrator
+            bool ok = I.K32.alloc(M.nnz) == cudaSuccess && I.Pinv32.alloc(3 * (size_t)I.n) == cudaSuccess;
+            for (DevBuf<float> *b : {&I.mJ32, &I.HJ32, &I.t32}) ok = ok && b->alloc(I.n) == cudaSuccess;
+            if (!ok) {
+              I.hd->last_error = "BDF: cannot allocate the FP32 Jacobian copies";
+              return -3;
+            }
+          }
+          k_to_f32<<<nblk((long long)M.nnz, 256), 256, 0, I.s()>>>(M.nnz, I.hd->exch_K(), I.K32);
+          ++I.hd->launches;
+        }
         k_pprep<<<nblk((long long)M.N * I.hd->nrep, 128), 128, 0, I.s()>>>(
             M.N, M.diag_pos, I.hd->exch_K(), M.vol, I.mJ, I.HJ, mt.exch_coeff, mt.C1, mt.C2, I.gammap, I.Pinv,
             I.hd->nrep, I.hd->pin.p, I.hd->pot ? I.hd->sites.site_mat.p : nullptr, I.hd->sites.mtab.p,
-            local_jac_args(I.hd));
+            local_jac_args(I.hd), f32 ? I.Pinv32.p : nullptr, I.mJ32.p, I.HJ32.p);
         ++I.hd->launches;
       }
     }
@@ -1126,6 +1247,10 @@ Integrator *ts_create(nmg_handle *h, int qmax, int maxl, double rtol, double ato
 }
 
 bool ts_matches(const Integrator *I, int qmax, int maxl) { return I->qmax == qmax && I->maxl == maxl; }
+// The next Newton iteration sets up its preconditioner afresh (the Jacobian's level changed).
+void ts_invalidate_setup(Integrator *I) {
+  if (I) I->setup_done = 0;
+}
 void ts_set_tolerances(Integrator *I, double rtol, double atol) { I->rtol = rtol; I->atol = atol; }
 
 void ts_destroy(Integrator *I) {
@@ -1228,6 +1353,22 @@ int rk4_device(nmg_handle *h, double *d_m, double dt, int nsteps) {
 // without the preconditioner.
 int jacobian_apply(nmg_handle *h, const double *d_m, const double *d_v, double *d_out) {
   if (rhs_eval(h, d_m, nullptr)) return 100;
+  if (jv_fp32(h)) {   // the FP32 form on FP32 copies, as the integrator forms them
+    const long long n = 3LL * h->mesh.N * h->nrep, nnz = h->mesh.nnz;
+    DevBuf<float> buf;
+    if (buf.alloc((size_t)(nnz + 3 * n)) != cudaSuccess) return 100;
+    float *K32 = buf.p, *m32 = K32 + nnz, *H32 = m32 + n, *t32 = H32 + n;
+    k_to_f32<<<nblk(nnz, 256), 256, 0, h->stream>>>(nnz, h->exch_K(), K32);
+    k_to_f32<<<nblk(n, 256), 256, 0, h->stream>>>(n, d_m, m32);
+    k_to_f32<<<nblk(n, 256), 256, 0, h->stream>>>(n, h->ws.h_total, H32);
+    k_to_f32<<<nblk(n, 256), 256, 0, h->stream>>>(n, d_v, t32);
+    Jv32Args a = jv32_base(h);
+    a.K = K32; a.mJ = m32; a.HJ = H32; a.t = t32; a.raw = 1; a.out = d_out;
+    k_jv32<<<nblk((long long)h->mesh.N * h->nrep, 128), 128, 0, h->stream>>>(a);
+    h->launches += 5;
+    if (cudaGetLastError() != cudaSuccess) return 100;
+    return check_device_error(h, "nmg_jacobian_apply");   // synchronises before buf is freed
+  }
   JvArgs a = jv_base(h);
   a.mJ = d_m; a.HJ = h->ws.h_total; a.t = d_v; a.raw = 1; a.out = d_out;
   if (demag_in_jacobian(h)) {

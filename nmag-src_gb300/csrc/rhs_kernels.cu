@@ -2721,7 +2721,7 @@ void bem_gemv(nmg_handle *h, const double *x, double *y) {
     ++h->launches;
     return;
   }
-  if (f == 1 && M.bem16lo.p) {   // compensated FP32 pair product
+  if (f == 1 && M.bem16lo.p && !h->bem_fp32_only) {   // compensated FP32 pair product
     float *xh = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
     float *xl = xh + M.ld;
     k_split_x<<<nblk(M.ld, 256), 256, 0, h->stream>>>(nb, M.ld, 1, x, xh, xl); ++h->launches;
@@ -2820,7 +2820,7 @@ void bem_gemm(nmg_handle *h, const double *x, double *y) {
       ++h->launches;
       continue;
     }
-    if (f == 1 && M.bem16lo.p) {   // compensated FP32 pair product on tiles
+    if (f == 1 && M.bem16lo.p && !h->bem_fp32_only) {   // compensated FP32 pair product on tiles
       float *xh = reinterpret_cast<float *>(W.bpart.p + W.gemv_x32_off);
       float *xl = xh + (size_t)nm * M.ld;
       k_split_x<<<nblk((long long)M.ld * nm, 256), 256, 0, h->stream>>>(nb, M.ld, nm, xc, xh, xl); ++h->launches;
@@ -3037,12 +3037,16 @@ int jac_demag_solve(nmg_handle *P, JacDemag &J, double rtol) {
   Workspace &W = P->ws;
   const double nr = P->opt.nbc_rtol, dr = P->opt.dbc_rtol;
   swap_jac_buffers(W, J);
-  P->anchor_hold++;   // the direction is no small change of the anchored state: plain product
+  // the direction is no small change of the anchored state, and the Newton
+  // matrix needs no compensated product: the plain FP32 one where it exists
+  P->anchor_hold++;
+  P->bem_fp32_only++;
   P->opt.nbc_rtol = rtol;
   P->opt.dbc_rtol = rtol;
   const int rc = demag_from_rho(P);
   P->opt.nbc_rtol = nr;
   P->opt.dbc_rtol = dr;
+  P->bem_fp32_only--;
   P->anchor_hold--;
   swap_jac_buffers(W, J);
   if (rc) return rc;

@@ -27,7 +27,8 @@ class Options(C.Structure):
                 ("dbc_rtol", C.c_double), ("dbc_atol", C.c_double), ("dbc_maxits", C.c_int),
                 ("bem_precision", C.c_int), ("cg_precision", C.c_int), ("cg_no_coarse", C.c_int),
                 ("n_members", C.c_int), ("bem_anchor_tol", C.c_double),
-                ("adjoint_cg_precision", C.c_int), ("anchor_product", C.c_int), ("cg_local_sweeps", C.c_int)]
+                ("adjoint_cg_precision", C.c_int), ("anchor_product", C.c_int), ("cg_local_sweeps", C.c_int),
+                ("jv_precision", C.c_int)]
 
 
 class Particle(C.Structure):

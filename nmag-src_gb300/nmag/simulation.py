@@ -123,7 +123,7 @@ class Simulation(object):
                  timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
                  lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1, cg_precision="fp64",
                  bem_anchor=0.0, adjoint_cg_precision="fp64", anchor_product="fp32", cg_local_sweeps=0,
-                 jacobian="approximate", jacobian_demag_rtol=1e-5):
+                 jacobian="approximate", jacobian_demag_rtol=1e-5, jv_precision="fp64"):
         if periodic_bc is not None:
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
@@ -164,6 +164,11 @@ class Simulation(object):
         self.jacobian_demag_rtol = float(jacobian_demag_rtol)
         if not 0.0 < self.jacobian_demag_rtol < 1.0:
             raise ValueError("jacobian_demag_rtol must be in (0, 1)")
+        # the approximate Jacobian's products and block preconditioner in FP32
+        # arithmetic ("fp32") or FP64; the Newton residual stays FP64
+        if jv_precision not in ("fp64", "fp32"):
+            raise ValueError("jv_precision must be 'fp64' or 'fp32'")
+        self.jv_precision = jv_precision
         # several magnetic materials: the site layout (None: one material)
         self.layer = None
         self.materials = []
@@ -248,6 +253,7 @@ class Simulation(object):
         opts.adjoint_cg_precision = {"fp64": 0, "fp32": 1}[self.adjoint_cg_precision]
         opts.anchor_product = {"fp32": 0, "fp16": 1}[self.anchor_product]
         opts.cg_local_sweeps = self.cg_local_sweeps
+        opts.jv_precision = {"fp64": 0, "fp32": 1}[self.jv_precision]
         self.layer = None
         if self._multi:
             names = [mt.name for mt in self.materials]

@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 
 def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0, anchor=0.0, adjoint_cg=0,
-                  anchor_product=0):
+                  anchor_product=0, jv_precision=0):
     from nmag import _lib
     single = make_engine(msh, mat, tol=tol, bem_precision=bem_precision)
     c = mat.coefficients("nmag")
@@ -31,6 +31,7 @@ def make_ensemble(msh, mat, B, tol=1e-12, bem_precision=0, cg_precision=0, ancho
     op.bem_anchor_tol = anchor
     op.adjoint_cg_precision = adjoint_cg
     op.anchor_product = anchor_product
+    op.jv_precision = jv_precision
     ens = _lib.Engine(msh.points, msh.simplices, mt, op)
     if c.get("anis_poly") is not None:
         ens.set_anisotropy_poly(*c["anis_poly"])

@@ -206,3 +206,63 @@ def test_simulation_exact_jacobian_option(cube):
     d = np.abs(finals[0] - finals[1]).max()
     print("Simulation after 50 ps, approximate against exact Jacobian: max |dm| %.2e" % d)
     assert d <= 1e-4
+
+
+def test_fp32_jacobian_products_match_fp64(cube):
+    """jv_precision 1: the approximate Jacobian's products in FP32 arithmetic
+    against the FP64 ones, for a smooth and a rough direction (relative to
+    max |J v|: FP32 rounding of ~15-term sums, 1e-5); one member and an
+    ensemble of three."""
+    from test_gpu_ensemble import make_ensemble
+    N = len(cube.points)
+    rng = np.random.default_rng(4)
+    for B in (1, 3):
+        engs = []
+        for prec in (0, 1):
+            if B == 1:
+                e = make_engine(cube, anis_material(), tol=1e-12, jv_precision=prec)
+            else:
+                e, single = make_ensemble(cube, anis_material(), B, tol=1e-12, jv_precision=prec)
+                single.close()
+            e.set_h_ext(np.array([0.02, 0.0, -0.01]))
+            engs.append(e)
+        ms = np.stack([seeded_m(N, base=(1.0, 0.3, 0.5), seed=60 + b, noise=0.2) for b in range(B)])
+        for kind in ("smooth", "rough"):
+            if kind == "smooth":
+                vs = np.stack([smooth_direction(cube.points, ms[b], 70 + b) for b in range(B)])
+            else:
+                vs = rng.standard_normal((B, N, 3))
+            m_in, v_in = (ms[0], vs[0]) if B == 1 else (ms, vs)
+            ref, got = jv(engs[0], m_in, v_in), jv(engs[1], m_in, v_in)
+            err = np.abs(got - ref).max() / np.abs(ref).max()
+            print("FP32 J v, %d member(s), %s direction: %.2e of max |J v|" % (B, kind, err))
+            assert err <= 1e-5, (B, kind, err)
+        for e in engs:
+            e.close()
+
+
+def test_fp32_jacobian_trajectory_matches_oracle(cube):
+    """The BDF with FP32 Jacobian-vector products: m(t) of the cube (uniaxial
+    anisotropy, alpha 0.5) every 10 ps over 300 ps against the oracle's BDF
+    within 1e-4, and the Newton / Krylov counts beside the FP64 form's."""
+    import oracle
+    from test_gpu_trajectory import _oracle_run
+    mat = anis_material(0.5)
+    om = oracle.OracleMesh(cube.points, cube.simplices)
+    m0 = seeded_m(om.n_nodes, base=(1.0, 0.6, -0.4), seed=2, noise=0.05)
+    h = np.array([0.02, 0.0, 0.0])
+    times = [10.0 * k for k in range(1, 31)]
+    mo, _, so = _oracle_run(om, mat, m0, h, times, 1e-10)
+    for prec in (0, 1):
+        eng = make_engine(cube, mat, tol=1e-10, jv_precision=prec)
+        eng.set_h_ext(h)
+        eng.set_m(m0)
+        eng.ts_init(0.0, 1e-6, 1e-6, 2, 300)
+        dm = []
+        for k, t in enumerate(times):
+            _, st = eng.ts_advance(t)
+            dm.append(np.abs(eng.get_m() - mo[k]).max())
+        print("jv_precision %d: max |dm| %.2e over 300 ps; steps %d, Newton %d, Krylov %d, convergence failures %d"
+              % (prec, max(dm), st["nst"], st["nni"], st["nli"], st["ncfn"]))
+        assert max(dm) <= 1e-4, (prec, max(dm))
+        eng.close()

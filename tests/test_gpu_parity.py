@@ -20,7 +20,7 @@ from conftest import permalloy, seeded_m
 pytestmark = pytest.mark.gpu
 
 
-def make_engine(msh, mat, do_demag=True, tol=1e-12, bem_precision=0):
+def make_engine(msh, mat, do_demag=True, tol=1e-12, bem_precision=0, jv_precision=0):
     from nmag import _lib
     c = mat.coefficients("nmag")
     mt = _lib.Material()
@@ -34,6 +34,7 @@ def make_engine(msh, mat, do_demag=True, tol=1e-12, bem_precision=0):
     op.nbc_atol = op.dbc_atol = 1e-50
     op.nbc_maxits = op.dbc_maxits = 20000
     op.bem_precision = bem_precision
+    op.jv_precision = jv_precision
     eng = _lib.Engine(msh.points, msh.simplices, mt, op)
     if c.get("anis_poly") is not None:
         eng.set_anisotropy_poly(*c["anis_poly"])
