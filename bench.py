@@ -288,7 +288,7 @@ def config_dict(args, msh):
             "step": "%g ps advance in %g ps records, each followed by an <m> read" % (args.step_ps, args.record_ps),
             "interval_ps": args.steps * args.step_ps,
             "form": args.form, "cg": args.cg, "cg_local_sweeps": args.cg_sweeps, "members": args.members,
-            "jv": args.jv,
+            "jv": args.jv, "cg_coarse": not args.cg_no_coarse,
             "bem_anchor": args.anchor if args.form == "fp32x2" else 0.0,
             "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
             "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % {"fp64": 8, "fp32": 4,
@@ -350,7 +350,7 @@ def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anc
     sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor,
                           anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps,
                           jacobian=jacobian, jacobian_demag_rtol=args.jac_rtol,
-                          jv_precision=jv if jv is not None else args.jv)
+                          jv_precision=jv if jv is not None else args.jv, cg_coarse=not args.cg_no_coarse)
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     sim.set_H_ext(h_ext_su() * 1e6, SI(1.0, "A/m"))
@@ -1132,6 +1132,8 @@ def main():
     ap.add_argument("--batch-seconds", type=float, default=0.0,
                     help="after the timed launches, keep sweeping for this wall time and report the progress")
     ap.add_argument("--rhs", type=int, default=128, help="--report bem: right-hand sides per product")
+    ap.add_argument("--cg-no-coarse", action="store_true",
+                    help="Neumann CG with Jacobi alone (no aggregation coarse level)")
     ap.add_argument("--jv", default="fp32", choices=["fp64", "fp32"],
                     help="arithmetic of the BDF's Jacobian-vector products and block preconditioner "
                          "(the chosen form; the plain FP64 comparison always uses fp64)")

@@ -123,7 +123,7 @@ class Simulation(object):
                  timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
                  lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1, cg_precision="fp64",
                  bem_anchor=0.0, adjoint_cg_precision="fp64", anchor_product="fp32", cg_local_sweeps=0,
-                 jacobian="approximate", jacobian_demag_rtol=1e-5, jv_precision="fp64"):
+                 jacobian="approximate", jacobian_demag_rtol=1e-5, jv_precision="fp64", cg_coarse=True):
         if periodic_bc is not None:
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
@@ -169,6 +169,8 @@ class Simulation(object):
         if jv_precision not in ("fp64", "fp32"):
             raise ValueError("jv_precision must be 'fp64' or 'fp32'")
         self.jv_precision = jv_precision
+        # the Neumann CG's aggregation coarse level (False: Jacobi alone)
+        self.cg_coarse = bool(cg_coarse)
         # several magnetic materials: the site layout (None: one material)
         self.layer = None
         self.materials = []
@@ -254,6 +256,7 @@ class Simulation(object):
         opts.anchor_product = {"fp32": 0, "fp16": 1}[self.anchor_product]
         opts.cg_local_sweeps = self.cg_local_sweeps
         opts.jv_precision = {"fp64": 0, "fp32": 1}[self.jv_precision]
+        opts.cg_no_coarse = 0 if self.cg_coarse else 1
         self.layer = None
         if self._multi:
             names = [mt.name for mt in self.materials]
