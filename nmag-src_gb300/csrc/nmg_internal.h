@@ -89,6 +89,9 @@ struct Workspace {
   DevBuf<int32_t> perm, prow, pcol, pbnd;     // CG solver ordering (spatially binned nodes)
   DevBuf<double> pK, xperm, ainv, rc;         // K in that order, iterate, coarse inverse, coarse residual
   DevBuf<float> ainv32, rc32, z32, rw32;      // FP32 copies / vectors of the mixed-precision CG
+  DevBuf<int32_t> mcol, mmid;                 // the mixed-precision CG's shared-memory row order
+  DevBuf<double> mK;                          //   its values, modes 0 and 1 (2 x nnz)
+  DevBuf<float> mK32;                         //   and their FP32 copies
   int cg_smem_mp = 0;                         // dynamic shared memory of the mixed-precision CG
   int nc = 0;                                 // aggregates of the two-level Neumann CG (0: none)
   int cg_blocks = 0;
@@ -270,7 +273,7 @@ struct nmg_handle {
   // local couplings); 2 also the demag response, from Poisson solves at
   // jac_rtol (one pair per Jacobian-vector product)
   int jac_level = 0;
-  double jac_rtol = 1e-5;
+  double jac_rtol = 1e-3;
   nmg::JacDemag jd;
   // the mixed-precision CG is used by the forward solves or the adjoint's
   bool mixed_cg() const { return opt.cg_precision == 1 || opt.adjoint_cg_precision == 1; }

@@ -178,6 +178,12 @@ struct CGArgs {
   float *rc32, *z32;  // coarse residual (nc x MB), published inner direction (N x MB)
   float *rw32;        // R w of every aggregate (nc x MB), published with the inner dot products
   float eta;          // inner relative tolerance
+  // the mixed-precision CG's rows as each block keeps them in shared memory:
+  // the columns inside the block's row range first (mmid[r] of them), values
+  // with the Dirichlet rows' boundary columns zeroed for mode 1
+  const int32_t *mcol, *mmid;
+  const double *mK0, *mK1;
+  const float *mK32_0, *mK32_1;
   int max_outer;      // FP64 refinement steps
   int local_sweeps;   // mixed-precision CG: damped Jacobi sweeps on the block's own rows (1: plain Jacobi)
 };
@@ -890,14 +896,19 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
   const int node = active ? a.perm[r] : 0;
   const int base = a.prow[row0];
   const int rend = a.prow[min(row0 + (int)blockDim.x, N)];
-  for (int k = base + tid; k < rend; k += blockDim.x) {
-    const int j = a.pcol[k];
-    const double kv = (a.mode == 1 && a.pbnd[j]) ? 0.0 : a.pK[k];
-    sC[k - base] = j;
-    sK[k - base] = kv;
-    sK32[k - base] = (float)kv;
+  {   // the block's rows in their shared-memory order (made at setup): in each row
+      // the columns inside the block's row range first, applied from the block's
+      // own u while the barrier that publishes u completes; independent loads only
+    const double *mK = a.mode == 1 ? a.mK1 : a.mK0;
+    const float *mK32 = a.mode == 1 ? a.mK32_1 : a.mK32_0;
+#pragma unroll 4
+    for (int k = base + tid; k < rend; k += blockDim.x) {
+      sC[k - base] = __ldg(a.mcol + k);
+      sK[k - base] = __ldg(mK + k);
+      sK32[k - base] = __ldg(mK32 + k);
+    }
   }
-  int lo = 0, hi = 0;
+  int lo = 0, hi = 0, mid = 0;
   bool ident = false;
   double dinv = 1.0;
   double xi[MB];
@@ -909,6 +920,7 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
   if (active) {
     lo = a.prow[r] - base;
     hi = a.prow[r + 1] - base;
+    mid = lo + a.mmid[r];
     ident = a.mode == 1 && a.pbnd[r];
     dinv = a.dinv[node];
 #pragma unroll
@@ -930,21 +942,6 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
     s_head[tid] = tid < nm ? B.ring[2 * tid + 1] : 0;
   }
   __syncthreads();
-  // each row's columns inside the block's row range first (read from shared
-  // memory while the barrier that publishes u completes); after the barrier
-  // above, every row's entries are in place
-  int mid = lo;
-  for (int k = lo; k < hi; ++k) {
-    const int j = sC[k];
-    if (j >= row0 && j < row0 + kCGThreads) {
-      if (k != mid) {
-        const int tc = sC[mid]; sC[mid] = j; sC[k] = tc;
-        const double td = sK[mid]; sK[mid] = sK[k]; sK[k] = td;
-        const float tf = sK32[mid]; sK32[mid] = sK32[k]; sK32[k] = tf;
-      }
-      ++mid;
-    }
-  }
   // FP64 operator on the published member-minor FP64 vector
   auto apply64 = [&](const double *v, double (&s)[MB]) {
 #pragma unroll
@@ -2349,6 +2346,42 @@ int build_cg_ordering(nmg_handle *h, std::string &err) {
   NMG_CUDA_TRY(cudaMemcpy(W.pcol.p, pcol.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice), "h2d");
   NMG_CUDA_TRY(cudaMemcpy(W.pbnd.p, pbnd.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "h2d");
   NMG_CUDA_TRY(cudaMemcpy(W.pK.p, pK.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice), "h2d");
+  if (h->mixed_cg()) {
+    // the mixed-precision CG's shared-memory row order, made once here: in each
+    // row the columns inside the block's row range (kCGThreads rows) first, by
+    // the same swaps the kernel would make; mode 1 zeroes boundary columns
+    std::vector<int32_t> mcol(pcol), mmid(N, 0);
+    std::vector<double> mK0(pK), mK1(nnz);
+    for (int k = 0; k < nnz; ++k) mK1[k] = 0.0;
+    for (int r = 0; r < N; ++r) {
+      const int row0 = (r / kCGThreads) * kCGThreads;
+      for (int k = prow[r]; k < prow[r + 1]; ++k) mK1[k] = pbnd[pcol[k]] ? 0.0 : pK[k];
+      int mid = prow[r];
+      for (int k = prow[r]; k < prow[r + 1]; ++k) {
+        const int j = mcol[k];
+        if (j >= row0 && j < row0 + kCGThreads) {
+          if (k != mid) {
+            std::swap(mcol[mid], mcol[k]);
+            std::swap(mK0[mid], mK0[k]);
+            std::swap(mK1[mid], mK1[k]);
+          }
+          ++mid;
+        }
+      }
+      mmid[r] = mid - prow[r];
+    }
+    std::vector<float> m32(2 * (size_t)nnz);
+    for (int k = 0; k < nnz; ++k) { m32[k] = (float)mK0[k]; m32[nnz + (size_t)k] = (float)mK1[k]; }
+    NMG_CUDA_TRY(W.mcol.alloc(nnz), "alloc");
+    NMG_CUDA_TRY(W.mmid.alloc(N), "alloc");
+    NMG_CUDA_TRY(W.mK.alloc(2 * (size_t)nnz), "alloc");
+    NMG_CUDA_TRY(W.mK32.alloc(2 * (size_t)nnz), "alloc");
+    NMG_CUDA_TRY(cudaMemcpy(W.mcol.p, mcol.data(), sizeof(int32_t) * nnz, cudaMemcpyHostToDevice), "h2d");
+    NMG_CUDA_TRY(cudaMemcpy(W.mmid.p, mmid.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice), "h2d");
+    NMG_CUDA_TRY(cudaMemcpy(W.mK.p, mK0.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice), "h2d");
+    NMG_CUDA_TRY(cudaMemcpy(W.mK.p + nnz, mK1.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice), "h2d");
+    NMG_CUDA_TRY(cudaMemcpy(W.mK32.p, m32.data(), sizeof(float) * 2 * nnz, cudaMemcpyHostToDevice), "h2d");
+  }
   W.nc = 0;
   const int nc = (N + kAgg - 1) / kAgg;
   if (h->opt.cg_no_coarse || nc > kMaxCoarse || nc < 2) return 0;
@@ -2458,6 +2491,8 @@ int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm,
   a.coarse = (mode == 0 && W.nc > 0) ? 1 : 0;
   a.nc = W.nc; a.ainv = W.ainv; a.rc = W.rc;
   a.ainv32 = W.ainv32; a.rc32 = W.rc32; a.z32 = W.z32; a.rw32 = W.rw32;
+  a.mcol = W.mcol; a.mmid = W.mmid; a.mK0 = W.mK; a.mK1 = W.mK.p ? W.mK.p + M.nnz : nullptr;
+  a.mK32_0 = W.mK32; a.mK32_1 = W.mK32.p ? W.mK32.p + M.nnz : nullptr;
   a.eta = 1e-3f; a.max_outer = 10;
   a.local_sweeps = h->opt.cg_local_sweeps > 1 ? h->opt.cg_local_sweeps : 1;
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);

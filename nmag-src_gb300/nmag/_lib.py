@@ -423,7 +423,7 @@ class Engine(object):
         """y_n = B x_n for n_rhs member-major boundary vectors (device addresses)."""
         check(lib().nmg_bem_apply(self.h, C.c_void_p(d_x), C.c_void_p(d_y), int(n_rhs)), self.h, "bem_apply")
 
-    def set_jacobian(self, level, demag_rtol=1e-5):
+    def set_jacobian(self, level, demag_rtol=1e-3):
         """The Newton matrix's Jacobian: 0 the reference's (exchange only), 1 + the local
         terms, 2 + the demag response (Poisson solves at demag_rtol)."""
         check(lib().nmg_set_jacobian(self.h, int(level), float(demag_rtol)), self.h, "set_jacobian")

@@ -123,7 +123,7 @@ class Simulation(object):
                  timestepper_krylov_max=300, ksp_tolerances=None, adjust_tolerances=False, use_pvode=True,
                  lam_debugfile=None, quirks="nmag", bem_precision="fp64", n_members=1, cg_precision="fp64",
                  bem_anchor=0.0, adjoint_cg_precision="fp64", anchor_product="fp32", cg_local_sweeps=0,
-                 jacobian="approximate", jacobian_demag_rtol=1e-5, jv_precision="fp64", cg_coarse=True):
+                 jacobian="approximate", jacobian_demag_rtol=1e-3, jv_precision="fp64", cg_coarse=True):
         if periodic_bc is not None:
             raise NotImplementedError("periodic boundary conditions are outside this path")
         if temperature is not None:
