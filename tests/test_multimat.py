@@ -163,3 +163,50 @@ def test_sites_where_each_material_is_defined():
             else:
                 with pytest.raises(KeyError):
                     L.site_index(name, node)
+
+
+def test_local_coupling_coefficients_host_side():
+    """Simulation.set_local_magnetic_coupling's coefficients against the
+    reference's formula (main.py:1234-1263): c = coupling / mu0, H_lc of
+    material 1 gains c Ms_2 (simulation units) and E_lc the energy density
+    0.5 mu0 Ms_1 Ms_2 times c, and the other way round; a pair gives one
+    coupling per direction; a second coupling of the same pair, a material
+    with itself, or a one-material simulation is refused.  The engine is a
+    stand-in that records the calls (no GPU)."""
+    from nmag import si, simulation_units
+    a = nmag.MagMaterial("A", Ms=SI(6e5, "A/m"), exchange_coupling=SI(1.0e-11, "J/m"))
+    b = nmag.MagMaterial("B", Ms=SI(1.0e6, "A/m"), exchange_coupling=SI(1.5e-11, "J/m"))
+    c = nmag.MagMaterial("C", Ms=SI(8e5, "A/m"), exchange_coupling=SI(1.3e-11, "J/m"))
+
+    class Recorder:
+        def __init__(self):
+            self.calls = []
+
+        def set_local_coupling(self, k1, k2, h, e):
+            self.calls.append((k1, k2, h, e))
+
+    sim = nmag.Simulation("lc")
+    with pytest.raises(KeyError):   # one material: no sites to couple
+        sim.set_local_magnetic_coupling(a, b, SI(-0.5e-6, "N/A^2"))
+    sim.layer = object()
+    sim.materials = [a, b, c]
+    sim.engine = Recorder()
+    sim.set_local_magnetic_coupling(a, b, SI(-0.5e-6, "N/A^2"))
+    sim.set_local_magnetic_coupling(c, a, (SI(-0.2e-6, "N/A^2"), SI(-0.3e-6, "N/A^2")))
+    mu0 = 4e-7 * np.pi
+    su_Ms = {m.name: simulation_units.of(m.Ms, compatible_with=SI("A/m")) for m in (a, b, c)}
+
+    def en(m1, m2):
+        return simulation_units.of(0.5 * si.mu0 * m1.Ms * m2.Ms, compatible_with=SI("J/m^3"))
+
+    want = [(0, 1, -0.5e-6 / mu0 * su_Ms["B"], -0.5e-6 / mu0 * en(a, b)),
+            (1, 0, -0.5e-6 / mu0 * su_Ms["A"], -0.5e-6 / mu0 * en(a, b)),
+            (2, 0, -0.2e-6 / mu0 * su_Ms["A"], -0.2e-6 / mu0 * en(c, a)),
+            (0, 2, -0.3e-6 / mu0 * su_Ms["C"], -0.3e-6 / mu0 * en(c, a))]
+    assert len(sim.engine.calls) == 4
+    for got, exp in zip(sim.engine.calls, want):
+        assert got[:2] == exp[:2]
+        assert np.allclose(got[2:], exp[2:], rtol=1e-12, atol=0.0), (got, exp)
+    for m1, m2 in ((b, a), (a, b), (a, a)):
+        with pytest.raises(ValueError):
+            sim.set_local_magnetic_coupling(m1, m2, SI(-0.1e-6, "N/A^2"))
