@@ -167,7 +167,82 @@ def load_ascii(filename):
     return Mesh(pts, simp, regions)
 
 
+def _tag(f, name):
+    """The first entry of /etc/<name> (a one-element string array), or None."""
+    if "etc" not in f or name not in f["etc"]:
+        return None
+    v = np.asarray(f["/etc/" + name].read()).reshape(-1)
+    return v[0].decode("latin-1") if isinstance(v[0], bytes) else str(v[0])
+
+
+def load_hdf5(filename):
+    """Read an nmesh HDF5 file (nmeshlib/lib1.py:773-836): /mesh/points,
+    /mesh/simplices, /mesh/simplicesregions, tagged in /etc as an nmesh 1.0
+    (or nsimdata 0.1) file.  Periodic point indices are not read (periodic
+    boundaries are not part of this path)."""
+    from . import h5
+    if not os.path.exists(filename):
+        raise IOError("file '%s' does not exist" % filename)
+    f = h5.File(filename)
+    if "mesh" not in f:
+        raise IOError("File '%s' does not contain a mesh" % filename)
+    if "etc" not in f:
+        raise IOError("File '%s' has no /etc node: cannot be nmesh file" % filename)
+    tag = (_tag(f, "filetype"), _tag(f, "fileversion"))
+    if tag not in (("nmesh", "1.0"), ("nsimdata", "0.1")):
+        raise IOError("File '%s' is tagged %s, not as an nmesh 1.0 file" % (filename, tag))
+    g = f["mesh"]
+    if not all(k in g for k in ("points", "simplices", "simplicesregions")):
+        raise IOError("File '%s' is not a valid mesh file: some mesh attributes are missing" % filename)
+    pts = np.asarray(g["points"].read(), dtype=np.float64).reshape(-1, 3)
+    simp = np.asarray(g["simplices"].read(), dtype=np.int32).reshape(-1, 4)
+    reg = np.asarray(g["simplicesregions"].read(), dtype=np.int32).reshape(-1)
+    m = Mesh(pts, simp, reg)
+    if "scale" in g and "sifactor" in g["scale"]:
+        m.sifactor = float(np.asarray(g["/mesh/scale/sifactor"].read()).reshape(-1)[0])
+    return m
+
+
+def save_hdf5(mesh, filename, sifactor=None, unit=None):
+    """Write the mesh in the layout of nfem/hdf5_v01.py:1370-1545 (tag
+    nmesh 1.0 in /etc; /mesh/points, /mesh/simplices and
+    /mesh/simplicesregions as deflate-compressed chunked arrays with
+    PyTables' node attributes; the optional /mesh/scale group)."""
+    from . import h5
+    w = h5.Writer()
+    w.set_attrs("/", {"CLASS": "GROUP", "VERSION": "1.0", "TITLE": "", "PYTABLES_FORMAT_VERSION": "1.6"})
+    w.create_group("/etc", {"CLASS": "GROUP", "VERSION": "1.0", "TITLE": "Configuration and version data"})
+    for name, val, title in (("filetype", "nmesh", "data file type"), ("fileversion", "1.0", "data file type version")):
+        w.create_dataset("/etc/" + name, np.array([val.encode("latin-1")]),
+                         attrs={"CLASS": "ARRAY", "VERSION": "2.3", "TITLE": title, "FLAVOR": "python"})
+    w.create_group("/mesh", {"CLASS": "GROUP", "VERSION": "1.0", "TITLE": "Mesh data"})
+    for name, arr, title in (
+            ("points", np.asarray(mesh.points, dtype=np.float64), "Positions of mesh nodes (=points)"),
+            ("simplices", np.asarray(mesh.simplices, dtype=np.int32),
+             "Indices of nodes (starting from zero). Each row is one simplex."),
+            ("simplicesregions", np.asarray(mesh.regions, dtype=np.int32), "Region ids (one for each simplex).")):
+        rows = max(1, -(-arr.shape[0] // 64))   # at most 64 chunks
+        w.create_dataset("/mesh/" + name, arr, chunks=(rows,) + arr.shape[1:], compression=5,
+                         attrs={"CLASS": "CARRAY", "VERSION": "1.0", "TITLE": title})
+    if sifactor is not None:
+        w.create_group("/mesh/scale", {"CLASS": "GROUP", "VERSION": "1.0",
+                                       "TITLE": "Mesh coordinate length scale group"})
+        w.create_dataset("/mesh/scale/sifactor", np.float64(sifactor),
+                         attrs={"CLASS": "ARRAY", "VERSION": "2.3", "FLAVOR": "python",
+                                "TITLE": "Multiply mesh coordinates with this number to obtain meters"})
+        if unit is not None:
+            w.create_dataset("/mesh/scale/unit", np.array(str(unit).encode("latin-1")),
+                             attrs={"CLASS": "ARRAY", "VERSION": "2.3", "FLAVOR": "python",
+                                    "TITLE": "SI object for coordinate to position conversion"})
+    w.save(filename)
+
+
 def load(filename_or_mesh):
+    """A Mesh, or a file in nmesh ASCII or nmesh HDF5 (recognised by the
+    HDF5 signature, like nmeshlib/lib1.py:838-863)."""
     if isinstance(filename_or_mesh, Mesh):
         return filename_or_mesh
+    from . import h5
+    if h5.is_hdf5(filename_or_mesh):
+        return load_hdf5(filename_or_mesh)
     return load_ascii(filename_or_mesh)

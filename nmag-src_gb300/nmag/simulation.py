@@ -18,6 +18,7 @@ import time as _time
 
 import numpy as np
 
+from . import h5data as _h5data
 from . import mesh as _mesh
 from . import sites as _sites
 from . import si as _si
@@ -814,9 +815,13 @@ class Simulation(object):
         return [(k, None, self._timers.get(k, 0.0)) for k in names]
 
     def save_mesh(self, filename):
-        """main.py:1228-1232: the magnetic mesh in nmesh ASCII, in simulation
-        units of length (as the reference's mesh object stores it)."""
-        _mesh.save_ascii(self.mesh, filename)
+        """main.py:1228-1232 / nmeshlib/lib1.py:498-515: the magnetic mesh in
+        simulation units of length (as the reference's mesh object stores it),
+        as nmesh HDF5 when the name ends in .h5, else as nmesh ASCII."""
+        if os.path.splitext(filename)[1].lower() == ".h5":
+            _mesh.save_hdf5(self.mesh, filename)
+        else:
+            _mesh.save_ascii(self.mesh, filename)
 
     def do_next_stage(self, stage=None):
         """main.py:2733-2735 / clock.py:84-94: start the next stage (or the
@@ -1018,8 +1023,9 @@ class Simulation(object):
     def save_data(self, fields=None, avoid_same_step=False):
         """main.py:2481-2536: append the averages to <name>_dat.ndt (a new
         clock id per row; with avoid_same_step a step already written is not
-        written again) and, when fields are given ('all' or names), save
-        them (here m, as <name>_fields_<step>.npz)."""
+        written again) and, when fields are given ('all' or field names),
+        append a row per field to <name>_dat.h5 (nfem/hdf5_v01.py:685-1022:
+        the fields' subfields at their sites, in SI)."""
         saved = getattr(self, "_saved_steps", None)
         if saved is None:
             saved = self._saved_steps = set()
@@ -1029,32 +1035,111 @@ class Simulation(object):
             names, values, units = self._compute_averages()
             self._save_data_table_to_ndt(names, values, units, "%s_dat.ndt" % self.name)
         if fields:
-            # the reference writes the fields into <name>_dat.h5 (main.py:2527-2534,
-            # _save_fields); here one .npz per save, arrays per site in SI
-            per_mat = list(self._PER_MATERIAL) if self.layer is None else [
-                "%s_%s" % (f, mt.name) for f in self._PER_MATERIAL for mt in self.materials]
-            names = per_mat + list(self._ON_MESH) if fields == "all" else (
-                [fields] if isinstance(fields, str) else list(fields))
-            for name in names:
-                self._field_of(name)   # KeyError for unknown fields
-            snap = {"f": self.engine.eval_fields(), "E": self.engine.energy_density()}
-            out = {name: self.get_subfield(name, _snap=snap) for name in names}
-            np.savez("%s_fields_%06d.npz" % (self.name, self.clock.step), **out)
+            all_fields = list(self._PER_MATERIAL) + list(self._ON_MESH)
+            req = all_fields if fields == "all" else ([fields] if isinstance(fields, str) else list(fields))
+            chosen = []
+            for name in req:
+                f = self._field_of(name)   # KeyError for unknown fields
+                if f not in chosen:
+                    chosen.append(f)
+            self._append_h5_fields("%s_dat.h5" % self.name, chosen, all_fields)
+
+    # ---- HDF5 data and restart files (nfem/hdf5_v01.py layout) ----
+    def _subfields_of(self, field):
+        """(subfield name, node index of each of its sites) of a field."""
+        if field in self._ON_MESH:
+            return [(field, np.arange(self.mesh.n_nodes))]
+        mats = self.materials if self.layer is not None else [self.material]
+        out = []
+        for mt in mats:
+            nodes = self.layer.site_node[self._sites_of(mt)] if self.layer is not None else np.arange(self.mesh.n_nodes)
+            out.append(("%s_%s" % (field, mt.name), nodes))
+        return out
+
+    def _h5_metadata(self, fields):
+        meta, sites = [], {}
+        for f in fields:
+            shape = "[3]" if f in self._VECTOR else "[]"
+            unit = repr(_FIELD_SI[self._KIND[f]])
+            for sub, nodes in self._subfields_of(f):
+                meta.append((f, sub, unit, shape))
+                sites[sub] = nodes
+        return meta, sites
+
+    def _h5_row(self, fields):
+        snap = {"f": self.engine.eval_fields(), "E": self.engine.energy_density()}
+        rows = {}
+        for f in fields:
+            data = {sub: self.get_subfield(sub, _snap=snap) for sub, _ in self._subfields_of(f)}
+            rows[f] = {"id": self.clock.id, "stage": self.clock.stage, "step": self.clock.step,
+                       "time": self.clock.time_su * 1e-12, "data": data}
+        return rows
+
+    def _append_h5_fields(self, path, fields, all_fields):
+        meta, sites = self._h5_metadata(all_fields)
+        old = _h5data.read(path) if os.path.exists(path) else None
+        tables = dict(old["tables"]) if old else {}
+        if old:
+            meta, sites = old["metadata"], old["dofsites"]
+        for f, row in self._h5_row(fields).items():
+            new = _h5data.field_rows([(sub, None) for sub, _ in self._subfields_of(f)], [row])
+            tables[f] = np.concatenate([tables[f], new]) if f in tables else new
+        _h5data.write(path, self.mesh, meta, sites, tables, sim_units=repr(simulation_units))
 
     def get_restart_file_name(self):
-        """The default restart file (simulation_core.py:343-345; .npz here)."""
-        return "%s_restart.npz" % self.name
+        """The default restart file (simulation_core.py:343-345)."""
+        return "%s_restart.h5" % self.name
 
-    def save_restart_file(self, filename=None):
-        """main.py:2764-2857: m and the clock, written via a temp file + rename."""
-        fn = filename or "%s_restart.npz" % self.name
-        tmp = fn + ".tmp.npz"
-        np.savez(tmp, m=self._m, clock=np.array([repr(dict(self.clock))]))
-        os.replace(tmp, fn)
+    def save_restart_file(self, filename=None, fieldnames=("m",), all=False):
+        """main.py:2764-2857: the fields (m by default, every field with
+        all=True) and the clock, written to a temporary file and renamed;
+        the clock is the attribute 'clock' of /data/fields/m."""
+        fn = filename or self.get_restart_file_name()
+        fields = list(self._PER_MATERIAL) + list(self._ON_MESH) if all else \
+            [self._field_of(n) for n in fieldnames]
+        if "m" not in fields:
+            fields = ["m"] + fields
+        meta, sites = self._h5_metadata(fields)
+        tables = {f: _h5data.field_rows([(sub, None) for sub, _ in self._subfields_of(f)], [row])
+                  for f, row in self._h5_row(fields).items()}
+        _h5data.write(fn, self.mesh, meta, sites, tables, sim_units=repr(simulation_units),
+                      clock=repr(dict(self.clock)))
+
+    def load_m_from_h5file(self, filename):
+        """main.py:1876-1902: set m from the first row of /data/fields/m of
+        an nmag data or restart file, subfield by subfield, placed by the
+        file's sites (the mesh must be the one the file was written with)."""
+        d = _h5data.read(filename)
+        if "m" not in d["tables"]:
+            raise IOError("File '%s' holds no field m" % filename)
+        row = d["tables"]["m"][0]
+        m = np.array(self._m, copy=True)
+        for sub, nodes in self._subfields_of("m"):
+            if sub not in row.dtype.names:
+                continue
+            vals = np.asarray(row[sub], dtype=np.float64)
+            file_nodes = d["dofsites"].get(sub)
+            if file_nodes is None or len(file_nodes) != len(nodes):
+                raise ValueError("load_m_from_h5file: the sites of '%s' differ from this simulation's" % sub)
+            pos = {int(n): k for k, n in enumerate(nodes)}
+            idx = np.array([pos[int(n)] for n in file_nodes])
+            target = self._sites_of(self._material_of(sub, "m"))[idx] if self.layer is not None else idx
+            m[..., target, :] = vals
+        self.set_m(m)
 
     def load_restart_file(self, filename=None):
-        fn = filename or "%s_restart.npz" % self.name
-        d = np.load(fn, allow_pickle=False)
-        self.set_m(d["m"])
-        import ast
-        self.clock.update(ast.literal_eval(str(d["clock"][0])))
+        """main.py:2859-2883: m and the clock of a restart file; a stage
+        saved at convergence continues with the next stage."""
+        fn = filename or self.get_restart_file_name()
+        self.load_m_from_h5file(fn)
+        clock = _h5data.read(fn)["clock"]
+        if clock:
+            import ast
+            try:   # this package's clock (a dict); another writer's clock is not read
+                values = ast.literal_eval(clock)
+            except (ValueError, SyntaxError):
+                log.warning("load_restart_file: the clock of '%s' is not readable; m only", fn)
+                return
+            self.clock.update(values)
+            if self.clock.convergence:
+                self.clock.stage += 1

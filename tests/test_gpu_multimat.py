@@ -218,8 +218,10 @@ def test_simulation_api_with_two_materials(tmp_path, monkeypatch):
     sim.set_damping(1.0)
     sim.relax()   # the default saves: averages and every field at the stage end
     assert sim.clock.convergence
-    saved = np.load(sorted(tmp_path.glob("two_fields_*.npz"))[-1])
-    assert saved["m_Co"].shape == (len(L.sites_of("Co")), 3) and saved["H_demag"].shape == (msh.n_nodes, 3)
+    from nmag import h5data
+    saved = h5data.read(str(tmp_path / "two_dat.h5"))["tables"]
+    assert saved["m"]["m_Co"][-1].shape == (len(L.sites_of("Co")), 3)
+    assert saved["H_demag"]["H_demag"][-1].shape == (msh.n_nodes, 3)
 
 
 def test_local_coupling_matches_oracle():

@@ -1,0 +1,183 @@
+"""The HDF5 reader and writer (nmag/h5.py) and the nmesh HDF5 mesh files.
+
+No HDF5 library is installed, and the reference tree holds no HDF5 file,
+so these tests check the module against itself: files written by the
+writer (every layout, filter, datatype and group size it produces) read
+back exactly, hand-assembled structures the writer does not produce (a
+version 2 object header with compact links, version 1/2 layout and
+version 2 filter-pipeline messages, version 3 attributes) parse as the
+format specification lays them out, and the mesh layout of
+nfem/hdf5_v01.py:1370-1545 (tags in /etc, /mesh/points, /mesh/simplices,
+/mesh/simplicesregions) round-trips through load / save.
+"""
+import os
+import struct
+import zlib
+
+import numpy as np
+import pytest
+
+from nmag import h5, mesh
+
+
+def test_writer_reader_round_trip(tmp_path):
+    rng = np.random.default_rng(3)
+    data = {
+        "/a/f64": rng.standard_normal((37, 3)),
+        "/a/f32": rng.standard_normal(11).astype(np.float32),
+        "/a/i32": rng.integers(-1000, 1000, (5, 4)).astype(np.int32),
+        "/a/u8": np.arange(200, dtype=np.uint8),
+        "/a/i64_3d": rng.integers(0, 1 << 40, (2, 3, 4)),
+        "/b/scalar": np.float64(2.5),
+        "/b/strings": np.array([b"nmesh", b"1.0"]),
+        "/b/empty": np.zeros((0, 3)),
+        "/c/d/e/deep": np.arange(7, dtype=np.int32),
+    }
+    w = h5.Writer()
+    for path, arr in data.items():
+        w.create_dataset(path, arr)
+    big = rng.standard_normal((1000, 3))
+    w.create_dataset("/chunked/deflate", big, chunks=(100, 3), compression=6)
+    w.create_dataset("/chunked/shuffle", big, chunks=(128, 2), shuffle=True, compression=1)
+    w.create_dataset("/chunked/plain", big[:, 0].copy(), chunks=(33,))
+    tab = np.zeros(4, dtype=[("t", "<f8"), ("step", "<i4"), ("m", "<f8", (3,)), ("name", "S6")])
+    tab["t"], tab["step"] = [0.0, 1e-12, 2e-12, 3e-12], [0, 5, 10, 15]
+    tab["m"] = rng.standard_normal((4, 3))
+    tab["name"] = [b"a", b"bb", b"ccc", b"dddd"]
+    w.create_dataset("/table", tab)
+    for k in range(40):   # several symbol-table nodes in one group
+        w.create_dataset("/many/x%03d" % k, np.full(2, k, np.int32))
+    w.set_attrs("/", {"TITLE": "root title", "VERSION": "1.0"})
+    w.set_attrs("/a/f64", {"CLASS": "ARRAY", "scale": np.array([1.5, 2.5]), "n": np.int32(7)})
+    path = str(tmp_path / "t.h5")
+    w.save(path)
+
+    assert h5.is_hdf5(path)
+    f = h5.File(path)
+    assert f.keys() == ["a", "b", "c", "chunked", "many", "table"]
+    for p, arr in data.items():
+        got = f[p].read()
+        assert got.shape == np.shape(arr) and got.dtype == np.asarray(arr).dtype, p
+        assert np.array_equal(got, arr), p
+    assert np.array_equal(f["/chunked/deflate"].read(), big)
+    assert np.array_equal(f["/chunked/shuffle"].read(), big)
+    assert np.array_equal(f["/chunked/plain"].read(), big[:, 0])
+    t = f["/table"].read()
+    for name in tab.dtype.names:
+        assert np.array_equal(t[name], tab[name]), name
+    assert f["many"].keys() == ["x%03d" % k for k in range(40)]
+    assert np.array_equal(f["/many/x039"].read(), [39, 39])
+    assert f.attrs["TITLE"] == "root title"
+    a = f["/a/f64"].attrs
+    assert a["CLASS"] == "ARRAY" and np.array_equal(a["scale"], [1.5, 2.5]) and a["n"] == 7
+    with pytest.raises(KeyError):
+        f["/a/missing"]
+
+
+def _ohdr_v2(msgs):
+    """A version 2 object header (no times, 1-byte chunk size; checksum bytes zero)."""
+    body = b"".join(struct.pack("<BHB", t, len(d), 0) + d for t, d in msgs)
+    return b"OHDR" + bytes([2, 0, len(body)]) + body + b"\0" * 4
+
+
+def test_reader_structures_the_writer_does_not_produce():
+    """A version 2 superblock whose root is a version 2 object header with
+    compact link messages to (1) a dataset with a version 1 layout and a
+    version 2 filter pipeline (deflate) over two chunks, and (2) a dataset
+    with a version 2 compact layout and a version 3 attribute."""
+    arr = np.arange(12, dtype="<f8").reshape(6, 2)
+    c0, c1 = zlib.compress(arr[:3].tobytes()), zlib.compress(arr[3:].tobytes())
+    out = bytearray(48)   # superblock v2 (filled in below)
+
+    def put(b):
+        while len(out) % 8:
+            out.append(0)
+        at = len(out)
+        out.extend(b)
+        return at
+
+    a0, a1 = put(c0), put(c1)
+    tree = b"TREE" + bytes([1, 0]) + struct.pack("<H", 2) + struct.pack("<QQ", h5.UNDEF, h5.UNDEF)
+    for off, at, n in ((0, a0, len(c0)), (3, a1, len(c1))):
+        tree += struct.pack("<II", n, 0) + struct.pack("<QQQ", off, 0, 0) + struct.pack("<Q", at)
+    tree += struct.pack("<II", 0, 0) + struct.pack("<QQQ", 6, 2, 0)
+    bt = put(tree)
+    f64 = h5._dt_msg(np.dtype("<f8"))
+    space_v2 = struct.pack("<BBBB", 2, 2, 0, 1) + struct.pack("<QQ", 6, 2)
+    layout_v1 = struct.pack("<BBB5x", 1, 3, 2) + struct.pack("<Q", bt) + struct.pack("<III", 3, 2, 8)
+    pipeline_v2 = struct.pack("<BB", 2, 1) + struct.pack("<HHH", 1, 0, 1) + struct.pack("<I", 4)
+    d1 = put(_ohdr_v2([(1, space_v2), (3, f64), (8, layout_v1), (11, pipeline_v2)]))
+    vals = np.array([7, 8, 9], dtype="<i4")
+    i32 = h5._dt_msg(np.dtype("<i4"))
+    space1 = struct.pack("<BBBB", 2, 1, 0, 1) + struct.pack("<Q", 3)
+    layout_c = struct.pack("<BBH", 3, 0, vals.nbytes) + vals.tobytes()
+    sdt = bytes([0x13, 0, 0, 0]) + struct.pack("<I", 5)
+    attr_v3 = struct.pack("<BBHHHB", 3, 0, 6, len(sdt), 4, 0) + b"TITLE\0" + sdt + \
+        struct.pack("<BBBB", 2, 0, 0, 0) + b"hello"
+    d2 = put(_ohdr_v2([(1, space1), (3, i32), (8, layout_c), (12, attr_v3)]))
+
+    def link(name, addr):
+        nm = name.encode()
+        return struct.pack("<BB", 1, 0) + bytes([len(nm)]) + nm + struct.pack("<Q", addr)
+
+    root = put(_ohdr_v2([(6, link("chunked", d1)), (6, link("compact", d2))]))
+    sb = h5.SIGNATURE + bytes([2, 8, 8, 0]) + struct.pack("<QQQQ", 0, h5.UNDEF, len(out), root) + b"\0" * 4
+    out[0:48] = sb
+    f = h5.File(bytes(out))
+    assert f.keys() == ["chunked", "compact"]
+    assert np.array_equal(f["chunked"].read(), arr)
+    assert np.array_equal(f["compact"].read(), vals)
+    assert f["compact"].attrs["TITLE"] == "hello"
+
+
+def test_nmesh_hdf5_round_trip_and_dispatch(tmp_path):
+    m = mesh.box_mesh(4, 3, 2, 2.0, 2.5, 1.5)
+    m.regions[:5] = 2
+    path = str(tmp_path / "box.nmesh.h5")
+    mesh.save_hdf5(m, path, sifactor=1e-9, unit="<SI: 1e-09 m >")
+    r = mesh.load(path)   # recognised by its signature
+    assert np.array_equal(r.points, m.points)
+    assert np.array_equal(r.simplices, m.simplices) and r.simplices.dtype == np.int32
+    assert np.array_equal(r.regions, m.regions)
+    assert r.sifactor == 1e-9
+    f = h5.File(path)
+    assert mesh._tag(f, "filetype") == "nmesh" and mesh._tag(f, "fileversion") == "1.0"
+    assert f["/mesh/points"].attrs["CLASS"] == "CARRAY"
+    # the ASCII file of the same mesh reads the same
+    apath = str(tmp_path / "box.nmesh")
+    mesh.save_ascii(m, apath)
+    a = mesh.load(apath)
+    assert np.array_equal(a.points, r.points) and np.array_equal(a.simplices, r.simplices)
+
+
+def test_nmesh_hdf5_refuses_other_files(tmp_path):
+    w = h5.Writer()
+    w.create_dataset("/etc/filetype", np.array([b"other"]))
+    w.create_dataset("/etc/fileversion", np.array([b"1.0"]))
+    w.create_dataset("/mesh/points", np.zeros((4, 3)))
+    path = str(tmp_path / "x.h5")
+    w.save(path)
+    with pytest.raises(IOError):
+        mesh.load_hdf5(path)
+    w2 = h5.Writer()
+    w2.create_dataset("/etc/filetype", np.array([b"nmesh"]))
+    w2.create_dataset("/etc/fileversion", np.array([b"1.0"]))
+    w2.create_dataset("/mesh/points", np.zeros((4, 3)))
+    w2.save(path)
+    with pytest.raises(IOError):   # simplices missing
+        mesh.load_hdf5(path)
+    with open(path, "wb") as fh:
+        fh.write(b"not hdf5 at all")
+    with pytest.raises(h5.HDF5Error):
+        h5.File(path)
+
+
+def test_simulation_save_mesh_by_extension(tmp_path):
+    import nmag
+    sim = nmag.Simulation("sm")
+    sim.mesh = mesh.box_mesh(2, 2, 2, 1.0)
+    sim.save_mesh(str(tmp_path / "m.nmesh.h5"))
+    sim.save_mesh(str(tmp_path / "m.nmesh"))
+    a, b = mesh.load(str(tmp_path / "m.nmesh.h5")), mesh.load(str(tmp_path / "m.nmesh"))
+    assert np.array_equal(a.simplices, b.simplices) and np.allclose(a.points, b.points)
+    assert os.path.getsize(str(tmp_path / "m.nmesh.h5")) > 96

@@ -125,7 +125,9 @@ def test_relax_runs_to_convergence_and_saves_at_stage_end(tmp_path, monkeypatch)
     assert sim.max_dm_dt < sim.stopping_dm_dt
     rows = [l for l in open("hyst_dat.ndt") if not l.startswith("#")]
     assert len(rows) == 1                        # averages at stage end only (the default save)
-    assert len(list(tmp_path.glob("hyst_fields_*.npz"))) == 1
+    from nmag import h5data
+    tab = h5data.read(str(tmp_path / "hyst_dat.h5"))["tables"]
+    assert len(tab["m"]) == 1                    # every field once, at the stage end
     assert sim.clock.id == 0                     # ids start at -1; one new id per averages row
 
 
@@ -227,18 +229,46 @@ def test_subfield_names_probe_and_units(tmp_path, monkeypatch):
 
 
 def test_save_fields_and_restart_name(tmp_path, monkeypatch):
+    """save_data(fields=...) appends rows to <name>_dat.h5 in the layout of
+    nfem/hdf5_v01.py:685-1022 (tags, mesh, metadata, sites, one table per
+    field with id / stage / step / time and the subfields in SI)."""
+    from nmag import h5data
     sim, eng = make_sim(tmp_path, monkeypatch)
     sim.save_data(fields="all")
-    d = np.load(list(tmp_path.glob("hyst_fields_*.npz"))[0])
-    assert {"m", "M", "H_demag", "E_total", "phi", "pin"} <= set(d.files)
-    assert np.allclose(d["H_demag"], 0.1e6)
+    d = h5data.read(str(tmp_path / "hyst_dat.h5"))
+    assert {"m", "M", "H_demag", "E_total", "phi", "pin"} <= set(d["tables"])
+    assert np.allclose(d["tables"]["H_demag"]["H_demag"], 0.1e6)
+    assert ("m", "m_Py", repr(nmag.SI(1.0)), "[3]") in d["metadata"]
+    assert np.array_equal(d["dofsites"]["m_Py"], np.arange(4))
+    assert np.array_equal(d["mesh"].simplices, sim.mesh.simplices)
     sim.clock.step = 7
     sim.save_data(fields=["m"])
-    d = np.load(str(tmp_path / "hyst_fields_000007.npz"))
-    assert d.files == ["m"]
+    t = h5data.read(str(tmp_path / "hyst_dat.h5"))["tables"]
+    assert list(t["m"]["step"]) == [0, 7] and len(t["H_demag"]) == 1
+    assert np.allclose(t["m"]["m_Py"][1], sim.get_subfield("m_Py"))
     with pytest.raises(KeyError):
         sim.save_data(fields=["B_field"])
-    assert sim.get_restart_file_name() == "hyst_restart.npz"
+    assert sim.get_restart_file_name() == "hyst_restart.h5"
+
+
+def test_restart_file_round_trip(tmp_path, monkeypatch):
+    """save_restart_file / load_restart_file (main.py:2764-2883): m and the
+    clock come back; a stage saved at convergence continues with the next
+    stage; load_m_from_h5file reads the first row of /data/fields/m."""
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    m0 = np.array([[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0], [0.6, 0.8, 0.0]])
+    sim.set_m(m0)
+    sim.clock.step, sim.clock.stage, sim.clock.convergence = 42, 3, True
+    sim.save_restart_file()
+    assert (tmp_path / "hyst_restart.h5").exists() and not (tmp_path / "hyst_restart.h5.internal").exists()
+    sim.set_m([0.0, 0.0, 1.0])
+    sim.clock.step, sim.clock.stage, sim.clock.convergence = 0, 1, False
+    sim.load_restart_file()
+    assert np.allclose(sim.get_subfield("m_Py"), m0, atol=1e-7)   # stored as FP32
+    assert sim.clock.step == 42 and sim.clock.stage == 4
+    sim.set_m([0.0, 0.0, 1.0])
+    sim.load_m_from_h5file(str(tmp_path / "hyst_restart.h5"))
+    assert np.allclose(sim.get_subfield("m"), m0, atol=1e-7)
 
 
 def test_current_density_needs_a_polarisation(tmp_path, monkeypatch):
