@@ -119,6 +119,21 @@ def _dtype(b, pos):
             formats.append((mdt, shape) if shape else mdt)
             offsets.append(off)
         return np.dtype({"names": names, "formats": formats, "offsets": offsets, "itemsize": size}), p - pos
+    if cls == 4:   # bitfield: unsigned integers of its size
+        order = ">" if bits & 1 else "<"
+        return np.dtype("%su%d" % (order, size)), 8 + 4
+    if cls == 5:   # opaque: raw bytes, then its tag (padded to 8)
+        taglen = bits & 0xFF
+        return np.dtype("V%d" % size), 8 + taglen
+    if cls == 8:   # enumeration: its base integer type, then names and values
+        nmemb = bits & 0xFFFF
+        base, blen = _dtype(b, p)
+        q = p + blen
+        for _ in range(nmemb):
+            name = b.cstr(q)
+            q += _round8(len(name) + 1) if ver < 3 else len(name) + 1
+        q += nmemb * base.itemsize
+        return base, q - pos
     if cls == 10:  # array
         ndim = b.d[p]
         if ver < 3:
@@ -197,33 +212,41 @@ def _attributes(b, msgs):
     for mtype, p, _ in msgs:
         if mtype != 0x0C:
             continue
-        ver = b.d[p]
-        nlen, tlen, slen = b.u(p + 2, 2), b.u(p + 4, 2), b.u(p + 6, 2)
-        if ver == 1:
-            q = p + 8
-            name = b.d[q:q + nlen].split(b"\0")[0].decode("latin-1")
-            q += _round8(nlen)
-            dt, _ = _dtype(b, q)
-            q += _round8(tlen)
-            shape = _dataspace(b, q)
-            q += _round8(slen)
-        else:
-            q = p + 8 + (1 if ver == 3 else 0)
-            name = b.d[q:q + nlen].split(b"\0")[0].decode("latin-1")
-            q += nlen
-            dt, _ = _dtype(b, q)
-            q += tlen
-            shape = _dataspace(b, q)
-            q += slen
-        if shape is None:
-            attrs[name] = None
-            continue
-        n = int(np.prod(shape)) if shape else 1
-        val = np.frombuffer(b.d, dtype=dt, count=n, offset=q).reshape(shape)
-        if dt.kind == "S":
-            val = val.astype(str)
-        attrs[name] = val[()] if shape == () else val
+        try:
+            name, value = _attribute(b, p)
+        except (NotImplementedError, ValueError, IndexError):
+            continue   # an attribute outside the subset (e.g. variable-length): not read
+        attrs[name] = value
     return attrs
+
+
+def _attribute(b, p):
+    """(name, value) of the attribute message at p."""
+    ver = b.d[p]
+    nlen, tlen, slen = b.u(p + 2, 2), b.u(p + 4, 2), b.u(p + 6, 2)
+    if ver == 1:
+        q = p + 8
+        name = b.d[q:q + nlen].split(b"\0")[0].decode("latin-1")
+        q += _round8(nlen)
+        dt, _ = _dtype(b, q)
+        q += _round8(tlen)
+        shape = _dataspace(b, q)
+        q += _round8(slen)
+    else:
+        q = p + 8 + (1 if ver == 3 else 0)
+        name = b.d[q:q + nlen].split(b"\0")[0].decode("latin-1")
+        q += nlen
+        dt, _ = _dtype(b, q)
+        q += tlen
+        shape = _dataspace(b, q)
+        q += slen
+    if shape is None:
+        return name, None
+    n = int(np.prod(shape)) if shape else 1
+    val = np.frombuffer(b.d, dtype=dt, count=n, offset=q).reshape(shape)
+    if dt.kind == "S":
+        val = val.astype(str)
+    return name, (val[()] if shape == () else val)
 
 
 class Node(object):

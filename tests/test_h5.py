@@ -114,7 +114,17 @@ def test_reader_structures_the_writer_does_not_produce():
     sdt = bytes([0x13, 0, 0, 0]) + struct.pack("<I", 5)
     attr_v3 = struct.pack("<BBHHHB", 3, 0, 6, len(sdt), 4, 0) + b"TITLE\0" + sdt + \
         struct.pack("<BBBB", 2, 0, 0, 0) + b"hello"
-    d2 = put(_ohdr_v2([(1, space1), (3, i32), (8, layout_c), (12, attr_v3)]))
+    # an enumeration attribute (read as its base integer) and a variable-length
+    # string attribute (outside the subset: skipped, the rest still read)
+    u8 = h5._dt_msg(np.dtype("u1"))
+    enum = bytes([0x18]) + (2).to_bytes(3, "little") + struct.pack("<I", 1) + u8 + \
+        b"OFF\0\0\0\0\0" + b"ON\0\0\0\0\0\0" + bytes([0, 1])
+    attr_enum = struct.pack("<BBHHHB", 3, 0, 5, len(enum), 4, 0) + b"FLAG\0" + enum + \
+        struct.pack("<BBBB", 2, 0, 0, 0) + bytes([1])
+    vl = bytes([0x19, 1, 0, 0]) + struct.pack("<I", 16) + u8
+    attr_vl = struct.pack("<BBHHHB", 3, 0, 3, len(vl), 4, 0) + b"VL\0" + vl + \
+        struct.pack("<BBBB", 2, 0, 0, 0) + b"\0" * 16
+    d2 = put(_ohdr_v2([(1, space1), (3, i32), (8, layout_c), (12, attr_v3), (12, attr_enum), (12, attr_vl)]))
 
     def link(name, addr):
         nm = name.encode()
@@ -128,6 +138,7 @@ def test_reader_structures_the_writer_does_not_produce():
     assert np.array_equal(f["chunked"].read(), arr)
     assert np.array_equal(f["compact"].read(), vals)
     assert f["compact"].attrs["TITLE"] == "hello"
+    assert f["compact"].attrs["FLAG"] == 1 and "VL" not in f["compact"].attrs
 
 
 def test_nmesh_hdf5_round_trip_and_dispatch(tmp_path):
