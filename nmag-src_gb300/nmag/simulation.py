@@ -1114,7 +1114,12 @@ class Simulation(object):
             raise IOError("File '%s' holds no field m" % filename)
         row = d["tables"]["m"][0]
         m = np.array(self._m, copy=True)
+        # a file of the whole mesh (vacuum included, as the reference writes
+        # it) numbers the nodes of the mesh as loaded, not of its magnetic part
+        whole = getattr(self, "node_map", None) is not None and len(d["mesh"].points) != self.mesh.n_nodes
         for sub, nodes in self._subfields_of("m"):
+            if whole:
+                nodes = np.asarray(self.node_map)[nodes]
             if sub not in row.dtype.names:
                 continue
             vals = np.asarray(row[sub], dtype=np.float64)

@@ -286,3 +286,23 @@ def test_progress_file(tmp_path, monkeypatch):
     assert "stage_step" in text and "max_dm_dt" in text
     step_line = [l for l in text.splitlines() if l.startswith("step ")][0]
     assert int(step_line.split()[1]) == sim.clock.step
+
+
+def test_load_m_from_a_whole_mesh_file(tmp_path, monkeypatch):
+    """A data file of the whole mesh (vacuum nodes included, as the reference
+    writes it) places m by the node numbers of the mesh as loaded: node k of
+    the magnetic part is node node_map[k] of the file's mesh."""
+    from nmag import h5data
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    sim.node_map = np.array([1, 2, 4, 5])
+    whole = nmag.mesh.Mesh(np.random.default_rng(0).standard_normal((6, 3)), [[0, 1, 2, 3], [2, 3, 4, 5]])
+    file_nodes = np.array([5, 4, 2, 1])
+    vals = np.array([[0.0, 0.0, 1.0], [0.0, 1.0, 0.0], [1.0, 0.0, 0.0], [0.6, 0.0, 0.8]])
+    row = {"id": 0, "stage": 1, "step": 3, "time": 0.0, "data": {"m_Py": vals}}
+    h5data.write(str(tmp_path / "whole.h5"), whole, [("m", "m_Py", "SI(1.0, '')", "[3]")],
+                 {"m_Py": file_nodes}, {"m": h5data.field_rows([("m_Py", None)], [row])})
+    sim.load_m_from_h5file(str(tmp_path / "whole.h5"))
+    want = {int(n): v for n, v in zip(file_nodes, vals)}
+    got = sim.get_subfield("m_Py")
+    for k, n in enumerate(sim.node_map):
+        assert np.allclose(got[k], want[int(n)], atol=1e-7)
