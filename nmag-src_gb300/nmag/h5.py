@@ -176,7 +176,11 @@ def _messages(b, addr):
         blocks = [(p, p + chunk)]   # the chunk's checksum follows it
         cre = bool(flags & 0x04)
         hsz = 6 if cre else 4
+        seen = 0
         while blocks:
+            seen += 1
+            if seen > 4096:
+                raise HDF5Error("HDF5: object header at %d does not end" % addr)
             start, end = blocks.pop(0)
             q = start
             while q + hsz <= end:
@@ -194,7 +198,11 @@ def _messages(b, addr):
     nmsg = b.u(addr + 2, 2)
     size = b.u(addr + 8, 4)
     blocks = [(addr + 16, addr + 16 + size)]
+    seen = 0
     while blocks and len(out) < nmsg:
+        seen += 1
+        if seen > 4096:   # continuation blocks that loop: a damaged file
+            raise HDF5Error("HDF5: object header at %d does not end" % addr)
         start, end = blocks.pop(0)
         q = start
         while q + 8 <= end:
