@@ -106,6 +106,12 @@ int nmg_destroy(nmg_handle *h) {
   h->ts = nullptr;
   nmg::tape_free(h);
   nmg_handle *pot = h->pot;
+  if (h->ws.aux) {   // the mixed-precision CG's auxiliary stream and its events
+    cudaStreamSynchronize(h->ws.aux);
+    for (cudaEvent_t ev : h->ws.ev_ldl) if (ev) cudaEventDestroy(ev);
+    if (h->ws.ev_cg) cudaEventDestroy(h->ws.ev_cg);
+    cudaStreamDestroy(h->ws.aux);
+  }
   if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
   delete h;  // member destructors release the device buffers
   if (pot) nmg_destroy(pot);   // several materials: the potential mesh's handle (and the shared stream)

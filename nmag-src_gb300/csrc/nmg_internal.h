@@ -75,6 +75,16 @@ struct Mesh {
   DevBuf<double> obs_max;
 };
 
+constexpr int kBasisMax = 10;   // warm-start basis size of the CG solves (kBasis)
+// A member's factor of its warm-start Gram system (row i of the unit lower
+// factor, 1 / D_i, the kept directions, the basis size it was formed for).
+struct GramLDL {
+  double L[kBasisMax * kBasisMax];
+  double rd[kBasisMax];
+  unsigned on;
+  int n;
+};
+
 struct Workspace {
   DevBuf<double> m, h_ext, h_exch, h_demag, h_anis, h_total, dmdt, rho, phi1, phi2, phi, rhs2;
   DevBuf<double> b1, b2, bpart, cg_r, cg_z, cg_p, cg_q, cg_w, cg_tot, dinv_n, dinv_d, red, E5;
@@ -82,6 +92,12 @@ struct Workspace {
   DevBuf<int> err;          // device error flags
   DevBuf<int> iters;        // CG iterations written by the persistent kernel
   DevBuf<double> basis_b, basis_x, basis_gram;  // CG initial-guess basis per solve kind
+  // mixed-precision CG: each basis's Gram factor, formed on the auxiliary
+  // stream after a solve for the next solve of that basis; one event per slot
+  DevBuf<GramLDL> basis_ldl, ens_basis_ldl;
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_cg = nullptr;
+  std::vector<cudaEvent_t> ev_ldl;
   DevBuf<int> basis_ring;
   // ensemble: a basis per solve kind and member ([kind][member][kBasis][N])
   DevBuf<double> ens_basis_b, ens_basis_x, ens_basis_gram;
@@ -235,6 +251,7 @@ struct JacDemag {
   DevBuf<double> rho, phi1, phi2, phi, rhs2, b1, b2;
   DevBuf<double> basis_b, basis_x, basis_gram, ens_basis_b, ens_basis_x, ens_basis_gram;
   DevBuf<int> basis_ring, ens_basis_ring, iters;
+  DevBuf<GramLDL> basis_ldl, ens_basis_ldl;
   DevBuf<double> hdv;
   bool ready = false;
 };

@@ -280,13 +280,14 @@ __device__ __forceinline__ bool reduce_all_to(const CGArgs &a, unsigned epoch, d
 // b.b_j come with the first reduction and also update the Gram matrix; every
 // block solves the small system identically.  With an empty basis the
 // previous solution is the start, like the reference's initial_guess_nonzero.
-constexpr int kBasis = 10;
+constexpr int kBasis = kBasisMax;
 constexpr int kCGSlots = 4;   // warm-start bases: 0/1 Neumann/Dirichlet, 2/3 the adjoint solves
 
 struct CGBasis {
   double *b, *x;   // kBasis x N right-hand sides and solutions
   double *gram;    // kBasis x kBasis
   int *ring;       // {count, head}
+  GramLDL *ldl;    // mixed-precision CG: the factor of each member's Gram system (null: none)
 };
 
 // Least squares for c: (G + eps diag G) c = v, one warp (every lane calls;
@@ -297,12 +298,15 @@ struct CGBasis {
 // reciprocals instead of ~n^2/2 FP64 divisions in one thread.  sD: kBasis
 // doubles of shared scratch for this warp (the pivots); c (shared or
 // global) receives c[0..n) from lanes 0..n-1.
-__device__ void small_solve_warp(int n, const double *G, const double *v, double *c, double *sD) {
+// The warp's LDL^T factorisation of (G + eps diag G): lane i keeps row i of
+// the unit lower factor in L, rd = 1 / D_i (0: dropped direction), `on` the
+// kept directions.  sD: kBasis doubles of shared scratch (the pivots).
+__device__ __forceinline__ void small_factor_warp(int n, const double *G, double *sD, double (&L)[kBasis],
+                                                  double &rd, unsigned &on) {
   const int lane = threadIdx.x & 31;
   const unsigned full = 0xffffffffu;
-  double L[kBasis];   // row `lane` of the unit lower factor
-  double rd = 0.0;    // 1 / D_lane (0: dropped direction)
-  unsigned on = 0u;
+  rd = 0.0;
+  on = 0u;
 #pragma unroll
   for (int j = 0; j < kBasis; ++j) L[j] = 0.0;
 #pragma unroll
@@ -326,7 +330,13 @@ __device__ void small_solve_warp(int n, const double *G, const double *v, double
     if (lane == j) rd = r;
     if (lane > j) L[j] = s * r;
   }
-  // L z = v, y = z / D
+}
+
+// c = (G + eps diag G)^-1 v from the factor: L z = v, y = z / D, L^T c = y.
+__device__ __forceinline__ void small_subst_warp(int n, const double (&L)[kBasis], double rd, unsigned on,
+                                                 const double *v, double *c) {
+  const int lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu;
   double z = lane < n ? v[lane] : 0.0;
 #pragma unroll
   for (int k = 0; k < kBasis; ++k) {
@@ -349,6 +359,34 @@ __device__ void small_solve_warp(int n, const double *G, const double *v, double
     }
   }
   if (lane < n) c[lane] = ((on >> lane) & 1u) ? ci : 0.0;
+}
+
+__device__ void small_solve_warp(int n, const double *G, const double *v, double *c, double *sD) {
+  double L[kBasis], rd;
+  unsigned on;
+  small_factor_warp(n, G, sD, L, rd, on);
+  small_subst_warp(n, L, rd, on, v, c);
+}
+
+// The mixed-precision CG's warm-start factor of each member's Gram system,
+// formed on the auxiliary stream after a solve for the next solve of that
+// basis (which then only substitutes: the same arithmetic as the whole warp
+// solve, off its critical path).  Warp m: member m.
+__global__ void __launch_bounds__(32 * kChunk) k_gram_factor(CGBasis B, int nm) {
+  __shared__ double sD[kChunk][kBasis];
+  const int m = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (m >= nm) return;
+  const int n = B.ring[2 * m];
+  double L[kBasis], rd;
+  unsigned on;
+  small_factor_warp(n, B.gram + (size_t)m * kBasis * kBasis, sD[m], L, rd, on);
+  GramLDL &f = B.ldl[m];
+  if (lane < kBasis) {
+#pragma unroll
+    for (int j = 0; j < kBasis; ++j) f.L[lane * kBasis + j] = L[j];
+    f.rd[lane] = rd;
+  }
+  if (lane == 0) { f.on = on; f.n = n; }
 }
 
 __global__ void __launch_bounds__(kCGThreads, 4) k_cg3(CGArgs a, int nnz_cap, CGBasis B) {
@@ -1164,9 +1202,20 @@ __global__ void __launch_bounds__(kCGThreads, 1) k_cgm_mp(CGArgs a, int nnz_cap,
   }
   if (tid < MB) s_tol[tid] = fmax(a.rtol * sqrt(sbdot[P * tid + kBasis]), a.atol);
   {
-    const int m = tid >> 5;
-    if (m < nm && s_cnt[m] > 0)   // warp m: member m's coefficients
-      small_solve_warp(s_cnt[m], B.gram + m * kBasis * kBasis, sbdot + P * m, scoef + m * kBasis, smem + m * kBasis);
+    const int m = tid >> 5, lane = tid & 31;
+    if (m < nm && s_cnt[m] > 0) {   // warp m: member m's coefficients
+      const GramLDL *f = B.ldl ? B.ldl + m : nullptr;
+      if (f && __ldcg(&f->n) == s_cnt[m]) {   // factored after this basis's last solve: substitute only
+        double L[kBasis];
+        const double rd = lane < kBasis ? __ldcg(f->rd + lane) : 0.0;
+#pragma unroll
+        for (int j = 0; j < kBasis; ++j) L[j] = lane < kBasis ? __ldcg(f->L + lane * kBasis + j) : 0.0;
+        small_subst_warp(s_cnt[m], L, rd, __ldcg(&f->on), sbdot + P * m, scoef + m * kBasis);
+      } else {
+        small_solve_warp(s_cnt[m], B.gram + m * kBasis * kBasis, sbdot + P * m, scoef + m * kBasis,
+                         smem + m * kBasis);
+      }
+    }
   }
   __syncthreads();
   if (active) {
@@ -2498,19 +2547,28 @@ int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm,
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
   int cap = W.cg_nnz_cap;
   CGBasis basis;
+  int ev_slot;   // the basis slot's event
   if (h->nrep > 1) {
     const size_t slot = (size_t)mode * h->nrep + c0;   // first member of this chunk
     basis.b = W.ens_basis_b.p + slot * kBasis * M.N;
     basis.x = W.ens_basis_x.p + slot * kBasis * M.N;
     basis.gram = W.ens_basis_gram.p + slot * kBasis * kBasis;
     basis.ring = W.ens_basis_ring.p + 2 * slot;
+    basis.ldl = W.ens_basis_ldl.p ? W.ens_basis_ldl.p + slot : nullptr;
+    ev_slot = kCGSlots + (int)slot;
   } else {   // one simulation: the single-solve bases of slot bslot (default `mode`)
     const int sl = bslot >= 0 ? bslot : mode;
     basis.b = W.basis_b.p + (size_t)sl * kBasis * M.N;
     basis.x = W.basis_x.p + (size_t)sl * kBasis * M.N;
     basis.gram = W.basis_gram.p + sl * kBasis * kBasis;
     basis.ring = W.basis_ring.p + 2 * sl;
+    basis.ldl = W.basis_ldl.p ? W.basis_ldl.p + sl : nullptr;
+    ev_slot = sl;
   }
+  const bool mp_f = (mp_sel >= 0 ? mp_sel == 1 : h->opt.cg_precision == 1) && W.aux && basis.ldl &&
+                    ev_slot < (int)W.ev_ldl.size();
+  if (!mp_f) basis.ldl = nullptr;   // the kernel factors in place
+  if (mp_f) cudaStreamWaitEvent(h->stream, W.ev_ldl[ev_slot], 0);   // this basis's factor is formed
   void *args[] = {&a, &cap, &nm, &basis};
   const bool mp = mp_sel >= 0 ? mp_sel == 1 : h->opt.cg_precision == 1;
   const void *fn;
@@ -2524,6 +2582,17 @@ int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm,
   if (e != cudaSuccess) {
     h->last_error = std::string("ensemble CG launch failed: ") + cudaGetErrorString(e);
     return 100;
+  }
+  if (mp_f) {   // the next solve's warm-start factor, off the main stream
+    cudaEventRecord(W.ev_cg, h->stream);
+    cudaStreamWaitEvent(W.aux, W.ev_cg, 0);
+    k_gram_factor<<<1, 32 * kChunk, 0, W.aux>>>(basis, nm);
+    ++h->launches;
+    cudaEventRecord(W.ev_ldl[ev_slot], W.aux);
+    if (cudaGetLastError() != cudaSuccess) {
+      h->last_error = "mixed-precision CG: the warm-start factor could not be launched";
+      return 100;
+    }
   }
   return 0;
 }
@@ -2688,11 +2757,23 @@ int init_workspace(nmg_handle *h, std::string &err) {
   NMG_CUDA_TRY(W.basis_b.alloc(kCGSlots * (size_t)kBasis * N), "alloc CG basis");
   NMG_CUDA_TRY(W.basis_x.alloc(kCGSlots * (size_t)kBasis * N), "alloc CG basis");
   NMG_CUDA_TRY(W.basis_gram.alloc(kCGSlots * kBasis * kBasis), "alloc");
+  if (h->mixed_cg() && h->opt.do_demag) {   // the mixed-precision CG's warm-start factors
+    NMG_CUDA_TRY(W.basis_ldl.alloc(kCGSlots), "alloc");
+    NMG_CUDA_TRY(cudaMemset(W.basis_ldl.p, 0, sizeof(GramLDL) * kCGSlots), "memset");
+    NMG_CUDA_TRY(cudaStreamCreateWithFlags(&W.aux, cudaStreamNonBlocking), "auxiliary stream");
+    NMG_CUDA_TRY(cudaEventCreateWithFlags(&W.ev_cg, cudaEventDisableTiming), "event");
+    W.ev_ldl.assign(kCGSlots + 2 * (size_t)B, nullptr);
+    for (cudaEvent_t &ev : W.ev_ldl) NMG_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+  }
   NMG_CUDA_TRY(W.basis_ring.alloc(2 * kCGSlots), "alloc");
   if (B > 1) {
     NMG_CUDA_TRY(W.ens_basis_b.alloc(2 * (size_t)B * kBasis * N), "alloc ensemble CG basis");
     NMG_CUDA_TRY(W.ens_basis_x.alloc(2 * (size_t)B * kBasis * N), "alloc ensemble CG basis");
     NMG_CUDA_TRY(W.ens_basis_gram.alloc(2 * (size_t)B * kBasis * kBasis), "alloc");
+    if (h->mixed_cg() && h->opt.do_demag) {
+      NMG_CUDA_TRY(W.ens_basis_ldl.alloc(2 * (size_t)B), "alloc");
+      NMG_CUDA_TRY(cudaMemset(W.ens_basis_ldl.p, 0, sizeof(GramLDL) * 2 * B), "memset");
+    }
     NMG_CUDA_TRY(W.ens_basis_ring.alloc(4 * (size_t)B), "alloc");
     cudaMemsetAsync(W.ens_basis_ring.p, 0, sizeof(int) * 4 * B, h->stream);
   }
@@ -3038,6 +3119,7 @@ void swap_jac_buffers(Workspace &W, JacDemag &J) {
   W.rho.swap(J.rho); W.phi1.swap(J.phi1); W.phi2.swap(J.phi2); W.phi.swap(J.phi); W.rhs2.swap(J.rhs2);
   W.b1.swap(J.b1); W.b2.swap(J.b2);
   W.basis_b.swap(J.basis_b); W.basis_x.swap(J.basis_x); W.basis_gram.swap(J.basis_gram);
+  W.basis_ldl.swap(J.basis_ldl); W.ens_basis_ldl.swap(J.ens_basis_ldl);
   W.basis_ring.swap(J.basis_ring);
   W.ens_basis_b.swap(J.ens_basis_b); W.ens_basis_x.swap(J.ens_basis_x); W.ens_basis_gram.swap(J.ens_basis_gram);
   W.ens_basis_ring.swap(J.ens_basis_ring);
@@ -3056,6 +3138,10 @@ int jac_alloc(nmg_handle *P, JacDemag &J) {
   for (auto &e : d) {
     if (e.first->alloc(e.second) != cudaSuccess) return 100;
     if (e.second) cudaMemsetAsync(e.first->p, 0, sizeof(double) * e.second, P->stream);
+  }
+  for (auto e : {std::make_pair(&J.basis_ldl, W.basis_ldl.n), std::make_pair(&J.ens_basis_ldl, W.ens_basis_ldl.n)}) {
+    if (e.first->alloc(e.second) != cudaSuccess) return 100;
+    if (e.second) cudaMemsetAsync(e.first->p, 0, sizeof(GramLDL) * e.second, P->stream);
   }
   std::pair<DevBuf<int> *, size_t> k[] = {
       {&J.basis_ring, W.basis_ring.n}, {&J.ens_basis_ring, W.ens_basis_ring.n}, {&J.iters, W.iters.n}};
