@@ -192,3 +192,41 @@ def test_simulation_save_mesh_by_extension(tmp_path):
     a, b = mesh.load(str(tmp_path / "m.nmesh.h5")), mesh.load(str(tmp_path / "m.nmesh"))
     assert np.array_equal(a.simplices, b.simplices) and np.allclose(a.points, b.points)
     assert os.path.getsize(str(tmp_path / "m.nmesh.h5")) > 96
+
+
+def test_reader_two_level_chunk_btree(tmp_path):
+    """A chunked dataset whose chunk index has an internal node over two
+    leaves (the form larger PyTables arrays take): every chunk is found."""
+    arr = np.arange(40, dtype="<i4").reshape(10, 4)
+    w = h5.Writer()
+    w.create_dataset("/d", arr, chunks=(3, 4))   # 4 chunks in one leaf; the leaf is split below
+    path = str(tmp_path / "c.h5")
+    w.save(path)
+    raw = bytearray(open(path, "rb").read())
+    f = h5.File(bytes(raw))
+    b = f.b
+    p, _ = f["d"]._msg(0x08)
+    leaf = b.addr(p + 3)
+    ksize = 8 + 8 * 3
+    keys = [(raw[leaf + 24 + k * (ksize + 8): leaf + 24 + k * (ksize + 8) + ksize],
+             raw[leaf + 24 + k * (ksize + 8) + ksize: leaf + 24 + (k + 1) * (ksize + 8)]) for k in range(4)]
+    last = raw[leaf + 24 + 4 * (ksize + 8): leaf + 24 + 4 * (ksize + 8) + ksize]
+
+    def node(level, entries, final):
+        t = b"TREE" + bytes([1, level]) + struct.pack("<H", len(entries)) + struct.pack("<QQ", h5.UNDEF, h5.UNDEF)
+        for key, child in entries:
+            t += bytes(key) + bytes(child)
+        return t + bytes(final)
+
+    def put(blob):
+        while len(raw) % 8:
+            raw.append(0)
+        at = len(raw)
+        raw.extend(blob)
+        return at
+
+    l0 = put(node(0, keys[:2], keys[2][0]))
+    l1 = put(node(0, keys[2:], last))
+    root = put(node(1, [(keys[0][0], struct.pack("<Q", l0)), (keys[2][0], struct.pack("<Q", l1))], last))
+    raw[p + 3:p + 11] = struct.pack("<Q", root)
+    assert np.array_equal(h5.File(bytes(raw))["d"].read(), arr)
