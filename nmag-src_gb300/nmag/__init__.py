@@ -17,7 +17,10 @@ from .simulation import Simulation, every, at, never
 from .sets import float_set, vector_set
 from .vectools import normalised_vector, vector3_dot, vector3_cross
 from ._lib import NmagGpuError
+from .h5data import (get_subfield_from_h5file, get_subfield_positions_from_h5file,
+                     get_subfield_sites_from_h5file)
 
 __all__ = ["SI", "simulation_units", "MagMaterial", "PredefinedAnisotropy", "uniaxial_anisotropy", "cubic_anisotropy",
            "Simulation", "every", "at", "never", "mesh",
-           "float_set", "vector_set", "normalised_vector", "vector3_dot", "vector3_cross", "NmagGpuError"]
+           "float_set", "vector_set", "normalised_vector", "vector3_dot", "vector3_cross", "NmagGpuError",
+           "get_subfield_from_h5file", "get_subfield_positions_from_h5file", "get_subfield_sites_from_h5file"]

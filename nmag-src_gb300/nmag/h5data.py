@@ -128,3 +128,53 @@ def read(path):
             if field == "m" and "clock" in node.attrs:
                 clock = str(node.attrs["clock"])
     return {"mesh": msh, "metadata": meta, "dofsites": dofsites, "tables": tables, "clock": clock}
+
+
+def _locate(d, subfieldname, id=None, row=None):
+    """The field of a subfield (from the metadata) and the table row: the
+    row with that id, else row `row` (0 by default; nfem/hdf5_v01.py:1625-1679)."""
+    field = None
+    for fieldname, dofname, _, _ in d["metadata"]:
+        if dofname == subfieldname:
+            field = fieldname
+            break
+    if field is None or field not in d["tables"]:
+        raise KeyError("no subfield '%s' saved in this file" % subfieldname)
+    tab = d["tables"][field]
+    if id is not None:
+        hits = np.nonzero(tab["id"] == id)[0]
+        if not len(hits):
+            raise KeyError("no row with id %d for field '%s'" % (id, field))
+        row = int(hits[0])
+    elif row is None:
+        row = 0
+    return field, tab[row]
+
+
+def get_subfield_from_h5file(filename, subfieldname, id=None, row=None, unit=None):
+    """main.py:2915-2956: a subfield's values (SI) at its sites from a saved
+    data file, the row with the given id or the row-th row (0 by default)."""
+    if unit:
+        raise NotImplementedError("This feature is not implemented yet (unit=*).")
+    d = read(filename)
+    _, r = _locate(d, subfieldname, id, row)
+    return np.array(r[subfieldname], dtype=np.float64)
+
+
+def get_subfield_sites_from_h5file(filename, subfieldname):
+    """main.py:2987-3015: the sites of a subfield as saved (one mesh node each)."""
+    d = read(filename)
+    if subfieldname not in d["dofsites"]:
+        raise KeyError("no subfield '%s' saved in this file" % subfieldname)
+    return d["dofsites"][subfieldname].reshape(-1, 1)
+
+
+def get_subfield_positions_from_h5file(filename, subfieldname):
+    """main.py:2958-2985: the positions (m) of a subfield's sites, from the
+    file's mesh and its length scale."""
+    f = h5.File(filename)
+    scale = float(np.asarray(f["/mesh/scale/sifactor"].read()).reshape(-1)[0]) \
+        if "scale" in f["mesh"] and "sifactor" in f["/mesh/scale"] else 1.0
+    d = read(filename)
+    sites = get_subfield_sites_from_h5file(filename, subfieldname).reshape(-1)
+    return np.asarray(d["mesh"].points)[sites] * scale

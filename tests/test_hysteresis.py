@@ -249,6 +249,17 @@ def test_save_fields_and_restart_name(tmp_path, monkeypatch):
     with pytest.raises(KeyError):
         sim.save_data(fields=["B_field"])
     assert sim.get_restart_file_name() == "hyst_restart.h5"
+    # the module-level read-out of saved fields (main.py:2915-3015)
+    fn = str(tmp_path / "hyst_dat.h5")
+    assert np.allclose(nmag.get_subfield_from_h5file(fn, "m_Py", row=1), sim.get_subfield("m_Py"), atol=1e-7)
+    assert np.allclose(nmag.get_subfield_from_h5file(fn, "H_demag"), 0.1e6)
+    id1 = int(t["m"]["id"][1])
+    assert np.allclose(nmag.get_subfield_from_h5file(fn, "m_Py", id=id1),
+                       nmag.get_subfield_from_h5file(fn, "m_Py", row=1))
+    assert np.array_equal(nmag.get_subfield_sites_from_h5file(fn, "m_Py"), np.arange(4).reshape(-1, 1))
+    assert np.allclose(nmag.get_subfield_positions_from_h5file(fn, "m_Py"), sim.mesh.points * 1e-9)
+    with pytest.raises(KeyError):
+        nmag.get_subfield_from_h5file(fn, "B_Py")
 
 
 def test_restart_file_round_trip(tmp_path, monkeypatch):
