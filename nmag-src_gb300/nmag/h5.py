@@ -34,6 +34,7 @@ Writing::
 """
 from __future__ import annotations
 
+import os
 import struct
 import zlib
 
@@ -476,11 +477,7 @@ class File(Group):
         else:
             with open(path_or_bytes, "rb") as fh:
                 data = fh.read()
-        start = None
-        for off in [0] + [512 << k for k in range(20)]:
-            if off + 8 <= len(data) and data[off:off + 8] == SIGNATURE:
-                start = off
-                break
+        start = _superblock_offset(data)
         if start is None:
             raise HDF5Error("not an HDF5 file")
         ver = data[start + 8]
@@ -510,13 +507,34 @@ class File(Group):
         return Dataset(self, addr, name)
 
 
+def _superblock_offset(data):
+    """Where the superblock starts: byte 0, or after a user block of 512,
+    1024, 2048, ... bytes (files whose first bytes belong to another
+    application, e.g. MATLAB's 512-byte header)."""
+    for off in [0] + [512 << k for k in range(20)]:
+        if off + 8 > len(data):
+            break
+        if data[off:off + 8] == SIGNATURE:
+            return off
+    return None
+
+
 def is_hdf5(path):
     try:
         with open(path, "rb") as fh:
             head = fh.read(8)
+            if head == SIGNATURE:
+                return True
+            size = os.fstat(fh.fileno()).st_size
+            for off in [512 << k for k in range(20)]:
+                if off + 8 > size:
+                    break
+                fh.seek(off)
+                if fh.read(8) == SIGNATURE:
+                    return True
     except IOError:
         return False
-    return head == SIGNATURE
+    return False
 
 
 # ---------------------------------------------------------------- writing --

@@ -1,7 +1,9 @@
 """The HDF5 reader and writer (nmag/h5.py) and the nmesh HDF5 mesh files.
 
-No HDF5 library is installed, and the reference tree holds no HDF5 file,
-so these tests check the module against itself: files written by the
+No HDF5 library is installed, and the reference tree holds no HDF5 file.
+The one file on the machine that the HDF5 library wrote (a MATLAB 7.3 file
+in scipy's test data) pins the reader's core structures; otherwise these
+tests check the module against itself: files written by the
 writer (every layout, filter, datatype and group size it produces) read
 back exactly, hand-assembled structures the writer does not produce (a
 version 2 object header with compact links, version 1/2 layout and
@@ -230,3 +232,35 @@ def test_reader_two_level_chunk_btree(tmp_path):
     root = put(node(1, [(keys[0][0], struct.pack("<Q", l0)), (keys[2][0], struct.pack("<Q", l1))], last))
     raw[p + 3:p + 11] = struct.pack("<Q", root)
     assert np.array_equal(h5.File(bytes(raw))["d"].read(), arr)
+
+
+def _scipy_matlab_data():
+    scipy_io = pytest.importorskip("scipy.io")
+    d = os.path.join(os.path.dirname(scipy_io.matlab.__file__), "tests", "data")
+    h5_file = os.path.join(d, "testhdf5_7.4_GLNX86.mat")
+    v5_file = os.path.join(d, "testdouble_7.1_GLNX86.mat")
+    if not (os.path.exists(h5_file) and os.path.exists(v5_file)):
+        pytest.skip("scipy's MATLAB test files are not installed")
+    return scipy_io, h5_file, v5_file
+
+
+def test_reader_on_a_file_the_hdf5_library_wrote():
+    """A file written by the HDF5 library itself (MATLAB 7.3 format through
+    libhdf5, shipped as test data with scipy): a 512-byte user block, then a
+    version 0 superblock with base address 512, the root group as a symbol
+    table, a contiguous float64 dataset and a string attribute -- the
+    structures of the HDF5 1.6/1.8 output PyTables writes.  The values equal
+    those scipy reads from the same variable saved in MATLAB's own format."""
+    scipy_io, h5_file, v5_file = _scipy_matlab_data()
+    assert h5.is_hdf5(h5_file)
+    f = h5.File(h5_file)
+    assert f.keys() == ["testdouble"]
+    d = f["testdouble"]
+    assert d.shape == (9, 1) and d.dtype == np.dtype("<f8")
+    assert str(d.attrs["MATLAB_class"]) == "double"
+    ref = scipy_io.loadmat(v5_file)["testdouble"]   # MATLAB's 1 x 9, stored column-major
+    got = d.read()
+    assert np.array_equal(got.T, ref)
+    assert np.array_equal(got.ravel(), np.arange(9) * np.pi / 4)
+    # absolute addresses in that file are relative to the superblock
+    assert f.b.base == 512
