@@ -1318,7 +1318,8 @@ int ts_advance(nmg_handle *h, double tout, int exact_tstop, int64_t max_steps, d
     st->npe = I.npe; st->nps = I.nps; st->njv = I.njv; st->nje = I.nsetups;
     st->hcur = I.h; st->tcur = I.tn; st->qcur = I.q;
     int it[2] = {0, 0};
-    cudaMemcpy(it, h->ws.iters.p, sizeof(it), cudaMemcpyDeviceToHost);
+    cudaMemcpyAsync(it, h->ws.iters.p, sizeof(it), cudaMemcpyDeviceToHost, h->stream);
+    cudaStreamSynchronize(h->stream);
     st->last_cg_iters_nbc = it[0]; st->last_cg_iters_dbc = it[1];
   }
   return rc;

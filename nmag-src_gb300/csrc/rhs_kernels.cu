@@ -2483,6 +2483,15 @@ int build_cg_ordering(nmg_handle *h, std::string &err) {
   return 0;
 }
 
+// Orders h->stream after the last warm-start factor formed for basis slot
+// ev_slot on the auxiliary stream: that kernel reads the basis (its ring,
+// Gram matrix) which the next solve or reset of the slot overwrites.
+void wait_basis_factor(nmg_handle *h, int ev_slot) {
+  const Workspace &W = h->ws;
+  if (W.aux && ev_slot >= 0 && ev_slot < (int)W.ev_ldl.size())
+    cudaStreamWaitEvent(h->stream, W.ev_ldl[ev_slot], 0);
+}
+
 int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, double atol, int maxits) {
   Mesh &M = h->mesh;
   Workspace &W = h->ws;
@@ -2499,6 +2508,7 @@ int run_cg(nmg_handle *h, int mode, const double *b, double *x, double rtol, dou
   a.nc = W.nc; a.ainv = W.ainv; a.rc = W.rc;
   // fresh barrier words per solve: epochs restart at 1 inside the kernel
   cudaMemsetAsync(W.bar.p, 0, sizeof(unsigned) * (W.cg_blocks + 1), h->stream);
+  wait_basis_factor(h, mode);
   NMG_PROF_BEGIN(h, 1 + (mode & 1));
   cudaError_t e;
   {
@@ -2568,7 +2578,7 @@ int run_cgm(nmg_handle *h, int mode, int c0, const double *b, double *x, int nm,
   const bool mp_f = (mp_sel >= 0 ? mp_sel == 1 : h->opt.cg_precision == 1) && W.aux && basis.ldl &&
                     ev_slot < (int)W.ev_ldl.size();
   if (!mp_f) basis.ldl = nullptr;   // the kernel factors in place
-  if (mp_f) cudaStreamWaitEvent(h->stream, W.ev_ldl[ev_slot], 0);   // this basis's factor is formed
+  wait_basis_factor(h, ev_slot);   // this basis's last factor is formed
   void *args[] = {&a, &cap, &nm, &basis};
   const bool mp = mp_sel >= 0 ? mp_sel == 1 : h->opt.cg_precision == 1;
   const void *fn;
@@ -2606,6 +2616,7 @@ int cg_solve(nmg_handle *h, int slot, const double *b, double *x, double rtol, d
 }
 
 void cg_reset_basis(nmg_handle *h, int slot) {
+  wait_basis_factor(h, slot);
   cudaMemsetAsync(h->ws.basis_ring.p + 2 * slot, 0, sizeof(int) * 2, h->stream);
 }
 
