@@ -55,7 +55,10 @@ typedef struct nmg_options {
                                                per term, FP32 sums over 2048 terms
                                                added in FP64 (~2^-24); an ensemble's
                                                members form one product              */
-  int cg_precision;                      /* 0: FP64 CG; reserved                       */
+  int cg_precision;                      /* 0: FP64 CG; 1: FP32 inner CG (two-level for
+                                            the Neumann system, warm-started from the
+                                            last solves) with FP64 residual refinement
+                                            to the same tolerance                     */
   int cg_no_coarse;                      /* 1: Jacobi only (no two-level Neumann CG)   */
   int n_members;                         /* ensemble size B (0 or 1: one simulation)   */
   double bem_anchor_tol;                 /* bem_precision 2 only; > 0: anchored product
