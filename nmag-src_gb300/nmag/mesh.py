@@ -8,7 +8,8 @@ cell (x-fastest) and, within a cell, by the axis permutation of the monotone
 path from the cell's (0,0,0) corner to its (1,1,1) corner, in lexicographic
 order.  (The reference's own structured mesher, utils/cubicmesh/cubicmesh.c
 :60-81,283-345, uses a mirrored split; the configurations here name the Kuhn
-split.)
+split.  ``cubicmesh`` restates that mesher: the same nodes, simplices and
+regions as its files.)
 
 ``load_ascii``/``save_ascii`` read and write the "# PYFEM mesh file version
 1.0" text format (writer: utils/cubicmesh/cubicmesh.c:348-385; reader:
@@ -122,6 +123,103 @@ def cube_mesh(edge_cells=10, h=3.0):
 def film_mesh():
     """The 500 x 125 x 3 nm film: 200 x 50 x 2 cells of 2.5 x 2.5 x 1.5 nm."""
     return box_mesh(200, 50, 2, 2.5, 2.5, 1.5)
+
+
+# One cell of the reference's structured mesher split into six tetrahedra,
+# each vertex given as its corner offset (x, y, z) in {0, 1}.  Along an axis
+# on which the cell's index is odd the offsets are mirrored (1 - c), so that
+# neighbouring cells split their shared face along the same diagonal and the
+# mesh is conforming.  Split, vertex order and mirroring are the reference's
+# (utils/cubicmesh/cubicmesh.c:60-81 for the split, :315-345 for the
+# mirroring), so the simplices come out identical to its files.
+_CUBICMESH_CELL = np.array([
+    [(1, 0, 1), (0, 1, 0), (1, 0, 0), (1, 1, 1)],
+    [(1, 0, 1), (0, 1, 0), (0, 1, 1), (0, 0, 0)],
+    [(1, 0, 1), (0, 1, 0), (1, 1, 1), (0, 1, 1)],
+    [(0, 1, 1), (1, 0, 1), (0, 0, 0), (0, 0, 1)],
+    [(1, 0, 1), (0, 1, 0), (0, 0, 0), (1, 0, 0)],
+    [(1, 0, 0), (0, 1, 0), (1, 1, 0), (1, 1, 1)],
+], dtype=np.int64)
+
+
+def _cubicmesh_filter(spec):
+    """(axis, thresholds) of the mesher's region filter: "x:1.5,3.0" (axis
+    x, y, z or its number, then ascending coordinates; cubicmesh.c:167-203)."""
+    if isinstance(spec, str):
+        head, _, rest = spec.partition(":")
+        axis = {"x": 0, "y": 1, "z": 2}.get(head.strip())
+        if axis is None:
+            try:
+                axis = int(head)
+            except ValueError:
+                raise ValueError("region filter '%s': give the axis as x, y, z or 0-2, then ':'" % spec)
+        thresholds = [float(v) for v in rest.split(",") if v.strip()] if rest else []
+    else:
+        axis, thresholds = int(spec[0]), [float(v) for v in spec[1]]
+    if axis not in (0, 1, 2):
+        raise ValueError("region filter: axis %r is not one of 0, 1, 2" % (axis,))
+    if any(b < a for a, b in zip(thresholds, thresholds[1:])):
+        raise ValueError("region filter: the coordinates must be ordered from smaller to greater")
+    return axis, thresholds
+
+
+def _cubicmesh_regions(points, simplices, region_filter):
+    """Region of each simplex under the mesher's filter (cubicmesh.c:205-246):
+    a vertex beyond the k-th threshold (of k = 0, 1, ... ascending, the
+    largest tested first) lies in region k + 2, below all of them in region
+    1, and within 1e-10 of a threshold in none; a simplex takes the region of
+    its last vertex that has one (-1 when none has)."""
+    if region_filter is None:
+        return np.ones(len(simplices), dtype=np.int32)
+    axis, thr = _cubicmesh_filter(region_filter)
+    x = points[:, axis]
+    vreg = np.ones(len(points), dtype=np.int64)
+    decided = np.zeros(len(points), dtype=bool)
+    for k in range(len(thr) - 1, -1, -1):
+        d = thr[k] - x
+        on = ~decided & (np.abs(d) <= 1e-10)
+        vreg[on] = -1
+        decided |= on
+        beyond = ~decided & (d < 0.0)
+        vreg[beyond] = k + 2
+        decided |= beyond
+    reg = np.full(len(simplices), -1, dtype=np.int64)
+    for c in range(simplices.shape[1]):
+        r = vreg[simplices[:, c]]
+        reg = np.where(r >= 0, r, reg)
+    return reg.astype(np.int32)
+
+
+def cubicmesh(sizes, divisions, region_filter=None):
+    """The mesh the reference's structured mesher writes for
+    ``cubicmesh out.nmesh,lx:nx,ly:ny,lz:nz [filter]`` (utils/cubicmesh/
+    cubicmesh.c:266-345): (nx+1)(ny+1)(nz+1) nodes at (i lx/nx, j ly/ny,
+    k lz/nz), numbered with k fastest, then j, then i; six tetrahedra per cell
+    (``_CUBICMESH_CELL``), cells in the same order.  Regions are 1, or set by
+    ``region_filter`` ("x:1.5,3.0" or (axis, [coordinates]), see
+    ``_cubicmesh_regions``).  Coordinates are kept at full precision; the
+    mesher's text file rounds them to six decimals."""
+    sizes = [float(v) for v in sizes]
+    nn = [int(v) for v in divisions]
+    if len(sizes) != 3 or len(nn) != 3:
+        raise ValueError("cubicmesh: three sizes and three divisions")
+    if min(nn) < 1:
+        raise ValueError("cubicmesh: the number of cells along each side must be positive")
+    if min(sizes) <= 0.0:
+        raise ValueError("cubicmesh: the sides must have positive lengths")
+    dd = [sizes[a] / nn[a] for a in range(3)]
+    ipos = np.stack(np.meshgrid(np.arange(nn[0] + 1), np.arange(nn[1] + 1), np.arange(nn[2] + 1),
+                                indexing="ij"), axis=-1).reshape(-1, 3)
+    points = np.empty(ipos.shape, dtype=np.float64)
+    for a in range(3):
+        points[:, a] = ipos[:, a].astype(np.float64) * dd[a]
+    cells = np.stack(np.meshgrid(np.arange(nn[0]), np.arange(nn[1]), np.arange(nn[2]), indexing="ij"),
+                     axis=-1).reshape(-1, 3)
+    odd = (cells % 2 == 1)[:, None, None, :]
+    corner = np.where(odd, 1 - _CUBICMESH_CELL[None], _CUBICMESH_CELL[None]) + cells[:, None, None, :]
+    node = (corner[..., 0] * (nn[1] + 1) + corner[..., 1]) * (nn[2] + 1) + corner[..., 2]
+    simplices = node.reshape(-1, 4).astype(np.int32)
+    return Mesh(points, simplices, _cubicmesh_regions(points, simplices, region_filter))
 
 
 def save_ascii(mesh, filename):

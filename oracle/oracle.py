@@ -8,7 +8,9 @@ The oracle restates nsim's LLG right-hand side and CVODE-style integrator on
 the CPU (see nmag_oracle.h for the reference citations).  Its BEM fill is
 pinned to the reference's own code: the reference's plain-C Lindholm stub
 (src/bem3d_stubs.c), compiled unmodified against a minimal caml shim into
-_ref/ (ref_bem), fills the same matrix bit for bit.  The rest of the path has
+_ref/ (ref_bem), fills the same matrix bit for bit; the reference's
+structured mesher (utils/cubicmesh/cubicmesh.c) is built there too
+(ref_cubicmesh) and its files pin the nmesh text reader.  The rest of the path has
 no compilable reference (OCaml, PETSc, SUNDIALS are absent), so known-answer
 tests pin the restatement there.
 """
@@ -98,6 +100,31 @@ def build_ref():
     if os.path.exists(os.path.join(REF_SRC, "bem3d_stubs.c")):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", "REF_SRC=" + REF_SRC])
     return os.path.exists(REF_LIB)
+
+
+REF_UTILS = os.environ.get("NMAG_REFERENCE_UTILS", os.path.join(os.path.dirname(REF_SRC), "utils"))
+REF_CUBICMESH = os.path.join(HERE, "_ref", "cubicmesh")
+
+
+def build_ref_cubicmesh():
+    """Compile the reference's structured mesher (REF_UTILS/cubicmesh/
+    cubicmesh.c, unmodified) into _ref/ when the reference tree is present;
+    return whether the program exists afterwards."""
+    if os.path.exists(os.path.join(REF_UTILS, "cubicmesh", "cubicmesh.c")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref-cubicmesh", "REF_SRC=" + REF_SRC,
+                               "REF_UTILS=" + REF_UTILS])
+    return os.path.exists(REF_CUBICMESH)
+
+
+def ref_cubicmesh(path, sizes, divisions, region_filter=None):
+    """Run the reference's mesher: ``cubicmesh path,lx:nx,ly:ny,lz:nz
+    [filter]`` writes an nmesh text file to path (cubicmesh.c:402-441)."""
+    if not os.path.exists(REF_CUBICMESH):
+        raise RuntimeError("reference mesher not built (oracle/_ref)")
+    spec = ",".join([path] + ["%r:%d" % (float(a), int(n)) for a, n in zip(sizes, divisions)])
+    cmd = [REF_CUBICMESH, spec] + ([region_filter] if region_filter else [])
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+    return path
 
 
 def ref_lib():
