@@ -13,13 +13,15 @@ regions as its files.)
 
 ``load_ascii``/``save_ascii`` read and write the "# PYFEM mesh file version
 1.0" text format (writer: utils/cubicmesh/cubicmesh.c:348-385; reader:
-interface/nmeshlib/lib1.py:805-863): points, then "region v0 v1 v2 v3" per
-simplex, then surfaces and periodic blocks, which are skipped.
+src/mesh.ml:6619-6760 behind interface/nmeshlib/lib1.py:838-863): points,
+then "region v0 v1 v2 v3" per simplex, then surfaces, which are skipped, and
+periodic point groups, which are refused.
 """
 from __future__ import annotations
 
 import itertools
 import os
+import re
 
 import numpy as np
 
@@ -249,19 +251,83 @@ def magnetic_part(mesh):
     return Mesh(mesh.points[used], renum[simp].astype(np.int32), mesh.regions[keep]), used
 
 
+_NMESH_TAG = re.compile(r"# PYFEM mesh file version ([0-9]+)\.([0-9]+)")
+_NMESH_SUMMARY = re.compile(r"# dim[ \t]*=[ \t]*([0-9]+)[ \t]*nodes[ \t]*=[ \t]*([0-9]+)[ \t]*"
+                            r"simplices[ \t]*=[ \t]*([0-9]+)[ \t]*surfaces[ \t]*=[ \t]*([0-9]+)[ \t]*"
+                            r"periodic[ \t]*=[ \t]*([0-9]+)")
+
+
 def load_ascii(filename):
-    """Read an nmesh ASCII file (points, region+simplices; surfaces ignored)."""
+    """Read an nmesh text file as the reference's reader does (src/mesh.ml
+    :6619-6760, read_mesh): line 1 "# PYFEM mesh file version 1.x", line 2
+    the summary "# dim = 3 nodes = N simplices = S surfaces = F periodic =
+    P" whose counts place the sections (points from line 4, simplices
+    "region v0 v1 v2 v3" from line N + 5, then the surfaces, which are
+    skipped, and the periodic point groups).  Refused as the reference
+    refuses them, with the line number: another major version, a missing
+    summary, rows with the wrong number of entries, vertex indices out of
+    range or repeated in a simplex.  Periodic point groups (P > 0) are
+    refused too: the LLG path here has no periodic identification."""
     if not os.path.exists(filename):
         raise IOError("file '%s' does not exist" % filename)
     with open(filename) as f:
-        lines = [ln for ln in (l.strip() for l in f) if ln and not ln.startswith("#")]
-    it = iter(lines)
-    n = int(next(it).split()[0])
-    pts = np.array([[float(v) for v in next(it).split()[:3]] for _ in range(n)], dtype=np.float64)
-    t = int(next(it).split()[0])
-    rows = [next(it).split() for _ in range(t)]
-    regions = np.array([int(r[0]) for r in rows], dtype=np.int32)
-    simp = np.array([[int(v) for v in r[1:5]] for r in rows], dtype=np.int32)
+        lines = f.read().splitlines()
+    if len(lines) < 2:
+        raise IOError("%s: mesh information not specified" % filename)
+    tag = _NMESH_TAG.match(lines[0])
+    if tag is None:
+        raise IOError("%s: version of the file not given (expected '# PYFEM mesh file version 1.0')" % filename)
+    if tag.group(1) != "1":
+        raise IOError("%s: wrong version of the file (%s.%s)" % (filename, tag.group(1), tag.group(2)))
+    summary = _NMESH_SUMMARY.match(lines[1])
+    if summary is None:
+        raise IOError("%s: mesh summary not given (line 2)" % filename)
+    dim, n, t, nsurf, nper = (int(v) for v in summary.groups())
+    if dim != 3:
+        raise IOError("%s: a %d-dimensional mesh (the LLG path needs 3 dimensions)" % (filename, dim))
+
+    def fields(k, what):
+        if k >= len(lines):
+            raise IOError("%s - LINE %d: the file ends before the %s" % (filename, k + 1, what))
+        return lines[k].split()
+
+    def fail(k, msg):
+        raise IOError("%s - LINE %d: %s" % (filename, k + 1, msg))
+
+    pts = np.empty((n, 3), dtype=np.float64)
+    for i in range(n):
+        k = 3 + i
+        row = fields(k, "points")
+        if len(row) != dim:
+            fail(k, "Wrong number of point coordinates")
+        try:
+            pts[i] = [float(v) for v in row]
+        except ValueError:
+            fail(k, "Wrong point coordinates")
+    simp = np.empty((t, 4), dtype=np.int32)
+    regions = np.empty(t, dtype=np.int32)
+    for i in range(t):
+        k = 4 + n + i
+        row = fields(k, "simplices")
+        if len(row) != dim + 2:
+            fail(k, "Wrong number of simplex coordinates")
+        try:
+            idx = [int(v) for v in row[1:]]
+        except ValueError:
+            fail(k, "Wrong simplex indices")
+        bad = [j for j, v in enumerate(idx) if v >= n or v < 0]
+        if bad:
+            fail(k, "Index %d out of range" % (bad[0] + 1))
+        if len(set(idx)) != len(idx):
+            fail(k, "Duplicate index")
+        try:
+            regions[i] = int(row[0])
+        except ValueError:
+            fail(k, "Wrong number of simplex region")
+        simp[i] = idx
+    if nper > 0:
+        raise IOError("%s: %d periodic point groups: periodic meshes are not supported by this path"
+                      % (filename, nper))
     return Mesh(pts, simp, regions)
 
 
@@ -336,11 +402,18 @@ def save_hdf5(mesh, filename, sifactor=None, unit=None):
 
 
 def load(filename_or_mesh):
-    """A Mesh, or a file in nmesh ASCII or nmesh HDF5 (recognised by the
-    HDF5 signature, like nmeshlib/lib1.py:838-863)."""
+    """A Mesh, or a file in nmesh ASCII (first line "# PYFEM ...") or nmesh
+    HDF5 (the HDF5 signature); anything else is refused
+    (nmeshlib/lib1.py:656-678,838-863)."""
     if isinstance(filename_or_mesh, Mesh):
         return filename_or_mesh
     from . import h5
+    if not os.path.exists(filename_or_mesh):
+        raise IOError("file '%s' does not exist" % filename_or_mesh)
+    with open(filename_or_mesh, "rb") as f:
+        ascii_tag = f.read(7) == b"# PYFEM"
+    if ascii_tag:
+        return load_ascii(filename_or_mesh)
     if h5.is_hdf5(filename_or_mesh):
         return load_hdf5(filename_or_mesh)
-    return load_ascii(filename_or_mesh)
+    raise IOError("%s is unknown file format (not ascii, not hdf5)" % filename_or_mesh)
