@@ -13,10 +13,12 @@
  * fixed-leading-coefficient BDF in Nordsieck form, its local error test,
  * step/order selection and the modified Newton iteration.
  *
- * The preconditioner for P = I - gamma J is one block-Jacobi sweep (exact
- * inverse of each node's 3x3 block); the reference instead runs PETSc
- * GMRES + bjacobi/ILU to rtol 1e-2 (nsim.ml:2210-2262).  This only changes
- * the Krylov iteration count, not the converged Newton corrections.
+ * The preconditioner for P = I - gamma J is by default one block-Jacobi
+ * sweep (exact inverse of each node's 3x3 block), as on the device.  The
+ * reference's own form -- P assembled, PETSc GMRES + bjacobi/ILU(0) to
+ * pc_rtol (nsim.ml:2210-2262,2419-2483) -- is restated below as well
+ * (om_bdf_set_precond kind 1) so that the two can be compared: they change
+ * the Krylov iteration counts, not the converged Newton corrections.
  */
 #include "nmag_oracle.h"
 #include <math.h>
@@ -69,6 +71,7 @@ struct om_bdf {
   int jcur, setup_done;
   double hu; int qu;
   double tstop; int tstop_set;
+  struct om_ilu_pc *pc;         /* the reference's preconditioner (kind 1), or NULL */
 };
 
 static double wrms(int n, const double *x, const double *w) {
@@ -79,6 +82,239 @@ static double wrms(int n, const double *x, const double *w) {
 
 static void set_ewt(om_bdf *B, const double *y) {
   for (int i = 0; i < B->n; ++i) B->ewt[i] = 1.0 / (B->rtol * fabs(y[i]) + B->atol);
+}
+
+/* ---- the reference's preconditioner: P = I - gamma J assembled over the
+ * node graph's 3x3 blocks (the reference copies its Jacobian matrix into mx,
+ * scales by -gamma and adds the identity at every PC setup), solved by PETSc
+ * KSP GMRES with bjacobi/ILU (nsim.ml:2210-2262,2419-2483).  On one process
+ * bjacobi has one block, so the preconditioner is ILU(0) of the whole
+ * matrix in natural (DOF) order.  GMRES: restarted (PETSc's default restart
+ * 30), left preconditioned, zero initial guess, stopped when the estimate of
+ * the preconditioned residual norm is <= max(pc_rtol * its initial value,
+ * pc_atol) or after maxit iterations (the reference passes no dtol/maxit, so
+ * PETSc's 10000 applies).  Restated from PETSc's documented KSPGMRES/PCILU
+ * behaviour (PETSc 2.3.3 is not in the reference tree). ---- */
+typedef struct om_ilu_pc {
+  int n, nnz, restart, maxit;
+  int *rp, *ci, *diag, *iw;
+  double *a;               /* P, then its ILU(0) factors in place */
+  double *a0;              /* P as assembled (matrix products) */
+  double **V, *Hh, *cs, *sn, *g, *w, *res;
+  long long iters;         /* GMRES iterations over the run */
+} om_ilu_pc;
+
+static void ilu_pc_free(om_ilu_pc *P) {
+  if (!P) return;
+  free(P->rp); free(P->ci); free(P->diag); free(P->iw); free(P->a); free(P->a0);
+  if (P->V) for (int j = 0; j <= P->restart; ++j) free(P->V[j]);
+  free(P->V); free(P->Hh); free(P->cs); free(P->sn); free(P->g); free(P->w); free(P->res);
+  free(P);
+}
+
+/* Scalar CSR pattern of the 3x3-block matrix over the node graph (columns
+ * ascending because the node columns are). */
+static om_ilu_pc *ilu_pc_create(const om_mesh *M, int restart, int maxit) {
+  om_ilu_pc *P = calloc(1, sizeof(om_ilu_pc));
+  int N = M->n_nodes;
+  P->n = 3 * N; P->restart = restart < 1 ? 30 : restart; P->maxit = maxit < 1 ? 10000 : maxit;
+  P->nnz = 9 * M->nnz;
+  P->rp = malloc(sizeof(int) * (P->n + 1)); P->ci = malloc(sizeof(int) * P->nnz);
+  P->diag = malloc(sizeof(int) * P->n); P->iw = malloc(sizeof(int) * P->n);
+  P->a = malloc(sizeof(double) * P->nnz); P->a0 = malloc(sizeof(double) * P->nnz);
+  int pos = 0;
+  for (int i = 0; i < N; ++i)
+    for (int r = 0; r < 3; ++r) {
+      int row = 3 * i + r;
+      P->rp[row] = pos;
+      for (int k = M->row_ptr[i]; k < M->row_ptr[i + 1]; ++k)
+        for (int c = 0; c < 3; ++c) {
+          int col = 3 * M->col_idx[k] + c;
+          if (col == row) P->diag[row] = pos;
+          P->ci[pos++] = col;
+        }
+    }
+  P->rp[P->n] = pos;
+  for (int i = 0; i < P->n; ++i) P->iw[i] = -1;
+  P->V = calloc(P->restart + 1, sizeof(double *));
+  for (int j = 0; j <= P->restart; ++j) P->V[j] = calloc(P->n, sizeof(double));
+  P->Hh = calloc((size_t)(P->restart + 1) * P->restart, sizeof(double));
+  P->cs = calloc(P->restart, sizeof(double)); P->sn = calloc(P->restart, sizeof(double));
+  P->g = calloc(P->restart + 1, sizeof(double));
+  P->w = calloc(P->n, sizeof(double)); P->res = calloc(P->n, sizeof(double));
+  return P;
+}
+
+/* The linearised LLG right-hand side of one node (the approximate
+ * Jacobian's row block, om_jv): C1 (w x H + m x hv) + C2 (w x (m x H) +
+ * m x (w x H + m x hv)). */
+static void llg_lin(double C1, double C2, const double *m, const double *H, const double *w, const double *hv,
+                    double *out) {
+  double a[3] = {w[1] * H[2] - w[2] * H[1] + (m[1] * hv[2] - m[2] * hv[1]),
+                 w[2] * H[0] - w[0] * H[2] + (m[2] * hv[0] - m[0] * hv[2]),
+                 w[0] * H[1] - w[1] * H[0] + (m[0] * hv[1] - m[1] * hv[0])};
+  double mxH[3] = {m[1] * H[2] - m[2] * H[1], m[2] * H[0] - m[0] * H[2], m[0] * H[1] - m[1] * H[0]};
+  double wxH[3] = {w[1] * H[2] - w[2] * H[1], w[2] * H[0] - w[0] * H[2], w[0] * H[1] - w[1] * H[0]};
+  double mxhv[3] = {m[1] * hv[2] - m[2] * hv[1], m[2] * hv[0] - m[0] * hv[2], m[0] * hv[1] - m[1] * hv[0]};
+  double t1[3] = {w[1] * mxH[2] - w[2] * mxH[1], w[2] * mxH[0] - w[0] * mxH[2], w[0] * mxH[1] - w[1] * mxH[0]};
+  double u[3] = {wxH[0] + mxhv[0], wxH[1] + mxhv[1], wxH[2] + mxhv[2]};
+  double t2[3] = {m[1] * u[2] - m[2] * u[1], m[2] * u[0] - m[0] * u[2], m[0] * u[1] - m[1] * u[0]};
+  for (int d = 0; d < 3; ++d) out[d] = C1 * a[d] + C2 * (t1[d] + t2[d]);
+}
+
+/* P = I - gamma J(mJ, HJ) into a0 and a (blocks probed column by column
+ * through the node's linearisation: exact, since it is linear in w, hv). */
+static void ilu_pc_assemble(om_ilu_pc *P, const om_state *S, const double *mJ, const double *HJ, double gamma) {
+  const om_mesh *M = S->M;
+  const double c = S->mat.exch_coeff, C1 = S->mat.C1, C2 = S->mat.C2;
+  for (int i = 0; i < M->n_nodes; ++i) {
+    const double *m = mJ + 3 * (size_t)i, *H = HJ + 3 * (size_t)i;
+    const double pin = S->pin ? S->pin[i] : 1.0;
+    const int deg = M->row_ptr[i + 1] - M->row_ptr[i];
+    for (int q = 0; q < deg; ++q) {
+      const int k = M->row_ptr[i] + q, j = M->col_idx[k];
+      const double kap = -c * M->K[k] / M->vol[i];
+      for (int cc = 0; cc < 3; ++cc) {
+        double w[3] = {0, 0, 0}, hv[3] = {0, 0, 0}, col[3];
+        hv[cc] = kap;
+        if (j == i) w[cc] = 1.0;
+        llg_lin(C1, C2, m, H, w, hv, col);
+        for (int r = 0; r < 3; ++r) {
+          const int at = P->rp[3 * i + r] + 3 * q + cc;
+          P->a0[at] = (j == i && r == cc ? 1.0 : 0.0) - gamma * (pin * col[r]);
+        }
+      }
+    }
+  }
+  memcpy(P->a, P->a0, sizeof(double) * P->nnz);
+}
+
+/* ILU(0) in place (row-wise IKJ form); 0, or -1 on a zero pivot. */
+static int ilu_pc_factor(om_ilu_pc *P) {
+  int *iw = P->iw;
+  double *a = P->a;
+  for (int i = 0; i < P->n; ++i) {
+    for (int p = P->rp[i]; p < P->rp[i + 1]; ++p) iw[P->ci[p]] = p;
+    for (int p = P->rp[i]; p < P->rp[i + 1] && P->ci[p] < i; ++p) {
+      const int k = P->ci[p];
+      const double piv = a[P->diag[k]];
+      if (piv == 0.0) return -1;
+      const double lik = a[p] / piv;
+      a[p] = lik;
+      for (int q = P->diag[k] + 1; q < P->rp[k + 1]; ++q) {
+        const int at = iw[P->ci[q]];
+        if (at >= 0) a[at] -= lik * a[q];
+      }
+    }
+    for (int p = P->rp[i]; p < P->rp[i + 1]; ++p) iw[P->ci[p]] = -1;
+    if (a[P->diag[i]] == 0.0) return -1;
+  }
+  return 0;
+}
+
+/* z = (LU)^{-1} r (unit lower L, upper U with the diagonal). */
+static void ilu_pc_subst(const om_ilu_pc *P, const double *r, double *z) {
+  for (int i = 0; i < P->n; ++i) {
+    double s = r[i];
+    for (int p = P->rp[i]; p < P->diag[i]; ++p) s -= P->a[p] * z[P->ci[p]];
+    z[i] = s;
+  }
+  for (int i = P->n - 1; i >= 0; --i) {
+    double s = z[i];
+    for (int p = P->diag[i] + 1; p < P->rp[i + 1]; ++p) s -= P->a[p] * z[P->ci[p]];
+    z[i] = s / P->a[P->diag[i]];
+  }
+}
+
+static void ilu_pc_matvec(const om_ilu_pc *P, const double *v, double *out) {
+  for (int i = 0; i < P->n; ++i) {
+    double s = 0.0;
+    for (int p = P->rp[i]; p < P->rp[i + 1]; ++p) s += P->a0[p] * v[P->ci[p]];
+    out[i] = s;
+  }
+}
+
+/* GMRES(restart) on P z = r, left-preconditioned by the ILU(0) factors. */
+static void ilu_pc_solve(om_ilu_pc *P, const double *r, double *z, double rtol, double atol) {
+  const int n = P->n, mr = P->restart;
+  double **V = P->V, *g = P->g, *w = P->w;
+#define HH(i, j) P->Hh[(size_t)(i) * mr + (j)]
+  memset(z, 0, sizeof(double) * n);
+  double tol = -1.0;
+  int it = 0;
+  for (;;) {
+    /* preconditioned residual of the current iterate */
+    if (it == 0) memcpy(P->res, r, sizeof(double) * n);
+    else {
+      ilu_pc_matvec(P, z, w);
+      for (int i = 0; i < n; ++i) P->res[i] = r[i] - w[i];
+    }
+    ilu_pc_subst(P, P->res, V[0]);
+    double beta = 0.0;
+    for (int i = 0; i < n; ++i) beta += V[0][i] * V[0][i];
+    beta = sqrt(beta);
+    if (tol < 0.0) tol = fmax(rtol * beta, atol);
+    if (beta <= tol || beta == 0.0 || it >= P->maxit) break;
+    for (int i = 0; i < n; ++i) V[0][i] /= beta;
+    memset(g, 0, sizeof(double) * (mr + 1));
+    g[0] = beta;
+    int kdim = 0;
+    double resid = beta;
+    for (int j = 0; j < mr && it < P->maxit; ++j) {
+      ilu_pc_matvec(P, V[j], P->res);
+      ilu_pc_subst(P, P->res, w);
+      ++it;
+      for (int k = 0; k <= j; ++k) {   /* modified Gram-Schmidt */
+        double h = 0.0;
+        for (int i = 0; i < n; ++i) h += V[k][i] * w[i];
+        HH(k, j) = h;
+        for (int i = 0; i < n; ++i) w[i] -= h * V[k][i];
+      }
+      double hn = 0.0;
+      for (int i = 0; i < n; ++i) hn += w[i] * w[i];
+      hn = sqrt(hn);
+      HH(j + 1, j) = hn;
+      for (int k = 0; k < j; ++k) {
+        const double t1 = HH(k, j), t2 = HH(k + 1, j);
+        HH(k, j) = P->cs[k] * t1 + P->sn[k] * t2;
+        HH(k + 1, j) = -P->sn[k] * t1 + P->cs[k] * t2;
+      }
+      const double aa = HH(j, j), bb = HH(j + 1, j), den = hypot(aa, bb);
+      P->cs[j] = den == 0.0 ? 1.0 : aa / den;
+      P->sn[j] = den == 0.0 ? 0.0 : bb / den;
+      HH(j, j) = den; HH(j + 1, j) = 0.0;
+      g[j + 1] = -P->sn[j] * g[j];
+      g[j] = P->cs[j] * g[j];
+      resid = fabs(g[j + 1]);
+      kdim = j + 1;
+      if (resid <= tol || hn == 0.0) break;
+      for (int i = 0; i < n; ++i) V[j + 1][i] = w[i] / hn;
+    }
+    for (int k = kdim - 1; k >= 0; --k) {   /* y = H^{-1} g, then z += V y */
+      double s = g[k];
+      for (int jj = k + 1; jj < kdim; ++jj) s -= HH(k, jj) * g[jj];
+      g[k] = s / HH(k, k);
+    }
+    for (int k = 0; k < kdim; ++k) for (int i = 0; i < n; ++i) z[i] += g[k] * V[k][i];
+    if (resid <= tol || it >= P->maxit) break;
+  }
+  P->iters += it;
+#undef HH
+}
+
+void om_bdf_set_precond(om_bdf *B, int kind, int restart, int maxit) {
+  ilu_pc_free(B->pc);
+  B->pc = kind == 1 ? ilu_pc_create(B->S->M, restart, maxit) : NULL;
+}
+
+long long om_bdf_pc_iterations(const om_bdf *B) { return B->pc ? B->pc->iters : 0; }
+
+void om_pc_matrix_apply(const om_state *S, const double *mJ, const double *HJ, double gamma, const double *v,
+                        double *out) {
+  om_ilu_pc *P = ilu_pc_create(S->M, 1, 1);
+  ilu_pc_assemble(P, S, mJ, HJ, gamma);
+  ilu_pc_matvec(P, v, out);
+  ilu_pc_free(P);
 }
 
 om_bdf *om_bdf_create(om_state *S, int qmax, int maxl, double rtol, double atol, double pc_rtol, double pc_atol) {
@@ -108,6 +344,7 @@ void om_bdf_free(om_bdf *B) {
   free(B->ewt); free(B->acor); free(B->y); free(B->tempv); free(B->ftemp); free(B->mJ); free(B->HJ);
   for (int j = 0; j <= B->maxl; ++j) free(B->V[j]);
   free(B->V); free(B->Hm); free(B->givens); free(B->yg); free(B->work); free(B->xsol);
+  ilu_pc_free(B->pc);
   free(B);
 }
 
@@ -200,6 +437,11 @@ static void block_of_J(const om_bdf *B, int i, double Jb[3][3]) {
 }
 
 static void psolve(om_bdf *B, const double *r, double *z) {
+  if (B->pc) {   /* the reference's form: GMRES + ILU(0) on the assembled P */
+    ilu_pc_solve(B->pc, r, z, B->pc_rtol, B->pc_atol);
+    B->nps++;
+    return;
+  }
   int N = B->S->M->n_nodes;
   double g = B->gammap; /* P = I - gamma J was built at the last setup */
   for (int i = 0; i < N; ++i) {
@@ -224,12 +466,19 @@ static void psolve(om_bdf *B, const double *r, double *z) {
  * as the Jacobian point (nsim.ml:2315-2398 re-Jacobi); returns jcur. */
 static int psetup(om_bdf *B, int jok, const double *ypred) {
   B->npe++;
-  if (jok) return 0;
-  /* f(ypred) was evaluated just before by the Newton driver, so S->h_total is
-     the field at ypred (the reference re-runs the RHS, nsim.ml:2338-2348). */
-  memcpy(B->mJ, ypred, sizeof(double) * B->n);
-  memcpy(B->HJ, B->S->h_total, sizeof(double) * B->n);
-  return 1;
+  int jcur = 0;
+  if (!jok) {
+    /* f(ypred) was evaluated just before by the Newton driver, so S->h_total
+       is the field at ypred (the reference re-runs the RHS, nsim.ml:2338-2348). */
+    memcpy(B->mJ, ypred, sizeof(double) * B->n);
+    memcpy(B->HJ, B->S->h_total, sizeof(double) * B->n);
+    jcur = 1;
+  }
+  if (B->pc) {   /* the reference rebuilds I - gamma J at every setup (nsim.ml:2440-2452) */
+    ilu_pc_assemble(B->pc, B->S, B->mJ, B->HJ, B->gamma);
+    if (ilu_pc_factor(B->pc)) return -1;
+  }
+  return jcur;
 }
 
 /* SPGMR with left preconditioning, scaling by ewt, modified Gram-Schmidt,

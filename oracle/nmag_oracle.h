@@ -152,6 +152,15 @@ int om_bdf_init(om_bdf *B, double t0, const double *m0);
 int om_bdf_advance(om_bdf *B, double tout, int exact_tstop, long long max_steps, double *t_reached,
                    double *m_out);
 void om_bdf_stats(const om_bdf *B, om_ts_stats *st);
+/* Preconditioner of the Newton systems: kind 0 (default) one exact 3x3
+ * block-Jacobi sweep; kind 1 the reference's (nsim.ml:2210-2262,2419-2483):
+ * P = I - gamma J assembled, GMRES(restart) with ILU(0), to pc_rtol/pc_atol
+ * or maxit iterations (restart, maxit < 1: PETSc's 30, 10000). */
+void om_bdf_set_precond(om_bdf *B, int kind, int restart, int maxit);
+long long om_bdf_pc_iterations(const om_bdf *B);
+/* Test hook: out = (I - gamma J(mJ, HJ)) v from the assembled matrix. */
+void om_pc_matrix_apply(const om_state *S, const double *mJ, const double *HJ, double gamma, const double *v,
+                        double *out);
 
 /* Fixed-step RK4 (differentiation form forward). */
 int om_rk4(om_state *S, double *m, double dt, int nsteps);

@@ -187,6 +187,10 @@ def lib():
         L.om_bdf_init.argtypes = [C.c_void_p, C.c_double, _f64p]
         L.om_bdf_advance.argtypes = [C.c_void_p, C.c_double, C.c_int, C.c_longlong, C.POINTER(C.c_double), _f64p]
         L.om_bdf_stats.argtypes = [C.c_void_p, C.POINTER(OmStats)]
+        L.om_bdf_set_precond.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.om_bdf_pc_iterations.argtypes = [C.c_void_p]
+        L.om_bdf_pc_iterations.restype = C.c_longlong
+        L.om_pc_matrix_apply.argtypes = [C.POINTER(OmState), _f64p, _f64p, C.c_double, _f64p, _f64p]
         L.om_rk4.argtypes = [C.POINTER(OmState), _f64p, C.c_double, C.c_int]
         L.om_triangle_space_angle.argtypes = [_f64p, _f64p, _f64p, _f64p]
         L.om_triangle_space_angle.restype = C.c_double
@@ -358,11 +362,25 @@ class OracleSim(object):
                     np.ascontiguousarray(v, dtype=np.float64).reshape(-1), out)
         return out
 
-    def ts_init(self, m0, t0=0.0, rtol=1e-6, atol=1e-6, max_order=2, krylov_max=300, pc_rtol=1e-2, pc_atol=1e-7):
+    def pc_matrix_apply(self, mJ, HJ, gamma, v):
+        """(I - gamma J(mJ, HJ)) v from the matrix the reference's
+        preconditioner assembles."""
+        out = np.zeros(3 * self.N)
+        lib().om_pc_matrix_apply(C.byref(self._s), np.ascontiguousarray(mJ, dtype=np.float64).reshape(-1),
+                                 np.ascontiguousarray(HJ, dtype=np.float64).reshape(-1), float(gamma),
+                                 np.ascontiguousarray(v, dtype=np.float64).reshape(-1), out)
+        return out
+
+    def ts_init(self, m0, t0=0.0, rtol=1e-6, atol=1e-6, max_order=2, krylov_max=300, pc_rtol=1e-2, pc_atol=1e-7,
+                precond="block", pc_restart=30, pc_maxit=10000):
+        """precond: "block" (one exact 3x3 block-Jacobi sweep, as on the
+        device) or "reference" (P = I - gamma J assembled, GMRES(pc_restart)
+        with ILU(0) to pc_rtol / pc_atol, nsim.ml:2210-2262,2419-2483)."""
         L = lib()
         if self._bdf:
             L.om_bdf_free(self._bdf)
         self._bdf = L.om_bdf_create(C.byref(self._s), max_order, krylov_max, rtol, atol, pc_rtol, pc_atol)
+        L.om_bdf_set_precond(self._bdf, {"block": 0, "reference": 1}[precond], pc_restart, pc_maxit)
         st = L.om_bdf_init(self._bdf, t0, np.ascontiguousarray(m0, dtype=np.float64).reshape(-1))
         if st:
             raise RuntimeError("oracle ts init failed: %d" % st)
@@ -378,7 +396,9 @@ class OracleSim(object):
     def ts_stats(self):
         s = OmStats()
         lib().om_bdf_stats(self._bdf, C.byref(s))
-        return {n: getattr(s, n) for n, _ in OmStats._fields_}
+        out = {n: getattr(s, n) for n, _ in OmStats._fields_}
+        out["pc_iterations"] = lib().om_bdf_pc_iterations(self._bdf)
+        return out
 
     def rk4(self, m, dt, nsteps):
         m = np.ascontiguousarray(m, dtype=np.float64).reshape(-1).copy()
