@@ -518,7 +518,12 @@ class Simulation(object):
 
     def is_converged(self):
         """convergence.py:54-100 / main.py:2737-2760: max dm/dt below
-        stopping_dm_dt twice in a row; sets clock.convergence."""
+        stopping_dm_dt twice in a row; sets clock.convergence.  The count of
+        checks below the threshold restarts at convergence and at a check
+        above it, not at a new stage, and a check with no max dm/dt yet
+        (None, after a new stage) leaves it unchanged.  (The reference's
+        tolerance-factor suggestions only act with adjust_tolerances=True, a
+        debugging path that waits for console input; they are not made.)"""
         self.clock.convergence = False
         if self.max_dm_dt is None:
             return False
@@ -624,8 +629,7 @@ class Simulation(object):
                     self.set_H_ext(H[0], H[1])
                 else:
                     self.set_H_ext(H)
-            self._countdown = self._countdown_initial
-            self.reinitialise(initial_time=0)
+            self.reinitialise(initial_time=0)   # the convergence countdown carries over, as in the reference
             for _, when, key in actions:
                 next_save[key] = _next_time(when, self.clock.view(), tols)
             while True:
