@@ -87,7 +87,7 @@ def vector_set(norm_list, direction, units=None, normalize=True):
     times units (sets.py:117-158)."""
     scale = _scaled(units)
     d = [float(x) for x in direction]
-    if normalize:
-        n = sum(x * x for x in d) ** 0.5
-        d = [x / n for x in d]
+    if normalize:   # times the reciprocal of the norm, as sets.py:139-141 scales
+        inv = 1.0 / sum(x * x for x in d) ** 0.5
+        d = [inv * x for x in d]
     return [[scale(norm * x) for x in d] for norm in float_set(norm_list)]
