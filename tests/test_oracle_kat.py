@@ -131,6 +131,26 @@ def test_exchange_of_uniform_state_is_zero(ocube):
     assert np.abs(s.field("H_exch")).max() < 1e-12
 
 
+def test_exchange_of_quadratic_state_is_the_laplacian():
+    """H_exch = exch_coeff * Laplacian(m) (the operator ($negJ$) <d/dxj H_exch||d/dxj m>
+    with negJ = -su_exch_prefactor, nmag_lam.py:256,445): on the
+    Kuhn-split box the P1 stiffness matrix is the 7-point stencil and the
+    box volumes the cell volume, so at interior nodes the discrete Laplacian
+    of a quadratic is exact -- on unequal spacings too."""
+    from nmag import mesh
+    msh = mesh.box_mesh(6, 5, 4, 2.0, 2.5, 1.5)
+    om = oracle.OracleMesh(msh.points, msh.simplices, fill_bem=False)
+    c = coeffs_of(permalloy())
+    s = oracle.OracleSim(om, c, do_demag=False)
+    p = msh.points
+    m = np.stack([p[:, 0] ** 2, p[:, 1] ** 2 + 0.5 * p[:, 2], p[:, 0] * p[:, 1] - p[:, 2] ** 2], axis=1)
+    s.rhs(m)
+    H = s.field("H_exch")
+    inner = np.all((p > p.min(0) + 1e-9) & (p < p.max(0) - 1e-9), axis=1)
+    assert inner.sum() == 5 * 4 * 3
+    assert np.abs(H[inner] / c["exch_coeff"] - np.array([2.0, 2.0, -2.0])).max() < 1e-12
+
+
 def test_cube_demag_factor_is_one_third(ocube):
     s = oracle.OracleSim(ocube, coeffs_of(permalloy()), nbc=(1e-10, 1e-50, 5000), dbc=(1e-10, 1e-50, 5000))
     m = np.tile([1.0, 0.0, 0.0], (ocube.n_nodes, 1))
