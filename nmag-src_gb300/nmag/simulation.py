@@ -1109,14 +1109,24 @@ class Simulation(object):
         _h5data.write(fn, self.mesh, meta, sites, tables, sim_units=repr(simulation_units),
                       clock=repr(dict(self.clock)))
 
-    def load_m_from_h5file(self, filename):
-        """main.py:1876-1902: set m from the first row of /data/fields/m of
-        an nmag data or restart file, subfield by subfield, placed by the
-        file's sites (the mesh must be the one the file was written with)."""
+    def load_m_from_h5file(self, filename, id=None, row=None, unit=None):
+        """main.py:1876-1902: set m from a row of /data/fields/m of an nmag
+        data or restart file -- the row with the given id, else row ``row``
+        (the first by default; hdf5_v01.py:1625-1679) -- subfield by
+        subfield, placed by the file's sites (the mesh must be the one the
+        file was written with)."""
+        if unit:
+            raise NotImplementedError("This feature is not implemented yet (unit=*).")
         d = _h5data.read(filename)
         if "m" not in d["tables"]:
             raise IOError("File '%s' holds no field m" % filename)
-        row = d["tables"]["m"][0]
+        tab = d["tables"]["m"]
+        if id is not None:
+            hits = np.nonzero(tab["id"] == id)[0]
+            if not len(hits):
+                raise KeyError("no row with id %d for field 'm' in '%s'" % (id, filename))
+            row = int(hits[0])
+        row = tab[0 if row is None else row]
         m = np.array(self._m, copy=True)
         # a file of the whole mesh (vacuum included, as the reference writes
         # it) numbers the nodes of the mesh as loaded, not of its magnetic part
@@ -1131,15 +1141,18 @@ class Simulation(object):
             if file_nodes is None or len(file_nodes) != len(nodes):
                 raise ValueError("load_m_from_h5file: the sites of '%s' differ from this simulation's" % sub)
             pos = {int(n): k for k, n in enumerate(nodes)}
+            if any(int(n) not in pos for n in file_nodes):
+                raise ValueError("load_m_from_h5file: the sites of '%s' differ from this simulation's" % sub)
             idx = np.array([pos[int(n)] for n in file_nodes])
             target = self._sites_of(self._material_of(sub, "m"))[idx] if self.layer is not None else idx
             m[..., target, :] = vals
         self.set_m(m)
 
-    def load_restart_file(self, filename=None):
-        """main.py:2859-2883: m and the clock of a restart file; a stage
-        saved at convergence continues with the next stage."""
-        fn = filename or self.get_restart_file_name()
+    def load_restart_file(self, file_name=None, filename=None):
+        """main.py:2859-2883: m and the clock of a restart file (file_name,
+        the reference's argument; filename is accepted too); a stage saved
+        at convergence continues with the next stage."""
+        fn = file_name or filename or self.get_restart_file_name()
         self.load_m_from_h5file(fn)
         clock = _h5data.read(fn)["clock"]
         if clock:

@@ -280,6 +280,33 @@ def test_restart_file_round_trip(tmp_path, monkeypatch):
     sim.set_m([0.0, 0.0, 1.0])
     sim.load_m_from_h5file(str(tmp_path / "hyst_restart.h5"))
     assert np.allclose(sim.get_subfield("m"), m0, atol=1e-7)
+    sim.set_m([0.0, 0.0, 1.0])
+    sim.load_restart_file(file_name=str(tmp_path / "hyst_restart.h5"))   # the reference's argument name
+    assert np.allclose(sim.get_subfield("m"), m0, atol=1e-7)
+
+
+def test_load_m_from_h5file_selects_a_row(tmp_path, monkeypatch):
+    """load_m_from_h5file(filename, id=..., row=...): the row with that id,
+    else the row-th row, else the first (hdf5_v01.py:1625-1679)."""
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    states = [np.tile(v, (4, 1)) for v in ([1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0])]
+    for m in states:
+        sim.set_m(m)
+        sim.save_data(fields=["m"])
+    fn = str(tmp_path / "hyst_dat.h5")
+    ids = list(nmag.h5data.read(fn)["tables"]["m"]["id"])
+    assert len(ids) == 3
+    for k, m in enumerate(states):
+        sim.set_m([0.6, 0.8, 0.0])
+        sim.load_m_from_h5file(fn, row=k)
+        assert np.allclose(sim.get_subfield("m"), m, atol=1e-7)
+        sim.set_m([0.6, 0.8, 0.0])
+        sim.load_m_from_h5file(fn, id=int(ids[k]))
+        assert np.allclose(sim.get_subfield("m"), m, atol=1e-7)
+    sim.load_m_from_h5file(fn)
+    assert np.allclose(sim.get_subfield("m"), states[0], atol=1e-7)
+    with pytest.raises(KeyError):
+        sim.load_m_from_h5file(fn, id=12345)
 
 
 def test_current_density_needs_a_polarisation(tmp_path, monkeypatch):
