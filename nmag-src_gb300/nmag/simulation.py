@@ -468,12 +468,19 @@ class Simulation(object):
         if exact_tstop is not None:
             self._default_exact_tstop = bool(exact_tstop)
 
-    def reinitialise(self, initial_time=None):
-        """main.py:2707: (re)create the integrator at the current state."""
+    def reinitialise(self, rel_tolerance=None, abs_tolerance=None, initial_time=None):
+        """main.py:2707-2731: (re)create the integrator at the current state,
+        from initial_time (SI, or simulation units) when given, with new
+        relative / absolute tolerances when given."""
+        if rel_tolerance is not None:
+            self.ts_rel_tol = float(rel_tolerance)
+        if abs_tolerance is not None:
+            self.ts_abs_tol = float(abs_tolerance)
         if initial_time is not None:
-            self.clock.stage_time_su = 0.0
+            t0 = (simulation_units.of(initial_time, compatible_with=SI("s")) if isinstance(initial_time, SI)
+                  else float(initial_time))
+            self.clock.stage_time_su = t0
             self.clock.stage_step = 0
-            t0 = 0.0
         else:
             t0 = self.clock.stage_time_su
         self.engine.ts_init(t0, self.ts_rel_tol, self.ts_abs_tol, self.max_order, self.krylov_max)
@@ -818,10 +825,21 @@ class Simulation(object):
         names = list(timers) or sorted(self._timers)
         return [(k, None, self._timers.get(k, 0.0)) for k in names]
 
-    def save_mesh(self, filename):
+    def region_volume(self, material_name):
+        """main.py:2105-2107: retired in the reference, which points to
+        material_volume."""
+        raise NotImplementedError("Use material_volume instead")
+
+    def save_fields(self, filename=None, fieldnames="all"):
+        """main.py:2637-2639: retired in the reference in favour of
+        save_data(fields=...)."""
+        raise RuntimeError("Use save_data(fields=fields) to save fields")
+
+    def save_mesh(self, filename, scontext=None):
         """main.py:1228-1232 / nmeshlib/lib1.py:498-515: the magnetic mesh in
         simulation units of length (as the reference's mesh object stores it),
-        as nmesh HDF5 when the name ends in .h5, else as nmesh ASCII."""
+        as nmesh HDF5 when the name ends in .h5, else as nmesh ASCII.
+        (scontext, the reference's MPI context, has no use on one GPU.)"""
         if os.path.splitext(filename)[1].lower() == ".h5":
             _mesh.save_hdf5(self.mesh, filename)
         else:
@@ -839,10 +857,11 @@ class Simulation(object):
         self.clock.zero_stage_time_su = self.clock.time_su
         self._ts_ready = False
 
-    def get_subfield_average_siv(self, field, subfield=None):
+    def get_subfield_average_siv(self, field_name, subfield_name=None):
         """main.py:2234-2290: volume average of a field in SI numbers (a
-        list for vectors); ``subfield`` names the material of per-material
-        fields ('m', 'Py' -> m_Py).  Member 0 of an ensemble."""
+        list for vectors); ``subfield_name`` names the material of
+        per-material fields ('m', 'Py' -> m_Py).  Member 0 of an ensemble."""
+        field, subfield = field_name, subfield_name
         if self.layer is not None:   # several materials: averages over one material's sites
             names = [mt.name for mt in self.materials]
             name, base = subfield, field
@@ -880,10 +899,10 @@ class Simulation(object):
             return list((vals * V[:, None]).sum(0) / V.sum())
         return float((vals * V).sum() / V.sum())
 
-    def get_subfield_average(self, field, subfield=None):
-        """main.py:2292-2312: as get_subfield_average_siv, as SI objects."""
-        v = self.get_subfield_average_siv(field, subfield)
-        u = self._unit_of(field)
+    def get_subfield_average(self, field_name, subfield_name=None):
+        """main.py:2290-2312: as get_subfield_average_siv, as SI objects."""
+        v = self.get_subfield_average_siv(field_name, subfield_name)
+        u = self._unit_of(field_name)
         return [x * u for x in v] if isinstance(v, list) else v * u
 
     def get_member_average_m(self, member):

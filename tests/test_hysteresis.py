@@ -344,3 +344,23 @@ def test_load_m_from_a_whole_mesh_file(tmp_path, monkeypatch):
     got = sim.get_subfield("m_Py")
     for k, n in enumerate(sim.node_map):
         assert np.allclose(got[k], want[int(n)], atol=1e-7)
+
+
+def test_reinitialise_tolerances_and_retired_methods(tmp_path, monkeypatch):
+    """reinitialise(rel_tolerance, abs_tolerance, initial_time) as
+    main.py:2707-2731; region_volume and save_fields refuse as the
+    reference's retired methods do (main.py:2105-2107,2637-2639)."""
+    sim, eng = make_sim(tmp_path, monkeypatch)
+    seen = []
+    eng.ts_init = lambda t0, rtol, atol, q, k: seen.append((t0, rtol, atol))
+    sim.reinitialise(rel_tolerance=1e-8, abs_tolerance=1e-7, initial_time=0)
+    assert seen[-1] == (0.0, 1e-8, 1e-7)
+    sim.reinitialise()
+    assert seen[-1][1:] == (1e-8, 1e-7)
+    sim.reinitialise(initial_time=SI(2e-12, "s"))
+    assert abs(seen[-1][0] - 2.0) < 1e-12 and abs(sim.clock.stage_time_su - 2.0) < 1e-12
+    with pytest.raises(NotImplementedError):
+        sim.region_volume("Py")
+    with pytest.raises(RuntimeError):
+        sim.save_fields()
+    assert sim.get_subfield_average_siv(field_name="m") == sim.get_subfield_average_siv("m")
