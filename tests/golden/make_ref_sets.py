@@ -71,7 +71,7 @@ def main():
                     vs.append({"spec": s, "direction": direction, "normalize": normalize, "units": units,
                                "out": [hexl(row) for row in v]})
     with open(os.path.join(HERE, "ref_sets.json"), "w") as f:
-        json.dump({"float_set": fl, "vector_set": vs}, f)
+        json.dump({"float_set": fl, "vector_set": vs}, f, separators=(",", ":"))
     print("wrote", len(fl), "float_set and", len(vs), "vector_set cases")
 
 
