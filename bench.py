@@ -115,6 +115,20 @@ def h_ext_su():
     return np.array([v * 1e-3 / MU0 for v in H_EXT_MT]) / 1e6
 
 
+def ksp_tolerances(args):
+    """The Poisson solves' tolerances: the reference's defaults (rtol 1e-5,
+    main.py ksp_tolerances) unless --poisson-rtol is given."""
+    if args.poisson_rtol is None:
+        return None
+    return {"NBC.rtol": args.poisson_rtol, "DBC.rtol": args.poisson_rtol}
+
+
+def oracle_tolerances(args):
+    """The same for the CPU legs (the oracle's (rtol, atol, maxits))."""
+    tol = 1e-5 if args.poisson_rtol is None else args.poisson_rtol
+    return (tol, 1e-50, 10000), (tol, 1e-50, 10000)
+
+
 def peaks_tensor():
     """Dense bf16 tensor peak (TFLOP/s): the measured burst figure, else the fallback."""
     try:
@@ -216,11 +230,13 @@ def cpu_reference_run(args, msh, base, seed, steps, warmup, max_wall=25.0, sampl
     om = oracle.OracleMesh(msh.points, msh.simplices, nthreads=0)
     m = initial_m(msh.n_nodes, base, seed)
     if args.relax_ps > 0:
-        r = oracle.OracleSim(om, material(1.0).coefficients("nmag"))
+        nbc, dbc = oracle_tolerances(args)
+        r = oracle.OracleSim(om, material(1.0).coefficients("nmag"), nbc=nbc, dbc=dbc)
         r.ts_init(m, rtol=1e-6, atol=1e-6)
         _, m = r.ts_advance(args.relax_ps)
         del r
-    s = oracle.OracleSim(om, material(0.02).coefficients("nmag"))
+    nbc, dbc = oracle_tolerances(args)
+    s = oracle.OracleSim(om, material(0.02).coefficients("nmag"), nbc=nbc, dbc=dbc)
     s.set_h_ext(h_ext_su())
     s.ts_init(m, rtol=1e-6, atol=1e-6)
     setup = time.perf_counter() - t0
@@ -291,6 +307,7 @@ def config_dict(args, msh):
             "jv": args.jv, "cg_coarse": not args.cg_no_coarse,
             "bem_anchor": args.anchor if args.form == "fp32x2" else 0.0,
             "rtol": 1e-6, "atol": 1e-6, "max_order": 2, "krylov_max": 300,
+            "poisson_rtol": 1e-5 if args.poisson_rtol is None else args.poisson_rtol,
             "l2": "BEM matrix (nb^2 x %d B) larger than L2; no explicit flush" % {"fp64": 8, "fp32": 4,
                                                                                   "fp32x2": 6, "bf16x3": 6}[args.form]}
 
@@ -311,7 +328,8 @@ def relax_states(args, form, cg, B, msh, base, seed, anchor):
     import nmag
     from nmag import SI, every
     sim = nmag.Simulation("relax", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor,
-                          anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps)
+                          anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps,
+                          ksp_tolerances=ksp_tolerances(args))
     sim.load_mesh(msh, [("film", material(1.0))], unit_length=SI(1e-9, "m"))
     if B > 1:   # member b starts from the workload's initial state with seed + b
         sim.set_m(np.stack([initial_m(msh.n_nodes, base, seed + b) for b in range(B)]))
@@ -350,7 +368,8 @@ def measure(args, form, cg, B, msh, start, world, local, sample_clocks=True, anc
     sim = nmag.Simulation("bench", bem_precision=form, cg_precision=cg, n_members=B, bem_anchor=anchor,
                           anchor_product=args.anchor_product, cg_local_sweeps=args.cg_sweeps,
                           jacobian=jacobian, jacobian_demag_rtol=args.jac_rtol,
-                          jv_precision=jv if jv is not None else args.jv, cg_coarse=not args.cg_no_coarse)
+                          jv_precision=jv if jv is not None else args.jv, cg_coarse=not args.cg_no_coarse,
+                          ksp_tolerances=ksp_tolerances(args))
     sim.load_mesh(msh, [("film", material(0.02))], unit_length=SI(1e-9, "m"))
     eng = sim.engine
     sim.set_H_ext(h_ext_su() * 1e6, SI(1.0, "A/m"))
@@ -1134,6 +1153,9 @@ def main():
     ap.add_argument("--rhs", type=int, default=128, help="--report bem: right-hand sides per product")
     ap.add_argument("--cg-no-coarse", action="store_true",
                     help="Neumann CG with Jacobi alone (no aggregation coarse level)")
+    ap.add_argument("--poisson-rtol", type=float, default=None,
+                    help="relative tolerance of the Neumann and Dirichlet solves in every leg (default: the "
+                         "reference's 1e-5)")
     ap.add_argument("--jv", default="fp32", choices=["fp64", "fp32"],
                     help="arithmetic of the BDF's Jacobian-vector products and block preconditioner "
                          "(the chosen form; the plain FP64 comparison always uses fp64)")
